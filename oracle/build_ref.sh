@@ -1,0 +1,23 @@
+#!/bin/sh
+# Builds oracle/_ref/ref_pipeline: the reference's own hot-path sources,
+# compiled unmodified from the reference checkout, linked with the project's
+# shims (oracle/ref_shims/) and CPU solver (oracle/solver.c).
+# Test infrastructure only; output stays in oracle/_ref/ (git-ignored).
+# usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+set -e
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+[ -f "$REF/src/fdtd.hpp" ] || { echo "reference sources not found under $REF" >&2; exit 1; }
+mkdir -p "$OUT"
+CXXFLAGS="-std=c++17 -O2 -ffp-contract=off -w -I$HERE/ref_shims -I$REF/src -I$HERE"
+gcc -std=c11 -O2 -ffp-contract=off -c "$HERE/solver.c" -I"$HERE" -o "$OUT/solver.o" &
+g++ $CXXFLAGS -c "$REF/src/mesh.cpp" -o "$OUT/mesh.o" &
+g++ $CXXFLAGS -c "$REF/src/generateStiff.cpp" -o "$OUT/generateStiff.o" &
+g++ $CXXFLAGS -c "$REF/src/matrixCon.cpp" -o "$OUT/matrixCon.o" &
+g++ $CXXFLAGS -c "$HERE/ref_shims/mkl_sparse_shim.cpp" -o "$OUT/mkl_sparse_shim.o" &
+g++ $CXXFLAGS -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness.o" &
+wait
+g++ -o "$OUT/ref_pipeline" "$OUT/ref_harness.o" "$OUT/mesh.o" "$OUT/generateStiff.o" "$OUT/matrixCon.o" \
+    "$OUT/mkl_sparse_shim.o" "$OUT/solver.o" -lm
+echo "built $OUT/ref_pipeline"

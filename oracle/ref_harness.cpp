@@ -1,0 +1,307 @@
+/* Driver that runs the reference's own hot-path sources (mesh.cpp portSet,
+ * generateStiff.cpp, matrixCon.cpp paraGenerator, and the fdtdMesh members
+ * in fdtd.hpp), compiled unmodified, on a layout given as raw arrays.
+ * TEST INFRASTRUCTURE ONLY: built by oracle/build_ref.sh into oracle/_ref/
+ * to pin the C restatement (oracle/pipeline.c) and generate tests/golden/.
+ *
+ * The reference fills fdtdMesh from GDSII through meshAndMark; this driver
+ * fills the same members from the rasterised marks instead and restates only
+ * the post-grid steps of meshAndMark that are not separate functions:
+ * conductor BFS (mesh.cpp:683-796), port/conductor association
+ * (mesh.cpp:884-960), PEC-plane sets (mesh.cpp:963-987) and edge colouring
+ * (mesh.cpp:1006-1020).  findPortNode, findBoundNodeEdge, findCond2CondIn,
+ * setMapEdge, portSet, generateStiff, merge_v0d1, generateAd, merge_v0c,
+ * generateAc and paraGenerator are the reference's own.
+ *
+ * usage: ref_pipeline <in_dir> <out_dir> */
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <map>
+#include <fstream>
+#include <sstream>
+#include <queue>
+#include "fdtd.hpp"
+#include "hypreSolver.h"
+#include "oracle.h"
+
+static std::string g_out;
+static int g_solve_calls = 0;
+
+static std::vector<char> read_file(const std::string &p) {
+    std::ifstream f(p, std::ios::binary);
+    if (!f) { fprintf(stderr, "cannot read %s\n", p.c_str()); exit(3); }
+    return std::vector<char>((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+}
+
+template <class T> static std::vector<T> read_arr(const std::string &dir, const char *name) {
+    std::vector<char> b = read_file(dir + "/" + name);
+    std::vector<T> v(b.size() / sizeof(T));
+    memcpy(v.data(), b.data(), v.size() * sizeof(T));
+    return v;
+}
+
+template <class T> static void write_arr(const char *name, const T *p, size_t n) {
+    std::string path = g_out + "/" + name;
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) { fprintf(stderr, "cannot write %s\n", path.c_str()); exit(3); }
+    if (n) fwrite(p, sizeof(T), n, f);
+    fclose(f);
+}
+
+/* The reference's hypreSolve boundary (hypreSolve.cpp:9), served by the
+ * project FP64 CPU solver at a tight tolerance; each call's right-hand side
+ * and solution are recorded for the fixtures. */
+int hypreSolve(fdtdMesh *sys, myint *ARowId, myint *AColId, double *Aval, myint leng_A, double *bin,
+               myint leng_v0, double *solution) {
+    (void)sys;
+    g2po_solver_opts o;
+    g2po_solver_default_opts(&o);
+    o.rtol = 1e-13; o.maxit = 4000; o.restart = 60;
+    g2po_solve_stats st;
+    int rc = g2po_solve_coo((const int64_t *)ARowId, (const int64_t *)AColId, Aval, leng_A, bin, leng_v0,
+                            solution, &o, &st);
+    char nb[64], nx[64];
+    snprintf(nb, sizeof nb, "solve%d_b.f64", g_solve_calls);
+    snprintf(nx, sizeof nx, "solve%d_x.f64", g_solve_calls);
+    write_arr(nb, bin, (size_t)leng_v0);
+    write_arr(nx, solution, (size_t)leng_v0);
+    fprintf(stderr, "[ref] solve %d n=%lld it=%d rel=%.3e rc=%d\n", g_solve_calls, (long long)leng_v0,
+            st.iterations, st.rel_residual, rc);
+    g_solve_calls++;
+    return 0;
+}
+
+int main(int argc, char **argv) {
+    if (argc < 3) { fprintf(stderr, "usage: %s in_dir out_dir\n", argv[0]); return 2; }
+    std::string in = argv[1];
+    g_out = argv[2];
+    std::map<std::string, double> meta;
+    {
+        std::ifstream f(in + "/meta.txt");
+        std::string k; double v;
+        while (f >> k >> v) meta[k] = v;
+    }
+    fdtdMesh sys;
+    sys.lengthUnit = 1.0;
+    sys.nx = (myint)meta["nx"]; sys.ny = (myint)meta["ny"]; sys.nz = (myint)meta["nz"];
+    sys.freqStart = meta["freqStart"]; sys.freqEnd = meta["freqEnd"]; sys.freqUnit = meta["freqUnit"];
+    sys.nfreq = (int)meta["nfreq"]; sys.freqScale = (int)meta["freqScale"];
+    sys.numCdtRow = (myint)meta["numBoxes"];
+    std::vector<double> xn = read_arr<double>(in, "xn.f64"), yn = read_arr<double>(in, "yn.f64"),
+                        zn = read_arr<double>(in, "zn.f64");
+    sys.xn = (double *)malloc(sizeof(double) * xn.size()); memcpy(sys.xn, xn.data(), sizeof(double) * xn.size());
+    sys.yn = (double *)malloc(sizeof(double) * yn.size()); memcpy(sys.yn, yn.data(), sizeof(double) * yn.size());
+    sys.zn = (double *)malloc(sizeof(double) * zn.size()); memcpy(sys.zn, zn.data(), sizeof(double) * zn.size());
+    std::vector<double> se = read_arr<double>(in, "stack_epsn.f64"), ss = read_arr<double>(in, "stack_sign.f64");
+    sys.stackEpsn.assign(se.begin(), se.end());
+    sys.stackSign.assign(ss.begin(), ss.end());
+    unordered_map<double, int> xi, yi, zi;
+    for (myint i = 0; i < sys.nx; i++) xi[sys.xn[i]] = (int)i;
+    for (myint i = 0; i < sys.ny; i++) yi[sys.yn[i]] = (int)i;
+    for (myint i = 0; i < sys.nz; i++) zi[sys.zn[i]] = (int)i;
+    /* mesh.cpp:393-406 */
+    sys.N_cell_x = sys.nx - 1; sys.N_cell_y = sys.ny - 1; sys.N_cell_z = sys.nz - 1;
+    sys.N_edge_s = sys.N_cell_y * (sys.N_cell_x + 1) + sys.N_cell_x * (sys.N_cell_y + 1);
+    sys.N_edge_v = (sys.N_cell_x + 1) * (sys.N_cell_y + 1);
+    sys.N_edge = sys.N_edge_s * (sys.N_cell_z + 1) + sys.N_edge_v * sys.N_cell_z;
+    sys.N_node_s = sys.N_edge_v;
+    sys.N_node = (sys.N_cell_z + 1) * sys.N_node_s;
+    sys.N_patch_s = sys.N_cell_x * sys.N_cell_y;
+    sys.N_patch_v = (sys.N_cell_x + 1) * sys.N_cell_y + (sys.N_cell_y + 1) * sys.N_cell_x;
+    sys.N_patch = sys.N_patch_s * (sys.N_cell_z + 1) + sys.N_patch_v * sys.N_cell_z;
+    std::vector<int64_t> me = read_arr<int64_t>(in, "mark_edge_raw.i64"), mn = read_arr<int64_t>(in, "mark_node_raw.i64");
+    if ((myint)me.size() != sys.N_edge || (myint)mn.size() != sys.N_node) { fprintf(stderr, "size mismatch\n"); return 3; }
+    sys.markEdge = (myint *)calloc(sys.N_edge, sizeof(myint));
+    sys.markNode = (myint *)calloc(sys.N_node, sizeof(myint));
+    memcpy(sys.markEdge, me.data(), sizeof(myint) * sys.N_edge);
+    memcpy(sys.markNode, mn.data(), sizeof(myint) * sys.N_node);
+
+    /* conductor BFS, restated from mesh.cpp:683-796 */
+    myint *visited = (myint *)calloc(sys.N_node, sizeof(myint));
+    myint count = 0;
+    std::queue<myint> qu;
+    myint Ny1 = sys.N_cell_y + 1, L = sys.N_edge_s + sys.N_edge_v;
+    for (myint indi = 0; indi < sys.N_node; indi++) {
+        if (sys.markNode[indi] == 0 || visited[indi] != 0) continue;
+        qu.push(indi);
+        count++;
+        visited[indi] = count;
+        while (!qu.empty()) {
+            myint f = qu.front();
+            myint inz = f / sys.N_node_s, inx = (f % sys.N_node_s) / Ny1, iny = (f % sys.N_node_s) % Ny1;
+            myint cand[6]; int nc = 0;
+            if (inz != 0) cand[nc++] = (inz - 1) * L + sys.N_edge_s + inx * Ny1 + iny;
+            if (inz != sys.nz - 1) cand[nc++] = inz * L + sys.N_edge_s + inx * Ny1 + iny;
+            if (inx != 0) cand[nc++] = inz * L + sys.N_cell_y * (sys.N_cell_x + 1) + (inx - 1) * Ny1 + iny;
+            if (inx != sys.nx - 1) cand[nc++] = inz * L + sys.N_cell_y * (sys.N_cell_x + 1) + inx * Ny1 + iny;
+            if (iny != 0) cand[nc++] = inz * L + inx * sys.N_cell_y + iny - 1;
+            if (iny != sys.ny - 1) cand[nc++] = inz * L + inx * sys.N_cell_y + iny;
+            for (int t = 0; t < nc; t++) {
+                myint eno = cand[t], n1, n2;
+                if (sys.markEdge[eno] == 0) continue;
+                sys.compute_edgelink(eno, n1, n2);
+                if (n1 != f && visited[n1] == 0) { visited[n1] = count; qu.push(n1); }
+                else if (n2 != f && visited[n2] == 0) { visited[n2] = count; qu.push(n2); }
+            }
+            qu.pop();
+        }
+    }
+    for (myint i = 0; i < sys.N_node; i++) sys.markNode[i] = visited[i];
+    sys.numCdt = count;
+    sys.conductor = (fdtdCdt *)malloc(sys.numCdt * sizeof(fdtdCdt));
+    sys.cdtNumNode = (myint *)calloc(sys.numCdt, sizeof(myint));
+    for (myint i = 0; i < sys.N_node; i++) if (visited[i]) sys.cdtNumNode[visited[i] - 1]++;
+    for (myint i = 0; i < sys.numCdt; i++) {
+        sys.conductor[i].node = (myint *)calloc(sys.cdtNumNode[i], sizeof(myint));
+        sys.conductor[i].cdtNodeind = 0;
+        sys.conductor[i].markPort = 0;
+    }
+    for (myint i = 0; i < sys.N_node; i++)
+        if (visited[i]) { fdtdCdt &c = sys.conductor[visited[i] - 1]; c.node[c.cdtNodeind++] = i; }
+
+    /* ports (solnoutclass.hpp:5894-5984 fills these from .sim_input) */
+    std::vector<double> ports = read_arr<double>(in, "ports.f64");    /* per side: port, x1 y1 z1 x2 y2 z2 dir */
+    sys.numPorts = (int)meta["numPorts"];
+    sys.portCoor.resize(sys.numPorts);
+    size_t nside = ports.size() / 8;
+    for (size_t s = 0; s < nside; s++) {
+        const double *r = &ports[8 * s];
+        fdtdPort &p = sys.portCoor[(int)r[0]];
+        p.multiplicity++;
+        p.x1.push_back(r[1]); p.y1.push_back(r[2]); p.z1.push_back(r[3]);
+        p.x2.push_back(r[4]); p.y2.push_back(r[5]); p.z2.push_back(r[6]);
+        p.portDirection.push_back((int)r[7]);
+    }
+    /* mesh.cpp:884-960 */
+    std::set<int> cond;
+    std::vector<uint8_t> cdt_return(sys.numCdt, 0);
+    for (int indi = 0; indi < sys.numPorts; indi++) {
+        fdtdPort &pc = sys.portCoor[indi];
+        myint n1 = 0, n2 = 0;
+        for (int k = 0; k < pc.multiplicity; k++) {
+            int mark = sys.findPortNode(50, xi[pc.x1[k]], yi[pc.y1[k]], zi[pc.z1[k]], xi[pc.x2[k]], yi[pc.y2[k]], zi[pc.z2[k]], indi, k);
+            n1 = sys.markNode[zi[pc.z1[k]] * sys.N_node_s + xi[pc.x1[k]] * Ny1 + yi[pc.y1[k]]];
+            n2 = sys.markNode[zi[pc.z2[k]] * sys.N_node_s + xi[pc.x2[k]] * Ny1 + yi[pc.y2[k]]];
+            if (mark == 0) { fprintf(stderr, "port node not in a conductor\n"); return 4; }
+        }
+        sys.conductor[n1 - 1].markPort = indi + 1;
+        sys.conductor[n2 - 1].markPort = -1;
+        if (cond.find((int)n1) == cond.end()) {
+            cond.insert((int)n1);
+            for (myint j = 0; j < sys.cdtNumNode[n1 - 1]; j++) {
+                myint nd = sys.conductor[n1 - 1].node[j];
+                sys.findCond2CondIn((int)((nd % sys.N_node_s) / Ny1), (int)((nd % sys.N_node_s) % Ny1), (int)(nd / sys.N_node_s));
+            }
+        }
+        if (cond.find((int)n2) == cond.end()) {
+            cond.insert((int)n2);
+            cdt_return[n2 - 1] = 1;
+            for (myint j = 0; j < sys.cdtNumNode[n2 - 1]; j++) {
+                myint nd = sys.conductor[n2 - 1].node[j];
+                int ix = (int)((nd % sys.N_node_s) / Ny1), iy = (int)((nd % sys.N_node_s) % Ny1), iz = (int)(nd / sys.N_node_s);
+                sys.findBoundNodeEdge(ix, iy, iz);
+                sys.findCond2CondIn(ix, iy, iz);
+            }
+        }
+    }
+    /* LOWER_BOUNDARY_PEC (mesh.cpp:963-972) */
+    for (myint i = 0; i < sys.N_edge_s; i++) sys.lbde.insert(i);
+    for (myint i = 0; i < sys.N_node_s; i++) sys.lbdn.insert(i);
+    sys.bden = (int)(sys.lbde.size() + sys.ubde.size());
+    sys.setMapEdge();
+    /* colouring (mesh.cpp:1006-1020) */
+    for (myint i = 0; i < sys.N_edge; i++) {
+        myint a, b;
+        sys.compute_edgelink(i, a, b);
+        if (sys.markEdge[i] != 0 && visited[a] == visited[b] && visited[a] != 0) sys.markEdge[i] = visited[b];
+    }
+    free(visited);
+    if (portSet(&sys, xi, yi, zi) != 0) { fprintf(stderr, "portSet failed\n"); return 5; }
+
+    write_arr("mark_node.i64", (int64_t *)sys.markNode, sys.N_node);
+    write_arr("mark_edge.i64", (int64_t *)sys.markEdge, sys.N_edge);
+    std::vector<int32_t> mp(sys.numCdt);
+    for (myint i = 0; i < sys.numCdt; i++) mp[i] = sys.conductor[i].markPort;
+    write_arr("mark_port.i32", mp.data(), mp.size());
+    write_arr("cdt_return.u8", cdt_return.data(), cdt_return.size());
+    write_arr("map_edge.i64", (int64_t *)sys.mapEdge, sys.N_edge);
+    {
+        std::vector<int64_t> pe; std::vector<int64_t> pptr{0}; std::vector<double> area; std::vector<int32_t> dir;
+        for (int p = 0; p < sys.numPorts; p++)
+            for (size_t s = 0; s < sys.portCoor[p].portEdge.size(); s++) {
+                for (myint e : sys.portCoor[p].portEdge[s]) pe.push_back(e);
+                pptr.push_back((int64_t)pe.size());
+                area.push_back(sys.portCoor[p].portArea[s]);
+                dir.push_back(sys.portCoor[p].portDirection[s]);
+            }
+        write_arr("side_edges.i64", pe.data(), pe.size());
+        write_arr("side_edge_ptr.i64", pptr.data(), pptr.size());
+        write_arr("side_area.f64", area.data(), area.size());
+        write_arr("side_dir.i32", dir.data(), dir.size());
+    }
+    std::ofstream meta_out(g_out + "/meta_out.txt");
+    meta_out << "numCdt " << sys.numCdt << "\nbden " << sys.bden << "\n";
+
+    if (meta["skipStiff"] == 0) {
+        generateStiff(&sys);
+        write_arr("S_row.i64", (int64_t *)sys.SRowId, sys.leng_S);
+        write_arr("S_col.i64", (int64_t *)sys.SColId, sys.leng_S);
+        write_arr("S_val.f64", sys.Sval, sys.leng_S);
+        meta_out << "leng_S " << sys.leng_S << "\n";
+    }
+    {
+        myint *map = (myint *)calloc(sys.N_node, sizeof(myint));
+        myint v0d1num = 0, leng_v0d1 = 0, v0d1anum = 0, leng_v0d1a = 0, leng_Ad = 0;
+        sys.merge_v0d1(0, 0, 0, 0, 0, 0, v0d1num, leng_v0d1, v0d1anum, leng_v0d1a, map, 0.);
+        write_arr("v0d_row.i64", (int64_t *)sys.v0d1RowId, v0d1num);
+        write_arr("v0d_col.i64", (int64_t *)sys.v0d1ColId, v0d1num);
+        write_arr("v0d_val.f64", sys.v0d1val, v0d1num);
+        write_arr("v0d_aval.f64", sys.v0d1aval, v0d1anum);
+        write_arr("v0d_map.i64", (int64_t *)map, sys.N_node);
+        sys.generateAd(map, v0d1num, v0d1anum, leng_v0d1, leng_Ad);
+        write_arr("Ad_row.i64", (int64_t *)sys.AdRowId, leng_Ad);
+        write_arr("Ad_col.i64", (int64_t *)sys.AdColId, leng_Ad);
+        write_arr("Ad_val.f64", sys.Adval, leng_Ad);
+        meta_out << "leng_v0d " << leng_v0d1 << "\nleng_Ad " << leng_Ad << "\n";
+        free(sys.v0d1RowId); free(sys.v0d1ColId); free(sys.v0d1val); free(sys.v0d1aval);
+        free(sys.AdRowId); free(sys.AdColId); free(sys.Adval);
+        sys.v0d1RowId = NULL; sys.v0d1ColId = NULL; sys.v0d1val = NULL; sys.v0d1aval = NULL;
+        sys.AdRowId = NULL; sys.AdColId = NULL; sys.Adval = NULL;
+        free(map);
+        map = (myint *)calloc(sys.N_node, sizeof(myint));
+        myint v0cnum = 0, leng_v0c = 0, v0canum = 0, leng_v0ca = 0, leng_Ac = 0;
+        sys.cindex.push_back(-1);
+        sys.acu_cnno.push_back(0);
+        sys.merge_v0c(0, 0, 0, 0, v0cnum, leng_v0c, v0canum, leng_v0ca, map);
+        write_arr("v0c_row.i64", (int64_t *)sys.v0cRowId, v0cnum);
+        write_arr("v0c_col.i64", (int64_t *)sys.v0cColId, v0cnum);
+        write_arr("v0c_val.f64", sys.v0cval, v0cnum);
+        write_arr("v0c_aval.f64", sys.v0caval, v0canum);
+        write_arr("v0c_map.i64", (int64_t *)map, sys.N_node);
+        sys.generateAc(map, v0cnum, v0canum, leng_v0c, leng_Ac);
+        write_arr("Ac_row.i64", (int64_t *)sys.AcRowId, leng_Ac);
+        write_arr("Ac_col.i64", (int64_t *)sys.AcColId, leng_Ac);
+        write_arr("Ac_val.f64", sys.Acval, leng_Ac);
+        meta_out << "leng_v0c " << leng_v0c << "\nleng_Ac " << leng_Ac << "\n";
+        free(sys.v0cRowId); free(sys.v0cColId); free(sys.v0cval); free(sys.v0caval);
+        free(sys.AcRowId); free(sys.AcColId); free(sys.Acval);
+        sys.v0cRowId = NULL; sys.v0cColId = NULL; sys.v0cval = NULL; sys.v0caval = NULL;
+        sys.AcRowId = NULL; sys.AcColId = NULL; sys.Acval = NULL;
+        sys.cindex.clear();
+        sys.acu_cnno.clear();
+        free(map);
+    }
+    if (meta["skipPara"] == 0) {
+        paraGenerator(&sys, xi, yi, zi);
+        write_arr("Z.c128", (double *)sys.x.data(), 2 * sys.x.size());
+    }
+    meta_out << "solves " << g_solve_calls << "\n";
+    meta_out.close();
+    /* paraGenerator released xn/yn/zn, markNode and conductor without
+       clearing every pointer the destructor frees, so leave without it */
+    fflush(stdout);
+    exit(0);
+}
