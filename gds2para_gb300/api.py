@@ -1,0 +1,193 @@
+"""The reference's entry points on the extraction path, over the C ABI.
+
+    FdtdMesh        <- fdtdMesh (src/fdtd.hpp:182), filled from a MeshDesc
+    generateStiff   <- generateStiff (src/generateStiff.cpp:6)
+    hypreSolve      <- hypreSolve (src/hypreSolve.cpp:9)
+    paraGenerator   <- paraGenerator (src/matrixCon.cpp:11)
+
+Names and argument meanings follow the reference; unlike it, failures raise
+G2PError instead of being ignored.  All compute runs in libgds2para_gb300.so
+on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Tuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import ExtractStats, G2PError, SolverParams, SolveStats, Sizes, check
+from .layout import MeshDesc
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def default_params(parity: bool = False, **kw) -> SolverParams:
+    """parity=True gives hypreSolve's settings (KDim 10, 100 iterations,
+    rtol 1e-4; src/hypreSolver.h:7-11); otherwise FP64 at rtol 1e-10."""
+    p = SolverParams()
+    _lib.load().g2p_default_params(C.byref(p), 1 if parity else 0)
+    for k, v in kw.items():
+        if k == "precision" and isinstance(v, str):
+            v = {"fp64": _lib.G2P_PREC_FP64, "mixed": _lib.G2P_PREC_MIXED}[v]
+        setattr(p, k, v)
+    return p
+
+
+class FdtdMesh:
+    """Device-resident mesh: the fdtdMesh fields the path reads."""
+
+    def __init__(self, desc: MeshDesc):
+        L = _lib.load()
+        self.desc = desc
+        self._keep = dict(
+            xn=_c(desc.xn, np.float64), yn=_c(desc.yn, np.float64), zn=_c(desc.zn, np.float64),
+            se=_c(desc.stack_epsn, np.float64), ss=_c(desc.stack_sign, np.float64),
+            mn=_c(desc.mark_node, np.int64), me=_c(desc.mark_edge, np.int64),
+            mp=_c(desc.mark_port, np.int32), cr=_c(desc.cdt_return, np.uint8),
+            psp=_c(desc.port_side_ptr, np.int32), sep=_c(desc.side_edge_ptr, np.int64),
+            sed=_c(desc.side_edges, np.int64), sa=_c(desc.side_area, np.float64), sd=_c(desc.side_dir, np.int32))
+        k = self._keep
+        p = lambda n: k[n].ctypes.data
+        self._desc = _lib.MeshDescC(desc.nx, desc.ny, desc.nz, p("xn"), p("yn"), p("zn"), p("se"), p("ss"),
+                                    p("mn"), p("me"), desc.num_cdt, p("mp"), p("cr"), desc.num_ports, p("psp"),
+                                    p("sep"), p("sed"), p("sa"), p("sd"), desc.freq_start, desc.freq_end,
+                                    desc.freq_unit, desc.nfreq, desc.freq_scale)
+        h = C.c_void_p()
+        check(L.g2p_mesh_create(C.byref(self._desc), C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().g2p_mesh_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- index maps (setMapEdge, fdtd.hpp:1508) ----
+    def index_maps(self) -> Tuple[np.ndarray, int]:
+        bden = C.c_int64()
+        me = np.empty(self.desc.N_edge, np.int64)
+        check(_lib.load().g2p_index_maps(self.handle, C.byref(bden), me.ctypes.data))
+        return me, int(bden.value)
+
+    def sizes(self) -> Sizes:
+        s = Sizes()
+        check(_lib.load().g2p_mesh_sizes(self.handle, C.byref(s)))
+        return s
+
+    def export_stiff(self):
+        n = self.sizes().leng_S
+        r, c, v = np.empty(n, np.int64), np.empty(n, np.int64), np.empty(n, np.float64)
+        check(_lib.load().g2p_export_stiff(self.handle, r.ctypes.data, c.ctypes.data, v.ctypes.data))
+        return r, c, v
+
+    def assemble_v0(self) -> Sizes:
+        s = Sizes()
+        check(_lib.load().g2p_assemble_v0(self.handle, C.byref(s)))
+        return s
+
+    def export_v0(self, which: str):
+        w = {"d": 0, "c": 1}[which]
+        s = self.sizes()
+        n = s.nnz_v0d if w == 0 else s.nnz_v0c
+        r, c = np.empty(n, np.int64), np.empty(n, np.int64)
+        v, a = np.empty(n, np.float64), np.empty(n, np.float64)
+        mp = np.empty(self.desc.N_node, np.int64)
+        check(_lib.load().g2p_export_v0(self.handle, w, r.ctypes.data, c.ctypes.data, v.ctypes.data, a.ctypes.data,
+                                        mp.ctypes.data))
+        return dict(row=r, col=c, val=v, aval=a, map=mp, ncol=s.leng_v0d if w == 0 else s.leng_v0c)
+
+    def export_laplacian(self, which: str):
+        w = {"d": 0, "c": 1}[which]
+        s = self.sizes()
+        n = s.nnz_ad if w == 0 else s.nnz_ac
+        r, c, v = np.empty(n, np.int64), np.empty(n, np.int64), np.empty(n, np.float64)
+        check(_lib.load().g2p_export_laplacian(self.handle, w, r.ctypes.data, c.ctypes.data, v.ctypes.data))
+        return r, c, v
+
+
+def generateStiff(sys: FdtdMesh) -> int:
+    """generateStiff (src/generateStiff.cpp:6): builds S on the device and
+    returns leng_S."""
+    n = C.c_int64()
+    check(_lib.load().g2p_generate_stiff(sys.handle, C.byref(n)))
+    return int(n.value)
+
+
+def hypreSolve(sys, ARowId, AColId, Aval, leng_A, bin, leng_v0, solution) -> int:
+    """hypreSolve (src/hypreSolve.cpp:9) with the reference's settings.  `sys`
+    is unused, as in the reference.  Writes `solution` in place; returns 0 on
+    convergence and raises on failure (the reference returns 0 regardless)."""
+    r = _c(ARowId, np.int64); c = _c(AColId, np.int64); v = _c(Aval, np.float64); b = _c(bin, np.float64)
+    if not (isinstance(solution, np.ndarray) and solution.dtype == np.float64 and solution.flags.c_contiguous):
+        raise TypeError("solution must be a contiguous float64 array")
+    st = _lib.load().g2p_hypre_solve(r.ctypes.data, c.ctypes.data, v.ctypes.data, int(leng_A), b.ctypes.data,
+                                     int(leng_v0), solution.ctypes.data)
+    check(st, allow=(_lib.G2P_OK, _lib.G2P_ERR_NOT_CONVERGED))
+    return 0
+
+
+class Solver:
+    """A reusable AMG-FGMRES solver over one matrix (row-sorted COO input)."""
+
+    def __init__(self, rows, cols, vals, n, params: Optional[SolverParams] = None):
+        self._r, self._c, self._v = _c(rows, np.int64), _c(cols, np.int64), _c(vals, np.float64)
+        self.n = int(n)
+        h = C.c_void_p()
+        p = params if params is not None else default_params()
+        check(_lib.load().g2p_solver_create(self._r.ctypes.data, self._c.ctypes.data, self._v.ctypes.data,
+                                            len(self._v), self.n, C.byref(p), C.byref(h)))
+        self.handle = h
+
+    def solve(self, b: np.ndarray, allow_unconverged: bool = False):
+        b = np.asarray(b, np.float64)
+        k = 1 if b.ndim == 1 else b.shape[1]
+        bc = np.asfortranarray(b.reshape(self.n, k))
+        x = np.zeros((self.n, k), np.float64, order="F")
+        st = SolveStats()
+        rc = _lib.load().g2p_solver_solve(self.handle, bc.ctypes.data, x.ctypes.data, k, C.byref(st))
+        check(rc, allow=(_lib.G2P_OK, _lib.G2P_ERR_NOT_CONVERGED) if allow_unconverged else (_lib.G2P_OK,))
+        return (x[:, 0] if b.ndim == 1 else x), st
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().g2p_solver_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def paraGenerator(sys: FdtdMesh, params: Optional[SolverParams] = None):
+    """paraGenerator (src/matrixCon.cpp:11): returns (Z, stats) with Z shaped
+    (nfreq, P, P) in sys->x's storage order: Z[f].ravel()[q + P*p] is the
+    response at port q to a unit source at port p for f = 0; later
+    frequencies are stored transposed, as print_z_V0 leaves them."""
+    d = sys.desc
+    z = np.zeros(2 * d.nfreq * d.num_ports * d.num_ports, np.float64)
+    st = ExtractStats()
+    p = params if params is not None else default_params()
+    rc = _lib.load().g2p_para_generator(sys.handle, C.byref(p), z.ctypes.data, C.byref(st))
+    check(rc)
+    zc = z[0::2] + 1j * z[1::2]
+    return zc.reshape(d.nfreq, d.num_ports, d.num_ports), st
+
+
+__all__ = ["FdtdMesh", "generateStiff", "hypreSolve", "paraGenerator", "Solver", "default_params", "G2PError"]

@@ -1,0 +1,333 @@
+// paraGenerator on the device (matrixCon.cpp:11-907, default SKIP_VH path).
+//
+// Per port the reference forms J on the port edges, solves Ad, Ac, Ad with
+// HYPRE and back-projects with MKL sparse mat-vecs (matrixCon.cpp:363-603),
+// then assembles Z with Construct_Z_V0 (fdtd.hpp:4173-4215) and rescales
+// Im Z by f0/f in print_z_V0 (fdtd.hpp:4249-4316).  Here all ports of a
+// block are right-hand sides of one batched solve per system, the V0
+// products use the per-edge view (V y) and the column lists (V^T x) built at
+// assembly, and the operations keep the reference's order per entry.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "primitives.cuh"
+#include "solver.h"
+
+g2p_status g2p_run_v0(g2p_mesh *m);
+g2p_status g2p_solver_build(const g2p::Csr<double> &A, const g2p_solver_params *p, cudaStream_t stream,
+                            g2p_solver **out);
+g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k, g2p_solve_stats *st);
+
+namespace g2p {
+
+// B[c, r] += aval * J over the port edges of the block (matrixCon.cpp:384, 436)
+__global__ void k_rhs_ports(int64_t nent, const int32_t *pe_edge, const int32_t *pe_port, const double *pe_J,
+                            const int32_t *ecol, const double *eaval, int k, double *B) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nent; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t e = pe_edge[t];
+        int r = pe_port[t];
+        double J = pe_J[t];
+        for (int s = 0; s < 2; s++) {
+            int32_t c = ecol[2 * e + s];
+            if (c >= 0) atomicAdd(&B[(int64_t)c * k + r], eaval[2 * e + s] * J);
+        }
+    }
+}
+
+__global__ void k_scale(int64_t n, double *x, double a) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] *= a;
+}
+
+__global__ void k_div(int64_t n, double *x, double a) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] /= a;
+}
+
+// y[e, r] = V x over the (<= 2) entries of edge e in ascending column order
+__global__ void k_v0_apply(int64_t nedge, int k, const int32_t *ecol, const double *eval, const double *X, double *Y) {
+    int64_t total = nedge * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t e = t / k;
+        int r = (int)(t - e * k);
+        double acc = 0.0;
+        int32_t c0 = ecol[2 * e], c1 = ecol[2 * e + 1];
+        if (c0 >= 0) acc += eval[2 * e] * (1.0 * X[(int64_t)c0 * k + r]);
+        if (c1 >= 0) acc += eval[2 * e + 1] * (1.0 * X[(int64_t)c1 * k + r]);
+        Y[t] = acc;
+    }
+}
+
+// Edge-side factor applied before a V^T product:
+//   mode 0 (crhs, matrixCon.cpp:445): src * (-1.0 * omega * stackEpsn * eps0)
+//   mode 1 (yccp, matrixCon.cpp:534): -src * stackEpsn * eps0
+struct EdgeFactor {
+    Dims d;
+    const double *epsn;
+    double omega, eps0;
+    int mode;
+    __device__ __forceinline__ double operator()(int64_t e, double v) const {
+        double ep = epsn[e / d.L];
+        if (mode == 0) return v * (-1.0 * omega * ep * eps0);
+        return -v * ep * eps0;
+    }
+};
+
+// out[c, r] = sum over column c's entries (in order) of aval * f(src[e, r])
+__global__ void k_v0t_short(int64_t ncol, int k, const int64_t *cptr, const int32_t *cedge, const double *caval,
+                            const double *src, EdgeFactor f, double *out) {
+    int64_t total = ncol * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c = t / k;
+        int r = (int)(t - c * k);
+        int64_t s0 = cptr[c], s1 = cptr[c + 1];
+        if (s1 - s0 > kLongRow) continue;
+        double acc = 0.0;
+        for (int64_t q = s0; q < s1; q++) {
+            int64_t e = cedge[q];
+            acc += caval[q] * f(e, src[e * k + r]);
+        }
+        out[t] = acc;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_v0t_long(const int32_t *cols, int k, const int64_t *cptr, const int32_t *cedge,
+                                                  const double *caval, const double *src, EdgeFactor f, double *out) {
+    __shared__ double red[256];
+    int64_t c = cols[blockIdx.x];
+    int64_t s0 = cptr[c], s1 = cptr[c + 1];
+    for (int r = 0; r < k; r++) {
+        double acc = 0.0;
+        for (int64_t q = s0 + threadIdx.x; q < s1; q += blockDim.x) {
+            int64_t e = cedge[q];
+            acc += caval[q] * f(e, src[e * k + r]);
+        }
+        red[threadIdx.x] = acc;
+        __syncthreads();
+        for (int o = 128; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[c * k + r] = red[0];
+        __syncthreads();
+    }
+}
+
+__global__ void k_add(int64_t n, double *a, const double *b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] += b[i];
+}
+
+// Construct_Z_V0 for the block: Z[q + P*p] over side-0 edges of port q.
+__global__ void k_construct_z(int P, int p0, int kb, const int64_t *rptr, const int32_t *redge, const int32_t *rdir,
+                              Dims d, const double *xn, const double *yn, const double *zn, const double *yd1,
+                              const double *yc, const double *yd2, const double *cur, double *zre, double *zim) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P * kb) return;
+    int q = t % P, r = t / P;
+    int p = p0 + r;
+    double re = 0.0, im = 0.0;
+    for (int64_t j = rptr[q]; j < rptr[q + 1]; j++) {
+        int64_t e = redge[j];
+        int64_t n1, n2, inz, inx, iny;
+        int kind = d.edge_nodes(e, n1, n2, inz, inx, iny);
+        double leng = kind == 2 ? zn[inz + 1] - zn[inz] : (kind == 1 ? xn[inx + 1] - xn[inx] : yn[iny + 1] - yn[iny]);
+        double dir = rdir[q] * 1.0;
+        double yre = (yd2[e * kb + r] - 0.0) + yc[e * kb + r];
+        double yim = 0.0 - yd1[e * kb + r];
+        re -= yre * leng * dir;
+        im -= yim * leng * dir;
+    }
+    zre[q + (int64_t)P * p] = re / cur[p];
+    zim[q + (int64_t)P * p] = im / cur[p];
+}
+
+// print_z_V0 layout: frequency 0 as assembled, later ones transposed with
+// Im Z scaled by f0/f (fdtd.hpp:4270-4300).
+__global__ void k_z_layout(int P, int nfreq, const double *fr, double f0, const double *zre, const double *zim,
+                           double *out) {
+    int64_t total = (int64_t)nfreq * P * P;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int f = (int)(t / ((int64_t)P * P));
+        int64_t w = t - (int64_t)f * P * P;
+        int i = (int)(w / P), j = (int)(w % P);   // w = j + i*P for the source entry
+        int64_t src = j + (int64_t)i * P;
+        int64_t o0 = (int64_t)f * P * P;
+        if (f == 0) {
+            out[2 * (o0 + src)] = zre[src];
+            out[2 * (o0 + src) + 1] = zim[src];
+        } else {
+            int64_t dst = o0 + i + (int64_t)j * P;
+            out[2 * dst] = zre[src] + 0.0;
+            out[2 * dst + 1] = zim[src] * f0 / fr[f];
+        }
+    }
+}
+
+static double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace g2p
+
+using namespace g2p;
+
+static double freq_of(const g2p_mesh *m, int id) {
+    if (m->nfreq == 1) return m->freq_start * m->freq_unit;
+    if (id == m->nfreq - 1) return m->freq_end * m->freq_unit;
+    if (m->freq_scale == 1)
+        return (m->freq_start + id * (m->freq_end - m->freq_start) / (m->nfreq - 1)) * m->freq_unit;
+    return m->freq_start * m->freq_unit * pow(m->freq_end / m->freq_start, (id * 1.0 / (m->nfreq - 1)));
+}
+
+extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *pin, double *z_out,
+                                         g2p_extract_stats *st) {
+    if (!m || !z_out) { set_last_message("null argument"); return G2P_ERR_INVALID; }
+    if (m->num_ports < 1) { set_last_message("mesh has no ports"); return G2P_ERR_INVALID; }
+    g2p_solver_params p;
+    if (pin) p = *pin; else g2p_default_params(&p, 0);
+    auto t_all = std::chrono::steady_clock::now();
+    cudaStream_t s = m->stream;
+    const Dims &d = m->d;
+    const int P = m->num_ports;
+    g2p_extract_stats local;
+    memset(&local, 0, sizeof(local));
+    auto t0 = std::chrono::steady_clock::now();
+    G2P_TRY(g2p_run_v0(m));
+    local.assembly_ms = ms_since(t0);
+    // ---- port data: J entries (last side wins, matrixCon.cpp:367-374),
+    //      response edges (side 0) and source currents
+    std::vector<int32_t> pe_edge, pe_port;
+    std::vector<double> pe_J, cur(P, 0.0);
+    std::vector<int64_t> pptr(P + 1, 0), rptr(P + 1, 0);
+    std::vector<int32_t> redge, rdir(P);
+    for (int q = 0; q < P; q++) {
+        std::map<int64_t, int> J;
+        for (int sd = m->port_side_ptr[q]; sd < m->port_side_ptr[q + 1]; sd++) {
+            for (int64_t j = m->side_edge_ptr[sd]; j < m->side_edge_ptr[sd + 1]; j++) J[m->side_edges[j]] = m->side_dir[sd];
+            cur[q] += m->side_area[sd];
+        }
+        for (auto &kv : J) { pe_edge.push_back((int32_t)kv.first); pe_port.push_back(q); pe_J.push_back((double)kv.second); }
+        pptr[q + 1] = (int64_t)pe_edge.size();
+        int s0 = m->port_side_ptr[q];
+        for (int64_t j = m->side_edge_ptr[s0]; j < m->side_edge_ptr[s0 + 1]; j++) redge.push_back((int32_t)m->side_edges[j]);
+        rptr[q + 1] = (int64_t)redge.size();
+        rdir[q] = m->side_dir[s0];
+    }
+    int32_t *d_pe_edge, *d_pe_port, *d_redge, *d_rdir;
+    double *d_pe_J, *d_cur;
+    int64_t *d_rptr;
+    int64_t npe = (int64_t)pe_edge.size();
+    G2P_TRY(dalloc(&d_pe_edge, npe, s)); G2P_TRY(dalloc(&d_pe_port, npe, s)); G2P_TRY(dalloc(&d_pe_J, npe, s));
+    G2P_TRY(dalloc(&d_redge, (int64_t)redge.size(), s)); G2P_TRY(dalloc(&d_rdir, P, s));
+    G2P_TRY(dalloc(&d_rptr, P + 1, s)); G2P_TRY(dalloc(&d_cur, P, s));
+    G2P_CUDA(cudaMemcpyAsync(d_pe_edge, pe_edge.data(), sizeof(int32_t) * npe, cudaMemcpyHostToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(d_pe_J, pe_J.data(), sizeof(double) * npe, cudaMemcpyHostToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(d_redge, redge.data(), sizeof(int32_t) * redge.size(), cudaMemcpyHostToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(d_rdir, rdir.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(d_rptr, rptr.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(d_cur, cur.data(), sizeof(double) * P, cudaMemcpyHostToDevice, s));
+    // ---- solvers (setup once per operator; the reference rebuilds per call)
+    t0 = std::chrono::steady_clock::now();
+    g2p_solver *Sd = nullptr, *Sc = nullptr;
+    G2P_TRY(g2p_solver_build(m->Ad, &p, s, &Sd));
+    g2p_status rs = g2p_solver_build(m->Ac, &p, s, &Sc);
+    if (rs != G2P_OK) { g2p_solver_destroy(Sd); return rs; }
+    local.setup_ms = ms_since(t0);
+    local.ad_levels = Sd->levels;
+    local.ac_levels = Sc->levels;
+    int32_t *d_long_d = nullptr;
+    int64_t nlong_d = 0;
+    {
+        // long columns of V0d (conductor columns)
+        Csr<double> tmp;
+        tmp.n = m->v0d.ncol; tmp.ptr = m->v0d.cptr;
+        G2P_TRY(find_long_rows(tmp, &d_long_d, &nlong_d, s));
+    }
+    const int kb = p.batch ? P : 1;
+    const int64_t nd = m->v0d.ncol, nc = m->v0c.ncol, ne = d.N_edge;
+    double *Bd, *Yd, *Bc, *Yc, *crhs, *yd1, *yc, *yd2, *zre, *zim;
+    G2P_TRY(dalloc(&Bd, nd * kb, s)); G2P_TRY(dalloc(&Yd, nd * kb, s));
+    G2P_TRY(dalloc(&Bc, nc * kb, s)); G2P_TRY(dalloc(&Yc, nc * kb, s)); G2P_TRY(dalloc(&crhs, nc * kb, s));
+    G2P_TRY(dalloc(&yd1, ne * kb, s)); G2P_TRY(dalloc(&yc, ne * kb, s)); G2P_TRY(dalloc(&yd2, ne * kb, s));
+    G2P_TRY(dalloc(&zre, (int64_t)P * P, s)); G2P_TRY(dalloc(&zim, (int64_t)P * P, s));
+    const double omega = (2 * 3.14159265358979323846 * m->freq_start * m->freq_unit);
+    EdgeFactor f0{d, m->epsn, omega, m->k.eps0, 0};
+    EdgeFactor f1{d, m->epsn, omega, m->k.eps0, 1};
+    t0 = std::chrono::steady_clock::now();
+    g2p_status worst_rc = G2P_OK;
+    for (int p0 = 0; p0 < P; p0 += kb) {
+        int kk = std::min(kb, P - p0);
+        // entries of this block's ports, renumbered 0..kk-1
+        int64_t e0 = pptr[p0], e1 = pptr[p0 + kk];
+        std::vector<int32_t> port_local(pe_port.begin() + e0, pe_port.begin() + e1);
+        for (auto &v : port_local) v -= p0;
+        G2P_CUDA(cudaMemcpyAsync(d_pe_port + e0, port_local.data(), sizeof(int32_t) * (e1 - e0), cudaMemcpyHostToDevice, s));
+        // (1) b_d = -V0da^T J
+        G2P_CUDA(cudaMemsetAsync(Bd, 0, sizeof(double) * nd * kk, s));
+        k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
+                                                           m->v0d.ecol, m->v0d.eaval, kk, Bd);
+        k_scale<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Bd, -1.0);
+        g2p_solve_stats ss;
+        g2p_status rc = g2p_solver_solve_dev(Sd, Bd, Yd, kk, &ss);
+        if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }
+        if (rc == G2P_ERR_NOT_CONVERGED) worst_rc = rc;
+        local.solves += kk; local.total_iterations += ss.iterations;
+        local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
+        // (2) y0d /= omega ; yd1 = V0d y0d
+        k_div<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Yd, omega);
+        k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd1);
+        // (3) b_c = -V0ca^T J + V0ca^T(-omega D_eps yd1)
+        G2P_CUDA(cudaMemsetAsync(Bc, 0, sizeof(double) * nc * kk, s));
+        k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
+                                                           m->v0c.ecol, m->v0c.eaval, kk, Bc);
+        k_scale<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, -1.0);
+        k_v0t_short<<<grid_for(nc * kk), kThreads, 0, s>>>(nc, kk, m->v0c.cptr, m->v0c.cedge, m->v0c.caval, yd1, f0, crhs);
+        k_add<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, crhs);
+        // (4) Ac y0c = b_c
+        rc = g2p_solver_solve_dev(Sc, Bc, Yc, kk, &ss);
+        if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }
+        if (rc == G2P_ERR_NOT_CONVERGED) worst_rc = rc;
+        local.solves += kk; local.total_iterations += ss.iterations;
+        local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
+        // (5) yc = V0c y0c ; b_d2 = V0da^T(-D_eps yc)
+        k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0c.ecol, m->v0c.eval, Yc, yc);
+        k_v0t_short<<<grid_for(nd * kk), kThreads, 0, s>>>(nd, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd);
+        if (nlong_d > 0)
+            k_v0t_long<<<(unsigned)nlong_d, 256, 0, s>>>(d_long_d, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd);
+        // (6) Ad y0d2 = b_d2 ; yd2 = V0d y0d2
+        rc = g2p_solver_solve_dev(Sd, Bd, Yd, kk, &ss);
+        if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }
+        if (rc == G2P_ERR_NOT_CONVERGED) worst_rc = rc;
+        local.solves += kk; local.total_iterations += ss.iterations;
+        local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
+        k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd2);
+        // (7) Construct_Z_V0
+        k_construct_z<<<(P * kk + 127) / 128, 128, 0, s>>>(P, p0, kk, d_rptr, d_redge, d_rdir, d, m->xn, m->yn, m->zn, yd1,
+                                                          yc, yd2, d_cur, zre, zim);
+    }
+    // ---- print_z_V0 layout
+    std::vector<double> fr(m->nfreq);
+    for (int f = 0; f < m->nfreq; f++) fr[f] = freq_of(m, f);
+    double *d_fr, *d_out;
+    G2P_TRY(dalloc(&d_fr, m->nfreq, s));
+    G2P_TRY(dalloc(&d_out, 2LL * m->nfreq * P * P, s));
+    G2P_CUDA(cudaMemcpyAsync(d_fr, fr.data(), sizeof(double) * m->nfreq, cudaMemcpyHostToDevice, s));
+    k_z_layout<<<grid_for((int64_t)m->nfreq * P * P), kThreads, 0, s>>>(P, m->nfreq, d_fr, m->freq_start * m->freq_unit,
+                                                                        zre, zim, d_out);
+    G2P_CUDA(cudaMemcpyAsync(z_out, d_out, sizeof(double) * 2 * m->nfreq * P * P, cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    local.solve_ms = ms_since(t0);
+    dfree(d_fr, s); dfree(d_out, s);
+    dfree(Bd, s); dfree(Yd, s); dfree(Bc, s); dfree(Yc, s); dfree(crhs, s);
+    dfree(yd1, s); dfree(yc, s); dfree(yd2, s); dfree(zre, s); dfree(zim, s);
+    dfree(d_pe_edge, s); dfree(d_pe_port, s); dfree(d_pe_J, s); dfree(d_redge, s); dfree(d_rdir, s);
+    dfree(d_rptr, s); dfree(d_cur, s); dfree(d_long_d, s);
+    g2p_solver_destroy(Sd);
+    g2p_solver_destroy(Sc);
+    G2P_CUDA(cudaStreamSynchronize(s));
+    local.total_ms = ms_since(t_all);
+    g2p_mesh_sizes(m, &local.sizes);
+    if (st) *st = local;
+    return worst_rc;
+}

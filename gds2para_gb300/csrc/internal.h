@@ -1,0 +1,83 @@
+// Internal handle layouts (not part of the ABI).
+#pragma once
+#include <vector>
+#include "common.cuh"
+
+namespace g2p {
+
+// Device CSR with int64 row offsets and int32 columns.
+template <class T>
+struct Csr {
+    int64_t n = 0, m = 0, nnz = 0;
+    int64_t *ptr = nullptr;
+    int32_t *col = nullptr;
+    T *val = nullptr;
+    void release(cudaStream_t s) { dfree(ptr, s); dfree(col, s); dfree(val, s); n = m = nnz = 0; }
+};
+
+// One V0 basis: column-major (CSR over columns, entries in the reference's
+// COO order) plus the per-edge view used by V0*y (at most two entries per
+// edge, ascending column).
+struct V0Basis {
+    int64_t ncol = 0, nnz = 0;
+    int64_t *cptr = nullptr;   // [ncol+1]
+    int32_t *cedge = nullptr;  // [nnz] original edge index
+    double *cval = nullptr;    // [nnz] +-1/h
+    double *caval = nullptr;   // [nnz] a-values
+    int32_t *map = nullptr;    // [N_node] column+1 or 0
+    // per-edge view: up to two (column, val, aval) per edge
+    int32_t *ecol = nullptr;   // [2*N_edge], -1 when absent
+    double *eval = nullptr;    // [2*N_edge]
+    double *eaval = nullptr;   // [2*N_edge]
+    void release(cudaStream_t s) {
+        dfree(cptr, s); dfree(cedge, s); dfree(cval, s); dfree(caval, s); dfree(map, s);
+        dfree(ecol, s); dfree(eval, s); dfree(eaval, s);
+        ncol = nnz = 0;
+    }
+};
+
+struct Constants {
+    double mu, eps0;
+};
+
+}  // namespace g2p
+
+struct g2p_mesh {
+    g2p::Dims d;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    g2p::Constants k;
+    // geometry and materials (device)
+    double *xn = nullptr, *yn = nullptr, *zn = nullptr;
+    double *dxa = nullptr, *dya = nullptr, *dza = nullptr;    // dual lengths (generateStiff.cpp:250-267)
+    double *epsn = nullptr, *sign = nullptr;
+    int32_t *mark_node = nullptr, *mark_edge = nullptr;
+    int64_t num_cdt = 0;
+    int32_t *mark_port = nullptr;
+    uint8_t *cdt_return = nullptr;
+    // host copies of small inputs
+    std::vector<double> h_xn, h_yn, h_zn, h_epsn, h_sign;
+    std::vector<int32_t> h_mark_port;
+    int32_t num_ports = 0;
+    std::vector<int32_t> port_side_ptr;
+    std::vector<int64_t> side_edge_ptr, side_edges;
+    std::vector<double> side_area;
+    std::vector<int32_t> side_dir;
+    double freq_start = 0, freq_end = 0, freq_unit = 1;
+    int32_t nfreq = 1, freq_scale = 1;
+    // index maps
+    bool maps_done = false;
+    uint8_t *pec_edge = nullptr, *pec_node = nullptr;
+    int32_t *map_edge = nullptr;
+    int64_t bden = 0;
+    // stiffness
+    bool stiff_done = false;
+    g2p::Csr<double> S;
+    // V0 bases and Laplacians
+    bool v0_done = false;
+    g2p::V0Basis v0d, v0c;
+    g2p::Csr<double> Ad, Ac;
+    // scratch for scans
+    int64_t *scan_work = nullptr;
+    int64_t scan_work_n = 0;
+};

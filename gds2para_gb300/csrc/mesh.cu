@@ -1,0 +1,521 @@
+// fdtdMesh upload, PEC index maps (a2-a4) and the curl-curl stiffness S (a7-a9).
+//
+// Index maps restate setMapEdge/findBoundNodeEdge (fdtd.hpp:1444-1529) and
+// the LOWER_BOUNDARY_PEC sets (mesh.cpp:963-987) as one flag pass plus an
+// exclusive scan.  S restates generateStiff (generateStiff.cpp:6-565): the
+// reference forms face-by-edge matrices Se (curl, +-1/h) and Sh (dual
+// lengths over dual areas) and multiplies S = Sh*Se^T/mu with MKL, dropping
+// PEC rows/columns.  Here each output row is generated directly from the
+// (at most four) faces that contain its edge, visited in increasing face
+// number so the sums run in the same order as the sparse product; at most 13
+// distinct columns per row are accumulated in registers and sorted.
+#include <cstdarg>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "internal.h"
+#include "primitives.cuh"
+
+namespace g2p {
+
+static thread_local std::string g_err;
+
+void set_last_error(cudaError_t e, const char *what, const char *file, int line) {
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    g_err = buf;
+}
+
+void set_last_message(const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+}
+
+const char *last_error() { return g_err.c_str(); }
+
+g2p_status ensure_scan_work(g2p_mesh *m, int64_t n) {
+    int64_t need = scan_work_size(n) + 16;
+    if (need <= m->scan_work_n) return G2P_OK;
+    dfree(m->scan_work, m->stream);
+    G2P_TRY(dalloc(&m->scan_work, need, m->stream));
+    m->scan_work_n = need;
+    return G2P_OK;
+}
+
+// ------------------------------------------------------------------ upload
+__global__ void k_narrow(const int64_t *__restrict__ in, int32_t *__restrict__ out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (int32_t)in[i];
+}
+
+// Conductor ids must lie in [0, num_cdt]; flag[0] is set otherwise.
+__global__ void k_check_marks(const int32_t *a, int64_t n, int64_t ncdt, int *flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (a[i] < 0 || a[i] > ncdt) atomicExch(flag, 1);
+}
+
+// Dual lengths dxa/dya/dza (generateStiff.cpp:250-267).
+__global__ void k_dual_lengths(const double *c, int64_t N, double *d) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= N; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i == 0) d[0] = c[1] - c[0];
+        else if (i == N) d[N] = c[N] - c[N - 1];
+        else d[i] = (c[i + 1] - c[i - 1]) / 2;
+    }
+}
+
+}  // namespace g2p
+
+using namespace g2p;
+
+extern "C" const char *g2p_last_error(void) { return g2p::last_error(); }
+extern "C" const char *g2p_version(void) { return "gds2para_gb300 0.1 (sm_103a)"; }
+
+extern "C" g2p_status g2p_mesh_create(const g2p_mesh_desc *in, g2p_mesh **out) {
+    if (!in || !out) { set_last_message("null argument"); return G2P_ERR_INVALID; }
+    *out = nullptr;
+    if (in->nx < 3 || in->ny < 3 || in->nz < 3) { set_last_message("grid must have at least 3 nodes per axis"); return G2P_ERR_INVALID; }
+    if (!in->xn || !in->yn || !in->zn || !in->stack_epsn || !in->stack_sign || !in->mark_node || !in->mark_edge) {
+        set_last_message("missing mesh array"); return G2P_ERR_INVALID;
+    }
+    if (in->num_cdt < 1 || !in->mark_port || !in->cdt_return) { set_last_message("mesh has no conductors"); return G2P_ERR_INVALID; }
+    if (in->num_ports < 0 || (in->num_ports > 0 && (!in->port_side_ptr || !in->side_edge_ptr || !in->side_edges || !in->side_area || !in->side_dir))) {
+        set_last_message("missing port arrays"); return G2P_ERR_INVALID;
+    }
+    if (in->nfreq < 1) { set_last_message("nfreq must be >= 1"); return G2P_ERR_INVALID; }
+    g2p_mesh *m = new g2p_mesh();
+    m->d.init(in->nx, in->ny, in->nz);
+    if (m->d.N_edge >= (int64_t)INT32_MAX || m->d.N_node >= (int64_t)INT32_MAX) {
+        delete m; set_last_message("grid exceeds 2^31 edges"); return G2P_ERR_UNSUPPORTED;
+    }
+    cudaGetDevice(&m->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { set_last_error(e, "cudaStreamCreate", __FILE__, __LINE__); delete m; return G2P_ERR_CUDA; }
+    m->k.mu = G2P_MU;
+    m->k.eps0 = G2P_EPSILON0;
+    const Dims &d = m->d;
+    cudaStream_t s = m->stream;
+    m->h_xn.assign(in->xn, in->xn + d.nx);
+    m->h_yn.assign(in->yn, in->yn + d.ny);
+    m->h_zn.assign(in->zn, in->zn + d.nz);
+    m->h_epsn.assign(in->stack_epsn, in->stack_epsn + d.nz);
+    m->h_sign.assign(in->stack_sign, in->stack_sign + d.nz);
+    m->num_cdt = in->num_cdt;
+    m->h_mark_port.assign(in->mark_port, in->mark_port + in->num_cdt);
+    m->num_ports = in->num_ports;
+    if (in->num_ports > 0) {
+        m->port_side_ptr.assign(in->port_side_ptr, in->port_side_ptr + in->num_ports + 1);
+        int64_t ns = m->port_side_ptr.back();
+        m->side_edge_ptr.assign(in->side_edge_ptr, in->side_edge_ptr + ns + 1);
+        m->side_edges.assign(in->side_edges, in->side_edges + m->side_edge_ptr.back());
+        m->side_area.assign(in->side_area, in->side_area + ns);
+        m->side_dir.assign(in->side_dir, in->side_dir + ns);
+        for (int64_t e2 : m->side_edges)
+            if (e2 < 0 || e2 >= d.N_edge) { set_last_message("port edge out of range"); g2p_mesh_destroy(m); return G2P_ERR_INVALID; }
+        for (int p = 0; p < in->num_ports; p++)
+            if (m->port_side_ptr[p + 1] <= m->port_side_ptr[p]) { set_last_message("port %d has no side", p); g2p_mesh_destroy(m); return G2P_ERR_INVALID; }
+    }
+    m->freq_start = in->freq_start; m->freq_end = in->freq_end; m->freq_unit = in->freq_unit;
+    m->nfreq = in->nfreq; m->freq_scale = in->freq_scale;
+    g2p_status st = G2P_OK;
+#define CK(x) do { st = (x); if (st != G2P_OK) { g2p_mesh_destroy(m); return st; } } while (0)
+    CK(dalloc(&m->xn, d.nx, s)); CK(dalloc(&m->yn, d.ny, s)); CK(dalloc(&m->zn, d.nz, s));
+    CK(dalloc(&m->dxa, d.nx, s)); CK(dalloc(&m->dya, d.ny, s)); CK(dalloc(&m->dza, d.nz, s));
+    CK(dalloc(&m->epsn, d.nz, s)); CK(dalloc(&m->sign, d.nz, s));
+    CK(dalloc(&m->mark_node, d.N_node, s)); CK(dalloc(&m->mark_edge, d.N_edge, s));
+    CK(dalloc(&m->mark_port, in->num_cdt, s)); CK(dalloc(&m->cdt_return, in->num_cdt, s));
+    int64_t *tmp = nullptr;
+    CK(dalloc(&tmp, d.N_edge > d.N_node ? d.N_edge : d.N_node, s));
+#define CP(dst, src, n) do { cudaError_t _e = cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s); \
+        if (_e != cudaSuccess) { set_last_error(_e, "H2D copy", __FILE__, __LINE__); dfree(tmp, s); g2p_mesh_destroy(m); return G2P_ERR_CUDA; } } while (0)
+    CP(m->xn, in->xn, sizeof(double) * d.nx);
+    CP(m->yn, in->yn, sizeof(double) * d.ny);
+    CP(m->zn, in->zn, sizeof(double) * d.nz);
+    CP(m->epsn, in->stack_epsn, sizeof(double) * d.nz);
+    CP(m->sign, in->stack_sign, sizeof(double) * d.nz);
+    CP(m->mark_port, in->mark_port, sizeof(int32_t) * in->num_cdt);
+    CP(m->cdt_return, in->cdt_return, in->num_cdt);
+    CP(tmp, in->mark_node, sizeof(int64_t) * d.N_node);
+    k_narrow<<<grid_for(d.N_node), kThreads, 0, s>>>(tmp, m->mark_node, d.N_node);
+    CP(tmp, in->mark_edge, sizeof(int64_t) * d.N_edge);
+    k_narrow<<<grid_for(d.N_edge), kThreads, 0, s>>>(tmp, m->mark_edge, d.N_edge);
+    int *flag = nullptr;
+    CK(dalloc(&flag, 1, s));
+    cudaMemsetAsync(flag, 0, sizeof(int), s);
+    k_check_marks<<<grid_for(d.N_node), kThreads, 0, s>>>(m->mark_node, d.N_node, in->num_cdt, flag);
+    k_check_marks<<<grid_for(d.N_edge), kThreads, 0, s>>>(m->mark_edge, d.N_edge, in->num_cdt, flag);
+    int hflag = 0;
+    cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    dfree(flag, s);
+    if (hflag) { dfree(tmp, s); g2p_mesh_destroy(m); set_last_message("mark_node/mark_edge hold ids outside [0, num_cdt]"); return G2P_ERR_INVALID; }
+    k_dual_lengths<<<1, 256, 0, s>>>(m->xn, d.Nx, m->dxa);
+    k_dual_lengths<<<1, 256, 0, s>>>(m->yn, d.Ny, m->dya);
+    k_dual_lengths<<<1, 256, 0, s>>>(m->zn, d.Nz, m->dza);
+    dfree(tmp, s);
+#undef CP
+#undef CK
+    cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) { set_last_error(le, "mesh upload", __FILE__, __LINE__); g2p_mesh_destroy(m); return G2P_ERR_CUDA; }
+    *out = m;
+    return G2P_OK;
+}
+
+extern "C" g2p_status g2p_mesh_destroy(g2p_mesh *m) {
+    if (!m) return G2P_OK;
+    cudaStream_t s = m->stream;
+    dfree(m->xn, s); dfree(m->yn, s); dfree(m->zn, s);
+    dfree(m->dxa, s); dfree(m->dya, s); dfree(m->dza, s);
+    dfree(m->epsn, s); dfree(m->sign, s);
+    dfree(m->mark_node, s); dfree(m->mark_edge, s); dfree(m->mark_port, s); dfree(m->cdt_return, s);
+    dfree(m->pec_edge, s); dfree(m->pec_node, s); dfree(m->map_edge, s);
+    m->S.release(s);
+    m->v0d.release(s); m->v0c.release(s);
+    m->Ad.release(s); m->Ac.release(s);
+    dfree(m->scan_work, s);
+    if (s) { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
+    delete m;
+    return G2P_OK;
+}
+
+extern "C" g2p_status g2p_mesh_sizes(const g2p_mesh *m, g2p_sizes *out) {
+    if (!m || !out) return G2P_ERR_INVALID;
+    memset(out, 0, sizeof(*out));
+    out->bden = m->bden;
+    out->leng_S = m->S.nnz;
+    out->leng_v0d = m->v0d.ncol; out->leng_v0c = m->v0c.ncol;
+    out->nnz_v0d = m->v0d.nnz; out->nnz_v0c = m->v0c.nnz;
+    out->nnz_ad = m->Ad.nnz; out->nnz_ac = m->Ac.nnz;
+    return G2P_OK;
+}
+
+// ---------------------------------------------------------------- index maps
+namespace g2p {
+
+// lbde = whole z = 0 plane; ubde = top-plane conductor edges of return
+// conductors (after colouring markEdge holds the conductor of both ends).
+__global__ void k_pec_flags(Dims d, const int32_t *__restrict__ mark_edge, const int32_t *__restrict__ mark_node,
+                            const uint8_t *__restrict__ cdt_return, uint8_t *__restrict__ pec_edge,
+                            uint8_t *__restrict__ pec_node) {
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < d.N_edge; e += stride) {
+        uint8_t f = 0;
+        if (e < d.Ns) f = 1;
+        else if (e >= d.N_edge - d.Ns) {
+            int32_t c = mark_edge[e];
+            f = (c != 0 && cdt_return[c - 1]) ? 1 : 0;
+        }
+        pec_edge[e] = f;
+    }
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < d.N_node; n += stride) {
+        uint8_t f = 0;
+        if (n < d.N_node_s) f = 1;
+        else if (n >= d.N_node - d.N_node_s) {
+            int32_t c = mark_node[n];
+            f = (c != 0 && cdt_return[c - 1]) ? 1 : 0;
+        }
+        pec_node[n] = f;
+    }
+}
+
+__global__ void k_finish_map(int64_t n, const uint8_t *__restrict__ pec, int32_t *__restrict__ map) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        map[e] = pec[e] ? -1 : (int32_t)(e - map[e]);
+}
+
+}  // namespace g2p
+
+g2p_status g2p_run_index_maps(g2p_mesh *m) {
+    if (m->maps_done) return G2P_OK;
+    const Dims &d = m->d;
+    cudaStream_t s = m->stream;
+    G2P_TRY(dalloc(&m->pec_edge, d.N_edge, s));
+    G2P_TRY(dalloc(&m->pec_node, d.N_node, s));
+    G2P_TRY(dalloc(&m->map_edge, d.N_edge, s));
+    G2P_TRY(ensure_scan_work(m, d.N_edge));
+    k_pec_flags<<<grid_for(d.N_edge), kThreads, 0, s>>>(d, m->mark_edge, m->mark_node, m->cdt_return, m->pec_edge,
+                                                         m->pec_node);
+    const uint8_t *pe = m->pec_edge;
+    auto op = [pe] __device__(int64_t i) -> int64_t { return pe[i]; };
+    G2P_TRY(exclusive_scan(op, d.N_edge, m->map_edge, m->scan_work, s));
+    k_finish_map<<<grid_for(d.N_edge), kThreads, 0, s>>>(d.N_edge, m->pec_edge, m->map_edge);
+    G2P_CUDA(cudaMemcpyAsync(&m->bden, m->scan_work + scan_total_index(d.N_edge), sizeof(int64_t),
+                             cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    m->maps_done = true;
+    return G2P_OK;
+}
+
+__global__ void k_widen_map(const int32_t *in, int64_t *out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = in[i];
+}
+
+extern "C" g2p_status g2p_index_maps(g2p_mesh *m, int64_t *bden, int64_t *map_edge) {
+    if (!m) return G2P_ERR_INVALID;
+    G2P_TRY(g2p_run_index_maps(m));
+    if (bden) *bden = m->bden;
+    if (map_edge) {
+        int64_t *tmp;
+        G2P_TRY(dalloc(&tmp, m->d.N_edge, m->stream));
+        k_widen_map<<<grid_for(m->d.N_edge), kThreads, 0, m->stream>>>(m->map_edge, tmp, m->d.N_edge);
+        G2P_CUDA(cudaMemcpyAsync(map_edge, tmp, sizeof(int64_t) * m->d.N_edge, cudaMemcpyDeviceToHost, m->stream));
+        dfree(tmp, m->stream);
+        G2P_CUDA(cudaStreamSynchronize(m->stream));
+    }
+    return G2P_OK;
+}
+
+// ----------------------------------------------------------------- stiffness
+namespace g2p {
+
+struct FaceEnt {
+    int64_t e[4];
+    double se[4], sh[4];
+};
+
+struct Geo {
+    Dims d;
+    const double *xn, *yn, *zn, *dxa, *dya, *dza;
+};
+
+// Face numbering of generateStiff: per (z, x, y) cell below the top layer
+// {xy-bottom, yz, xz}; top layer cells {xy-bottom, yz, xz, xy-top}; then the
+// x = Nx yz plane; then the y = Ny xz plane (generateStiff.cpp:33-245).
+__device__ __forceinline__ int64_t fid_cell(const Dims &d, int64_t cz, int64_t cx, int64_t cy, int k) {
+    if (cz < d.Nz - 1) return 3 * (cz * d.Nx * d.Ny + cx * d.Ny + cy) + k;
+    return 3 * (d.Nz - 1) * d.Nx * d.Ny + 4 * (cx * d.Ny + cy) + k;
+}
+__device__ __forceinline__ int64_t fid_xy(const Dims &d, int64_t p, int64_t cx, int64_t cy) {
+    return p < d.Nz ? fid_cell(d, p, cx, cy, 0) : fid_cell(d, d.Nz - 1, cx, cy, 3);
+}
+__device__ __forceinline__ int64_t fid_yz(const Dims &d, int64_t i, int64_t cz, int64_t cy) {
+    return i < d.Nx ? fid_cell(d, cz, i, cy, 1) : d.Nx * d.Ny * (3 * d.Nz + 1) + cz * d.Ny + cy;
+}
+__device__ __forceinline__ int64_t fid_xz(const Dims &d, int64_t j, int64_t cz, int64_t cx) {
+    return j < d.Ny ? fid_cell(d, cz, cx, j, 2) : d.Nx * d.Ny * (3 * d.Nz + 1) + d.Nz * d.Ny + cz * d.Nx + cx;
+}
+
+// The four (edge, Se, Sh) entries of each face kind, with the reference's
+// expressions (generateStiff.cpp:33-484; the top xy face keeps dza[Nz-1]).
+__device__ __forceinline__ void face_xy(const Geo &g, int64_t p, int64_t cx, int64_t cy, FaceEnt &f) {
+    const Dims &d = g.d;
+    double dx = g.xn[cx + 1] - g.xn[cx], dy = g.yn[cy + 1] - g.yn[cy];
+    double q = g.dza[p < d.Nz ? p : d.Nz - 1];
+    f.e[0] = d.ye(p, cx, cy);     f.se[0] = -1 / dx; f.sh[0] = -q / (g.dxa[cx] * q);
+    f.e[1] = d.ye(p, cx + 1, cy); f.se[1] = 1 / dx;  f.sh[1] = q / (g.dxa[cx + 1] * q);
+    f.e[2] = d.xe(p, cx, cy);     f.se[2] = 1 / dy;  f.sh[2] = q / (q * g.dya[cy]);
+    f.e[3] = d.xe(p, cx, cy + 1); f.se[3] = -1 / dy; f.sh[3] = -q / (q * g.dya[cy + 1]);
+}
+__device__ __forceinline__ void face_yz(const Geo &g, int64_t i, int64_t cz, int64_t cy, FaceEnt &f) {
+    const Dims &d = g.d;
+    double dy = g.yn[cy + 1] - g.yn[cy], dz = g.zn[cz + 1] - g.zn[cz];
+    double a = g.dxa[i];
+    f.e[0] = d.ye(cz, i, cy);     f.se[0] = 1 / dz;  f.sh[0] = a / (a * g.dza[cz]);
+    f.e[1] = d.ze(cz, i, cy);     f.se[1] = -1 / dy; f.sh[1] = -a / (a * g.dya[cy]);
+    f.e[2] = d.ze(cz, i, cy + 1); f.se[2] = 1 / dy;  f.sh[2] = a / (a * g.dya[cy + 1]);
+    f.e[3] = d.ye(cz + 1, i, cy); f.se[3] = -1 / dz; f.sh[3] = -a / (a * g.dza[cz + 1]);
+}
+__device__ __forceinline__ void face_xz(const Geo &g, int64_t j, int64_t cz, int64_t cx, FaceEnt &f) {
+    const Dims &d = g.d;
+    double dx = g.xn[cx + 1] - g.xn[cx], dz = g.zn[cz + 1] - g.zn[cz];
+    double b = g.dya[j];
+    f.e[0] = d.xe(cz, cx, j);     f.se[0] = -1 / dz; f.sh[0] = -b / (g.dza[cz] * b);
+    f.e[1] = d.ze(cz, cx, j);     f.se[1] = 1 / dx;  f.sh[1] = b / (g.dxa[cx] * b);
+    f.e[2] = d.ze(cz, cx + 1, j); f.se[2] = -1 / dx; f.sh[2] = -b / (b * g.dxa[cx + 1]);
+    f.e[3] = d.xe(cz + 1, cx, j); f.se[3] = 1 / dz;  f.sh[3] = b / (b * g.dza[cz + 1]);
+}
+
+// Faces containing edge e: kind (0 xy, 1 yz, 2 xz) and (a, b, c) arguments.
+struct FaceRef {
+    int64_t id;
+    int kind;
+    int64_t a, b, c;
+};
+
+__device__ __forceinline__ int edge_faces(const Dims &d, int64_t e, FaceRef *fr) {
+    int64_t n1, n2, z, x, y;
+    int kind = d.edge_nodes(e, n1, n2, z, x, y);
+    int nf = 0;
+    if (kind == 0) {  // y-edge: plane z, node x, cell y
+        if (x >= 1) fr[nf++] = {fid_xy(d, z, x - 1, y), 0, z, x - 1, y};
+        if (x < d.Nx) fr[nf++] = {fid_xy(d, z, x, y), 0, z, x, y};
+        if (z >= 1) fr[nf++] = {fid_yz(d, x, z - 1, y), 1, x, z - 1, y};
+        if (z < d.Nz) fr[nf++] = {fid_yz(d, x, z, y), 1, x, z, y};
+    } else if (kind == 1) {  // x-edge: plane z, cell x, node y
+        if (y >= 1) fr[nf++] = {fid_xy(d, z, x, y - 1), 0, z, x, y - 1};
+        if (y < d.Ny) fr[nf++] = {fid_xy(d, z, x, y), 0, z, x, y};
+        if (z >= 1) fr[nf++] = {fid_xz(d, y, z - 1, x), 2, y, z - 1, x};
+        if (z < d.Nz) fr[nf++] = {fid_xz(d, y, z, x), 2, y, z, x};
+    } else {  // z-edge: layer z, node (x, y)
+        if (y >= 1) fr[nf++] = {fid_yz(d, x, z, y - 1), 1, x, z, y - 1};
+        if (y < d.Ny) fr[nf++] = {fid_yz(d, x, z, y), 1, x, z, y};
+        if (x >= 1) fr[nf++] = {fid_xz(d, y, z, x - 1), 2, y, z, x - 1};
+        if (x < d.Nx) fr[nf++] = {fid_xz(d, y, z, x), 2, y, z, x};
+    }
+    // increasing face number (insertion sort of <= 4)
+    for (int i = 1; i < nf; i++) {
+        FaceRef t = fr[i];
+        int j = i - 1;
+        while (j >= 0 && fr[j].id > t.id) { fr[j + 1] = fr[j]; j--; }
+        fr[j + 1] = t;
+    }
+    return nf;
+}
+
+constexpr int kMaxS = 16;
+
+// Accumulates the row of edge e in (cols, vals), sorted by column; returns the
+// number of columns (PEC columns included).
+__device__ __forceinline__ int stiff_row(const Geo &g, int64_t e, int64_t *cols, double *vals) {
+    FaceRef fr[4];
+    int nf = edge_faces(g.d, e, fr);
+    int nc = 0;
+    for (int t = 0; t < nf; t++) {
+        FaceEnt f;
+        if (fr[t].kind == 0) face_xy(g, fr[t].a, fr[t].b, fr[t].c, f);
+        else if (fr[t].kind == 1) face_yz(g, fr[t].a, fr[t].b, fr[t].c, f);
+        else face_xz(g, fr[t].a, fr[t].b, fr[t].c, f);
+        double sh = 0.0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) if (f.e[k] == e) sh = f.sh[k];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            int q = 0;
+            while (q < nc && cols[q] != f.e[k]) q++;
+            if (q == nc) { cols[nc] = f.e[k]; vals[nc] = 0.0; nc++; }
+            vals[q] += sh * f.se[k];
+        }
+    }
+    for (int i = 1; i < nc; i++) {
+        int64_t c = cols[i]; double v = vals[i];
+        int j = i - 1;
+        while (j >= 0 && cols[j] > c) { cols[j + 1] = cols[j]; vals[j + 1] = vals[j]; j--; }
+        cols[j + 1] = c; vals[j + 1] = v;
+    }
+    return nc;
+}
+
+__global__ void __launch_bounds__(256) k_stiff_count(Geo g, const uint8_t *__restrict__ pec, const int32_t *__restrict__ map,
+                                                     int64_t *__restrict__ rowlen) {
+    const Dims &d = g.d;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < d.N_edge; e += (int64_t)gridDim.x * blockDim.x) {
+        if (pec[e]) continue;
+        int64_t cols[kMaxS];
+        double vals[kMaxS];
+        int nc = stiff_row(g, e, cols, vals);
+        int cnt = 0;
+        for (int q = 0; q < nc; q++) cnt += pec[cols[q]] ? 0 : 1;
+        rowlen[map[e]] = cnt;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_stiff_fill(Geo g, const uint8_t *__restrict__ pec, const int32_t *__restrict__ map,
+                                                    const int64_t *__restrict__ rowptr, int32_t *__restrict__ col,
+                                                    double *__restrict__ val, double mu) {
+    const Dims &d = g.d;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < d.N_edge; e += (int64_t)gridDim.x * blockDim.x) {
+        if (pec[e]) continue;
+        int64_t cols[kMaxS];
+        double vals[kMaxS];
+        int nc = stiff_row(g, e, cols, vals);
+        int64_t o = rowptr[map[e]];
+        for (int q = 0; q < nc; q++) {
+            if (pec[cols[q]]) continue;
+            col[o] = map[cols[q]];
+            val[o] = vals[q] / mu;
+            o++;
+        }
+    }
+}
+
+__global__ void k_csr_rows_i64(const int64_t *ptr, int64_t n, int64_t *rows) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t k = ptr[i]; k < ptr[i + 1]; k++) rows[k] = i;
+}
+
+__global__ void k_i32_to_i64(const int32_t *in, int64_t *out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = in[i];
+}
+
+}  // namespace g2p
+
+g2p_status g2p_build_rowptr(g2p_mesh *m, int64_t *rowlen, int64_t n, int64_t **ptr_out, int64_t *nnz_out) {
+    // ptr = exclusive scan of rowlen with ptr[n] = total
+    cudaStream_t s = m->stream;
+    G2P_TRY(ensure_scan_work(m, n + 1));
+    int64_t *ptr;
+    G2P_TRY(dalloc(&ptr, n + 1, s));
+    const int64_t *rl = rowlen;
+    auto op = [rl, n] __device__(int64_t i) -> int64_t { return i < n ? rl[i] : 0; };
+    G2P_TRY(exclusive_scan(op, n + 1, ptr, m->scan_work, s));
+    G2P_CUDA(cudaMemcpyAsync(nnz_out, ptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    *ptr_out = ptr;
+    return G2P_OK;
+}
+
+g2p_status g2p_run_stiff(g2p_mesh *m) {
+    if (m->stiff_done) return G2P_OK;
+    G2P_TRY(g2p_run_index_maps(m));
+    const Dims &d = m->d;
+    cudaStream_t s = m->stream;
+    Geo g{d, m->xn, m->yn, m->zn, m->dxa, m->dya, m->dza};
+    int64_t n = d.N_edge - m->bden;
+    int64_t *rowlen;
+    G2P_TRY(dalloc(&rowlen, n, s));
+    k_stiff_count<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, rowlen);
+    int64_t nnz = 0;
+    g2p_status st = g2p_build_rowptr(m, rowlen, n, &m->S.ptr, &nnz);
+    dfree(rowlen, s);
+    if (st != G2P_OK) return st;
+    m->S.n = m->S.m = n;
+    m->S.nnz = nnz;
+    G2P_TRY(dalloc(&m->S.col, nnz, s));
+    G2P_TRY(dalloc(&m->S.val, nnz, s));
+    k_stiff_fill<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, m->S.ptr, m->S.col,
+                                                                     m->S.val, m->k.mu);
+    G2P_CUDA(cudaGetLastError());
+    G2P_CUDA(cudaStreamSynchronize(s));
+    m->stiff_done = true;
+    return G2P_OK;
+}
+
+extern "C" g2p_status g2p_generate_stiff(g2p_mesh *m, int64_t *leng_S) {
+    if (!m) return G2P_ERR_INVALID;
+    G2P_TRY(g2p_run_stiff(m));
+    if (leng_S) *leng_S = m->S.nnz;
+    return G2P_OK;
+}
+
+// COO export of a device CSR (rows, int64 cols, values) to host buffers.
+g2p_status g2p_export_csr(g2p_mesh *m, const Csr<double> &A, int64_t *row, int64_t *col, double *val) {
+    cudaStream_t s = m->stream;
+    int64_t *tmp;
+    G2P_TRY(dalloc(&tmp, A.nnz, s));
+    if (row) {
+        k_csr_rows_i64<<<grid_for(A.n), kThreads, 0, s>>>(A.ptr, A.n, tmp);
+        G2P_CUDA(cudaMemcpyAsync(row, tmp, sizeof(int64_t) * A.nnz, cudaMemcpyDeviceToHost, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
+    }
+    if (col) {
+        k_i32_to_i64<<<grid_for(A.nnz), kThreads, 0, s>>>(A.col, tmp, A.nnz);
+        G2P_CUDA(cudaMemcpyAsync(col, tmp, sizeof(int64_t) * A.nnz, cudaMemcpyDeviceToHost, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
+    }
+    if (val) G2P_CUDA(cudaMemcpyAsync(val, A.val, sizeof(double) * A.nnz, cudaMemcpyDeviceToHost, s));
+    dfree(tmp, s);
+    G2P_CUDA(cudaStreamSynchronize(s));
+    return G2P_OK;
+}
+
+extern "C" g2p_status g2p_export_stiff(g2p_mesh *m, int64_t *row, int64_t *col, double *val) {
+    if (!m) return G2P_ERR_INVALID;
+    if (!m->stiff_done) { set_last_message("g2p_generate_stiff has not run"); return G2P_ERR_STATE; }
+    return g2p_export_csr(m, m->S, row, col, val);
+}

@@ -1,0 +1,318 @@
+// hypreSolve replacement on the device (hypreSolve.cpp:9-283, hypreSolver.h:7-14).
+//
+// Two methods share one AMG code path:
+//   FP64 ("plain"): FGMRES(restart) on A with the FP64 hierarchy, stopping at
+//     ||b - A x|| <= rtol ||b|| per right-hand side, as HYPRE's FlexGMRES does.
+//   mixed: iterative refinement in FP64 (true residual b - A x with the FP64
+//     operator, same stopping test) around an FP32 FGMRES/AMG solve of the
+//     diagonally equilibrated system S A S d^ = S r.
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "primitives.cuh"
+#include "solver.h"
+
+namespace g2p {
+
+__global__ void k_scale_vec(const int64_t *ptr, const int32_t *col, const double *val, int64_t n, double *scale) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double d = 0;
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) if (col[q] == i) { d = val[q]; break; }
+        scale[i] = d != 0.0 ? 1.0 / sqrt(fabs(d)) : 1.0;
+    }
+}
+
+__global__ void k_scale_mat(const int64_t *ptr, const int32_t *col, const double *val, int64_t n, const double *scale,
+                            double *out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) out[q] = scale[i] * val[q] * scale[col[q]];
+}
+
+// rf = float(scale .* r)
+__global__ void k_to_scaled_f(int64_t nk, int k, const double *scale, const double *r, float *rf) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x)
+        rf[t] = (float)(scale[t / k] * r[t]);
+}
+// x += scale .* double(df)
+__global__ void k_add_scaled(int64_t nk, int k, const double *scale, const float *df, double *x) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x)
+        x[t] += scale[t / k] * (double)df[t];
+}
+
+__global__ void k_coo_count(const int64_t *rows, int64_t nnz, int64_t n, int64_t *cnt, int *bad) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = rows[q];
+        if (r < 0 || r >= n || (q > 0 && rows[q - 1] > r)) { atomicExch(bad, 1); continue; }
+        atomicAdd((unsigned long long *)&cnt[r], 1ull);
+    }
+}
+__global__ void k_coo_cols(const int64_t *cols, int64_t nnz, int64_t n, int32_t *out, int *bad) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c = cols[q];
+        if (c < 0 || c >= n) atomicExch(bad, 1);
+        out[q] = (int32_t)c;
+    }
+}
+
+__global__ void k_colmajor_to_interleaved(const double *in, double *out, int64_t n, int k) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = t / k;
+        out[t] = in[(t - i * k) * n + i];
+    }
+}
+__global__ void k_interleaved_to_colmajor(const double *in, double *out, int64_t n, int k) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = t / k;
+        out[(t - i * k) * n + i] = in[t];
+    }
+}
+
+static double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace g2p
+
+using namespace g2p;
+
+extern "C" void g2p_default_params(g2p_solver_params *p, int32_t parity_mode) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->precision = G2P_PREC_FP64;
+    if (parity_mode) {
+        p->restart = 10; p->maxit = 100; p->rtol = 1e-4;     // hypreSolver.h:7-11, hypreSolve.cpp:211
+    } else {
+        p->restart = 30; p->maxit = 400; p->rtol = 1e-10;
+    }
+    p->smoother_degree = 2;
+    p->coarse_size = 256;
+    p->strength = 0.08;
+    p->max_levels = 20;
+    p->inner_rtol = 1e-4;
+    p->inner_maxit = 40;
+    p->batch = 1;
+    p->use_graphs = 0;
+}
+
+static SolverConfig cfg_from(const g2p_solver_params *p) {
+    SolverConfig c;
+    c.restart = p->restart > 0 ? p->restart : 30;
+    if (c.restart > 64) c.restart = 64;
+    c.maxit = p->maxit > 0 ? p->maxit : 300;
+    c.rtol = p->rtol > 0 ? p->rtol : 1e-10;
+    c.degree = p->smoother_degree > 0 ? p->smoother_degree : 2;
+    c.coarse_size = p->coarse_size > 0 ? p->coarse_size : 256;
+    c.strength = p->strength > 0 ? p->strength : 0.08;
+    c.max_levels = p->max_levels > 0 ? p->max_levels : 20;
+    return c;
+}
+
+// Builds a solver around a device CSR (copied).  Shared by the C ABI and
+// the paraGenerator pipeline.
+g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cudaStream_t stream, g2p_solver **out) {
+    auto t0 = std::chrono::steady_clock::now();
+    g2p_solver *S = new g2p_solver();
+    S->stream = stream;
+    S->cfg = cfg_from(p);
+    S->precision = p->precision;
+    S->inner_rtol = p->inner_rtol > 0 ? p->inner_rtol : 1e-4;
+    S->inner_maxit = p->inner_maxit > 0 ? p->inner_maxit : 40;
+    cudaStream_t s = stream;
+    auto fail = [&](g2p_status st) { g2p_solver_destroy(S); return st; };
+    g2p_status st;
+    S->A.n = S->A.m = A.n; S->A.nnz = A.nnz;
+    if ((st = dalloc(&S->A.ptr, A.n + 1, s)) != G2P_OK) return fail(st);
+    if ((st = dalloc(&S->A.col, A.nnz, s)) != G2P_OK) return fail(st);
+    if ((st = dalloc(&S->A.val, A.nnz, s)) != G2P_OK) return fail(st);
+    cudaMemcpyAsync(S->A.ptr, A.ptr, sizeof(int64_t) * (A.n + 1), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(S->A.col, A.col, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(S->A.val, A.val, sizeof(double) * A.nnz, cudaMemcpyDeviceToDevice, s);
+    if ((st = find_long_rows(S->A, &S->long_rows, &S->nlong, s)) != G2P_OK) return fail(st);
+    if (S->precision == G2P_PREC_MIXED) {
+        if ((st = dalloc(&S->scale, A.n, s)) != G2P_OK) return fail(st);
+        k_scale_vec<<<grid_for(A.n), kThreads, 0, s>>>(S->A.ptr, S->A.col, S->A.val, A.n, S->scale);
+        Csr<double> As = S->A;   // shares structure; scaled values in a temporary
+        double *sv;
+        if ((st = dalloc(&sv, A.nnz, s)) != G2P_OK) return fail(st);
+        k_scale_mat<<<grid_for(A.n), kThreads, 0, s>>>(S->A.ptr, S->A.col, S->A.val, A.n, S->scale, sv);
+        As.val = sv;
+        st = amg_setup(As, S->cfg, s, nullptr, S->H64);
+        dfree(sv, s);
+        if (st != G2P_OK) return fail(st);
+        if ((st = amg_to_float(S->H64, s, S->H32)) != G2P_OK) return fail(st);
+        S->H64.release(s);
+        S->levels = (int)S->H32.lv.size();
+        S->coarse_rows = S->H32.nc;
+    } else {
+        if ((st = amg_setup(S->A, S->cfg, s, nullptr, S->H64)) != G2P_OK) return fail(st);
+        S->levels = (int)S->H64.lv.size();
+        S->coarse_rows = S->H64.nc;
+    }
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { set_last_error(e, "solver setup", __FILE__, __LINE__); return fail(G2P_ERR_CUDA); }
+    S->setup_ms = ms_since(t0);
+    *out = S;
+    return G2P_OK;
+}
+
+static g2p_status reserve_block(g2p_solver *S, int k) {
+    if (k <= S->kcap) return G2P_OK;
+    cudaStream_t s = S->stream;
+    dfree(S->rb, s); dfree(S->rf, s); dfree(S->df, s);
+    int64_t nk = S->A.n * k;
+    G2P_TRY(dalloc(&S->rb, nk, s));
+    if (S->precision == G2P_PREC_MIXED) {
+        G2P_TRY(dalloc(&S->rf, nk, s));
+        G2P_TRY(dalloc(&S->df, nk, s));
+    }
+    S->kcap = k;
+    return G2P_OK;
+}
+
+// Solve with device right-hand sides b (n x k interleaved); x is zeroed first.
+g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k, g2p_solve_stats *st) {
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = S->stream;
+    int64_t n = S->A.n, nk = n * k;
+    G2P_TRY(reserve_block(S, k));
+    G2P_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * nk, s));
+    SolveReport rep;
+    int refinements = 0, iters = 0;
+    if (S->precision != G2P_PREC_MIXED) {
+        G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep));
+        iters = rep.iterations;
+    } else {
+        // FP64 refinement around FP32 inner solves
+        G2P_TRY(krylov_alloc<double>(S->K64, n, k, 1, s));
+        double *bn = S->K64.bnorm, *rn = S->K64.beta;
+        colnorms<double>(b, n, k, S->K64.partial, bn, s);
+        std::vector<double> hb(k), hr(k);
+        G2P_CUDA(cudaMemcpyAsync(hb.data(), bn, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+        SolverConfig inner = S->cfg;
+        inner.rtol = S->inner_rtol;
+        inner.maxit = S->inner_maxit;
+        inner.reorth = false;
+        const int max_ref = S->cfg.maxit > 0 ? std::max(2, S->cfg.maxit / std::max(1, S->inner_maxit / 2)) : 20;
+        rep.converged = false;
+        for (int ref = 0; ref <= max_ref; ref++) {
+            residual64(S->A, S->long_rows, S->nlong, b, x, S->rb, k, s);
+            colnorms<double>(S->rb, n, k, S->K64.partial, rn, s);
+            G2P_CUDA(cudaMemcpyAsync(hr.data(), rn, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+            G2P_CUDA(cudaStreamSynchronize(s));
+            double worst = 0;
+            for (int r = 0; r < k; r++) worst = std::max(worst, hb[r] > 0 ? hr[r] / hb[r] : 0.0);
+            rep.rel_residual = worst;
+            if (worst <= S->cfg.rtol) { rep.converged = true; break; }
+            if (ref == max_ref) break;
+            k_to_scaled_f<<<grid_for(nk), kThreads, 0, s>>>(nk, k, S->scale, S->rb, S->rf);
+            G2P_CUDA(cudaMemsetAsync(S->df, 0, sizeof(float) * nk, s));
+            SolveReport ir;
+            G2P_TRY(fgmres<float>(S->H32.lv[0].A, S->H32, S->K32, S->rf, S->df, k, inner, nullptr, s, ir));
+            k_add_scaled<<<grid_for(nk), kThreads, 0, s>>>(nk, k, S->scale, S->df, x);
+            iters += ir.iterations;
+            refinements++;
+        }
+    }
+    G2P_CUDA(cudaStreamSynchronize(s));
+    if (st) {
+        st->iterations = iters;
+        st->refinements = refinements;
+        st->rel_residual = rep.rel_residual;
+        st->levels = S->levels;
+        st->converged = rep.converged ? 1 : 0;
+        st->coarse_rows = S->coarse_rows;
+        st->setup_ms = S->setup_ms;
+        st->solve_ms = ms_since(t0);
+    }
+    return rep.converged ? G2P_OK : G2P_ERR_NOT_CONVERGED;
+}
+
+extern "C" g2p_status g2p_solver_create(const int64_t *ARowId, const int64_t *AColId, const double *Aval,
+                                        int64_t leng_A, int64_t n, const g2p_solver_params *p, g2p_solver **out) {
+    if (!ARowId || !AColId || !Aval || !out || n <= 0 || leng_A < 0) { set_last_message("bad solver arguments"); return G2P_ERR_INVALID; }
+    if (n >= INT32_MAX) { set_last_message("matrix too large"); return G2P_ERR_UNSUPPORTED; }
+    g2p_solver_params def;
+    if (!p) { g2p_default_params(&def, 0); p = &def; }
+    cudaStream_t s;
+    G2P_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    // row-sorted COO (hypreSolve's input) -> CSR on the device
+    Csr<double> A;
+    A.n = A.m = n; A.nnz = leng_A;
+    int64_t *rows, *cols, *cnt, *work;
+    int *bad;
+    G2P_TRY(dalloc(&rows, leng_A, s)); G2P_TRY(dalloc(&cols, leng_A, s));
+    G2P_TRY(dalloc(&cnt, n + 1, s)); G2P_TRY(dalloc(&work, scan_work_size(n + 1) + 4, s));
+    G2P_TRY(dalloc(&bad, 1, s));
+    G2P_TRY(dalloc(&A.ptr, n + 1, s)); G2P_TRY(dalloc(&A.col, leng_A, s)); G2P_TRY(dalloc(&A.val, leng_A, s));
+    G2P_CUDA(cudaMemcpyAsync(rows, ARowId, sizeof(int64_t) * leng_A, cudaMemcpyHostToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(cols, AColId, sizeof(int64_t) * leng_A, cudaMemcpyHostToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(A.val, Aval, sizeof(double) * leng_A, cudaMemcpyHostToDevice, s));
+    G2P_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (n + 1), s));
+    G2P_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
+    k_coo_count<<<grid_for(leng_A), kThreads, 0, s>>>(rows, leng_A, n, cnt, bad);
+    k_coo_cols<<<grid_for(leng_A), kThreads, 0, s>>>(cols, leng_A, n, A.col, bad);
+    const int64_t *cp = cnt;
+    auto op = [cp, n] __device__(int64_t i) -> int64_t { return i < n ? cp[i] : 0; };
+    G2P_TRY(exclusive_scan(op, n + 1, A.ptr, work, s));
+    int hbad = 0;
+    G2P_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    dfree(rows, s); dfree(cols, s); dfree(cnt, s); dfree(work, s); dfree(bad, s);
+    if (hbad) {
+        A.release(s);
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+        set_last_message("COO is not row-sorted or has indices outside [0, n)");
+        return G2P_ERR_INVALID;
+    }
+    g2p_status st = g2p_solver_build(A, p, s, out);
+    A.release(s);
+    if (st != G2P_OK) { cudaStreamSynchronize(s); cudaStreamDestroy(s); return st; }
+    (*out)->owns_stream = true;
+    return st;
+}
+
+extern "C" g2p_status g2p_solver_solve(g2p_solver *S, const double *b, double *x, int32_t nrhs, g2p_solve_stats *st) {
+    if (!S || !b || !x || nrhs < 1) { set_last_message("bad solve arguments"); return G2P_ERR_INVALID; }
+    cudaStream_t s = S->stream;
+    int64_t n = S->A.n;
+    double *db, *dx, *tb;
+    G2P_TRY(dalloc(&db, n * nrhs, s)); G2P_TRY(dalloc(&dx, n * nrhs, s)); G2P_TRY(dalloc(&tb, n * nrhs, s));
+    // host column-major <-> device interleaved
+    G2P_CUDA(cudaMemcpyAsync(tb, b, sizeof(double) * n * nrhs, cudaMemcpyHostToDevice, s));
+    k_colmajor_to_interleaved<<<grid_for(n * nrhs), kThreads, 0, s>>>(tb, db, n, nrhs);
+    g2p_status rc = g2p_solver_solve_dev(S, db, dx, nrhs, st);
+    k_interleaved_to_colmajor<<<grid_for(n * nrhs), kThreads, 0, s>>>(dx, tb, n, nrhs);
+    G2P_CUDA(cudaMemcpyAsync(x, tb, sizeof(double) * n * nrhs, cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    dfree(db, s); dfree(dx, s); dfree(tb, s);
+    G2P_CUDA(cudaStreamSynchronize(s));
+    return rc;
+}
+
+extern "C" g2p_status g2p_solver_destroy(g2p_solver *S) {
+    if (!S) return G2P_OK;
+    cudaStream_t s = S->stream;
+    S->A.release(s);
+    dfree(S->long_rows, s); dfree(S->scale, s);
+    S->H64.release(s); S->H32.release(s);
+    S->K64.release(s); S->K32.release(s);
+    dfree(S->xb, s); dfree(S->bb, s); dfree(S->rb, s); dfree(S->rf, s); dfree(S->df, s);
+    dfree(S->scan_work, s);
+    cudaStreamSynchronize(s);
+    if (S->owns_stream) cudaStreamDestroy(s);
+    delete S;
+    return G2P_OK;
+}
+
+extern "C" g2p_status g2p_hypre_solve(const int64_t *ARowId, const int64_t *AColId, const double *Aval, int64_t leng_A,
+                                      const double *bin, int64_t leng_v0, double *solution) {
+    g2p_solver_params p;
+    g2p_default_params(&p, 1);
+    g2p_solver *S = nullptr;
+    G2P_TRY(g2p_solver_create(ARowId, AColId, Aval, leng_A, leng_v0, &p, &S));
+    g2p_status rc = g2p_solver_solve(S, bin, solution, 1, nullptr);
+    g2p_solver_destroy(S);
+    return rc;
+}

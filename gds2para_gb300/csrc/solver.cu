@@ -1,0 +1,988 @@
+// AMG setup and application, multi-RHS sparse kernels, batched FGMRES.
+//
+// Replaces hypreSolve (hypreSolve.cpp:9-283): the reference solves each
+// system with HYPRE FlexGMRES(10) preconditioned by one BoomerAMG V-cycle
+// and rebuilds the hierarchy on every call.  Here the hierarchy is built on
+// the device once per matrix:
+//   * strength graph |a_ij| >= theta sqrt(|a_ii a_jj|) (rows longer than a
+//     level-relative limit -- the lumped conductor potentials of Ad -- stay
+//     singleton aggregates),
+//   * aggregation from a distance-2 maximal independent set computed with
+//     hashed priorities (two max-propagation sweeps per round), neighbours
+//     joining the strongest root, distance-2 nodes joining a neighbour's
+//     aggregate,
+//   * Galerkin coarse operators P^T A P of the piecewise-constant
+//     prolongation by expand / stable radix sort / ordered reduce,
+//   * Chebyshev smoothing on D^-1 A (bounds from the Gershgorin radius),
+//   * an explicit FP64 inverse on the coarsest level.
+// All right-hand sides of a block advance together through FGMRES.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "primitives.cuh"
+#include "solver.h"
+
+namespace g2p {
+
+// ------------------------------------------------------------ sparse kernels
+template <class T>
+__global__ void __launch_bounds__(256) k_spmm(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                                              const T *__restrict__ val, const T *__restrict__ x, T *__restrict__ y,
+                                              int k, const T *__restrict__ b) {
+    int64_t total = n * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = t / k;
+        int r = (int)(t - i * k);
+        int64_t s0 = ptr[i], s1 = ptr[i + 1];
+        if (s1 - s0 > kLongRow) continue;
+        T acc = 0;
+        for (int64_t q = s0; q < s1; q++) acc += val[q] * x[(int64_t)col[q] * k + r];
+        y[t] = b ? b[t] - acc : acc;
+    }
+}
+
+// One block per long row; deterministic tree reduction per right-hand side.
+template <class T>
+__global__ void __launch_bounds__(256) k_spmm_long(const int32_t *__restrict__ rows, const int64_t *__restrict__ ptr,
+                                                   const int32_t *__restrict__ col, const T *__restrict__ val,
+                                                   const T *__restrict__ x, T *__restrict__ y, int k,
+                                                   const T *__restrict__ b) {
+    __shared__ double red[256];
+    int64_t i = rows[blockIdx.x];
+    int64_t s0 = ptr[i], s1 = ptr[i + 1];
+    for (int r = 0; r < k; r++) {
+        double acc = 0;
+        for (int64_t q = s0 + threadIdx.x; q < s1; q += blockDim.x) acc += (double)val[q] * (double)x[(int64_t)col[q] * k + r];
+        red[threadIdx.x] = acc;
+        __syncthreads();
+        for (int o = 128; o > 0; o >>= 1) {
+            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            T v = (T)red[0];
+            y[i * k + r] = b ? b[i * k + r] - v : v;
+        }
+        __syncthreads();
+    }
+}
+
+template <class T>
+void spmm_b(const Csr<T> &A, const int32_t *long_rows, int64_t nlong, const T *x, T *y, int k, const T *b,
+            cudaStream_t s) {
+    k_spmm<T><<<grid_for(A.n * k, 256, 152LL * 48), 256, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y, k, b);
+    if (nlong > 0) k_spmm_long<T><<<(unsigned)nlong, 256, 0, s>>>(long_rows, A.ptr, A.col, A.val, x, y, k, b);
+}
+
+template <class T>
+void spmm(const Csr<T> &A, const int32_t *long_rows, int64_t nlong, const T *x, T *y, int k, cudaStream_t s) {
+    spmm_b<T>(A, long_rows, nlong, x, y, k, nullptr, s);
+}
+template void spmm<double>(const Csr<double> &, const int32_t *, int64_t, const double *, double *, int, cudaStream_t);
+template void spmm<float>(const Csr<float> &, const int32_t *, int64_t, const float *, float *, int, cudaStream_t);
+
+void residual64(const Csr<double> &A, const int32_t *long_rows, int64_t nlong, const double *b, const double *x,
+                double *r, int k, cudaStream_t s) {
+    spmm_b<double>(A, long_rows, nlong, x, r, k, b, s);
+}
+
+__global__ void k_mark_long(int64_t n, const int64_t *ptr, int64_t *flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        flag[i] = (ptr[i + 1] - ptr[i]) > kLongRow ? 1 : 0;
+}
+__global__ void k_list_long(int64_t n, const int64_t *ptr, const int64_t *pos, int32_t *rows) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if ((ptr[i + 1] - ptr[i]) > kLongRow) rows[pos[i]] = (int32_t)i;
+}
+
+template <class T>
+g2p_status find_long_rows_t(const Csr<T> &A, int32_t **rows, int64_t *nlong, cudaStream_t s) {
+    int64_t *pos, *work;
+    int64_t n = A.n;
+    G2P_TRY(dalloc(&pos, n + 1, s));
+    G2P_TRY(dalloc(&work, scan_work_size(n + 1) + 4, s));
+    const int64_t *p = A.ptr;
+    auto op = [p, n] __device__(int64_t i) -> int64_t { return i < n ? ((p[i + 1] - p[i]) > kLongRow ? 1 : 0) : 0; };
+    G2P_TRY(exclusive_scan(op, n + 1, pos, work, s));
+    G2P_CUDA(cudaMemcpyAsync(nlong, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    *rows = nullptr;
+    if (*nlong > 0) {
+        G2P_TRY(dalloc(rows, *nlong, s));
+        k_list_long<<<grid_for(n), kThreads, 0, s>>>(n, A.ptr, pos, *rows);
+    }
+    dfree(pos, s); dfree(work, s);
+    return G2P_OK;
+}
+
+g2p_status find_long_rows(const Csr<double> &A, int32_t **rows, int64_t *nlong, cudaStream_t s) {
+    return find_long_rows_t<double>(A, rows, nlong, s);
+}
+
+// --------------------------------------------------------------- reductions
+// Deterministic per-column sums of squares: block partials, then an ordered
+// final pass.
+constexpr int kRedBlocks = 152 * 4;
+constexpr int64_t kMaxDenseCoarse = 768;
+
+// Block shape (kx, 256 / kx) with kx the power of two >= k: threadIdx.x is
+// the right-hand side, threadIdx.y strides over rows, so every thread keeps
+// one column's partial sum and the block reduces in a fixed order.
+static inline int pow2_at_least(int k) {
+    int p = 1;
+    while (p < k) p <<= 1;
+    return p;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_colsq_partial(const T *x, int64_t n, int k, double *partial) {
+    __shared__ double sm[256];
+    const int r = threadIdx.x, ty = threadIdx.y, ny = blockDim.y;
+    double acc = 0;
+    if (r < k)
+        for (int64_t i = blockIdx.x * (int64_t)ny + ty; i < n; i += (int64_t)gridDim.x * ny) {
+            double v = (double)x[i * k + r];
+            acc += v * v;
+        }
+    sm[ty * blockDim.x + r] = acc;
+    __syncthreads();
+    if (ty == 0 && r < k) {
+        double s = 0;
+        for (int q = 0; q < ny; q++) s += sm[q * blockDim.x + r];
+        partial[(int64_t)r * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+__global__ void k_reduce_partials(const double *partial, int nb, int cnt, double *out, bool take_sqrt) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cnt) return;
+    double s = 0;
+    for (int b = 0; b < nb; b++) s += partial[(int64_t)c * nb + b];
+    out[c] = take_sqrt ? sqrt(s) : s;
+}
+
+template <class T>
+void colnorms(const T *x, int64_t n, int k, double *partial, double *out, cudaStream_t s) {
+    int kx = pow2_at_least(k);
+    dim3 blk(kx, 256 / kx);
+    k_colsq_partial<T><<<kRedBlocks, blk, 0, s>>>(x, n, k, partial);
+    k_reduce_partials<<<(k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, k, out, true);
+}
+template void colnorms<double>(const double *, int64_t, int, double *, double *, cudaStream_t);
+template void colnorms<float>(const float *, int64_t, int, double *, double *, cudaStream_t);
+
+// dots[j*k + r] = <V_j[:, r], w[:, r]> for j < J.
+template <class T>
+__global__ void __launch_bounds__(256) k_mdot_partial(const T *V, int64_t n, int J, const T *w, int k, double *partial) {
+    __shared__ double sm[256];
+    const int r = threadIdx.x, ty = threadIdx.y, ny = blockDim.y;
+    const int64_t nk = n * k;
+    for (int j = 0; j < J; j++) {
+        const T *Vj = V + (int64_t)j * nk;
+        double acc = 0;
+        if (r < k)
+            for (int64_t i = blockIdx.x * (int64_t)ny + ty; i < n; i += (int64_t)gridDim.x * ny)
+                acc += (double)Vj[i * k + r] * (double)w[i * k + r];
+        sm[ty * blockDim.x + r] = acc;
+        __syncthreads();
+        if (ty == 0 && r < k) {
+            double s = 0;
+            for (int q = 0; q < ny; q++) s += sm[q * blockDim.x + r];
+            partial[((int64_t)j * k + r) * gridDim.x + blockIdx.x] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// w -= sum_j h[j*k + r] V_j ; also h_acc += h (for reorthogonalisation)
+template <class T>
+__global__ void __launch_bounds__(256) k_maxpy(const T *V, int64_t nk, int J, const double *h, int k, T *w) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
+        int r = (int)(t % k);
+        double acc = (double)w[t];
+        for (int j = 0; j < J; j++) acc -= h[j * k + r] * (double)V[(int64_t)j * nk + t];
+        w[t] = (T)acc;
+    }
+}
+
+// ---------------------------------------------------------------- smoothing
+template <class T>
+__global__ void k_cheb_first(int64_t nk, int k, const T *dinv, const T *b, T *x, T *d, double inv_theta, bool add) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
+        // add == false: x0 = 0 so the residual is b; add == true: b holds b - A x
+        T dd = (T)(inv_theta * (double)dinv[t / k] * (double)b[t]);
+        d[t] = dd;
+        x[t] = add ? x[t] + dd : dd;
+    }
+}
+
+// d = c1 d + c2 D^-1 (b - A x) with t = b - A x precomputed; x += d
+template <class T>
+__global__ void k_cheb_step(int64_t nk, int k, const T *dinv, const T *res, T *x, T *d, double c1, double c2) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
+        double dd = c1 * (double)d[t] + c2 * (double)dinv[t / k] * (double)res[t];
+        d[t] = (T)dd;
+        x[t] = (T)((double)x[t] + dd);
+    }
+}
+
+template <class T>
+static void chebyshev(Level<T> &L, int deg, double ratio, const T *b, T *x, bool zero_guess, int k, cudaStream_t s) {
+    double lmax = L.lmax * 1.05, lmin = L.lmax * ratio;
+    double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+    double sigma = theta / delta, rho = 1.0 / sigma;
+    int64_t nk = L.n * k;
+    unsigned g = grid_for(nk);
+    if (zero_guess) {
+        k_cheb_first<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, b, x, L.d, 1.0 / theta, false);
+    } else {
+        spmm_b<T>(L.A, L.long_rows, L.nlong, x, L.t0, k, b, s);
+        k_cheb_first<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, L.t0, x, L.d, 1.0 / theta, true);
+    }
+    for (int it = 1; it < deg; it++) {
+        spmm_b<T>(L.A, L.long_rows, L.nlong, x, L.t0, k, b, s);
+        double rn = 1.0 / (2.0 * sigma - rho);
+        k_cheb_step<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, L.t0, x, L.d, rn * rho, 2.0 * rn / delta);
+        rho = rn;
+    }
+}
+
+// b_c[I] = sum over members i of I of (b_i - (A x)_i)  (t0 holds b - A x)
+template <class T>
+__global__ void k_restrict(int64_t nc, int k, const int64_t *rptr, const int32_t *rmem, const T *res, T *bc) {
+    int64_t total = nc * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t I = t / k;
+        int r = (int)(t - I * k);
+        double acc = 0;
+        for (int64_t q = rptr[I]; q < rptr[I + 1]; q++) acc += (double)res[(int64_t)rmem[q] * k + r];
+        bc[t] = (T)acc;
+    }
+}
+
+template <class T>
+__global__ void k_prolong(int64_t n, int k, const int32_t *agg, const T *xc, T *x) {
+    int64_t total = n * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = t / k;
+        int a = agg[i];
+        if (a >= 0) x[t] = (T)((double)x[t] + (double)xc[(int64_t)a * k + (t - i * k)]);
+    }
+}
+
+template <class T>
+__global__ void k_dense_apply(int64_t n, int k, const double *Ainv, const T *b, T *x) {
+    int64_t total = n * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = t / k;
+        int r = (int)(t - i * k);
+        double acc = 0;
+        for (int64_t j = 0; j < n; j++) acc += Ainv[i * n + j] * (double)b[j * k + r];
+        x[t] = (T)acc;
+    }
+}
+
+template <class T>
+static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaStream_t s) {
+    Level<T> &L = H.lv[l];
+    if (l == (int)H.lv.size() - 1) {
+        if (H.cinv) k_dense_apply<T><<<grid_for(L.n * k), kThreads, 0, s>>>(L.n, k, H.cinv, L.b, L.x);
+        else {
+            chebyshev<T>(L, 4, cfg.cheb_ratio, L.b, L.x, true, k, s);
+            for (int q = 0; q < 4; q++) chebyshev<T>(L, 4, cfg.cheb_ratio, L.b, L.x, false, k, s);
+        }
+        return;
+    }
+    chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, L.b, L.x, true, k, s);
+    spmm_b<T>(L.A, L.long_rows, L.nlong, L.x, L.t0, k, L.b, s);
+    Level<T> &C = H.lv[l + 1];
+    k_restrict<T><<<grid_for(C.n * k), kThreads, 0, s>>>(C.n, k, L.rptr, L.rmem, L.t0, C.b);
+    vcycle<T>(H, cfg, l + 1, k, s);
+    k_prolong<T><<<grid_for(L.n * k), kThreads, 0, s>>>(L.n, k, L.agg, C.x, L.x);
+    chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, L.b, L.x, false, k, s);
+}
+
+// ------------------------------------------------------------- AMG setup
+__global__ void k_diag(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, double *diag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double d = 0;
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) if (col[q] == i) { d = val[q]; break; }
+        diag[i] = d;
+    }
+}
+
+__global__ void k_dinv_gersh(int64_t n, const int64_t *ptr, const double *val, const double *diag, double *dinv,
+                             unsigned long long *lmax_bits) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double d = diag[i];
+        if (d == 0.0) d = 1.0;
+        dinv[i] = 1.0 / d;
+        double s = 0;
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) s += fabs(val[q]);
+        double ratio = s / fabs(d);
+        atomicMax(lmax_bits, (unsigned long long)__double_as_longlong(ratio));
+    }
+}
+
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+
+// strong(i, q) for entry q of row i
+__device__ __forceinline__ bool strong(int64_t i, int64_t q, const int32_t *col, const double *val, const double *diag,
+                                       const uint8_t *dense, double theta) {
+    int32_t j = col[q];
+    if (j == i || dense[j]) return false;
+    return fabs(val[q]) >= theta * sqrt(fabs(diag[i] * diag[j]));
+}
+
+// dense flag and eligibility (state): 0 out/ineligible, 1 undecided
+__global__ void k_agg_init(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
+                           int64_t lim, double theta, uint8_t *dense, uint64_t *T) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dense[i] = (ptr[i + 1] - ptr[i]) > lim ? 1 : 0;
+}
+
+__global__ void k_agg_state(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
+                            double theta, const uint8_t *dense, uint64_t *T) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        bool elig = false;
+        if (!dense[i])
+            for (int64_t q = ptr[i]; q < ptr[i + 1]; q++)
+                if (strong(i, q, col, val, diag, dense, theta)) { elig = true; break; }
+        uint64_t st = elig ? 1ull : 0ull;
+        T[i] = (st << 62) | ((uint64_t)(hash32((uint32_t)i * 2654435761u + 12345u) & 0x3fffffffu) << 32) | (uint64_t)(uint32_t)i;
+    }
+}
+
+__global__ void k_mis_max(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
+                          double theta, const uint8_t *dense, const uint64_t *in, uint64_t *out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t m = in[i];
+        if (!dense[i])
+            for (int64_t q = ptr[i]; q < ptr[i + 1]; q++)
+                if (strong(i, q, col, val, diag, dense, theta)) { uint64_t v = in[col[q]]; m = v > m ? v : m; }
+        out[i] = m;
+    }
+}
+
+__global__ void k_mis_update(int64_t n, uint64_t *T, const uint64_t *M, int *undecided) {
+    int cnt = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t t = T[i];
+        if ((t >> 62) != 1) continue;
+        uint64_t m = M[i];
+        if (m == t) T[i] = (t & ~(3ull << 62)) | (2ull << 62);           // IN
+        else if ((m >> 62) == 2) T[i] = t & ~(3ull << 62);              // OUT (state 0)
+        else cnt++;
+    }
+    if (cnt) atomicAdd(undecided, cnt);
+}
+
+// roots: IN nodes and dense rows
+__global__ void k_root_flag(int64_t n, const uint64_t *T, const uint8_t *dense, int64_t *flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        flag[i] = ((T[i] >> 62) == 2 || dense[i]) ? 1 : 0;
+}
+
+__global__ void k_agg_phase1(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
+                             double theta, const uint8_t *dense, const uint64_t *T, const int64_t *rootid,
+                             int32_t *agg1) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t t = T[i];
+        if ((t >> 62) == 2 || dense[i]) { agg1[i] = (int32_t)rootid[i]; continue; }
+        // eligible nodes were set IN or OUT; an OUT node with a strong root
+        // neighbour joins the highest-priority one
+        uint64_t best = 0;
+        int64_t bj = -1;
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) {
+            if (!strong(i, q, col, val, diag, dense, theta)) continue;
+            uint64_t v = T[col[q]];
+            if ((v >> 62) == 2 && v > best) { best = v; bj = col[q]; }
+        }
+        agg1[i] = bj >= 0 ? (int32_t)rootid[bj] : -2;
+    }
+}
+
+__global__ void k_agg_phase2(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
+                             double theta, const uint8_t *dense, const uint64_t *T, const int32_t *agg1,
+                             int32_t *agg) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t a = agg1[i];
+        if (a != -2) { agg[i] = a; continue; }
+        bool elig = false;
+        double best = -1;
+        int32_t ba = -1;
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) {
+            if (!strong(i, q, col, val, diag, dense, theta)) continue;
+            elig = true;
+            int32_t aj = agg1[col[q]];
+            if (aj >= 0 && fabs(val[q]) > best) { best = fabs(val[q]); ba = aj; }
+        }
+        agg[i] = elig ? ba : -1;
+    }
+}
+
+// RAP of the piecewise-constant prolongation: expand (agg_i, agg_j, a_ij)
+__global__ void k_rap_count(int64_t n, const int64_t *ptr, const int32_t *col, const int32_t *agg, int64_t *cnt) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c = 0;
+        if (agg[i] >= 0)
+            for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) c += agg[col[q]] >= 0;
+        cnt[i] = c;
+    }
+}
+
+__global__ void k_rap_expand(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const int32_t *agg,
+                             const int64_t *off, uint64_t nc, uint64_t *keys, double *vals) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t ai = agg[i];
+        if (ai < 0) continue;
+        int64_t o = off[i];
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) {
+            int32_t aj = agg[col[q]];
+            if (aj < 0) continue;
+            keys[o] = (uint64_t)ai * nc + (uint64_t)aj;
+            vals[o] = val[q];
+            o++;
+        }
+    }
+}
+
+__global__ void k_heads64(const uint64_t *keys, int64_t n, int64_t *head) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        head[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+__global__ void k_seg_reduce(const uint64_t *keys, const double *vals, int64_t n, const int64_t *segid, uint64_t nc,
+                             int64_t *rowcnt, int32_t *ocol, double *oval) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!(i == 0 || keys[i] != keys[i - 1])) continue;
+        double sacc = 0;
+        int64_t j = i;
+        while (j < n && keys[j] == keys[i]) { sacc += vals[j]; j++; }
+        int64_t sg = segid[i];
+        ocol[sg] = (int32_t)(keys[i] % nc);
+        oval[sg] = sacc;
+        atomicAdd((unsigned long long *)&rowcnt[keys[i] / nc], 1ull);
+    }
+}
+
+__global__ void k_agg_key(int64_t n, const int32_t *agg, const int64_t *pos, uint32_t *key, int32_t *node) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (agg[i] >= 0) { key[pos[i]] = (uint32_t)agg[i]; node[pos[i]] = (int32_t)i; }
+}
+
+__global__ void k_member_ptr(int64_t m, const uint32_t *skey, int64_t nc, int64_t *rptr) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= m; i += (int64_t)gridDim.x * blockDim.x) {
+        // rptr[a] = first position with key >= a
+        if (i == 0) { for (int64_t a = 0; a <= (m > 0 ? skey[0] : nc - 1) && a < nc; a++) rptr[a] = 0; }
+        else if (i == m) { for (int64_t a = skey[m - 1] + 1; a <= nc; a++) rptr[a] = m; }
+        else if (skey[i] != skey[i - 1]) { for (int64_t a = skey[i - 1] + 1; a <= skey[i]; a++) rptr[a] = i; }
+    }
+}
+
+__global__ void k_dense_fill(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, double *Dm) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) Dm[i * n + col[q]] += val[q];
+}
+
+// Gauss-Jordan inverse with partial pivoting in one block (n <= a few 1000).
+__global__ void __launch_bounds__(1024) k_gauss_jordan(double *a, double *inv, int64_t n, int *singular) {
+    __shared__ int64_t piv;
+    __shared__ double pval;
+    for (int64_t i = threadIdx.x; i < n * n; i += blockDim.x) inv[i] = (i / n == i % n) ? 1.0 : 0.0;
+    __syncthreads();
+    for (int64_t kk = 0; kk < n; kk++) {
+        if (threadIdx.x == 0) {
+            int64_t p = kk;
+            double mx = fabs(a[kk * n + kk]);
+            for (int64_t i = kk + 1; i < n; i++) if (fabs(a[i * n + kk]) > mx) { mx = fabs(a[i * n + kk]); p = i; }
+            piv = p;
+            pval = a[p * n + kk];
+            if (pval == 0.0) { *singular = 1; pval = 1e-300; }
+        }
+        __syncthreads();
+        int64_t p = piv;
+        if (p != kk)
+            for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+                double t = a[kk * n + j]; a[kk * n + j] = a[p * n + j]; a[p * n + j] = t;
+                t = inv[kk * n + j]; inv[kk * n + j] = inv[p * n + j]; inv[p * n + j] = t;
+            }
+        __syncthreads();
+        double pv = pval;
+        for (int64_t j = threadIdx.x; j < n; j += blockDim.x) { a[kk * n + j] /= pv; inv[kk * n + j] /= pv; }
+        __syncthreads();
+        for (int64_t idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+            int64_t i = idx / n, j = idx - i * n;
+            if (i == kk) continue;
+            double f = a[i * n + kk];
+            if (f == 0.0) continue;
+            if (j != kk) a[i * n + j] -= f * a[kk * n + j];
+            inv[i * n + j] -= f * inv[kk * n + j];
+        }
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) if (i != kk) a[i * n + kk] = 0.0;
+        __syncthreads();
+    }
+}
+
+template <class T>
+void Hierarchy<T>::release(cudaStream_t s) {
+    for (auto &L : lv) {
+        L.A.release(s);
+        dfree(L.long_rows, s); dfree(L.dinv, s); dfree(L.agg, s); dfree(L.rptr, s); dfree(L.rmem, s);
+        dfree(L.x, s); dfree(L.b, s); dfree(L.t0, s); dfree(L.t1, s); dfree(L.d, s);
+    }
+    lv.clear();
+    dfree(cinv, s);
+    kcap = 0;
+}
+template struct Hierarchy<double>;
+template struct Hierarchy<float>;
+
+static int key_bits(uint64_t v) {
+    int b = 0;
+    while (b < 64 && (v >> b) != 0) b++;
+    return b < 8 ? 8 : ((b + 7) / 8) * 8;
+}
+
+g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_t s, int64_t *, Hierarchy<double> &H) {
+    H.release(s);
+    // level 0 owns a copy of the operator
+    Level<double> L0;
+    L0.n = A0.n;
+    L0.A.n = L0.A.m = A0.n; L0.A.nnz = A0.nnz;
+    G2P_TRY(dalloc(&L0.A.ptr, A0.n + 1, s)); G2P_TRY(dalloc(&L0.A.col, A0.nnz, s)); G2P_TRY(dalloc(&L0.A.val, A0.nnz, s));
+    G2P_CUDA(cudaMemcpyAsync(L0.A.ptr, A0.ptr, sizeof(int64_t) * (A0.n + 1), cudaMemcpyDeviceToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(L0.A.col, A0.col, sizeof(int32_t) * A0.nnz, cudaMemcpyDeviceToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(L0.A.val, A0.val, sizeof(double) * A0.nnz, cudaMemcpyDeviceToDevice, s));
+    H.lv.push_back(L0);
+    int64_t *work = nullptr;
+    int64_t work_n = 0;
+    auto need_work = [&](int64_t n) -> g2p_status {
+        int64_t w = scan_work_size(n) + 8;
+        if (w > work_n) { dfree(work, s); G2P_TRY(dalloc(&work, w, s)); work_n = w; }
+        return G2P_OK;
+    };
+    int *d_int = nullptr;
+    unsigned long long *d_lmax = nullptr;
+    G2P_TRY(dalloc(&d_int, 4, s));
+    G2P_TRY(dalloc(&d_lmax, 1, s));
+    for (int l = 0;; l++) {
+        Level<double> &L = H.lv[l];
+        int64_t n = L.n;
+        double *diag;
+        G2P_TRY(dalloc(&diag, n, s));
+        G2P_TRY(dalloc(&L.dinv, n, s));
+        k_diag<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag);
+        G2P_CUDA(cudaMemsetAsync(d_lmax, 0, sizeof(unsigned long long), s));
+        k_dinv_gersh<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.val, diag, L.dinv, d_lmax);
+        unsigned long long lb = 0;
+        G2P_CUDA(cudaMemcpyAsync(&lb, d_lmax, sizeof(lb), cudaMemcpyDeviceToHost, s));
+        G2P_TRY(find_long_rows_t<double>(L.A, &L.long_rows, &L.nlong, s));   // synchronizes
+        double lm;
+        memcpy(&lm, &lb, sizeof(lm));
+        L.lmax = lm > 0 ? lm : 2.0;
+        bool last = n <= cfg.coarse_size || l + 1 >= cfg.max_levels;
+        if (!last) {
+            // ---- aggregation
+            int64_t lim = 32 + 4 * (L.A.nnz / (n > 0 ? n : 1));
+            uint8_t *dense;
+            uint64_t *T, *M1, *M2;
+            G2P_TRY(dalloc(&dense, n, s)); G2P_TRY(dalloc(&T, n, s)); G2P_TRY(dalloc(&M1, n, s)); G2P_TRY(dalloc(&M2, n, s));
+            unsigned g = grid_for(n);
+            k_agg_init<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, lim, cfg.strength, dense, T);
+            k_agg_state<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T);
+            for (int round = 0; round < 200; round++) {
+                k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, M1);
+                k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, M1, M2);
+                G2P_CUDA(cudaMemsetAsync(d_int, 0, sizeof(int), s));
+                k_mis_update<<<g, kThreads, 0, s>>>(n, T, M2, d_int);
+                int und = 0;
+                G2P_CUDA(cudaMemcpyAsync(&und, d_int, sizeof(int), cudaMemcpyDeviceToHost, s));
+                G2P_CUDA(cudaStreamSynchronize(s));
+                if (und == 0) break;
+            }
+            int64_t *rootid;
+            G2P_TRY(dalloc(&rootid, n + 1, s));
+            G2P_TRY(need_work(n + 1));
+            {
+                const uint64_t *Tp = T;
+                const uint8_t *dp = dense;
+                auto rop = [Tp, dp, n] __device__(int64_t i) -> int64_t {
+                    return i < n ? (((Tp[i] >> 62) == 2 || dp[i]) ? 1 : 0) : 0;
+                };
+                G2P_TRY(exclusive_scan(rop, n + 1, rootid, work, s));
+            }
+            int64_t nc = 0;
+            G2P_CUDA(cudaMemcpyAsync(&nc, rootid + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+            int32_t *agg1;
+            G2P_TRY(dalloc(&agg1, n, s));
+            G2P_TRY(dalloc(&L.agg, n, s));
+            k_agg_phase1<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, rootid, agg1);
+            k_agg_phase2<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, agg1, L.agg);
+            G2P_CUDA(cudaStreamSynchronize(s));
+            dfree(agg1, s); dfree(rootid, s); dfree(dense, s); dfree(T, s); dfree(M1, s); dfree(M2, s);
+            if (nc == 0 || nc > (n * 9) / 10) {
+                dfree(L.agg, s);
+                last = true;
+            } else {
+                // ---- member lists (aggregate -> rows, ascending)
+                int64_t *pos;
+                G2P_TRY(dalloc(&pos, n + 1, s));
+                const int32_t *ag = L.agg;
+                auto mop = [ag, n] __device__(int64_t i) -> int64_t { return i < n ? (ag[i] >= 0 ? 1 : 0) : 0; };
+                G2P_TRY(exclusive_scan(mop, n + 1, pos, work, s));
+                int64_t nm = 0;
+                G2P_CUDA(cudaMemcpyAsync(&nm, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+                G2P_CUDA(cudaStreamSynchronize(s));
+                uint32_t *k0, *k1;
+                int32_t *v0, *v1;
+                G2P_TRY(dalloc(&k0, nm, s)); G2P_TRY(dalloc(&k1, nm, s)); G2P_TRY(dalloc(&v0, nm, s)); G2P_TRY(dalloc(&v1, nm, s));
+                k_agg_key<<<g, kThreads, 0, s>>>(n, L.agg, pos, k0, v0);
+                int64_t *counts;
+                G2P_TRY(dalloc(&counts, sort_counts_size(nm), s));
+                G2P_TRY(need_work(sort_counts_size(nm)));
+                bool in1 = false;
+                G2P_TRY(radix_sort_pairs(k0, v0, k1, v1, nm, key_bits((uint64_t)nc), counts, work, &in1, s));
+                dfree(counts, s);
+                G2P_TRY(dalloc(&L.rptr, nc + 1, s));
+                k_member_ptr<<<grid_for(nm + 1), kThreads, 0, s>>>(nm, in1 ? k1 : k0, nc, L.rptr);
+                L.rmem = in1 ? v1 : v0;
+                dfree(in1 ? v0 : v1, s);
+                dfree(k0, s); dfree(k1, s); dfree(pos, s);
+                // ---- Galerkin coarse operator
+                int64_t *cnt, *off;
+                G2P_TRY(dalloc(&cnt, n + 1, s));
+                G2P_TRY(dalloc(&off, n + 1, s));
+                k_rap_count<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.agg, cnt);
+                const int64_t *cp = cnt;
+                auto cop = [cp, n] __device__(int64_t i) -> int64_t { return i < n ? cp[i] : 0; };
+                G2P_TRY(exclusive_scan(cop, n + 1, off, work, s));
+                int64_t ne = 0;
+                G2P_CUDA(cudaMemcpyAsync(&ne, off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+                G2P_CUDA(cudaStreamSynchronize(s));
+                uint64_t *ek0, *ek1;
+                double *ev0, *ev1;
+                G2P_TRY(dalloc(&ek0, ne, s)); G2P_TRY(dalloc(&ek1, ne, s)); G2P_TRY(dalloc(&ev0, ne, s)); G2P_TRY(dalloc(&ev1, ne, s));
+                k_rap_expand<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.agg, off, (uint64_t)nc, ek0, ev0);
+                dfree(cnt, s); dfree(off, s);
+                G2P_TRY(dalloc(&counts, sort_counts_size(ne), s));
+                G2P_TRY(need_work(sort_counts_size(ne)));
+                G2P_TRY(radix_sort_pairs(ek0, ev0, ek1, ev1, ne, key_bits((uint64_t)nc * (uint64_t)nc), counts, work, &in1, s));
+                dfree(counts, s);
+                uint64_t *sk = in1 ? ek1 : ek0;
+                double *sv = in1 ? ev1 : ev0;
+                int64_t *head, *segid;
+                G2P_TRY(dalloc(&head, ne + 1, s)); G2P_TRY(dalloc(&segid, ne + 1, s));
+                k_heads64<<<grid_for(ne), kThreads, 0, s>>>(sk, ne, head);
+                const int64_t *hp = head;
+                G2P_TRY(need_work(ne + 1));
+                auto hop = [hp, ne] __device__(int64_t i) -> int64_t { return i < ne ? hp[i] : 0; };
+                G2P_TRY(exclusive_scan(hop, ne + 1, segid, work, s));
+                int64_t nseg = 0;
+                G2P_CUDA(cudaMemcpyAsync(&nseg, segid + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+                G2P_CUDA(cudaStreamSynchronize(s));
+                Level<double> C;
+                C.n = nc;
+                C.A.n = C.A.m = nc; C.A.nnz = nseg;
+                int64_t *rowcnt;
+                G2P_TRY(dalloc(&rowcnt, nc + 1, s));
+                G2P_CUDA(cudaMemsetAsync(rowcnt, 0, sizeof(int64_t) * (nc + 1), s));
+                G2P_TRY(dalloc(&C.A.col, nseg, s)); G2P_TRY(dalloc(&C.A.val, nseg, s)); G2P_TRY(dalloc(&C.A.ptr, nc + 1, s));
+                k_seg_reduce<<<grid_for(ne), kThreads, 0, s>>>(sk, sv, ne, segid, (uint64_t)nc, rowcnt, C.A.col, C.A.val);
+                const int64_t *rc = rowcnt;
+                G2P_TRY(need_work(nc + 1));
+                auto rcop = [rc, nc] __device__(int64_t i) -> int64_t { return i < nc ? rc[i] : 0; };
+                G2P_TRY(exclusive_scan(rcop, nc + 1, C.A.ptr, work, s));
+                G2P_CUDA(cudaStreamSynchronize(s));
+                dfree(rowcnt, s); dfree(head, s); dfree(segid, s);
+                dfree(ek0, s); dfree(ek1, s); dfree(ev0, s); dfree(ev1, s);
+                L.nc = nc;
+                H.lv.push_back(C);
+            }
+        }
+        dfree(diag, s);
+        if (last) {
+            Level<double> &Cl = H.lv[l];
+            int64_t nn = Cl.n;
+            H.nc = nn;
+            if (nn > kMaxDenseCoarse) break;   // coarsest level solved by smoothing
+            double *Dm;
+            G2P_TRY(dalloc(&Dm, nn * nn, s));
+            G2P_TRY(dalloc(&H.cinv, nn * nn, s));
+            G2P_CUDA(cudaMemsetAsync(Dm, 0, sizeof(double) * nn * nn, s));
+            k_dense_fill<<<grid_for(nn), kThreads, 0, s>>>(nn, Cl.A.ptr, Cl.A.col, Cl.A.val, Dm);
+            G2P_CUDA(cudaMemsetAsync(d_int, 0, sizeof(int), s));
+            k_gauss_jordan<<<1, 1024, 0, s>>>(Dm, H.cinv, nn, d_int);
+            G2P_CUDA(cudaStreamSynchronize(s));
+            dfree(Dm, s);
+            break;
+        }
+    }
+    dfree(d_int, s); dfree(d_lmax, s); dfree(work, s);
+    G2P_CUDA(cudaGetLastError());
+    G2P_CUDA(cudaStreamSynchronize(s));
+    return G2P_OK;
+}
+
+__global__ void k_d2f(const double *in, float *out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+g2p_status amg_to_float(const Hierarchy<double> &H, cudaStream_t s, Hierarchy<float> &F) {
+    F.release(s);
+    for (size_t l = 0; l < H.lv.size(); l++) {
+        const Level<double> &L = H.lv[l];
+        Level<float> f;
+        f.n = L.n; f.nc = L.nc; f.lmax = L.lmax; f.nlong = L.nlong;
+        f.A.n = f.A.m = L.A.n; f.A.nnz = L.A.nnz;
+        // structure is shared by copying (owned separately for simple release)
+        G2P_TRY(dalloc(&f.A.ptr, L.A.n + 1, s)); G2P_TRY(dalloc(&f.A.col, L.A.nnz, s)); G2P_TRY(dalloc(&f.A.val, L.A.nnz, s));
+        G2P_CUDA(cudaMemcpyAsync(f.A.ptr, L.A.ptr, sizeof(int64_t) * (L.A.n + 1), cudaMemcpyDeviceToDevice, s));
+        G2P_CUDA(cudaMemcpyAsync(f.A.col, L.A.col, sizeof(int32_t) * L.A.nnz, cudaMemcpyDeviceToDevice, s));
+        k_d2f<<<grid_for(L.A.nnz), kThreads, 0, s>>>(L.A.val, f.A.val, L.A.nnz);
+        G2P_TRY(dalloc(&f.dinv, L.n, s));
+        k_d2f<<<grid_for(L.n), kThreads, 0, s>>>(L.dinv, f.dinv, L.n);
+        if (L.nlong > 0) {
+            G2P_TRY(dalloc(&f.long_rows, L.nlong, s));
+            G2P_CUDA(cudaMemcpyAsync(f.long_rows, L.long_rows, sizeof(int32_t) * L.nlong, cudaMemcpyDeviceToDevice, s));
+        }
+        if (L.agg) {
+            G2P_TRY(dalloc(&f.agg, L.n, s));
+            G2P_CUDA(cudaMemcpyAsync(f.agg, L.agg, sizeof(int32_t) * L.n, cudaMemcpyDeviceToDevice, s));
+            G2P_TRY(dalloc(&f.rptr, L.nc + 1, s));
+            G2P_CUDA(cudaMemcpyAsync(f.rptr, L.rptr, sizeof(int64_t) * (L.nc + 1), cudaMemcpyDeviceToDevice, s));
+            int64_t nm = 0;
+            G2P_CUDA(cudaMemcpyAsync(&nm, L.rptr + L.nc, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+            G2P_CUDA(cudaStreamSynchronize(s));
+            G2P_TRY(dalloc(&f.rmem, nm, s));
+            G2P_CUDA(cudaMemcpyAsync(f.rmem, L.rmem, sizeof(int32_t) * nm, cudaMemcpyDeviceToDevice, s));
+        }
+        F.lv.push_back(f);
+    }
+    F.nc = H.nc;
+    if (H.cinv) {
+        G2P_TRY(dalloc(&F.cinv, H.nc * H.nc, s));
+        G2P_CUDA(cudaMemcpyAsync(F.cinv, H.cinv, sizeof(double) * H.nc * H.nc, cudaMemcpyDeviceToDevice, s));
+    }
+    G2P_CUDA(cudaStreamSynchronize(s));
+    return G2P_OK;
+}
+
+template <class T>
+g2p_status hierarchy_reserve(Hierarchy<T> &H, int k, cudaStream_t s) {
+    if (k <= H.kcap) return G2P_OK;
+    for (auto &L : H.lv) {
+        dfree(L.x, s); dfree(L.b, s); dfree(L.t0, s); dfree(L.t1, s); dfree(L.d, s);
+        G2P_TRY(dalloc(&L.x, L.n * k, s)); G2P_TRY(dalloc(&L.b, L.n * k, s));
+        G2P_TRY(dalloc(&L.t0, L.n * k, s)); G2P_TRY(dalloc(&L.d, L.n * k, s));
+    }
+    H.kcap = k;
+    return G2P_OK;
+}
+template g2p_status hierarchy_reserve<double>(Hierarchy<double> &, int, cudaStream_t);
+template g2p_status hierarchy_reserve<float>(Hierarchy<float> &, int, cudaStream_t);
+
+// ------------------------------------------------------------------- FGMRES
+template <class T>
+void Krylov<T>::release(cudaStream_t s) {
+    dfree(V, s); dfree(Z, s); dfree(w, s); dfree(r, s);
+    dfree(H, s); dfree(cs, s); dfree(sn, s); dfree(g, s); dfree(y, s);
+    dfree(beta, s); dfree(bnorm, s); dfree(partial, s); dfree(hcol, s);
+    if (h_est) cudaFreeHost(h_est);
+    h_est = nullptr;
+    n = 0; k = 0; m = 0;
+}
+template struct Krylov<double>;
+template struct Krylov<float>;
+
+template <class T>
+g2p_status krylov_alloc(Krylov<T> &K, int64_t n, int k, int m, cudaStream_t s) {
+    if (K.n == n && K.k >= k && K.m >= m) return G2P_OK;
+    K.release(s);
+    K.n = n; K.k = k; K.m = m;
+    G2P_TRY(dalloc(&K.V, n * k * (m + 1), s));
+    G2P_TRY(dalloc(&K.Z, n * k * m, s));
+    G2P_TRY(dalloc(&K.w, n * k, s));
+    G2P_TRY(dalloc(&K.r, n * k, s));
+    G2P_TRY(dalloc(&K.H, (int64_t)k * (m + 1) * m, s));
+    G2P_TRY(dalloc(&K.cs, (int64_t)k * m, s));
+    G2P_TRY(dalloc(&K.sn, (int64_t)k * m, s));
+    G2P_TRY(dalloc(&K.g, (int64_t)k * (m + 1), s));
+    G2P_TRY(dalloc(&K.y, (int64_t)k * m, s));
+    G2P_TRY(dalloc(&K.beta, k, s));
+    G2P_TRY(dalloc(&K.bnorm, k, s));
+    G2P_TRY(dalloc(&K.partial, (int64_t)kRedBlocks * k * (m + 2), s));
+    G2P_TRY(dalloc(&K.hcol, (int64_t)k * (2 * m + 4), s));
+    G2P_CUDA(cudaMallocHost(&K.h_est, sizeof(double) * 2 * k));
+    return G2P_OK;
+}
+template g2p_status krylov_alloc<double>(Krylov<double> &, int64_t, int, int, cudaStream_t);
+template g2p_status krylov_alloc<float>(Krylov<float> &, int64_t, int, int, cudaStream_t);
+
+template <class T>
+__global__ void k_start(int64_t nk, int k, const T *r, const double *beta, T *v0) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
+        double b = beta[t % k];
+        v0[t] = b > 0 ? (T)((double)r[t] / b) : (T)0;
+    }
+}
+
+// hcol = [dots (j+1 per rhs); norm]; form V_{j+1}, update H, Givens, g
+template <class T>
+__global__ void k_arnoldi_finish(int64_t nk, int k, const double *hnorm, const T *w, T *vnext) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
+        double h = hnorm[t % k];
+        vnext[t] = h > 0 ? (T)((double)w[t] / h) : (T)0;
+    }
+}
+
+__global__ void k_givens(int k, int m, int j, const double *hdots, const double *hnorm, double *H, double *cs, double *sn,
+                         double *g, const double *bnorm, double *est) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= k) return;
+    double *Hr = H + (int64_t)r * (m + 1) * m;    // column-major (m+1) x m
+    for (int i = 0; i <= j; i++) Hr[j * (m + 1) + i] = hdots[i * k + r];
+    Hr[j * (m + 1) + j + 1] = hnorm[r];
+    double *c = cs + (int64_t)r * m, *s = sn + (int64_t)r * m, *gr = g + (int64_t)r * (m + 1);
+    for (int i = 0; i < j; i++) {
+        double a = Hr[j * (m + 1) + i], b = Hr[j * (m + 1) + i + 1];
+        Hr[j * (m + 1) + i] = c[i] * a + s[i] * b;
+        Hr[j * (m + 1) + i + 1] = -s[i] * a + c[i] * b;
+    }
+    double a = Hr[j * (m + 1) + j], b = Hr[j * (m + 1) + j + 1];
+    double rr = sqrt(a * a + b * b);
+    c[j] = rr != 0 ? a / rr : 1.0;
+    s[j] = rr != 0 ? b / rr : 0.0;
+    Hr[j * (m + 1) + j] = rr;
+    Hr[j * (m + 1) + j + 1] = 0.0;
+    gr[j + 1] = -s[j] * gr[j];
+    gr[j] = c[j] * gr[j];
+    double bn = bnorm[r];
+    est[r] = bn > 0 ? fabs(gr[j + 1]) / bn : 0.0;
+}
+
+__global__ void k_g_init(int k, int m, const double *beta, double *g) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= k) return;
+    for (int i = 0; i <= m; i++) g[(int64_t)r * (m + 1) + i] = 0.0;
+    g[(int64_t)r * (m + 1)] = beta[r];
+}
+
+__global__ void k_backsolve(int k, int m, int j, const double *H, const double *g, double *y) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= k) return;
+    const double *Hr = H + (int64_t)r * (m + 1) * m;
+    const double *gr = g + (int64_t)r * (m + 1);
+    double *yr = y + (int64_t)r * m;
+    for (int i = j - 1; i >= 0; i--) {
+        double sacc = gr[i];
+        for (int q = i + 1; q < j; q++) sacc -= Hr[q * (m + 1) + i] * yr[q];
+        double d = Hr[i * (m + 1) + i];
+        yr[i] = d != 0 ? sacc / d : 0.0;
+    }
+}
+
+// x += sum_i Z_i y_i, and y is laid out [r * m + i]
+template <class T>
+__global__ void k_xupdate(int64_t nk, int k, int m, int j, const T *Z, const double *y, T *x) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
+        int r = (int)(t % k);
+        double acc = (double)x[t];
+        for (int i = 0; i < j; i++) acc += (double)Z[(int64_t)i * nk + t] * y[(int64_t)r * m + i];
+        x[t] = (T)acc;
+    }
+}
+
+template <class T>
+static void mdot(const T *V, int64_t n, int J, const T *w, int k, double *partial, double *out, cudaStream_t s) {
+    int kx = pow2_at_least(k);
+    dim3 blk(kx, 256 / kx);
+    k_mdot_partial<T><<<kRedBlocks, blk, 0, s>>>(V, n, J, w, k, partial);
+    k_reduce_partials<<<(J * k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, J * k, out, false);
+}
+
+__global__ void k_add_vec(double *a, const double *b, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] += b[i];
+}
+
+template <class T>
+g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T *x, int k, const SolverConfig &cfg,
+                  const double *bnorm_override, cudaStream_t s, SolveReport &rep) {
+    const int64_t n = A.n, nk = n * k;
+    const int m = cfg.restart;
+    G2P_TRY(krylov_alloc<T>(K, n, k, m, s));
+    G2P_TRY(hierarchy_reserve<T>(H, k, s));
+    Level<T> &L0 = H.lv[0];
+    unsigned g = grid_for(nk);
+    if (bnorm_override) G2P_CUDA(cudaMemcpyAsync(K.bnorm, bnorm_override, sizeof(double) * k, cudaMemcpyDeviceToDevice, s));
+    else colnorms<T>(b, n, k, K.partial, K.bnorm, s);
+    int it = 0;
+    rep.converged = false;
+    double *dots2 = K.hcol + (int64_t)k * (m + 1);
+    for (;;) {
+        // r = b - A x ; beta = ||r||
+        spmm_b<T>(A, L0.long_rows, L0.nlong, x, K.r, k, b, s);
+        colnorms<T>(K.r, n, k, K.partial, K.beta, s);
+        G2P_CUDA(cudaMemcpyAsync(K.h_est, K.beta, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+        G2P_CUDA(cudaMemcpyAsync(K.h_est + k, K.bnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
+        double worst = 0;
+        for (int r = 0; r < k; r++) {
+            double bn = K.h_est[k + r];
+            double rel = bn > 0 ? K.h_est[r] / bn : 0.0;
+            worst = std::max(worst, rel);
+        }
+        rep.rel_residual = worst;
+        if (worst <= cfg.rtol) { rep.converged = true; break; }
+        if (it >= cfg.maxit) break;
+        k_start<T><<<g, kThreads, 0, s>>>(nk, k, K.r, K.beta, K.V);
+        k_g_init<<<(k + 63) / 64, 64, 0, s>>>(k, m, K.beta, K.g);
+        int j = 0;
+        for (; j < m && it < cfg.maxit; j++) {
+            T *Vj = K.V + (int64_t)j * nk, *Zj = K.Z + (int64_t)j * nk;
+            // Z_j = M^-1 V_j (one V-cycle)
+            G2P_CUDA(cudaMemcpyAsync(L0.b, Vj, sizeof(T) * nk, cudaMemcpyDeviceToDevice, s));
+            vcycle<T>(H, cfg, 0, k, s);
+            G2P_CUDA(cudaMemcpyAsync(Zj, L0.x, sizeof(T) * nk, cudaMemcpyDeviceToDevice, s));
+            spmm<T>(A, L0.long_rows, L0.nlong, Zj, K.w, k, s);
+            // classical Gram-Schmidt, optionally twice
+            mdot<T>(K.V, n, j + 1, K.w, k, K.partial, K.hcol, s);
+            k_maxpy<T><<<g, kThreads, 0, s>>>(K.V, nk, j + 1, K.hcol, k, K.w);
+            if (cfg.reorth) {
+                mdot<T>(K.V, n, j + 1, K.w, k, K.partial, dots2, s);
+                k_maxpy<T><<<g, kThreads, 0, s>>>(K.V, nk, j + 1, dots2, k, K.w);
+                k_add_vec<<<((j + 1) * k + 255) / 256, 256, 0, s>>>(K.hcol, dots2, (j + 1) * k);
+            }
+            double *hnorm = K.beta;   // reuse
+            colnorms<T>(K.w, n, k, K.partial, hnorm, s);
+            k_arnoldi_finish<T><<<g, kThreads, 0, s>>>(nk, k, hnorm, K.w, K.V + (int64_t)(j + 1) * nk);
+            double *est = K.y;        // scratch for the estimates (k values)
+            k_givens<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.hcol, hnorm, K.H, K.cs, K.sn, K.g, K.bnorm, est);
+            G2P_CUDA(cudaMemcpyAsync(K.h_est, est, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+            G2P_CUDA(cudaStreamSynchronize(s));
+            it++;
+            double worst = 0;
+            for (int r = 0; r < k; r++) worst = std::max(worst, K.h_est[r]);
+            if (worst <= cfg.rtol) { j++; break; }
+        }
+        k_backsolve<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.H, K.g, K.y);
+        k_xupdate<T><<<g, kThreads, 0, s>>>(nk, k, m, j, K.Z, K.y, x);
+    }
+    rep.iterations = it;
+    G2P_CUDA(cudaGetLastError());
+    return G2P_OK;
+}
+template g2p_status fgmres<double>(const Csr<double> &, Hierarchy<double> &, Krylov<double> &, const double *, double *,
+                                   int, const SolverConfig &, const double *, cudaStream_t, SolveReport &);
+template g2p_status fgmres<float>(const Csr<float> &, Hierarchy<float> &, Krylov<float> &, const float *, float *, int,
+                                  const SolverConfig &, const double *, cudaStream_t, SolveReport &);
+
+}  // namespace g2p

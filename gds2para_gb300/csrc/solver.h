@@ -1,0 +1,117 @@
+// Device AMG-preconditioned flexible GMRES: the hypreSolve replacement.
+#pragma once
+#include <vector>
+#include "internal.h"
+
+namespace g2p {
+
+// Multi-RHS vectors are row-interleaved: x[i * k + r].
+template <class T>
+struct Level {
+    int64_t n = 0, nc = 0;
+    Csr<T> A;                   // operator in working precision
+    int32_t *long_rows = nullptr;  // rows with > kLongRow entries
+    int64_t nlong = 0;
+    T *dinv = nullptr;          // 1 / a_ii
+    double lmax = 2.0;          // spectral radius estimate of D^-1 A
+    int32_t *agg = nullptr;     // aggregate of each row (-1: none)
+    int64_t *rptr = nullptr;    // aggregate -> members (ascending)
+    int32_t *rmem = nullptr;
+    T *x = nullptr, *b = nullptr, *t0 = nullptr, *t1 = nullptr, *d = nullptr;
+};
+
+struct SolverConfig {
+    int restart = 30;
+    int maxit = 300;
+    double rtol = 1e-10;
+    int degree = 2;
+    int coarse_size = 256;
+    double strength = 0.08;
+    int max_levels = 20;
+    double cheb_ratio = 0.1;     // lower Chebyshev bound = ratio * lmax
+    bool reorth = true;
+};
+
+template <class T>
+struct Hierarchy {
+    std::vector<Level<T>> lv;
+    double *cinv = nullptr;     // coarsest inverse (FP64, row-major)
+    int64_t nc = 0;
+    int kcap = 0;               // RHS capacity of the work vectors
+    void release(cudaStream_t s);
+};
+
+// FP64 hierarchy built from A64 (device CSR); an FP32 copy can be derived.
+g2p_status amg_setup(const Csr<double> &A, const SolverConfig &cfg, cudaStream_t s, int64_t *scan_work_holder,
+                     Hierarchy<double> &H);
+g2p_status amg_to_float(const Hierarchy<double> &H, cudaStream_t s, Hierarchy<float> &F);
+
+template <class T>
+struct Krylov {
+    int64_t n = 0;
+    int k = 0, m = 0;
+    T *V = nullptr, *Z = nullptr, *w = nullptr, *r = nullptr;
+    double *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr;
+    double *beta = nullptr, *bnorm = nullptr, *partial = nullptr, *hcol = nullptr;
+    double *h_est = nullptr;    // pinned host copy of residual estimates
+    void release(cudaStream_t s);
+};
+
+struct SolveReport {
+    int iterations = 0;
+    double rel_residual = 0.0;
+    bool converged = false;
+};
+
+// FGMRES(m) right-preconditioned by one V-cycle per iteration, for k right-
+// hand sides at once.  x holds the initial guess on entry.
+template <class T>
+g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T *x, int k, const SolverConfig &cfg,
+                  const double *bnorm_override, cudaStream_t s, SolveReport &rep);
+
+template <class T>
+g2p_status krylov_alloc(Krylov<T> &K, int64_t n, int k, int m, cudaStream_t s);
+template <class T>
+g2p_status hierarchy_reserve(Hierarchy<T> &H, int k, cudaStream_t s);
+
+// y = A x for k interleaved right-hand sides (FP64 or FP32).
+template <class T>
+void spmm(const Csr<T> &A, const int32_t *long_rows, int64_t nlong, const T *x, T *y, int k, cudaStream_t s);
+// r = b - A x (FP64)
+void residual64(const Csr<double> &A, const int32_t *long_rows, int64_t nlong, const double *b, const double *x,
+                double *r, int k, cudaStream_t s);
+// per-column 2-norms of an n x k interleaved block into out[k] (device)
+template <class T>
+void colnorms(const T *x, int64_t n, int k, double *partial, double *out, cudaStream_t s);
+
+g2p_status find_long_rows(const Csr<double> &A, int32_t **rows, int64_t *nlong, cudaStream_t s);
+
+constexpr int kLongRow = 64;
+
+}  // namespace g2p
+
+struct g2p_solver {
+    cudaStream_t stream = nullptr;
+    bool owns_stream = false;
+    g2p::SolverConfig cfg;
+    int precision = 0;
+    int inner_maxit = 60;
+    double inner_rtol = 1e-4;
+    g2p::Csr<double> A;                 // original FP64 operator
+    int32_t *long_rows = nullptr;
+    int64_t nlong = 0;
+    double *scale = nullptr;            // diagonal equilibration (mixed)
+    g2p::Csr<double> As;                // scaled operator (mixed, FP64 for setup)
+    g2p::Hierarchy<double> H64;
+    g2p::Hierarchy<float> H32;
+    g2p::Krylov<double> K64;
+    g2p::Krylov<float> K32;
+    int kcap = 0;
+    // work
+    double *xb = nullptr, *bb = nullptr, *rb = nullptr;
+    float *rf = nullptr, *df = nullptr;
+    int64_t *scan_work = nullptr;
+    double setup_ms = 0;
+    int levels = 0;
+    int64_t coarse_rows = 0;
+};

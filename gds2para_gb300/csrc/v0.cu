@@ -1,0 +1,758 @@
+// V0 bases and the node Laplacians Ad, Ac (a10-a13).
+//
+// merge_v0d1 (fdtd.hpp:1823-2774) with the block sizes paraGenerator uses
+// (0; matrixCon.cpp:35-40) gives one column per dielectric node off the PEC
+// planes, in node order, with entries on its <= 6 incident edges (V0d1),
+// then one column per non-reference conductor with entries on its dielectric
+// boundary edges in node order (V0d2).  merge_v0c (fdtd.hpp:2866-3479) gives
+// one column per conductor node, conductor by conductor, dropping the last
+// node of every non-reference conductor and the PEC-plane nodes of reference
+// and passive conductors.  generateAd / generateAc (fdtd.hpp:2778-2862,
+// 3481-3574) accumulate each column's entries through the other endpoint's
+// column; the Ad rows of conductor columns, which can hold 10^4-10^5 entries,
+// go through a stable radix sort so every (row, column) sum still runs in
+// the reference's entry order.
+//
+// Compiled without FMA contraction so values match the reference bit for bit.
+#include <vector>
+
+#include "internal.h"
+#include "primitives.cuh"
+
+g2p_status g2p_run_index_maps(g2p_mesh *m);
+g2p_status g2p_build_rowptr(g2p_mesh *m, int64_t *rowlen, int64_t n, int64_t **ptr_out, int64_t *nnz_out);
+g2p_status g2p_export_csr(g2p_mesh *m, const g2p::Csr<double> &A, int64_t *row, int64_t *col, double *val);
+namespace g2p { g2p_status ensure_scan_work(g2p_mesh *m, int64_t n); }
+
+namespace g2p {
+
+struct V0Ctx {
+    Dims d;
+    const double *xn, *yn, *zn, *epsn, *sign;
+    const int32_t *mark_node, *mark_edge, *mark_port;
+    const uint8_t *pec_node;
+    double LX, LY, LZ, eps0;
+};
+
+// One incident edge of a node, in the reference's order (lower z, upper z,
+// left x, right x, front y, back y).
+struct Inc {
+    int64_t e, other;
+    double val, aval, area;   // +-1/h, +-1/l_avg, +-area-weighted (V0d2)
+};
+
+__device__ __forceinline__ void node_ijk(const Dims &d, int64_t n, int64_t &iz, int64_t &ix, int64_t &iy) {
+    iz = n / d.N_node_s;
+    int64_t r = n - iz * d.N_node_s;
+    ix = r / (d.Ny + 1);
+    iy = r - ix * (d.Ny + 1);
+}
+
+// avg_length (fdtd.hpp:4074-4104)
+__device__ __forceinline__ void avg_len(const V0Ctx &c, int64_t iz, int64_t iy, int64_t ix, double &lx, double &ly,
+                                        double &lz) {
+    const Dims &d = c.d;
+    if (iz == 0) lz = c.zn[1] - c.zn[0];
+    else if (iz == d.nz - 1) lz = c.zn[iz] - c.zn[iz - 1];
+    else lz = (c.zn[iz + 1] - c.zn[iz - 1]) / 2;
+    if (iy == 0) ly = c.yn[1] - c.yn[0];
+    else if (iy == d.ny - 1) ly = c.yn[iy] - c.yn[iy - 1];
+    else ly = (c.yn[iy + 1] - c.yn[iy - 1]) / 2;
+    if (ix == 0) lx = c.xn[1] - c.xn[0];
+    else if (ix == d.nx - 1) lx = c.xn[ix] - c.xn[ix - 1];
+    else lx = (c.xn[ix + 1] - c.xn[ix - 1]) / 2;
+}
+
+__device__ __forceinline__ int incident(const V0Ctx &c, int64_t n, Inc *out) {
+    const Dims &d = c.d;
+    int64_t iz, ix, iy;
+    node_ijk(d, n, iz, ix, iy);
+    double lx, ly, lz;
+    avg_len(c, iz, iy, ix, lx, ly, lz);
+    double W = c.LX * c.LY * c.LZ;
+    int k = 0;
+    if (iz != 0) out[k++] = {(iz - 1) * d.L + d.Ns + ix * (d.Ny + 1) + iy, n - d.N_node_s,
+                             -1 / (c.zn[iz] - c.zn[iz - 1]), -1 / lz, -lx * ly / W};
+    if (iz != d.nz - 1) out[k++] = {iz * d.L + d.Ns + ix * (d.Ny + 1) + iy, n + d.N_node_s,
+                                    1 / (c.zn[iz + 1] - c.zn[iz]), 1 / lz, lx * ly / W};
+    if (ix != 0) out[k++] = {iz * d.L + d.XO + (ix - 1) * (d.Ny + 1) + iy, n - (d.Ny + 1),
+                             -1 / (c.xn[ix] - c.xn[ix - 1]), -1 / lx, -ly * lz / W};
+    if (ix != d.nx - 1) out[k++] = {iz * d.L + d.XO + ix * (d.Ny + 1) + iy, n + (d.Ny + 1),
+                                    1 / (c.xn[ix + 1] - c.xn[ix]), 1 / lx, ly * lz / W};
+    if (iy != 0) out[k++] = {iz * d.L + ix * d.Ny + iy - 1, n - 1, -1 / (c.yn[iy] - c.yn[iy - 1]), -1 / ly,
+                             -lx * lz / W};
+    if (iy != d.ny - 1) out[k++] = {iz * d.L + ix * d.Ny + iy, n + 1, 1 / (c.yn[iy + 1] - c.yn[iy]), 1 / ly,
+                                    lx * lz / W};
+    return k;
+}
+
+__device__ __forceinline__ int node_degree(const Dims &d, int64_t n) {
+    int64_t iz, ix, iy;
+    node_ijk(d, n, iz, ix, iy);
+    return (iz != 0) + (iz != d.nz - 1) + (ix != 0) + (ix != d.nx - 1) + (iy != 0) + (iy != d.ny - 1);
+}
+
+__device__ __forceinline__ bool is_d1(const V0Ctx &c, int64_t n) {
+    if (c.mark_node[n] != 0) return false;
+    int64_t iz = n / c.d.N_node_s;
+    return !((iz == 0 || iz == c.d.nz - 1) && c.pec_node[n]);
+}
+
+// Entry of V0d2 on edge e of conductor node n (fdtd.hpp:2676-2757).
+__device__ __forceinline__ bool d2_edge(const V0Ctx &c, const Inc &in, int32_t me) {
+    return c.mark_edge[in.e] == 0 && c.mark_node[in.other] != me;
+}
+
+// Edge length and layer for the Laplacian terms (generateAd's h and inz).
+__device__ __forceinline__ void edge_geom(const V0Ctx &c, int64_t e, int64_t &n1, int64_t &n2, int64_t &inz, double &h) {
+    int64_t inx, iny;
+    int k = c.d.edge_nodes(e, n1, n2, inz, inx, iny);
+    if (k == 2) h = c.zn[inz + 1] - c.zn[inz];
+    else if (k == 1) h = c.xn[inx + 1] - c.xn[inx];
+    else h = c.yn[iny + 1] - c.yn[iny];
+}
+
+// One V0 entry's contribution to row `col` of Ad (coef = stackEpsn*eps0
+// path, is_ac = 0) or Ac (stackSign, only conductor edges).  Returns the
+// other column (-1 for none) with its value, and the diagonal increment.
+__device__ __forceinline__ bool lap_term(const V0Ctx &c, const int32_t *map, bool is_ac, int64_t e, int64_t col,
+                                         double a, int64_t &other, double &off, double &dg) {
+    if (is_ac && c.mark_edge[e] == 0) return false;
+    int64_t n1, n2, inz;
+    double h;
+    edge_geom(c, e, n1, n2, inz, h);
+    int32_t m1 = map[n1], m2 = map[n2];
+    other = -1;
+    off = 0.0;
+    if (is_ac) {
+        double s = c.sign[inz];
+        if (m1 != col + 1 && m1 != 0) { other = m1 - 1; off = a * 1 / h * s; dg = a * (-1) / h * s; }
+        else if (m2 != col + 1 && m2 != 0) { other = m2 - 1; off = a * (-1) / h * s; dg = a * 1 / h * s; }
+        else dg = fabs(a * 1 / h * s);
+    } else {
+        double ep = c.epsn[inz];
+        if (m1 != col + 1 && m1 != 0) { other = m1 - 1; off = a * 1 / h * ep * c.eps0; dg = a * (-1) / h * ep * c.eps0; }
+        else if (m2 != col + 1 && m2 != 0) { other = m2 - 1; off = a * (-1) / h * ep * c.eps0; dg = a * 1 / h * ep * c.eps0; }
+        else dg = fabs(a * 1 / h * ep * c.eps0);
+    }
+    return true;
+}
+
+// --------------------------------------------------------------- V0d kernels
+// Per conductor: has_entries and entry count of its V0d2 column.
+__global__ void k_d2_count(V0Ctx c, int64_t *cnt, int32_t *bcnt) {
+    const Dims &d = c.d;
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < d.N_node; n += (int64_t)gridDim.x * blockDim.x) {
+        int32_t me = c.mark_node[n];
+        int b = 0;
+        if (me != 0 && c.mark_port[me - 1] != -1) {
+            Inc in[6];
+            int k = incident(c, n, in);
+            for (int t = 0; t < k; t++) b += d2_edge(c, in[t], me);
+            if (b) atomicAdd((unsigned long long *)&cnt[me - 1], (unsigned long long)b);
+        }
+        bcnt[n] = b;
+    }
+}
+
+__global__ void k_cond_flags(int64_t ncdt, const int64_t *cnt, const int32_t *mark_port, int32_t *flags /*[2]*/) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncdt; i += (int64_t)gridDim.x * blockDim.x) {
+        if (mark_port[i] == -1) continue;
+        if (cnt[i] > 0) atomicAdd(&flags[0], 1);
+        else atomicAdd(&flags[1], 1);
+    }
+}
+
+// map for V0d: dielectric nodes -> their column, conductor nodes of
+// non-reference conductors -> the conductor's column.
+__global__ void k_d_map(V0Ctx c, const int32_t *d1col, const int64_t *ccol, int32_t *map) {
+    const Dims &d = c.d;
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < d.N_node; n += (int64_t)gridDim.x * blockDim.x) {
+        int32_t me = c.mark_node[n];
+        int32_t v = 0;
+        if (me == 0) v = is_d1(c, n) ? d1col[n] + 1 : 0;
+        else if (c.mark_port[me - 1] != -1) v = (int32_t)ccol[me - 1] + 1;
+        map[n] = v;
+    }
+}
+
+// V0d1 entries and column pointers.
+__global__ void k_d1_fill(V0Ctx c, const int32_t *d1col, const int64_t *d1off, int64_t *cptr, int32_t *cedge,
+                          double *cval, double *caval) {
+    const Dims &d = c.d;
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < d.N_node; n += (int64_t)gridDim.x * blockDim.x) {
+        if (!is_d1(c, n)) continue;
+        Inc in[6];
+        int k = incident(c, n, in);
+        int64_t o = d1off[n];
+        cptr[d1col[n]] = o;
+        for (int t = 0; t < k; t++) { cedge[o + t] = (int32_t)in[t].e; cval[o + t] = in[t].val; caval[o + t] = in[t].aval; }
+    }
+}
+
+// V0d2 entries: `list` holds conductor nodes grouped by conductor in node
+// order; off[i] is the entry offset of list[i].
+__global__ void k_d2_fill(V0Ctx c, const int32_t *list, int64_t nlist, const int64_t *off, int32_t *cedge,
+                          double *cval, double *caval) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nlist; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t n = list[i];
+        int32_t me = c.mark_node[n];
+        if (c.mark_port[me - 1] == -1) continue;
+        Inc in[6];
+        int k = incident(c, n, in);
+        int64_t o = off[i];
+        for (int t = 0; t < k; t++)
+            if (d2_edge(c, in[t], me)) { cedge[o] = (int32_t)in[t].e; cval[o] = in[t].val; caval[o] = in[t].area; o++; }
+    }
+}
+
+__global__ void k_cond_cptr(int64_t ncdt, const int32_t *mark_port, const int64_t *cnt, const int64_t *ccol,
+                            const int64_t *coff, int64_t *cptr) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncdt; i += (int64_t)gridDim.x * blockDim.x)
+        if (mark_port[i] != -1 && cnt[i] > 0) cptr[ccol[i]] = coff[i];
+}
+
+// --------------------------------------------------------------- V0c kernels
+// list position -> keeps a V0c column? (fdtd.hpp:2900-2912,3106-3110)
+__device__ __forceinline__ bool c_keep(const V0Ctx &c, const int32_t *list, int64_t nlist, int64_t i) {
+    int64_t n = list[i];
+    int32_t me = c.mark_node[n];
+    int mp = c.mark_port[me - 1];
+    bool last = (i + 1 == nlist) || c.mark_node[list[i + 1]] != me;
+    if (mp >= 0 && last) return false;
+    if (mp <= 0 && c.pec_node[n]) return false;
+    return true;
+}
+
+__global__ void k_c_fill(V0Ctx c, const int32_t *list, int64_t nlist, const int32_t *ccolv, const int64_t *coff,
+                         int32_t *map, int64_t *cptr, int32_t *cedge, double *cval, double *caval) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nlist; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!c_keep(c, list, nlist, i)) continue;
+        int64_t n = list[i];
+        Inc in[6];
+        int k = incident(c, n, in);
+        int64_t o = coff[i];
+        int32_t col = ccolv[i];
+        map[n] = col + 1;
+        cptr[col] = o;
+        for (int t = 0; t < k; t++) { cedge[o + t] = (int32_t)in[t].e; cval[o + t] = in[t].val; caval[o + t] = in[t].aval; }
+    }
+}
+
+// ------------------------------------------------------- per-edge V0 views
+// Up to two entries per edge, ascending column: the endpoint columns.
+__global__ void k_edge_view(V0Ctx c, bool is_c, const int32_t *map, const int32_t *d1col, int32_t *ecol, double *eval,
+                            double *eaval) {
+    const Dims &d = c.d;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < d.N_edge; e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t n[2], inz, inx, iny;
+        d.edge_nodes(e, n[0], n[1], inz, inx, iny);
+        int32_t col[2] = {-1, -1};
+        double v[2] = {0, 0}, a[2] = {0, 0};
+        for (int s = 0; s < 2; s++) {
+            int64_t nn = n[s];
+            int32_t me = c.mark_node[nn];
+            bool has = false;
+            int32_t cc = -1;
+            if (is_c) {
+                if (me != 0 && map[nn] != 0) { has = true; cc = map[nn] - 1; }
+            } else if (me == 0) {
+                if (is_d1(c, nn)) { has = true; cc = d1col[nn]; }
+            } else if (c.mark_port[me - 1] != -1 && map[nn] != 0) {
+                int64_t other = n[1 - s];
+                if (c.mark_edge[e] == 0 && c.mark_node[other] != me) { has = true; cc = map[nn] - 1; }
+            }
+            if (!has) continue;
+            Inc in[6];
+            int k = incident(c, nn, in);
+            for (int t = 0; t < k; t++)
+                if (in[t].e == e) {
+                    col[s] = cc;
+                    v[s] = in[t].val;
+                    a[s] = (is_c || me == 0) ? in[t].aval : in[t].area;
+                }
+        }
+        int lo = 0, hi = 1;
+        if (col[0] < 0 || (col[1] >= 0 && col[1] < col[0])) { lo = 1; hi = 0; }
+        ecol[2 * e] = col[lo]; eval[2 * e] = v[lo]; eaval[2 * e] = a[lo];
+        ecol[2 * e + 1] = col[hi]; eval[2 * e + 1] = v[hi]; eaval[2 * e + 1] = a[hi];
+    }
+}
+
+// ----------------------------------------------------------- Laplacian rows
+constexpr int kRowMax = 8;
+
+// Row of a single-node column (V0d1 or V0c): <= 6 entries + diagonal,
+// accumulated in entry order, sorted, optionally filtered |v| > 1e-8.
+__device__ __forceinline__ int short_row(const V0Ctx &c, const int32_t *map, bool is_ac, const int64_t *cptr,
+                                         const int32_t *cedge, const double *caval, int64_t col, int64_t *cols,
+                                         double *vals) {
+    int nr = 0;
+    for (int64_t k = cptr[col]; k < cptr[col + 1]; k++) {
+        int64_t other;
+        double off, dg;
+        if (!lap_term(c, map, is_ac, cedge[k], col, caval[k], other, off, dg)) continue;
+        if (other >= 0) {
+            int q = 0;
+            while (q < nr && cols[q] != other) q++;
+            if (q == nr) { cols[nr] = other; vals[nr] = 0.0; nr++; }
+            vals[q] += off;
+        }
+        int q = 0;
+        while (q < nr && cols[q] != col) q++;
+        if (q == nr) { cols[nr] = col; vals[nr] = 0.0; nr++; }
+        vals[q] += dg;
+    }
+    for (int i = 1; i < nr; i++) {
+        int64_t cc = cols[i]; double v = vals[i];
+        int j = i - 1;
+        while (j >= 0 && cols[j] > cc) { cols[j + 1] = cols[j]; vals[j + 1] = vals[j]; j--; }
+        cols[j + 1] = cc; vals[j + 1] = v;
+    }
+    if (!is_ac) {
+        int w = 0;
+        for (int i = 0; i < nr; i++)
+            if (fabs(vals[i]) > 1e-8) { cols[w] = cols[i]; vals[w] = vals[i]; w++; }
+        nr = w;
+    }
+    return nr;
+}
+
+__global__ void k_short_rows_count(V0Ctx c, const int32_t *map, bool is_ac, const int64_t *cptr, const int32_t *cedge,
+                                   const double *caval, int64_t nrows, int64_t *rowlen) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
+        int64_t cols[kRowMax];
+        double vals[kRowMax];
+        rowlen[r] = short_row(c, map, is_ac, cptr, cedge, caval, r, cols, vals);
+    }
+}
+
+__global__ void k_short_rows_fill(V0Ctx c, const int32_t *map, bool is_ac, const int64_t *cptr, const int32_t *cedge,
+                                  const double *caval, int64_t nrows, const int64_t *rowptr, int32_t *col, double *val) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
+        int64_t cols[kRowMax];
+        double vals[kRowMax];
+        int nr = short_row(c, map, is_ac, cptr, cedge, caval, r, cols, vals);
+        int64_t o = rowptr[r];
+        for (int q = 0; q < nr; q++) { col[o + q] = (int32_t)cols[q]; val[o + q] = vals[q]; }
+    }
+}
+
+// Long (conductor) rows of Ad: every entry emits (row, col) keys with values
+// in entry order; a stable sort by key and an ordered per-key sum follow.
+__global__ void k_long_terms(V0Ctx c, const int32_t *map, const int64_t *cptr, const int32_t *cedge,
+                             const double *caval, int64_t row0, int64_t nrows, int64_t ncolall, const int64_t *toff,
+                             uint64_t *keys, double *vals) {
+    int64_t k0 = cptr[row0];
+    int64_t nent = cptr[row0 + nrows] - k0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nent; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t k = k0 + t;
+        // row of entry k: binary search in cptr[row0 .. row0+nrows]
+        int64_t lo = row0, hi = row0 + nrows - 1;
+        while (lo < hi) {
+            int64_t mid = (lo + hi + 1) >> 1;
+            if (cptr[mid] <= k) lo = mid; else hi = mid - 1;
+        }
+        int64_t row = lo;
+        int64_t other;
+        double off, dg;
+        lap_term(c, map, false, cedge[k], row, caval[k], other, off, dg);
+        int64_t o = toff[t];
+        if (other >= 0) { keys[o] = (uint64_t)(row - row0) * (uint64_t)ncolall + (uint64_t)other; vals[o] = off; o++; }
+        keys[o] = (uint64_t)(row - row0) * (uint64_t)ncolall + (uint64_t)row;
+        vals[o] = dg;
+    }
+}
+
+__global__ void k_long_nterms(V0Ctx c, const int32_t *map, const int64_t *cptr, const int32_t *cedge,
+                              const double *caval, int64_t row0, int64_t nrows, int64_t *nt) {
+    int64_t k0 = cptr[row0];
+    int64_t nent = cptr[row0 + nrows] - k0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nent; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t k = k0 + t;
+        int64_t lo = row0, hi = row0 + nrows - 1;
+        while (lo < hi) {
+            int64_t mid = (lo + hi + 1) >> 1;
+            if (cptr[mid] <= k) lo = mid; else hi = mid - 1;
+        }
+        int64_t other;
+        double off, dg;
+        lap_term(c, map, false, cedge[k], lo, caval[k], other, off, dg);
+        nt[t] = other >= 0 ? 2 : 1;
+    }
+}
+
+// Segment heads of sorted keys: head[i] = 1 when keys[i] starts a new key.
+__global__ void k_heads(const uint64_t *keys, int64_t n, int64_t *head) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        head[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+// Ordered sum of each key's values; keeps |v| > 1e-8 (fdtd.hpp:2852).
+__global__ void k_seg_sum(const uint64_t *keys, const double *vals, int64_t n, const int64_t *segid, int64_t ncolall,
+                          uint64_t *okey, double *oval, int64_t *keep) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!(i == 0 || keys[i] != keys[i - 1])) continue;
+        double s = 0.0;
+        int64_t j = i;
+        while (j < n && keys[j] == keys[i]) { s += vals[j]; j++; }
+        int64_t sg = segid[i];
+        okey[sg] = keys[i];
+        oval[sg] = s;
+        keep[sg] = fabs(s) > 1e-8 ? 1 : 0;
+    }
+}
+
+__global__ void k_long_rowlen(const uint64_t *okey, const int64_t *keep, int64_t nseg, int64_t ncolall, int64_t *rowlen) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nseg; i += (int64_t)gridDim.x * blockDim.x)
+        if (keep[i]) atomicAdd((unsigned long long *)&rowlen[okey[i] / (uint64_t)ncolall], 1ull);
+}
+
+__global__ void k_long_scatter(const uint64_t *okey, const double *oval, const int64_t *keep, const int64_t *kpos,
+                               int64_t nseg, int64_t ncolall, int64_t row0, const int64_t *rowptr, int64_t rowbase,
+                               int32_t *col, double *val) {
+    // kept segments are in (row, col) order, so position = rowptr[row0] + rank
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nseg; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!keep[i]) continue;
+        int64_t o = rowptr[row0] - rowbase + kpos[i];
+        col[o] = (int32_t)(okey[i] % (uint64_t)ncolall);
+        val[o] = oval[i];
+    }
+}
+
+__global__ void k_add_i64(int64_t *a, int64_t n, int64_t v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] += v;
+}
+
+}  // namespace g2p
+
+using namespace g2p;
+
+static V0Ctx make_ctx(g2p_mesh *m) {
+    V0Ctx c;
+    c.d = m->d;
+    c.xn = m->xn; c.yn = m->yn; c.zn = m->zn; c.epsn = m->epsn; c.sign = m->sign;
+    c.mark_node = m->mark_node; c.mark_edge = m->mark_edge; c.mark_port = m->mark_port;
+    c.pec_node = m->pec_node;
+    const Dims &d = m->d;
+    c.LX = (m->h_xn[d.nx - 1] - m->h_xn[0]) / (d.nx - 1);
+    c.LY = (m->h_yn[d.ny - 1] - m->h_yn[0]) / (d.ny - 1);
+    c.LZ = (m->h_zn[d.nz - 1] - m->h_zn[0]) / (d.nz - 1);
+    c.eps0 = m->k.eps0;
+    return c;
+}
+
+static int bits_for(uint64_t v) {
+    int b = 0;
+    while (b < 64 && (v >> b) != 0) b++;
+    return b < 8 ? 8 : ((b + 7) / 8) * 8;
+}
+
+// Builds one Laplacian (Ad when is_ac false) from a V0 basis; rows [0, nshort)
+// are single-node columns, rows [nshort, ncol) conductor columns.
+static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool is_ac, int64_t nshort, Csr<double> &A) {
+    cudaStream_t s = m->stream;
+    int64_t ncol = B.ncol;
+    int64_t nlong = ncol - nshort;
+    int64_t *rowlen;
+    G2P_TRY(dalloc(&rowlen, ncol + 1, s));
+    G2P_CUDA(cudaMemsetAsync(rowlen, 0, sizeof(int64_t) * (ncol + 1), s));
+    if (nshort > 0)
+        k_short_rows_count<<<grid_for(nshort), kThreads, 0, s>>>(c, B.map, is_ac, B.cptr, B.cedge, B.caval, nshort, rowlen);
+    // long rows through sort + ordered reduce
+    uint64_t *okey = nullptr;
+    double *oval = nullptr;
+    int64_t *keep = nullptr, *kpos = nullptr;
+    int64_t nseg = 0;
+    if (nlong > 0) {
+        int64_t h_ent[2];
+        G2P_CUDA(cudaMemcpyAsync(h_ent, B.cptr + nshort, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        G2P_CUDA(cudaMemcpyAsync(h_ent + 1, B.cptr + ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
+        int64_t nent = h_ent[1] - h_ent[0];
+        int64_t *nt, *toff;
+        G2P_TRY(dalloc(&nt, nent + 1, s));
+        G2P_TRY(dalloc(&toff, nent + 1, s));
+        if (nent > 0)
+            k_long_nterms<<<grid_for(nent), kThreads, 0, s>>>(c, B.map, B.cptr, B.cedge, B.caval, nshort, nlong, nt);
+        G2P_TRY(ensure_scan_work(m, nent + 1));
+        const int64_t *ntp = nt;
+        auto op = [ntp, nent] __device__(int64_t i) -> int64_t { return i < nent ? ntp[i] : 0; };
+        G2P_TRY(exclusive_scan(op, nent + 1, toff, m->scan_work, s));
+        int64_t nterm = 0;
+        G2P_CUDA(cudaMemcpyAsync(&nterm, toff + nent, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
+        uint64_t *k0, *k1;
+        double *v0, *v1;
+        G2P_TRY(dalloc(&k0, nterm, s)); G2P_TRY(dalloc(&k1, nterm, s));
+        G2P_TRY(dalloc(&v0, nterm, s)); G2P_TRY(dalloc(&v1, nterm, s));
+        if (nent > 0)
+            k_long_terms<<<grid_for(nent), kThreads, 0, s>>>(c, B.map, B.cptr, B.cedge, B.caval, nshort, nlong, ncol, toff,
+                                                             k0, v0);
+        dfree(nt, s); dfree(toff, s);
+        int64_t *counts;
+        G2P_TRY(dalloc(&counts, sort_counts_size(nterm), s));
+        G2P_TRY(ensure_scan_work(m, sort_counts_size(nterm)));
+        bool in1 = false;
+        G2P_TRY(radix_sort_pairs(k0, v0, k1, v1, nterm, bits_for((uint64_t)nlong * (uint64_t)ncol), counts,
+                                 m->scan_work, &in1, s));
+        dfree(counts, s);
+        uint64_t *sk = in1 ? k1 : k0;
+        double *sv = in1 ? v1 : v0;
+        int64_t *head, *segid;
+        G2P_TRY(dalloc(&head, nterm + 1, s));
+        G2P_TRY(dalloc(&segid, nterm + 1, s));
+        k_heads<<<grid_for(nterm), kThreads, 0, s>>>(sk, nterm, head);
+        G2P_TRY(ensure_scan_work(m, nterm + 1));
+        const int64_t *hp = head;
+        auto hop = [hp, nterm] __device__(int64_t i) -> int64_t { return i < nterm ? hp[i] : 0; };
+        G2P_TRY(exclusive_scan(hop, nterm + 1, segid, m->scan_work, s));
+        G2P_CUDA(cudaMemcpyAsync(&nseg, segid + nterm, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
+        G2P_TRY(dalloc(&okey, nseg, s)); G2P_TRY(dalloc(&oval, nseg, s));
+        G2P_TRY(dalloc(&keep, nseg + 1, s)); G2P_TRY(dalloc(&kpos, nseg + 1, s));
+        k_seg_sum<<<grid_for(nterm), kThreads, 0, s>>>(sk, sv, nterm, segid, ncol, okey, oval, keep);
+        k_long_rowlen<<<grid_for(nseg), kThreads, 0, s>>>(okey, keep, nseg, ncol, rowlen + nshort);
+        const int64_t *kp = keep;
+        auto kop = [kp, nseg] __device__(int64_t i) -> int64_t { return i < nseg ? kp[i] : 0; };
+        G2P_TRY(ensure_scan_work(m, nseg + 1));
+        G2P_TRY(exclusive_scan(kop, nseg + 1, kpos, m->scan_work, s));
+        dfree(head, s); dfree(segid, s);
+        dfree(k0, s); dfree(k1, s); dfree(v0, s); dfree(v1, s);
+    }
+    int64_t nnz = 0;
+    G2P_TRY(g2p_build_rowptr(m, rowlen, ncol, &A.ptr, &nnz));
+    dfree(rowlen, s);
+    A.n = A.m = ncol;
+    A.nnz = nnz;
+    G2P_TRY(dalloc(&A.col, nnz, s));
+    G2P_TRY(dalloc(&A.val, nnz, s));
+    if (nshort > 0)
+        k_short_rows_fill<<<grid_for(nshort), kThreads, 0, s>>>(c, B.map, is_ac, B.cptr, B.cedge, B.caval, nshort, A.ptr,
+                                                                A.col, A.val);
+    if (nlong > 0) {
+        k_long_scatter<<<grid_for(nseg), kThreads, 0, s>>>(okey, oval, keep, kpos, nseg, ncol, nshort, A.ptr, 0, A.col,
+                                                           A.val);
+        dfree(okey, s); dfree(oval, s); dfree(keep, s); dfree(kpos, s);
+    }
+    G2P_CUDA(cudaGetLastError());
+    G2P_CUDA(cudaStreamSynchronize(s));
+    return G2P_OK;
+}
+
+__global__ void k_is_cond_node(const int32_t *mark_node, int64_t n, int64_t *flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        flag[i] = mark_node[i] != 0;
+}
+
+__global__ void k_compact_cond(const int32_t *mark_node, int64_t n, const int64_t *pos, uint32_t *key, int32_t *node) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (mark_node[i] != 0) { key[pos[i]] = (uint32_t)mark_node[i]; node[pos[i]] = (int32_t)i; }
+}
+
+g2p_status g2p_run_v0(g2p_mesh *m) {
+    if (m->v0_done) return G2P_OK;
+    G2P_TRY(g2p_run_index_maps(m));
+    const Dims &d = m->d;
+    cudaStream_t s = m->stream;
+    V0Ctx c = make_ctx(m);
+    const int64_t ncdt = m->num_cdt;
+    // ---- conductor node lists grouped by conductor, node order kept
+    int64_t *pos;
+    G2P_TRY(dalloc(&pos, d.N_node + 1, s));
+    G2P_TRY(ensure_scan_work(m, d.N_node + 1));
+    const int32_t *mn = m->mark_node;
+    int64_t NN = d.N_node;
+    auto cop = [mn, NN] __device__(int64_t i) -> int64_t { return i < NN ? (mn[i] != 0) : 0; };
+    G2P_TRY(exclusive_scan(cop, NN + 1, pos, m->scan_work, s));
+    int64_t ncn = 0;
+    G2P_CUDA(cudaMemcpyAsync(&ncn, pos + NN, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    uint32_t *ck0, *ck1;
+    int32_t *cn0, *cn1;
+    G2P_TRY(dalloc(&ck0, ncn, s)); G2P_TRY(dalloc(&ck1, ncn, s));
+    G2P_TRY(dalloc(&cn0, ncn, s)); G2P_TRY(dalloc(&cn1, ncn, s));
+    k_compact_cond<<<grid_for(NN), kThreads, 0, s>>>(mn, NN, pos, ck0, cn0);
+    dfree(pos, s);
+    int64_t *counts;
+    G2P_TRY(dalloc(&counts, sort_counts_size(ncn), s));
+    G2P_TRY(ensure_scan_work(m, sort_counts_size(ncn)));
+    bool in1 = false;
+    G2P_TRY(radix_sort_pairs(ck0, cn0, ck1, cn1, ncn, bits_for((uint64_t)ncdt + 1), counts, m->scan_work, &in1, s));
+    dfree(counts, s);
+    int32_t *list = in1 ? cn1 : cn0;
+    dfree(ck0, s); dfree(ck1, s);
+    if (in1) dfree(cn0, s); else dfree(cn1, s);
+
+    // ---- V0d numbering
+    int64_t *cnt, *ccol, *coff;
+    int32_t *bcnt, *flags, *d1col;
+    int64_t *d1off;
+    G2P_TRY(dalloc(&cnt, ncdt + 1, s));
+    G2P_TRY(dalloc(&ccol, ncdt + 1, s));
+    G2P_TRY(dalloc(&coff, ncdt + 1, s));
+    G2P_TRY(dalloc(&bcnt, NN, s));
+    G2P_TRY(dalloc(&flags, 2, s));
+    G2P_TRY(dalloc(&d1col, NN + 1, s));
+    G2P_TRY(dalloc(&d1off, NN + 1, s));
+    G2P_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (ncdt + 1), s));
+    G2P_CUDA(cudaMemsetAsync(flags, 0, sizeof(int32_t) * 2, s));
+    k_d2_count<<<grid_for(NN), kThreads, 0, s>>>(c, cnt, bcnt);
+    k_cond_flags<<<grid_for(ncdt), kThreads, 0, s>>>(ncdt, cnt, m->mark_port, flags);
+    int32_t hflags[2];
+    G2P_CUDA(cudaMemcpyAsync(hflags, flags, sizeof(hflags), cudaMemcpyDeviceToHost, s));
+    // dielectric columns and their entry offsets
+    V0Ctx cc = c;
+    auto d1op = [cc, NN] __device__(int64_t i) -> int64_t { return i < NN ? (is_d1(cc, i) ? 1 : 0) : 0; };
+    G2P_TRY(exclusive_scan(d1op, NN + 1, d1col, m->scan_work, s));
+    auto degop = [cc, NN] __device__(int64_t i) -> int64_t { return i < NN ? (is_d1(cc, i) ? node_degree(cc.d, i) : 0) : 0; };
+    G2P_TRY(exclusive_scan(degop, NN + 1, d1off, m->scan_work, s));
+    int32_t nd1 = 0;
+    int64_t nnz_d1 = 0;
+    G2P_CUDA(cudaMemcpyAsync(&nd1, d1col + NN, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaMemcpyAsync(&nnz_d1, d1off + NN, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    if (hflags[1] > 0) {
+        set_last_message("%d non-reference conductor(s) have no dielectric boundary edge; the reference's V0d2 "
+                         "numbering (fdtd.hpp:2424-2759) is inconsistent for such layouts", hflags[1]);
+        return G2P_ERR_UNSUPPORTED;
+    }
+    // conductor columns: nd1 + rank among conductors with entries
+    const int64_t *cntp = cnt;
+    const int32_t *mpp = m->mark_port;
+    auto ccop = [cntp, mpp, ncdt] __device__(int64_t i) -> int64_t {
+        return i < ncdt ? ((mpp[i] != -1 && cntp[i] > 0) ? 1 : 0) : 0;
+    };
+    G2P_TRY(exclusive_scan(ccop, ncdt + 1, ccol, m->scan_work, s));
+    auto cnop = [cntp, mpp, ncdt] __device__(int64_t i) -> int64_t {
+        return i < ncdt ? ((mpp[i] != -1) ? cntp[i] : 0) : 0;
+    };
+    G2P_TRY(exclusive_scan(cnop, ncdt + 1, coff, m->scan_work, s));
+    int64_t nd2 = 0, nnz_d2 = 0;
+    G2P_CUDA(cudaMemcpyAsync(&nd2, ccol + ncdt, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaMemcpyAsync(&nnz_d2, coff + ncdt, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    k_add_i64<<<grid_for(ncdt), kThreads, 0, s>>>(ccol, ncdt, nd1);
+    V0Basis &Vd = m->v0d;
+    Vd.ncol = nd1 + nd2;
+    Vd.nnz = nnz_d1 + nnz_d2;
+    G2P_TRY(dalloc(&Vd.cptr, Vd.ncol + 1, s));
+    G2P_TRY(dalloc(&Vd.cedge, Vd.nnz, s));
+    G2P_TRY(dalloc(&Vd.cval, Vd.nnz, s));
+    G2P_TRY(dalloc(&Vd.caval, Vd.nnz, s));
+    G2P_TRY(dalloc(&Vd.map, NN, s));
+    k_d_map<<<grid_for(NN), kThreads, 0, s>>>(c, d1col, ccol, Vd.map);
+    k_d1_fill<<<grid_for(NN), kThreads, 0, s>>>(c, d1col, d1off, Vd.cptr, Vd.cedge, Vd.cval, Vd.caval);
+    k_add_i64<<<grid_for(ncdt), kThreads, 0, s>>>(coff, ncdt, nnz_d1);
+    k_cond_cptr<<<grid_for(ncdt), kThreads, 0, s>>>(ncdt, m->mark_port, cnt, ccol, coff, Vd.cptr);
+    G2P_CUDA(cudaMemcpyAsync(Vd.cptr + Vd.ncol, &Vd.nnz, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    int64_t *loff;
+    G2P_TRY(dalloc(&loff, ncn + 1, s));
+    G2P_TRY(ensure_scan_work(m, ncn + 1));
+    {
+        const int32_t *lp = list, *bp = bcnt;
+        auto bop = [lp, bp, ncn] __device__(int64_t i) -> int64_t { return i < ncn ? bp[lp[i]] : 0; };
+        G2P_TRY(exclusive_scan(bop, ncn + 1, loff, m->scan_work, s));
+    }
+    k_add_i64<<<grid_for(ncn), kThreads, 0, s>>>(loff, ncn, nnz_d1);
+    k_d2_fill<<<grid_for(ncn), kThreads, 0, s>>>(c, list, ncn, loff, Vd.cedge, Vd.cval, Vd.caval);
+    dfree(cnt, s); dfree(ccol, s); dfree(coff, s); dfree(bcnt, s); dfree(flags, s); dfree(d1off, s);
+
+    // ---- V0c
+    V0Basis &Vc = m->v0c;
+    int32_t *ccolv;
+    int64_t *coffv;
+    G2P_TRY(dalloc(&ccolv, ncn + 1, s));
+    G2P_TRY(dalloc(&coffv, ncn + 1, s));
+    {
+        V0Ctx c2 = c;
+        const int32_t *lp = list;
+        auto kop = [c2, lp, ncn] __device__(int64_t i) -> int64_t { return i < ncn ? (c_keep(c2, lp, ncn, i) ? 1 : 0) : 0; };
+        G2P_TRY(exclusive_scan(kop, ncn + 1, ccolv, m->scan_work, s));
+        auto dop = [c2, lp, ncn] __device__(int64_t i) -> int64_t {
+            return i < ncn ? (c_keep(c2, lp, ncn, i) ? node_degree(c2.d, lp[i]) : 0) : 0;
+        };
+        G2P_TRY(exclusive_scan(dop, ncn + 1, coffv, m->scan_work, s));
+    }
+    int32_t ncc = 0;
+    int64_t nnz_c = 0;
+    G2P_CUDA(cudaMemcpyAsync(&ncc, ccolv + ncn, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaMemcpyAsync(&nnz_c, coffv + ncn, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    Vc.ncol = ncc;
+    Vc.nnz = nnz_c;
+    G2P_TRY(dalloc(&Vc.cptr, Vc.ncol + 1, s));
+    G2P_TRY(dalloc(&Vc.cedge, Vc.nnz, s));
+    G2P_TRY(dalloc(&Vc.cval, Vc.nnz, s));
+    G2P_TRY(dalloc(&Vc.caval, Vc.nnz, s));
+    G2P_TRY(dalloc(&Vc.map, NN, s));
+    G2P_CUDA(cudaMemsetAsync(Vc.map, 0, sizeof(int32_t) * NN, s));
+    k_c_fill<<<grid_for(ncn), kThreads, 0, s>>>(c, list, ncn, ccolv, coffv, Vc.map, Vc.cptr, Vc.cedge, Vc.cval, Vc.caval);
+    G2P_CUDA(cudaMemcpyAsync(Vc.cptr + Vc.ncol, &Vc.nnz, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    dfree(ccolv, s); dfree(coffv, s); dfree(list, s); dfree(loff, s);
+
+    // ---- per-edge views
+    for (int which = 0; which < 2; which++) {
+        V0Basis &B = which ? Vc : Vd;
+        G2P_TRY(dalloc(&B.ecol, 2 * d.N_edge, s));
+        G2P_TRY(dalloc(&B.eval, 2 * d.N_edge, s));
+        G2P_TRY(dalloc(&B.eaval, 2 * d.N_edge, s));
+        k_edge_view<<<grid_for(d.N_edge), kThreads, 0, s>>>(c, which == 1, B.map, d1col, B.ecol, B.eval, B.eaval);
+    }
+    G2P_CUDA(cudaGetLastError());
+    // ---- Laplacians
+    G2P_TRY(build_laplacian(m, c, Vd, false, nd1, m->Ad));
+    G2P_TRY(build_laplacian(m, c, Vc, true, Vc.ncol, m->Ac));
+    dfree(d1col, s);
+    G2P_CUDA(cudaStreamSynchronize(s));
+    m->v0_done = true;
+    return G2P_OK;
+}
+
+extern "C" g2p_status g2p_assemble_v0(g2p_mesh *m, g2p_sizes *out) {
+    if (!m) return G2P_ERR_INVALID;
+    G2P_TRY(g2p_run_v0(m));
+    if (out) G2P_TRY(g2p_mesh_sizes(m, out));
+    return G2P_OK;
+}
+
+__global__ void k_v0_export(const int64_t *cptr, int64_t ncol, const int32_t *cedge, int64_t *row, int64_t *col) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncol; c += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t k = cptr[c]; k < cptr[c + 1]; k++) { row[k] = cedge[k]; col[k] = c; }
+}
+
+__global__ void k_map_export(const int32_t *map, int64_t n, int64_t *out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = map[i];
+}
+
+extern "C" g2p_status g2p_export_v0(g2p_mesh *m, int32_t which, int64_t *row, int64_t *col, double *val, double *aval,
+                                    int64_t *map) {
+    if (!m || (which != 0 && which != 1)) return G2P_ERR_INVALID;
+    if (!m->v0_done) { set_last_message("g2p_assemble_v0 has not run"); return G2P_ERR_STATE; }
+    V0Basis &B = which ? m->v0c : m->v0d;
+    cudaStream_t s = m->stream;
+    int64_t *r, *c2;
+    G2P_TRY(dalloc(&r, B.nnz, s));
+    G2P_TRY(dalloc(&c2, B.nnz > m->d.N_node ? B.nnz : m->d.N_node, s));
+    k_v0_export<<<grid_for(B.ncol), kThreads, 0, s>>>(B.cptr, B.ncol, B.cedge, r, c2);
+    if (row) G2P_CUDA(cudaMemcpyAsync(row, r, sizeof(int64_t) * B.nnz, cudaMemcpyDeviceToHost, s));
+    if (col) G2P_CUDA(cudaMemcpyAsync(col, c2, sizeof(int64_t) * B.nnz, cudaMemcpyDeviceToHost, s));
+    if (val) G2P_CUDA(cudaMemcpyAsync(val, B.cval, sizeof(double) * B.nnz, cudaMemcpyDeviceToHost, s));
+    if (aval) G2P_CUDA(cudaMemcpyAsync(aval, B.caval, sizeof(double) * B.nnz, cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    if (map) {
+        k_map_export<<<grid_for(m->d.N_node), kThreads, 0, s>>>(B.map, m->d.N_node, c2);
+        G2P_CUDA(cudaMemcpyAsync(map, c2, sizeof(int64_t) * m->d.N_node, cudaMemcpyDeviceToHost, s));
+    }
+    G2P_CUDA(cudaStreamSynchronize(s));
+    dfree(r, s); dfree(c2, s);
+    G2P_CUDA(cudaStreamSynchronize(s));
+    return G2P_OK;
+}
+
+extern "C" g2p_status g2p_export_laplacian(g2p_mesh *m, int32_t which, int64_t *row, int64_t *col, double *val) {
+    if (!m || (which != 0 && which != 1)) return G2P_ERR_INVALID;
+    if (!m->v0_done) { set_last_message("g2p_assemble_v0 has not run"); return G2P_ERR_STATE; }
+    return g2p_export_csr(m, which ? m->Ac : m->Ad, row, col, val);
+}

@@ -326,6 +326,36 @@ def microstrip(nx=101, ny=41, nz=11, pitch=1e-6, freq_ghz=1.0) -> Layout:
                   freq_start=freq_ghz, freq_end=freq_ghz, freq_unit=1e9, nfreq=1)
 
 
+def multistrip(nx=256, ny=256, nz=16, n_strips=32, pitch=1e-6, width=None, freq_start=1e7, freq_end=1e11,
+               freq_unit=1.0, nfreq=64, freq_scale=0, eps_r=3.9) -> Layout:
+    """The microstrip stack with n_strips parallel strips, one port each.
+
+    Cell layers as in microstrip(): ground 0-1, dielectric up to the strip
+    layer, strips along x in the layer below the top air layer.  Strips are
+    evenly spaced in y; each port runs from a strip's bottom at x = 0 down to
+    the ground top."""
+    assert nz >= 5
+    zs = nz - 1
+    strip_z = zs - 2
+    eps = np.ones(zs)
+    sig = np.zeros(zs)
+    eps[1:strip_z] = eps_r
+    sig[0] = SIGMA_CU
+    sig[strip_z] = SIGMA_CU
+    slot = (ny - 2) // n_strips
+    if slot < 2:
+        raise ValueError("grid too narrow for the strip count")
+    w = width if width is not None else max(1, slot // 2)
+    boxes = [Box(0, nx - 1, 0, ny - 1, 0, 1)]
+    ports: List[List[PortSpec]] = []
+    for s in range(n_strips):
+        y0 = 1 + s * slot + (slot - w) // 2
+        boxes.append(Box(0, nx - 1, y0, y0 + w, strip_z, strip_z + 1))
+        ports.append([PortSpec((0, y0 + w // 2, strip_z), (0, y0 + w // 2, 1))])
+    return Layout("multistrip", nx, ny, nz, (pitch, pitch, pitch), eps, sig, boxes, ports,
+                  freq_start=freq_start, freq_end=freq_end, freq_unit=freq_unit, nfreq=nfreq, freq_scale=freq_scale)
+
+
 def manhattan(nx=512, ny=512, nz=24, n_metal=4, wires_per_layer=64, n_ports=8, seed=1001,
               pitch=1e-6, via_p=0.3, freq_start=10.0, freq_end=10.0, nfreq=1, freq_unit=1e9,
               freq_scale=1, wmin=2, wmax=8, lmin=20, lmax=200) -> Layout:
@@ -403,21 +433,26 @@ def manhattan(nx=512, ny=512, nz=24, n_metal=4, wires_per_layer=64, n_ports=8, s
     lay = Layout("manhattan", nx, ny, nz, (pitch, pitch, pitch), eps, sig, boxes, [],
                  freq_start=freq_start, freq_end=freq_end, freq_unit=freq_unit, nfreq=nfreq,
                  freq_scale=freq_scale)
-    # ports at the low end of lowest-layer wires, each on a distinct net
+    # ports at wire ends, lowest layers first, each on a distinct net and with
+    # a conductor-free column down to the ground plane
     Y, X, Z, node = _rasterise(nx, ny, nz, boxes)
     lab, _ = _label(Y, X, Z, node)
     used = set()
     ports: List[List[PortSpec]] = []
-    for b in layer_wires[0]:
-        if len(ports) == n_ports:
-            break
-        xc, yc = b.x0, (b.y0 + b.y1) // 2
-        net = int(lab[b.z0, xc, yc])
-        col = lab[1:b.z0, xc, yc]
-        if net in used or np.any(col != 0):
-            continue
-        used.add(net)
-        ports.append([PortSpec((xc, yc, b.z0), (xc, yc, 0))])
+    for k in range(n_metal):
+        for b in layer_wires[k]:
+            if len(ports) == n_ports:
+                break
+            along_x = k % 2 == 0
+            ends = [(b.x0, (b.y0 + b.y1) // 2), (b.x1, (b.y0 + b.y1) // 2)] if along_x else \
+                   [((b.x0 + b.x1) // 2, b.y0), ((b.x0 + b.x1) // 2, b.y1)]
+            for xc, yc in ends:
+                net = int(lab[b.z0, xc, yc])
+                if net in used or np.any(lab[1:b.z0, xc, yc] != 0):
+                    continue
+                used.add(net)
+                ports.append([PortSpec((xc, yc, b.z0), (xc, yc, 0))])
+                break
     if len(ports) < n_ports:
         raise ValueError(f"only {len(ports)} distinct port nets available")
     lay.ports = ports
@@ -426,7 +461,8 @@ def manhattan(nx=512, ny=512, nz=24, n_metal=4, wires_per_layer=64, n_ports=8, s
 
 def config(name: str, **kw) -> Layout:
     """The named workloads: c1 microstrip, c2 random Manhattan at 10 GHz,
-    c3 batched block-RHS (32 ports x 64 log-spaced points 1e7..1e11 Hz)."""
+    c3 the microstrip stack with 32 strips (32 ports x 64 log-spaced points
+    1e7..1e11 Hz)."""
     if name == "c1":
         return microstrip(**kw)
     if name == "c2":
@@ -434,8 +470,7 @@ def config(name: str, **kw) -> Layout:
         args.update(kw)
         return manhattan(**args)
     if name == "c3":
-        args = dict(nx=256, ny=256, nz=16, n_ports=32, seed=1002, freq_start=1e7, freq_end=1e11,
-                    freq_unit=1.0, nfreq=64, freq_scale=0)
+        args = dict(nx=256, ny=256, nz=16, n_strips=32)
         args.update(kw)
-        return manhattan(**args)
+        return multistrip(**args)
     raise KeyError(name)

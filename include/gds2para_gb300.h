@@ -1,0 +1,170 @@
+/* gds2para_gb300 -- GB300-native (sm_103a) full-wave extraction hot path of
+ * purdue-onchip/gds2Para behind a plain C ABI.
+ *
+ * The reference's C++ entry points on this path and their replacements:
+ *
+ *   fdtdMesh (src/fdtd.hpp:182-356)            -> g2p_mesh_desc + g2p_mesh
+ *   setMapEdge/findBoundNodeEdge
+ *            (src/fdtd.hpp:1444-1529)           -> g2p_index_maps
+ *   generateStiff (src/generateStiff.cpp:6)    -> g2p_generate_stiff (+ g2p_export_stiff)
+ *   merge_v0d1/generateAd, merge_v0c/generateAc
+ *            (src/fdtd.hpp:1823-3574)           -> g2p_assemble_v0 (+ g2p_export_v0,
+ *                                                  g2p_export_laplacian)
+ *   hypreSolve (src/hypreSolve.cpp:9,
+ *            src/hypreSolver.h:14)              -> g2p_hypre_solve, g2p_solver_*
+ *   paraGenerator (src/matrixCon.cpp:11)       -> g2p_para_generator
+ *
+ * All pointers in g2p_mesh_desc and every output buffer are HOST pointers
+ * owned by the caller; device memory is owned by the handles.  Every entry
+ * point returns a g2p_status and never exits the process; g2p_last_error()
+ * describes the most recent failure of the calling thread.  A handle must be
+ * used by one host thread at a time.  The library runs on CUDA device 0 (or
+ * the device current when the handle is created) and requires sm_103a. */
+#ifndef GDS2PARA_GB300_H
+#define GDS2PARA_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    G2P_OK = 0,
+    G2P_ERR_INVALID = 1,        /* bad argument or inconsistent mesh description */
+    G2P_ERR_CUDA = 2,           /* CUDA runtime failure (see g2p_last_error) */
+    G2P_ERR_NOMEM = 3,          /* device allocation failed */
+    G2P_ERR_NOT_CONVERGED = 4,  /* solver hit maxit above rtol (result still written) */
+    G2P_ERR_UNSUPPORTED = 5,    /* layout outside what the path handles (message says which) */
+    G2P_ERR_STATE = 6,          /* a required earlier step has not run */
+    G2P_ERR_ADMISSION = 7       /* job rejected: its device footprint exceeds the budget */
+} g2p_status;
+
+/* The fdtdMesh members the path reads, after meshAndMark and portSet
+ * (src/mesh.cpp:5-1133,1196-1594).  Field meanings follow the reference:
+ * node n = iz*N_node_s + ix*ny + iy; edges are numbered per z plane as
+ * y-edges, x-edges, then z-edges (src/fdtd.hpp:4107-4130). */
+typedef struct {
+    int64_t nx, ny, nz;                /* node counts */
+    const double *xn, *yn, *zn;        /* node coordinates (m) */
+    const double *stack_epsn;          /* [nz] stackEpsn (relative permittivity) */
+    const double *stack_sign;          /* [nz] stackSign (S/m) */
+    const int64_t *mark_node;          /* [N_node] conductor id (1-based) or 0 */
+    const int64_t *mark_edge;          /* [N_edge] conductor id or 0 */
+    int64_t num_cdt;                   /* numCdt */
+    const int32_t *mark_port;          /* [num_cdt] conductor[].markPort: -1 return, 0 passive, p+1 excited */
+    const uint8_t *cdt_return;         /* [num_cdt] 1 if findBoundNodeEdge ran on it (src/mesh.cpp:943-953) */
+    int32_t num_ports;
+    const int32_t *port_side_ptr;      /* [num_ports+1] sides of each port */
+    const int64_t *side_edge_ptr;      /* [num_sides+1] */
+    const int64_t *side_edges;         /* portEdge, return -> supply */
+    const double *side_area;           /* portArea */
+    const int32_t *side_dir;           /* portDirection */
+    double freq_start, freq_end, freq_unit;
+    int32_t nfreq, freq_scale;         /* freqScale 1 linear, 0 logarithmic */
+} g2p_mesh_desc;
+
+typedef struct g2p_mesh g2p_mesh;
+typedef struct g2p_solver g2p_solver;
+
+enum { G2P_PREC_FP64 = 0, G2P_PREC_MIXED = 1 };
+
+typedef struct {
+    int32_t precision;        /* G2P_PREC_FP64: plain FP64 method; G2P_PREC_MIXED: FP32
+                                 Krylov/AMG inside FP64 iterative refinement */
+    int32_t restart;          /* FGMRES restart length (KDim) */
+    int32_t maxit;            /* max FGMRES iterations (FP64) / refinement sweeps x inner (mixed) */
+    double rtol;              /* ||b - A x|| <= rtol * ||b|| per right-hand side */
+    int32_t smoother_degree;  /* Chebyshev degree of the AMG smoother */
+    int32_t coarse_size;      /* dense LU below this many rows */
+    double strength;          /* aggregation strength threshold */
+    int32_t max_levels;
+    double inner_rtol;        /* mixed: inner FP32 solve tolerance */
+    int32_t inner_maxit;      /* mixed: inner FP32 iterations per refinement step */
+    int32_t batch;            /* paraGenerator: 1 = all ports as one RHS block, 0 = port by port */
+    int32_t use_graphs;       /* capture Krylov cycles in CUDA graphs */
+} g2p_solver_params;
+
+typedef struct {
+    int32_t iterations;       /* total inner iterations (max over right-hand sides) */
+    int32_t refinements;      /* outer FP64 refinement steps (mixed) */
+    double rel_residual;      /* max over right-hand sides, FP64 true residual */
+    int32_t levels;
+    int32_t converged;
+    int64_t coarse_rows;
+    double setup_ms, solve_ms;
+} g2p_solve_stats;
+
+typedef struct {
+    int64_t bden, leng_S, leng_v0d, leng_v0c, nnz_v0d, nnz_v0c, nnz_ad, nnz_ac;
+} g2p_sizes;
+
+typedef struct {
+    g2p_sizes sizes;
+    int32_t solves;           /* linear systems solved (3 per port) */
+    int32_t total_iterations;
+    double max_rel_residual;
+    double assembly_ms, setup_ms, solve_ms, total_ms;
+    int32_t ad_levels, ac_levels;
+} g2p_extract_stats;
+
+/* ---- library ---- */
+const char *g2p_last_error(void);
+const char *g2p_version(void);
+/* parity_mode 1: the reference's hypreSolve settings (FlexGMRES KDim 10, 100
+ * iterations, rtol 1e-4; src/hypreSolver.h:7-11); 0: the oracle settings
+ * (FP64, rtol 1e-10). */
+void g2p_default_params(g2p_solver_params *p, int32_t parity_mode);
+
+/* ---- fdtdMesh ---- */
+g2p_status g2p_mesh_create(const g2p_mesh_desc *desc, g2p_mesh **out);
+g2p_status g2p_mesh_destroy(g2p_mesh *m);
+g2p_status g2p_mesh_sizes(const g2p_mesh *m, g2p_sizes *out);
+
+/* ---- index maps: setMapEdge / findBoundNodeEdge / LOWER_BOUNDARY_PEC
+ * (src/fdtd.hpp:1444-1529, src/mesh.cpp:943-987).  map_edge (nullable) gets
+ * N_edge values: the edge's index after PEC removal, or -1. ---- */
+g2p_status g2p_index_maps(g2p_mesh *m, int64_t *bden, int64_t *map_edge);
+
+/* ---- generateStiff (src/generateStiff.cpp:6-565): S = Sh*Se^T/mu over the
+ * non-PEC edges, kept on the device as CSR.  g2p_export_stiff writes the
+ * reference's COO (SRowId, SColId, Sval; leng_S entries). ---- */
+g2p_status g2p_generate_stiff(g2p_mesh *m, int64_t *leng_S);
+g2p_status g2p_export_stiff(g2p_mesh *m, int64_t *row, int64_t *col, double *val);
+
+/* ---- V0 bases and Laplacians (src/fdtd.hpp:1823-3574).  which = 0 for
+ * V0d/Ad, 1 for V0c/Ac.  g2p_export_v0 writes the COO of V0 (rows = original
+ * edge index, in the reference's entry order) with its a-values and the node
+ * map (column+1 or 0; N_node values); g2p_export_laplacian writes the
+ * row-sorted COO the reference hands to hypreSolve. ---- */
+g2p_status g2p_assemble_v0(g2p_mesh *m, g2p_sizes *out);
+g2p_status g2p_export_v0(g2p_mesh *m, int32_t which, int64_t *row, int64_t *col, double *val, double *aval,
+                         int64_t *map);
+g2p_status g2p_export_laplacian(g2p_mesh *m, int32_t which, int64_t *row, int64_t *col, double *val);
+
+/* ---- hypreSolve (src/hypreSolve.cpp:9): x = A^-1 b for a row-sorted COO A
+ * (0-based int64), with the reference's parity settings.  Unlike the
+ * reference it reports non-convergence (G2P_ERR_NOT_CONVERGED) instead of
+ * returning 0 unconditionally; the solution is written either way. ---- */
+g2p_status g2p_hypre_solve(const int64_t *ARowId, const int64_t *AColId, const double *Aval, int64_t leng_A,
+                           const double *bin, int64_t leng_v0, double *solution);
+
+/* Reusable AMG-FGMRES solver on one matrix (setup once, many solves). */
+g2p_status g2p_solver_create(const int64_t *ARowId, const int64_t *AColId, const double *Aval, int64_t leng_A,
+                             int64_t n, const g2p_solver_params *p, g2p_solver **out);
+/* b, x: host, column-major n x nrhs. */
+g2p_status g2p_solver_solve(g2p_solver *s, const double *b, double *x, int32_t nrhs, g2p_solve_stats *st);
+g2p_status g2p_solver_destroy(g2p_solver *s);
+
+/* ---- paraGenerator (src/matrixCon.cpp:11-907, default V0 path): per port
+ * the three solves Ad, Ac, Ad, the back-projections and Construct_Z_V0
+ * (src/fdtd.hpp:4173-4215), then print_z_V0's frequency rescale
+ * (src/fdtd.hpp:4249-4316).  z_out (host) receives nfreq*P*P complex values
+ * as interleaved (re, im) doubles in sys->x's layout, including the
+ * reference's transposed storage of frequencies after the first.  Runs
+ * g2p_index_maps and g2p_assemble_v0 first if they have not run. ---- */
+g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p, double *z_out, g2p_extract_stats *st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

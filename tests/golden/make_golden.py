@@ -1,0 +1,85 @@
+"""Generates tests/golden/*.npz from the reference's own sources.
+
+Runs oracle/_ref/ref_pipeline (the reference's mesh.cpp portSet,
+generateStiff.cpp, matrixCon.cpp paraGenerator and fdtdMesh members,
+compiled unmodified by oracle/build_ref.sh) on seeded synthetic layouts and
+stores what it produced.  Arrays up to SMALL elements are stored whole;
+larger ones as a SHA-256 of their bytes plus a few statistics, which is
+enough to check bit-exact integer and FP64 results.
+
+Needs the reference checkout (default /root/reference); the fixtures it
+writes are self-contained.  Usage:
+    python tests/golden/make_golden.py [reference_root]
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from gds2para_gb300 import layout as lay  # noqa: E402
+from oracle.harness import run_reference  # noqa: E402
+
+SMALL = 6000
+
+# name -> (generator, kwargs); kept small enough for the reference's CPU code
+CASES = {
+    "multistrip_small": ("multistrip", dict(nx=24, ny=20, nz=8, n_strips=3, freq_start=1e8, freq_end=1e10,
+                                            nfreq=4)),
+    "strip_tiny": ("microstrip", dict(nx=13, ny=9, nz=6)),
+    "strip_c1": ("microstrip", dict()),
+    "manhattan_small": ("manhattan", dict(nx=40, ny=36, nz=12, n_metal=3, wires_per_layer=10, n_ports=3, seed=10,
+                                          lmin=6, lmax=24)),
+    "manhattan_sweep": ("manhattan", dict(nx=33, ny=29, nz=12, n_metal=2, wires_per_layer=8, n_ports=2, seed=1,
+                                          lmin=6, lmax=20, freq_start=1e8, freq_end=1e10, freq_unit=1.0, nfreq=5,
+                                          freq_scale=0)),
+}
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def make_layout(gen: str, kw: dict):
+    return lay.build(getattr(lay, gen)(**kw))
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), ref])
+    for name, (gen, kw) in CASES.items():
+        d = make_layout(gen, kw)
+        R = run_reference(d)
+        out = {}
+        meta = {"generator": gen, "kwargs": kw, "hashes": {}, "stats": {}}
+        for k, v in R.items():
+            if k == "_log":
+                continue
+            if isinstance(v, int):
+                meta[k] = v
+                continue
+            if v.size <= SMALL:
+                out[k] = v
+            else:
+                meta["hashes"][k] = digest(v)
+                meta["stats"][k] = dict(size=int(v.size), dtype=str(v.dtype),
+                                        sum=float(np.sum(v.astype(np.float64))),
+                                        absmax=float(np.max(np.abs(v))) if v.size else 0.0)
+        # the reference's Z is always stored whole
+        out["Z"] = R["Z"]
+        out["_meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"{name}: {os.path.getsize(path) / 1024:.1f} KiB, solves={R.get('solves')}, Z[0]={R['Z'][0]}")
+
+
+if __name__ == "__main__":
+    main()
