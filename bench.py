@@ -1,0 +1,308 @@
+"""Benchmark of the extraction hot path on GB300.
+
+One step = one complete V0 extraction of a synthetic layout through the C ABI
+(include/gds2para_gb300.h): upload of the fdtdMesh fields, index maps,
+generateStiff, V0 bases and Ad/Ac assembly, AMG setup, the three solves of
+every port (all ports as one block of right-hand sides) and the Z matrix.
+
+metric: port-frequency solves per second = ports x frequency points / step.
+`value` starts from inputs already resident in HBM; `e2e` starts from pinned
+host buffers and includes the host->device copies and the Z read-back.
+
+    python bench.py [--gpus N --steps K --warmup W --impl gb300|reference
+                     --config c2 --precision mixed|fp64 --batch 1]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "port-freq solves/s at 1e-6 rel Z err, mixed+batched vs FP64 GPU; p50/p99 job ms"
+UNIT = "port-freq solves/s"
+RTOL = {"c1": 1e-10, "c2": 1e-8, "c3": 1e-8}
+WORKLOAD = {
+    "c1": "microstrip 101x41x11 nodes at 1 um, 1 port, 1 GHz, rtol 1e-10",
+    "c2": "random Manhattan 512x512x24 nodes, 4 metal layers x 64 wires, 8 ports, 10 GHz, rtol 1e-8",
+    "c3": "microstrip stack 256x256x16 nodes, 32 strips/ports x 64 log-spaced points 1e7..1e11 Hz, rtol 1e-8",
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c2", choices=list(WORKLOAD))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--batch", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-ports", type=int, default=1)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi samples (SM clock, throttle reasons) during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": len(self.rows)}
+        if not self.rows:
+            return out
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        out["sm_mhz"] = statistics.median(sm) if sm else None
+        out["sm_max_mhz"] = max(mx) if mx else None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if r[5 + i].lower().startswith("active"):
+                    reasons.add(n)
+        out["reasons"] = sorted(reasons)
+        return out
+
+
+def make_desc(d, place, torch):
+    """MeshDesc arrays as torch tensors on `place` ('pinned' or 'cuda')."""
+    arrays = dict(
+        xn=(d.xn, np.float64), yn=(d.yn, np.float64), zn=(d.zn, np.float64),
+        stack_epsn=(d.stack_epsn, np.float64), stack_sign=(d.stack_sign, np.float64),
+        mark_node=(d.mark_node, np.int64), mark_edge=(d.mark_edge, np.int64),
+        mark_port=(d.mark_port, np.int32), cdt_return=(d.cdt_return, np.uint8),
+        port_side_ptr=(d.port_side_ptr, np.int32), side_edge_ptr=(d.side_edge_ptr, np.int64),
+        side_edges=(d.side_edges, np.int64), side_area=(d.side_area, np.float64), side_dir=(d.side_dir, np.int32))
+    out = {}
+    for k, (a, dt) in arrays.items():
+        t = torch.from_numpy(np.ascontiguousarray(a, dtype=dt))
+        out[k] = t.pin_memory() if place == "pinned" else t.cuda()
+    return out
+
+
+def desc_struct(d, T, _lib):
+    p = lambda k: T[k].data_ptr()
+    host_ports = ("port_side_ptr", "side_edge_ptr", "side_edges", "side_area", "side_dir")
+    return _lib.MeshDescC(d.nx, d.ny, d.nz, p("xn"), p("yn"), p("zn"), p("stack_epsn"), p("stack_sign"),
+                          p("mark_node"), p("mark_edge"), d.num_cdt, p("mark_port"), p("cdt_return"), d.num_ports,
+                          p("port_side_ptr"), p("side_edge_ptr"), p("side_edges"), p("side_area"), p("side_dir"),
+                          d.freq_start, d.freq_end, d.freq_unit, d.nfreq, d.freq_scale)
+
+
+def run_gb300(args):
+    import torch
+    from gds2para_gb300 import _lib, layout
+    from gds2para_gb300.api import default_params
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    L = _lib.load()
+    d = layout.build(layout.config(args.config))
+    params = default_params(precision=args.precision, batch=args.batch, rtol=RTOL[args.config])
+    dev = make_desc(d, "cuda", torch)
+    pin = make_desc(d, "pinned", torch)
+    z =torch.zeros(2 * d.nfreq * d.num_ports * d.num_ports, dtype=torch.float64).pin_memory()
+    stats = _lib.ExtractStats()
+
+    def step(T):
+        desc = desc_struct(d, T, _lib)
+        h = C.c_void_p()
+        _lib.check(L.g2p_mesh_create(C.byref(desc), C.byref(h)))
+        n = C.c_int64()
+        _lib.check(L.g2p_generate_stiff(h, C.byref(n)))
+        _lib.check(L.g2p_para_generator(h, C.byref(params), C.c_void_p(z.data_ptr()), C.byref(stats)))
+        L.g2p_mesh_destroy(h)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed(T, k, profile=False):
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = L.g2p_launch_count()
+        if profile:
+            L.g2p_profile_begin()
+        e0.record()
+        for _ in range(k):
+            step(T)
+        e1.record()
+        barrier()
+        kern = None
+        if profile:
+            ms, by, nl = C.c_double(), C.c_double(), C.c_int64()
+            _lib.check(L.g2p_profile_end(C.byref(ms), C.byref(by), C.byref(nl)))
+            kern = (ms.value, by.value, nl.value)
+        el = e0.elapsed_time(e1) / k
+        if world > 1:
+            t = torch.tensor([el], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        return el, L.g2p_launch_count() - n0, kern
+
+    for _ in range(max(args.warmup, 3)):
+        step(dev)
+    clocks = Clocks(local)
+    clocks.start()
+    ms, launches, kern = timed(dev, args.steps, profile=True)
+    clk = clocks.stop()
+    ms_e2e, _, _ = timed(pin, max(1, min(args.steps, 3)))
+    units = d.num_ports * d.nfreq
+    value = world * units / (ms / 1e3)
+    e2e = world * units / (ms_e2e / 1e3)
+    h2d = sum(int(pin[k].numel() * pin[k].element_size()) for k in pin)
+    d2h = int(z.numel() * z.element_size())
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    peak_gbs = peaks.get("hbm_gbs", 6800.0)
+    k_ms, k_bytes, k_n = kern
+    achieved = (k_bytes / (k_ms / 1e3)) / 1e9 if k_ms > 0 else None
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "spmm_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get(f"{args.config}_{args.precision}_bytes_per_launch")
+        except Exception:
+            traffic = None
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+        "data": "synthetic (seeded layout generator; no dataset)",
+        "config": {"workload": WORKLOAD[args.config], "config": args.config, "precision": args.precision,
+                   "batch": bool(args.batch), "ports": d.num_ports, "nfreq": d.nfreq,
+                   "rtol": RTOL[args.config], "l2": "inputs larger than L2 (>129 MB per step)",
+                   "parallelism": f"replicas x{world}",
+                   "sizes": {"N_edge": d.N_edge, "N_node": d.N_node, "leng_S": stats.sizes.leng_S,
+                             "leng_v0d": stats.sizes.leng_v0d, "leng_v0c": stats.sizes.leng_v0c,
+                             "nnz_ad": stats.sizes.nnz_ad, "nnz_ac": stats.sizes.nnz_ac},
+                   "last_step": {"assembly_ms": stats.assembly_ms, "setup_ms": stats.setup_ms,
+                                 "solve_ms": stats.solve_ms, "iterations": stats.total_iterations,
+                                 "max_rel_residual": stats.max_rel_residual}},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": ms_e2e},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "roofline": {"bound": "hbm", "kernel": "k_spmm (sparse matrix x RHS block)",
+                     "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                     "frac": (achieved / peak_gbs) if achieved else None, "traffic": traffic,
+                     "launches": int(k_n), "avg_launch_us": 1e3 * k_ms / max(k_n, 1),
+                     "algorithmic_bytes_per_launch": k_bytes / max(k_n, 1),
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s"},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(d, args, RTOL[args.config])
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out, rank
+
+
+def cpu_baseline(d, args, rtol, steps=1):
+    """The C restatement of the reference's path (oracle/), single-threaded,
+    on a bounded sample: assembly once, then the first `cpu_sample_ports`
+    ports with the reference's per-solve AMG setup; extrapolated to the job."""
+    from oracle.harness import COracle
+    O = COracle()
+    o = O.default_opts(rtol=rtol, maxit=400, restart=30, reuse_setup=0)
+    t0 = time.perf_counter()
+    _, st = O.para_generator(d, o, max_ports=args.cpu_sample_ports)
+    wall = time.perf_counter() - t0
+    np_ = max(1, min(args.cpu_sample_ports, d.num_ports))
+    per_port = (st.t_setup + st.t_solve) / np_
+    job = st.t_assembly + per_port * d.num_ports
+    return {"value": d.num_ports * d.nfreq / job, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"oracle/ C restatement on the host: assembly + {np_} of {d.num_ports} ports "
+                      f"(3 solves each, AMG setup per solve as hypreSolve does) took {wall:.1f} s; "
+                      f"job time extrapolated as assembly {st.t_assembly:.2f} s + {d.num_ports} x {per_port:.2f} s",
+            "seconds": wall}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return None, rank
+    from gds2para_gb300 import layout
+    d = layout.build(layout.config(args.config))
+    vals = []
+    cb = None
+    for i in range(max(args.warmup, 0) + args.steps):
+        cb = cpu_baseline(d, args, RTOL[args.config])
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = statistics.median(vals)
+    cb["value"] = v
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * d.num_ports * d.nfreq / v, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded layout generator)",
+           "config": {"workload": WORKLOAD[args.config], "config": args.config, "rtol": RTOL[args.config],
+                      "parallelism": "1 host thread"},
+           "cpu_baseline": cb,
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return out, rank
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        out, rank = run_reference(args)
+    else:
+        out, rank = run_gb300(args)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

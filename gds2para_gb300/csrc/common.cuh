@@ -27,6 +27,10 @@ namespace g2p {
 void set_last_error(cudaError_t e, const char *what, const char *file, int line);
 void set_last_message(const char *fmt, ...);
 
+// Counts kernel launches issued by the library (diagnostics).
+void launch_tick();
+int64_t launch_count();
+
 constexpr int kSMs = 152;            // GB300: 2 dies x 76 SMs
 constexpr int kThreads = 256;
 

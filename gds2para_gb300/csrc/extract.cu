@@ -265,9 +265,9 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         G2P_CUDA(cudaMemcpyAsync(d_pe_port + e0, port_local.data(), sizeof(int32_t) * (e1 - e0), cudaMemcpyHostToDevice, s));
         // (1) b_d = -V0da^T J
         G2P_CUDA(cudaMemsetAsync(Bd, 0, sizeof(double) * nd * kk, s));
-        k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
-                                                           m->v0d.ecol, m->v0d.eaval, kk, Bd);
-        k_scale<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Bd, -1.0);
+        (g2p::launch_tick(), k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
+                                                           m->v0d.ecol, m->v0d.eaval, kk, Bd));
+        (g2p::launch_tick(), k_scale<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Bd, -1.0));
         g2p_solve_stats ss;
         g2p_status rc = g2p_solver_solve_dev(Sd, Bd, Yd, kk, &ss);
         if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }
@@ -275,15 +275,15 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         local.solves += kk; local.total_iterations += ss.iterations;
         local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
         // (2) y0d /= omega ; yd1 = V0d y0d
-        k_div<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Yd, omega);
-        k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd1);
+        (g2p::launch_tick(), k_div<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Yd, omega));
+        (g2p::launch_tick(), k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd1));
         // (3) b_c = -V0ca^T J + V0ca^T(-omega D_eps yd1)
         G2P_CUDA(cudaMemsetAsync(Bc, 0, sizeof(double) * nc * kk, s));
-        k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
-                                                           m->v0c.ecol, m->v0c.eaval, kk, Bc);
-        k_scale<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, -1.0);
-        k_v0t_short<<<grid_for(nc * kk), kThreads, 0, s>>>(nc, kk, m->v0c.cptr, m->v0c.cedge, m->v0c.caval, yd1, f0, crhs);
-        k_add<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, crhs);
+        (g2p::launch_tick(), k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
+                                                           m->v0c.ecol, m->v0c.eaval, kk, Bc));
+        (g2p::launch_tick(), k_scale<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, -1.0));
+        (g2p::launch_tick(), k_v0t_short<<<grid_for(nc * kk), kThreads, 0, s>>>(nc, kk, m->v0c.cptr, m->v0c.cedge, m->v0c.caval, yd1, f0, crhs));
+        (g2p::launch_tick(), k_add<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, crhs));
         // (4) Ac y0c = b_c
         rc = g2p_solver_solve_dev(Sc, Bc, Yc, kk, &ss);
         if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }
@@ -291,20 +291,20 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         local.solves += kk; local.total_iterations += ss.iterations;
         local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
         // (5) yc = V0c y0c ; b_d2 = V0da^T(-D_eps yc)
-        k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0c.ecol, m->v0c.eval, Yc, yc);
-        k_v0t_short<<<grid_for(nd * kk), kThreads, 0, s>>>(nd, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd);
+        (g2p::launch_tick(), k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0c.ecol, m->v0c.eval, Yc, yc));
+        (g2p::launch_tick(), k_v0t_short<<<grid_for(nd * kk), kThreads, 0, s>>>(nd, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd));
         if (nlong_d > 0)
-            k_v0t_long<<<(unsigned)nlong_d, 256, 0, s>>>(d_long_d, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd);
+            (g2p::launch_tick(), k_v0t_long<<<(unsigned)nlong_d, 256, 0, s>>>(d_long_d, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd));
         // (6) Ad y0d2 = b_d2 ; yd2 = V0d y0d2
         rc = g2p_solver_solve_dev(Sd, Bd, Yd, kk, &ss);
         if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }
         if (rc == G2P_ERR_NOT_CONVERGED) worst_rc = rc;
         local.solves += kk; local.total_iterations += ss.iterations;
         local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
-        k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd2);
+        (g2p::launch_tick(), k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd2));
         // (7) Construct_Z_V0
-        k_construct_z<<<(P * kk + 127) / 128, 128, 0, s>>>(P, p0, kk, d_rptr, d_redge, d_rdir, d, m->xn, m->yn, m->zn, yd1,
-                                                          yc, yd2, d_cur, zre, zim);
+        (g2p::launch_tick(), k_construct_z<<<(P * kk + 127) / 128, 128, 0, s>>>(P, p0, kk, d_rptr, d_redge, d_rdir, d, m->xn, m->yn, m->zn, yd1,
+                                                          yc, yd2, d_cur, zre, zim));
     }
     // ---- print_z_V0 layout
     std::vector<double> fr(m->nfreq);
@@ -313,8 +313,8 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     G2P_TRY(dalloc(&d_fr, m->nfreq, s));
     G2P_TRY(dalloc(&d_out, 2LL * m->nfreq * P * P, s));
     G2P_CUDA(cudaMemcpyAsync(d_fr, fr.data(), sizeof(double) * m->nfreq, cudaMemcpyHostToDevice, s));
-    k_z_layout<<<grid_for((int64_t)m->nfreq * P * P), kThreads, 0, s>>>(P, m->nfreq, d_fr, m->freq_start * m->freq_unit,
-                                                                        zre, zim, d_out);
+    (g2p::launch_tick(), k_z_layout<<<grid_for((int64_t)m->nfreq * P * P), kThreads, 0, s>>>(P, m->nfreq, d_fr, m->freq_start * m->freq_unit,
+                                                                        zre, zim, d_out));
     G2P_CUDA(cudaMemcpyAsync(z_out, d_out, sizeof(double) * 2 * m->nfreq * P * P, cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
     local.solve_ms = ms_since(t0);

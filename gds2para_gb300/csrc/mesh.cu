@@ -9,6 +9,7 @@
 // (at most four) faces that contain its edge, visited in increasing face
 // number so the sums run in the same order as the sparse product; at most 13
 // distinct columns per row are accumulated in registers and sorted.
+#include <atomic>
 #include <cstdarg>
 #include <cstring>
 #include <mutex>
@@ -37,6 +38,10 @@ void set_last_message(const char *fmt, ...) {
 }
 
 const char *last_error() { return g_err.c_str(); }
+
+static std::atomic<int64_t> g_launches{0};
+void launch_tick() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 g2p_status ensure_scan_work(g2p_mesh *m, int64_t n) {
     int64_t need = scan_work_size(n) + 16;
@@ -74,6 +79,7 @@ using namespace g2p;
 
 extern "C" const char *g2p_last_error(void) { return g2p::last_error(); }
 extern "C" const char *g2p_version(void) { return "gds2para_gb300 0.1 (sm_103a)"; }
+extern "C" int64_t g2p_launch_count(void) { return g2p::launch_count(); }
 
 extern "C" g2p_status g2p_mesh_create(const g2p_mesh_desc *in, g2p_mesh **out) {
     if (!in || !out) { set_last_message("null argument"); return G2P_ERR_INVALID; }
@@ -99,26 +105,32 @@ extern "C" g2p_status g2p_mesh_create(const g2p_mesh_desc *in, g2p_mesh **out) {
     m->k.eps0 = G2P_EPSILON0;
     const Dims &d = m->d;
     cudaStream_t s = m->stream;
-    m->h_xn.assign(in->xn, in->xn + d.nx);
-    m->h_yn.assign(in->yn, in->yn + d.ny);
-    m->h_zn.assign(in->zn, in->zn + d.nz);
-    m->h_epsn.assign(in->stack_epsn, in->stack_epsn + d.nz);
-    m->h_sign.assign(in->stack_sign, in->stack_sign + d.nz);
+    // small arrays the host reads: copied with unified addressing so the
+    // descriptor may point to host or device memory
+    auto fetch = [&](auto &vec, const auto *src, int64_t n) -> bool {
+        vec.resize((size_t)n);
+        if (n == 0) return true;
+        return cudaMemcpy(vec.data(), src, sizeof(vec[0]) * (size_t)n, cudaMemcpyDefault) == cudaSuccess;
+    };
+    bool ok = fetch(m->h_xn, in->xn, d.nx) && fetch(m->h_yn, in->yn, d.ny) && fetch(m->h_zn, in->zn, d.nz) &&
+              fetch(m->h_epsn, in->stack_epsn, d.nz) && fetch(m->h_sign, in->stack_sign, d.nz) &&
+              fetch(m->h_mark_port, in->mark_port, in->num_cdt);
     m->num_cdt = in->num_cdt;
-    m->h_mark_port.assign(in->mark_port, in->mark_port + in->num_cdt);
     m->num_ports = in->num_ports;
-    if (in->num_ports > 0) {
-        m->port_side_ptr.assign(in->port_side_ptr, in->port_side_ptr + in->num_ports + 1);
-        int64_t ns = m->port_side_ptr.back();
-        m->side_edge_ptr.assign(in->side_edge_ptr, in->side_edge_ptr + ns + 1);
-        m->side_edges.assign(in->side_edges, in->side_edges + m->side_edge_ptr.back());
-        m->side_area.assign(in->side_area, in->side_area + ns);
-        m->side_dir.assign(in->side_dir, in->side_dir + ns);
-        for (int64_t e2 : m->side_edges)
-            if (e2 < 0 || e2 >= d.N_edge) { set_last_message("port edge out of range"); g2p_mesh_destroy(m); return G2P_ERR_INVALID; }
-        for (int p = 0; p < in->num_ports; p++)
-            if (m->port_side_ptr[p + 1] <= m->port_side_ptr[p]) { set_last_message("port %d has no side", p); g2p_mesh_destroy(m); return G2P_ERR_INVALID; }
+    if (ok && in->num_ports > 0) {
+        ok = fetch(m->port_side_ptr, in->port_side_ptr, in->num_ports + 1);
+        int64_t ns = ok ? m->port_side_ptr.back() : 0;
+        ok = ok && ns >= in->num_ports && fetch(m->side_edge_ptr, in->side_edge_ptr, ns + 1);
+        ok = ok && fetch(m->side_edges, in->side_edges, m->side_edge_ptr.back()) &&
+             fetch(m->side_area, in->side_area, ns) && fetch(m->side_dir, in->side_dir, ns);
+        if (ok) {
+            for (int64_t e2 : m->side_edges)
+                if (e2 < 0 || e2 >= d.N_edge) { set_last_message("port edge out of range"); g2p_mesh_destroy(m); return G2P_ERR_INVALID; }
+            for (int p = 0; p < in->num_ports; p++)
+                if (m->port_side_ptr[p + 1] <= m->port_side_ptr[p]) { set_last_message("port %d has no side", p); g2p_mesh_destroy(m); return G2P_ERR_INVALID; }
+        }
     }
+    if (!ok) { set_last_message("could not read the mesh description arrays"); g2p_mesh_destroy(m); return G2P_ERR_INVALID; }
     m->freq_start = in->freq_start; m->freq_end = in->freq_end; m->freq_unit = in->freq_unit;
     m->nfreq = in->nfreq; m->freq_scale = in->freq_scale;
     g2p_status st = G2P_OK;
@@ -130,7 +142,7 @@ extern "C" g2p_status g2p_mesh_create(const g2p_mesh_desc *in, g2p_mesh **out) {
     CK(dalloc(&m->mark_port, in->num_cdt, s)); CK(dalloc(&m->cdt_return, in->num_cdt, s));
     int64_t *tmp = nullptr;
     CK(dalloc(&tmp, d.N_edge > d.N_node ? d.N_edge : d.N_node, s));
-#define CP(dst, src, n) do { cudaError_t _e = cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s); \
+#define CP(dst, src, n) do { cudaError_t _e = cudaMemcpyAsync(dst, src, n, cudaMemcpyDefault, s); \
         if (_e != cudaSuccess) { set_last_error(_e, "H2D copy", __FILE__, __LINE__); dfree(tmp, s); g2p_mesh_destroy(m); return G2P_ERR_CUDA; } } while (0)
     CP(m->xn, in->xn, sizeof(double) * d.nx);
     CP(m->yn, in->yn, sizeof(double) * d.ny);
@@ -140,22 +152,22 @@ extern "C" g2p_status g2p_mesh_create(const g2p_mesh_desc *in, g2p_mesh **out) {
     CP(m->mark_port, in->mark_port, sizeof(int32_t) * in->num_cdt);
     CP(m->cdt_return, in->cdt_return, in->num_cdt);
     CP(tmp, in->mark_node, sizeof(int64_t) * d.N_node);
-    k_narrow<<<grid_for(d.N_node), kThreads, 0, s>>>(tmp, m->mark_node, d.N_node);
+    (g2p::launch_tick(), k_narrow<<<grid_for(d.N_node), kThreads, 0, s>>>(tmp, m->mark_node, d.N_node));
     CP(tmp, in->mark_edge, sizeof(int64_t) * d.N_edge);
-    k_narrow<<<grid_for(d.N_edge), kThreads, 0, s>>>(tmp, m->mark_edge, d.N_edge);
+    (g2p::launch_tick(), k_narrow<<<grid_for(d.N_edge), kThreads, 0, s>>>(tmp, m->mark_edge, d.N_edge));
     int *flag = nullptr;
     CK(dalloc(&flag, 1, s));
     cudaMemsetAsync(flag, 0, sizeof(int), s);
-    k_check_marks<<<grid_for(d.N_node), kThreads, 0, s>>>(m->mark_node, d.N_node, in->num_cdt, flag);
-    k_check_marks<<<grid_for(d.N_edge), kThreads, 0, s>>>(m->mark_edge, d.N_edge, in->num_cdt, flag);
+    (g2p::launch_tick(), k_check_marks<<<grid_for(d.N_node), kThreads, 0, s>>>(m->mark_node, d.N_node, in->num_cdt, flag));
+    (g2p::launch_tick(), k_check_marks<<<grid_for(d.N_edge), kThreads, 0, s>>>(m->mark_edge, d.N_edge, in->num_cdt, flag));
     int hflag = 0;
     cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
     dfree(flag, s);
     if (hflag) { dfree(tmp, s); g2p_mesh_destroy(m); set_last_message("mark_node/mark_edge hold ids outside [0, num_cdt]"); return G2P_ERR_INVALID; }
-    k_dual_lengths<<<1, 256, 0, s>>>(m->xn, d.Nx, m->dxa);
-    k_dual_lengths<<<1, 256, 0, s>>>(m->yn, d.Ny, m->dya);
-    k_dual_lengths<<<1, 256, 0, s>>>(m->zn, d.Nz, m->dza);
+    (g2p::launch_tick(), k_dual_lengths<<<1, 256, 0, s>>>(m->xn, d.Nx, m->dxa));
+    (g2p::launch_tick(), k_dual_lengths<<<1, 256, 0, s>>>(m->yn, d.Ny, m->dya));
+    (g2p::launch_tick(), k_dual_lengths<<<1, 256, 0, s>>>(m->zn, d.Nz, m->dza));
     dfree(tmp, s);
 #undef CP
 #undef CK
@@ -237,12 +249,12 @@ g2p_status g2p_run_index_maps(g2p_mesh *m) {
     G2P_TRY(dalloc(&m->pec_node, d.N_node, s));
     G2P_TRY(dalloc(&m->map_edge, d.N_edge, s));
     G2P_TRY(ensure_scan_work(m, d.N_edge));
-    k_pec_flags<<<grid_for(d.N_edge), kThreads, 0, s>>>(d, m->mark_edge, m->mark_node, m->cdt_return, m->pec_edge,
-                                                         m->pec_node);
+    (g2p::launch_tick(), k_pec_flags<<<grid_for(d.N_edge), kThreads, 0, s>>>(d, m->mark_edge, m->mark_node, m->cdt_return, m->pec_edge,
+                                                         m->pec_node));
     const uint8_t *pe = m->pec_edge;
     auto op = [pe] __device__(int64_t i) -> int64_t { return pe[i]; };
     G2P_TRY(exclusive_scan(op, d.N_edge, m->map_edge, m->scan_work, s));
-    k_finish_map<<<grid_for(d.N_edge), kThreads, 0, s>>>(d.N_edge, m->pec_edge, m->map_edge);
+    (g2p::launch_tick(), k_finish_map<<<grid_for(d.N_edge), kThreads, 0, s>>>(d.N_edge, m->pec_edge, m->map_edge));
     G2P_CUDA(cudaMemcpyAsync(&m->bden, m->scan_work + scan_total_index(d.N_edge), sizeof(int64_t),
                              cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
@@ -262,7 +274,7 @@ extern "C" g2p_status g2p_index_maps(g2p_mesh *m, int64_t *bden, int64_t *map_ed
     if (map_edge) {
         int64_t *tmp;
         G2P_TRY(dalloc(&tmp, m->d.N_edge, m->stream));
-        k_widen_map<<<grid_for(m->d.N_edge), kThreads, 0, m->stream>>>(m->map_edge, tmp, m->d.N_edge);
+        (g2p::launch_tick(), k_widen_map<<<grid_for(m->d.N_edge), kThreads, 0, m->stream>>>(m->map_edge, tmp, m->d.N_edge));
         G2P_CUDA(cudaMemcpyAsync(map_edge, tmp, sizeof(int64_t) * m->d.N_edge, cudaMemcpyDeviceToHost, m->stream));
         dfree(tmp, m->stream);
         G2P_CUDA(cudaStreamSynchronize(m->stream));
@@ -469,7 +481,7 @@ g2p_status g2p_run_stiff(g2p_mesh *m) {
     int64_t n = d.N_edge - m->bden;
     int64_t *rowlen;
     G2P_TRY(dalloc(&rowlen, n, s));
-    k_stiff_count<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, rowlen);
+    (g2p::launch_tick(), k_stiff_count<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, rowlen));
     int64_t nnz = 0;
     g2p_status st = g2p_build_rowptr(m, rowlen, n, &m->S.ptr, &nnz);
     dfree(rowlen, s);
@@ -478,8 +490,8 @@ g2p_status g2p_run_stiff(g2p_mesh *m) {
     m->S.nnz = nnz;
     G2P_TRY(dalloc(&m->S.col, nnz, s));
     G2P_TRY(dalloc(&m->S.val, nnz, s));
-    k_stiff_fill<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, m->S.ptr, m->S.col,
-                                                                     m->S.val, m->k.mu);
+    (g2p::launch_tick(), k_stiff_fill<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, m->S.ptr, m->S.col,
+                                                                     m->S.val, m->k.mu));
     G2P_CUDA(cudaGetLastError());
     G2P_CUDA(cudaStreamSynchronize(s));
     m->stiff_done = true;
@@ -499,12 +511,12 @@ g2p_status g2p_export_csr(g2p_mesh *m, const Csr<double> &A, int64_t *row, int64
     int64_t *tmp;
     G2P_TRY(dalloc(&tmp, A.nnz, s));
     if (row) {
-        k_csr_rows_i64<<<grid_for(A.n), kThreads, 0, s>>>(A.ptr, A.n, tmp);
+        (g2p::launch_tick(), k_csr_rows_i64<<<grid_for(A.n), kThreads, 0, s>>>(A.ptr, A.n, tmp));
         G2P_CUDA(cudaMemcpyAsync(row, tmp, sizeof(int64_t) * A.nnz, cudaMemcpyDeviceToHost, s));
         G2P_CUDA(cudaStreamSynchronize(s));
     }
     if (col) {
-        k_i32_to_i64<<<grid_for(A.nnz), kThreads, 0, s>>>(A.col, tmp, A.nnz);
+        (g2p::launch_tick(), k_i32_to_i64<<<grid_for(A.nnz), kThreads, 0, s>>>(A.col, tmp, A.nnz));
         G2P_CUDA(cudaMemcpyAsync(col, tmp, sizeof(int64_t) * A.nnz, cudaMemcpyDeviceToHost, s));
         G2P_CUDA(cudaStreamSynchronize(s));
     }

@@ -98,9 +98,9 @@ template <class F, class OutT>
 g2p_status exclusive_scan(F op, int64_t n, OutT *out, int64_t *work, cudaStream_t s) {
     int64_t nb = (n + kScanTile - 1) / kScanTile;
     if (nb == 0) nb = 1;
-    k_scan_reduce<F><<<(unsigned)nb, kScanThreads, 0, s>>>(op, n, work);
-    k_scan_partials<<<1, 1024, 0, s>>>(work, nb);
-    k_scan_down<F, OutT><<<(unsigned)nb, kScanThreads, 0, s>>>(op, n, work, out);
+    (g2p::launch_tick(), k_scan_reduce<F><<<(unsigned)nb, kScanThreads, 0, s>>>(op, n, work));
+    (g2p::launch_tick(), k_scan_partials<<<1, 1024, 0, s>>>(work, nb));
+    (g2p::launch_tick(), k_scan_down<F, OutT><<<(unsigned)nb, kScanThreads, 0, s>>>(op, n, work, out));
     G2P_CUDA(cudaGetLastError());
     return G2P_OK;
 }
@@ -189,11 +189,11 @@ g2p_status radix_sort_pairs(K *k0, V *v0, K *k1, V *v1, int64_t n, int bits, int
     V *vs = v0, *vd = v1;
     bool in1 = false;
     for (int shift = 0; shift < bits; shift += 8) {
-        k_sort_hist<K><<<(unsigned)nb, kSortThreads, 0, s>>>(ks, n, shift, nb, counts);
+        (g2p::launch_tick(), k_sort_hist<K><<<(unsigned)nb, kSortThreads, 0, s>>>(ks, n, shift, nb, counts));
         const int64_t *c = counts;
         auto op = [c] __device__(int64_t i) { return c[i]; };
         G2P_TRY(exclusive_scan(op, 256 * nb, counts + 256 * nb, work, s));
-        k_sort_scatter<K, V><<<(unsigned)nb, kSortThreads, 0, s>>>(ks, vs, n, shift, nb, counts + 256 * nb, kd, vd);
+        (g2p::launch_tick(), k_sort_scatter<K, V><<<(unsigned)nb, kSortThreads, 0, s>>>(ks, vs, n, shift, nb, counts + 256 * nb, kd, vd));
         G2P_CUDA(cudaGetLastError());
         K *tk = ks; ks = kd; kd = tk;
         V *tv = vs; vs = vd; vd = tv;

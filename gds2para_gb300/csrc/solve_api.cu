@@ -4,9 +4,12 @@
 //   FP64 ("plain"): FGMRES(restart) on A with the FP64 hierarchy, stopping at
 //     ||b - A x|| <= rtol ||b|| per right-hand side, as HYPRE's FlexGMRES does.
 //   mixed: iterative refinement in FP64 (true residual b - A x with the FP64
-//     operator, same stopping test) around an FP32 FGMRES/AMG solve of the
-//     diagonally equilibrated system S A S d^ = S r.
+//     operator, same stopping test) around an FP32 FGMRES/AMG solve of
+//     (c A) d^ = r, c a power of two bringing the largest diagonal to ~1
+//     (exact in binary, and unlike a diagonal equilibration it leaves the
+//     near-null space the aggregates must represent unchanged).
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -15,29 +18,26 @@
 
 namespace g2p {
 
-__global__ void k_scale_vec(const int64_t *ptr, const int32_t *col, const double *val, int64_t n, double *scale) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double d = 0;
-        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) if (col[q] == i) { d = val[q]; break; }
-        scale[i] = d != 0.0 ? 1.0 / sqrt(fabs(d)) : 1.0;
-    }
-}
-
-__global__ void k_scale_mat(const int64_t *ptr, const int32_t *col, const double *val, int64_t n, const double *scale,
-                            double *out) {
+__global__ void k_max_abs_diag(const int64_t *ptr, const int32_t *col, const double *val, int64_t n,
+                               unsigned long long *mx) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) out[q] = scale[i] * val[q] * scale[col[q]];
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++)
+            if (col[q] == i) { atomicMax(mx, (unsigned long long)__double_as_longlong(fabs(val[q]))); break; }
 }
 
-// rf = float(scale .* r)
-__global__ void k_to_scaled_f(int64_t nk, int k, const double *scale, const double *r, float *rf) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x)
-        rf[t] = (float)(scale[t / k] * r[t]);
+__global__ void k_scale_vals(const double *val, int64_t nnz, double c, double *out) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x)
+        out[q] = c * val[q];
 }
-// x += scale .* double(df)
-__global__ void k_add_scaled(int64_t nk, int k, const double *scale, const float *df, double *x) {
+
+__global__ void k_to_f(int64_t nk, const double *r, float *rf) {
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x)
-        x[t] += scale[t / k] * (double)df[t];
+        rf[t] = (float)r[t];
+}
+// x += c * double(df)
+__global__ void k_add_scaled(int64_t nk, double c, const float *df, double *x) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x)
+        x[t] += c * (double)df[t];
 }
 
 __global__ void k_coo_count(const int64_t *rows, int64_t nnz, int64_t n, int64_t *cnt, int *bad) {
@@ -130,12 +130,21 @@ g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cu
     cudaMemcpyAsync(S->A.val, A.val, sizeof(double) * A.nnz, cudaMemcpyDeviceToDevice, s);
     if ((st = find_long_rows(S->A, &S->long_rows, &S->nlong, s)) != G2P_OK) return fail(st);
     if (S->precision == G2P_PREC_MIXED) {
-        if ((st = dalloc(&S->scale, A.n, s)) != G2P_OK) return fail(st);
-        k_scale_vec<<<grid_for(A.n), kThreads, 0, s>>>(S->A.ptr, S->A.col, S->A.val, A.n, S->scale);
+        unsigned long long *mx;
+        if ((st = dalloc(&mx, 1, s)) != G2P_OK) return fail(st);
+        cudaMemsetAsync(mx, 0, sizeof(unsigned long long), s);
+        (g2p::launch_tick(), k_max_abs_diag<<<grid_for(A.n), kThreads, 0, s>>>(S->A.ptr, S->A.col, S->A.val, A.n, mx));
+        unsigned long long hb = 0;
+        cudaMemcpyAsync(&hb, mx, sizeof(hb), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        dfree(mx, s);
+        double dmax;
+        memcpy(&dmax, &hb, sizeof(dmax));
+        S->cscale = dmax > 0 ? std::ldexp(1.0, -std::ilogb(dmax)) : 1.0;
         Csr<double> As = S->A;   // shares structure; scaled values in a temporary
         double *sv;
         if ((st = dalloc(&sv, A.nnz, s)) != G2P_OK) return fail(st);
-        k_scale_mat<<<grid_for(A.n), kThreads, 0, s>>>(S->A.ptr, S->A.col, S->A.val, A.n, S->scale, sv);
+        (g2p::launch_tick(), k_scale_vals<<<grid_for(A.nnz), kThreads, 0, s>>>(S->A.val, A.nnz, S->cscale, sv));
         As.val = sv;
         st = amg_setup(As, S->cfg, s, nullptr, S->H64);
         dfree(sv, s);
@@ -205,11 +214,11 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
             rep.rel_residual = worst;
             if (worst <= S->cfg.rtol) { rep.converged = true; break; }
             if (ref == max_ref) break;
-            k_to_scaled_f<<<grid_for(nk), kThreads, 0, s>>>(nk, k, S->scale, S->rb, S->rf);
+            (g2p::launch_tick(), k_to_f<<<grid_for(nk), kThreads, 0, s>>>(nk, S->rb, S->rf));
             G2P_CUDA(cudaMemsetAsync(S->df, 0, sizeof(float) * nk, s));
             SolveReport ir;
             G2P_TRY(fgmres<float>(S->H32.lv[0].A, S->H32, S->K32, S->rf, S->df, k, inner, nullptr, s, ir));
-            k_add_scaled<<<grid_for(nk), kThreads, 0, s>>>(nk, k, S->scale, S->df, x);
+            (g2p::launch_tick(), k_add_scaled<<<grid_for(nk), kThreads, 0, s>>>(nk, S->cscale, S->df, x));
             iters += ir.iterations;
             refinements++;
         }
@@ -250,8 +259,8 @@ extern "C" g2p_status g2p_solver_create(const int64_t *ARowId, const int64_t *AC
     G2P_CUDA(cudaMemcpyAsync(A.val, Aval, sizeof(double) * leng_A, cudaMemcpyHostToDevice, s));
     G2P_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (n + 1), s));
     G2P_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
-    k_coo_count<<<grid_for(leng_A), kThreads, 0, s>>>(rows, leng_A, n, cnt, bad);
-    k_coo_cols<<<grid_for(leng_A), kThreads, 0, s>>>(cols, leng_A, n, A.col, bad);
+    (g2p::launch_tick(), k_coo_count<<<grid_for(leng_A), kThreads, 0, s>>>(rows, leng_A, n, cnt, bad));
+    (g2p::launch_tick(), k_coo_cols<<<grid_for(leng_A), kThreads, 0, s>>>(cols, leng_A, n, A.col, bad));
     const int64_t *cp = cnt;
     auto op = [cp, n] __device__(int64_t i) -> int64_t { return i < n ? cp[i] : 0; };
     G2P_TRY(exclusive_scan(op, n + 1, A.ptr, work, s));
@@ -281,9 +290,9 @@ extern "C" g2p_status g2p_solver_solve(g2p_solver *S, const double *b, double *x
     G2P_TRY(dalloc(&db, n * nrhs, s)); G2P_TRY(dalloc(&dx, n * nrhs, s)); G2P_TRY(dalloc(&tb, n * nrhs, s));
     // host column-major <-> device interleaved
     G2P_CUDA(cudaMemcpyAsync(tb, b, sizeof(double) * n * nrhs, cudaMemcpyHostToDevice, s));
-    k_colmajor_to_interleaved<<<grid_for(n * nrhs), kThreads, 0, s>>>(tb, db, n, nrhs);
+    (g2p::launch_tick(), k_colmajor_to_interleaved<<<grid_for(n * nrhs), kThreads, 0, s>>>(tb, db, n, nrhs));
     g2p_status rc = g2p_solver_solve_dev(S, db, dx, nrhs, st);
-    k_interleaved_to_colmajor<<<grid_for(n * nrhs), kThreads, 0, s>>>(dx, tb, n, nrhs);
+    (g2p::launch_tick(), k_interleaved_to_colmajor<<<grid_for(n * nrhs), kThreads, 0, s>>>(dx, tb, n, nrhs));
     G2P_CUDA(cudaMemcpyAsync(x, tb, sizeof(double) * n * nrhs, cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
     dfree(db, s); dfree(dx, s); dfree(tb, s);

@@ -11,8 +11,11 @@
 //     hashed priorities (two max-propagation sweeps per round), neighbours
 //     joining the strongest root, distance-2 nodes joining a neighbour's
 //     aggregate,
-//   * Galerkin coarse operators P^T A P of the piecewise-constant
-//     prolongation by expand / stable radix sort / ordered reduce,
+//   * smoothed prolongation P = (I - w D^-1 A) T of the piecewise-constant
+//     aggregate basis T (w = 4 / (3 rho), rho the Gershgorin radius of
+//     D^-1 A; long rows keep T), restriction by aggregate sums T^T, and the
+//     Petrov-Galerkin coarse operator T^T A P formed as (T^T A) P, each
+//     product by expand / stable radix sort / ordered reduce,
 //   * Chebyshev smoothing on D^-1 A (bounds from the Gershgorin radius),
 //   * an explicit FP64 inverse on the coarsest level.
 // All right-hand sides of a block advance together through FGMRES.
@@ -69,11 +72,40 @@ __global__ void __launch_bounds__(256) k_spmm_long(const int32_t *__restrict__ r
     }
 }
 
+// Event timing of the sparse matrix-multi-vector kernel (the dominant
+// kernel of the solves) with its algorithmic bytes, enabled between
+// g2p_profile_begin and g2p_profile_end.
+struct KernelProfile {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;
+    size_t used = 0;
+    double bytes = 0;
+    int64_t launches = 0;
+};
+static KernelProfile g_prof;
+
+static void prof_event(cudaStream_t s) {
+    if (g_prof.used == g_prof.ev.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        g_prof.ev.push_back(e);
+    }
+    cudaEventRecord(g_prof.ev[g_prof.used++], s);
+}
+
 template <class T>
 void spmm_b(const Csr<T> &A, const int32_t *long_rows, int64_t nlong, const T *x, T *y, int k, const T *b,
             cudaStream_t s) {
-    k_spmm<T><<<grid_for(A.n * k, 256, 152LL * 48), 256, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y, k, b);
-    if (nlong > 0) k_spmm_long<T><<<(unsigned)nlong, 256, 0, s>>>(long_rows, A.ptr, A.col, A.val, x, y, k, b);
+    bool prof = g_prof.on && g_prof.used + 2 <= (size_t)1 << 20;
+    if (prof) {
+        prof_event(s);
+        g_prof.bytes += (double)A.nnz * (sizeof(T) + 4) + (double)(A.n + 1) * 8 +
+                        (double)A.n * k * sizeof(T) * (b ? 3 : 2);
+        g_prof.launches++;
+    }
+    (g2p::launch_tick(), k_spmm<T><<<grid_for(A.n * k, 256, 152LL * 48), 256, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y, k, b));
+    if (prof) prof_event(s);
+    if (nlong > 0) (g2p::launch_tick(), k_spmm_long<T><<<(unsigned)nlong, 256, 0, s>>>(long_rows, A.ptr, A.col, A.val, x, y, k, b));
 }
 
 template <class T>
@@ -111,7 +143,7 @@ g2p_status find_long_rows_t(const Csr<T> &A, int32_t **rows, int64_t *nlong, cud
     *rows = nullptr;
     if (*nlong > 0) {
         G2P_TRY(dalloc(rows, *nlong, s));
-        k_list_long<<<grid_for(n), kThreads, 0, s>>>(n, A.ptr, pos, *rows);
+        (g2p::launch_tick(), k_list_long<<<grid_for(n), kThreads, 0, s>>>(n, A.ptr, pos, *rows));
     }
     dfree(pos, s); dfree(work, s);
     return G2P_OK;
@@ -167,8 +199,8 @@ template <class T>
 void colnorms(const T *x, int64_t n, int k, double *partial, double *out, cudaStream_t s) {
     int kx = pow2_at_least(k);
     dim3 blk(kx, 256 / kx);
-    k_colsq_partial<T><<<kRedBlocks, blk, 0, s>>>(x, n, k, partial);
-    k_reduce_partials<<<(k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, k, out, true);
+    (g2p::launch_tick(), k_colsq_partial<T><<<kRedBlocks, blk, 0, s>>>(x, n, k, partial));
+    (g2p::launch_tick(), k_reduce_partials<<<(k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, k, out, true));
 }
 template void colnorms<double>(const double *, int64_t, int, double *, double *, cudaStream_t);
 template void colnorms<float>(const float *, int64_t, int, double *, double *, cudaStream_t);
@@ -236,15 +268,15 @@ static void chebyshev(Level<T> &L, int deg, double ratio, const T *b, T *x, bool
     int64_t nk = L.n * k;
     unsigned g = grid_for(nk);
     if (zero_guess) {
-        k_cheb_first<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, b, x, L.d, 1.0 / theta, false);
+        (g2p::launch_tick(), k_cheb_first<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, b, x, L.d, 1.0 / theta, false));
     } else {
         spmm_b<T>(L.A, L.long_rows, L.nlong, x, L.t0, k, b, s);
-        k_cheb_first<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, L.t0, x, L.d, 1.0 / theta, true);
+        (g2p::launch_tick(), k_cheb_first<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, L.t0, x, L.d, 1.0 / theta, true));
     }
     for (int it = 1; it < deg; it++) {
         spmm_b<T>(L.A, L.long_rows, L.nlong, x, L.t0, k, b, s);
         double rn = 1.0 / (2.0 * sigma - rho);
-        k_cheb_step<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, L.t0, x, L.d, rn * rho, 2.0 * rn / delta);
+        (g2p::launch_tick(), k_cheb_step<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, L.t0, x, L.d, rn * rho, 2.0 * rn / delta));
         rho = rn;
     }
 }
@@ -285,10 +317,22 @@ __global__ void k_dense_apply(int64_t n, int k, const double *Ainv, const T *b, 
 }
 
 template <class T>
+__global__ void k_prolong_csr(int64_t n, int k, const int64_t *ptr, const int32_t *col, const T *val, const T *xc, T *x) {
+    int64_t total = n * k;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = t / k;
+        int r = (int)(t - i * k);
+        double acc = (double)x[t];
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) acc += (double)val[q] * (double)xc[(int64_t)col[q] * k + r];
+        x[t] = (T)acc;
+    }
+}
+
+template <class T>
 static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaStream_t s) {
     Level<T> &L = H.lv[l];
     if (l == (int)H.lv.size() - 1) {
-        if (H.cinv) k_dense_apply<T><<<grid_for(L.n * k), kThreads, 0, s>>>(L.n, k, H.cinv, L.b, L.x);
+        if (H.cinv) (g2p::launch_tick(), k_dense_apply<T><<<grid_for(L.n * k), kThreads, 0, s>>>(L.n, k, H.cinv, L.b, L.x));
         else {
             chebyshev<T>(L, 4, cfg.cheb_ratio, L.b, L.x, true, k, s);
             for (int q = 0; q < 4; q++) chebyshev<T>(L, 4, cfg.cheb_ratio, L.b, L.x, false, k, s);
@@ -298,9 +342,9 @@ static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaS
     chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, L.b, L.x, true, k, s);
     spmm_b<T>(L.A, L.long_rows, L.nlong, L.x, L.t0, k, L.b, s);
     Level<T> &C = H.lv[l + 1];
-    k_restrict<T><<<grid_for(C.n * k), kThreads, 0, s>>>(C.n, k, L.rptr, L.rmem, L.t0, C.b);
+    (g2p::launch_tick(), k_restrict<T><<<grid_for(C.n * k), kThreads, 0, s>>>(C.n, k, L.rptr, L.rmem, L.t0, C.b));
     vcycle<T>(H, cfg, l + 1, k, s);
-    k_prolong<T><<<grid_for(L.n * k), kThreads, 0, s>>>(L.n, k, L.agg, C.x, L.x);
+    (g2p::launch_tick(), k_prolong_csr<T><<<grid_for(L.n * k), kThreads, 0, s>>>(L.n, k, L.P.ptr, L.P.col, L.P.val, C.x, L.x));
     chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, L.b, L.x, false, k, s);
 }
 
@@ -530,10 +574,102 @@ __global__ void __launch_bounds__(1024) k_gauss_jordan(double *a, double *inv, i
     }
 }
 
+
+// Smoothed prolongation row i: T row plus -w/a_ii * sum_j a_ij T row j,
+// columns deduplicated in first-seen order then sorted.
+constexpr int kPsMax = kLongRow + 1;
+__device__ __forceinline__ int ps_row(int64_t i, const int64_t *ptr, const int32_t *col, const double *val,
+                                      const double *diag, const int32_t *agg, double w, int32_t *cols, double *vals) {
+    int nr = 0;
+    int32_t ai = agg[i];
+    if (ai >= 0) { cols[0] = ai; vals[0] = 1.0; nr = 1; }
+    int64_t s0 = ptr[i], s1 = ptr[i + 1];
+    if (s1 - s0 > kLongRow || diag[i] == 0.0) return nr;
+    double f = -w / diag[i];
+    for (int64_t q = s0; q < s1; q++) {
+        int32_t aj = agg[col[q]];
+        if (aj < 0) continue;
+        int t = 0;
+        while (t < nr && cols[t] != aj) t++;
+        if (t == nr) { cols[nr] = aj; vals[nr] = 0.0; nr++; }
+        vals[t] += f * val[q];
+    }
+    for (int a = 1; a < nr; a++) {
+        int32_t c = cols[a]; double v = vals[a];
+        int b = a - 1;
+        while (b >= 0 && cols[b] > c) { cols[b + 1] = cols[b]; vals[b + 1] = vals[b]; b--; }
+        cols[b + 1] = c; vals[b + 1] = v;
+    }
+    return nr;
+}
+
+__global__ void k_ps_count(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
+                           const int32_t *agg, double w, int64_t *cnt) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t cols[kPsMax];
+        double vals[kPsMax];
+        cnt[i] = ps_row(i, ptr, col, val, diag, agg, w, cols, vals);
+    }
+}
+
+__global__ void k_ps_fill(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
+                          const int32_t *agg, double w, const int64_t *pptr, int32_t *pcol, double *pval) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t cols[kPsMax];
+        double vals[kPsMax];
+        int nr = ps_row(i, ptr, col, val, diag, agg, w, cols, vals);
+        int64_t o = pptr[i];
+        for (int t = 0; t < nr; t++) { pcol[o + t] = cols[t]; pval[o + t] = vals[t]; }
+    }
+}
+
+// (T^T A): rows of A summed by aggregate; key agg(i) * n + j
+__global__ void k_ta_count(int64_t n, const int64_t *ptr, const int32_t *agg, int64_t *cnt) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        cnt[i] = agg[i] >= 0 ? ptr[i + 1] - ptr[i] : 0;
+}
+__global__ void k_ta_expand(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const int32_t *agg,
+                            const int64_t *off, uint64_t ncols, uint64_t *keys, double *vals) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int32_t a = agg[i];
+        if (a < 0) continue;
+        int64_t o = off[i];
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++, o++) {
+            keys[o] = (uint64_t)a * ncols + (uint64_t)col[q];
+            vals[o] = val[q];
+        }
+    }
+}
+// (T^T A) P: key I * nc + J
+__global__ void k_bp_count(int64_t nr, const int64_t *bptr, const int32_t *bcol, const int64_t *pptr, int64_t *cnt) {
+    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nr; I += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c = 0;
+        for (int64_t q = bptr[I]; q < bptr[I + 1]; q++) c += pptr[bcol[q] + 1] - pptr[bcol[q]];
+        cnt[I] = c;
+    }
+}
+__global__ void k_bp_expand(int64_t nr, const int64_t *bptr, const int32_t *bcol, const double *bval, const int64_t *pptr,
+                            const int32_t *pcol, const double *pval, const int64_t *off, uint64_t nc, uint64_t *keys,
+                            double *vals) {
+    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nr; I += (int64_t)gridDim.x * blockDim.x) {
+        int64_t o = off[I];
+        for (int64_t q = bptr[I]; q < bptr[I + 1]; q++) {
+            int64_t j = bcol[q];
+            double b = bval[q];
+            for (int64_t t = pptr[j]; t < pptr[j + 1]; t++, o++) {
+                keys[o] = (uint64_t)I * nc + (uint64_t)pcol[t];
+                vals[o] = b * pval[t];
+            }
+        }
+    }
+}
+
+
 template <class T>
 void Hierarchy<T>::release(cudaStream_t s) {
     for (auto &L : lv) {
         L.A.release(s);
+        L.P.release(s);
         dfree(L.long_rows, s); dfree(L.dinv, s); dfree(L.agg, s); dfree(L.rptr, s); dfree(L.rmem, s);
         dfree(L.x, s); dfree(L.b, s); dfree(L.t0, s); dfree(L.t1, s); dfree(L.d, s);
     }
@@ -548,6 +684,61 @@ static int key_bits(uint64_t v) {
     int b = 0;
     while (b < 64 && (v >> b) != 0) b++;
     return b < 8 ? 8 : ((b + 7) / 8) * 8;
+}
+
+// Sorted, ordered reduction of expanded (key, value) pairs into a CSR with
+// nrows rows and key = row * ncols + col.
+static g2p_status esc_to_csr(uint64_t *&k0, double *&v0, int64_t ne, int64_t nrows, int64_t ncols, cudaStream_t s,
+                             Csr<double> &out) {
+    uint64_t *k1;
+    double *v1;
+    G2P_TRY(dalloc(&k1, ne, s));
+    G2P_TRY(dalloc(&v1, ne, s));
+    int64_t *counts, *work;
+    int64_t wn = scan_work_size(std::max(sort_counts_size(ne), ne + 1) + nrows + 1) + 8;
+    G2P_TRY(dalloc(&counts, sort_counts_size(ne), s));
+    G2P_TRY(dalloc(&work, wn, s));
+    bool in1 = false;
+    G2P_TRY(radix_sort_pairs(k0, v0, k1, v1, ne, key_bits((uint64_t)nrows * (uint64_t)ncols), counts, work, &in1, s));
+    dfree(counts, s);
+    uint64_t *sk = in1 ? k1 : k0;
+    double *sv = in1 ? v1 : v0;
+    int64_t *head, *segid;
+    G2P_TRY(dalloc(&head, ne + 1, s));
+    G2P_TRY(dalloc(&segid, ne + 1, s));
+    (g2p::launch_tick(), k_heads64<<<grid_for(ne), kThreads, 0, s>>>(sk, ne, head));
+    const int64_t *hp = head;
+    auto hop = [hp, ne] __device__(int64_t i) -> int64_t { return i < ne ? hp[i] : 0; };
+    G2P_TRY(exclusive_scan(hop, ne + 1, segid, work, s));
+    int64_t nseg = 0;
+    G2P_CUDA(cudaMemcpyAsync(&nseg, segid + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    out.n = nrows; out.m = ncols; out.nnz = nseg;
+    int64_t *rowcnt;
+    G2P_TRY(dalloc(&rowcnt, nrows + 1, s));
+    G2P_CUDA(cudaMemsetAsync(rowcnt, 0, sizeof(int64_t) * (nrows + 1), s));
+    G2P_TRY(dalloc(&out.col, nseg, s)); G2P_TRY(dalloc(&out.val, nseg, s)); G2P_TRY(dalloc(&out.ptr, nrows + 1, s));
+    (g2p::launch_tick(), k_seg_reduce<<<grid_for(ne), kThreads, 0, s>>>(sk, sv, ne, segid, (uint64_t)ncols, rowcnt, out.col, out.val));
+    const int64_t *rc = rowcnt;
+    auto rcop = [rc, nrows] __device__(int64_t i) -> int64_t { return i < nrows ? rc[i] : 0; };
+    G2P_TRY(exclusive_scan(rcop, nrows + 1, out.ptr, work, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    dfree(rowcnt, s); dfree(head, s); dfree(segid, s); dfree(work, s);
+    dfree(k0, s); dfree(k1, s); dfree(v0, s); dfree(v1, s);
+    k0 = nullptr; v0 = nullptr;
+    return G2P_OK;
+}
+
+// Row lengths -> offsets (exclusive scan); returns the total.
+static g2p_status offsets_of(const int64_t *cnt, int64_t n, int64_t *off, cudaStream_t s, int64_t *total) {
+    int64_t *work;
+    G2P_TRY(dalloc(&work, scan_work_size(n + 1) + 4, s));
+    auto op = [cnt, n] __device__(int64_t i) -> int64_t { return i < n ? cnt[i] : 0; };
+    G2P_TRY(exclusive_scan(op, n + 1, off, work, s));
+    G2P_CUDA(cudaMemcpyAsync(total, off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    dfree(work, s);
+    return G2P_OK;
 }
 
 g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_t s, int64_t *, Hierarchy<double> &H) {
@@ -578,9 +769,9 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
         double *diag;
         G2P_TRY(dalloc(&diag, n, s));
         G2P_TRY(dalloc(&L.dinv, n, s));
-        k_diag<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag);
+        (g2p::launch_tick(), k_diag<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag));
         G2P_CUDA(cudaMemsetAsync(d_lmax, 0, sizeof(unsigned long long), s));
-        k_dinv_gersh<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.val, diag, L.dinv, d_lmax);
+        (g2p::launch_tick(), k_dinv_gersh<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.val, diag, L.dinv, d_lmax));
         unsigned long long lb = 0;
         G2P_CUDA(cudaMemcpyAsync(&lb, d_lmax, sizeof(lb), cudaMemcpyDeviceToHost, s));
         G2P_TRY(find_long_rows_t<double>(L.A, &L.long_rows, &L.nlong, s));   // synchronizes
@@ -595,13 +786,13 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             uint64_t *T, *M1, *M2;
             G2P_TRY(dalloc(&dense, n, s)); G2P_TRY(dalloc(&T, n, s)); G2P_TRY(dalloc(&M1, n, s)); G2P_TRY(dalloc(&M2, n, s));
             unsigned g = grid_for(n);
-            k_agg_init<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, lim, cfg.strength, dense, T);
-            k_agg_state<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T);
+            (g2p::launch_tick(), k_agg_init<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, lim, cfg.strength, dense, T));
+            (g2p::launch_tick(), k_agg_state<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T));
             for (int round = 0; round < 200; round++) {
-                k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, M1);
-                k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, M1, M2);
+                (g2p::launch_tick(), k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, M1));
+                (g2p::launch_tick(), k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, M1, M2));
                 G2P_CUDA(cudaMemsetAsync(d_int, 0, sizeof(int), s));
-                k_mis_update<<<g, kThreads, 0, s>>>(n, T, M2, d_int);
+                (g2p::launch_tick(), k_mis_update<<<g, kThreads, 0, s>>>(n, T, M2, d_int));
                 int und = 0;
                 G2P_CUDA(cudaMemcpyAsync(&und, d_int, sizeof(int), cudaMemcpyDeviceToHost, s));
                 G2P_CUDA(cudaStreamSynchronize(s));
@@ -623,8 +814,8 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             int32_t *agg1;
             G2P_TRY(dalloc(&agg1, n, s));
             G2P_TRY(dalloc(&L.agg, n, s));
-            k_agg_phase1<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, rootid, agg1);
-            k_agg_phase2<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, agg1, L.agg);
+            (g2p::launch_tick(), k_agg_phase1<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, rootid, agg1));
+            (g2p::launch_tick(), k_agg_phase2<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, agg1, L.agg));
             G2P_CUDA(cudaStreamSynchronize(s));
             dfree(agg1, s); dfree(rootid, s); dfree(dense, s); dfree(T, s); dfree(M1, s); dfree(M2, s);
             if (nc == 0 || nc > (n * 9) / 10) {
@@ -643,7 +834,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 uint32_t *k0, *k1;
                 int32_t *v0, *v1;
                 G2P_TRY(dalloc(&k0, nm, s)); G2P_TRY(dalloc(&k1, nm, s)); G2P_TRY(dalloc(&v0, nm, s)); G2P_TRY(dalloc(&v1, nm, s));
-                k_agg_key<<<g, kThreads, 0, s>>>(n, L.agg, pos, k0, v0);
+                (g2p::launch_tick(), k_agg_key<<<g, kThreads, 0, s>>>(n, L.agg, pos, k0, v0));
                 int64_t *counts;
                 G2P_TRY(dalloc(&counts, sort_counts_size(nm), s));
                 G2P_TRY(need_work(sort_counts_size(nm)));
@@ -651,57 +842,47 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 G2P_TRY(radix_sort_pairs(k0, v0, k1, v1, nm, key_bits((uint64_t)nc), counts, work, &in1, s));
                 dfree(counts, s);
                 G2P_TRY(dalloc(&L.rptr, nc + 1, s));
-                k_member_ptr<<<grid_for(nm + 1), kThreads, 0, s>>>(nm, in1 ? k1 : k0, nc, L.rptr);
+                (g2p::launch_tick(), k_member_ptr<<<grid_for(nm + 1), kThreads, 0, s>>>(nm, in1 ? k1 : k0, nc, L.rptr));
                 L.rmem = in1 ? v1 : v0;
                 dfree(in1 ? v0 : v1, s);
                 dfree(k0, s); dfree(k1, s); dfree(pos, s);
-                // ---- Galerkin coarse operator
+                // ---- smoothed prolongation P = (I - w D^-1 A) T
+                double w = 4.0 / (3.0 * L.lmax);
+                int64_t *pc;
+                G2P_TRY(dalloc(&pc, n + 1, s));
+                G2P_TRY(dalloc(&L.P.ptr, n + 1, s));
+                (g2p::launch_tick(), k_ps_count<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, L.agg, w, pc));
+                int64_t pnnz = 0;
+                G2P_TRY(offsets_of(pc, n, L.P.ptr, s, &pnnz));
+                dfree(pc, s);
+                L.P.n = n; L.P.m = nc; L.P.nnz = pnnz;
+                G2P_TRY(dalloc(&L.P.col, pnnz, s)); G2P_TRY(dalloc(&L.P.val, pnnz, s));
+                (g2p::launch_tick(), k_ps_fill<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, L.agg, w, L.P.ptr, L.P.col, L.P.val));
+                // ---- B = T^T A (nc x n)
                 int64_t *cnt, *off;
-                G2P_TRY(dalloc(&cnt, n + 1, s));
-                G2P_TRY(dalloc(&off, n + 1, s));
-                k_rap_count<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.agg, cnt);
-                const int64_t *cp = cnt;
-                auto cop = [cp, n] __device__(int64_t i) -> int64_t { return i < n ? cp[i] : 0; };
-                G2P_TRY(exclusive_scan(cop, n + 1, off, work, s));
+                G2P_TRY(dalloc(&cnt, n + 1, s)); G2P_TRY(dalloc(&off, n + 1, s));
+                (g2p::launch_tick(), k_ta_count<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.agg, cnt));
                 int64_t ne = 0;
-                G2P_CUDA(cudaMemcpyAsync(&ne, off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-                G2P_CUDA(cudaStreamSynchronize(s));
-                uint64_t *ek0, *ek1;
-                double *ev0, *ev1;
-                G2P_TRY(dalloc(&ek0, ne, s)); G2P_TRY(dalloc(&ek1, ne, s)); G2P_TRY(dalloc(&ev0, ne, s)); G2P_TRY(dalloc(&ev1, ne, s));
-                k_rap_expand<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.agg, off, (uint64_t)nc, ek0, ev0);
+                G2P_TRY(offsets_of(cnt, n, off, s, &ne));
+                uint64_t *ek0;
+                double *ev0;
+                G2P_TRY(dalloc(&ek0, ne, s)); G2P_TRY(dalloc(&ev0, ne, s));
+                (g2p::launch_tick(), k_ta_expand<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.agg, off, (uint64_t)n, ek0, ev0));
                 dfree(cnt, s); dfree(off, s);
-                G2P_TRY(dalloc(&counts, sort_counts_size(ne), s));
-                G2P_TRY(need_work(sort_counts_size(ne)));
-                G2P_TRY(radix_sort_pairs(ek0, ev0, ek1, ev1, ne, key_bits((uint64_t)nc * (uint64_t)nc), counts, work, &in1, s));
-                dfree(counts, s);
-                uint64_t *sk = in1 ? ek1 : ek0;
-                double *sv = in1 ? ev1 : ev0;
-                int64_t *head, *segid;
-                G2P_TRY(dalloc(&head, ne + 1, s)); G2P_TRY(dalloc(&segid, ne + 1, s));
-                k_heads64<<<grid_for(ne), kThreads, 0, s>>>(sk, ne, head);
-                const int64_t *hp = head;
-                G2P_TRY(need_work(ne + 1));
-                auto hop = [hp, ne] __device__(int64_t i) -> int64_t { return i < ne ? hp[i] : 0; };
-                G2P_TRY(exclusive_scan(hop, ne + 1, segid, work, s));
-                int64_t nseg = 0;
-                G2P_CUDA(cudaMemcpyAsync(&nseg, segid + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-                G2P_CUDA(cudaStreamSynchronize(s));
+                Csr<double> B;
+                G2P_TRY(esc_to_csr(ek0, ev0, ne, nc, n, s, B));
+                // ---- A_c = B P (nc x nc)
+                G2P_TRY(dalloc(&cnt, nc + 1, s)); G2P_TRY(dalloc(&off, nc + 1, s));
+                (g2p::launch_tick(), k_bp_count<<<grid_for(nc), kThreads, 0, s>>>(nc, B.ptr, B.col, L.P.ptr, cnt));
+                G2P_TRY(offsets_of(cnt, nc, off, s, &ne));
+                G2P_TRY(dalloc(&ek0, ne, s)); G2P_TRY(dalloc(&ev0, ne, s));
+                (g2p::launch_tick(), k_bp_expand<<<grid_for(nc), kThreads, 0, s>>>(nc, B.ptr, B.col, B.val, L.P.ptr, L.P.col, L.P.val, off,
+                                                            (uint64_t)nc, ek0, ev0));
+                dfree(cnt, s); dfree(off, s);
+                B.release(s);
                 Level<double> C;
                 C.n = nc;
-                C.A.n = C.A.m = nc; C.A.nnz = nseg;
-                int64_t *rowcnt;
-                G2P_TRY(dalloc(&rowcnt, nc + 1, s));
-                G2P_CUDA(cudaMemsetAsync(rowcnt, 0, sizeof(int64_t) * (nc + 1), s));
-                G2P_TRY(dalloc(&C.A.col, nseg, s)); G2P_TRY(dalloc(&C.A.val, nseg, s)); G2P_TRY(dalloc(&C.A.ptr, nc + 1, s));
-                k_seg_reduce<<<grid_for(ne), kThreads, 0, s>>>(sk, sv, ne, segid, (uint64_t)nc, rowcnt, C.A.col, C.A.val);
-                const int64_t *rc = rowcnt;
-                G2P_TRY(need_work(nc + 1));
-                auto rcop = [rc, nc] __device__(int64_t i) -> int64_t { return i < nc ? rc[i] : 0; };
-                G2P_TRY(exclusive_scan(rcop, nc + 1, C.A.ptr, work, s));
-                G2P_CUDA(cudaStreamSynchronize(s));
-                dfree(rowcnt, s); dfree(head, s); dfree(segid, s);
-                dfree(ek0, s); dfree(ek1, s); dfree(ev0, s); dfree(ev1, s);
+                G2P_TRY(esc_to_csr(ek0, ev0, ne, nc, nc, s, C.A));
                 L.nc = nc;
                 H.lv.push_back(C);
             }
@@ -716,9 +897,9 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             G2P_TRY(dalloc(&Dm, nn * nn, s));
             G2P_TRY(dalloc(&H.cinv, nn * nn, s));
             G2P_CUDA(cudaMemsetAsync(Dm, 0, sizeof(double) * nn * nn, s));
-            k_dense_fill<<<grid_for(nn), kThreads, 0, s>>>(nn, Cl.A.ptr, Cl.A.col, Cl.A.val, Dm);
+            (g2p::launch_tick(), k_dense_fill<<<grid_for(nn), kThreads, 0, s>>>(nn, Cl.A.ptr, Cl.A.col, Cl.A.val, Dm));
             G2P_CUDA(cudaMemsetAsync(d_int, 0, sizeof(int), s));
-            k_gauss_jordan<<<1, 1024, 0, s>>>(Dm, H.cinv, nn, d_int);
+            (g2p::launch_tick(), k_gauss_jordan<<<1, 1024, 0, s>>>(Dm, H.cinv, nn, d_int));
             G2P_CUDA(cudaStreamSynchronize(s));
             dfree(Dm, s);
             break;
@@ -746,12 +927,19 @@ g2p_status amg_to_float(const Hierarchy<double> &H, cudaStream_t s, Hierarchy<fl
         G2P_TRY(dalloc(&f.A.ptr, L.A.n + 1, s)); G2P_TRY(dalloc(&f.A.col, L.A.nnz, s)); G2P_TRY(dalloc(&f.A.val, L.A.nnz, s));
         G2P_CUDA(cudaMemcpyAsync(f.A.ptr, L.A.ptr, sizeof(int64_t) * (L.A.n + 1), cudaMemcpyDeviceToDevice, s));
         G2P_CUDA(cudaMemcpyAsync(f.A.col, L.A.col, sizeof(int32_t) * L.A.nnz, cudaMemcpyDeviceToDevice, s));
-        k_d2f<<<grid_for(L.A.nnz), kThreads, 0, s>>>(L.A.val, f.A.val, L.A.nnz);
+        (g2p::launch_tick(), k_d2f<<<grid_for(L.A.nnz), kThreads, 0, s>>>(L.A.val, f.A.val, L.A.nnz));
         G2P_TRY(dalloc(&f.dinv, L.n, s));
-        k_d2f<<<grid_for(L.n), kThreads, 0, s>>>(L.dinv, f.dinv, L.n);
+        (g2p::launch_tick(), k_d2f<<<grid_for(L.n), kThreads, 0, s>>>(L.dinv, f.dinv, L.n));
         if (L.nlong > 0) {
             G2P_TRY(dalloc(&f.long_rows, L.nlong, s));
             G2P_CUDA(cudaMemcpyAsync(f.long_rows, L.long_rows, sizeof(int32_t) * L.nlong, cudaMemcpyDeviceToDevice, s));
+        }
+        if (L.P.ptr) {
+            f.P.n = L.P.n; f.P.m = L.P.m; f.P.nnz = L.P.nnz;
+            G2P_TRY(dalloc(&f.P.ptr, L.P.n + 1, s)); G2P_TRY(dalloc(&f.P.col, L.P.nnz, s)); G2P_TRY(dalloc(&f.P.val, L.P.nnz, s));
+            G2P_CUDA(cudaMemcpyAsync(f.P.ptr, L.P.ptr, sizeof(int64_t) * (L.P.n + 1), cudaMemcpyDeviceToDevice, s));
+            G2P_CUDA(cudaMemcpyAsync(f.P.col, L.P.col, sizeof(int32_t) * L.P.nnz, cudaMemcpyDeviceToDevice, s));
+            (g2p::launch_tick(), k_d2f<<<grid_for(L.P.nnz), kThreads, 0, s>>>(L.P.val, f.P.val, L.P.nnz));
         }
         if (L.agg) {
             G2P_TRY(dalloc(&f.agg, L.n, s));
@@ -904,8 +1092,8 @@ template <class T>
 static void mdot(const T *V, int64_t n, int J, const T *w, int k, double *partial, double *out, cudaStream_t s) {
     int kx = pow2_at_least(k);
     dim3 blk(kx, 256 / kx);
-    k_mdot_partial<T><<<kRedBlocks, blk, 0, s>>>(V, n, J, w, k, partial);
-    k_reduce_partials<<<(J * k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, J * k, out, false);
+    (g2p::launch_tick(), k_mdot_partial<T><<<kRedBlocks, blk, 0, s>>>(V, n, J, w, k, partial));
+    (g2p::launch_tick(), k_reduce_partials<<<(J * k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, J * k, out, false));
 }
 
 __global__ void k_add_vec(double *a, const double *b, int n) {
@@ -943,8 +1131,8 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
         rep.rel_residual = worst;
         if (worst <= cfg.rtol) { rep.converged = true; break; }
         if (it >= cfg.maxit) break;
-        k_start<T><<<g, kThreads, 0, s>>>(nk, k, K.r, K.beta, K.V);
-        k_g_init<<<(k + 63) / 64, 64, 0, s>>>(k, m, K.beta, K.g);
+        (g2p::launch_tick(), k_start<T><<<g, kThreads, 0, s>>>(nk, k, K.r, K.beta, K.V));
+        (g2p::launch_tick(), k_g_init<<<(k + 63) / 64, 64, 0, s>>>(k, m, K.beta, K.g));
         int j = 0;
         for (; j < m && it < cfg.maxit; j++) {
             T *Vj = K.V + (int64_t)j * nk, *Zj = K.Z + (int64_t)j * nk;
@@ -955,17 +1143,17 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
             spmm<T>(A, L0.long_rows, L0.nlong, Zj, K.w, k, s);
             // classical Gram-Schmidt, optionally twice
             mdot<T>(K.V, n, j + 1, K.w, k, K.partial, K.hcol, s);
-            k_maxpy<T><<<g, kThreads, 0, s>>>(K.V, nk, j + 1, K.hcol, k, K.w);
+            (g2p::launch_tick(), k_maxpy<T><<<g, kThreads, 0, s>>>(K.V, nk, j + 1, K.hcol, k, K.w));
             if (cfg.reorth) {
                 mdot<T>(K.V, n, j + 1, K.w, k, K.partial, dots2, s);
-                k_maxpy<T><<<g, kThreads, 0, s>>>(K.V, nk, j + 1, dots2, k, K.w);
-                k_add_vec<<<((j + 1) * k + 255) / 256, 256, 0, s>>>(K.hcol, dots2, (j + 1) * k);
+                (g2p::launch_tick(), k_maxpy<T><<<g, kThreads, 0, s>>>(K.V, nk, j + 1, dots2, k, K.w));
+                (g2p::launch_tick(), k_add_vec<<<((j + 1) * k + 255) / 256, 256, 0, s>>>(K.hcol, dots2, (j + 1) * k));
             }
             double *hnorm = K.beta;   // reuse
             colnorms<T>(K.w, n, k, K.partial, hnorm, s);
-            k_arnoldi_finish<T><<<g, kThreads, 0, s>>>(nk, k, hnorm, K.w, K.V + (int64_t)(j + 1) * nk);
+            (g2p::launch_tick(), k_arnoldi_finish<T><<<g, kThreads, 0, s>>>(nk, k, hnorm, K.w, K.V + (int64_t)(j + 1) * nk));
             double *est = K.y;        // scratch for the estimates (k values)
-            k_givens<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.hcol, hnorm, K.H, K.cs, K.sn, K.g, K.bnorm, est);
+            (g2p::launch_tick(), k_givens<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.hcol, hnorm, K.H, K.cs, K.sn, K.g, K.bnorm, est));
             G2P_CUDA(cudaMemcpyAsync(K.h_est, est, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
             G2P_CUDA(cudaStreamSynchronize(s));
             it++;
@@ -973,8 +1161,8 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
             for (int r = 0; r < k; r++) worst = std::max(worst, K.h_est[r]);
             if (worst <= cfg.rtol) { j++; break; }
         }
-        k_backsolve<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.H, K.g, K.y);
-        k_xupdate<T><<<g, kThreads, 0, s>>>(nk, k, m, j, K.Z, K.y, x);
+        (g2p::launch_tick(), k_backsolve<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.H, K.g, K.y));
+        (g2p::launch_tick(), k_xupdate<T><<<g, kThreads, 0, s>>>(nk, k, m, j, K.Z, K.y, x));
     }
     rep.iterations = it;
     G2P_CUDA(cudaGetLastError());
@@ -986,3 +1174,27 @@ template g2p_status fgmres<float>(const Csr<float> &, Hierarchy<float> &, Krylov
                                   const SolverConfig &, const double *, cudaStream_t, SolveReport &);
 
 }  // namespace g2p
+
+extern "C" void g2p_profile_begin(void) {
+    g2p::g_prof.on = true;
+    g2p::g_prof.used = 0;
+    g2p::g_prof.bytes = 0;
+    g2p::g_prof.launches = 0;
+}
+
+extern "C" g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, int64_t *launches) {
+    using namespace g2p;
+    g_prof.on = false;
+    G2P_CUDA(cudaDeviceSynchronize());
+    double ms = 0;
+    for (size_t i = 0; i + 1 < g_prof.used; i += 2) {
+        float t = 0;
+        G2P_CUDA(cudaEventElapsedTime(&t, g_prof.ev[i], g_prof.ev[i + 1]));
+        ms += t;
+    }
+    if (kernel_ms) *kernel_ms = ms;
+    if (kernel_bytes) *kernel_bytes = g_prof.bytes;
+    if (launches) *launches = g_prof.launches;
+    g_prof.used = 0;
+    return G2P_OK;
+}

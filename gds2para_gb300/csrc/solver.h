@@ -15,6 +15,7 @@ struct Level {
     T *dinv = nullptr;          // 1 / a_ii
     double lmax = 2.0;          // spectral radius estimate of D^-1 A
     int32_t *agg = nullptr;     // aggregate of each row (-1: none)
+    Csr<T> P;                   // smoothed prolongation (n x nc)
     int64_t *rptr = nullptr;    // aggregate -> members (ascending)
     int32_t *rmem = nullptr;
     T *x = nullptr, *b = nullptr, *t0 = nullptr, *t1 = nullptr, *d = nullptr;
@@ -100,7 +101,8 @@ struct g2p_solver {
     g2p::Csr<double> A;                 // original FP64 operator
     int32_t *long_rows = nullptr;
     int64_t nlong = 0;
-    double *scale = nullptr;            // diagonal equilibration (mixed)
+    double *scale = nullptr;            // unused
+    double cscale = 1.0;                // mixed: power-of-two scale of the FP32 operator
     g2p::Csr<double> As;                // scaled operator (mixed, FP64 for setup)
     g2p::Hierarchy<double> H64;
     g2p::Hierarchy<float> H32;

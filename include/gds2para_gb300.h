@@ -14,7 +14,8 @@
  *            src/hypreSolver.h:14)              -> g2p_hypre_solve, g2p_solver_*
  *   paraGenerator (src/matrixCon.cpp:11)       -> g2p_para_generator
  *
- * All pointers in g2p_mesh_desc and every output buffer are HOST pointers
+ * Arrays in g2p_mesh_desc may live in host or device memory (they are
+ * copied with unified addressing); every output buffer is a HOST pointer
  * owned by the caller; device memory is owned by the handles.  Every entry
  * point returns a g2p_status and never exits the process; g2p_last_error()
  * describes the most recent failure of the calling thread.  A handle must be
@@ -163,6 +164,17 @@ g2p_status g2p_solver_destroy(g2p_solver *s);
  * reference's transposed storage of frequencies after the first.  Runs
  * g2p_index_maps and g2p_assemble_v0 first if they have not run. ---- */
 g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p, double *z_out, g2p_extract_stats *st);
+
+/* ---- diagnostics (no counterpart in the reference) ----
+ * g2p_launch_count: kernels launched by the library so far in this process.
+ * g2p_profile_begin/end: CUDA-event timing of the sparse matrix-multi-vector
+ * kernel (the solves' dominant kernel) between the two calls: total device
+ * milliseconds, algorithmic bytes (values + column indices + row offsets
+ * read once, vectors read and written once) and launches.  Single-threaded
+ * use only. */
+int64_t g2p_launch_count(void);
+void g2p_profile_begin(void);
+g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, int64_t *launches);
 
 #ifdef __cplusplus
 }

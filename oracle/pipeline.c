@@ -437,6 +437,10 @@ static int assemble_laplacian(const g2po_mesh *m, const g2po_v0 *v, int is_ac, g
     A->val = (double *)malloc(sizeof(double) * (size_t)cap);
     kv_t *row = NULL;
     int64_t rowcap = 0, nnz = 0;
+    /* pos[c]: slot of column c in the current row (the reference keeps an
+       unordered_map per row, fdtd.hpp:2779); reset after each row */
+    int64_t *pos = (int64_t *)malloc(sizeof(int64_t) * (size_t)(ncol + 1));
+    for (int64_t c = 0; c <= ncol; c++) pos[c] = -1;
     int64_t k = 0;
     for (int64_t c = 0; c < ncol; c++) {
         int64_t nr = 0;
@@ -477,16 +481,13 @@ static int assemble_laplacian(const g2po_mesh *m, const g2po_v0 *v, int is_ac, g
             /* unordered_map accumulation in entry order (off-diagonal first) */
             if (nr + 2 > rowcap) { rowcap = rowcap ? rowcap * 2 : 64; row = (kv_t *)realloc(row, sizeof(kv_t) * (size_t)rowcap); }
             if (other >= 0) {
-                int64_t t;
-                for (t = 0; t < nr; t++) if (row[t].col == other) break;
-                if (t == nr) { row[nr].col = other; row[nr].val = 0.0; nr++; }
-                row[t].val += off;
+                if (pos[other] < 0) { pos[other] = nr; row[nr].col = other; row[nr].val = 0.0; nr++; }
+                row[pos[other]].val += off;
             }
-            int64_t t;
-            for (t = 0; t < nr; t++) if (row[t].col == c) break;
-            if (t == nr) { row[nr].col = c; row[nr].val = 0.0; nr++; }
-            row[t].val += dg;
+            if (pos[c] < 0) { pos[c] = nr; row[nr].col = c; row[nr].val = 0.0; nr++; }
+            row[pos[c]].val += dg;
         }
+        for (int64_t t = 0; t < nr; t++) pos[row[t].col] = -1;
         qsort(row, (size_t)nr, sizeof(kv_t), cmp_kv);
         for (int64_t t = 0; t < nr; t++) {
             if (!is_ac && !(fabs(row[t].val) > 1e-8)) continue;    /* fdtd.hpp:2852 */
@@ -496,6 +497,7 @@ static int assemble_laplacian(const g2po_mesh *m, const g2po_v0 *v, int is_ac, g
         A->ptr[c + 1] = nnz;
     }
     free(row);
+    free(pos);
     return 0;
 }
 
