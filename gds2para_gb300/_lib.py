@@ -17,7 +17,7 @@ EXPORTS = [
     "g2p_index_maps", "g2p_generate_stiff", "g2p_export_stiff",
     "g2p_assemble_v0", "g2p_export_v0", "g2p_export_laplacian",
     "g2p_hypre_solve", "g2p_solver_create", "g2p_solver_solve", "g2p_solver_destroy",
-    "g2p_para_generator", "g2p_launch_count", "g2p_profile_begin", "g2p_profile_end",
+    "g2p_para_generator", "g2p_launch_count", "g2p_profile_begin", "g2p_profile_end", "g2p_profile_report",
 ]
 
 STATUS = {0: "G2P_OK", 1: "G2P_ERR_INVALID", 2: "G2P_ERR_CUDA", 3: "G2P_ERR_NOMEM", 4: "G2P_ERR_NOT_CONVERGED",
@@ -110,12 +110,22 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_profile_begin.restype = None
     L.g2p_profile_begin.argtypes = []
     L.g2p_profile_end.argtypes = [C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)]
+    L.g2p_profile_report.restype = C.c_int64
+    L.g2p_profile_report.argtypes = [C.c_char_p, i64]
     for name in EXPORTS:
         if name not in ("g2p_last_error", "g2p_version", "g2p_default_params", "g2p_launch_count",
-                        "g2p_profile_begin"):
+                        "g2p_profile_begin", "g2p_profile_report"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
+
+
+def profile_report() -> str:
+    L = load()
+    n = L.g2p_profile_report(None, 0)
+    buf = C.create_string_buffer(int(n) + 1)
+    L.g2p_profile_report(buf, int(n) + 1)
+    return buf.value.decode()
 
 
 def check(status: int, allow=(G2P_OK,)):

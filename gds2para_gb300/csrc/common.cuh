@@ -26,10 +26,17 @@ namespace g2p {
 
 void set_last_error(cudaError_t e, const char *what, const char *file, int line);
 void set_last_message(const char *fmt, ...);
+void retain_pool_memory(int device);
 
-// Counts kernel launches issued by the library (diagnostics).
+// Counts kernel launches issued by the library and, while profiling is on,
+// brackets each launch with CUDA events keyed by the kernel's name.
 void launch_tick();
 int64_t launch_count();
+void kbegin(const char *name, cudaStream_t s);
+void kend(cudaStream_t s);
+bool kprof_on();
+void kprof_set(bool on);
+g2p_status kprof_collect();
 
 constexpr int kSMs = 152;            // GB300: 2 dies x 76 SMs
 constexpr int kThreads = 256;

@@ -7,6 +7,7 @@
 // block are right-hand sides of one batched solve per system, the V0
 // products use the per-edge view (V y) and the column lists (V^T x) built at
 // assembly, and the operations keep the reference's order per entry.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -47,10 +48,10 @@ __global__ void k_div(int64_t n, double *x, double a) {
 
 // y[e, r] = V x over the (<= 2) entries of edge e in ascending column order
 __global__ void k_v0_apply(int64_t nedge, int k, const int32_t *ecol, const double *eval, const double *X, double *Y) {
-    int64_t total = nedge * k;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t e = t / k;
-        int r = (int)(t - e * k);
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    G2P_FOR_ROWS(e, nedge) {
+        int64_t t = e * k + r;
         double acc = 0.0;
         int32_t c0 = ecol[2 * e], c1 = ecol[2 * e + 1];
         if (c0 >= 0) acc += eval[2 * e] * (1.0 * X[(int64_t)c0 * k + r]);
@@ -77,10 +78,10 @@ struct EdgeFactor {
 // out[c, r] = sum over column c's entries (in order) of aval * f(src[e, r])
 __global__ void k_v0t_short(int64_t ncol, int k, const int64_t *cptr, const int32_t *cedge, const double *caval,
                             const double *src, EdgeFactor f, double *out) {
-    int64_t total = ncol * k;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t c = t / k;
-        int r = (int)(t - c * k);
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    G2P_FOR_ROWS(c, ncol) {
+        int64_t t = c * k + r;
         int64_t s0 = cptr[c], s1 = cptr[c + 1];
         if (s1 - s0 > kLongRow) continue;
         double acc = 0.0;
@@ -231,20 +232,25 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     t0 = std::chrono::steady_clock::now();
     g2p_solver *Sd = nullptr, *Sc = nullptr;
     G2P_TRY(g2p_solver_build(m->Ad, &p, s, &Sd));
-    g2p_status rs = g2p_solver_build(m->Ac, &p, s, &Sc);
+    // Ac, the conductor Laplacian, stays FP64: a floating wire grounded at one
+    // node gives it a condition number near (length/h)^2, beyond what an FP32
+    // refinement sweep resolves; it is an order of magnitude smaller than Ad.
+    g2p_solver_params pc = p;
+    pc.precision = G2P_PREC_FP64;
+    g2p_status rs = g2p_solver_build(m->Ac, &pc, s, &Sc);
     if (rs != G2P_OK) { g2p_solver_destroy(Sd); return rs; }
     local.setup_ms = ms_since(t0);
     local.ad_levels = Sd->levels;
     local.ac_levels = Sc->levels;
-    int32_t *d_long_d = nullptr;
-    int64_t nlong_d = 0;
+    LongRows lcol;   // long columns of V0d (conductor columns)
     {
-        // long columns of V0d (conductor columns)
         Csr<double> tmp;
         tmp.n = m->v0d.ncol; tmp.ptr = m->v0d.cptr;
-        G2P_TRY(find_long_rows(tmp, &d_long_d, &nlong_d, s));
+        G2P_TRY(find_long_rows<double>(tmp, lcol, s));
     }
-    const int kb = p.batch ? P : 1;
+    int32_t *d_long_d = lcol.rows;
+    int64_t nlong_d = lcol.n;
+    const int kb = p.batch ? std::min(P, kMaxRhs) : 1;
     const int64_t nd = m->v0d.ncol, nc = m->v0c.ncol, ne = d.N_edge;
     double *Bd, *Yd, *Bc, *Yc, *crhs, *yd1, *yc, *yd2, *zre, *zim;
     G2P_TRY(dalloc(&Bd, nd * kb, s)); G2P_TRY(dalloc(&Yd, nd * kb, s));
@@ -265,9 +271,9 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         G2P_CUDA(cudaMemcpyAsync(d_pe_port + e0, port_local.data(), sizeof(int32_t) * (e1 - e0), cudaMemcpyHostToDevice, s));
         // (1) b_d = -V0da^T J
         G2P_CUDA(cudaMemsetAsync(Bd, 0, sizeof(double) * nd * kk, s));
-        (g2p::launch_tick(), k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
-                                                           m->v0d.ecol, m->v0d.eaval, kk, Bd));
-        (g2p::launch_tick(), k_scale<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Bd, -1.0));
+        (g2p::kbegin("k_rhs_ports", s), k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
+                                                           m->v0d.ecol, m->v0d.eaval, kk, Bd), g2p::kend(s));
+        (g2p::kbegin("k_scale", s), k_scale<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Bd, -1.0), g2p::kend(s));
         g2p_solve_stats ss;
         g2p_status rc = g2p_solver_solve_dev(Sd, Bd, Yd, kk, &ss);
         if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }
@@ -275,15 +281,15 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         local.solves += kk; local.total_iterations += ss.iterations;
         local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
         // (2) y0d /= omega ; yd1 = V0d y0d
-        (g2p::launch_tick(), k_div<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Yd, omega));
-        (g2p::launch_tick(), k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd1));
+        (g2p::kbegin("k_div", s), k_div<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Yd, omega), g2p::kend(s));
+        (g2p::kbegin("k_v0_apply", s), k_v0_apply<<<row_grid(ne, kk), row_block(kk), 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd1), g2p::kend(s));
         // (3) b_c = -V0ca^T J + V0ca^T(-omega D_eps yd1)
         G2P_CUDA(cudaMemsetAsync(Bc, 0, sizeof(double) * nc * kk, s));
-        (g2p::launch_tick(), k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
-                                                           m->v0c.ecol, m->v0c.eaval, kk, Bc));
-        (g2p::launch_tick(), k_scale<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, -1.0));
-        (g2p::launch_tick(), k_v0t_short<<<grid_for(nc * kk), kThreads, 0, s>>>(nc, kk, m->v0c.cptr, m->v0c.cedge, m->v0c.caval, yd1, f0, crhs));
-        (g2p::launch_tick(), k_add<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, crhs));
+        (g2p::kbegin("k_rhs_ports", s), k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
+                                                           m->v0c.ecol, m->v0c.eaval, kk, Bc), g2p::kend(s));
+        (g2p::kbegin("k_scale", s), k_scale<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, -1.0), g2p::kend(s));
+        (g2p::kbegin("k_v0t_short", s), k_v0t_short<<<row_grid(nc, kk), row_block(kk), 0, s>>>(nc, kk, m->v0c.cptr, m->v0c.cedge, m->v0c.caval, yd1, f0, crhs), g2p::kend(s));
+        (g2p::kbegin("k_add", s), k_add<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, crhs), g2p::kend(s));
         // (4) Ac y0c = b_c
         rc = g2p_solver_solve_dev(Sc, Bc, Yc, kk, &ss);
         if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }
@@ -291,20 +297,20 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         local.solves += kk; local.total_iterations += ss.iterations;
         local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
         // (5) yc = V0c y0c ; b_d2 = V0da^T(-D_eps yc)
-        (g2p::launch_tick(), k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0c.ecol, m->v0c.eval, Yc, yc));
-        (g2p::launch_tick(), k_v0t_short<<<grid_for(nd * kk), kThreads, 0, s>>>(nd, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd));
+        (g2p::kbegin("k_v0_apply", s), k_v0_apply<<<row_grid(ne, kk), row_block(kk), 0, s>>>(ne, kk, m->v0c.ecol, m->v0c.eval, Yc, yc), g2p::kend(s));
+        (g2p::kbegin("k_v0t_short", s), k_v0t_short<<<row_grid(nd, kk), row_block(kk), 0, s>>>(nd, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd), g2p::kend(s));
         if (nlong_d > 0)
-            (g2p::launch_tick(), k_v0t_long<<<(unsigned)nlong_d, 256, 0, s>>>(d_long_d, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd));
+            (g2p::kbegin("k_v0t_long", s), k_v0t_long<<<(unsigned)nlong_d, 256, 0, s>>>(d_long_d, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd), g2p::kend(s));
         // (6) Ad y0d2 = b_d2 ; yd2 = V0d y0d2
         rc = g2p_solver_solve_dev(Sd, Bd, Yd, kk, &ss);
         if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }
         if (rc == G2P_ERR_NOT_CONVERGED) worst_rc = rc;
         local.solves += kk; local.total_iterations += ss.iterations;
         local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
-        (g2p::launch_tick(), k_v0_apply<<<grid_for(ne * kk), kThreads, 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd2));
+        (g2p::kbegin("k_v0_apply", s), k_v0_apply<<<row_grid(ne, kk), row_block(kk), 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd2), g2p::kend(s));
         // (7) Construct_Z_V0
-        (g2p::launch_tick(), k_construct_z<<<(P * kk + 127) / 128, 128, 0, s>>>(P, p0, kk, d_rptr, d_redge, d_rdir, d, m->xn, m->yn, m->zn, yd1,
-                                                          yc, yd2, d_cur, zre, zim));
+        (g2p::kbegin("k_construct_z", s), k_construct_z<<<(P * kk + 127) / 128, 128, 0, s>>>(P, p0, kk, d_rptr, d_redge, d_rdir, d, m->xn, m->yn, m->zn, yd1,
+                                                          yc, yd2, d_cur, zre, zim), g2p::kend(s));
     }
     // ---- print_z_V0 layout
     std::vector<double> fr(m->nfreq);
@@ -313,8 +319,8 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     G2P_TRY(dalloc(&d_fr, m->nfreq, s));
     G2P_TRY(dalloc(&d_out, 2LL * m->nfreq * P * P, s));
     G2P_CUDA(cudaMemcpyAsync(d_fr, fr.data(), sizeof(double) * m->nfreq, cudaMemcpyHostToDevice, s));
-    (g2p::launch_tick(), k_z_layout<<<grid_for((int64_t)m->nfreq * P * P), kThreads, 0, s>>>(P, m->nfreq, d_fr, m->freq_start * m->freq_unit,
-                                                                        zre, zim, d_out));
+    (g2p::kbegin("k_z_layout", s), k_z_layout<<<grid_for((int64_t)m->nfreq * P * P), kThreads, 0, s>>>(P, m->nfreq, d_fr, m->freq_start * m->freq_unit,
+                                                                        zre, zim, d_out), g2p::kend(s));
     G2P_CUDA(cudaMemcpyAsync(z_out, d_out, sizeof(double) * 2 * m->nfreq * P * P, cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
     local.solve_ms = ms_since(t0);
@@ -322,7 +328,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     dfree(Bd, s); dfree(Yd, s); dfree(Bc, s); dfree(Yc, s); dfree(crhs, s);
     dfree(yd1, s); dfree(yc, s); dfree(yd2, s); dfree(zre, s); dfree(zim, s);
     dfree(d_pe_edge, s); dfree(d_pe_port, s); dfree(d_pe_J, s); dfree(d_redge, s); dfree(d_rdir, s);
-    dfree(d_rptr, s); dfree(d_cur, s); dfree(d_long_d, s);
+    dfree(d_rptr, s); dfree(d_cur, s); lcol.release(s);
     g2p_solver_destroy(Sd);
     g2p_solver_destroy(Sc);
     G2P_CUDA(cudaStreamSynchronize(s));

@@ -12,8 +12,11 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstring>
+#include <algorithm>
+#include <map>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "internal.h"
 #include "primitives.cuh"
@@ -42,6 +45,65 @@ const char *last_error() { return g_err.c_str(); }
 static std::atomic<int64_t> g_launches{0};
 void launch_tick() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+struct NamedProfile {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;
+    size_t used = 0;
+    std::vector<const char *> names;
+    std::map<std::string, std::pair<int64_t, double>> totals;   // name -> (launches, ms)
+};
+static NamedProfile g_np;
+
+static void np_record(cudaStream_t s) {
+    if (g_np.used == g_np.ev.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        g_np.ev.push_back(e);
+    }
+    cudaEventRecord(g_np.ev[g_np.used++], s);
+}
+void kbegin(const char *name, cudaStream_t s) {
+    launch_tick();
+    if (!g_np.on) return;
+    g_np.names.push_back(name);
+    np_record(s);
+}
+void kend(cudaStream_t s) {
+    if (g_np.on) np_record(s);
+}
+bool kprof_on() { return g_np.on; }
+void kprof_set(bool on) {
+    if (on) { g_np.used = 0; g_np.names.clear(); g_np.totals.clear(); }
+    g_np.on = on;
+}
+g2p_status kprof_collect() {
+    G2P_CUDA(cudaDeviceSynchronize());
+    for (size_t i = 0; i < g_np.names.size() && 2 * i + 1 < g_np.used; i++) {
+        float t = 0;
+        G2P_CUDA(cudaEventElapsedTime(&t, g_np.ev[2 * i], g_np.ev[2 * i + 1]));
+        auto &tot = g_np.totals[g_np.names[i]];
+        tot.first += 1;
+        tot.second += t;
+    }
+    g_np.used = 0;
+    g_np.names.clear();
+    return G2P_OK;
+}
+
+// Keeps freed stream-ordered allocations in the device pool instead of
+// returning them to the driver at every synchronization (the default
+// threshold of 0 makes each large allocation re-map its pages).
+void retain_pool_memory(int device) {
+    static std::once_flag once;
+    std::call_once(once, [device]() {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+    });
+}
 
 g2p_status ensure_scan_work(g2p_mesh *m, int64_t n) {
     int64_t need = scan_work_size(n) + 16;
@@ -81,6 +143,25 @@ extern "C" const char *g2p_last_error(void) { return g2p::last_error(); }
 extern "C" const char *g2p_version(void) { return "gds2para_gb300 0.1 (sm_103a)"; }
 extern "C" int64_t g2p_launch_count(void) { return g2p::launch_count(); }
 
+// One line per kernel, "name<TAB>launches<TAB>total_ms", by decreasing time.
+extern "C" int64_t g2p_profile_report(char *buf, int64_t cap) {
+    std::vector<std::pair<double, std::string>> rows;
+    for (auto &kv : g2p::g_np.totals) {
+        char line[256];
+        snprintf(line, sizeof line, "%s\t%lld\t%.6f\n", kv.first.c_str(), (long long)kv.second.first, kv.second.second);
+        rows.push_back({kv.second.second, line});
+    }
+    std::sort(rows.begin(), rows.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+    std::string out;
+    for (auto &r : rows) out += r.second;
+    if (buf && cap > 0) {
+        int64_t n = std::min<int64_t>(cap - 1, (int64_t)out.size());
+        memcpy(buf, out.data(), (size_t)n);
+        buf[n] = 0;
+    }
+    return (int64_t)out.size();
+}
+
 extern "C" g2p_status g2p_mesh_create(const g2p_mesh_desc *in, g2p_mesh **out) {
     if (!in || !out) { set_last_message("null argument"); return G2P_ERR_INVALID; }
     *out = nullptr;
@@ -99,6 +180,7 @@ extern "C" g2p_status g2p_mesh_create(const g2p_mesh_desc *in, g2p_mesh **out) {
         delete m; set_last_message("grid exceeds 2^31 edges"); return G2P_ERR_UNSUPPORTED;
     }
     cudaGetDevice(&m->device);
+    retain_pool_memory(m->device);
     cudaError_t e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { set_last_error(e, "cudaStreamCreate", __FILE__, __LINE__); delete m; return G2P_ERR_CUDA; }
     m->k.mu = G2P_MU;
@@ -152,22 +234,22 @@ extern "C" g2p_status g2p_mesh_create(const g2p_mesh_desc *in, g2p_mesh **out) {
     CP(m->mark_port, in->mark_port, sizeof(int32_t) * in->num_cdt);
     CP(m->cdt_return, in->cdt_return, in->num_cdt);
     CP(tmp, in->mark_node, sizeof(int64_t) * d.N_node);
-    (g2p::launch_tick(), k_narrow<<<grid_for(d.N_node), kThreads, 0, s>>>(tmp, m->mark_node, d.N_node));
+    (g2p::kbegin("k_narrow", s), k_narrow<<<grid_for(d.N_node), kThreads, 0, s>>>(tmp, m->mark_node, d.N_node), g2p::kend(s));
     CP(tmp, in->mark_edge, sizeof(int64_t) * d.N_edge);
-    (g2p::launch_tick(), k_narrow<<<grid_for(d.N_edge), kThreads, 0, s>>>(tmp, m->mark_edge, d.N_edge));
+    (g2p::kbegin("k_narrow", s), k_narrow<<<grid_for(d.N_edge), kThreads, 0, s>>>(tmp, m->mark_edge, d.N_edge), g2p::kend(s));
     int *flag = nullptr;
     CK(dalloc(&flag, 1, s));
     cudaMemsetAsync(flag, 0, sizeof(int), s);
-    (g2p::launch_tick(), k_check_marks<<<grid_for(d.N_node), kThreads, 0, s>>>(m->mark_node, d.N_node, in->num_cdt, flag));
-    (g2p::launch_tick(), k_check_marks<<<grid_for(d.N_edge), kThreads, 0, s>>>(m->mark_edge, d.N_edge, in->num_cdt, flag));
+    (g2p::kbegin("k_check_marks", s), k_check_marks<<<grid_for(d.N_node), kThreads, 0, s>>>(m->mark_node, d.N_node, in->num_cdt, flag), g2p::kend(s));
+    (g2p::kbegin("k_check_marks", s), k_check_marks<<<grid_for(d.N_edge), kThreads, 0, s>>>(m->mark_edge, d.N_edge, in->num_cdt, flag), g2p::kend(s));
     int hflag = 0;
     cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
     dfree(flag, s);
     if (hflag) { dfree(tmp, s); g2p_mesh_destroy(m); set_last_message("mark_node/mark_edge hold ids outside [0, num_cdt]"); return G2P_ERR_INVALID; }
-    (g2p::launch_tick(), k_dual_lengths<<<1, 256, 0, s>>>(m->xn, d.Nx, m->dxa));
-    (g2p::launch_tick(), k_dual_lengths<<<1, 256, 0, s>>>(m->yn, d.Ny, m->dya));
-    (g2p::launch_tick(), k_dual_lengths<<<1, 256, 0, s>>>(m->zn, d.Nz, m->dza));
+    (g2p::kbegin("k_dual_lengths", s), k_dual_lengths<<<1, 256, 0, s>>>(m->xn, d.Nx, m->dxa), g2p::kend(s));
+    (g2p::kbegin("k_dual_lengths", s), k_dual_lengths<<<1, 256, 0, s>>>(m->yn, d.Ny, m->dya), g2p::kend(s));
+    (g2p::kbegin("k_dual_lengths", s), k_dual_lengths<<<1, 256, 0, s>>>(m->zn, d.Nz, m->dza), g2p::kend(s));
     dfree(tmp, s);
 #undef CP
 #undef CK
@@ -249,12 +331,12 @@ g2p_status g2p_run_index_maps(g2p_mesh *m) {
     G2P_TRY(dalloc(&m->pec_node, d.N_node, s));
     G2P_TRY(dalloc(&m->map_edge, d.N_edge, s));
     G2P_TRY(ensure_scan_work(m, d.N_edge));
-    (g2p::launch_tick(), k_pec_flags<<<grid_for(d.N_edge), kThreads, 0, s>>>(d, m->mark_edge, m->mark_node, m->cdt_return, m->pec_edge,
-                                                         m->pec_node));
+    (g2p::kbegin("k_pec_flags", s), k_pec_flags<<<grid_for(d.N_edge), kThreads, 0, s>>>(d, m->mark_edge, m->mark_node, m->cdt_return, m->pec_edge,
+                                                         m->pec_node), g2p::kend(s));
     const uint8_t *pe = m->pec_edge;
     auto op = [pe] __device__(int64_t i) -> int64_t { return pe[i]; };
     G2P_TRY(exclusive_scan(op, d.N_edge, m->map_edge, m->scan_work, s));
-    (g2p::launch_tick(), k_finish_map<<<grid_for(d.N_edge), kThreads, 0, s>>>(d.N_edge, m->pec_edge, m->map_edge));
+    (g2p::kbegin("k_finish_map", s), k_finish_map<<<grid_for(d.N_edge), kThreads, 0, s>>>(d.N_edge, m->pec_edge, m->map_edge), g2p::kend(s));
     G2P_CUDA(cudaMemcpyAsync(&m->bden, m->scan_work + scan_total_index(d.N_edge), sizeof(int64_t),
                              cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
@@ -274,7 +356,7 @@ extern "C" g2p_status g2p_index_maps(g2p_mesh *m, int64_t *bden, int64_t *map_ed
     if (map_edge) {
         int64_t *tmp;
         G2P_TRY(dalloc(&tmp, m->d.N_edge, m->stream));
-        (g2p::launch_tick(), k_widen_map<<<grid_for(m->d.N_edge), kThreads, 0, m->stream>>>(m->map_edge, tmp, m->d.N_edge));
+        (g2p::kbegin("k_widen_map", m->stream), k_widen_map<<<grid_for(m->d.N_edge), kThreads, 0, m->stream>>>(m->map_edge, tmp, m->d.N_edge), g2p::kend(m->stream));
         G2P_CUDA(cudaMemcpyAsync(map_edge, tmp, sizeof(int64_t) * m->d.N_edge, cudaMemcpyDeviceToHost, m->stream));
         dfree(tmp, m->stream);
         G2P_CUDA(cudaStreamSynchronize(m->stream));
@@ -481,7 +563,7 @@ g2p_status g2p_run_stiff(g2p_mesh *m) {
     int64_t n = d.N_edge - m->bden;
     int64_t *rowlen;
     G2P_TRY(dalloc(&rowlen, n, s));
-    (g2p::launch_tick(), k_stiff_count<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, rowlen));
+    (g2p::kbegin("k_stiff_count", s), k_stiff_count<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, rowlen), g2p::kend(s));
     int64_t nnz = 0;
     g2p_status st = g2p_build_rowptr(m, rowlen, n, &m->S.ptr, &nnz);
     dfree(rowlen, s);
@@ -490,8 +572,8 @@ g2p_status g2p_run_stiff(g2p_mesh *m) {
     m->S.nnz = nnz;
     G2P_TRY(dalloc(&m->S.col, nnz, s));
     G2P_TRY(dalloc(&m->S.val, nnz, s));
-    (g2p::launch_tick(), k_stiff_fill<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, m->S.ptr, m->S.col,
-                                                                     m->S.val, m->k.mu));
+    (g2p::kbegin("k_stiff_fill", s), k_stiff_fill<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, m->S.ptr, m->S.col,
+                                                                     m->S.val, m->k.mu), g2p::kend(s));
     G2P_CUDA(cudaGetLastError());
     G2P_CUDA(cudaStreamSynchronize(s));
     m->stiff_done = true;
@@ -511,12 +593,12 @@ g2p_status g2p_export_csr(g2p_mesh *m, const Csr<double> &A, int64_t *row, int64
     int64_t *tmp;
     G2P_TRY(dalloc(&tmp, A.nnz, s));
     if (row) {
-        (g2p::launch_tick(), k_csr_rows_i64<<<grid_for(A.n), kThreads, 0, s>>>(A.ptr, A.n, tmp));
+        (g2p::kbegin("k_csr_rows_i64", s), k_csr_rows_i64<<<grid_for(A.n), kThreads, 0, s>>>(A.ptr, A.n, tmp), g2p::kend(s));
         G2P_CUDA(cudaMemcpyAsync(row, tmp, sizeof(int64_t) * A.nnz, cudaMemcpyDeviceToHost, s));
         G2P_CUDA(cudaStreamSynchronize(s));
     }
     if (col) {
-        (g2p::launch_tick(), k_i32_to_i64<<<grid_for(A.nnz), kThreads, 0, s>>>(A.col, tmp, A.nnz));
+        (g2p::kbegin("k_i32_to_i64", s), k_i32_to_i64<<<grid_for(A.nnz), kThreads, 0, s>>>(A.col, tmp, A.nnz), g2p::kend(s));
         G2P_CUDA(cudaMemcpyAsync(col, tmp, sizeof(int64_t) * A.nnz, cudaMemcpyDeviceToHost, s));
         G2P_CUDA(cudaStreamSynchronize(s));
     }

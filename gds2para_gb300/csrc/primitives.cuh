@@ -30,6 +30,28 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+// Per-row kernels over k interleaved right-hand sides use blocks of shape
+// (kx, 256 / kx): threadIdx.x is the right-hand side (kx the power of two
+// >= k), threadIdx.y the row -- no integer division in the index math.
+inline int pow2_ge(int k) {
+    int p = 1;
+    while (p < k) p <<= 1;
+    return p;
+}
+inline dim3 row_block(int k) {
+    int kx = pow2_ge(k);
+    return dim3(kx, 256 / kx);
+}
+inline unsigned row_grid(int64_t n, int k, int64_t cap = 152LL * 32) {
+    int64_t ny = 256 / pow2_ge(k);
+    int64_t b = (n + ny - 1) / ny;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (unsigned)b;
+}
+#define G2P_FOR_ROWS(i, n) \
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.y + threadIdx.y; i < (n); i += (int64_t)gridDim.x * blockDim.y)
+
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
@@ -98,9 +120,9 @@ template <class F, class OutT>
 g2p_status exclusive_scan(F op, int64_t n, OutT *out, int64_t *work, cudaStream_t s) {
     int64_t nb = (n + kScanTile - 1) / kScanTile;
     if (nb == 0) nb = 1;
-    (g2p::launch_tick(), k_scan_reduce<F><<<(unsigned)nb, kScanThreads, 0, s>>>(op, n, work));
-    (g2p::launch_tick(), k_scan_partials<<<1, 1024, 0, s>>>(work, nb));
-    (g2p::launch_tick(), k_scan_down<F, OutT><<<(unsigned)nb, kScanThreads, 0, s>>>(op, n, work, out));
+    (g2p::kbegin("k_scan_reduce", s), k_scan_reduce<F><<<(unsigned)nb, kScanThreads, 0, s>>>(op, n, work), g2p::kend(s));
+    (g2p::kbegin("k_scan_partials", s), k_scan_partials<<<1, 1024, 0, s>>>(work, nb), g2p::kend(s));
+    (g2p::kbegin("k_scan_down", s), k_scan_down<F, OutT><<<(unsigned)nb, kScanThreads, 0, s>>>(op, n, work, out), g2p::kend(s));
     G2P_CUDA(cudaGetLastError());
     return G2P_OK;
 }
@@ -189,11 +211,11 @@ g2p_status radix_sort_pairs(K *k0, V *v0, K *k1, V *v1, int64_t n, int bits, int
     V *vs = v0, *vd = v1;
     bool in1 = false;
     for (int shift = 0; shift < bits; shift += 8) {
-        (g2p::launch_tick(), k_sort_hist<K><<<(unsigned)nb, kSortThreads, 0, s>>>(ks, n, shift, nb, counts));
+        (g2p::kbegin("k_sort_hist", s), k_sort_hist<K><<<(unsigned)nb, kSortThreads, 0, s>>>(ks, n, shift, nb, counts), g2p::kend(s));
         const int64_t *c = counts;
         auto op = [c] __device__(int64_t i) { return c[i]; };
         G2P_TRY(exclusive_scan(op, 256 * nb, counts + 256 * nb, work, s));
-        (g2p::launch_tick(), k_sort_scatter<K, V><<<(unsigned)nb, kSortThreads, 0, s>>>(ks, vs, n, shift, nb, counts + 256 * nb, kd, vd));
+        (g2p::kbegin("k_sort_scatter", s), k_sort_scatter<K, V><<<(unsigned)nb, kSortThreads, 0, s>>>(ks, vs, n, shift, nb, counts + 256 * nb, kd, vd), g2p::kend(s));
         G2P_CUDA(cudaGetLastError());
         K *tk = ks; ks = kd; kd = tk;
         V *tv = vs; vs = vd; vd = tv;

@@ -10,6 +10,8 @@
 //     near-null space the aggregates must represent unchanged).
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -20,9 +22,16 @@ namespace g2p {
 
 __global__ void k_max_abs_diag(const int64_t *ptr, const int32_t *col, const double *val, int64_t n,
                                unsigned long long *mx) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++)
-            if (col[q] == i) { atomicMax(mx, (unsigned long long)__double_as_longlong(fabs(val[q]))); break; }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t lo = ptr[i], hi = ptr[i + 1] - 1, q = -1;
+        while (lo <= hi) {
+            int64_t mid = (lo + hi) >> 1;
+            if (col[mid] == i) { q = mid; break; }
+            if (col[mid] < i) lo = mid + 1; else hi = mid - 1;
+        }
+        if (q < 0) for (int64_t t = ptr[i]; t < ptr[i + 1]; t++) if (col[t] == i) { q = t; break; }
+        if (q >= 0) atomicMax(mx, (unsigned long long)__double_as_longlong(fabs(val[q])));
+    }
 }
 
 __global__ void k_scale_vals(const double *val, int64_t nnz, double c, double *out) {
@@ -56,16 +65,14 @@ __global__ void k_coo_cols(const int64_t *cols, int64_t nnz, int64_t n, int32_t 
 }
 
 __global__ void k_colmajor_to_interleaved(const double *in, double *out, int64_t n, int k) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t i = t / k;
-        out[t] = in[(t - i * k) * n + i];
-    }
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    G2P_FOR_ROWS(i, n) out[i * k + r] = in[(int64_t)r * n + i];
 }
 __global__ void k_interleaved_to_colmajor(const double *in, double *out, int64_t n, int k) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * k; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t i = t / k;
-        out[(t - i * k) * n + i] = in[t];
-    }
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    G2P_FOR_ROWS(i, n) out[(int64_t)r * n + i] = in[i * k + r];
 }
 
 static double ms_since(std::chrono::steady_clock::time_point t0) {
@@ -89,7 +96,7 @@ extern "C" void g2p_default_params(g2p_solver_params *p, int32_t parity_mode) {
     p->coarse_size = 256;
     p->strength = 0.08;
     p->max_levels = 20;
-    p->inner_rtol = 1e-4;
+    p->inner_rtol = 1e-3;
     p->inner_maxit = 40;
     p->batch = 1;
     p->use_graphs = 0;
@@ -105,6 +112,8 @@ static SolverConfig cfg_from(const g2p_solver_params *p) {
     c.coarse_size = p->coarse_size > 0 ? p->coarse_size : 256;
     c.strength = p->strength > 0 ? p->strength : 0.08;
     c.max_levels = p->max_levels > 0 ? p->max_levels : 20;
+    c.reorth = false;   // classical Gram-Schmidt once: same iteration counts, half the passes
+    if (const char *e = getenv("G2P_REORTH")) c.reorth = atoi(e) != 0;
     return c;
 }
 
@@ -116,7 +125,7 @@ g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cu
     S->stream = stream;
     S->cfg = cfg_from(p);
     S->precision = p->precision;
-    S->inner_rtol = p->inner_rtol > 0 ? p->inner_rtol : 1e-4;
+    S->inner_rtol = p->inner_rtol > 0 ? p->inner_rtol : 1e-3;
     S->inner_maxit = p->inner_maxit > 0 ? p->inner_maxit : 40;
     cudaStream_t s = stream;
     auto fail = [&](g2p_status st) { g2p_solver_destroy(S); return st; };
@@ -128,12 +137,12 @@ g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cu
     cudaMemcpyAsync(S->A.ptr, A.ptr, sizeof(int64_t) * (A.n + 1), cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(S->A.col, A.col, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(S->A.val, A.val, sizeof(double) * A.nnz, cudaMemcpyDeviceToDevice, s);
-    if ((st = find_long_rows(S->A, &S->long_rows, &S->nlong, s)) != G2P_OK) return fail(st);
+    if ((st = find_long_rows<double>(S->A, S->lr, s)) != G2P_OK) return fail(st);
     if (S->precision == G2P_PREC_MIXED) {
         unsigned long long *mx;
         if ((st = dalloc(&mx, 1, s)) != G2P_OK) return fail(st);
         cudaMemsetAsync(mx, 0, sizeof(unsigned long long), s);
-        (g2p::launch_tick(), k_max_abs_diag<<<grid_for(A.n), kThreads, 0, s>>>(S->A.ptr, S->A.col, S->A.val, A.n, mx));
+        (g2p::kbegin("k_max_abs_diag", s), k_max_abs_diag<<<grid_for(A.n), kThreads, 0, s>>>(S->A.ptr, S->A.col, S->A.val, A.n, mx), g2p::kend(s));
         unsigned long long hb = 0;
         cudaMemcpyAsync(&hb, mx, sizeof(hb), cudaMemcpyDeviceToHost, s);
         cudaStreamSynchronize(s);
@@ -144,7 +153,7 @@ g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cu
         Csr<double> As = S->A;   // shares structure; scaled values in a temporary
         double *sv;
         if ((st = dalloc(&sv, A.nnz, s)) != G2P_OK) return fail(st);
-        (g2p::launch_tick(), k_scale_vals<<<grid_for(A.nnz), kThreads, 0, s>>>(S->A.val, A.nnz, S->cscale, sv));
+        (g2p::kbegin("k_scale_vals", s), k_scale_vals<<<grid_for(A.nnz), kThreads, 0, s>>>(S->A.val, A.nnz, S->cscale, sv), g2p::kend(s));
         As.val = sv;
         st = amg_setup(As, S->cfg, s, nullptr, S->H64);
         dfree(sv, s);
@@ -191,6 +200,8 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
     if (S->precision != G2P_PREC_MIXED) {
         G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep));
         iters = rep.iterations;
+        if (getenv("G2P_DEBUG"))
+            fprintf(stderr, "[g2p] n=%lld k=%d fp64: its %d rel %.3e\n", (long long)n, k, rep.iterations, rep.rel_residual);
     } else {
         // FP64 refinement around FP32 inner solves
         G2P_TRY(krylov_alloc<double>(S->K64, n, k, 1, s));
@@ -201,11 +212,11 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
         SolverConfig inner = S->cfg;
         inner.rtol = S->inner_rtol;
         inner.maxit = S->inner_maxit;
-        inner.reorth = false;
+        if (const char *e = getenv("G2P_INNER_REORTH")) inner.reorth = atoi(e) != 0;
         const int max_ref = S->cfg.maxit > 0 ? std::max(2, S->cfg.maxit / std::max(1, S->inner_maxit / 2)) : 20;
         rep.converged = false;
         for (int ref = 0; ref <= max_ref; ref++) {
-            residual64(S->A, S->long_rows, S->nlong, b, x, S->rb, k, s);
+            residual64(S->A, S->lr, b, x, S->rb, k, s);
             colnorms<double>(S->rb, n, k, S->K64.partial, rn, s);
             G2P_CUDA(cudaMemcpyAsync(hr.data(), rn, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
             G2P_CUDA(cudaStreamSynchronize(s));
@@ -214,11 +225,14 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
             rep.rel_residual = worst;
             if (worst <= S->cfg.rtol) { rep.converged = true; break; }
             if (ref == max_ref) break;
-            (g2p::launch_tick(), k_to_f<<<grid_for(nk), kThreads, 0, s>>>(nk, S->rb, S->rf));
+            (g2p::kbegin("k_to_f", s), k_to_f<<<grid_for(nk), kThreads, 0, s>>>(nk, S->rb, S->rf), g2p::kend(s));
             G2P_CUDA(cudaMemsetAsync(S->df, 0, sizeof(float) * nk, s));
             SolveReport ir;
             G2P_TRY(fgmres<float>(S->H32.lv[0].A, S->H32, S->K32, S->rf, S->df, k, inner, nullptr, s, ir));
-            (g2p::launch_tick(), k_add_scaled<<<grid_for(nk), kThreads, 0, s>>>(nk, S->cscale, S->df, x));
+            if (getenv("G2P_DEBUG"))
+                fprintf(stderr, "[g2p] n=%lld k=%d refinement %d: outer rel %.3e, inner its %d inner rel %.3e\n",
+                        (long long)n, k, ref, worst, ir.iterations, ir.rel_residual);
+            (g2p::kbegin("k_add_scaled", s), k_add_scaled<<<grid_for(nk), kThreads, 0, s>>>(nk, S->cscale, S->df, x), g2p::kend(s));
             iters += ir.iterations;
             refinements++;
         }
@@ -243,6 +257,9 @@ extern "C" g2p_status g2p_solver_create(const int64_t *ARowId, const int64_t *AC
     if (n >= INT32_MAX) { set_last_message("matrix too large"); return G2P_ERR_UNSUPPORTED; }
     g2p_solver_params def;
     if (!p) { g2p_default_params(&def, 0); p = &def; }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    retain_pool_memory(dev);
     cudaStream_t s;
     G2P_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     // row-sorted COO (hypreSolve's input) -> CSR on the device
@@ -259,8 +276,8 @@ extern "C" g2p_status g2p_solver_create(const int64_t *ARowId, const int64_t *AC
     G2P_CUDA(cudaMemcpyAsync(A.val, Aval, sizeof(double) * leng_A, cudaMemcpyHostToDevice, s));
     G2P_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (n + 1), s));
     G2P_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), s));
-    (g2p::launch_tick(), k_coo_count<<<grid_for(leng_A), kThreads, 0, s>>>(rows, leng_A, n, cnt, bad));
-    (g2p::launch_tick(), k_coo_cols<<<grid_for(leng_A), kThreads, 0, s>>>(cols, leng_A, n, A.col, bad));
+    (g2p::kbegin("k_coo_count", s), k_coo_count<<<grid_for(leng_A), kThreads, 0, s>>>(rows, leng_A, n, cnt, bad), g2p::kend(s));
+    (g2p::kbegin("k_coo_cols", s), k_coo_cols<<<grid_for(leng_A), kThreads, 0, s>>>(cols, leng_A, n, A.col, bad), g2p::kend(s));
     const int64_t *cp = cnt;
     auto op = [cp, n] __device__(int64_t i) -> int64_t { return i < n ? cp[i] : 0; };
     G2P_TRY(exclusive_scan(op, n + 1, A.ptr, work, s));
@@ -290,9 +307,9 @@ extern "C" g2p_status g2p_solver_solve(g2p_solver *S, const double *b, double *x
     G2P_TRY(dalloc(&db, n * nrhs, s)); G2P_TRY(dalloc(&dx, n * nrhs, s)); G2P_TRY(dalloc(&tb, n * nrhs, s));
     // host column-major <-> device interleaved
     G2P_CUDA(cudaMemcpyAsync(tb, b, sizeof(double) * n * nrhs, cudaMemcpyHostToDevice, s));
-    (g2p::launch_tick(), k_colmajor_to_interleaved<<<grid_for(n * nrhs), kThreads, 0, s>>>(tb, db, n, nrhs));
+    (g2p::kbegin("k_colmajor_to_interleaved", s), k_colmajor_to_interleaved<<<row_grid(n, nrhs), row_block(nrhs), 0, s>>>(tb, db, n, nrhs), g2p::kend(s));
     g2p_status rc = g2p_solver_solve_dev(S, db, dx, nrhs, st);
-    (g2p::launch_tick(), k_interleaved_to_colmajor<<<grid_for(n * nrhs), kThreads, 0, s>>>(dx, tb, n, nrhs));
+    (g2p::kbegin("k_interleaved_to_colmajor", s), k_interleaved_to_colmajor<<<row_grid(n, nrhs), row_block(nrhs), 0, s>>>(dx, tb, n, nrhs), g2p::kend(s));
     G2P_CUDA(cudaMemcpyAsync(x, tb, sizeof(double) * n * nrhs, cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
     dfree(db, s); dfree(dx, s); dfree(tb, s);
@@ -304,7 +321,7 @@ extern "C" g2p_status g2p_solver_destroy(g2p_solver *S) {
     if (!S) return G2P_OK;
     cudaStream_t s = S->stream;
     S->A.release(s);
-    dfree(S->long_rows, s); dfree(S->scale, s);
+    S->lr.release(s); dfree(S->scale, s);
     S->H64.release(s); S->H32.release(s);
     S->K64.release(s); S->K32.release(s);
     dfree(S->xb, s); dfree(S->bb, s); dfree(S->rb, s); dfree(S->rf, s); dfree(S->df, s);

@@ -23,6 +23,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "primitives.cuh"
 #include "solver.h"
@@ -30,46 +31,68 @@
 namespace g2p {
 
 // ------------------------------------------------------------ sparse kernels
+
+// y = A x (or b - A x) for rows up to kLongRow entries.  Block shape
+// (kx, 256/kx): threadIdx.x is the right-hand side, threadIdx.y the row.
 template <class T>
 __global__ void __launch_bounds__(256) k_spmm(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
                                               const T *__restrict__ val, const T *__restrict__ x, T *__restrict__ y,
                                               int k, const T *__restrict__ b) {
-    int64_t total = n * k;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t i = t / k;
-        int r = (int)(t - i * k);
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    G2P_FOR_ROWS(i, n) {
         int64_t s0 = ptr[i], s1 = ptr[i + 1];
         if (s1 - s0 > kLongRow) continue;
         T acc = 0;
-        for (int64_t q = s0; q < s1; q++) acc += val[q] * x[(int64_t)col[q] * k + r];
+        int64_t q = s0;
+        // four independent gathers in flight per step
+        for (; q + 4 <= s1; q += 4) {
+            int32_t c0 = col[q], c1 = col[q + 1], c2 = col[q + 2], c3 = col[q + 3];
+            T v0 = val[q], v1 = val[q + 1], v2 = val[q + 2], v3 = val[q + 3];
+            T x0 = x[(int64_t)c0 * k + r], x1 = x[(int64_t)c1 * k + r];
+            T x2 = x[(int64_t)c2 * k + r], x3 = x[(int64_t)c3 * k + r];
+            acc += v0 * x0 + v1 * x1 + v2 * x2 + v3 * x3;
+        }
+        for (; q < s1; q++) acc += val[q] * x[(int64_t)col[q] * k + r];
+        int64_t t = i * k + r;
         y[t] = b ? b[t] - acc : acc;
     }
 }
 
-// One block per long row; deterministic tree reduction per right-hand side.
+// Long rows, stage 1: one block per chunk of kLongChunk entries; partial
+// sums for every right-hand side.
 template <class T>
-__global__ void __launch_bounds__(256) k_spmm_long(const int32_t *__restrict__ rows, const int64_t *__restrict__ ptr,
+__global__ void __launch_bounds__(256) k_spmm_long(const int32_t *__restrict__ rows, const int32_t *__restrict__ crow,
+                                                   const int64_t *__restrict__ cbeg, const int64_t *__restrict__ ptr,
                                                    const int32_t *__restrict__ col, const T *__restrict__ val,
-                                                   const T *__restrict__ x, T *__restrict__ y, int k,
-                                                   const T *__restrict__ b) {
-    __shared__ double red[256];
-    int64_t i = rows[blockIdx.x];
-    int64_t s0 = ptr[i], s1 = ptr[i + 1];
-    for (int r = 0; r < k; r++) {
-        double acc = 0;
-        for (int64_t q = s0 + threadIdx.x; q < s1; q += blockDim.x) acc += (double)val[q] * (double)x[(int64_t)col[q] * k + r];
-        red[threadIdx.x] = acc;
-        __syncthreads();
-        for (int o = 128; o > 0; o >>= 1) {
-            if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) {
-            T v = (T)red[0];
-            y[i * k + r] = b ? b[i * k + r] - v : v;
-        }
-        __syncthreads();
+                                                   const T *__restrict__ x, int k, double *__restrict__ partial) {
+    __shared__ double sm[256];
+    const int r = threadIdx.x, ty = threadIdx.y, ny = blockDim.y;
+    int64_t row = rows[crow[blockIdx.x]];
+    int64_t q0 = cbeg[blockIdx.x], q1 = min(q0 + (int64_t)kLongChunk, ptr[row + 1]);
+    T acc = 0;
+    if (r < k)
+        for (int64_t q = q0 + ty; q < q1; q += ny) acc += val[q] * x[(int64_t)col[q] * k + r];
+    sm[ty * blockDim.x + r] = (double)acc;
+    __syncthreads();
+    if (ty == 0 && r < k) {
+        double s = 0;
+        for (int t = 0; t < ny; t++) s += sm[t * blockDim.x + r];
+        partial[(int64_t)blockIdx.x * kMaxRhs + r] = s;
     }
+}
+
+// Long rows, stage 2: ordered sum of each row's chunk partials.
+template <class T>
+__global__ void k_spmm_long_finish(int64_t nl, const int32_t *rows, const int64_t *rcp, const double *partial, int k,
+                                   T *y, const T *b) {
+    int64_t l = blockIdx.x;
+    int r = threadIdx.x;
+    if (l >= nl || r >= k) return;
+    double s = 0;
+    for (int64_t c = rcp[l]; c < rcp[l + 1]; c++) s += partial[c * kMaxRhs + r];
+    int64_t o = (int64_t)rows[l] * k + r;
+    y[o] = b ? (T)((double)b[o] - s) : (T)s;
 }
 
 // Event timing of the sparse matrix-multi-vector kernel (the dominant
@@ -94,8 +117,7 @@ static void prof_event(cudaStream_t s) {
 }
 
 template <class T>
-void spmm_b(const Csr<T> &A, const int32_t *long_rows, int64_t nlong, const T *x, T *y, int k, const T *b,
-            cudaStream_t s) {
+void spmm_b(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, const T *b, cudaStream_t s) {
     bool prof = g_prof.on && g_prof.used + 2 <= (size_t)1 << 20;
     if (prof) {
         prof_event(s);
@@ -103,21 +125,25 @@ void spmm_b(const Csr<T> &A, const int32_t *long_rows, int64_t nlong, const T *x
                         (double)A.n * k * sizeof(T) * (b ? 3 : 2);
         g_prof.launches++;
     }
-    (g2p::launch_tick(), k_spmm<T><<<grid_for(A.n * k, 256, 152LL * 48), 256, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y, k, b));
+    dim3 blk = row_block(k);
+    (g2p::kbegin("k_spmm", s), k_spmm<T><<<row_grid(A.n, k, 152LL * 48), blk, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y, k, b), g2p::kend(s));
     if (prof) prof_event(s);
-    if (nlong > 0) (g2p::launch_tick(), k_spmm_long<T><<<(unsigned)nlong, 256, 0, s>>>(long_rows, A.ptr, A.col, A.val, x, y, k, b));
+    if (lr.n > 0) {
+        (g2p::kbegin("k_spmm_long", s), k_spmm_long<T><<<(unsigned)lr.nchunk, blk, 0, s>>>(lr.rows, lr.crow, lr.cbeg, A.ptr, A.col, A.val, x, k, lr.partial), g2p::kend(s));
+        (g2p::kbegin("k_spmm_long_finish", s), k_spmm_long_finish<T><<<(unsigned)lr.n, pow2_ge(k), 0, s>>>(lr.n, lr.rows, lr.rcp, lr.partial, k, y, b), g2p::kend(s));
+    }
 }
 
 template <class T>
-void spmm(const Csr<T> &A, const int32_t *long_rows, int64_t nlong, const T *x, T *y, int k, cudaStream_t s) {
-    spmm_b<T>(A, long_rows, nlong, x, y, k, nullptr, s);
+void spmm(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, cudaStream_t s) {
+    spmm_b<T>(A, lr, x, y, k, nullptr, s);
 }
-template void spmm<double>(const Csr<double> &, const int32_t *, int64_t, const double *, double *, int, cudaStream_t);
-template void spmm<float>(const Csr<float> &, const int32_t *, int64_t, const float *, float *, int, cudaStream_t);
+template void spmm<double>(const Csr<double> &, const LongRows &, const double *, double *, int, cudaStream_t);
+template void spmm<float>(const Csr<float> &, const LongRows &, const float *, float *, int, cudaStream_t);
 
-void residual64(const Csr<double> &A, const int32_t *long_rows, int64_t nlong, const double *b, const double *x,
-                double *r, int k, cudaStream_t s) {
-    spmm_b<double>(A, long_rows, nlong, x, r, k, b, s);
+void residual64(const Csr<double> &A, const LongRows &lr, const double *b, const double *x, double *r, int k,
+                cudaStream_t s) {
+    spmm_b<double>(A, lr, x, r, k, b, s);
 }
 
 __global__ void k_mark_long(int64_t n, const int64_t *ptr, int64_t *flag) {
@@ -130,7 +156,8 @@ __global__ void k_list_long(int64_t n, const int64_t *ptr, const int64_t *pos, i
 }
 
 template <class T>
-g2p_status find_long_rows_t(const Csr<T> &A, int32_t **rows, int64_t *nlong, cudaStream_t s) {
+g2p_status find_long_rows(const Csr<T> &A, LongRows &lr, cudaStream_t s) {
+    lr.release(s);
     int64_t *pos, *work;
     int64_t n = A.n;
     G2P_TRY(dalloc(&pos, n + 1, s));
@@ -138,19 +165,57 @@ g2p_status find_long_rows_t(const Csr<T> &A, int32_t **rows, int64_t *nlong, cud
     const int64_t *p = A.ptr;
     auto op = [p, n] __device__(int64_t i) -> int64_t { return i < n ? ((p[i + 1] - p[i]) > kLongRow ? 1 : 0) : 0; };
     G2P_TRY(exclusive_scan(op, n + 1, pos, work, s));
-    G2P_CUDA(cudaMemcpyAsync(nlong, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    int64_t nl = 0;
+    G2P_CUDA(cudaMemcpyAsync(&nl, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
-    *rows = nullptr;
-    if (*nlong > 0) {
-        G2P_TRY(dalloc(rows, *nlong, s));
-        (g2p::launch_tick(), k_list_long<<<grid_for(n), kThreads, 0, s>>>(n, A.ptr, pos, *rows));
+    if (nl > 0) {
+        G2P_TRY(dalloc(&lr.rows, nl, s));
+        (g2p::kbegin("k_list_long", s), k_list_long<<<grid_for(n), kThreads, 0, s>>>(n, A.ptr, pos, lr.rows), g2p::kend(s));
+        // chunk table on the host from the (few) long rows' extents
+        std::vector<int32_t> rows(nl);
+        G2P_CUDA(cudaMemcpyAsync(rows.data(), lr.rows, sizeof(int32_t) * nl, cudaMemcpyDeviceToHost, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
+        std::vector<int64_t> beg(nl), end(nl);
+        for (int64_t l = 0; l < nl; l++) {
+            G2P_CUDA(cudaMemcpyAsync(&beg[l], A.ptr + rows[l], sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+            G2P_CUDA(cudaMemcpyAsync(&end[l], A.ptr + rows[l] + 1, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        }
+        G2P_CUDA(cudaStreamSynchronize(s));
+        std::vector<int32_t> crow;
+        std::vector<int64_t> cbeg, rcp(nl + 1, 0);
+        for (int64_t l = 0; l < nl; l++) {
+            for (int64_t q = beg[l]; q < end[l]; q += kLongChunk) { crow.push_back((int32_t)l); cbeg.push_back(q); }
+            rcp[l + 1] = (int64_t)crow.size();
+        }
+        lr.n = nl;
+        lr.nchunk = (int64_t)crow.size();
+        G2P_TRY(dalloc(&lr.crow, lr.nchunk, s));
+        G2P_TRY(dalloc(&lr.cbeg, lr.nchunk, s));
+        G2P_TRY(dalloc(&lr.rcp, nl + 1, s));
+        G2P_TRY(dalloc(&lr.partial, lr.nchunk * kMaxRhs, s));
+        G2P_CUDA(cudaMemcpyAsync(lr.crow, crow.data(), sizeof(int32_t) * lr.nchunk, cudaMemcpyHostToDevice, s));
+        G2P_CUDA(cudaMemcpyAsync(lr.cbeg, cbeg.data(), sizeof(int64_t) * lr.nchunk, cudaMemcpyHostToDevice, s));
+        G2P_CUDA(cudaMemcpyAsync(lr.rcp, rcp.data(), sizeof(int64_t) * (nl + 1), cudaMemcpyHostToDevice, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
     }
     dfree(pos, s); dfree(work, s);
     return G2P_OK;
 }
+template g2p_status find_long_rows<double>(const Csr<double> &, LongRows &, cudaStream_t);
+template g2p_status find_long_rows<float>(const Csr<float> &, LongRows &, cudaStream_t);
 
-g2p_status find_long_rows(const Csr<double> &A, int32_t **rows, int64_t *nlong, cudaStream_t s) {
-    return find_long_rows_t<double>(A, rows, nlong, s);
+g2p_status copy_long_rows(const LongRows &src, LongRows &dst, cudaStream_t s) {
+    dst.release(s);
+    if (src.n == 0) return G2P_OK;
+    dst.n = src.n; dst.nchunk = src.nchunk;
+    G2P_TRY(dalloc(&dst.rows, src.n, s)); G2P_TRY(dalloc(&dst.crow, src.nchunk, s));
+    G2P_TRY(dalloc(&dst.cbeg, src.nchunk, s)); G2P_TRY(dalloc(&dst.rcp, src.n + 1, s));
+    G2P_TRY(dalloc(&dst.partial, src.nchunk * kMaxRhs, s));
+    G2P_CUDA(cudaMemcpyAsync(dst.rows, src.rows, sizeof(int32_t) * src.n, cudaMemcpyDeviceToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(dst.crow, src.crow, sizeof(int32_t) * src.nchunk, cudaMemcpyDeviceToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(dst.cbeg, src.cbeg, sizeof(int64_t) * src.nchunk, cudaMemcpyDeviceToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(dst.rcp, src.rcp, sizeof(int64_t) * (src.n + 1), cudaMemcpyDeviceToDevice, s));
+    return G2P_OK;
 }
 
 // --------------------------------------------------------------- reductions
@@ -162,23 +227,18 @@ constexpr int64_t kMaxDenseCoarse = 768;
 // Block shape (kx, 256 / kx) with kx the power of two >= k: threadIdx.x is
 // the right-hand side, threadIdx.y strides over rows, so every thread keeps
 // one column's partial sum and the block reduces in a fixed order.
-static inline int pow2_at_least(int k) {
-    int p = 1;
-    while (p < k) p <<= 1;
-    return p;
-}
 
 template <class T>
 __global__ void __launch_bounds__(256) k_colsq_partial(const T *x, int64_t n, int k, double *partial) {
     __shared__ double sm[256];
     const int r = threadIdx.x, ty = threadIdx.y, ny = blockDim.y;
-    double acc = 0;
+    T acc = 0;
     if (r < k)
         for (int64_t i = blockIdx.x * (int64_t)ny + ty; i < n; i += (int64_t)gridDim.x * ny) {
-            double v = (double)x[i * k + r];
+            T v = x[i * k + r];
             acc += v * v;
         }
-    sm[ty * blockDim.x + r] = acc;
+    sm[ty * blockDim.x + r] = (double)acc;
     __syncthreads();
     if (ty == 0 && r < k) {
         double s = 0;
@@ -197,32 +257,44 @@ __global__ void k_reduce_partials(const double *partial, int nb, int cnt, double
 
 template <class T>
 void colnorms(const T *x, int64_t n, int k, double *partial, double *out, cudaStream_t s) {
-    int kx = pow2_at_least(k);
+    int kx = pow2_ge(k);
     dim3 blk(kx, 256 / kx);
-    (g2p::launch_tick(), k_colsq_partial<T><<<kRedBlocks, blk, 0, s>>>(x, n, k, partial));
-    (g2p::launch_tick(), k_reduce_partials<<<(k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, k, out, true));
+    (g2p::kbegin("k_colsq_partial", s), k_colsq_partial<T><<<kRedBlocks, blk, 0, s>>>(x, n, k, partial), g2p::kend(s));
+    (g2p::kbegin("k_reduce_partials", s), k_reduce_partials<<<(k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, k, out, true), g2p::kend(s));
 }
 template void colnorms<double>(const double *, int64_t, int, double *, double *, cudaStream_t);
 template void colnorms<float>(const float *, int64_t, int, double *, double *, cudaStream_t);
 
-// dots[j*k + r] = <V_j[:, r], w[:, r]> for j < J.
+// dots[j*k + r] = <V_j[:, r], w[:, r]> for j < J, eight basis vectors per pass
+// over w; block partials are reduced in a fixed order.
+constexpr int kDotGroup = 8;
 template <class T>
 __global__ void __launch_bounds__(256) k_mdot_partial(const T *V, int64_t n, int J, const T *w, int k, double *partial) {
-    __shared__ double sm[256];
+    __shared__ double sm[kDotGroup][256];
     const int r = threadIdx.x, ty = threadIdx.y, ny = blockDim.y;
     const int64_t nk = n * k;
-    for (int j = 0; j < J; j++) {
-        const T *Vj = V + (int64_t)j * nk;
-        double acc = 0;
+    for (int j0 = 0; j0 < J; j0 += kDotGroup) {
+        T acc[kDotGroup];
+#pragma unroll
+        for (int g = 0; g < kDotGroup; g++) acc[g] = 0;
         if (r < k)
-            for (int64_t i = blockIdx.x * (int64_t)ny + ty; i < n; i += (int64_t)gridDim.x * ny)
-                acc += (double)Vj[i * k + r] * (double)w[i * k + r];
-        sm[ty * blockDim.x + r] = acc;
+            for (int64_t i = blockIdx.x * (int64_t)ny + ty; i < n; i += (int64_t)gridDim.x * ny) {
+                int64_t t = i * k + r;
+                T wv = w[t];
+#pragma unroll
+                for (int g = 0; g < kDotGroup; g++)
+                    if (j0 + g < J) acc[g] += V[(int64_t)(j0 + g) * nk + t] * wv;
+            }
+#pragma unroll
+        for (int g = 0; g < kDotGroup; g++) sm[g][ty * blockDim.x + r] = (double)acc[g];
         __syncthreads();
-        if (ty == 0 && r < k) {
-            double s = 0;
-            for (int q = 0; q < ny; q++) s += sm[q * blockDim.x + r];
-            partial[((int64_t)j * k + r) * gridDim.x + blockIdx.x] = s;
+        for (int idx = ty * blockDim.x + r; idx < kDotGroup * (int)blockDim.x; idx += blockDim.x * blockDim.y) {
+            int g = idx / blockDim.x, rr = idx % blockDim.x;
+            if (rr < k && j0 + g < J) {
+                double sacc = 0;
+                for (int t2 = 0; t2 < ny; t2++) sacc += sm[g][t2 * blockDim.x + rr];
+                partial[((int64_t)(j0 + g) * k + rr) * gridDim.x + blockIdx.x] = sacc;
+            }
         }
         __syncthreads();
     }
@@ -230,21 +302,29 @@ __global__ void __launch_bounds__(256) k_mdot_partial(const T *V, int64_t n, int
 
 // w -= sum_j h[j*k + r] V_j ; also h_acc += h (for reorthogonalisation)
 template <class T>
-__global__ void __launch_bounds__(256) k_maxpy(const T *V, int64_t nk, int J, const double *h, int k, T *w) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
-        int r = (int)(t % k);
-        double acc = (double)w[t];
-        for (int j = 0; j < J; j++) acc -= h[j * k + r] * (double)V[(int64_t)j * nk + t];
-        w[t] = (T)acc;
+__global__ void __launch_bounds__(256) k_maxpy(const T *V, int64_t n, int J, const double *h, int k, T *w) {
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    const int64_t nk = n * k;
+    T hr[64];
+    for (int j = 0; j < J; j++) hr[j] = (T)h[j * k + r];
+    G2P_FOR_ROWS(i, n) {
+        int64_t t = i * k + r;
+        T acc = w[t];
+        for (int j = 0; j < J; j++) acc -= hr[j] * V[(int64_t)j * nk + t];
+        w[t] = acc;
     }
 }
 
 // ---------------------------------------------------------------- smoothing
 template <class T>
-__global__ void k_cheb_first(int64_t nk, int k, const T *dinv, const T *b, T *x, T *d, double inv_theta, bool add) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
+__global__ void k_cheb_first(int64_t n, int k, const T *dinv, const T *b, T *x, T *d, double inv_theta, bool add) {
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    G2P_FOR_ROWS(i, n) {
         // add == false: x0 = 0 so the residual is b; add == true: b holds b - A x
-        T dd = (T)(inv_theta * (double)dinv[t / k] * (double)b[t]);
+        int64_t t = i * k + r;
+        T dd = (T)inv_theta * dinv[i] * b[t];
         d[t] = dd;
         x[t] = add ? x[t] + dd : dd;
     }
@@ -252,11 +332,15 @@ __global__ void k_cheb_first(int64_t nk, int k, const T *dinv, const T *b, T *x,
 
 // d = c1 d + c2 D^-1 (b - A x) with t = b - A x precomputed; x += d
 template <class T>
-__global__ void k_cheb_step(int64_t nk, int k, const T *dinv, const T *res, T *x, T *d, double c1, double c2) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
-        double dd = c1 * (double)d[t] + c2 * (double)dinv[t / k] * (double)res[t];
-        d[t] = (T)dd;
-        x[t] = (T)((double)x[t] + dd);
+__global__ void k_cheb_step(int64_t n, int k, const T *dinv, const T *res, T *x, T *d, double c1, double c2) {
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    const T a = (T)c1, b = (T)c2;
+    G2P_FOR_ROWS(i, n) {
+        int64_t t = i * k + r;
+        T dd = a * d[t] + b * dinv[i] * res[t];
+        d[t] = dd;
+        x[t] = x[t] + dd;
     }
 }
 
@@ -265,18 +349,18 @@ static void chebyshev(Level<T> &L, int deg, double ratio, const T *b, T *x, bool
     double lmax = L.lmax * 1.05, lmin = L.lmax * ratio;
     double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
     double sigma = theta / delta, rho = 1.0 / sigma;
-    int64_t nk = L.n * k;
-    unsigned g = grid_for(nk);
+    unsigned g = row_grid(L.n, k);
+    dim3 blk = row_block(k);
     if (zero_guess) {
-        (g2p::launch_tick(), k_cheb_first<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, b, x, L.d, 1.0 / theta, false));
+        (g2p::kbegin("k_cheb_first", s), k_cheb_first<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, b, x, L.d, 1.0 / theta, false), g2p::kend(s));
     } else {
-        spmm_b<T>(L.A, L.long_rows, L.nlong, x, L.t0, k, b, s);
-        (g2p::launch_tick(), k_cheb_first<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, L.t0, x, L.d, 1.0 / theta, true));
+        spmm_b<T>(L.A, L.lr, x, L.t0, k, b, s);
+        (g2p::kbegin("k_cheb_first", s), k_cheb_first<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, L.t0, x, L.d, 1.0 / theta, true), g2p::kend(s));
     }
     for (int it = 1; it < deg; it++) {
-        spmm_b<T>(L.A, L.long_rows, L.nlong, x, L.t0, k, b, s);
+        spmm_b<T>(L.A, L.lr, x, L.t0, k, b, s);
         double rn = 1.0 / (2.0 * sigma - rho);
-        (g2p::launch_tick(), k_cheb_step<T><<<g, kThreads, 0, s>>>(nk, k, L.dinv, L.t0, x, L.d, rn * rho, 2.0 * rn / delta));
+        (g2p::kbegin("k_cheb_step", s), k_cheb_step<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, L.t0, x, L.d, rn * rho, 2.0 * rn / delta), g2p::kend(s));
         rho = rn;
     }
 }
@@ -284,47 +368,36 @@ static void chebyshev(Level<T> &L, int deg, double ratio, const T *b, T *x, bool
 // b_c[I] = sum over members i of I of (b_i - (A x)_i)  (t0 holds b - A x)
 template <class T>
 __global__ void k_restrict(int64_t nc, int k, const int64_t *rptr, const int32_t *rmem, const T *res, T *bc) {
-    int64_t total = nc * k;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t I = t / k;
-        int r = (int)(t - I * k);
-        double acc = 0;
-        for (int64_t q = rptr[I]; q < rptr[I + 1]; q++) acc += (double)res[(int64_t)rmem[q] * k + r];
-        bc[t] = (T)acc;
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    G2P_FOR_ROWS(I, nc) {
+        T acc = 0;
+        for (int64_t q = rptr[I]; q < rptr[I + 1]; q++) acc += res[(int64_t)rmem[q] * k + r];
+        bc[I * k + r] = acc;
     }
 }
 
-template <class T>
-__global__ void k_prolong(int64_t n, int k, const int32_t *agg, const T *xc, T *x) {
-    int64_t total = n * k;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t i = t / k;
-        int a = agg[i];
-        if (a >= 0) x[t] = (T)((double)x[t] + (double)xc[(int64_t)a * k + (t - i * k)]);
-    }
-}
 
 template <class T>
 __global__ void k_dense_apply(int64_t n, int k, const double *Ainv, const T *b, T *x) {
-    int64_t total = n * k;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t i = t / k;
-        int r = (int)(t - i * k);
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    G2P_FOR_ROWS(i, n) {
         double acc = 0;
         for (int64_t j = 0; j < n; j++) acc += Ainv[i * n + j] * (double)b[j * k + r];
-        x[t] = (T)acc;
+        x[i * k + r] = (T)acc;
     }
 }
 
 template <class T>
 __global__ void k_prolong_csr(int64_t n, int k, const int64_t *ptr, const int32_t *col, const T *val, const T *xc, T *x) {
-    int64_t total = n * k;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t i = t / k;
-        int r = (int)(t - i * k);
-        double acc = (double)x[t];
-        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) acc += (double)val[q] * (double)xc[(int64_t)col[q] * k + r];
-        x[t] = (T)acc;
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    G2P_FOR_ROWS(i, n) {
+        int64_t t = i * k + r;
+        T acc = x[t];
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) acc += val[q] * xc[(int64_t)col[q] * k + r];
+        x[t] = acc;
     }
 }
 
@@ -332,7 +405,7 @@ template <class T>
 static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaStream_t s) {
     Level<T> &L = H.lv[l];
     if (l == (int)H.lv.size() - 1) {
-        if (H.cinv) (g2p::launch_tick(), k_dense_apply<T><<<grid_for(L.n * k), kThreads, 0, s>>>(L.n, k, H.cinv, L.b, L.x));
+        if (H.cinv) (g2p::kbegin("k_dense_apply", s), k_dense_apply<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, H.cinv, L.b, L.x), g2p::kend(s));
         else {
             chebyshev<T>(L, 4, cfg.cheb_ratio, L.b, L.x, true, k, s);
             for (int q = 0; q < 4; q++) chebyshev<T>(L, 4, cfg.cheb_ratio, L.b, L.x, false, k, s);
@@ -340,34 +413,77 @@ static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaS
         return;
     }
     chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, L.b, L.x, true, k, s);
-    spmm_b<T>(L.A, L.long_rows, L.nlong, L.x, L.t0, k, L.b, s);
+    spmm_b<T>(L.A, L.lr, L.x, L.t0, k, L.b, s);
     Level<T> &C = H.lv[l + 1];
-    (g2p::launch_tick(), k_restrict<T><<<grid_for(C.n * k), kThreads, 0, s>>>(C.n, k, L.rptr, L.rmem, L.t0, C.b));
+    (g2p::kbegin("k_restrict", s), k_restrict<T><<<row_grid(C.n, k), row_block(k), 0, s>>>(C.n, k, L.rptr, L.rmem, L.t0, C.b), g2p::kend(s));
     vcycle<T>(H, cfg, l + 1, k, s);
-    (g2p::launch_tick(), k_prolong_csr<T><<<grid_for(L.n * k), kThreads, 0, s>>>(L.n, k, L.P.ptr, L.P.col, L.P.val, C.x, L.x));
+    (g2p::kbegin("k_prolong_csr", s), k_prolong_csr<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, L.P.ptr, L.P.col, L.P.val, C.x, L.x), g2p::kend(s));
     chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, L.b, L.x, false, k, s);
 }
 
 // ------------------------------------------------------------- AMG setup
+// Position of the diagonal in row i (columns ascending; linear fallback).
+__device__ __forceinline__ int64_t diag_pos(const int64_t *ptr, const int32_t *col, int64_t i) {
+    int64_t lo = ptr[i], hi = ptr[i + 1] - 1;
+    while (lo <= hi) {
+        int64_t mid = (lo + hi) >> 1;
+        int32_t c = col[mid];
+        if (c == i) return mid;
+        if (c < i) lo = mid + 1; else hi = mid - 1;
+    }
+    for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) if (col[q] == i) return q;
+    return -1;
+}
+
 __global__ void k_diag(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, double *diag) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double d = 0;
-        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) if (col[q] == i) { d = val[q]; break; }
-        diag[i] = d;
+        int64_t q = diag_pos(ptr, col, i);
+        diag[i] = q >= 0 ? val[q] : 0.0;
     }
 }
 
+// 1/a_ii and the Gershgorin radius max_i sum_j |a_ij| / |a_ii| of D^-1 A;
+// rows longer than kLongRow are summed by k_gersh_long.
 __global__ void k_dinv_gersh(int64_t n, const int64_t *ptr, const double *val, const double *diag, double *dinv,
                              unsigned long long *lmax_bits) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double d = diag[i];
         if (d == 0.0) d = 1.0;
         dinv[i] = 1.0 / d;
+        if (ptr[i + 1] - ptr[i] > kLongRow) continue;
         double s = 0;
         for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) s += fabs(val[q]);
-        double ratio = s / fabs(d);
-        atomicMax(lmax_bits, (unsigned long long)__double_as_longlong(ratio));
+        atomicMax(lmax_bits, (unsigned long long)__double_as_longlong(s / fabs(d)));
     }
+}
+
+__global__ void __launch_bounds__(256) k_gersh_long(const int32_t *rows, const int64_t *ptr, const double *val,
+                                                    const double *diag, unsigned long long *lmax_bits) {
+    __shared__ double sm[256];
+    int64_t i = rows[blockIdx.x];
+    double s = 0;
+    for (int64_t q = ptr[i] + threadIdx.x; q < ptr[i + 1]; q += blockDim.x) s += fabs(val[q]);
+    sm[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double d = diag[i];
+        if (d == 0.0) d = 1.0;
+        atomicMax(lmax_bits, (unsigned long long)__double_as_longlong(sm[0] / fabs(d)));
+    }
+}
+
+// row containing entry q (ptr ascending)
+__device__ __forceinline__ int64_t row_of(const int64_t *ptr, int64_t n, int64_t q) {
+    int64_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int64_t mid = (lo + hi + 1) >> 1;
+        if (ptr[mid] <= q) lo = mid; else hi = mid - 1;
+    }
+    return lo;
 }
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
@@ -628,49 +744,40 @@ __global__ void k_ta_count(int64_t n, const int64_t *ptr, const int32_t *agg, in
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         cnt[i] = agg[i] >= 0 ? ptr[i + 1] - ptr[i] : 0;
 }
-__global__ void k_ta_expand(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const int32_t *agg,
-                            const int64_t *off, uint64_t ncols, uint64_t *keys, double *vals) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+__global__ void k_ta_expand(int64_t n, int64_t nnz, const int64_t *ptr, const int32_t *col, const double *val,
+                            const int32_t *agg, const int64_t *off, uint64_t ncols, uint64_t *keys, double *vals) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = row_of(ptr, n, q);
         int32_t a = agg[i];
         if (a < 0) continue;
-        int64_t o = off[i];
-        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++, o++) {
-            keys[o] = (uint64_t)a * ncols + (uint64_t)col[q];
-            vals[o] = val[q];
-        }
+        int64_t o = off[i] + (q - ptr[i]);
+        keys[o] = (uint64_t)a * ncols + (uint64_t)col[q];
+        vals[o] = val[q];
     }
 }
 // (T^T A) P: key I * nc + J
-__global__ void k_bp_count(int64_t nr, const int64_t *bptr, const int32_t *bcol, const int64_t *pptr, int64_t *cnt) {
-    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nr; I += (int64_t)gridDim.x * blockDim.x) {
-        int64_t c = 0;
-        for (int64_t q = bptr[I]; q < bptr[I + 1]; q++) c += pptr[bcol[q] + 1] - pptr[bcol[q]];
-        cnt[I] = c;
-    }
-}
-__global__ void k_bp_expand(int64_t nr, const int64_t *bptr, const int32_t *bcol, const double *bval, const int64_t *pptr,
-                            const int32_t *pcol, const double *pval, const int64_t *off, uint64_t nc, uint64_t *keys,
-                            double *vals) {
-    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nr; I += (int64_t)gridDim.x * blockDim.x) {
-        int64_t o = off[I];
-        for (int64_t q = bptr[I]; q < bptr[I + 1]; q++) {
-            int64_t j = bcol[q];
-            double b = bval[q];
-            for (int64_t t = pptr[j]; t < pptr[j + 1]; t++, o++) {
-                keys[o] = (uint64_t)I * nc + (uint64_t)pcol[t];
-                vals[o] = b * pval[t];
-            }
+// (T^T A) P, one thread per entry of B = T^T A; off[q] = output offset
+__global__ void k_bp_expand(int64_t nr, int64_t nnzb, const int64_t *bptr, const int32_t *bcol, const double *bval,
+                            const int64_t *pptr, const int32_t *pcol, const double *pval, const int64_t *off,
+                            uint64_t nc, uint64_t *keys, double *vals) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnzb; q += (int64_t)gridDim.x * blockDim.x) {
+        int64_t I = row_of(bptr, nr, q);
+        int64_t j = bcol[q];
+        double b = bval[q];
+        int64_t o = off[q];
+        for (int64_t t = pptr[j]; t < pptr[j + 1]; t++, o++) {
+            keys[o] = (uint64_t)I * nc + (uint64_t)pcol[t];
+            vals[o] = b * pval[t];
         }
     }
 }
-
 
 template <class T>
 void Hierarchy<T>::release(cudaStream_t s) {
     for (auto &L : lv) {
         L.A.release(s);
         L.P.release(s);
-        dfree(L.long_rows, s); dfree(L.dinv, s); dfree(L.agg, s); dfree(L.rptr, s); dfree(L.rmem, s);
+        L.lr.release(s); dfree(L.dinv, s); dfree(L.agg, s); dfree(L.rptr, s); dfree(L.rmem, s);
         dfree(L.x, s); dfree(L.b, s); dfree(L.t0, s); dfree(L.t1, s); dfree(L.d, s);
     }
     lv.clear();
@@ -706,7 +813,7 @@ static g2p_status esc_to_csr(uint64_t *&k0, double *&v0, int64_t ne, int64_t nro
     int64_t *head, *segid;
     G2P_TRY(dalloc(&head, ne + 1, s));
     G2P_TRY(dalloc(&segid, ne + 1, s));
-    (g2p::launch_tick(), k_heads64<<<grid_for(ne), kThreads, 0, s>>>(sk, ne, head));
+    (g2p::kbegin("k_heads64", s), k_heads64<<<grid_for(ne), kThreads, 0, s>>>(sk, ne, head), g2p::kend(s));
     const int64_t *hp = head;
     auto hop = [hp, ne] __device__(int64_t i) -> int64_t { return i < ne ? hp[i] : 0; };
     G2P_TRY(exclusive_scan(hop, ne + 1, segid, work, s));
@@ -718,7 +825,7 @@ static g2p_status esc_to_csr(uint64_t *&k0, double *&v0, int64_t ne, int64_t nro
     G2P_TRY(dalloc(&rowcnt, nrows + 1, s));
     G2P_CUDA(cudaMemsetAsync(rowcnt, 0, sizeof(int64_t) * (nrows + 1), s));
     G2P_TRY(dalloc(&out.col, nseg, s)); G2P_TRY(dalloc(&out.val, nseg, s)); G2P_TRY(dalloc(&out.ptr, nrows + 1, s));
-    (g2p::launch_tick(), k_seg_reduce<<<grid_for(ne), kThreads, 0, s>>>(sk, sv, ne, segid, (uint64_t)ncols, rowcnt, out.col, out.val));
+    (g2p::kbegin("k_seg_reduce", s), k_seg_reduce<<<grid_for(ne), kThreads, 0, s>>>(sk, sv, ne, segid, (uint64_t)ncols, rowcnt, out.col, out.val), g2p::kend(s));
     const int64_t *rc = rowcnt;
     auto rcop = [rc, nrows] __device__(int64_t i) -> int64_t { return i < nrows ? rc[i] : 0; };
     G2P_TRY(exclusive_scan(rcop, nrows + 1, out.ptr, work, s));
@@ -769,12 +876,14 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
         double *diag;
         G2P_TRY(dalloc(&diag, n, s));
         G2P_TRY(dalloc(&L.dinv, n, s));
-        (g2p::launch_tick(), k_diag<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag));
+        (g2p::kbegin("k_diag", s), k_diag<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag), g2p::kend(s));
         G2P_CUDA(cudaMemsetAsync(d_lmax, 0, sizeof(unsigned long long), s));
-        (g2p::launch_tick(), k_dinv_gersh<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.val, diag, L.dinv, d_lmax));
+        G2P_TRY(find_long_rows<double>(L.A, L.lr, s));   // synchronizes
+        (g2p::kbegin("k_dinv_gersh", s), k_dinv_gersh<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.val, diag, L.dinv, d_lmax), g2p::kend(s));
+        if (L.lr.n > 0) (g2p::kbegin("k_gersh_long", s), k_gersh_long<<<(unsigned)L.lr.n, 256, 0, s>>>(L.lr.rows, L.A.ptr, L.A.val, diag, d_lmax), g2p::kend(s));
         unsigned long long lb = 0;
         G2P_CUDA(cudaMemcpyAsync(&lb, d_lmax, sizeof(lb), cudaMemcpyDeviceToHost, s));
-        G2P_TRY(find_long_rows_t<double>(L.A, &L.long_rows, &L.nlong, s));   // synchronizes
+        G2P_CUDA(cudaStreamSynchronize(s));
         double lm;
         memcpy(&lm, &lb, sizeof(lm));
         L.lmax = lm > 0 ? lm : 2.0;
@@ -786,13 +895,13 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             uint64_t *T, *M1, *M2;
             G2P_TRY(dalloc(&dense, n, s)); G2P_TRY(dalloc(&T, n, s)); G2P_TRY(dalloc(&M1, n, s)); G2P_TRY(dalloc(&M2, n, s));
             unsigned g = grid_for(n);
-            (g2p::launch_tick(), k_agg_init<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, lim, cfg.strength, dense, T));
-            (g2p::launch_tick(), k_agg_state<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T));
+            (g2p::kbegin("k_agg_init", s), k_agg_init<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, lim, cfg.strength, dense, T), g2p::kend(s));
+            (g2p::kbegin("k_agg_state", s), k_agg_state<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T), g2p::kend(s));
             for (int round = 0; round < 200; round++) {
-                (g2p::launch_tick(), k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, M1));
-                (g2p::launch_tick(), k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, M1, M2));
+                (g2p::kbegin("k_mis_max", s), k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, M1), g2p::kend(s));
+                (g2p::kbegin("k_mis_max", s), k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, M1, M2), g2p::kend(s));
                 G2P_CUDA(cudaMemsetAsync(d_int, 0, sizeof(int), s));
-                (g2p::launch_tick(), k_mis_update<<<g, kThreads, 0, s>>>(n, T, M2, d_int));
+                (g2p::kbegin("k_mis_update", s), k_mis_update<<<g, kThreads, 0, s>>>(n, T, M2, d_int), g2p::kend(s));
                 int und = 0;
                 G2P_CUDA(cudaMemcpyAsync(&und, d_int, sizeof(int), cudaMemcpyDeviceToHost, s));
                 G2P_CUDA(cudaStreamSynchronize(s));
@@ -814,8 +923,8 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             int32_t *agg1;
             G2P_TRY(dalloc(&agg1, n, s));
             G2P_TRY(dalloc(&L.agg, n, s));
-            (g2p::launch_tick(), k_agg_phase1<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, rootid, agg1));
-            (g2p::launch_tick(), k_agg_phase2<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, agg1, L.agg));
+            (g2p::kbegin("k_agg_phase1", s), k_agg_phase1<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, rootid, agg1), g2p::kend(s));
+            (g2p::kbegin("k_agg_phase2", s), k_agg_phase2<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, agg1, L.agg), g2p::kend(s));
             G2P_CUDA(cudaStreamSynchronize(s));
             dfree(agg1, s); dfree(rootid, s); dfree(dense, s); dfree(T, s); dfree(M1, s); dfree(M2, s);
             if (nc == 0 || nc > (n * 9) / 10) {
@@ -834,7 +943,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 uint32_t *k0, *k1;
                 int32_t *v0, *v1;
                 G2P_TRY(dalloc(&k0, nm, s)); G2P_TRY(dalloc(&k1, nm, s)); G2P_TRY(dalloc(&v0, nm, s)); G2P_TRY(dalloc(&v1, nm, s));
-                (g2p::launch_tick(), k_agg_key<<<g, kThreads, 0, s>>>(n, L.agg, pos, k0, v0));
+                (g2p::kbegin("k_agg_key", s), k_agg_key<<<g, kThreads, 0, s>>>(n, L.agg, pos, k0, v0), g2p::kend(s));
                 int64_t *counts;
                 G2P_TRY(dalloc(&counts, sort_counts_size(nm), s));
                 G2P_TRY(need_work(sort_counts_size(nm)));
@@ -842,7 +951,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 G2P_TRY(radix_sort_pairs(k0, v0, k1, v1, nm, key_bits((uint64_t)nc), counts, work, &in1, s));
                 dfree(counts, s);
                 G2P_TRY(dalloc(&L.rptr, nc + 1, s));
-                (g2p::launch_tick(), k_member_ptr<<<grid_for(nm + 1), kThreads, 0, s>>>(nm, in1 ? k1 : k0, nc, L.rptr));
+                (g2p::kbegin("k_member_ptr", s), k_member_ptr<<<grid_for(nm + 1), kThreads, 0, s>>>(nm, in1 ? k1 : k0, nc, L.rptr), g2p::kend(s));
                 L.rmem = in1 ? v1 : v0;
                 dfree(in1 ? v0 : v1, s);
                 dfree(k0, s); dfree(k1, s); dfree(pos, s);
@@ -851,34 +960,43 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 int64_t *pc;
                 G2P_TRY(dalloc(&pc, n + 1, s));
                 G2P_TRY(dalloc(&L.P.ptr, n + 1, s));
-                (g2p::launch_tick(), k_ps_count<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, L.agg, w, pc));
+                (g2p::kbegin("k_ps_count", s), k_ps_count<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, L.agg, w, pc), g2p::kend(s));
                 int64_t pnnz = 0;
                 G2P_TRY(offsets_of(pc, n, L.P.ptr, s, &pnnz));
                 dfree(pc, s);
                 L.P.n = n; L.P.m = nc; L.P.nnz = pnnz;
                 G2P_TRY(dalloc(&L.P.col, pnnz, s)); G2P_TRY(dalloc(&L.P.val, pnnz, s));
-                (g2p::launch_tick(), k_ps_fill<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, L.agg, w, L.P.ptr, L.P.col, L.P.val));
+                (g2p::kbegin("k_ps_fill", s), k_ps_fill<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, L.agg, w, L.P.ptr, L.P.col, L.P.val), g2p::kend(s));
                 // ---- B = T^T A (nc x n)
                 int64_t *cnt, *off;
                 G2P_TRY(dalloc(&cnt, n + 1, s)); G2P_TRY(dalloc(&off, n + 1, s));
-                (g2p::launch_tick(), k_ta_count<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.agg, cnt));
+                (g2p::kbegin("k_ta_count", s), k_ta_count<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.agg, cnt), g2p::kend(s));
                 int64_t ne = 0;
                 G2P_TRY(offsets_of(cnt, n, off, s, &ne));
                 uint64_t *ek0;
                 double *ev0;
                 G2P_TRY(dalloc(&ek0, ne, s)); G2P_TRY(dalloc(&ev0, ne, s));
-                (g2p::launch_tick(), k_ta_expand<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, L.agg, off, (uint64_t)n, ek0, ev0));
+                (g2p::kbegin("k_ta_expand", s), k_ta_expand<<<grid_for(L.A.nnz), kThreads, 0, s>>>(n, L.A.nnz, L.A.ptr, L.A.col, L.A.val, L.agg, off, (uint64_t)n, ek0, ev0), g2p::kend(s));
                 dfree(cnt, s); dfree(off, s);
                 Csr<double> B;
                 G2P_TRY(esc_to_csr(ek0, ev0, ne, nc, n, s, B));
-                // ---- A_c = B P (nc x nc)
-                G2P_TRY(dalloc(&cnt, nc + 1, s)); G2P_TRY(dalloc(&off, nc + 1, s));
-                (g2p::launch_tick(), k_bp_count<<<grid_for(nc), kThreads, 0, s>>>(nc, B.ptr, B.col, L.P.ptr, cnt));
-                G2P_TRY(offsets_of(cnt, nc, off, s, &ne));
+                // ---- A_c = B P (nc x nc), entry-parallel over B
+                G2P_TRY(dalloc(&off, B.nnz + 1, s));
+                {
+                    int64_t *wk;
+                    G2P_TRY(dalloc(&wk, scan_work_size(B.nnz + 1) + 4, s));
+                    const int32_t *bc = B.col;
+                    const int64_t *pp = L.P.ptr;
+                    int64_t nb = B.nnz;
+                    auto pop = [bc, pp, nb] __device__(int64_t q) -> int64_t { return q < nb ? pp[bc[q] + 1] - pp[bc[q]] : 0; };
+                    G2P_TRY(exclusive_scan(pop, nb + 1, off, wk, s));
+                    G2P_CUDA(cudaMemcpyAsync(&ne, off + nb, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+                    G2P_CUDA(cudaStreamSynchronize(s));
+                    dfree(wk, s);
+                }
                 G2P_TRY(dalloc(&ek0, ne, s)); G2P_TRY(dalloc(&ev0, ne, s));
-                (g2p::launch_tick(), k_bp_expand<<<grid_for(nc), kThreads, 0, s>>>(nc, B.ptr, B.col, B.val, L.P.ptr, L.P.col, L.P.val, off,
-                                                            (uint64_t)nc, ek0, ev0));
-                dfree(cnt, s); dfree(off, s);
+                (g2p::kbegin("k_bp_expand", s), k_bp_expand<<<grid_for(B.nnz), kThreads, 0, s>>>(nc, B.nnz, B.ptr, B.col, B.val, L.P.ptr, L.P.col, L.P.val, off, (uint64_t)nc, ek0, ev0), g2p::kend(s));
+                dfree(off, s);
                 B.release(s);
                 Level<double> C;
                 C.n = nc;
@@ -897,9 +1015,9 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             G2P_TRY(dalloc(&Dm, nn * nn, s));
             G2P_TRY(dalloc(&H.cinv, nn * nn, s));
             G2P_CUDA(cudaMemsetAsync(Dm, 0, sizeof(double) * nn * nn, s));
-            (g2p::launch_tick(), k_dense_fill<<<grid_for(nn), kThreads, 0, s>>>(nn, Cl.A.ptr, Cl.A.col, Cl.A.val, Dm));
+            (g2p::kbegin("k_dense_fill", s), k_dense_fill<<<grid_for(nn), kThreads, 0, s>>>(nn, Cl.A.ptr, Cl.A.col, Cl.A.val, Dm), g2p::kend(s));
             G2P_CUDA(cudaMemsetAsync(d_int, 0, sizeof(int), s));
-            (g2p::launch_tick(), k_gauss_jordan<<<1, 1024, 0, s>>>(Dm, H.cinv, nn, d_int));
+            (g2p::kbegin("k_gauss_jordan", s), k_gauss_jordan<<<1, 1024, 0, s>>>(Dm, H.cinv, nn, d_int), g2p::kend(s));
             G2P_CUDA(cudaStreamSynchronize(s));
             dfree(Dm, s);
             break;
@@ -921,25 +1039,22 @@ g2p_status amg_to_float(const Hierarchy<double> &H, cudaStream_t s, Hierarchy<fl
     for (size_t l = 0; l < H.lv.size(); l++) {
         const Level<double> &L = H.lv[l];
         Level<float> f;
-        f.n = L.n; f.nc = L.nc; f.lmax = L.lmax; f.nlong = L.nlong;
+        f.n = L.n; f.nc = L.nc; f.lmax = L.lmax;
         f.A.n = f.A.m = L.A.n; f.A.nnz = L.A.nnz;
         // structure is shared by copying (owned separately for simple release)
         G2P_TRY(dalloc(&f.A.ptr, L.A.n + 1, s)); G2P_TRY(dalloc(&f.A.col, L.A.nnz, s)); G2P_TRY(dalloc(&f.A.val, L.A.nnz, s));
         G2P_CUDA(cudaMemcpyAsync(f.A.ptr, L.A.ptr, sizeof(int64_t) * (L.A.n + 1), cudaMemcpyDeviceToDevice, s));
         G2P_CUDA(cudaMemcpyAsync(f.A.col, L.A.col, sizeof(int32_t) * L.A.nnz, cudaMemcpyDeviceToDevice, s));
-        (g2p::launch_tick(), k_d2f<<<grid_for(L.A.nnz), kThreads, 0, s>>>(L.A.val, f.A.val, L.A.nnz));
+        (g2p::kbegin("k_d2f", s), k_d2f<<<grid_for(L.A.nnz), kThreads, 0, s>>>(L.A.val, f.A.val, L.A.nnz), g2p::kend(s));
         G2P_TRY(dalloc(&f.dinv, L.n, s));
-        (g2p::launch_tick(), k_d2f<<<grid_for(L.n), kThreads, 0, s>>>(L.dinv, f.dinv, L.n));
-        if (L.nlong > 0) {
-            G2P_TRY(dalloc(&f.long_rows, L.nlong, s));
-            G2P_CUDA(cudaMemcpyAsync(f.long_rows, L.long_rows, sizeof(int32_t) * L.nlong, cudaMemcpyDeviceToDevice, s));
-        }
+        (g2p::kbegin("k_d2f", s), k_d2f<<<grid_for(L.n), kThreads, 0, s>>>(L.dinv, f.dinv, L.n), g2p::kend(s));
+        G2P_TRY(copy_long_rows(L.lr, f.lr, s));
         if (L.P.ptr) {
             f.P.n = L.P.n; f.P.m = L.P.m; f.P.nnz = L.P.nnz;
             G2P_TRY(dalloc(&f.P.ptr, L.P.n + 1, s)); G2P_TRY(dalloc(&f.P.col, L.P.nnz, s)); G2P_TRY(dalloc(&f.P.val, L.P.nnz, s));
             G2P_CUDA(cudaMemcpyAsync(f.P.ptr, L.P.ptr, sizeof(int64_t) * (L.P.n + 1), cudaMemcpyDeviceToDevice, s));
             G2P_CUDA(cudaMemcpyAsync(f.P.col, L.P.col, sizeof(int32_t) * L.P.nnz, cudaMemcpyDeviceToDevice, s));
-            (g2p::launch_tick(), k_d2f<<<grid_for(L.P.nnz), kThreads, 0, s>>>(L.P.val, f.P.val, L.P.nnz));
+            (g2p::kbegin("k_d2f", s), k_d2f<<<grid_for(L.P.nnz), kThreads, 0, s>>>(L.P.val, f.P.val, L.P.nnz), g2p::kend(s));
         }
         if (L.agg) {
             G2P_TRY(dalloc(&f.agg, L.n, s));
@@ -1015,19 +1130,27 @@ template g2p_status krylov_alloc<double>(Krylov<double> &, int64_t, int, int, cu
 template g2p_status krylov_alloc<float>(Krylov<float> &, int64_t, int, int, cudaStream_t);
 
 template <class T>
-__global__ void k_start(int64_t nk, int k, const T *r, const double *beta, T *v0) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
-        double b = beta[t % k];
-        v0[t] = b > 0 ? (T)((double)r[t] / b) : (T)0;
+__global__ void k_start(int64_t n, int k, const T *r, const double *beta, T *v0) {
+    const int rr = threadIdx.x;
+    if (rr >= k) return;
+    double b = beta[rr];
+    const T inv = b > 0 ? (T)(1.0 / b) : (T)0;
+    G2P_FOR_ROWS(i, n) {
+        int64_t t = i * k + rr;
+        v0[t] = r[t] * inv;
     }
 }
 
 // hcol = [dots (j+1 per rhs); norm]; form V_{j+1}, update H, Givens, g
 template <class T>
-__global__ void k_arnoldi_finish(int64_t nk, int k, const double *hnorm, const T *w, T *vnext) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
-        double h = hnorm[t % k];
-        vnext[t] = h > 0 ? (T)((double)w[t] / h) : (T)0;
+__global__ void k_arnoldi_finish(int64_t n, int k, const double *hnorm, const T *w, T *vnext) {
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    double h = hnorm[r];
+    const T inv = h > 0 ? (T)(1.0 / h) : (T)0;
+    G2P_FOR_ROWS(i, n) {
+        int64_t t = i * k + r;
+        vnext[t] = w[t] * inv;
     }
 }
 
@@ -1079,21 +1202,26 @@ __global__ void k_backsolve(int k, int m, int j, const double *H, const double *
 
 // x += sum_i Z_i y_i, and y is laid out [r * m + i]
 template <class T>
-__global__ void k_xupdate(int64_t nk, int k, int m, int j, const T *Z, const double *y, T *x) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nk; t += (int64_t)gridDim.x * blockDim.x) {
-        int r = (int)(t % k);
-        double acc = (double)x[t];
-        for (int i = 0; i < j; i++) acc += (double)Z[(int64_t)i * nk + t] * y[(int64_t)r * m + i];
-        x[t] = (T)acc;
+__global__ void k_xupdate(int64_t n, int k, int m, int j, const T *Z, const double *y, T *x) {
+    const int r = threadIdx.x;
+    if (r >= k) return;
+    const int64_t nk = n * k;
+    T yr[64];
+    for (int q = 0; q < j; q++) yr[q] = (T)y[(int64_t)r * m + q];
+    G2P_FOR_ROWS(i, n) {
+        int64_t t = i * k + r;
+        T acc = x[t];
+        for (int q = 0; q < j; q++) acc += Z[(int64_t)q * nk + t] * yr[q];
+        x[t] = acc;
     }
 }
 
 template <class T>
 static void mdot(const T *V, int64_t n, int J, const T *w, int k, double *partial, double *out, cudaStream_t s) {
-    int kx = pow2_at_least(k);
+    int kx = pow2_ge(k);
     dim3 blk(kx, 256 / kx);
-    (g2p::launch_tick(), k_mdot_partial<T><<<kRedBlocks, blk, 0, s>>>(V, n, J, w, k, partial));
-    (g2p::launch_tick(), k_reduce_partials<<<(J * k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, J * k, out, false));
+    (g2p::kbegin("k_mdot_partial", s), k_mdot_partial<T><<<kRedBlocks, blk, 0, s>>>(V, n, J, w, k, partial), g2p::kend(s));
+    (g2p::kbegin("k_reduce_partials", s), k_reduce_partials<<<(J * k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, J * k, out, false), g2p::kend(s));
 }
 
 __global__ void k_add_vec(double *a, const double *b, int n) {
@@ -1106,10 +1234,12 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
                   const double *bnorm_override, cudaStream_t s, SolveReport &rep) {
     const int64_t n = A.n, nk = n * k;
     const int m = cfg.restart;
+    if (k < 1 || k > kMaxRhs) { set_last_message("block of %d right-hand sides (1..%d supported)", k, kMaxRhs); return G2P_ERR_INVALID; }
     G2P_TRY(krylov_alloc<T>(K, n, k, m, s));
     G2P_TRY(hierarchy_reserve<T>(H, k, s));
     Level<T> &L0 = H.lv[0];
-    unsigned g = grid_for(nk);
+    const unsigned rg = row_grid(n, k);
+    const dim3 rb = row_block(k);
     if (bnorm_override) G2P_CUDA(cudaMemcpyAsync(K.bnorm, bnorm_override, sizeof(double) * k, cudaMemcpyDeviceToDevice, s));
     else colnorms<T>(b, n, k, K.partial, K.bnorm, s);
     int it = 0;
@@ -1117,7 +1247,7 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
     double *dots2 = K.hcol + (int64_t)k * (m + 1);
     for (;;) {
         // r = b - A x ; beta = ||r||
-        spmm_b<T>(A, L0.long_rows, L0.nlong, x, K.r, k, b, s);
+        spmm_b<T>(A, L0.lr, x, K.r, k, b, s);
         colnorms<T>(K.r, n, k, K.partial, K.beta, s);
         G2P_CUDA(cudaMemcpyAsync(K.h_est, K.beta, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
         G2P_CUDA(cudaMemcpyAsync(K.h_est + k, K.bnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
@@ -1131,8 +1261,8 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
         rep.rel_residual = worst;
         if (worst <= cfg.rtol) { rep.converged = true; break; }
         if (it >= cfg.maxit) break;
-        (g2p::launch_tick(), k_start<T><<<g, kThreads, 0, s>>>(nk, k, K.r, K.beta, K.V));
-        (g2p::launch_tick(), k_g_init<<<(k + 63) / 64, 64, 0, s>>>(k, m, K.beta, K.g));
+        (g2p::kbegin("k_start", s), k_start<T><<<rg, rb, 0, s>>>(n, k, K.r, K.beta, K.V), g2p::kend(s));
+        (g2p::kbegin("k_g_init", s), k_g_init<<<(k + 63) / 64, 64, 0, s>>>(k, m, K.beta, K.g), g2p::kend(s));
         int j = 0;
         for (; j < m && it < cfg.maxit; j++) {
             T *Vj = K.V + (int64_t)j * nk, *Zj = K.Z + (int64_t)j * nk;
@@ -1140,20 +1270,20 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
             G2P_CUDA(cudaMemcpyAsync(L0.b, Vj, sizeof(T) * nk, cudaMemcpyDeviceToDevice, s));
             vcycle<T>(H, cfg, 0, k, s);
             G2P_CUDA(cudaMemcpyAsync(Zj, L0.x, sizeof(T) * nk, cudaMemcpyDeviceToDevice, s));
-            spmm<T>(A, L0.long_rows, L0.nlong, Zj, K.w, k, s);
+            spmm<T>(A, L0.lr, Zj, K.w, k, s);
             // classical Gram-Schmidt, optionally twice
             mdot<T>(K.V, n, j + 1, K.w, k, K.partial, K.hcol, s);
-            (g2p::launch_tick(), k_maxpy<T><<<g, kThreads, 0, s>>>(K.V, nk, j + 1, K.hcol, k, K.w));
+            (g2p::kbegin("k_maxpy", s), k_maxpy<T><<<rg, rb, 0, s>>>(K.V, n, j + 1, K.hcol, k, K.w), g2p::kend(s));
             if (cfg.reorth) {
                 mdot<T>(K.V, n, j + 1, K.w, k, K.partial, dots2, s);
-                (g2p::launch_tick(), k_maxpy<T><<<g, kThreads, 0, s>>>(K.V, nk, j + 1, dots2, k, K.w));
-                (g2p::launch_tick(), k_add_vec<<<((j + 1) * k + 255) / 256, 256, 0, s>>>(K.hcol, dots2, (j + 1) * k));
+                (g2p::kbegin("k_maxpy", s), k_maxpy<T><<<rg, rb, 0, s>>>(K.V, n, j + 1, dots2, k, K.w), g2p::kend(s));
+                (g2p::kbegin("k_add_vec", s), k_add_vec<<<((j + 1) * k + 255) / 256, 256, 0, s>>>(K.hcol, dots2, (j + 1) * k), g2p::kend(s));
             }
             double *hnorm = K.beta;   // reuse
             colnorms<T>(K.w, n, k, K.partial, hnorm, s);
-            (g2p::launch_tick(), k_arnoldi_finish<T><<<g, kThreads, 0, s>>>(nk, k, hnorm, K.w, K.V + (int64_t)(j + 1) * nk));
+            (g2p::kbegin("k_arnoldi_finish", s), k_arnoldi_finish<T><<<rg, rb, 0, s>>>(n, k, hnorm, K.w, K.V + (int64_t)(j + 1) * nk), g2p::kend(s));
             double *est = K.y;        // scratch for the estimates (k values)
-            (g2p::launch_tick(), k_givens<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.hcol, hnorm, K.H, K.cs, K.sn, K.g, K.bnorm, est));
+            (g2p::kbegin("k_givens", s), k_givens<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.hcol, hnorm, K.H, K.cs, K.sn, K.g, K.bnorm, est), g2p::kend(s));
             G2P_CUDA(cudaMemcpyAsync(K.h_est, est, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
             G2P_CUDA(cudaStreamSynchronize(s));
             it++;
@@ -1161,8 +1291,8 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
             for (int r = 0; r < k; r++) worst = std::max(worst, K.h_est[r]);
             if (worst <= cfg.rtol) { j++; break; }
         }
-        (g2p::launch_tick(), k_backsolve<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.H, K.g, K.y));
-        (g2p::launch_tick(), k_xupdate<T><<<g, kThreads, 0, s>>>(nk, k, m, j, K.Z, K.y, x));
+        (g2p::kbegin("k_backsolve", s), k_backsolve<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.H, K.g, K.y), g2p::kend(s));
+        (g2p::kbegin("k_xupdate", s), k_xupdate<T><<<rg, rb, 0, s>>>(n, k, m, j, K.Z, K.y, x), g2p::kend(s));
     }
     rep.iterations = it;
     G2P_CUDA(cudaGetLastError());
@@ -1176,6 +1306,7 @@ template g2p_status fgmres<float>(const Csr<float> &, Hierarchy<float> &, Krylov
 }  // namespace g2p
 
 extern "C" void g2p_profile_begin(void) {
+    g2p::kprof_set(true);
     g2p::g_prof.on = true;
     g2p::g_prof.used = 0;
     g2p::g_prof.bytes = 0;
@@ -1185,7 +1316,8 @@ extern "C" void g2p_profile_begin(void) {
 extern "C" g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, int64_t *launches) {
     using namespace g2p;
     g_prof.on = false;
-    G2P_CUDA(cudaDeviceSynchronize());
+    kprof_set(false);
+    G2P_TRY(kprof_collect());
     double ms = 0;
     for (size_t i = 0; i + 1 < g_prof.used; i += 2) {
         float t = 0;

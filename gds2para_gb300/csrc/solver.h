@@ -5,13 +5,32 @@
 
 namespace g2p {
 
+constexpr int kLongRow = 64;
+constexpr int kLongChunk = 4096;    // entries per block in the long-row kernel
+constexpr int kMaxRhs = 256;
+
+// Rows longer than kLongRow (the lumped conductor potentials of Ad and
+// their coarse images), split into chunks of kLongChunk entries.
+struct LongRows {
+    int32_t *rows = nullptr;     // [n] row ids
+    int64_t n = 0;
+    int32_t *crow = nullptr;     // [nchunk] index into rows
+    int64_t *cbeg = nullptr;     // [nchunk] first entry
+    int64_t *rcp = nullptr;      // [n+1] chunks of each long row
+    int64_t nchunk = 0;
+    double *partial = nullptr;   // [nchunk * kMaxRhs]
+    void release(cudaStream_t s) {
+        dfree(rows, s); dfree(crow, s); dfree(cbeg, s); dfree(rcp, s); dfree(partial, s);
+        n = nchunk = 0;
+    }
+};
+
 // Multi-RHS vectors are row-interleaved: x[i * k + r].
 template <class T>
 struct Level {
     int64_t n = 0, nc = 0;
     Csr<T> A;                   // operator in working precision
-    int32_t *long_rows = nullptr;  // rows with > kLongRow entries
-    int64_t nlong = 0;
+    LongRows lr;
     T *dinv = nullptr;          // 1 / a_ii
     double lmax = 2.0;          // spectral radius estimate of D^-1 A
     int32_t *agg = nullptr;     // aggregate of each row (-1: none)
@@ -77,17 +96,17 @@ g2p_status hierarchy_reserve(Hierarchy<T> &H, int k, cudaStream_t s);
 
 // y = A x for k interleaved right-hand sides (FP64 or FP32).
 template <class T>
-void spmm(const Csr<T> &A, const int32_t *long_rows, int64_t nlong, const T *x, T *y, int k, cudaStream_t s);
+void spmm(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, cudaStream_t s);
 // r = b - A x (FP64)
-void residual64(const Csr<double> &A, const int32_t *long_rows, int64_t nlong, const double *b, const double *x,
-                double *r, int k, cudaStream_t s);
+void residual64(const Csr<double> &A, const LongRows &lr, const double *b, const double *x, double *r, int k,
+                cudaStream_t s);
 // per-column 2-norms of an n x k interleaved block into out[k] (device)
 template <class T>
 void colnorms(const T *x, int64_t n, int k, double *partial, double *out, cudaStream_t s);
 
-g2p_status find_long_rows(const Csr<double> &A, int32_t **rows, int64_t *nlong, cudaStream_t s);
-
-constexpr int kLongRow = 64;
+template <class T>
+g2p_status find_long_rows(const Csr<T> &A, LongRows &lr, cudaStream_t s);
+g2p_status copy_long_rows(const LongRows &src, LongRows &dst, cudaStream_t s);
 
 }  // namespace g2p
 
@@ -99,8 +118,7 @@ struct g2p_solver {
     int inner_maxit = 60;
     double inner_rtol = 1e-4;
     g2p::Csr<double> A;                 // original FP64 operator
-    int32_t *long_rows = nullptr;
-    int64_t nlong = 0;
+    g2p::LongRows lr;
     double *scale = nullptr;            // unused
     double cscale = 1.0;                // mixed: power-of-two scale of the FP32 operator
     g2p::Csr<double> As;                // scaled operator (mixed, FP64 for setup)

@@ -458,7 +458,7 @@ static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool 
     G2P_TRY(dalloc(&rowlen, ncol + 1, s));
     G2P_CUDA(cudaMemsetAsync(rowlen, 0, sizeof(int64_t) * (ncol + 1), s));
     if (nshort > 0)
-        (g2p::launch_tick(), k_short_rows_count<<<grid_for(nshort), kThreads, 0, s>>>(c, B.map, is_ac, B.cptr, B.cedge, B.caval, nshort, rowlen));
+        (g2p::kbegin("k_short_rows_count", s), k_short_rows_count<<<grid_for(nshort), kThreads, 0, s>>>(c, B.map, is_ac, B.cptr, B.cedge, B.caval, nshort, rowlen), g2p::kend(s));
     // long rows through sort + ordered reduce
     uint64_t *okey = nullptr;
     double *oval = nullptr;
@@ -474,7 +474,7 @@ static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool 
         G2P_TRY(dalloc(&nt, nent + 1, s));
         G2P_TRY(dalloc(&toff, nent + 1, s));
         if (nent > 0)
-            (g2p::launch_tick(), k_long_nterms<<<grid_for(nent), kThreads, 0, s>>>(c, B.map, B.cptr, B.cedge, B.caval, nshort, nlong, nt));
+            (g2p::kbegin("k_long_nterms", s), k_long_nterms<<<grid_for(nent), kThreads, 0, s>>>(c, B.map, B.cptr, B.cedge, B.caval, nshort, nlong, nt), g2p::kend(s));
         G2P_TRY(ensure_scan_work(m, nent + 1));
         const int64_t *ntp = nt;
         auto op = [ntp, nent] __device__(int64_t i) -> int64_t { return i < nent ? ntp[i] : 0; };
@@ -487,8 +487,8 @@ static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool 
         G2P_TRY(dalloc(&k0, nterm, s)); G2P_TRY(dalloc(&k1, nterm, s));
         G2P_TRY(dalloc(&v0, nterm, s)); G2P_TRY(dalloc(&v1, nterm, s));
         if (nent > 0)
-            (g2p::launch_tick(), k_long_terms<<<grid_for(nent), kThreads, 0, s>>>(c, B.map, B.cptr, B.cedge, B.caval, nshort, nlong, ncol, toff,
-                                                             k0, v0));
+            (g2p::kbegin("k_long_terms", s), k_long_terms<<<grid_for(nent), kThreads, 0, s>>>(c, B.map, B.cptr, B.cedge, B.caval, nshort, nlong, ncol, toff,
+                                                             k0, v0), g2p::kend(s));
         dfree(nt, s); dfree(toff, s);
         int64_t *counts;
         G2P_TRY(dalloc(&counts, sort_counts_size(nterm), s));
@@ -502,7 +502,7 @@ static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool 
         int64_t *head, *segid;
         G2P_TRY(dalloc(&head, nterm + 1, s));
         G2P_TRY(dalloc(&segid, nterm + 1, s));
-        (g2p::launch_tick(), k_heads<<<grid_for(nterm), kThreads, 0, s>>>(sk, nterm, head));
+        (g2p::kbegin("k_heads", s), k_heads<<<grid_for(nterm), kThreads, 0, s>>>(sk, nterm, head), g2p::kend(s));
         G2P_TRY(ensure_scan_work(m, nterm + 1));
         const int64_t *hp = head;
         auto hop = [hp, nterm] __device__(int64_t i) -> int64_t { return i < nterm ? hp[i] : 0; };
@@ -511,8 +511,8 @@ static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool 
         G2P_CUDA(cudaStreamSynchronize(s));
         G2P_TRY(dalloc(&okey, nseg, s)); G2P_TRY(dalloc(&oval, nseg, s));
         G2P_TRY(dalloc(&keep, nseg + 1, s)); G2P_TRY(dalloc(&kpos, nseg + 1, s));
-        (g2p::launch_tick(), k_seg_sum<<<grid_for(nterm), kThreads, 0, s>>>(sk, sv, nterm, segid, ncol, okey, oval, keep));
-        (g2p::launch_tick(), k_long_rowlen<<<grid_for(nseg), kThreads, 0, s>>>(okey, keep, nseg, ncol, rowlen + nshort));
+        (g2p::kbegin("k_seg_sum", s), k_seg_sum<<<grid_for(nterm), kThreads, 0, s>>>(sk, sv, nterm, segid, ncol, okey, oval, keep), g2p::kend(s));
+        (g2p::kbegin("k_long_rowlen", s), k_long_rowlen<<<grid_for(nseg), kThreads, 0, s>>>(okey, keep, nseg, ncol, rowlen + nshort), g2p::kend(s));
         const int64_t *kp = keep;
         auto kop = [kp, nseg] __device__(int64_t i) -> int64_t { return i < nseg ? kp[i] : 0; };
         G2P_TRY(ensure_scan_work(m, nseg + 1));
@@ -528,11 +528,11 @@ static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool 
     G2P_TRY(dalloc(&A.col, nnz, s));
     G2P_TRY(dalloc(&A.val, nnz, s));
     if (nshort > 0)
-        (g2p::launch_tick(), k_short_rows_fill<<<grid_for(nshort), kThreads, 0, s>>>(c, B.map, is_ac, B.cptr, B.cedge, B.caval, nshort, A.ptr,
-                                                                A.col, A.val));
+        (g2p::kbegin("k_short_rows_fill", s), k_short_rows_fill<<<grid_for(nshort), kThreads, 0, s>>>(c, B.map, is_ac, B.cptr, B.cedge, B.caval, nshort, A.ptr,
+                                                                A.col, A.val), g2p::kend(s));
     if (nlong > 0) {
-        (g2p::launch_tick(), k_long_scatter<<<grid_for(nseg), kThreads, 0, s>>>(okey, oval, keep, kpos, nseg, ncol, nshort, A.ptr, 0, A.col,
-                                                           A.val));
+        (g2p::kbegin("k_long_scatter", s), k_long_scatter<<<grid_for(nseg), kThreads, 0, s>>>(okey, oval, keep, kpos, nseg, ncol, nshort, A.ptr, 0, A.col,
+                                                           A.val), g2p::kend(s));
         dfree(okey, s); dfree(oval, s); dfree(keep, s); dfree(kpos, s);
     }
     G2P_CUDA(cudaGetLastError());
@@ -572,7 +572,7 @@ g2p_status g2p_run_v0(g2p_mesh *m) {
     int32_t *cn0, *cn1;
     G2P_TRY(dalloc(&ck0, ncn, s)); G2P_TRY(dalloc(&ck1, ncn, s));
     G2P_TRY(dalloc(&cn0, ncn, s)); G2P_TRY(dalloc(&cn1, ncn, s));
-    (g2p::launch_tick(), k_compact_cond<<<grid_for(NN), kThreads, 0, s>>>(mn, NN, pos, ck0, cn0));
+    (g2p::kbegin("k_compact_cond", s), k_compact_cond<<<grid_for(NN), kThreads, 0, s>>>(mn, NN, pos, ck0, cn0), g2p::kend(s));
     dfree(pos, s);
     int64_t *counts;
     G2P_TRY(dalloc(&counts, sort_counts_size(ncn), s));
@@ -597,8 +597,8 @@ g2p_status g2p_run_v0(g2p_mesh *m) {
     G2P_TRY(dalloc(&d1off, NN + 1, s));
     G2P_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int64_t) * (ncdt + 1), s));
     G2P_CUDA(cudaMemsetAsync(flags, 0, sizeof(int32_t) * 2, s));
-    (g2p::launch_tick(), k_d2_count<<<grid_for(NN), kThreads, 0, s>>>(c, cnt, bcnt));
-    (g2p::launch_tick(), k_cond_flags<<<grid_for(ncdt), kThreads, 0, s>>>(ncdt, cnt, m->mark_port, flags));
+    (g2p::kbegin("k_d2_count", s), k_d2_count<<<grid_for(NN), kThreads, 0, s>>>(c, cnt, bcnt), g2p::kend(s));
+    (g2p::kbegin("k_cond_flags", s), k_cond_flags<<<grid_for(ncdt), kThreads, 0, s>>>(ncdt, cnt, m->mark_port, flags), g2p::kend(s));
     int32_t hflags[2];
     G2P_CUDA(cudaMemcpyAsync(hflags, flags, sizeof(hflags), cudaMemcpyDeviceToHost, s));
     // dielectric columns and their entry offsets
@@ -632,7 +632,7 @@ g2p_status g2p_run_v0(g2p_mesh *m) {
     G2P_CUDA(cudaMemcpyAsync(&nd2, ccol + ncdt, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaMemcpyAsync(&nnz_d2, coff + ncdt, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
-    (g2p::launch_tick(), k_add_i64<<<grid_for(ncdt), kThreads, 0, s>>>(ccol, ncdt, nd1));
+    (g2p::kbegin("k_add_i64", s), k_add_i64<<<grid_for(ncdt), kThreads, 0, s>>>(ccol, ncdt, nd1), g2p::kend(s));
     V0Basis &Vd = m->v0d;
     Vd.ncol = nd1 + nd2;
     Vd.nnz = nnz_d1 + nnz_d2;
@@ -641,10 +641,10 @@ g2p_status g2p_run_v0(g2p_mesh *m) {
     G2P_TRY(dalloc(&Vd.cval, Vd.nnz, s));
     G2P_TRY(dalloc(&Vd.caval, Vd.nnz, s));
     G2P_TRY(dalloc(&Vd.map, NN, s));
-    (g2p::launch_tick(), k_d_map<<<grid_for(NN), kThreads, 0, s>>>(c, d1col, ccol, Vd.map));
-    (g2p::launch_tick(), k_d1_fill<<<grid_for(NN), kThreads, 0, s>>>(c, d1col, d1off, Vd.cptr, Vd.cedge, Vd.cval, Vd.caval));
-    (g2p::launch_tick(), k_add_i64<<<grid_for(ncdt), kThreads, 0, s>>>(coff, ncdt, nnz_d1));
-    (g2p::launch_tick(), k_cond_cptr<<<grid_for(ncdt), kThreads, 0, s>>>(ncdt, m->mark_port, cnt, ccol, coff, Vd.cptr));
+    (g2p::kbegin("k_d_map", s), k_d_map<<<grid_for(NN), kThreads, 0, s>>>(c, d1col, ccol, Vd.map), g2p::kend(s));
+    (g2p::kbegin("k_d1_fill", s), k_d1_fill<<<grid_for(NN), kThreads, 0, s>>>(c, d1col, d1off, Vd.cptr, Vd.cedge, Vd.cval, Vd.caval), g2p::kend(s));
+    (g2p::kbegin("k_add_i64", s), k_add_i64<<<grid_for(ncdt), kThreads, 0, s>>>(coff, ncdt, nnz_d1), g2p::kend(s));
+    (g2p::kbegin("k_cond_cptr", s), k_cond_cptr<<<grid_for(ncdt), kThreads, 0, s>>>(ncdt, m->mark_port, cnt, ccol, coff, Vd.cptr), g2p::kend(s));
     G2P_CUDA(cudaMemcpyAsync(Vd.cptr + Vd.ncol, &Vd.nnz, sizeof(int64_t), cudaMemcpyHostToDevice, s));
     int64_t *loff;
     G2P_TRY(dalloc(&loff, ncn + 1, s));
@@ -654,8 +654,8 @@ g2p_status g2p_run_v0(g2p_mesh *m) {
         auto bop = [lp, bp, ncn] __device__(int64_t i) -> int64_t { return i < ncn ? bp[lp[i]] : 0; };
         G2P_TRY(exclusive_scan(bop, ncn + 1, loff, m->scan_work, s));
     }
-    (g2p::launch_tick(), k_add_i64<<<grid_for(ncn), kThreads, 0, s>>>(loff, ncn, nnz_d1));
-    (g2p::launch_tick(), k_d2_fill<<<grid_for(ncn), kThreads, 0, s>>>(c, list, ncn, loff, Vd.cedge, Vd.cval, Vd.caval));
+    (g2p::kbegin("k_add_i64", s), k_add_i64<<<grid_for(ncn), kThreads, 0, s>>>(loff, ncn, nnz_d1), g2p::kend(s));
+    (g2p::kbegin("k_d2_fill", s), k_d2_fill<<<grid_for(ncn), kThreads, 0, s>>>(c, list, ncn, loff, Vd.cedge, Vd.cval, Vd.caval), g2p::kend(s));
     dfree(cnt, s); dfree(ccol, s); dfree(coff, s); dfree(bcnt, s); dfree(flags, s); dfree(d1off, s);
 
     // ---- V0c
@@ -687,7 +687,7 @@ g2p_status g2p_run_v0(g2p_mesh *m) {
     G2P_TRY(dalloc(&Vc.caval, Vc.nnz, s));
     G2P_TRY(dalloc(&Vc.map, NN, s));
     G2P_CUDA(cudaMemsetAsync(Vc.map, 0, sizeof(int32_t) * NN, s));
-    (g2p::launch_tick(), k_c_fill<<<grid_for(ncn), kThreads, 0, s>>>(c, list, ncn, ccolv, coffv, Vc.map, Vc.cptr, Vc.cedge, Vc.cval, Vc.caval));
+    (g2p::kbegin("k_c_fill", s), k_c_fill<<<grid_for(ncn), kThreads, 0, s>>>(c, list, ncn, ccolv, coffv, Vc.map, Vc.cptr, Vc.cedge, Vc.cval, Vc.caval), g2p::kend(s));
     G2P_CUDA(cudaMemcpyAsync(Vc.cptr + Vc.ncol, &Vc.nnz, sizeof(int64_t), cudaMemcpyHostToDevice, s));
     dfree(ccolv, s); dfree(coffv, s); dfree(list, s); dfree(loff, s);
 
@@ -697,7 +697,7 @@ g2p_status g2p_run_v0(g2p_mesh *m) {
         G2P_TRY(dalloc(&B.ecol, 2 * d.N_edge, s));
         G2P_TRY(dalloc(&B.eval, 2 * d.N_edge, s));
         G2P_TRY(dalloc(&B.eaval, 2 * d.N_edge, s));
-        (g2p::launch_tick(), k_edge_view<<<grid_for(d.N_edge), kThreads, 0, s>>>(c, which == 1, B.map, d1col, B.ecol, B.eval, B.eaval));
+        (g2p::kbegin("k_edge_view", s), k_edge_view<<<grid_for(d.N_edge), kThreads, 0, s>>>(c, which == 1, B.map, d1col, B.ecol, B.eval, B.eaval), g2p::kend(s));
     }
     G2P_CUDA(cudaGetLastError());
     // ---- Laplacians
@@ -735,14 +735,14 @@ extern "C" g2p_status g2p_export_v0(g2p_mesh *m, int32_t which, int64_t *row, in
     int64_t *r, *c2;
     G2P_TRY(dalloc(&r, B.nnz, s));
     G2P_TRY(dalloc(&c2, B.nnz > m->d.N_node ? B.nnz : m->d.N_node, s));
-    (g2p::launch_tick(), k_v0_export<<<grid_for(B.ncol), kThreads, 0, s>>>(B.cptr, B.ncol, B.cedge, r, c2));
+    (g2p::kbegin("k_v0_export", s), k_v0_export<<<grid_for(B.ncol), kThreads, 0, s>>>(B.cptr, B.ncol, B.cedge, r, c2), g2p::kend(s));
     if (row) G2P_CUDA(cudaMemcpyAsync(row, r, sizeof(int64_t) * B.nnz, cudaMemcpyDeviceToHost, s));
     if (col) G2P_CUDA(cudaMemcpyAsync(col, c2, sizeof(int64_t) * B.nnz, cudaMemcpyDeviceToHost, s));
     if (val) G2P_CUDA(cudaMemcpyAsync(val, B.cval, sizeof(double) * B.nnz, cudaMemcpyDeviceToHost, s));
     if (aval) G2P_CUDA(cudaMemcpyAsync(aval, B.caval, sizeof(double) * B.nnz, cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
     if (map) {
-        (g2p::launch_tick(), k_map_export<<<grid_for(m->d.N_node), kThreads, 0, s>>>(B.map, m->d.N_node, c2));
+        (g2p::kbegin("k_map_export", s), k_map_export<<<grid_for(m->d.N_node), kThreads, 0, s>>>(B.map, m->d.N_node, c2), g2p::kend(s));
         G2P_CUDA(cudaMemcpyAsync(map, c2, sizeof(int64_t) * m->d.N_node, cudaMemcpyDeviceToHost, s));
     }
     G2P_CUDA(cudaStreamSynchronize(s));

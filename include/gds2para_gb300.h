@@ -175,6 +175,10 @@ g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p, double *z
 int64_t g2p_launch_count(void);
 void g2p_profile_begin(void);
 g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, int64_t *launches);
+/* Per-kernel device time of the last profiled interval, one line per kernel
+ * ("name<TAB>launches<TAB>total_ms"); returns the full length, writes at most
+ * cap-1 bytes plus a terminator. */
+int64_t g2p_profile_report(char *buf, int64_t cap);
 
 #ifdef __cplusplus
 }
