@@ -1,0 +1,72 @@
+"""g2p_map_edge_noalloc (setMapEdge on device pointers, static scratch) against
+g2p_index_maps, the allocating entry point, on the same layouts.
+
+The file name sorts last so that the run also covers the entry point after
+every other GPU test has used the device; it passes on its own as well."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import golden_layout
+
+pytestmark = pytest.mark.gpu
+
+MAX_EDGES = 32767 * 2048
+
+
+def _noalloc(L, d, torch):
+    dev = torch.device("cuda:0")
+    me = torch.from_numpy(np.ascontiguousarray(d.mark_edge, dtype=np.int64)).to(dev)
+    cr = torch.from_numpy(np.ascontiguousarray(d.cdt_return, dtype=np.uint8)).to(dev)
+    # Outputs start as garbage: the entry point must not rely on them.
+    out = torch.full((d.N_edge,), -7, dtype=torch.int64, device=dev)
+    bden = torch.full((1,), -7, dtype=torch.int64, device=dev)
+    s = torch.cuda.current_stream()
+    st = L.g2p_map_edge_noalloc(d.nx, d.ny, d.nz, me.data_ptr(), cr.data_ptr(), int(d.num_cdt),
+                                out.data_ptr(), bden.data_ptr(), C.c_void_p(s.cuda_stream))
+    from gds2para_gb300 import _lib
+    _lib.check(st)
+    s.synchronize()
+    return out.cpu().numpy(), int(bden.cpu().item())
+
+
+def _allocating(d):
+    from gds2para_gb300 import api
+    with api.FdtdMesh(d) as m:
+        return m.index_maps()
+
+
+def test_noalloc_map_edge_matches_index_maps_two_calls_in_a_row():
+    torch = pytest.importorskip("torch")
+    from gds2para_gb300 import _lib, layout as lay
+    L = _lib.load()
+    big = lay.build(lay.config("c1"))
+    small, _, _ = golden_layout("manhattan_small")
+    want_big, want_small = _allocating(big), _allocating(small)
+    # Larger layout, then smaller, then larger again: stale partials from a
+    # previous call must not leak into the next one.
+    for d, (want_map, want_bden) in ((big, want_big), (small, want_small), (big, want_big)):
+        got_map, got_bden = _noalloc(L, d, torch)
+        assert got_bden == want_bden
+        np.testing.assert_array_equal(got_map, want_map)
+
+
+def test_noalloc_rejects_sizes_beyond_its_scratch():
+    torch = pytest.importorskip("torch")
+    from gds2para_gb300 import _lib
+    L = _lib.load()
+    buf = torch.zeros(64, dtype=torch.int64, device="cuda:0")   # >= 54 edges of a 3x3x3 grid
+    cr = torch.zeros(1, dtype=torch.uint8, device="cuda:0")
+    nx = ny = 3000
+    nz = 5
+    n_edge = ((ny - 1) * nx + (nx - 1) * ny) * nz + nx * ny * (nz - 1)
+    assert n_edge > MAX_EDGES
+    st = L.g2p_map_edge_noalloc(nx, ny, nz, buf.data_ptr(), cr.data_ptr(), 1, buf.data_ptr(), buf.data_ptr(),
+                                None)
+    assert st == 1
+    assert b"67106816" in L.g2p_last_error()
+    # Host memory the device cannot address is refused too.
+    host = np.zeros(64, np.int64)
+    st = L.g2p_map_edge_noalloc(3, 3, 3, host.ctypes.data, cr.data_ptr(), 1, buf.data_ptr(), buf.data_ptr(), None)
+    assert st == 1
