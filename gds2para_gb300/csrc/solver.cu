@@ -155,6 +155,13 @@ __global__ void k_list_long(int64_t n, const int64_t *ptr, const int64_t *pos, i
         if ((ptr[i + 1] - ptr[i]) > kLongRow) rows[pos[i]] = (int32_t)i;
 }
 
+__global__ void k_long_extent(int64_t nl, const int32_t *rows, const int64_t *ptr, int64_t *ext) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x) {
+        ext[2 * i] = ptr[rows[i]];
+        ext[2 * i + 1] = ptr[rows[i] + 1];
+    }
+}
+
 template <class T>
 g2p_status find_long_rows(const Csr<T> &A, LongRows &lr, cudaStream_t s) {
     lr.release(s);
@@ -171,20 +178,18 @@ g2p_status find_long_rows(const Csr<T> &A, LongRows &lr, cudaStream_t s) {
     if (nl > 0) {
         G2P_TRY(dalloc(&lr.rows, nl, s));
         (g2p::kbegin("k_list_long", s), k_list_long<<<grid_for(n), kThreads, 0, s>>>(n, A.ptr, pos, lr.rows), g2p::kend(s));
-        // chunk table on the host from the (few) long rows' extents
-        std::vector<int32_t> rows(nl);
-        G2P_CUDA(cudaMemcpyAsync(rows.data(), lr.rows, sizeof(int32_t) * nl, cudaMemcpyDeviceToHost, s));
+        // chunk table on the host from the long rows' extents (one copy)
+        int64_t *ext;
+        G2P_TRY(dalloc(&ext, 2 * nl, s));
+        (g2p::kbegin("k_long_extent", s), k_long_extent<<<grid_for(nl), kThreads, 0, s>>>(nl, lr.rows, A.ptr, ext), g2p::kend(s));
+        std::vector<int64_t> be(2 * nl);
+        G2P_CUDA(cudaMemcpyAsync(be.data(), ext, sizeof(int64_t) * 2 * nl, cudaMemcpyDeviceToHost, s));
         G2P_CUDA(cudaStreamSynchronize(s));
-        std::vector<int64_t> beg(nl), end(nl);
-        for (int64_t l = 0; l < nl; l++) {
-            G2P_CUDA(cudaMemcpyAsync(&beg[l], A.ptr + rows[l], sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-            G2P_CUDA(cudaMemcpyAsync(&end[l], A.ptr + rows[l] + 1, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-        }
-        G2P_CUDA(cudaStreamSynchronize(s));
+        dfree(ext, s);
         std::vector<int32_t> crow;
         std::vector<int64_t> cbeg, rcp(nl + 1, 0);
         for (int64_t l = 0; l < nl; l++) {
-            for (int64_t q = beg[l]; q < end[l]; q += kLongChunk) { crow.push_back((int32_t)l); cbeg.push_back(q); }
+            for (int64_t q = be[2 * l]; q < be[2 * l + 1]; q += kLongChunk) { crow.push_back((int32_t)l); cbeg.push_back(q); }
             rcp[l + 1] = (int64_t)crow.size();
         }
         lr.n = nl;
@@ -848,7 +853,27 @@ static g2p_status offsets_of(const int64_t *cnt, int64_t n, int64_t *off, cudaSt
     return G2P_OK;
 }
 
+// Host wall time of setup phases, printed with G2P_DEBUG >= 2 (synchronizes).
+struct PhaseClock {
+    bool on = false;
+    std::chrono::steady_clock::time_point t0;
+    PhaseClock() {
+        const char *e = getenv("G2P_DEBUG");
+        on = e && atoi(e) >= 2;
+        t0 = std::chrono::steady_clock::now();
+    }
+    void mark(const char *what, int level, cudaStream_t s) {
+        if (!on) return;
+        cudaStreamSynchronize(s);
+        auto t = std::chrono::steady_clock::now();
+        fprintf(stderr, "[g2p setup] L%d %-14s %8.3f ms\n", level, what,
+                std::chrono::duration<double, std::milli>(t - t0).count());
+        t0 = t;
+    }
+};
+
 g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_t s, int64_t *, Hierarchy<double> &H) {
+    PhaseClock pc_;
     H.release(s);
     // level 0 owns a copy of the operator
     Level<double> L0;
@@ -878,7 +903,9 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
         G2P_TRY(dalloc(&L.dinv, n, s));
         (g2p::kbegin("k_diag", s), k_diag<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag), g2p::kend(s));
         G2P_CUDA(cudaMemsetAsync(d_lmax, 0, sizeof(unsigned long long), s));
+        pc_.mark("start", l, s);
         G2P_TRY(find_long_rows<double>(L.A, L.lr, s));   // synchronizes
+        pc_.mark("long rows", l, s);
         (g2p::kbegin("k_dinv_gersh", s), k_dinv_gersh<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.val, diag, L.dinv, d_lmax), g2p::kend(s));
         if (L.lr.n > 0) (g2p::kbegin("k_gersh_long", s), k_gersh_long<<<(unsigned)L.lr.n, 256, 0, s>>>(L.lr.rows, L.A.ptr, L.A.val, diag, d_lmax), g2p::kend(s));
         unsigned long long lb = 0;
@@ -887,6 +914,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
         double lm;
         memcpy(&lm, &lb, sizeof(lm));
         L.lmax = lm > 0 ? lm : 2.0;
+        pc_.mark("gershgorin", l, s);
         bool last = n <= cfg.coarse_size || l + 1 >= cfg.max_levels;
         if (!last) {
             // ---- aggregation
@@ -907,6 +935,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 G2P_CUDA(cudaStreamSynchronize(s));
                 if (und == 0) break;
             }
+            pc_.mark("mis", l, s);
             int64_t *rootid;
             G2P_TRY(dalloc(&rootid, n + 1, s));
             G2P_TRY(need_work(n + 1));
@@ -927,6 +956,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             (g2p::kbegin("k_agg_phase2", s), k_agg_phase2<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, agg1, L.agg), g2p::kend(s));
             G2P_CUDA(cudaStreamSynchronize(s));
             dfree(agg1, s); dfree(rootid, s); dfree(dense, s); dfree(T, s); dfree(M1, s); dfree(M2, s);
+            pc_.mark("aggregates", l, s);
             if (nc == 0 || nc > (n * 9) / 10) {
                 dfree(L.agg, s);
                 last = true;
@@ -955,6 +985,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 L.rmem = in1 ? v1 : v0;
                 dfree(in1 ? v0 : v1, s);
                 dfree(k0, s); dfree(k1, s); dfree(pos, s);
+                pc_.mark("members", l, s);
                 // ---- smoothed prolongation P = (I - w D^-1 A) T
                 double w = 4.0 / (3.0 * L.lmax);
                 int64_t *pc;
@@ -967,6 +998,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 L.P.n = n; L.P.m = nc; L.P.nnz = pnnz;
                 G2P_TRY(dalloc(&L.P.col, pnnz, s)); G2P_TRY(dalloc(&L.P.val, pnnz, s));
                 (g2p::kbegin("k_ps_fill", s), k_ps_fill<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, L.agg, w, L.P.ptr, L.P.col, L.P.val), g2p::kend(s));
+                pc_.mark("prolongation", l, s);
                 // ---- B = T^T A (nc x n)
                 int64_t *cnt, *off;
                 G2P_TRY(dalloc(&cnt, n + 1, s)); G2P_TRY(dalloc(&off, n + 1, s));
@@ -980,6 +1012,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 dfree(cnt, s); dfree(off, s);
                 Csr<double> B;
                 G2P_TRY(esc_to_csr(ek0, ev0, ne, nc, n, s, B));
+                pc_.mark("T^T A", l, s);
                 // ---- A_c = B P (nc x nc), entry-parallel over B
                 G2P_TRY(dalloc(&off, B.nnz + 1, s));
                 {
@@ -1003,6 +1036,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 G2P_TRY(esc_to_csr(ek0, ev0, ne, nc, nc, s, C.A));
                 L.nc = nc;
                 H.lv.push_back(C);
+                pc_.mark("galerkin", l, s);
             }
         }
         dfree(diag, s);
@@ -1020,6 +1054,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             (g2p::kbegin("k_gauss_jordan", s), k_gauss_jordan<<<1, 1024, 0, s>>>(Dm, H.cinv, nn, d_int), g2p::kend(s));
             G2P_CUDA(cudaStreamSynchronize(s));
             dfree(Dm, s);
+            pc_.mark("coarse inverse", l, s);
             break;
         }
     }
