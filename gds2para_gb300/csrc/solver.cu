@@ -511,25 +511,35 @@ __global__ void k_agg_init(int64_t n, const int64_t *ptr, const int32_t *col, co
         dense[i] = (ptr[i + 1] - ptr[i]) > lim ? 1 : 0;
 }
 
-__global__ void k_agg_state(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
-                            double theta, const uint8_t *dense, uint64_t *T) {
+// Strong-connection mask per entry, evaluated once per level:
+// |a_ij| >= theta sqrt(|a_ii a_jj|), j != i, j not dense.  Dense rows are
+// left unwritten; every reader skips them.
+__global__ void k_strong_mask(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
+                              double theta, const uint8_t *dense, uint8_t *sm) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (dense[i]) continue;
+        for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) sm[q] = strong(i, q, col, val, diag, dense, theta) ? 1 : 0;
+    }
+}
+
+__global__ void k_agg_state(int64_t n, const int64_t *ptr, const uint8_t *sm, const uint8_t *dense, uint64_t *T) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         bool elig = false;
         if (!dense[i])
             for (int64_t q = ptr[i]; q < ptr[i + 1]; q++)
-                if (strong(i, q, col, val, diag, dense, theta)) { elig = true; break; }
+                if (sm[q]) { elig = true; break; }
         uint64_t st = elig ? 1ull : 0ull;
         T[i] = (st << 62) | ((uint64_t)(hash32((uint32_t)i * 2654435761u + 12345u) & 0x3fffffffu) << 32) | (uint64_t)(uint32_t)i;
     }
 }
 
-__global__ void k_mis_max(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
-                          double theta, const uint8_t *dense, const uint64_t *in, uint64_t *out) {
+__global__ void k_mis_max(int64_t n, const int64_t *ptr, const int32_t *col, const uint8_t *sm, const uint8_t *dense,
+                          const uint64_t *in, uint64_t *out) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         uint64_t m = in[i];
         if (!dense[i])
             for (int64_t q = ptr[i]; q < ptr[i + 1]; q++)
-                if (strong(i, q, col, val, diag, dense, theta)) { uint64_t v = in[col[q]]; m = v > m ? v : m; }
+                if (sm[q]) { uint64_t v = in[col[q]]; m = v > m ? v : m; }
         out[i] = m;
     }
 }
@@ -553,9 +563,8 @@ __global__ void k_root_flag(int64_t n, const uint64_t *T, const uint8_t *dense, 
         flag[i] = ((T[i] >> 62) == 2 || dense[i]) ? 1 : 0;
 }
 
-__global__ void k_agg_phase1(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
-                             double theta, const uint8_t *dense, const uint64_t *T, const int64_t *rootid,
-                             int32_t *agg1) {
+__global__ void k_agg_phase1(int64_t n, const int64_t *ptr, const int32_t *col, const uint8_t *sm, const uint8_t *dense,
+                             const uint64_t *T, const int64_t *rootid, int32_t *agg1) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         uint64_t t = T[i];
         if ((t >> 62) == 2 || dense[i]) { agg1[i] = (int32_t)rootid[i]; continue; }
@@ -564,7 +573,7 @@ __global__ void k_agg_phase1(int64_t n, const int64_t *ptr, const int32_t *col, 
         uint64_t best = 0;
         int64_t bj = -1;
         for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) {
-            if (!strong(i, q, col, val, diag, dense, theta)) continue;
+            if (!sm[q]) continue;
             uint64_t v = T[col[q]];
             if ((v >> 62) == 2 && v > best) { best = v; bj = col[q]; }
         }
@@ -572,9 +581,8 @@ __global__ void k_agg_phase1(int64_t n, const int64_t *ptr, const int32_t *col, 
     }
 }
 
-__global__ void k_agg_phase2(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const double *diag,
-                             double theta, const uint8_t *dense, const uint64_t *T, const int32_t *agg1,
-                             int32_t *agg) {
+__global__ void k_agg_phase2(int64_t n, const int64_t *ptr, const int32_t *col, const double *val, const uint8_t *sm,
+                             const int32_t *agg1, int32_t *agg) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int32_t a = agg1[i];
         if (a != -2) { agg[i] = a; continue; }
@@ -582,7 +590,7 @@ __global__ void k_agg_phase2(int64_t n, const int64_t *ptr, const int32_t *col, 
         double best = -1;
         int32_t ba = -1;
         for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) {
-            if (!strong(i, q, col, val, diag, dense, theta)) continue;
+            if (!sm[q]) continue;
             elig = true;
             int32_t aj = agg1[col[q]];
             if (aj >= 0 && fabs(val[q]) > best) { best = fabs(val[q]); ba = aj; }
@@ -622,17 +630,59 @@ __global__ void k_heads64(const uint64_t *keys, int64_t n, int64_t *head) {
         head[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
 }
 
-__global__ void k_seg_reduce(const uint64_t *keys, const double *vals, int64_t n, const int64_t *segid, uint64_t nc,
-                             int64_t *rowcnt, int32_t *ocol, double *oval) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        if (!(i == 0 || keys[i] != keys[i - 1])) continue;
-        double sacc = 0;
-        int64_t j = i;
-        while (j < n && keys[j] == keys[i]) { sacc += vals[j]; j++; }
-        int64_t sg = segid[i];
-        ocol[sg] = (int32_t)(keys[i] % nc);
-        oval[sg] = sacc;
-        atomicAdd((unsigned long long *)&rowcnt[keys[i] / nc], 1ull);
+// Segmented sums of the sorted expansion, deterministic: segments of at
+// most kSegShort entries are summed in order by one thread, longer ones
+// (the coarse conductor couplings) by a block in a fixed tree order.
+constexpr int64_t kSegShort = 32;
+
+__global__ void k_seg_start(const int64_t *head, const int64_t *segid, int64_t ne, int64_t nseg, int64_t *sstart) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ne; i += (int64_t)gridDim.x * blockDim.x)
+        if (head[i]) sstart[segid[i]] = i;
+    if (blockIdx.x == 0 && threadIdx.x == 0) sstart[nseg] = ne;
+}
+
+__global__ void k_seg_short(const uint64_t *keys, const double *vals, int64_t nseg, const int64_t *sstart, uint64_t nc,
+                            int32_t *ocol, double *oval, int64_t *longlist, unsigned long long *nlong) {
+    for (int64_t sg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sg < nseg; sg += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = sstart[sg], e = sstart[sg + 1];
+        ocol[sg] = (int32_t)(keys[b] % nc);
+        if (e - b <= kSegShort) {
+            double acc = 0;
+            for (int64_t j = b; j < e; j++) acc += vals[j];
+            oval[sg] = acc;
+        } else {
+            longlist[atomicAdd(nlong, 1ull)] = sg;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_seg_long(const double *vals, const int64_t *sstart, const int64_t *longlist,
+                                                  const unsigned long long *nlong, double *oval) {
+    __shared__ double sm[256];
+    const int64_t nl = (int64_t)*nlong;
+    for (int64_t li = blockIdx.x; li < nl; li += gridDim.x) {
+        const int64_t sg = longlist[li];
+        const int64_t b = sstart[sg], e = sstart[sg + 1];
+        double acc = 0;
+        for (int64_t j = b + threadIdx.x; j < e; j += 256) acc += vals[j];
+        sm[threadIdx.x] = acc;
+        __syncthreads();
+        for (int w = 128; w > 0; w >>= 1) {
+            if (threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) oval[sg] = sm[0];
+        __syncthreads();
+    }
+}
+
+// Row offsets of the reduced matrix: keys are sorted by (row, column).
+__global__ void k_seg_rowptr(const uint64_t *keys, const int64_t *sstart, int64_t nseg, uint64_t nc, int64_t nrows,
+                             int64_t *ptr) {
+    for (int64_t sg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sg <= nseg; sg += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = sg < nseg ? (int64_t)(keys[sstart[sg]] / nc) : nrows;
+        const int64_t rp = sg > 0 ? (int64_t)(keys[sstart[sg - 1]] / nc) : -1;
+        for (int64_t a = rp + 1; a <= r; a++) ptr[a] = sg;
     }
 }
 
@@ -826,16 +876,24 @@ static g2p_status esc_to_csr(uint64_t *&k0, double *&v0, int64_t ne, int64_t nro
     G2P_CUDA(cudaMemcpyAsync(&nseg, segid + ne, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
     out.n = nrows; out.m = ncols; out.nnz = nseg;
-    int64_t *rowcnt;
-    G2P_TRY(dalloc(&rowcnt, nrows + 1, s));
-    G2P_CUDA(cudaMemsetAsync(rowcnt, 0, sizeof(int64_t) * (nrows + 1), s));
     G2P_TRY(dalloc(&out.col, nseg, s)); G2P_TRY(dalloc(&out.val, nseg, s)); G2P_TRY(dalloc(&out.ptr, nrows + 1, s));
-    (g2p::kbegin("k_seg_reduce", s), k_seg_reduce<<<grid_for(ne), kThreads, 0, s>>>(sk, sv, ne, segid, (uint64_t)ncols, rowcnt, out.col, out.val), g2p::kend(s));
-    const int64_t *rc = rowcnt;
-    auto rcop = [rc, nrows] __device__(int64_t i) -> int64_t { return i < nrows ? rc[i] : 0; };
-    G2P_TRY(exclusive_scan(rcop, nrows + 1, out.ptr, work, s));
+    int64_t *sstart, *longlist;
+    unsigned long long *nlong;
+    G2P_TRY(dalloc(&sstart, nseg + 1, s));
+    G2P_TRY(dalloc(&longlist, ne / (kSegShort + 1) + 1, s));
+    G2P_TRY(dalloc(&nlong, 1, s));
+    G2P_CUDA(cudaMemsetAsync(nlong, 0, sizeof(unsigned long long), s));
+    (g2p::kbegin("k_seg_start", s), k_seg_start<<<grid_for(ne), kThreads, 0, s>>>(head, segid, ne, nseg, sstart), g2p::kend(s));
+    (g2p::kbegin("k_seg_short", s), k_seg_short<<<grid_for(nseg), kThreads, 0, s>>>(sk, sv, nseg, sstart, (uint64_t)ncols, out.col, out.val, longlist, nlong), g2p::kend(s));
+    (g2p::kbegin("k_seg_long", s), k_seg_long<<<kSMs * 4, 256, 0, s>>>(sv, sstart, longlist, nlong, out.val), g2p::kend(s));
+    if (nseg > 0) {
+        (g2p::kbegin("k_seg_rowptr", s), k_seg_rowptr<<<grid_for(nseg + 1), kThreads, 0, s>>>(sk, sstart, nseg, (uint64_t)ncols, nrows, out.ptr), g2p::kend(s));
+    } else {
+        G2P_CUDA(cudaMemsetAsync(out.ptr, 0, sizeof(int64_t) * (nrows + 1), s));
+    }
     G2P_CUDA(cudaStreamSynchronize(s));
-    dfree(rowcnt, s); dfree(head, s); dfree(segid, s); dfree(work, s);
+    dfree(sstart, s); dfree(longlist, s); dfree(nlong, s);
+    dfree(head, s); dfree(segid, s); dfree(work, s);
     dfree(k0, s); dfree(k1, s); dfree(v0, s); dfree(v1, s);
     k0 = nullptr; v0 = nullptr;
     return G2P_OK;
@@ -924,10 +982,13 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             G2P_TRY(dalloc(&dense, n, s)); G2P_TRY(dalloc(&T, n, s)); G2P_TRY(dalloc(&M1, n, s)); G2P_TRY(dalloc(&M2, n, s));
             unsigned g = grid_for(n);
             (g2p::kbegin("k_agg_init", s), k_agg_init<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, lim, cfg.strength, dense, T), g2p::kend(s));
-            (g2p::kbegin("k_agg_state", s), k_agg_state<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T), g2p::kend(s));
+            uint8_t *smask;
+            G2P_TRY(dalloc(&smask, L.A.nnz, s));
+            (g2p::kbegin("k_strong_mask", s), k_strong_mask<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, smask), g2p::kend(s));
+            (g2p::kbegin("k_agg_state", s), k_agg_state<<<g, kThreads, 0, s>>>(n, L.A.ptr, smask, dense, T), g2p::kend(s));
             for (int round = 0; round < 200; round++) {
-                (g2p::kbegin("k_mis_max", s), k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, M1), g2p::kend(s));
-                (g2p::kbegin("k_mis_max", s), k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, M1, M2), g2p::kend(s));
+                (g2p::kbegin("k_mis_max", s), k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, smask, dense, T, M1), g2p::kend(s));
+                (g2p::kbegin("k_mis_max", s), k_mis_max<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, smask, dense, M1, M2), g2p::kend(s));
                 G2P_CUDA(cudaMemsetAsync(d_int, 0, sizeof(int), s));
                 (g2p::kbegin("k_mis_update", s), k_mis_update<<<g, kThreads, 0, s>>>(n, T, M2, d_int), g2p::kend(s));
                 int und = 0;
@@ -952,10 +1013,10 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             int32_t *agg1;
             G2P_TRY(dalloc(&agg1, n, s));
             G2P_TRY(dalloc(&L.agg, n, s));
-            (g2p::kbegin("k_agg_phase1", s), k_agg_phase1<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, rootid, agg1), g2p::kend(s));
-            (g2p::kbegin("k_agg_phase2", s), k_agg_phase2<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, cfg.strength, dense, T, agg1, L.agg), g2p::kend(s));
+            (g2p::kbegin("k_agg_phase1", s), k_agg_phase1<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, smask, dense, T, rootid, agg1), g2p::kend(s));
+            (g2p::kbegin("k_agg_phase2", s), k_agg_phase2<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, smask, agg1, L.agg), g2p::kend(s));
             G2P_CUDA(cudaStreamSynchronize(s));
-            dfree(agg1, s); dfree(rootid, s); dfree(dense, s); dfree(T, s); dfree(M1, s); dfree(M2, s);
+            dfree(agg1, s); dfree(rootid, s); dfree(dense, s); dfree(smask, s); dfree(T, s); dfree(M1, s); dfree(M2, s);
             pc_.mark("aggregates", l, s);
             if (nc == 0 || nc > (n * 9) / 10) {
                 dfree(L.agg, s);

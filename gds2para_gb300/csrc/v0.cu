@@ -388,16 +388,30 @@ __global__ void k_heads(const uint64_t *keys, int64_t n, int64_t *head) {
         head[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
 }
 
-// Ordered sum of each key's values; keeps |v| > 1e-8 (fdtd.hpp:2852).
-__global__ void k_seg_sum(const uint64_t *keys, const double *vals, int64_t n, const int64_t *segid, int64_t ncolall,
+__global__ void k_seg_bounds(const int64_t *head, const int64_t *segid, int64_t n, int64_t nseg, int64_t *sstart) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (head[i]) sstart[segid[i]] = i;
+    if (blockIdx.x == 0 && threadIdx.x == 0) sstart[nseg] = n;
+}
+
+// Ordered sum of each key's values (left to right, from 0.0, so bit-equal
+// to the reference's accumulation); keeps |v| > 1e-8 (fdtd.hpp:2852).  The
+// loads run eight ahead of the dependent additions.
+__global__ void k_seg_sum(const uint64_t *keys, const double *vals, int64_t nseg, const int64_t *sstart,
                           uint64_t *okey, double *oval, int64_t *keep) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        if (!(i == 0 || keys[i] != keys[i - 1])) continue;
+    for (int64_t sg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sg < nseg; sg += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = sstart[sg], e = sstart[sg + 1];
         double s = 0.0;
-        int64_t j = i;
-        while (j < n && keys[j] == keys[i]) { s += vals[j]; j++; }
-        int64_t sg = segid[i];
-        okey[sg] = keys[i];
+        int64_t j = b;
+        for (; j + 8 <= e; j += 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) v[u] = vals[j + u];
+#pragma unroll
+            for (int u = 0; u < 8; u++) s += v[u];
+        }
+        for (; j < e; j++) s += vals[j];
+        okey[sg] = keys[b];
         oval[sg] = s;
         keep[sg] = fabs(s) > 1e-8 ? 1 : 0;
     }
@@ -511,7 +525,11 @@ static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool 
         G2P_CUDA(cudaStreamSynchronize(s));
         G2P_TRY(dalloc(&okey, nseg, s)); G2P_TRY(dalloc(&oval, nseg, s));
         G2P_TRY(dalloc(&keep, nseg + 1, s)); G2P_TRY(dalloc(&kpos, nseg + 1, s));
-        (g2p::kbegin("k_seg_sum", s), k_seg_sum<<<grid_for(nterm), kThreads, 0, s>>>(sk, sv, nterm, segid, ncol, okey, oval, keep), g2p::kend(s));
+        int64_t *sstart;
+        G2P_TRY(dalloc(&sstart, nseg + 1, s));
+        (g2p::kbegin("k_seg_bounds", s), k_seg_bounds<<<grid_for(nterm), kThreads, 0, s>>>(head, segid, nterm, nseg, sstart), g2p::kend(s));
+        (g2p::kbegin("k_seg_sum", s), k_seg_sum<<<grid_for(nseg), kThreads, 0, s>>>(sk, sv, nseg, sstart, okey, oval, keep), g2p::kend(s));
+        dfree(sstart, s);
         (g2p::kbegin("k_long_rowlen", s), k_long_rowlen<<<grid_for(nseg), kThreads, 0, s>>>(okey, keep, nseg, ncol, rowlen + nshort), g2p::kend(s));
         const int64_t *kp = keep;
         auto kop = [kp, nseg] __device__(int64_t i) -> int64_t { return i < nseg ? kp[i] : 0; };
