@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-ports", type=int, default=1)
+    ap.add_argument("--once", action="store_true",
+                    help="run one untimed step and exit (for profiler captures; prints no bench line)")
     return ap.parse_args()
 
 
@@ -191,6 +193,11 @@ def run_gb300(args):
             el = float(t.item())
         return el, L.g2p_launch_count() - n0, kern
 
+    if args.once:
+        step(dev)
+        torch.cuda.synchronize()
+        return {"once": True, "config": args.config, "precision": args.precision,
+                "iterations": stats.total_iterations}, rank
     for _ in range(max(args.warmup, 3)):
         step(dev)
     clocks = Clocks(local)

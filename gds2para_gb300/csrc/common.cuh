@@ -37,6 +37,7 @@ void kend(cudaStream_t s);
 bool kprof_on();
 void kprof_set(bool on);
 g2p_status kprof_collect();
+void kprof_add_total(const char *name, int64_t launches, double ms);
 
 constexpr int kSMs = 152;            // GB300: 2 dies x 76 SMs
 constexpr int kThreads = 256;

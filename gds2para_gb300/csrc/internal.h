@@ -5,14 +5,32 @@
 
 namespace g2p {
 
-// Device CSR with int64 row offsets and int32 columns.
+constexpr uint8_t kSellLong = 255;   // rlen of a row served by the long-row kernels
+
+// Device CSR with int64 row offsets and int32 columns, plus an optional
+// sliced-ELL copy of its short rows for the SpMM: slices of 32 rows whose
+// entries are stored column by column (entry j of row 32 s + t at
+// sptr[s] + 32 j + t), rlen[i] the row's entry count or kSellLong.
 template <class T>
 struct Csr {
     int64_t n = 0, m = 0, nnz = 0;
     int64_t *ptr = nullptr;
     int32_t *col = nullptr;
     T *val = nullptr;
-    void release(cudaStream_t s) { dfree(ptr, s); dfree(col, s); dfree(val, s); n = m = nnz = 0; }
+    int64_t *sptr = nullptr;
+    int32_t *scol = nullptr;
+    T *sval = nullptr;
+    uint8_t *rlen = nullptr;
+    int64_t short_nnz = 0, sell_slots = 0;
+    void release_sell(cudaStream_t s) {
+        dfree(sptr, s); dfree(scol, s); dfree(sval, s); dfree(rlen, s);
+        short_nnz = sell_slots = 0;
+    }
+    void release(cudaStream_t s) {
+        dfree(ptr, s); dfree(col, s); dfree(val, s);
+        release_sell(s);
+        n = m = nnz = 0;
+    }
 };
 
 // One V0 basis: column-major (CSR over columns, entries in the reference's

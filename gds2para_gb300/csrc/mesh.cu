@@ -144,6 +144,14 @@ extern "C" const char *g2p_version(void) { return "gds2para_gb300 0.1 (sm_103a)"
 extern "C" int64_t g2p_launch_count(void) { return g2p::launch_count(); }
 
 // One line per kernel, "name<TAB>launches<TAB>total_ms", by decreasing time.
+namespace g2p {
+void kprof_add_total(const char *name, int64_t launches, double ms) {
+    auto &t = g_np.totals[name];
+    t.first += launches;
+    t.second += ms;
+}
+}  // namespace g2p
+
 extern "C" int64_t g2p_profile_report(char *buf, int64_t cap) {
     std::vector<std::pair<double, std::string>> rows;
     for (auto &kv : g2p::g_np.totals) {

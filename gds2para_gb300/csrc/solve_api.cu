@@ -167,6 +167,15 @@ g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cu
         S->levels = (int)S->H64.lv.size();
         S->coarse_rows = S->H64.nc;
     }
+    // sliced-ELL copies of every operator the solves multiply by
+    if ((st = sell_build<double>(S->A, s)) != G2P_OK) return fail(st);
+    if (S->precision == G2P_PREC_MIXED) {
+        for (auto &L : S->H32.lv)
+            if ((st = sell_build<float>(L.A, s)) != G2P_OK) return fail(st);
+    } else {
+        for (auto &L : S->H64.lv)
+            if ((st = sell_build<double>(L.A, s)) != G2P_OK) return fail(st);
+    }
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) { set_last_error(e, "solver setup", __FILE__, __LINE__); return fail(G2P_ERR_CUDA); }
     S->setup_ms = ms_since(t0);

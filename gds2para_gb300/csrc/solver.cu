@@ -59,39 +59,181 @@ __global__ void __launch_bounds__(256) k_spmm(int64_t n, const int64_t *__restri
     }
 }
 
-// Long rows, stage 1: one block per chunk of kLongChunk entries; partial
-// sums for every right-hand side.
+// ---- sliced-ELL SpMM: one row per thread group, V right-hand sides per
+// thread loaded as 16- or 8-byte vectors; the slice layout makes the column
+// and value loads of a warp contiguous.
+template <class T, int V>
+struct XVec {
+    T v[V];
+    __device__ __forceinline__ void load(const T *__restrict__ p) {
+        if constexpr (V * sizeof(T) >= 16) {
+            constexpr int W = 16 / sizeof(T);
+#pragma unroll
+            for (int u = 0; u < V; u += W) {
+                if constexpr (sizeof(T) == 4) {
+                    float4 t = __ldg(reinterpret_cast<const float4 *>(p + u));
+                    v[u] = t.x; v[u + 1] = t.y; v[u + 2] = t.z; v[u + 3] = t.w;
+                } else {
+                    double2 t = __ldg(reinterpret_cast<const double2 *>(p + u));
+                    v[u] = t.x; v[u + 1] = t.y;
+                }
+            }
+        } else if constexpr (V * sizeof(T) == 8 && sizeof(T) == 4) {
+            float2 t = __ldg(reinterpret_cast<const float2 *>(p));
+            v[0] = t.x; v[1] = t.y;
+        } else {
+#pragma unroll
+            for (int u = 0; u < V; u++) v[u] = __ldg(p + u);
+        }
+    }
+    __device__ __forceinline__ void store(T *__restrict__ p) const {
+        if constexpr (V * sizeof(T) >= 16) {
+            constexpr int W = 16 / sizeof(T);
+#pragma unroll
+            for (int u = 0; u < V; u += W) {
+                if constexpr (sizeof(T) == 4) *reinterpret_cast<float4 *>(p + u) = make_float4(v[u], v[u + 1], v[u + 2], v[u + 3]);
+                else *reinterpret_cast<double2 *>(p + u) = make_double2(v[u], v[u + 1]);
+            }
+        } else if constexpr (V * sizeof(T) == 8 && sizeof(T) == 4) {
+            *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
+        } else {
+#pragma unroll
+            for (int u = 0; u < V; u++) p[u] = v[u];
+        }
+    }
+};
+
+constexpr int kSellUnroll = 8;
+
+// y = A x (or b - A x) over the short rows.  Block (tpr, 256 / tpr): the
+// tpr = k / V threads of a row each own V consecutive right-hand sides.
+template <class T, int V>
+__global__ void __launch_bounds__(256) k_spmm_sell(int64_t n, const int64_t *__restrict__ sptr,
+                                                   const int32_t *__restrict__ scol, const T *__restrict__ sval,
+                                                   const uint8_t *__restrict__ rlen, const T *__restrict__ x,
+                                                   T *__restrict__ y, int k, const T *__restrict__ b) {
+    const int xo = threadIdx.x * V;
+    G2P_FOR_ROWS(i, n) {
+        const int len = rlen[i];
+        if (len == kSellLong) continue;
+        const int64_t base = sptr[i >> 5] + (i & 31);
+        T acc[V];
+#pragma unroll
+        for (int u = 0; u < V; u++) acc[u] = 0;
+        for (int j0 = 0; j0 < len; j0 += kSellUnroll) {
+            // all gathers of the chunk are issued before the first use; past
+            // the row's end they repeat its first column and are not added
+            int32_t c[kSellUnroll];
+            T a[kSellUnroll];
+#pragma unroll
+            for (int u = 0; u < kSellUnroll; u++) {
+                const bool in = j0 + u < len;
+                c[u] = in ? __ldg(scol + base + 32 * (int64_t)(j0 + u)) : c[0];
+                a[u] = in ? __ldg(sval + base + 32 * (int64_t)(j0 + u)) : T(0);
+            }
+            XVec<T, V> xv[kSellUnroll];
+#pragma unroll
+            for (int u = 0; u < kSellUnroll; u++) xv[u].load(x + (int64_t)c[u] * k + xo);
+#pragma unroll
+            for (int u = 0; u < kSellUnroll; u++)
+                if (j0 + u < len) {
+#pragma unroll
+                    for (int w = 0; w < V; w++) acc[w] += a[u] * xv[u].v[w];
+                }
+        }
+        const int64_t t = i * k + xo;
+        XVec<T, V> out;
+        if (b) {
+            XVec<T, V> bv;
+            bv.load(b + t);
+#pragma unroll
+            for (int w = 0; w < V; w++) out.v[w] = bv.v[w] - acc[w];
+        } else {
+#pragma unroll
+            for (int w = 0; w < V; w++) out.v[w] = acc[w];
+        }
+        out.store(y + t);
+    }
+}
+
+// Slice widths (entries of the slice's longest short row) and row lengths.
+__global__ void k_sell_width(int64_t n, const int64_t *__restrict__ ptr, int64_t nslice, int64_t *__restrict__ width,
+                             uint8_t *__restrict__ rlen) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nslice; s += (int64_t)gridDim.x * blockDim.x) {
+        int64_t w = 0;
+        for (int64_t i = 32 * s; i < 32 * s + 32 && i < n; i++) {
+            int64_t l = ptr[i + 1] - ptr[i];
+            if (l > kLongRow) { rlen[i] = kSellLong; continue; }
+            rlen[i] = (uint8_t)l;
+            w = l > w ? l : w;
+        }
+        width[s] = 32 * w;
+    }
+}
+
+template <class T>
+__global__ void k_sell_fill(int64_t n, const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                            const T *__restrict__ val, const uint8_t *__restrict__ rlen, const int64_t *__restrict__ sptr,
+                            int32_t *__restrict__ scol, T *__restrict__ sval) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int len = rlen[i];
+        if (len == kSellLong) continue;
+        const int64_t base = sptr[i >> 5] + (i & 31), p0 = ptr[i];
+        for (int j = 0; j < len; j++) {
+            scol[base + 32 * (int64_t)j] = col[p0 + j];
+            sval[base + 32 * (int64_t)j] = val[p0 + j];
+        }
+    }
+}
+
+// Long rows: one block per chunk of kLongChunk entries writes its partial
+// sums for every right-hand side; the block that finishes a row's last
+// chunk adds the row's partials in chunk order (deterministic) and writes y.
 template <class T>
 __global__ void __launch_bounds__(256) k_spmm_long(const int32_t *__restrict__ rows, const int32_t *__restrict__ crow,
-                                                   const int64_t *__restrict__ cbeg, const int64_t *__restrict__ ptr,
-                                                   const int32_t *__restrict__ col, const T *__restrict__ val,
-                                                   const T *__restrict__ x, int k, double *__restrict__ partial) {
+                                                   const int64_t *__restrict__ cbeg, const int64_t *__restrict__ rcp,
+                                                   const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                                                   const T *__restrict__ val, const T *__restrict__ x, int k,
+                                                   double *partial, int32_t *done, T *__restrict__ y,
+                                                   const T *__restrict__ b) {
     __shared__ double sm[256];
+    __shared__ int last;
     const int r = threadIdx.x, ty = threadIdx.y, ny = blockDim.y;
-    int64_t row = rows[crow[blockIdx.x]];
-    int64_t q0 = cbeg[blockIdx.x], q1 = min(q0 + (int64_t)kLongChunk, ptr[row + 1]);
-    T acc = 0;
-    if (r < k)
-        for (int64_t q = q0 + ty; q < q1; q += ny) acc += val[q] * x[(int64_t)col[q] * k + r];
-    sm[ty * blockDim.x + r] = (double)acc;
+    const int l = crow[blockIdx.x];
+    const int64_t row = rows[l];
+    const int64_t q0 = cbeg[blockIdx.x], q1 = min(q0 + (int64_t)kLongChunk, ptr[row + 1]);
+    T acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;
+    if (r < k) {
+        int64_t q = q0 + ty;
+        for (; q + 3 * ny < q1; q += 4 * ny) {
+            const int32_t c0 = col[q], c1 = col[q + ny], c2 = col[q + 2 * ny], c3 = col[q + 3 * ny];
+            const T v0 = val[q], v1 = val[q + ny], v2 = val[q + 2 * ny], v3 = val[q + 3 * ny];
+            const T x0 = x[(int64_t)c0 * k + r], x1 = x[(int64_t)c1 * k + r];
+            const T x2 = x[(int64_t)c2 * k + r], x3 = x[(int64_t)c3 * k + r];
+            acc0 += v0 * x0; acc1 += v1 * x1; acc2 += v2 * x2; acc3 += v3 * x3;
+        }
+        for (; q < q1; q += ny) acc0 += val[q] * x[(int64_t)col[q] * k + r];
+    }
+    sm[ty * blockDim.x + r] = (double)((acc0 + acc1) + (acc2 + acc3));
     __syncthreads();
     if (ty == 0 && r < k) {
         double s = 0;
         for (int t = 0; t < ny; t++) s += sm[t * blockDim.x + r];
         partial[(int64_t)blockIdx.x * kMaxRhs + r] = s;
     }
-}
-
-// Long rows, stage 2: ordered sum of each row's chunk partials.
-template <class T>
-__global__ void k_spmm_long_finish(int64_t nl, const int32_t *rows, const int64_t *rcp, const double *partial, int k,
-                                   T *y, const T *b) {
-    int64_t l = blockIdx.x;
-    int r = threadIdx.x;
-    if (l >= nl || r >= k) return;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0 && ty == 0) {
+        const int nch = (int)(rcp[l + 1] - rcp[l]);
+        last = atomicAdd(&done[l], 1) == nch - 1;
+        if (last) done[l] = 0;
+    }
+    __syncthreads();
+    if (!last || ty != 0 || r >= k) return;
+    __threadfence();
     double s = 0;
-    for (int64_t c = rcp[l]; c < rcp[l + 1]; c++) s += partial[c * kMaxRhs + r];
-    int64_t o = (int64_t)rows[l] * k + r;
+    for (int64_t c = rcp[l]; c < rcp[l + 1]; c++) s += __ldcg(partial + c * kMaxRhs + r);
+    const int64_t o = row * k + r;
     y[o] = b ? (T)((double)b[o] - s) : (T)s;
 }
 
@@ -104,6 +246,7 @@ struct KernelProfile {
     size_t used = 0;
     double bytes = 0;
     int64_t launches = 0;
+    std::vector<double> launch_bytes;   // per launch, for the size buckets
 };
 static KernelProfile g_prof;
 
@@ -116,21 +259,70 @@ static void prof_event(cudaStream_t s) {
     cudaEventRecord(g_prof.ev[g_prof.used++], s);
 }
 
+// Right-hand sides per thread of the sliced-ELL kernel for k columns: one
+// 16-byte load where k allows, so the threads of a row cover whole sectors.
+template <class T>
+static int sell_vec(int k) {
+    int v = (int)(16 / sizeof(T));
+    while (v > 1 && k % v) v >>= 1;
+    return v;
+}
+
+template <class T, int V>
+static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cudaStream_t s) {
+    // one block per 256 / tpr rows, never grid-strided: blocks retire in row
+    // order, so the rows in flight form one window and the x rows a stencil
+    // shares (z-neighbours one layer apart) are still in L2 when reused
+    const int tpr = k / V;
+    const int rows = 256 / tpr;
+    int64_t g = (A.n + rows - 1) / rows;
+    if (g > 0x7fffffffLL) g = 0x7fffffffLL;
+    if (g < 1) g = 1;
+    (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_sell<f64>" : "k_spmm_sell<f32>", s),
+     k_spmm_sell<T, V><<<(unsigned)g, dim3(tpr, rows), 0, s>>>(A.n, A.sptr, A.scol, A.sval, A.rlen, x, y, k, b),
+     g2p::kend(s));
+}
+
 template <class T>
 void spmm_b(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, const T *b, cudaStream_t s) {
     bool prof = g_prof.on && g_prof.used + 2 <= (size_t)1 << 20;
+    const bool sell = A.sptr != nullptr;
     if (prof) {
         prof_event(s);
-        g_prof.bytes += (double)A.nnz * (sizeof(T) + 4) + (double)(A.n + 1) * 8 +
-                        (double)A.n * k * sizeof(T) * (b ? 3 : 2);
+        if (sell)
+            g_prof.bytes += (double)A.short_nnz * (sizeof(T) + 4) + (double)A.n + (double)((A.n + 31) / 32) * 8 +
+                            (double)A.n * k * sizeof(T) * (b ? 3 : 2);
+        else
+            g_prof.bytes += (double)A.nnz * (sizeof(T) + 4) + (double)(A.n + 1) * 8 +
+                            (double)A.n * k * sizeof(T) * (b ? 3 : 2);
         g_prof.launches++;
+        const double lb = sell ? (double)A.short_nnz * (sizeof(T) + 4) + (double)A.n + (double)((A.n + 31) / 32) * 8 +
+                                     (double)A.n * k * sizeof(T) * (b ? 3 : 2)
+                               : (double)A.nnz * (sizeof(T) + 4) + (double)(A.n + 1) * 8 +
+                                     (double)A.n * k * sizeof(T) * (b ? 3 : 2);
+        g_prof.launch_bytes.push_back(lb);
     }
     dim3 blk = row_block(k);
-    (g2p::kbegin("k_spmm", s), k_spmm<T><<<row_grid(A.n, k, 152LL * 48), blk, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y, k, b), g2p::kend(s));
+    if (sell) {
+        // vector width only where every x row, y row and b row is aligned to it
+        int v = sell_vec<T>(k);
+        auto aligned = [&](const void *p) {
+            size_t w = (size_t)v * sizeof(T) >= 16 ? 16 : (size_t)v * sizeof(T);
+            return p == nullptr || ((uintptr_t)p % w) == 0;
+        };
+        while (v > 1 && !(aligned(x) && aligned(y) && aligned(b))) v >>= 1;
+        switch (v) {
+            case 8: launch_sell<T, 8>(A, x, y, k, b, s); break;
+            case 4: launch_sell<T, 4>(A, x, y, k, b, s); break;
+            case 2: launch_sell<T, 2>(A, x, y, k, b, s); break;
+            default: launch_sell<T, 1>(A, x, y, k, b, s); break;
+        }
+    } else {
+        (g2p::kbegin("k_spmm", s), k_spmm<T><<<row_grid(A.n, k, 152LL * 48), blk, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y, k, b), g2p::kend(s));
+    }
     if (prof) prof_event(s);
     if (lr.n > 0) {
-        (g2p::kbegin("k_spmm_long", s), k_spmm_long<T><<<(unsigned)lr.nchunk, blk, 0, s>>>(lr.rows, lr.crow, lr.cbeg, A.ptr, A.col, A.val, x, k, lr.partial), g2p::kend(s));
-        (g2p::kbegin("k_spmm_long_finish", s), k_spmm_long_finish<T><<<(unsigned)lr.n, pow2_ge(k), 0, s>>>(lr.n, lr.rows, lr.rcp, lr.partial, k, y, b), g2p::kend(s));
+        (g2p::kbegin("k_spmm_long", s), k_spmm_long<T><<<(unsigned)lr.nchunk, blk, 0, s>>>(lr.rows, lr.crow, lr.cbeg, lr.rcp, A.ptr, A.col, A.val, x, k, lr.partial, lr.done, y, b), g2p::kend(s));
     }
 }
 
@@ -198,6 +390,8 @@ g2p_status find_long_rows(const Csr<T> &A, LongRows &lr, cudaStream_t s) {
         G2P_TRY(dalloc(&lr.cbeg, lr.nchunk, s));
         G2P_TRY(dalloc(&lr.rcp, nl + 1, s));
         G2P_TRY(dalloc(&lr.partial, lr.nchunk * kMaxRhs, s));
+        G2P_TRY(dalloc(&lr.done, nl, s));
+        G2P_CUDA(cudaMemsetAsync(lr.done, 0, sizeof(int32_t) * nl, s));
         G2P_CUDA(cudaMemcpyAsync(lr.crow, crow.data(), sizeof(int32_t) * lr.nchunk, cudaMemcpyHostToDevice, s));
         G2P_CUDA(cudaMemcpyAsync(lr.cbeg, cbeg.data(), sizeof(int64_t) * lr.nchunk, cudaMemcpyHostToDevice, s));
         G2P_CUDA(cudaMemcpyAsync(lr.rcp, rcp.data(), sizeof(int64_t) * (nl + 1), cudaMemcpyHostToDevice, s));
@@ -216,12 +410,56 @@ g2p_status copy_long_rows(const LongRows &src, LongRows &dst, cudaStream_t s) {
     G2P_TRY(dalloc(&dst.rows, src.n, s)); G2P_TRY(dalloc(&dst.crow, src.nchunk, s));
     G2P_TRY(dalloc(&dst.cbeg, src.nchunk, s)); G2P_TRY(dalloc(&dst.rcp, src.n + 1, s));
     G2P_TRY(dalloc(&dst.partial, src.nchunk * kMaxRhs, s));
+    G2P_TRY(dalloc(&dst.done, src.n, s));
+    G2P_CUDA(cudaMemsetAsync(dst.done, 0, sizeof(int32_t) * src.n, s));
     G2P_CUDA(cudaMemcpyAsync(dst.rows, src.rows, sizeof(int32_t) * src.n, cudaMemcpyDeviceToDevice, s));
     G2P_CUDA(cudaMemcpyAsync(dst.crow, src.crow, sizeof(int32_t) * src.nchunk, cudaMemcpyDeviceToDevice, s));
     G2P_CUDA(cudaMemcpyAsync(dst.cbeg, src.cbeg, sizeof(int64_t) * src.nchunk, cudaMemcpyDeviceToDevice, s));
     G2P_CUDA(cudaMemcpyAsync(dst.rcp, src.rcp, sizeof(int64_t) * (src.n + 1), cudaMemcpyDeviceToDevice, s));
     return G2P_OK;
 }
+
+// Sliced-ELL copy of A's short rows (kept beside the CSR).
+template <class T>
+g2p_status sell_build(Csr<T> &A, cudaStream_t s) {
+    A.release_sell(s);
+    const int64_t n = A.n, nslice = (n + 31) / 32;
+    int64_t *width, *work;
+    G2P_TRY(dalloc(&width, nslice + 1, s));
+    G2P_TRY(dalloc(&work, scan_work_size(nslice + 1) + 4, s));
+    G2P_TRY(dalloc(&A.rlen, n, s));
+    G2P_TRY(dalloc(&A.sptr, nslice + 1, s));
+    (g2p::kbegin("k_sell_width", s), k_sell_width<<<grid_for(nslice), kThreads, 0, s>>>(n, A.ptr, nslice, width, A.rlen), g2p::kend(s));
+    const int64_t *wp = width;
+    auto op = [wp, nslice] __device__(int64_t i) -> int64_t { return i < nslice ? wp[i] : 0; };
+    G2P_TRY(exclusive_scan(op, nslice + 1, A.sptr, work, s));
+    int64_t slots = 0;
+    G2P_CUDA(cudaMemcpyAsync(&slots, A.sptr + nslice, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    dfree(width, s); dfree(work, s);
+    A.sell_slots = slots;
+    G2P_TRY(dalloc(&A.scol, slots, s));
+    G2P_TRY(dalloc(&A.sval, slots, s));
+    (g2p::kbegin("k_sell_fill", s), k_sell_fill<T><<<grid_for(n), kThreads, 0, s>>>(n, A.ptr, A.col, A.val, A.rlen, A.sptr, A.scol, A.sval), g2p::kend(s));
+    // entries of the long rows are not in the copy
+    int64_t *lp, *lw;
+    G2P_TRY(dalloc(&lp, n + 1, s));
+    G2P_TRY(dalloc(&lw, scan_work_size(n + 1) + 4, s));
+    const int64_t *pp = A.ptr;
+    auto lop = [pp, n] __device__(int64_t i) -> int64_t {
+        if (i >= n) return 0;
+        int64_t l = pp[i + 1] - pp[i];
+        return l > kLongRow ? 0 : l;
+    };
+    G2P_TRY(exclusive_scan(lop, n + 1, lp, lw, s));
+    G2P_CUDA(cudaMemcpyAsync(&A.short_nnz, lp + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    dfree(lp, s); dfree(lw, s);
+    G2P_CUDA(cudaGetLastError());
+    return G2P_OK;
+}
+template g2p_status sell_build<double>(Csr<double> &, cudaStream_t);
+template g2p_status sell_build<float>(Csr<float> &, cudaStream_t);
 
 // --------------------------------------------------------------- reductions
 // Deterministic per-column sums of squares: block partials, then an ordered
@@ -1407,6 +1645,7 @@ extern "C" void g2p_profile_begin(void) {
     g2p::g_prof.used = 0;
     g2p::g_prof.bytes = 0;
     g2p::g_prof.launches = 0;
+    g2p::g_prof.launch_bytes.clear();
 }
 
 extern "C" g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, int64_t *launches) {
@@ -1415,11 +1654,28 @@ extern "C" g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, i
     kprof_set(false);
     G2P_TRY(kprof_collect());
     double ms = 0;
+    // size buckets of the SpMM launches by algorithmic bytes
+    const double edges[] = {0, 1e6, 16e6, 128e6, 1e30};
+    double bms[4] = {0, 0, 0, 0}, bby[4] = {0, 0, 0, 0};
+    int64_t bn[4] = {0, 0, 0, 0};
     for (size_t i = 0; i + 1 < g_prof.used; i += 2) {
         float t = 0;
         G2P_CUDA(cudaEventElapsedTime(&t, g_prof.ev[i], g_prof.ev[i + 1]));
         ms += t;
+        const size_t li = i / 2;
+        if (li < g_prof.launch_bytes.size()) {
+            const double lb = g_prof.launch_bytes[li];
+            for (int q = 0; q < 4; q++)
+                if (lb >= edges[q] && lb < edges[q + 1]) { bms[q] += t; bby[q] += lb; bn[q]++; }
+        }
     }
+    const char *bname[4] = {"<1MB", "1-16MB", "16-128MB", ">=128MB"};
+    for (int q = 0; q < 4; q++)
+        if (bn[q]) {
+            char nm[96];
+            snprintf(nm, sizeof nm, "spmm[%s]@%.0fGB/s", bname[q], bms[q] > 0 ? bby[q] / (bms[q] * 1e6) : 0.0);
+            kprof_add_total(nm, bn[q], bms[q]);
+        }
     if (kernel_ms) *kernel_ms = ms;
     if (kernel_bytes) *kernel_bytes = g_prof.bytes;
     if (launches) *launches = g_prof.launches;

@@ -6,7 +6,7 @@
 namespace g2p {
 
 constexpr int kLongRow = 64;
-constexpr int kLongChunk = 4096;    // entries per block in the long-row kernel
+constexpr int kLongChunk = 2048;    // entries per block in the long-row kernel
 constexpr int kMaxRhs = 256;
 
 // Rows longer than kLongRow (the lumped conductor potentials of Ad and
@@ -19,8 +19,9 @@ struct LongRows {
     int64_t *rcp = nullptr;      // [n+1] chunks of each long row
     int64_t nchunk = 0;
     double *partial = nullptr;   // [nchunk * kMaxRhs]
+    int32_t *done = nullptr;     // [n] chunks finished per row; zero between launches
     void release(cudaStream_t s) {
-        dfree(rows, s); dfree(crow, s); dfree(cbeg, s); dfree(rcp, s); dfree(partial, s);
+        dfree(rows, s); dfree(crow, s); dfree(cbeg, s); dfree(rcp, s); dfree(partial, s); dfree(done, s);
         n = nchunk = 0;
     }
 };
@@ -107,6 +108,8 @@ void colnorms(const T *x, int64_t n, int k, double *partial, double *out, cudaSt
 template <class T>
 g2p_status find_long_rows(const Csr<T> &A, LongRows &lr, cudaStream_t s);
 g2p_status copy_long_rows(const LongRows &src, LongRows &dst, cudaStream_t s);
+template <class T>
+g2p_status sell_build(Csr<T> &A, cudaStream_t s);
 
 }  // namespace g2p
 
