@@ -156,13 +156,13 @@ def run_gb300(args):
     z =torch.zeros(2 * d.nfreq * d.num_ports * d.num_ports, dtype=torch.float64).pin_memory()
     stats = _lib.ExtractStats()
 
-    def step(T):
+    def step(T, prm=None):
         desc = desc_struct(d, T, _lib)
         h = C.c_void_p()
         _lib.check(L.g2p_mesh_create(C.byref(desc), C.byref(h)))
         n = C.c_int64()
         _lib.check(L.g2p_generate_stiff(h, C.byref(n)))
-        _lib.check(L.g2p_para_generator(h, C.byref(params), C.c_void_p(z.data_ptr()), C.byref(stats)))
+        _lib.check(L.g2p_para_generator(h, C.byref(prm or params), C.c_void_p(z.data_ptr()), C.byref(stats)))
         L.g2p_mesh_destroy(h)
 
     def barrier():
@@ -170,22 +170,27 @@ def run_gb300(args):
         if world > 1:
             torch.distributed.barrier()
 
-    def timed(T, k, profile=False):
+    def timed(T, k, profile=False, prm=None, per_step=None):
         barrier()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(k + 1)]
         n0 = L.g2p_launch_count()
         if profile:
             L.g2p_profile_begin()
-        e0.record()
-        for _ in range(k):
-            step(T)
-        e1.record()
+        ev[0].record()
+        for i in range(k):
+            step(T, prm)
+            ev[i + 1].record()
         barrier()
+        e0, e1 = ev[0], ev[k]
+        if per_step is not None:
+            per_step.extend(ev[i].elapsed_time(ev[i + 1]) for i in range(k))
         kern = None
         if profile:
             ms, by, nl = C.c_double(), C.c_double(), C.c_int64()
             _lib.check(L.g2p_profile_end(C.byref(ms), C.byref(by), C.byref(nl)))
-            kern = (ms.value, by.value, nl.value)
+            bms, bby, bn = (C.c_double * 8)(), (C.c_double * 8)(), (C.c_int64 * 8)()
+            L.g2p_profile_buckets(bms, bby, bn)
+            kern = (ms.value, by.value, nl.value, list(bms), list(bby), list(bn))
         el = e0.elapsed_time(e1) / k
         if world > 1:
             t = torch.tensor([el], device="cuda")
@@ -202,9 +207,21 @@ def run_gb300(args):
         step(dev)
     clocks = Clocks(local)
     clocks.start()
-    ms, launches, kern = timed(dev, args.steps, profile=True)
+    step_ms = []
+    ms, launches, kern = timed(dev, args.steps, profile=True, per_step=step_ms)
     clk = clocks.stop()
     ms_e2e, _, _ = timed(pin, max(1, min(args.steps, 3)))
+    # accuracy of this run's Z against the plain FP64 GPU method, and that
+    # method's own speed (FP64 throughout, one port at a time), untimed above
+    z_run = z.numpy().copy()
+    p64 = default_params(precision="fp64", batch=0, rtol=RTOL[args.config])
+    step(dev, p64)
+    z64 = z.numpy().copy()
+    zr = z_run.reshape(-1, 2)
+    zf = z64.reshape(-1, 2)
+    zc, z64c = zr[:, 0] + 1j * zr[:, 1], zf[:, 0] + 1j * zf[:, 1]
+    z_err = float(np.max(np.abs(zc - z64c)) / max(np.max(np.abs(z64c)), 1e-300))
+    fp64_ms, _, _ = timed(dev, 1, prm=p64) if args.precision == "mixed" or args.batch else (ms, 0, None)
     units = d.num_ports * d.nfreq
     value = world * units / (ms / 1e3)
     e2e = world * units / (ms_e2e / 1e3)
@@ -215,8 +232,13 @@ def run_gb300(args):
     if os.path.exists(pk):
         peaks = json.load(open(pk))
     peak_gbs = peaks.get("hbm_gbs", 6800.0)
-    k_ms, k_bytes, k_n = kern
-    achieved = (k_bytes / (k_ms / 1e3)) / 1e9 if k_ms > 0 else None
+    k_ms, k_bytes, k_n, b_ms, b_bytes, b_n = kern
+    achieved_all = (k_bytes / (k_ms / 1e3)) / 1e9 if k_ms > 0 else None
+    # the fine-level operator's launches (>= 128 MB of algorithmic bytes each)
+    # in the working precision of the preconditioned solves
+    fi = 3 if args.precision == "mixed" else 7
+    f_ms, f_bytes, f_n = b_ms[fi], b_bytes[fi], b_n[fi]
+    achieved = (f_bytes / (f_ms / 1e3)) / 1e9 if f_ms > 0 else None
     traffic = None
     tf = os.path.join(ROOT, "profiles", "spmm_traffic.json")
     if os.path.exists(tf):
@@ -224,6 +246,8 @@ def run_gb300(args):
             traffic = json.load(open(tf)).get(f"{args.config}_{args.precision}_bytes_per_launch")
         except Exception:
             traffic = None
+    srt = sorted(step_ms)
+    pct = lambda q: srt[min(len(srt) - 1, int(round(q * (len(srt) - 1))))] if srt else None
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -242,12 +266,28 @@ def run_gb300(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": ms_e2e},
         "gpu_launches": int(launches),
+        "job_ms": {"p50": pct(0.5), "p99": pct(0.99), "per_step": step_ms},
+        "accuracy": {"z_rel_err_vs_fp64_gpu": z_err, "bound": 1e-6,
+                     "note": "max |Z - Z_fp64| / max |Z_fp64| over all entries and frequencies"},
+        "fp64_plain": {"value": world * units / (fp64_ms / 1e3), "unit": UNIT, "ms_per_step": fp64_ms,
+                       "what": "same job, FP64 AMG-FGMRES, one port at a time (batch 0)",
+                       "speedup_of_this_run": (world * units / (ms / 1e3)) / (world * units / (fp64_ms / 1e3))},
         "clocks": clk,
-        "roofline": {"bound": "hbm", "kernel": "k_spmm (sparse matrix x RHS block)",
+        "roofline": {"bound": "hbm",
+                     "kernel": ("k_spmm_sell<f32>" if args.precision == "mixed" else "k_spmm_sell<f64>") +
+                               ": sliced-ELL sparse matrix x block of right-hand sides, fine-level Ad "
+                               "(launches of >= 128 MB algorithmic bytes)",
                      "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
                      "frac": (achieved / peak_gbs) if achieved else None, "traffic": traffic,
-                     "launches": int(k_n), "avg_launch_us": 1e3 * k_ms / max(k_n, 1),
-                     "algorithmic_bytes_per_launch": k_bytes / max(k_n, 1),
+                     "launches": int(f_n), "avg_launch_us": 1e3 * f_ms / max(f_n, 1),
+                     "algorithmic_bytes_per_launch": f_bytes / max(f_n, 1),
+                     "all_levels": {"achieved": achieved_all, "launches": int(k_n),
+                                    "avg_launch_us": 1e3 * k_ms / max(k_n, 1),
+                                    "frac": (achieved_all / peak_gbs) if achieved_all else None},
+                     "buckets": {f"{p}{nm}": [b_n[o + q], b_ms[o + q], b_bytes[o + q]]
+                                 for o, p in ((0, "f32 "), (4, "f64 "))
+                                 for q, nm in enumerate(("<1MB", "1-16MB", "16-128MB", ">=128MB")) if b_n[o + q]},
+                     "bucket_fields": "launches, ms, algorithmic bytes",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s"},
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -257,44 +297,74 @@ def run_gb300(args):
     return out, rank
 
 
-def cpu_baseline(d, args, rtol, steps=1):
-    """The C restatement of the reference's path (oracle/), single-threaded,
-    on a bounded sample: assembly once, then the first `cpu_sample_ports`
-    ports with the reference's per-solve AMG setup; extrapolated to the job."""
+def cpu_sample(d, rtol, O=None, fixed=None):
+    """One bounded sample of the job on the host with the oracle/ C
+    restatement of the reference's path (single thread): generateStiff and
+    the V0/Ad/Ac assembly (or their times from `fixed`), then port 0's first
+    Ad solve and its Ac solve, each with its own AMG setup as hypreSolve
+    does.  The job time is extrapolated as S + assembly + ports x (2 Ad + Ac):
+    a port's two Ad solves share the matrix."""
     from oracle.harness import COracle
-    O = COracle()
-    o = O.default_opts(rtol=rtol, maxit=400, restart=30, reuse_setup=0)
+    O = O or COracle()
     t0 = time.perf_counter()
-    _, st = O.para_generator(d, o, max_ports=args.cpu_sample_ports)
+    if fixed is None:
+        t = time.perf_counter()
+        O.stiffness(d)
+        t_s = time.perf_counter() - t
+    else:
+        t_s = fixed["t_stiff"]
+    o = O.default_opts(rtol=rtol, maxit=400, restart=30, reuse_setup=0, stop_after_solves=2)
+    _, st = O.para_generator(d, o, max_ports=1)
+    t_asm = st.t_assembly if fixed is None else fixed["t_assembly"]
+    t_ad, t_ac = st.t_each[0], st.t_each[1]
     wall = time.perf_counter() - t0
-    np_ = max(1, min(args.cpu_sample_ports, d.num_ports))
-    per_port = (st.t_setup + st.t_solve) / np_
-    job = st.t_assembly + per_port * d.num_ports
+    job = t_s + t_asm + d.num_ports * (2 * t_ad + t_ac)
     return {"value": d.num_ports * d.nfreq / job, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"oracle/ C restatement on the host: assembly + {np_} of {d.num_ports} ports "
-                      f"(3 solves each, AMG setup per solve as hypreSolve does) took {wall:.1f} s; "
-                      f"job time extrapolated as assembly {st.t_assembly:.2f} s + {d.num_ports} x {per_port:.2f} s",
-            "seconds": wall}
+            "sample": f"oracle/ C restatement, 1 host thread: generateStiff {t_s:.2f} s, V0/Ad/Ac assembly "
+                      f"{t_asm:.2f} s, port 0 Ad solve {t_ad:.2f} s and Ac solve {t_ac:.2f} s (AMG setup per "
+                      f"solve); job = S + assembly + {d.num_ports} x (2 Ad + Ac) = {job:.1f} s",
+            "seconds": wall, "t_stiff": t_s, "t_assembly": st.t_assembly, "t_ad": t_ad, "t_ac": t_ac,
+            "job_seconds": job}
+
+
+def cpu_baseline(d, args, rtol):
+    return cpu_sample(d, rtol)
 
 
 def run_reference(args):
+    """The reference's CPU path, restated in oracle/ (the reference's own
+    build needs MKL, HYPRE and MPI, absent here), timed on the host.  Warm-up
+    steps run the V0/Ad/Ac assembly alone; the first also times generateStiff;
+    each timed step is one bounded sample (port 0's Ad and Ac solves)."""
     rank, world, _ = dist_info()
     if rank != 0:
         return None, rank
     from gds2para_gb300 import layout
+    from oracle.harness import COracle
     d = layout.build(layout.config(args.config))
-    vals = []
-    cb = None
-    for i in range(max(args.warmup, 0) + args.steps):
-        cb = cpu_baseline(d, args, RTOL[args.config])
-        if i >= args.warmup:
-            vals.append(cb["value"])
+    O = COracle()
+    rtol = RTOL[args.config]
+    t = time.perf_counter()
+    O.stiffness(d)
+    fixed = {"t_stiff": time.perf_counter() - t}
+    for _ in range(max(args.warmup, 0)):
+        t = time.perf_counter()
+        O.v0_and_laplacians(d)
+        fixed["t_assembly"] = time.perf_counter() - t
+    if "t_assembly" not in fixed:
+        t = time.perf_counter()
+        O.v0_and_laplacians(d)
+        fixed["t_assembly"] = time.perf_counter() - t
+    vals, cb = [], None
+    for _ in range(args.steps):
+        cb = cpu_sample(d, rtol, O, fixed)
+        vals.append(cb["value"])
     v = statistics.median(vals)
     cb["value"] = v
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * d.num_ports * d.nfreq / v, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded layout generator)",
-           "config": {"workload": WORKLOAD[args.config], "config": args.config, "rtol": RTOL[args.config],
+           "config": {"workload": WORKLOAD[args.config], "config": args.config, "rtol": rtol,
                       "parallelism": "1 host thread"},
            "cpu_baseline": cb,
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

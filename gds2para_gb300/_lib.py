@@ -18,7 +18,7 @@ EXPORTS = [
     "g2p_assemble_v0", "g2p_export_v0", "g2p_export_laplacian",
     "g2p_hypre_solve", "g2p_solver_create", "g2p_solver_solve", "g2p_solver_destroy",
     "g2p_para_generator", "g2p_launch_count", "g2p_profile_begin", "g2p_profile_end", "g2p_profile_report",
-    "g2p_map_edge_noalloc",
+    "g2p_map_edge_noalloc", "g2p_profile_buckets",
 ]
 
 STATUS = {0: "G2P_OK", 1: "G2P_ERR_INVALID", 2: "G2P_ERR_CUDA", 3: "G2P_ERR_NOMEM", 4: "G2P_ERR_NOT_CONVERGED",
@@ -113,10 +113,12 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_profile_end.argtypes = [C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)]
     L.g2p_profile_report.restype = C.c_int64
     L.g2p_profile_report.argtypes = [C.c_char_p, i64]
+    L.g2p_profile_buckets.restype = None
+    L.g2p_profile_buckets.argtypes = [C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)]
     L.g2p_map_edge_noalloc.argtypes = [i64, i64, i64, vp, vp, i64, vp, vp, vp]
     for name in EXPORTS:
         if name not in ("g2p_last_error", "g2p_version", "g2p_default_params", "g2p_launch_count",
-                        "g2p_profile_begin", "g2p_profile_report"):
+                        "g2p_profile_begin", "g2p_profile_report", "g2p_profile_buckets"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L

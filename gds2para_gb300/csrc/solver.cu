@@ -229,12 +229,58 @@ __global__ void __launch_bounds__(256) k_spmm_long(const int32_t *__restrict__ r
         if (last) done[l] = 0;
     }
     __syncthreads();
-    if (!last || ty != 0 || r >= k) return;
+    if (!last) return;
     __threadfence();
+    // the row's chunk partials: thread ty adds chunks ty, ty + ny, ... in
+    // order, then thread 0 of each column adds the ny sums in order
     double s = 0;
-    for (int64_t c = rcp[l]; c < rcp[l + 1]; c++) s += __ldcg(partial + c * kMaxRhs + r);
+    if (r < k)
+        for (int64_t c = rcp[l] + ty; c < rcp[l + 1]; c += ny) s += __ldcg(partial + c * kMaxRhs + r);
+    sm[ty * blockDim.x + r] = s;
+    __syncthreads();
+    if (ty != 0 || r >= k) return;
+    double t = 0;
+    for (int q = 0; q < ny; q++) t += sm[q * blockDim.x + r];
     const int64_t o = row * k + r;
-    y[o] = b ? (T)((double)b[o] - s) : (T)s;
+    y[o] = b ? (T)((double)b[o] - t) : (T)t;
+}
+
+// Rows of kLongRow < length <= kHugeRow: one warp per row.  Lane = (entry
+// lane e, right-hand side r): kx = min(32, pow2 >= k) lanes cover the
+// right-hand sides (looping when k > 32), 32 / kx lanes stride over the
+// entries; a fixed shuffle tree adds the entry lanes.
+template <class T>
+__global__ void __launch_bounds__(256) k_spmm_mid(int64_t nmid, const int32_t *__restrict__ mid,
+                                                  const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                                                  const T *__restrict__ val, const T *__restrict__ x, int k, int kx,
+                                                  T *__restrict__ y, const T *__restrict__ b) {
+    const int lane = threadIdx.x & 31;
+    const int r = lane % kx, e = lane / kx, ey = 32 / kx;
+    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (w >= nmid) return;
+    const int64_t row = mid[w];
+    const int64_t q0 = ptr[row], q1 = ptr[row + 1];
+    for (int r0 = 0; r0 < k; r0 += kx) {
+        const int rr = r0 + r;
+        const bool on = rr < k;
+        T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        if (on) {
+            int64_t q = q0 + e;
+            for (; q + 3 * ey < q1; q += 4 * ey) {
+                const int32_t c0 = col[q], c1 = col[q + ey], c2 = col[q + 2 * ey], c3 = col[q + 3 * ey];
+                const T v0 = val[q], v1 = val[q + ey], v2 = val[q + 2 * ey], v3 = val[q + 3 * ey];
+                a0 += v0 * x[(int64_t)c0 * k + rr]; a1 += v1 * x[(int64_t)c1 * k + rr];
+                a2 += v2 * x[(int64_t)c2 * k + rr]; a3 += v3 * x[(int64_t)c3 * k + rr];
+            }
+            for (; q < q1; q += ey) a0 += val[q] * x[(int64_t)col[q] * k + rr];
+        }
+        T acc = (a0 + a1) + (a2 + a3);
+        for (int off = kx; off < 32; off <<= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+        if (e == 0 && on) {
+            const int64_t o = row * k + rr;
+            y[o] = b ? b[o] - acc : acc;
+        }
+    }
 }
 
 // Event timing of the sparse matrix-multi-vector kernel (the dominant
@@ -247,8 +293,11 @@ struct KernelProfile {
     double bytes = 0;
     int64_t launches = 0;
     std::vector<double> launch_bytes;   // per launch, for the size buckets
+    std::vector<char> launch_f64;       // per launch: FP64 operator
 };
 static KernelProfile g_prof;
+static double g_bucket_ms[8], g_bucket_bytes[8];
+static int64_t g_bucket_n[8];
 
 static void prof_event(cudaStream_t s) {
     if (g_prof.used == g_prof.ev.size()) {
@@ -301,6 +350,7 @@ void spmm_b(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, const 
                                : (double)A.nnz * (sizeof(T) + 4) + (double)(A.n + 1) * 8 +
                                      (double)A.n * k * sizeof(T) * (b ? 3 : 2);
         g_prof.launch_bytes.push_back(lb);
+        g_prof.launch_f64.push_back(sizeof(T) == 8);
     }
     dim3 blk = row_block(k);
     if (sell) {
@@ -321,8 +371,16 @@ void spmm_b(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, const 
         (g2p::kbegin("k_spmm", s), k_spmm<T><<<row_grid(A.n, k, 152LL * 48), blk, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y, k, b), g2p::kend(s));
     }
     if (prof) prof_event(s);
-    if (lr.n > 0) {
-        (g2p::kbegin("k_spmm_long", s), k_spmm_long<T><<<(unsigned)lr.nchunk, blk, 0, s>>>(lr.rows, lr.crow, lr.cbeg, lr.rcp, A.ptr, A.col, A.val, x, k, lr.partial, lr.done, y, b), g2p::kend(s));
+    if (lr.nmid > 0) {
+        const int kx = k >= 32 ? 32 : pow2_ge(k);
+        const int64_t blocks = (lr.nmid + 7) / 8;
+        (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_mid<f64>" : "k_spmm_mid<f32>", s),
+         k_spmm_mid<T><<<(unsigned)blocks, 256, 0, s>>>(lr.nmid, lr.mid, A.ptr, A.col, A.val, x, k, kx, y, b), g2p::kend(s));
+    }
+    if (lr.nchunk > 0) {
+        (g2p::kbegin(A.n >= (1 << 20) ? (sizeof(T) == 8 ? "k_spmm_long<f64,fine>" : "k_spmm_long<f32,fine>")
+                                      : (sizeof(T) == 8 ? "k_spmm_long<f64,coarse>" : "k_spmm_long<f32,coarse>"), s),
+         k_spmm_long<T><<<(unsigned)lr.nchunk, blk, 0, s>>>(lr.rows, lr.crow, lr.cbeg, lr.rcp, A.ptr, A.col, A.val, x, k, lr.partial, lr.done, y, b), g2p::kend(s));
     }
 }
 
@@ -378,14 +436,26 @@ g2p_status find_long_rows(const Csr<T> &A, LongRows &lr, cudaStream_t s) {
         G2P_CUDA(cudaMemcpyAsync(be.data(), ext, sizeof(int64_t) * 2 * nl, cudaMemcpyDeviceToHost, s));
         G2P_CUDA(cudaStreamSynchronize(s));
         dfree(ext, s);
-        std::vector<int32_t> crow;
+        std::vector<int32_t> crow, mid;
         std::vector<int64_t> cbeg, rcp(nl + 1, 0);
+        std::vector<int32_t> rows(nl);
+        G2P_CUDA(cudaMemcpyAsync(rows.data(), lr.rows, sizeof(int32_t) * nl, cudaMemcpyDeviceToHost, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
         for (int64_t l = 0; l < nl; l++) {
-            for (int64_t q = be[2 * l]; q < be[2 * l + 1]; q += kLongChunk) { crow.push_back((int32_t)l); cbeg.push_back(q); }
+            if (be[2 * l + 1] - be[2 * l] <= kHugeRow) mid.push_back(rows[l]);
+            else
+                for (int64_t q = be[2 * l]; q < be[2 * l + 1]; q += kLongChunk) { crow.push_back((int32_t)l); cbeg.push_back(q); }
             rcp[l + 1] = (int64_t)crow.size();
         }
         lr.n = nl;
         lr.nchunk = (int64_t)crow.size();
+        lr.nmid = (int64_t)mid.size();
+        if (const char *e = getenv("G2P_DEBUG"))
+            if (atoi(e) >= 2)
+                fprintf(stderr, "[g2p long rows] n=%lld nnz=%lld long=%lld mid=%lld chunks=%lld\n", (long long)n,
+                        (long long)A.nnz, (long long)nl, (long long)lr.nmid, (long long)lr.nchunk);
+        G2P_TRY(dalloc(&lr.mid, lr.nmid, s));
+        if (lr.nmid) G2P_CUDA(cudaMemcpyAsync(lr.mid, mid.data(), sizeof(int32_t) * lr.nmid, cudaMemcpyHostToDevice, s));
         G2P_TRY(dalloc(&lr.crow, lr.nchunk, s));
         G2P_TRY(dalloc(&lr.cbeg, lr.nchunk, s));
         G2P_TRY(dalloc(&lr.rcp, nl + 1, s));
@@ -411,6 +481,9 @@ g2p_status copy_long_rows(const LongRows &src, LongRows &dst, cudaStream_t s) {
     G2P_TRY(dalloc(&dst.cbeg, src.nchunk, s)); G2P_TRY(dalloc(&dst.rcp, src.n + 1, s));
     G2P_TRY(dalloc(&dst.partial, src.nchunk * kMaxRhs, s));
     G2P_TRY(dalloc(&dst.done, src.n, s));
+    dst.nmid = src.nmid;
+    G2P_TRY(dalloc(&dst.mid, src.nmid, s));
+    if (src.nmid) G2P_CUDA(cudaMemcpyAsync(dst.mid, src.mid, sizeof(int32_t) * src.nmid, cudaMemcpyDeviceToDevice, s));
     G2P_CUDA(cudaMemsetAsync(dst.done, 0, sizeof(int32_t) * src.n, s));
     G2P_CUDA(cudaMemcpyAsync(dst.rows, src.rows, sizeof(int32_t) * src.n, cudaMemcpyDeviceToDevice, s));
     G2P_CUDA(cudaMemcpyAsync(dst.crow, src.crow, sizeof(int32_t) * src.nchunk, cudaMemcpyDeviceToDevice, s));
@@ -1646,6 +1719,7 @@ extern "C" void g2p_profile_begin(void) {
     g2p::g_prof.bytes = 0;
     g2p::g_prof.launches = 0;
     g2p::g_prof.launch_bytes.clear();
+    g2p::g_prof.launch_f64.clear();
 }
 
 extern "C" g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, int64_t *launches) {
@@ -1656,8 +1730,8 @@ extern "C" g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, i
     double ms = 0;
     // size buckets of the SpMM launches by algorithmic bytes
     const double edges[] = {0, 1e6, 16e6, 128e6, 1e30};
-    double bms[4] = {0, 0, 0, 0}, bby[4] = {0, 0, 0, 0};
-    int64_t bn[4] = {0, 0, 0, 0};
+    double bms[8] = {0}, bby[8] = {0};
+    int64_t bn[8] = {0};
     for (size_t i = 0; i + 1 < g_prof.used; i += 2) {
         float t = 0;
         G2P_CUDA(cudaEventElapsedTime(&t, g_prof.ev[i], g_prof.ev[i + 1]));
@@ -1665,15 +1739,18 @@ extern "C" g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, i
         const size_t li = i / 2;
         if (li < g_prof.launch_bytes.size()) {
             const double lb = g_prof.launch_bytes[li];
+            const int o = g_prof.launch_f64[li] ? 4 : 0;
             for (int q = 0; q < 4; q++)
-                if (lb >= edges[q] && lb < edges[q + 1]) { bms[q] += t; bby[q] += lb; bn[q]++; }
+                if (lb >= edges[q] && lb < edges[q + 1]) { bms[o + q] += t; bby[o + q] += lb; bn[o + q]++; }
         }
     }
+    for (int q = 0; q < 8; q++) { g_bucket_ms[q] = bms[q]; g_bucket_bytes[q] = bby[q]; g_bucket_n[q] = bn[q]; }
     const char *bname[4] = {"<1MB", "1-16MB", "16-128MB", ">=128MB"};
-    for (int q = 0; q < 4; q++)
+    for (int q = 0; q < 8; q++)
         if (bn[q]) {
             char nm[96];
-            snprintf(nm, sizeof nm, "spmm[%s]@%.0fGB/s", bname[q], bms[q] > 0 ? bby[q] / (bms[q] * 1e6) : 0.0);
+            snprintf(nm, sizeof nm, "spmm_%s[%s]@%.0fGB/s", q < 4 ? "f32" : "f64", bname[q % 4],
+                     bms[q] > 0 ? bby[q] / (bms[q] * 1e6) : 0.0);
             kprof_add_total(nm, bn[q], bms[q]);
         }
     if (kernel_ms) *kernel_ms = ms;
@@ -1681,4 +1758,12 @@ extern "C" g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, i
     if (launches) *launches = g_prof.launches;
     g_prof.used = 0;
     return G2P_OK;
+}
+
+extern "C" void g2p_profile_buckets(double *ms, double *bytes, int64_t *launches) {
+    for (int q = 0; q < 8; q++) {
+        if (ms) ms[q] = g2p::g_bucket_ms[q];
+        if (bytes) bytes[q] = g2p::g_bucket_bytes[q];
+        if (launches) launches[q] = g2p::g_bucket_n[q];
+    }
 }

@@ -6,14 +6,19 @@
 namespace g2p {
 
 constexpr int kLongRow = 64;
-constexpr int kLongChunk = 2048;    // entries per block in the long-row kernel
+constexpr int kLongChunk = 512;     // entries per block in the long-row kernel
+constexpr int kHugeRow = 256;       // rows above this are split into chunks; shorter long rows get a warp
 constexpr int kMaxRhs = 256;
 
-// Rows longer than kLongRow (the lumped conductor potentials of Ad and
-// their coarse images), split into chunks of kLongChunk entries.
+// Rows longer than kLongRow: the lumped conductor potentials of Ad and the
+// wide rows of coarse Galerkin operators.  Rows of up to kHugeRow entries
+// are listed in mid (one warp each); longer ones are split into chunks of
+// kLongChunk entries (one block each).
 struct LongRows {
     int32_t *rows = nullptr;     // [n] row ids
     int64_t n = 0;
+    int32_t *mid = nullptr;      // [nmid] row ids of rows with at most kHugeRow entries
+    int64_t nmid = 0;
     int32_t *crow = nullptr;     // [nchunk] index into rows
     int64_t *cbeg = nullptr;     // [nchunk] first entry
     int64_t *rcp = nullptr;      // [n+1] chunks of each long row
@@ -22,7 +27,8 @@ struct LongRows {
     int32_t *done = nullptr;     // [n] chunks finished per row; zero between launches
     void release(cudaStream_t s) {
         dfree(rows, s); dfree(crow, s); dfree(cbeg, s); dfree(rcp, s); dfree(partial, s); dfree(done, s);
-        n = nchunk = 0;
+        dfree(mid, s);
+        n = nchunk = nmid = 0;
     }
 };
 

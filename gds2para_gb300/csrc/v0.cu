@@ -397,10 +397,13 @@ __global__ void k_seg_bounds(const int64_t *head, const int64_t *segid, int64_t 
 // Ordered sum of each key's values (left to right, from 0.0, so bit-equal
 // to the reference's accumulation); keeps |v| > 1e-8 (fdtd.hpp:2852).  The
 // loads run eight ahead of the dependent additions.
+constexpr int64_t kSegWarp = 256;   // segments longer than this are summed by a warp
+
 __global__ void k_seg_sum(const uint64_t *keys, const double *vals, int64_t nseg, const int64_t *sstart,
                           uint64_t *okey, double *oval, int64_t *keep) {
     for (int64_t sg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sg < nseg; sg += (int64_t)gridDim.x * blockDim.x) {
         const int64_t b = sstart[sg], e = sstart[sg + 1];
+        if (e - b > kSegWarp) continue;
         double s = 0.0;
         int64_t j = b;
         for (; j + 8 <= e; j += 8) {
@@ -414,6 +417,41 @@ __global__ void k_seg_sum(const uint64_t *keys, const double *vals, int64_t nseg
         okey[sg] = keys[b];
         oval[sg] = s;
         keep[sg] = fabs(s) > 1e-8 ? 1 : 0;
+    }
+}
+
+// The same ordered sum for segments longer than kSegWarp, one warp per
+// segment: the lanes load 32 x 8 consecutive values at a time and every lane
+// adds them left to right from the broadcasts, so the result is the
+// sequential sum.
+__global__ void k_seg_sum_long(const uint64_t *keys, const double *vals, int64_t nseg, const int64_t *sstart,
+                               uint64_t *okey, double *oval, int64_t *keep) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t sg = warp; sg < nseg; sg += nwarp) {
+        const int64_t b = sstart[sg], e = sstart[sg + 1];
+        if (e - b <= kSegWarp) continue;
+        double s = 0.0;
+        for (int64_t j0 = b; j0 < e; j0 += 32 * 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int64_t j = j0 + 32 * u + lane;
+                v[u] = j < e ? vals[j] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int64_t jb = j0 + 32 * u;
+                const int cnt = e - jb >= 32 ? 32 : (int)(e - jb);
+                for (int t = 0; t < cnt; t++) s += __shfl_sync(0xffffffffu, v[u], t);
+            }
+        }
+        if (lane == 0) {
+            okey[sg] = keys[b];
+            oval[sg] = s;
+            keep[sg] = fabs(s) > 1e-8 ? 1 : 0;
+        }
     }
 }
 
@@ -529,6 +567,7 @@ static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool 
         G2P_TRY(dalloc(&sstart, nseg + 1, s));
         (g2p::kbegin("k_seg_bounds", s), k_seg_bounds<<<grid_for(nterm), kThreads, 0, s>>>(head, segid, nterm, nseg, sstart), g2p::kend(s));
         (g2p::kbegin("k_seg_sum", s), k_seg_sum<<<grid_for(nseg), kThreads, 0, s>>>(sk, sv, nseg, sstart, okey, oval, keep), g2p::kend(s));
+        (g2p::kbegin("k_seg_sum_long", s), k_seg_sum_long<<<grid_for(32 * nseg), kThreads, 0, s>>>(sk, sv, nseg, sstart, okey, oval, keep), g2p::kend(s));
         dfree(sstart, s);
         (g2p::kbegin("k_long_rowlen", s), k_long_rowlen<<<grid_for(nseg), kThreads, 0, s>>>(okey, keep, nseg, ncol, rowlen + nshort), g2p::kend(s));
         const int64_t *kp = keep;

@@ -179,6 +179,12 @@ g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, int64_t *lau
  * ("name<TAB>launches<TAB>total_ms"); returns the full length, writes at most
  * cap-1 bytes plus a terminator. */
 int64_t g2p_profile_report(char *buf, int64_t cap);
+/* The short-row SpMM launches (k_spmm_sell) of the last profiled interval
+ * in eight classes: FP32 operators then FP64 operators, each split by
+ * algorithmic bytes per launch (<1 MB, 1-16 MB, 16-128 MB, >=128 MB).
+ * Writes device milliseconds, algorithmic bytes and launches per class
+ * (arrays of 8). */
+void g2p_profile_buckets(double *ms, double *bytes, int64_t *launches);
 
 /* ---- setMapEdge without device allocation (no counterpart in the
  * reference; its nearest reference code is setMapEdge, src/fdtd.hpp:1444-1529,

@@ -65,7 +65,7 @@ class _V0(C.Structure):
 class SolverOpts(C.Structure):
     _fields_ = [("restart", C.c_int), ("maxit", C.c_int), ("rtol", C.c_double), ("pc_tol", C.c_double),
                 ("pc_mod_sweeps", C.c_int), ("coarse_size", C.c_int), ("strength", C.c_double),
-                ("reuse_setup", C.c_int)]
+                ("reuse_setup", C.c_int), ("stop_after_solves", C.c_int)]
 
 
 class SolveStats(C.Structure):
@@ -77,7 +77,8 @@ class ParaStats(C.Structure):
     _fields_ = [("leng_v0d", C.c_int64), ("leng_v0c", C.c_int64), ("nnz_ad", C.c_int64),
                 ("nnz_ac", C.c_int64), ("bden", C.c_int64), ("solves", C.c_int),
                 ("total_iterations", C.c_int), ("max_rel_residual", C.c_double),
-                ("t_assembly", C.c_double), ("t_setup", C.c_double), ("t_solve", C.c_double)]
+                ("t_assembly", C.c_double), ("t_setup", C.c_double), ("t_solve", C.c_double),
+                ("t_each", C.c_double * 3)]
 
 
 def _arr(a, dtype):

@@ -43,6 +43,7 @@ typedef struct {
     int reuse_setup;    /* 0: rebuild the hierarchy on every solve, as the
                            reference does (hypreSolve.cpp:36-68,251); 1: build
                            once per matrix and reuse it across ports */
+    int stop_after_solves;    /* paraGenerator timing samples: stop after this many solves (0 = all) */
 } g2po_solver_opts;
 
 typedef struct {
@@ -110,6 +111,7 @@ typedef struct {
     int solves, total_iterations;
     double max_rel_residual;
     double t_assembly, t_setup, t_solve;     /* seconds */
+    double t_each[3];                        /* first port's Ad, Ac, Ad solves incl. setup (s) */
 } g2po_para_stats;
 int g2po_para_generator(const g2po_mesh *m, const g2po_solver_opts *o, int max_ports,
                         double *z_out, g2po_para_stats *st);

@@ -584,6 +584,8 @@ int g2po_para_generator(const g2po_mesh *m, const g2po_solver_opts *o, int max_p
         if (!reuse) g2po_amg_destroy(_h);                                   \
         st->solves++; st->total_iterations += ss.iterations;                \
         if (ss.rel_residual > st->max_rel_residual) st->max_rel_residual = ss.rel_residual; \
+        if (st->solves <= 3) st->t_each[st->solves - 1] = now_s() - _t;     \
+        if (o->stop_after_solves > 0 && st->solves >= o->stop_after_solves) goto sampled; \
     } while (0)
     for (int p = 0; p < np; p++) {
         /* matrixCon.cpp:365-374 */
@@ -639,6 +641,7 @@ int g2po_para_generator(const g2po_mesh *m, const g2po_solver_opts *o, int max_p
             zi[q + (int64_t)P * p] = im / cur;
         }
     }
+sampled:
 #undef SOLVE
     /* print_z_V0 (fdtd.hpp:4249-4316): freq 0 as stored, others transposed
        with Im scaled by f0/f */

@@ -355,6 +355,7 @@ void g2po_solver_default_opts(g2po_solver_opts *o) {
     o->restart = 10; o->maxit = 100; o->rtol = 1e-4;
     o->pc_tol = 0.1; o->pc_mod_sweeps = 10;
     o->coarse_size = 400; o->strength = 0.08; o->reuse_setup = 0;
+    o->stop_after_solves = 0;
 }
 
 static int fgmres(const g2po_csr *A, amg_t *h, const double *b, double *x,
