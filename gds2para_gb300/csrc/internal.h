@@ -10,7 +10,10 @@ constexpr uint8_t kSellLong = 255;   // rlen of a row served by the long-row ker
 // Device CSR with int64 row offsets and int32 columns, plus an optional
 // sliced-ELL copy of its short rows for the SpMM: slices of 32 rows whose
 // entries are stored column by column (entry j of row 32 s + t at
-// sptr[s] + 32 j + t), rlen[i] the row's entry count or kSellLong.
+// sptr[s] + 32 j + t), rlen[i] the row's entry count or kSellLong.  When
+// ell_w > 0 every slice is ell_w wide (sptr[s] = 32 ell_w s) and the unused
+// slots hold (column = the row, value = 0), so the kernel needs neither
+// sptr nor rlen.
 template <class T>
 struct Csr {
     int64_t n = 0, m = 0, nnz = 0;
@@ -22,9 +25,11 @@ struct Csr {
     T *sval = nullptr;
     uint8_t *rlen = nullptr;
     int64_t short_nnz = 0, sell_slots = 0;
+    int32_t ell_w = 0;           // > 0: every slice has this width, padded with (row, 0)
     void release_sell(cudaStream_t s) {
         dfree(sptr, s); dfree(scol, s); dfree(sval, s); dfree(rlen, s);
         short_nnz = sell_slots = 0;
+        ell_w = 0;
     }
     void release(cudaStream_t s) {
         dfree(ptr, s); dfree(col, s); dfree(val, s);
@@ -93,6 +98,7 @@ struct g2p_mesh {
     g2p::Csr<double> S;
     // V0 bases and Laplacians
     bool v0_done = false;
+    double *v0_tab = nullptr;      // per-line quotient tables of the V0 entries
     g2p::V0Basis v0d, v0c;
     g2p::Csr<double> Ad, Ac;
     // scratch for scans

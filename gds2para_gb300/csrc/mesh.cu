@@ -271,7 +271,7 @@ extern "C" g2p_status g2p_mesh_destroy(g2p_mesh *m) {
     if (!m) return G2P_OK;
     cudaStream_t s = m->stream;
     dfree(m->xn, s); dfree(m->yn, s); dfree(m->zn, s);
-    dfree(m->dxa, s); dfree(m->dya, s); dfree(m->dza, s);
+    dfree(m->dxa, s); dfree(m->dya, s); dfree(m->dza, s); dfree(m->v0_tab, s);
     dfree(m->epsn, s); dfree(m->sign, s);
     dfree(m->mark_node, s); dfree(m->mark_edge, s); dfree(m->mark_port, s); dfree(m->cdt_return, s);
     dfree(m->pec_edge, s); dfree(m->pec_node, s); dfree(m->map_edge, s);
@@ -383,6 +383,14 @@ struct FaceEnt {
 struct Geo {
     Dims d;
     const double *xn, *yn, *zn, *dxa, *dya, *dza;
+    // Quotients of generateStiff's face expressions, one per grid line or
+    // line pair, computed once with the same IEEE operations (so bit-equal):
+    // ivx[c] = 1 / (xn[c+1] - xn[c]) (likewise y, z), and
+    // qa_b[i][j] = a[i] / (a[i] * b[j]) for the dual-length pairs a, b.
+    const double *ivx, *ivy, *ivz;
+    const double *qz_x, *qz_y;    // [Nz][Nx+1], [Nz][Ny+1]: a = dza
+    const double *qx_z, *qx_y;    // [Nx+1][Nz+1], [Nx+1][Ny+1]: a = dxa
+    const double *qy_z, *qy_x;    // [Ny+1][Nz+1], [Ny+1][Nx+1]: a = dya
 };
 
 // Face numbering of generateStiff: per (z, x, y) cell below the top layer
@@ -404,32 +412,60 @@ __device__ __forceinline__ int64_t fid_xz(const Dims &d, int64_t j, int64_t cz, 
 
 // The four (edge, Se, Sh) entries of each face kind, with the reference's
 // expressions (generateStiff.cpp:33-484; the top xy face keeps dza[Nz-1]).
+// The reference's face expressions, e.g. se = -1 / dx and sh = -q / (dxa * q),
+// read from the Geo tables: -1 / dx == -(1 / dx) and q / (dxa * q) ==
+// q / (q * dxa) in IEEE arithmetic, so every value is bit-equal to the
+// expression evaluated in place.
 __device__ __forceinline__ void face_xy(const Geo &g, int64_t p, int64_t cx, int64_t cy, FaceEnt &f) {
     const Dims &d = g.d;
-    double dx = g.xn[cx + 1] - g.xn[cx], dy = g.yn[cy + 1] - g.yn[cy];
-    double q = g.dza[p < d.Nz ? p : d.Nz - 1];
-    f.e[0] = d.ye(p, cx, cy);     f.se[0] = -1 / dx; f.sh[0] = -q / (g.dxa[cx] * q);
-    f.e[1] = d.ye(p, cx + 1, cy); f.se[1] = 1 / dx;  f.sh[1] = q / (g.dxa[cx + 1] * q);
-    f.e[2] = d.xe(p, cx, cy);     f.se[2] = 1 / dy;  f.sh[2] = q / (q * g.dya[cy]);
-    f.e[3] = d.xe(p, cx, cy + 1); f.se[3] = -1 / dy; f.sh[3] = -q / (q * g.dya[cy + 1]);
+    const double ix = g.ivx[cx], iy = g.ivy[cy];
+    const double *qx = g.qz_x + (p < d.Nz ? p : d.Nz - 1) * (d.Nx + 1);
+    const double *qy = g.qz_y + (p < d.Nz ? p : d.Nz - 1) * (d.Ny + 1);
+    f.e[0] = d.ye(p, cx, cy);     f.se[0] = -ix; f.sh[0] = -qx[cx];
+    f.e[1] = d.ye(p, cx + 1, cy); f.se[1] = ix;  f.sh[1] = qx[cx + 1];
+    f.e[2] = d.xe(p, cx, cy);     f.se[2] = iy;  f.sh[2] = qy[cy];
+    f.e[3] = d.xe(p, cx, cy + 1); f.se[3] = -iy; f.sh[3] = -qy[cy + 1];
 }
 __device__ __forceinline__ void face_yz(const Geo &g, int64_t i, int64_t cz, int64_t cy, FaceEnt &f) {
     const Dims &d = g.d;
-    double dy = g.yn[cy + 1] - g.yn[cy], dz = g.zn[cz + 1] - g.zn[cz];
-    double a = g.dxa[i];
-    f.e[0] = d.ye(cz, i, cy);     f.se[0] = 1 / dz;  f.sh[0] = a / (a * g.dza[cz]);
-    f.e[1] = d.ze(cz, i, cy);     f.se[1] = -1 / dy; f.sh[1] = -a / (a * g.dya[cy]);
-    f.e[2] = d.ze(cz, i, cy + 1); f.se[2] = 1 / dy;  f.sh[2] = a / (a * g.dya[cy + 1]);
-    f.e[3] = d.ye(cz + 1, i, cy); f.se[3] = -1 / dz; f.sh[3] = -a / (a * g.dza[cz + 1]);
+    const double iy = g.ivy[cy], iz = g.ivz[cz];
+    const double *qz = g.qx_z + i * (d.Nz + 1), *qy = g.qx_y + i * (d.Ny + 1);
+    f.e[0] = d.ye(cz, i, cy);     f.se[0] = iz;  f.sh[0] = qz[cz];
+    f.e[1] = d.ze(cz, i, cy);     f.se[1] = -iy; f.sh[1] = -qy[cy];
+    f.e[2] = d.ze(cz, i, cy + 1); f.se[2] = iy;  f.sh[2] = qy[cy + 1];
+    f.e[3] = d.ye(cz + 1, i, cy); f.se[3] = -iz; f.sh[3] = -qz[cz + 1];
 }
 __device__ __forceinline__ void face_xz(const Geo &g, int64_t j, int64_t cz, int64_t cx, FaceEnt &f) {
     const Dims &d = g.d;
-    double dx = g.xn[cx + 1] - g.xn[cx], dz = g.zn[cz + 1] - g.zn[cz];
-    double b = g.dya[j];
-    f.e[0] = d.xe(cz, cx, j);     f.se[0] = -1 / dz; f.sh[0] = -b / (g.dza[cz] * b);
-    f.e[1] = d.ze(cz, cx, j);     f.se[1] = 1 / dx;  f.sh[1] = b / (g.dxa[cx] * b);
-    f.e[2] = d.ze(cz, cx + 1, j); f.se[2] = -1 / dx; f.sh[2] = -b / (b * g.dxa[cx + 1]);
-    f.e[3] = d.xe(cz + 1, cx, j); f.se[3] = 1 / dz;  f.sh[3] = b / (b * g.dza[cz + 1]);
+    const double ix = g.ivx[cx], iz = g.ivz[cz];
+    const double *qz = g.qy_z + j * (d.Nz + 1), *qx = g.qy_x + j * (d.Nx + 1);
+    f.e[0] = d.xe(cz, cx, j);     f.se[0] = -iz; f.sh[0] = -qz[cz];
+    f.e[1] = d.ze(cz, cx, j);     f.se[1] = ix;  f.sh[1] = qx[cx];
+    f.e[2] = d.ze(cz, cx + 1, j); f.se[2] = -ix; f.sh[2] = -qx[cx + 1];
+    f.e[3] = d.xe(cz + 1, cx, j); f.se[3] = iz;  f.sh[3] = qz[cz + 1];
+}
+
+// Edges of a face (no values), for the row-length pass.
+__device__ __forceinline__ void face_edges(const Dims &d, int kind, int64_t a, int64_t b, int64_t c, int64_t *e) {
+    if (kind == 0) { e[0] = d.ye(a, b, c); e[1] = d.ye(a, b + 1, c); e[2] = d.xe(a, b, c); e[3] = d.xe(a, b, c + 1); }
+    else if (kind == 1) { e[0] = d.ye(b, a, c); e[1] = d.ze(b, a, c); e[2] = d.ze(b, a, c + 1); e[3] = d.ye(b + 1, a, c); }
+    else { e[0] = d.xe(b, c, a); e[1] = d.ze(b, c, a); e[2] = d.ze(b, c + 1, a); e[3] = d.xe(b + 1, c, a); }
+}
+
+__global__ void k_inv_len(const double *xn, int64_t n, double *inv) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double h = xn[i + 1] - xn[i];
+        inv[i] = 1 / h;
+    }
+}
+
+// q[i][j] = a[i] / (a[i] * b[j])
+__global__ void k_quot(const double *a, int64_t na, const double *b, int64_t nb, double *q) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < na * nb; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / nb, j = t - i * nb;
+        const double ai = a[i];
+        q[t] = ai / (ai * b[j]);
+    }
 }
 
 // Faces containing edge e: kind (0 xy, 1 yz, 2 xz) and (a, b, c) arguments.
@@ -507,11 +543,17 @@ __global__ void __launch_bounds__(256) k_stiff_count(Geo g, const uint8_t *__res
     const Dims &d = g.d;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < d.N_edge; e += (int64_t)gridDim.x * blockDim.x) {
         if (pec[e]) continue;
-        int64_t cols[kMaxS];
-        double vals[kMaxS];
-        int nc = stiff_row(g, e, cols, vals);
-        int cnt = 0;
-        for (int q = 0; q < nc; q++) cnt += pec[cols[q]] ? 0 : 1;
+        // the structural row: e and the other edges of its faces (two faces
+        // of the grid share at most one edge, so none repeats)
+        FaceRef fr[4];
+        const int nf = edge_faces(d, e, fr);
+        int cnt = 1;
+        for (int t = 0; t < nf; t++) {
+            int64_t fe[4];
+            face_edges(d, fr[t].kind, fr[t].a, fr[t].b, fr[t].c, fe);
+#pragma unroll
+            for (int k = 0; k < 4; k++) cnt += (fe[k] != e && !pec[fe[k]]) ? 1 : 0;
+        }
         rowlen[map[e]] = cnt;
     }
 }
@@ -567,7 +609,25 @@ g2p_status g2p_run_stiff(g2p_mesh *m) {
     G2P_TRY(g2p_run_index_maps(m));
     const Dims &d = m->d;
     cudaStream_t s = m->stream;
+    // per-line quotient tables (see Geo)
+    const int64_t NX = d.Nx + 1, NY = d.Ny + 1, NZ = d.Nz + 1;
+    double *tab;
+    const int64_t ntab = d.Nx + d.Ny + d.Nz + d.Nz * NX + d.Nz * NY + NX * NZ + NX * NY + NY * NZ + NY * NX;
+    G2P_TRY(dalloc(&tab, ntab, s));
     Geo g{d, m->xn, m->yn, m->zn, m->dxa, m->dya, m->dza};
+    double *t = tab;
+    g.ivx = t; (g2p::kbegin("k_inv_len", s), k_inv_len<<<grid_for(d.Nx), kThreads, 0, s>>>(m->xn, d.Nx, t), g2p::kend(s)); t += d.Nx;
+    g.ivy = t; (g2p::kbegin("k_inv_len", s), k_inv_len<<<grid_for(d.Ny), kThreads, 0, s>>>(m->yn, d.Ny, t), g2p::kend(s)); t += d.Ny;
+    g.ivz = t; (g2p::kbegin("k_inv_len", s), k_inv_len<<<grid_for(d.Nz), kThreads, 0, s>>>(m->zn, d.Nz, t), g2p::kend(s)); t += d.Nz;
+    struct QT { const double **dst; const double *a; int64_t na; const double *b; int64_t nb; };
+    const QT qts[6] = {{&g.qz_x, m->dza, d.Nz, m->dxa, NX}, {&g.qz_y, m->dza, d.Nz, m->dya, NY},
+                       {&g.qx_z, m->dxa, NX, m->dza, NZ}, {&g.qx_y, m->dxa, NX, m->dya, NY},
+                       {&g.qy_z, m->dya, NY, m->dza, NZ}, {&g.qy_x, m->dya, NY, m->dxa, NX}};
+    for (const QT &q : qts) {
+        *q.dst = t;
+        (g2p::kbegin("k_quot", s), k_quot<<<grid_for(q.na * q.nb), kThreads, 0, s>>>(q.a, q.na, q.b, q.nb, t), g2p::kend(s));
+        t += q.na * q.nb;
+    }
     int64_t n = d.N_edge - m->bden;
     int64_t *rowlen;
     G2P_TRY(dalloc(&rowlen, n, s));
@@ -575,13 +635,14 @@ g2p_status g2p_run_stiff(g2p_mesh *m) {
     int64_t nnz = 0;
     g2p_status st = g2p_build_rowptr(m, rowlen, n, &m->S.ptr, &nnz);
     dfree(rowlen, s);
-    if (st != G2P_OK) return st;
+    if (st != G2P_OK) { dfree(tab, s); return st; }
     m->S.n = m->S.m = n;
     m->S.nnz = nnz;
     G2P_TRY(dalloc(&m->S.col, nnz, s));
     G2P_TRY(dalloc(&m->S.val, nnz, s));
     (g2p::kbegin("k_stiff_fill", s), k_stiff_fill<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, m->S.ptr, m->S.col,
                                                                      m->S.val, m->k.mu), g2p::kend(s));
+    dfree(tab, s);
     G2P_CUDA(cudaGetLastError());
     G2P_CUDA(cudaStreamSynchronize(s));
     m->stiff_done = true;

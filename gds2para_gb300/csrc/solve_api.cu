@@ -94,9 +94,9 @@ extern "C" void g2p_default_params(g2p_solver_params *p, int32_t parity_mode) {
     }
     p->smoother_degree = 2;
     p->coarse_size = 256;
-    p->strength = 0.08;
+    p->strength = 0.04;
     p->max_levels = 20;
-    p->inner_rtol = 1e-3;
+    p->inner_rtol = 3e-3;
     p->inner_maxit = 40;
     p->batch = 1;
     p->use_graphs = 0;
@@ -110,7 +110,7 @@ static SolverConfig cfg_from(const g2p_solver_params *p) {
     c.rtol = p->rtol > 0 ? p->rtol : 1e-10;
     c.degree = p->smoother_degree > 0 ? p->smoother_degree : 2;
     c.coarse_size = p->coarse_size > 0 ? p->coarse_size : 256;
-    c.strength = p->strength > 0 ? p->strength : 0.08;
+    c.strength = p->strength > 0 ? p->strength : 0.04;
     c.max_levels = p->max_levels > 0 ? p->max_levels : 20;
     c.reorth = false;   // classical Gram-Schmidt once: same iteration counts, half the passes
     if (const char *e = getenv("G2P_REORTH")) c.reorth = atoi(e) != 0;
@@ -125,7 +125,7 @@ g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cu
     S->stream = stream;
     S->cfg = cfg_from(p);
     S->precision = p->precision;
-    S->inner_rtol = p->inner_rtol > 0 ? p->inner_rtol : 1e-3;
+    S->inner_rtol = p->inner_rtol > 0 ? p->inner_rtol : 3e-3;
     S->inner_maxit = p->inner_maxit > 0 ? p->inner_maxit : 40;
     cudaStream_t s = stream;
     auto fail = [&](g2p_status st) { g2p_solver_destroy(S); return st; };
@@ -330,7 +330,7 @@ extern "C" g2p_status g2p_solver_destroy(g2p_solver *S) {
     if (!S) return G2P_OK;
     cudaStream_t s = S->stream;
     S->A.release(s);
-    S->lr.release(s); dfree(S->scale, s);
+    S->lr.release(s);
     S->H64.release(s); S->H32.release(s);
     S->K64.release(s); S->K32.release(s);
     dfree(S->xb, s); dfree(S->bb, s); dfree(S->rb, s); dfree(S->rf, s); dfree(S->df, s);

@@ -156,6 +156,72 @@ __global__ void __launch_bounds__(256) k_spmm_sell(int64_t n, const int64_t *__r
     }
 }
 
+// The same product on the uniform-width layout: the slot of entry j of row i
+// is 32 (ell_w (i / 32) + j) + i % 32, so the only dependent loads are the
+// column and value, then x.  Padding slots add 0 x_i.
+template <class T, int V>
+__global__ void __launch_bounds__(256) k_spmm_ell(int64_t n, int w, const int32_t *__restrict__ scol,
+                                                  const T *__restrict__ sval, const T *__restrict__ x,
+                                                  T *__restrict__ y, int k, const T *__restrict__ b) {
+    const int xo = threadIdx.x * V;
+    G2P_FOR_ROWS(i, n) {
+        const int64_t base = 32 * (int64_t)w * (i >> 5) + (i & 31);
+        T acc[V];
+#pragma unroll
+        for (int u = 0; u < V; u++) acc[u] = 0;
+        XVec<T, V> bv;
+        if (b) bv.load(b + i * k + xo);
+        for (int j0 = 0; j0 < w; j0 += kSellUnroll) {
+            int32_t c[kSellUnroll];
+            T a[kSellUnroll];
+#pragma unroll
+            for (int u = 0; u < kSellUnroll; u++) {
+                const bool in = j0 + u < w;
+                c[u] = in ? __ldg(scol + base + 32 * (int64_t)(j0 + u)) : (int32_t)i;
+                a[u] = in ? __ldg(sval + base + 32 * (int64_t)(j0 + u)) : T(0);
+            }
+            XVec<T, V> xv[kSellUnroll];
+#pragma unroll
+            for (int u = 0; u < kSellUnroll; u++) xv[u].load(x + (int64_t)c[u] * k + xo);
+#pragma unroll
+            for (int u = 0; u < kSellUnroll; u++)
+#pragma unroll
+                for (int q = 0; q < V; q++) acc[q] += a[u] * xv[u].v[q];
+        }
+        XVec<T, V> out;
+#pragma unroll
+        for (int q = 0; q < V; q++) out.v[q] = b ? bv.v[q] - acc[q] : acc[q];
+        out.store(y + i * k + xo);
+    }
+}
+
+// Padding of the uniform layout: (column = row, value = 0) in every slot a
+// row does not use, and in all slots of long rows.
+template <class T>
+__global__ void k_ell_pad(int64_t n, int w, const uint8_t *__restrict__ rlen, int32_t *__restrict__ scol,
+                          T *__restrict__ sval) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int len = rlen[i] == kSellLong ? 0 : rlen[i];
+        const int64_t base = 32 * (int64_t)w * (i >> 5) + (i & 31);
+        for (int j = len; j < w; j++) {
+            scol[base + 32 * (int64_t)j] = (int32_t)i;
+            sval[base + 32 * (int64_t)j] = T(0);
+        }
+    }
+}
+
+__global__ void k_width_max(const int64_t *width, int64_t nslice, unsigned long long *mx) {
+    unsigned long long m = 0;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nslice; s += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, (unsigned long long)width[s]);
+    if (m) atomicMax(mx, m);
+}
+
+__global__ void k_ell_sptr(int64_t *sptr, int64_t nslice, int64_t stride) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s <= nslice; s += (int64_t)gridDim.x * blockDim.x)
+        sptr[s] = stride * s;
+}
+
 // Slice widths (entries of the slice's longest short row) and row lengths.
 __global__ void k_sell_width(int64_t n, const int64_t *__restrict__ ptr, int64_t nslice, int64_t *__restrict__ width,
                              uint8_t *__restrict__ rlen) {
@@ -327,9 +393,14 @@ static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cu
     int64_t g = (A.n + rows - 1) / rows;
     if (g > 0x7fffffffLL) g = 0x7fffffffLL;
     if (g < 1) g = 1;
-    (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_sell<f64>" : "k_spmm_sell<f32>", s),
-     k_spmm_sell<T, V><<<(unsigned)g, dim3(tpr, rows), 0, s>>>(A.n, A.sptr, A.scol, A.sval, A.rlen, x, y, k, b),
-     g2p::kend(s));
+    if (A.ell_w > 0)
+        (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_sell<f64>" : "k_spmm_sell<f32>", s),
+         k_spmm_ell<T, V><<<(unsigned)g, dim3(tpr, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b),
+         g2p::kend(s));
+    else
+        (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_sell<f64>" : "k_spmm_sell<f32>", s),
+         k_spmm_sell<T, V><<<(unsigned)g, dim3(tpr, rows), 0, s>>>(A.n, A.sptr, A.scol, A.sval, A.rlen, x, y, k, b),
+         g2p::kend(s));
 }
 
 template <class T>
@@ -506,14 +577,34 @@ g2p_status sell_build(Csr<T> &A, cudaStream_t s) {
     const int64_t *wp = width;
     auto op = [wp, nslice] __device__(int64_t i) -> int64_t { return i < nslice ? wp[i] : 0; };
     G2P_TRY(exclusive_scan(op, nslice + 1, A.sptr, work, s));
+    unsigned long long *dmax;
+    G2P_TRY(dalloc(&dmax, 1, s));
+    G2P_CUDA(cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), s));
+    (g2p::kbegin("k_width_max", s), k_width_max<<<grid_for(nslice), kThreads, 0, s>>>(width, nslice, dmax), g2p::kend(s));
     int64_t slots = 0;
+    unsigned long long hmax = 0;
     G2P_CUDA(cudaMemcpyAsync(&slots, A.sptr + nslice, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaMemcpyAsync(&hmax, dmax, sizeof(hmax), cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
-    dfree(width, s); dfree(work, s);
+    dfree(width, s); dfree(work, s); dfree(dmax, s);
+    // one width for all slices when that costs at most a quarter more slots
+    const int64_t wmax = (int64_t)hmax / 32;
+    const bool uniform = wmax > 0 && 32 * wmax * nslice <= slots + slots / 4;
+    if (uniform) {
+        (g2p::kbegin("k_ell_sptr", s), k_ell_sptr<<<grid_for(nslice + 1), kThreads, 0, s>>>(A.sptr, nslice, 32 * wmax), g2p::kend(s));
+        slots = 32 * wmax * nslice;
+        A.ell_w = (int32_t)wmax;
+    }
     A.sell_slots = slots;
+    if (const char *e = getenv("G2P_DEBUG"))
+        if (atoi(e) >= 2)
+            fprintf(stderr, "[g2p sell] n=%lld nnz=%lld slots=%lld wmax=%lld uniform=%d\n", (long long)n,
+                    (long long)A.nnz, (long long)slots, (long long)wmax, (int)uniform);
     G2P_TRY(dalloc(&A.scol, slots, s));
     G2P_TRY(dalloc(&A.sval, slots, s));
     (g2p::kbegin("k_sell_fill", s), k_sell_fill<T><<<grid_for(n), kThreads, 0, s>>>(n, A.ptr, A.col, A.val, A.rlen, A.sptr, A.scol, A.sval), g2p::kend(s));
+    if (uniform)
+        (g2p::kbegin("k_ell_pad", s), k_ell_pad<T><<<grid_for(n), kThreads, 0, s>>>(n, A.ell_w, A.rlen, A.scol, A.sval), g2p::kend(s));
     // entries of the long rows are not in the copy
     int64_t *lp, *lw;
     G2P_TRY(dalloc(&lp, n + 1, s));

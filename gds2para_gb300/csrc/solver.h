@@ -53,7 +53,7 @@ struct SolverConfig {
     double rtol = 1e-10;
     int degree = 2;
     int coarse_size = 256;
-    double strength = 0.08;
+    double strength = 0.04;
     int max_levels = 20;
     double cheb_ratio = 0.1;     // lower Chebyshev bound = ratio * lmax
     bool reorth = true;
@@ -124,13 +124,11 @@ struct g2p_solver {
     bool owns_stream = false;
     g2p::SolverConfig cfg;
     int precision = 0;
-    int inner_maxit = 60;
-    double inner_rtol = 1e-4;
+    int inner_maxit = 40;
+    double inner_rtol = 3e-3;
     g2p::Csr<double> A;                 // original FP64 operator
     g2p::LongRows lr;
-    double *scale = nullptr;            // unused
     double cscale = 1.0;                // mixed: power-of-two scale of the FP32 operator
-    g2p::Csr<double> As;                // scaled operator (mixed, FP64 for setup)
     g2p::Hierarchy<double> H64;
     g2p::Hierarchy<float> H32;
     g2p::Krylov<double> K64;

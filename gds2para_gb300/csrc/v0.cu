@@ -32,6 +32,12 @@ struct V0Ctx {
     const int32_t *mark_node, *mark_edge, *mark_port;
     const uint8_t *pec_node;
     double LX, LY, LZ, eps0;
+    // Values of the reference's entry expressions per grid line, computed
+    // once by k_v0_lines/k_v0_areas with the same operations (bit-equal):
+    // ivx[i] = 1 / (xn[i+1] - xn[i]), ilx[i] = 1 / lx(i) with lx the
+    // avg_length of node line i (likewise y, z), and the V0d2 area weights
+    // axy[ix][iy] = lx*ly / W, ayz[iy][iz] = ly*lz / W, axz[ix][iz] = lx*lz / W.
+    const double *ivx, *ivy, *ivz, *ilx, *ily, *ilz, *axy, *ayz, *axz;
 };
 
 // One incident edge of a node, in the reference's order (lower z, upper z,
@@ -48,42 +54,57 @@ __device__ __forceinline__ void node_ijk(const Dims &d, int64_t n, int64_t &iz, 
     iy = r - ix * (d.Ny + 1);
 }
 
-// avg_length (fdtd.hpp:4074-4104)
-__device__ __forceinline__ void avg_len(const V0Ctx &c, int64_t iz, int64_t iy, int64_t ix, double &lx, double &ly,
-                                        double &lz) {
-    const Dims &d = c.d;
-    if (iz == 0) lz = c.zn[1] - c.zn[0];
-    else if (iz == d.nz - 1) lz = c.zn[iz] - c.zn[iz - 1];
-    else lz = (c.zn[iz + 1] - c.zn[iz - 1]) / 2;
-    if (iy == 0) ly = c.yn[1] - c.yn[0];
-    else if (iy == d.ny - 1) ly = c.yn[iy] - c.yn[iy - 1];
-    else ly = (c.yn[iy + 1] - c.yn[iy - 1]) / 2;
-    if (ix == 0) lx = c.xn[1] - c.xn[0];
-    else if (ix == d.nx - 1) lx = c.xn[ix] - c.xn[ix - 1];
-    else lx = (c.xn[ix + 1] - c.xn[ix - 1]) / 2;
-}
 
 __device__ __forceinline__ int incident(const V0Ctx &c, int64_t n, Inc *out) {
     const Dims &d = c.d;
     int64_t iz, ix, iy;
     node_ijk(d, n, iz, ix, iy);
-    double lx, ly, lz;
-    avg_len(c, iz, iy, ix, lx, ly, lz);
-    double W = c.LX * c.LY * c.LZ;
+    // -1 / h == -(1 / h) and -lx * ly / W == -(lx * ly / W) exactly
+    const double azxy = c.axy[ix * d.ny + iy], axyz = c.ayz[iy * d.nz + iz], ayxz = c.axz[ix * d.nz + iz];
     int k = 0;
-    if (iz != 0) out[k++] = {(iz - 1) * d.L + d.Ns + ix * (d.Ny + 1) + iy, n - d.N_node_s,
-                             -1 / (c.zn[iz] - c.zn[iz - 1]), -1 / lz, -lx * ly / W};
-    if (iz != d.nz - 1) out[k++] = {iz * d.L + d.Ns + ix * (d.Ny + 1) + iy, n + d.N_node_s,
-                                    1 / (c.zn[iz + 1] - c.zn[iz]), 1 / lz, lx * ly / W};
-    if (ix != 0) out[k++] = {iz * d.L + d.XO + (ix - 1) * (d.Ny + 1) + iy, n - (d.Ny + 1),
-                             -1 / (c.xn[ix] - c.xn[ix - 1]), -1 / lx, -ly * lz / W};
-    if (ix != d.nx - 1) out[k++] = {iz * d.L + d.XO + ix * (d.Ny + 1) + iy, n + (d.Ny + 1),
-                                    1 / (c.xn[ix + 1] - c.xn[ix]), 1 / lx, ly * lz / W};
-    if (iy != 0) out[k++] = {iz * d.L + ix * d.Ny + iy - 1, n - 1, -1 / (c.yn[iy] - c.yn[iy - 1]), -1 / ly,
-                             -lx * lz / W};
-    if (iy != d.ny - 1) out[k++] = {iz * d.L + ix * d.Ny + iy, n + 1, 1 / (c.yn[iy + 1] - c.yn[iy]), 1 / ly,
-                                    lx * lz / W};
+    if (iz != 0) out[k++] = {(iz - 1) * d.L + d.Ns + ix * (d.Ny + 1) + iy, n - d.N_node_s, -c.ivz[iz - 1], -c.ilz[iz],
+                             -azxy};
+    if (iz != d.nz - 1) out[k++] = {iz * d.L + d.Ns + ix * (d.Ny + 1) + iy, n + d.N_node_s, c.ivz[iz], c.ilz[iz], azxy};
+    if (ix != 0) out[k++] = {iz * d.L + d.XO + (ix - 1) * (d.Ny + 1) + iy, n - (d.Ny + 1), -c.ivx[ix - 1], -c.ilx[ix],
+                             -axyz};
+    if (ix != d.nx - 1) out[k++] = {iz * d.L + d.XO + ix * (d.Ny + 1) + iy, n + (d.Ny + 1), c.ivx[ix], c.ilx[ix], axyz};
+    if (iy != 0) out[k++] = {iz * d.L + ix * d.Ny + iy - 1, n - 1, -c.ivy[iy - 1], -c.ily[iy], -ayxz};
+    if (iy != d.ny - 1) out[k++] = {iz * d.L + ix * d.Ny + iy, n + 1, c.ivy[iy], c.ily[iy], ayxz};
     return k;
+}
+
+// Per-line tables (see V0Ctx): blockIdx.y picks the axis.
+__global__ void k_v0_lines(V0Ctx c, double *ivx, double *ivy, double *ivz, double *lx, double *ly, double *lz,
+                           double *ilx, double *ily, double *ilz) {
+    const Dims &d = c.d;
+    const int ax = blockIdx.y;
+    const int64_t nn = ax == 0 ? d.nx : ax == 1 ? d.ny : d.nz;
+    const double *p = ax == 0 ? c.xn : ax == 1 ? c.yn : c.zn;
+    double *iv = ax == 0 ? ivx : ax == 1 ? ivy : ivz;
+    double *la = ax == 0 ? lx : ax == 1 ? ly : lz;
+    double *il = ax == 0 ? ilx : ax == 1 ? ily : ilz;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < nn - 1) iv[i] = 1 / (p[i + 1] - p[i]);
+        // avg_length (fdtd.hpp:4074-4104)
+        double l;
+        if (i == 0) l = p[1] - p[0];
+        else if (i == nn - 1) l = p[i] - p[i - 1];
+        else l = (p[i + 1] - p[i - 1]) / 2;
+        la[i] = l;
+        il[i] = 1 / l;
+    }
+}
+
+__global__ void k_v0_areas(V0Ctx c, const double *lx, const double *ly, const double *lz, double *axy, double *ayz,
+                           double *axz) {
+    const Dims &d = c.d;
+    const double W = c.LX * c.LY * c.LZ;
+    const int64_t n1 = d.nx * d.ny, n2 = d.ny * d.nz, n3 = d.nx * d.nz;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n1 + n2 + n3; t += (int64_t)gridDim.x * blockDim.x) {
+        if (t < n1) { const int64_t ix = t / d.ny, iy = t - ix * d.ny; axy[t] = lx[ix] * ly[iy] / W; }
+        else if (t < n1 + n2) { const int64_t u = t - n1, iy = u / d.nz, iz = u - iy * d.nz; ayz[u] = ly[iy] * lz[iz] / W; }
+        else { const int64_t u = t - n1 - n2, ix = u / d.nz, iz = u - ix * d.nz; axz[u] = lx[ix] * lz[iz] / W; }
+    }
 }
 
 __device__ __forceinline__ int node_degree(const Dims &d, int64_t n) {
@@ -124,16 +145,19 @@ __device__ __forceinline__ bool lap_term(const V0Ctx &c, const int32_t *map, boo
     int32_t m1 = map[n1], m2 = map[n2];
     other = -1;
     off = 0.0;
+    // the reference's a * 1 / h * s and a * (-1) / h * s: (a * 1) / h == q and
+    // (a * (-1)) / h == -q exactly, so one division serves both
+    const double q = a / h;
     if (is_ac) {
         double s = c.sign[inz];
-        if (m1 != col + 1 && m1 != 0) { other = m1 - 1; off = a * 1 / h * s; dg = a * (-1) / h * s; }
-        else if (m2 != col + 1 && m2 != 0) { other = m2 - 1; off = a * (-1) / h * s; dg = a * 1 / h * s; }
-        else dg = fabs(a * 1 / h * s);
+        if (m1 != col + 1 && m1 != 0) { other = m1 - 1; off = q * s; dg = -q * s; }
+        else if (m2 != col + 1 && m2 != 0) { other = m2 - 1; off = -q * s; dg = q * s; }
+        else dg = fabs(q * s);
     } else {
         double ep = c.epsn[inz];
-        if (m1 != col + 1 && m1 != 0) { other = m1 - 1; off = a * 1 / h * ep * c.eps0; dg = a * (-1) / h * ep * c.eps0; }
-        else if (m2 != col + 1 && m2 != 0) { other = m2 - 1; off = a * (-1) / h * ep * c.eps0; dg = a * 1 / h * ep * c.eps0; }
-        else dg = fabs(a * 1 / h * ep * c.eps0);
+        if (m1 != col + 1 && m1 != 0) { other = m1 - 1; off = q * ep * c.eps0; dg = -q * ep * c.eps0; }
+        else if (m2 != col + 1 && m2 != 0) { other = m2 - 1; off = -q * ep * c.eps0; dg = q * ep * c.eps0; }
+        else dg = fabs(q * ep * c.eps0);
     }
     return true;
 }
@@ -613,6 +637,22 @@ g2p_status g2p_run_v0(g2p_mesh *m) {
     const Dims &d = m->d;
     cudaStream_t s = m->stream;
     V0Ctx c = make_ctx(m);
+    {
+        // per-line tables, kept with the mesh
+        const int64_t nl = 3 * (d.nx + d.ny + d.nz), na = d.nx * d.ny + d.ny * d.nz + d.nx * d.nz;
+        dfree(m->v0_tab, s);
+        G2P_TRY(dalloc(&m->v0_tab, 3 * nl + na, s));
+        double *t = m->v0_tab;
+        double *ivx = t, *ivy = ivx + d.nx, *ivz = ivy + d.ny;
+        double *lx = ivz + d.nz, *ly = lx + d.nx, *lz = ly + d.ny;
+        double *ilx = lz + d.nz, *ily = ilx + d.nx, *ilz = ily + d.ny;
+        double *axy = ilz + d.nz, *ayz = axy + d.nx * d.ny, *axz = ayz + d.ny * d.nz;
+        const int64_t nmax = std::max(d.nx, std::max(d.ny, d.nz));
+        (g2p::kbegin("k_v0_lines", s), k_v0_lines<<<dim3(grid_for(nmax), 3), kThreads, 0, s>>>(c, ivx, ivy, ivz, lx, ly, lz, ilx, ily, ilz), g2p::kend(s));
+        (g2p::kbegin("k_v0_areas", s), k_v0_areas<<<grid_for(na), kThreads, 0, s>>>(c, lx, ly, lz, axy, ayz, axz), g2p::kend(s));
+        c.ivx = ivx; c.ivy = ivy; c.ivz = ivz; c.ilx = ilx; c.ily = ily; c.ilz = ilz;
+        c.axy = axy; c.ayz = ayz; c.axz = axz;
+    }
     const int64_t ncdt = m->num_cdt;
     // ---- conductor node lists grouped by conductor, node order kept
     int64_t *pos;
