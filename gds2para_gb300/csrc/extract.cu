@@ -115,6 +115,54 @@ __global__ void __launch_bounds__(256) k_v0t_long(const int32_t *cols, int k, co
     }
 }
 
+// Columns longer than kHugeRow: one block per chunk of kLongChunk entries
+// (threadIdx.x = right-hand side, threadIdx.y strides over the entries);
+// the block that finishes a column's last chunk adds the column's partials
+// in chunk order and writes out.
+__global__ void __launch_bounds__(256) k_v0t_chunk(const int32_t *cols, const int32_t *crow, const int64_t *cbeg,
+                                                   const int64_t *rcp, int k, const int64_t *cptr,
+                                                   const int32_t *cedge, const double *caval, const double *src,
+                                                   EdgeFactor f, double *partial, int32_t *done, double *out) {
+    __shared__ double sm[256];
+    __shared__ int last;
+    const int r = threadIdx.x, ty = threadIdx.y, ny = blockDim.y;
+    const int l = crow[blockIdx.x];
+    const int64_t c = cols[l];
+    const int64_t q0 = cbeg[blockIdx.x], q1 = min(q0 + (int64_t)kLongChunk, cptr[c + 1]);
+    double acc = 0.0;
+    if (r < k)
+        for (int64_t q = q0 + ty; q < q1; q += ny) {
+            const int64_t e = cedge[q];
+            acc += caval[q] * f(e, src[e * k + r]);
+        }
+    sm[ty * blockDim.x + r] = acc;
+    __syncthreads();
+    if (ty == 0 && r < k) {
+        double t = 0;
+        for (int q = 0; q < ny; q++) t += sm[q * blockDim.x + r];
+        partial[(int64_t)blockIdx.x * kMaxRhs + r] = t;
+    }
+    __threadfence();
+    __syncthreads();
+    if (r == 0 && ty == 0) {
+        const int nch = (int)(rcp[l + 1] - rcp[l]);
+        last = atomicAdd(&done[l], 1) == nch - 1;
+        if (last) done[l] = 0;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double t = 0;
+    if (r < k)
+        for (int64_t ch = rcp[l] + ty; ch < rcp[l + 1]; ch += ny) t += __ldcg(partial + ch * kMaxRhs + r);
+    sm[ty * blockDim.x + r] = t;
+    __syncthreads();
+    if (ty != 0 || r >= k) return;
+    double u = 0;
+    for (int q = 0; q < ny; q++) u += sm[q * blockDim.x + r];
+    out[c * k + r] = u;
+}
+
 __global__ void k_add(int64_t n, double *a, const double *b) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] += b[i];
 }
@@ -248,8 +296,9 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         tmp.n = m->v0d.ncol; tmp.ptr = m->v0d.cptr;
         G2P_TRY(find_long_rows<double>(tmp, lcol, s));
     }
-    int32_t *d_long_d = lcol.rows;
-    int64_t nlong_d = lcol.n;
+    // long V0d columns: up to kHugeRow entries one block each, longer ones in chunks
+    const int32_t *d_mid_d = lcol.mid;
+    const int64_t nmid_d = lcol.nmid;
     const int kb = p.batch ? std::min(P, kMaxRhs) : 1;
     const int64_t nd = m->v0d.ncol, nc = m->v0c.ncol, ne = d.N_edge;
     double *Bd, *Yd, *Bc, *Yc, *crhs, *yd1, *yc, *yd2, *zre, *zim;
@@ -299,8 +348,10 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         // (5) yc = V0c y0c ; b_d2 = V0da^T(-D_eps yc)
         (g2p::kbegin("k_v0_apply", s), k_v0_apply<<<row_grid(ne, kk), row_block(kk), 0, s>>>(ne, kk, m->v0c.ecol, m->v0c.eval, Yc, yc), g2p::kend(s));
         (g2p::kbegin("k_v0t_short", s), k_v0t_short<<<row_grid(nd, kk), row_block(kk), 0, s>>>(nd, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd), g2p::kend(s));
-        if (nlong_d > 0)
-            (g2p::kbegin("k_v0t_long", s), k_v0t_long<<<(unsigned)nlong_d, 256, 0, s>>>(d_long_d, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd), g2p::kend(s));
+        if (nmid_d > 0)
+            (g2p::kbegin("k_v0t_long", s), k_v0t_long<<<(unsigned)nmid_d, 256, 0, s>>>(d_mid_d, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd), g2p::kend(s));
+        if (lcol.nchunk > 0)
+            (g2p::kbegin("k_v0t_chunk", s), k_v0t_chunk<<<(unsigned)lcol.nchunk, row_block(kk), 0, s>>>(lcol.rows, lcol.crow, lcol.cbeg, lcol.rcp, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, lcol.partial, lcol.done, Bd), g2p::kend(s));
         // (6) Ad y0d2 = b_d2 ; yd2 = V0d y0d2
         rc = g2p_solver_solve_dev(Sd, Bd, Yd, kk, &ss);
         if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }

@@ -22,6 +22,7 @@ namespace g2p {
 
 __global__ void k_max_abs_diag(const int64_t *ptr, const int32_t *col, const double *val, int64_t n,
                                unsigned long long *mx) {
+    unsigned long long m = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int64_t lo = ptr[i], hi = ptr[i + 1] - 1, q = -1;
         while (lo <= hi) {
@@ -30,8 +31,18 @@ __global__ void k_max_abs_diag(const int64_t *ptr, const int32_t *col, const dou
             if (col[mid] < i) lo = mid + 1; else hi = mid - 1;
         }
         if (q < 0) for (int64_t t = ptr[i]; t < ptr[i + 1]; t++) if (col[t] == i) { q = t; break; }
-        if (q >= 0) atomicMax(mx, (unsigned long long)__double_as_longlong(fabs(val[q])));
+        if (q >= 0) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(val[q]));
+            m = b > m ? b : m;
+        }
     }
+    // non-negative doubles order like their bits: one atomic per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, m, o);
+        m = w > m ? w : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(mx, m);
 }
 
 __global__ void k_scale_vals(const double *val, int64_t nnz, double c, double *out) {

@@ -195,6 +195,53 @@ __global__ void __launch_bounds__(256) k_spmm_ell(int64_t n, int w, const int32_
     }
 }
 
+// Uniform layout of width w <= kSellUnroll, persistent and software
+// pipelined: each thread walks row groups with a grid stride and issues the
+// next group's column and value loads before the current group's x gathers,
+// so one memory round trip per group is exposed instead of two.
+template <class T, int V>
+__global__ void __launch_bounds__(256) k_spmm_ell_pipe(int64_t n, int w, const int32_t *__restrict__ scol,
+                                                       const T *__restrict__ sval, const T *__restrict__ x,
+                                                       T *__restrict__ y, int k, const T *__restrict__ b) {
+    const int xo = threadIdx.x * V;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.y;
+    int64_t i = blockIdx.x * (int64_t)blockDim.y + threadIdx.y;
+    int32_t c[kSellUnroll];
+    T a[kSellUnroll];
+    auto fetch = [&](int64_t r) {
+        const int64_t base = 32 * (int64_t)w * (r >> 5) + (r & 31);
+#pragma unroll
+        for (int u = 0; u < kSellUnroll; u++) {
+            const bool in = u < w;
+            c[u] = in ? __ldg(scol + base + 32 * (int64_t)u) : (int32_t)r;
+            a[u] = in ? __ldg(sval + base + 32 * (int64_t)u) : T(0);
+        }
+    };
+    if (i < n) fetch(i);
+    for (; i < n; i += stride) {
+        XVec<T, V> xv[kSellUnroll];
+#pragma unroll
+        for (int u = 0; u < kSellUnroll; u++) xv[u].load(x + (int64_t)c[u] * k + xo);
+        T av[kSellUnroll];
+#pragma unroll
+        for (int u = 0; u < kSellUnroll; u++) av[u] = a[u];
+        XVec<T, V> bv;
+        if (b) bv.load(b + i * k + xo);
+        if (i + stride < n) fetch(i + stride);
+        T acc[V];
+#pragma unroll
+        for (int q = 0; q < V; q++) acc[q] = 0;
+#pragma unroll
+        for (int u = 0; u < kSellUnroll; u++)
+#pragma unroll
+            for (int q = 0; q < V; q++) acc[q] += av[u] * xv[u].v[q];
+        XVec<T, V> out;
+#pragma unroll
+        for (int q = 0; q < V; q++) out.v[q] = b ? bv.v[q] - acc[q] : acc[q];
+        out.store(y + i * k + xo);
+    }
+}
+
 // Padding of the uniform layout: (column = row, value = 0) in every slot a
 // row does not use, and in all slots of long rows.
 template <class T>
@@ -383,6 +430,16 @@ static int sell_vec(int k) {
     return v;
 }
 
+// G2P_ELL_PIPE=0 selects the one-group-per-block kernel (for comparisons).
+static bool pipe_ok() {
+    static int on = -1;
+    if (on < 0) {
+        const char *e = getenv("G2P_ELL_PIPE");
+        on = e ? atoi(e) != 0 : 1;
+    }
+    return on != 0;
+}
+
 template <class T, int V>
 static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cudaStream_t s) {
     // one block per 256 / tpr rows, never grid-strided: blocks retire in row
@@ -393,7 +450,19 @@ static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cu
     int64_t g = (A.n + rows - 1) / rows;
     if (g > 0x7fffffffLL) g = 0x7fffffffLL;
     if (g < 1) g = 1;
-    if (A.ell_w > 0)
+    if (A.ell_w > 0 && A.ell_w <= kSellUnroll && pipe_ok()) {
+        // persistent: as many blocks as fit on the SMs at once
+        static int resident = 0;
+        if (!resident) {
+            int per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmm_ell_pipe<T, V>, tpr * rows, 0);
+            resident = (per_sm > 0 ? per_sm : 4) * kSMs;
+        }
+        const int64_t gp = std::min<int64_t>(g, resident);
+        (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_sell<f64>" : "k_spmm_sell<f32>", s),
+         k_spmm_ell_pipe<T, V><<<(unsigned)gp, dim3(tpr, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b),
+         g2p::kend(s));
+    } else if (A.ell_w > 0)
         (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_sell<f64>" : "k_spmm_sell<f32>", s),
          k_spmm_ell<T, V><<<(unsigned)g, dim3(tpr, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b),
          g2p::kend(s));
@@ -851,8 +920,20 @@ __global__ void k_diag(int64_t n, const int64_t *ptr, const int32_t *col, const 
 
 // 1/a_ii and the Gershgorin radius max_i sum_j |a_ij| / |a_ii| of D^-1 A;
 // rows longer than kLongRow are summed by k_gersh_long.
+// Non-negative doubles order like their bit patterns, so a maximum can be
+// kept as an unsigned integer; one atomic per warp.
+__device__ __forceinline__ void warp_atomic_max(unsigned long long *dst, unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    if ((threadIdx.x & 31) == 0 && v) atomicMax(dst, v);
+}
+
 __global__ void k_dinv_gersh(int64_t n, const int64_t *ptr, const double *val, const double *diag, double *dinv,
                              unsigned long long *lmax_bits) {
+    unsigned long long m = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double d = diag[i];
         if (d == 0.0) d = 1.0;
@@ -860,8 +941,10 @@ __global__ void k_dinv_gersh(int64_t n, const int64_t *ptr, const double *val, c
         if (ptr[i + 1] - ptr[i] > kLongRow) continue;
         double s = 0;
         for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) s += fabs(val[q]);
-        atomicMax(lmax_bits, (unsigned long long)__double_as_longlong(s / fabs(d)));
+        const unsigned long long b = (unsigned long long)__double_as_longlong(s / fabs(d));
+        m = b > m ? b : m;
     }
+    warp_atomic_max(lmax_bits, m);
 }
 
 __global__ void __launch_bounds__(256) k_gersh_long(const int32_t *rows, const int64_t *ptr, const double *val,
@@ -1108,42 +1191,54 @@ __global__ void k_dense_fill(int64_t n, const int64_t *ptr, const int32_t *col, 
 }
 
 // Gauss-Jordan inverse with partial pivoting in one block (n <= a few 1000).
-__global__ void __launch_bounds__(1024) k_gauss_jordan(double *a, double *inv, int64_t n, int *singular) {
-    __shared__ int64_t piv;
-    __shared__ double pval;
-    for (int64_t i = threadIdx.x; i < n * n; i += blockDim.x) inv[i] = (i / n == i % n) ? 1.0 : 0.0;
+// Gauss-Jordan inversion with partial pivoting, one launch per pivot step
+// over the whole GPU.  Step kk reads (a_in, inv_in) and writes (a_out,
+// inv_out), so no block waits on another: block i owns row i, repeats the
+// (cheap) pivot search of column kk itself -- largest |a_ik|, i >= kk, the
+// first one on ties -- and writes its row after the swap of rows kk and p
+// and the elimination.  Columns of a at or left of kk are never read again
+// and are not written.
+__global__ void __launch_bounds__(256) k_gj_step(const double *__restrict__ a_in, const double *__restrict__ inv_in,
+                                                 double *__restrict__ a_out, double *__restrict__ inv_out, int64_t n,
+                                                 int64_t kk, int *singular) {
+    __shared__ double bv[256];
+    __shared__ int64_t bi[256];
+    const int t = threadIdx.x;
+    double mv = -1.0;
+    int64_t mi = n;
+    for (int64_t r = kk + t; r < n; r += blockDim.x) {
+        const double v = fabs(a_in[r * n + kk]);
+        if (v > mv) { mv = v; mi = r; }
+    }
+    bv[t] = mv; bi[t] = mi;
     __syncthreads();
-    for (int64_t kk = 0; kk < n; kk++) {
-        if (threadIdx.x == 0) {
-            int64_t p = kk;
-            double mx = fabs(a[kk * n + kk]);
-            for (int64_t i = kk + 1; i < n; i++) if (fabs(a[i * n + kk]) > mx) { mx = fabs(a[i * n + kk]); p = i; }
-            piv = p;
-            pval = a[p * n + kk];
-            if (pval == 0.0) { *singular = 1; pval = 1e-300; }
-        }
+    for (int o = 128; o > 0; o >>= 1) {
+        if (t < o && (bv[t + o] > bv[t] || (bv[t + o] == bv[t] && bi[t + o] < bi[t]))) { bv[t] = bv[t + o]; bi[t] = bi[t + o]; }
         __syncthreads();
-        int64_t p = piv;
-        if (p != kk)
-            for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
-                double t = a[kk * n + j]; a[kk * n + j] = a[p * n + j]; a[p * n + j] = t;
-                t = inv[kk * n + j]; inv[kk * n + j] = inv[p * n + j]; inv[p * n + j] = t;
-            }
-        __syncthreads();
-        double pv = pval;
-        for (int64_t j = threadIdx.x; j < n; j += blockDim.x) { a[kk * n + j] /= pv; inv[kk * n + j] /= pv; }
-        __syncthreads();
-        for (int64_t idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-            int64_t i = idx / n, j = idx - i * n;
-            if (i == kk) continue;
-            double f = a[i * n + kk];
-            if (f == 0.0) continue;
-            if (j != kk) a[i * n + j] -= f * a[kk * n + j];
-            inv[i * n + j] -= f * inv[kk * n + j];
-        }
-        __syncthreads();
-        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) if (i != kk) a[i * n + kk] = 0.0;
-        __syncthreads();
+    }
+    const int64_t p = bi[0];
+    double pval = a_in[p * n + kk];
+    if (pval == 0.0) {
+        if (blockIdx.x == 0 && t == 0) *singular = 1;
+        pval = 1e-300;
+    }
+    const int64_t i = blockIdx.x;
+    const int64_t src = i == kk ? p : (i == p ? kk : i);     // row i after the swap
+    const double f = i == kk ? 0.0 : a_in[src * n + kk];
+    for (int64_t c = kk + 1 + t; c < n; c += blockDim.x) {
+        const double pr = a_in[p * n + c] / pval;
+        a_out[i * n + c] = i == kk ? pr : a_in[src * n + c] - f * pr;
+    }
+    for (int64_t c = t; c < n; c += blockDim.x) {
+        const double pr = inv_in[p * n + c] / pval;
+        inv_out[i * n + c] = i == kk ? pr : inv_in[src * n + c] - f * pr;
+    }
+}
+
+__global__ void k_identity(double *m, int64_t n) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = t / n;
+        m[t] = (t - r * n == r) ? 1.0 : 0.0;
     }
 }
 
@@ -1507,15 +1602,27 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             Level<double> &Cl = H.lv[l];
             int64_t nn = Cl.n;
             H.nc = nn;
-            if (nn > kMaxDenseCoarse) break;   // coarsest level solved by smoothing
+            if (nn > kMaxDenseCoarse || nn == 0) break;   // coarsest level solved by smoothing
             double *Dm;
             G2P_TRY(dalloc(&Dm, nn * nn, s));
             G2P_TRY(dalloc(&H.cinv, nn * nn, s));
             G2P_CUDA(cudaMemsetAsync(Dm, 0, sizeof(double) * nn * nn, s));
             (g2p::kbegin("k_dense_fill", s), k_dense_fill<<<grid_for(nn), kThreads, 0, s>>>(nn, Cl.A.ptr, Cl.A.col, Cl.A.val, Dm), g2p::kend(s));
             G2P_CUDA(cudaMemsetAsync(d_int, 0, sizeof(int), s));
-            (g2p::kbegin("k_gauss_jordan", s), k_gauss_jordan<<<1, 1024, 0, s>>>(Dm, H.cinv, nn, d_int), g2p::kend(s));
-            G2P_CUDA(cudaStreamSynchronize(s));
+            {
+                double *a1, *i0, *i1;
+                G2P_TRY(dalloc(&a1, nn * nn, s)); G2P_TRY(dalloc(&i0, nn * nn, s)); G2P_TRY(dalloc(&i1, nn * nn, s));
+                (g2p::kbegin("k_identity", s), k_identity<<<grid_for(nn * nn), kThreads, 0, s>>>(i0, nn), g2p::kend(s));
+                double *ain = Dm, *aout = a1, *iin = i0, *iout = i1;
+                for (int64_t kk = 0; kk < nn; kk++) {
+                    (g2p::kbegin("k_gj_step", s), k_gj_step<<<(unsigned)nn, 256, 0, s>>>(ain, iin, aout, iout, nn, kk, d_int), g2p::kend(s));
+                    std::swap(ain, aout);
+                    std::swap(iin, iout);
+                }
+                G2P_CUDA(cudaMemcpyAsync(H.cinv, iin, sizeof(double) * nn * nn, cudaMemcpyDeviceToDevice, s));
+                G2P_CUDA(cudaStreamSynchronize(s));
+                dfree(a1, s); dfree(i0, s); dfree(i1, s);
+            }
             dfree(Dm, s);
             pc_.mark("coarse inverse", l, s);
             break;

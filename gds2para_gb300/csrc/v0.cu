@@ -445,31 +445,38 @@ __global__ void k_seg_sum(const uint64_t *keys, const double *vals, int64_t nseg
 }
 
 // The same ordered sum for segments longer than kSegWarp, one warp per
-// segment: the lanes load 32 x 8 consecutive values at a time and every lane
-// adds them left to right from the broadcasts, so the result is the
-// sequential sum.
-__global__ void k_seg_sum_long(const uint64_t *keys, const double *vals, int64_t nseg, const int64_t *sstart,
-                               uint64_t *okey, double *oval, int64_t *keep) {
-    const int lane = threadIdx.x & 31;
+// segment: the lanes stage 256 consecutive values in shared memory with
+// coalesced loads, then lane 0 adds them left to right, so the result is the
+// sequential sum and the dependent chain holds only the additions.
+__global__ void __launch_bounds__(256) k_seg_sum_long(const uint64_t *keys, const double *vals, int64_t nseg,
+                                                      const int64_t *sstart, uint64_t *okey, double *oval,
+                                                      int64_t *keep) {
+    __shared__ double stage[8][256];
+    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    double *st = stage[wi];
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t sg = warp; sg < nseg; sg += nwarp) {
         const int64_t b = sstart[sg], e = sstart[sg + 1];
         if (e - b <= kSegWarp) continue;
         double s = 0.0;
-        for (int64_t j0 = b; j0 < e; j0 += 32 * 8) {
-            double v[8];
+        for (int64_t j0 = b; j0 < e; j0 += 256) {
+            const int cnt = e - j0 >= 256 ? 256 : (int)(e - j0);
 #pragma unroll
             for (int u = 0; u < 8; u++) {
-                const int64_t j = j0 + 32 * u + lane;
-                v[u] = j < e ? vals[j] : 0.0;
+                const int t = 32 * u + lane;
+                if (t < cnt) st[t] = vals[j0 + t];
             }
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const int64_t jb = j0 + 32 * u;
-                const int cnt = e - jb >= 32 ? 32 : (int)(e - jb);
-                for (int t = 0; t < cnt; t++) s += __shfl_sync(0xffffffffu, v[u], t);
+            __syncwarp();
+            if (lane == 0) {
+                if (cnt == 256) {
+#pragma unroll 16
+                    for (int t = 0; t < 256; t++) s += st[t];
+                } else {
+                    for (int t = 0; t < cnt; t++) s += st[t];
+                }
             }
+            __syncwarp();
         }
         if (lane == 0) {
             okey[sg] = keys[b];
