@@ -31,11 +31,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "port-freq solves/s at 1e-6 rel Z err, mixed+batched vs FP64 GPU; p50/p99 job ms"
 UNIT = "port-freq solves/s"
-RTOL = {"c1": 1e-10, "c2": 1e-8, "c3": 1e-8}
+RTOL = {"c1": 1e-10, "c2": 1e-8, "c3": 1e-8, "c4": 1e-8}
 WORKLOAD = {
     "c1": "microstrip 101x41x11 nodes at 1 um, 1 port, 1 GHz, rtol 1e-10",
     "c2": "random Manhattan 512x512x24 nodes, 4 metal layers x 64 wires, 8 ports, 10 GHz, rtol 1e-8",
     "c3": "microstrip stack 256x256x16 nodes, 32 strips/ports x 64 log-spaced points 1e7..1e11 Hz, rtol 1e-8",
+    "c4": "served stream of 48 random Manhattan jobs (sides log-uniform 64..384, nz 10..16, 1..8 ports, 1..16 "
+          "log-spaced points 1e8..1e10 Hz), Poisson arrivals at 0.8 x the serial capacity, 150 GB budget, rtol 1e-8",
 }
 
 
@@ -208,8 +210,11 @@ def run_gb300(args):
     clocks = Clocks(local)
     clocks.start()
     step_ms = []
-    ms, launches, kern = timed(dev, args.steps, profile=True, per_step=step_ms)
+    ms, launches, _ = timed(dev, args.steps, per_step=step_ms)
     clk = clocks.stop()
+    # kernel-level figures from separate profiled steps (events around every
+    # launch add overhead, so they stay out of the timed region above)
+    _, _, kern = timed(dev, max(1, min(args.steps, 2)), profile=True)
     ms_e2e, _, _ = timed(pin, max(1, min(args.steps, 3)))
     # accuracy of this run's Z against the plain FP64 GPU method, and that
     # method's own speed (FP64 throughout, one port at a time), untimed above
@@ -297,6 +302,91 @@ def run_gb300(args):
     return out, rank
 
 
+def c4_jobs(n=48, seed=1004):
+    """The served workload: seeded random Manhattan layouts of mixed sizes."""
+    from gds2para_gb300 import layout
+    rng = np.random.default_rng(seed)
+    jobs = []
+    while len(jobs) < n:
+        side = int(round(np.exp(rng.uniform(np.log(64), np.log(384)))))
+        nz = int(rng.choice([10, 12, 16]))
+        ports = int(rng.integers(1, 9))
+        nfreq = int(rng.integers(1, 17))
+        try:
+            lay = layout.manhattan(nx=side, ny=side, nz=nz, n_metal=3 if nz < 16 else 4,
+                                   wires_per_layer=max(8, side // 8), n_ports=ports, seed=int(rng.integers(1 << 30)),
+                                   lmin=max(6, side // 16), lmax=max(12, side // 3), freq_start=1e8, freq_end=1e10,
+                                   freq_unit=1.0, nfreq=nfreq, freq_scale=0 if nfreq > 1 else 1)
+            jobs.append(layout.build(lay))
+        except (ValueError, RuntimeError):
+            continue
+    return jobs
+
+
+def run_c4(args):
+    """Continuous batching: jobs arrive (Poisson) while others run; the
+    service admits them by memory footprint and runs up to 8 at once."""
+    import torch
+    from gds2para_gb300 import api
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    jobs = c4_jobs()
+    params = api.default_params(precision=args.precision, batch=args.batch, rtol=RTOL["c4"])
+    units = sum(d.num_ports * d.nfreq for d in jobs)
+    budget = 150 << 30
+    # serial pass (one job at a time; also the warm-up): capacity of the GPU
+    with api.Server(budget, max_active=1) as srv:
+        t0 = time.perf_counter()
+        ids = [srv.submit(d, params) for d in jobs]
+        for j in ids:
+            srv.wait(j)
+        serial_s = time.perf_counter() - t0
+    # saturated pass: every job queued at once; throughput of the service
+    clocks = Clocks(local)
+    clocks.start()
+    with api.Server(budget, max_active=8) as srv:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ids = [srv.submit(d, params) for d in jobs]
+        sat = [srv.wait(j) for j in ids]
+        torch.cuda.synchronize()
+        sat_s = time.perf_counter() - t0
+    clk = clocks.stop()
+    # latency pass: Poisson arrivals at 0.8 x the serial capacity
+    rate = 0.8 * len(jobs) / serial_s
+    gaps = np.random.default_rng(4).exponential(1.0 / rate, size=len(jobs))
+    with api.Server(budget, max_active=8) as srv:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ids = []
+        for d, g in zip(jobs, gaps):
+            time.sleep(g)
+            ids.append(srv.submit(d, params))
+        res = [srv.wait(j) for j in ids]
+        torch.cuda.synchronize()
+        span = time.perf_counter() - t0
+    lat = sorted(t.total_ms for _, _, t in res)
+    pct = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]
+    overlapped = sum(1 for _, _, t in res if not t.ran_alone)
+    out = {
+        "metric": METRIC, "value": units / sat_s, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": 1e3 * sat_s, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic (seeded layout generator)",
+        "config": {"workload": WORKLOAD["c4"], "config": "c4", "jobs": len(jobs), "port_freq_columns": units,
+                   "arrival_rate_per_s": rate, "max_active": 8, "budget_bytes": budget,
+                   "l2": "each job's inputs are resident only while it runs"},
+        "job_ms": {"p50": pct(0.5), "p99": pct(0.99), "max": lat[-1],
+                   "load": "Poisson arrivals at 0.8 x serial capacity", "arrival_span_s": span,
+                   "jobs_overlapped": overlapped},
+        "serial": {"value": units / serial_s, "seconds": serial_s, "what": "same jobs, one at a time"},
+        "served_over_serial": serial_s / sat_s,
+        "clocks": clk,
+        "e2e": {"value": units / sat_s, "unit": UNIT, "note": "jobs submitted from host arrays; Z read back per job",
+                "h2d_bytes_per_step": None, "d2h_bytes_per_step": int(sum(16 * d.nfreq * d.num_ports ** 2 for d in jobs))},
+    }
+    return out, rank
+
+
 def cpu_sample(d, rtol, O=None, fixed=None):
     """One bounded sample of the job on the host with the oracle/ C
     restatement of the reference's path (single thread): generateStiff and
@@ -341,6 +431,9 @@ def run_reference(args):
         return None, rank
     from gds2para_gb300 import layout
     from oracle.harness import COracle
+    if args.config == "c4":
+        return {"impl": "reference", "unavailable": "the reference extracts one layout per process and has no "
+                                                    "service to time on a job stream"}, rank
     d = layout.build(layout.config(args.config))
     O = COracle()
     rtol = RTOL[args.config]
@@ -375,6 +468,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         out, rank = run_reference(args)
+    elif args.config == "c4":
+        out, rank = run_c4(args)
     else:
         out, rank = run_gb300(args)
     if rank == 0 and out is not None:

@@ -19,6 +19,7 @@ EXPORTS = [
     "g2p_hypre_solve", "g2p_solver_create", "g2p_solver_solve", "g2p_solver_destroy",
     "g2p_para_generator", "g2p_launch_count", "g2p_profile_begin", "g2p_profile_end", "g2p_profile_report",
     "g2p_map_edge_noalloc", "g2p_profile_buckets",
+    "g2p_server_create", "g2p_server_submit", "g2p_server_wait", "g2p_server_destroy",
 ]
 
 STATUS = {0: "G2P_OK", 1: "G2P_ERR_INVALID", 2: "G2P_ERR_CUDA", 3: "G2P_ERR_NOMEM", 4: "G2P_ERR_NOT_CONVERGED",
@@ -62,6 +63,11 @@ class ExtractStats(C.Structure):
                 ("max_rel_residual", C.c_double), ("assembly_ms", C.c_double), ("setup_ms", C.c_double),
                 ("solve_ms", C.c_double), ("total_ms", C.c_double), ("ad_levels", C.c_int32),
                 ("ac_levels", C.c_int32)]
+
+
+class JobTimes(C.Structure):
+    _fields_ = [("queued_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double),
+                ("footprint_estimate", C.c_int64), ("footprint_measured", C.c_int64), ("ran_alone", C.c_int32)]
 
 
 class G2PError(RuntimeError):
@@ -113,6 +119,10 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_profile_end.argtypes = [C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)]
     L.g2p_profile_report.restype = C.c_int64
     L.g2p_profile_report.argtypes = [C.c_char_p, i64]
+    L.g2p_server_create.argtypes = [i64, i32, C.POINTER(vp)]
+    L.g2p_server_submit.argtypes = [vp, C.POINTER(MeshDescC), C.POINTER(SolverParams), C.POINTER(i64)]
+    L.g2p_server_wait.argtypes = [vp, i64, vp, C.POINTER(ExtractStats), C.POINTER(JobTimes)]
+    L.g2p_server_destroy.argtypes = [vp]
     L.g2p_profile_buckets.restype = None
     L.g2p_profile_buckets.argtypes = [C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)]
     L.g2p_map_edge_noalloc.argtypes = [i64, i64, i64, vp, vp, i64, vp, vp, vp]

@@ -190,4 +190,64 @@ def paraGenerator(sys: FdtdMesh, params: Optional[SolverParams] = None):
     return zc.reshape(d.nfreq, d.num_ports, d.num_ports), st
 
 
-__all__ = ["FdtdMesh", "generateStiff", "hypreSolve", "paraGenerator", "Solver", "default_params", "G2PError"]
+__all__ = ["FdtdMesh", "generateStiff", "hypreSolve", "paraGenerator", "Solver", "Server", "default_params",
+           "G2PError"]
+
+
+class Server:
+    """Extraction service over the C ABI (g2p_server_*): jobs are queued,
+    admitted onto the GPU while their device-memory estimate fits the budget
+    and fewer than max_active run, and run concurrently, each on its own
+    stream.  No counterpart in the reference, which extracts one layout per
+    process."""
+
+    def __init__(self, mem_budget_bytes: int, max_active: int = 4):
+        h = C.c_void_p()
+        check(_lib.load().g2p_server_create(int(mem_budget_bytes), int(max_active), C.byref(h)))
+        self.handle = h
+        self._pending = {}
+
+    def submit(self, desc: MeshDesc, params: Optional[SolverParams] = None) -> int:
+        keep, cdesc = _pack_desc(desc)      # copied by the library before submit returns
+        job = C.c_int64()
+        check(_lib.load().g2p_server_submit(self.handle, C.byref(cdesc), C.byref(params) if params else None,
+                                            C.byref(job)))
+        self._pending[job.value] = desc
+        return job.value
+
+    def wait(self, job: int, allow_unconverged: bool = False):
+        desc = self._pending.pop(job)
+        z = np.zeros(2 * desc.nfreq * desc.num_ports * desc.num_ports)
+        st = ExtractStats()
+        t = _lib.JobTimes()
+        allow = (_lib.G2P_OK, _lib.G2P_ERR_NOT_CONVERGED) if allow_unconverged else (_lib.G2P_OK,)
+        check(_lib.load().g2p_server_wait(self.handle, job, z.ctypes.data, C.byref(st), C.byref(t)), allow)
+        zc = z[0::2] + 1j * z[1::2]
+        return zc.reshape(desc.nfreq, desc.num_ports, desc.num_ports), st, t
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().g2p_server_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def _pack_desc(desc: MeshDesc):
+    keep = dict(
+        xn=_c(desc.xn, np.float64), yn=_c(desc.yn, np.float64), zn=_c(desc.zn, np.float64),
+        se=_c(desc.stack_epsn, np.float64), ss=_c(desc.stack_sign, np.float64),
+        mn=_c(desc.mark_node, np.int64), me=_c(desc.mark_edge, np.int64),
+        mp=_c(desc.mark_port, np.int32), cr=_c(desc.cdt_return, np.uint8),
+        psp=_c(desc.port_side_ptr, np.int32), sep=_c(desc.side_edge_ptr, np.int64),
+        sed=_c(desc.side_edges, np.int64), sa=_c(desc.side_area, np.float64), sd=_c(desc.side_dir, np.int32))
+    p = lambda n: keep[n].ctypes.data
+    cdesc = _lib.MeshDescC(desc.nx, desc.ny, desc.nz, p("xn"), p("yn"), p("zn"), p("se"), p("ss"),
+                           p("mn"), p("me"), desc.num_cdt, p("mp"), p("cr"), desc.num_ports, p("psp"),
+                           p("sep"), p("sed"), p("sa"), p("sd"), desc.freq_start, desc.freq_end,
+                           desc.freq_unit, desc.nfreq, desc.freq_scale)
+    return keep, cdesc

@@ -24,16 +24,19 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
 
 namespace g2p {
 
-// B[c, r] += aval * J over the port edges of the block (matrixCon.cpp:384, 436)
-__global__ void k_rhs_ports(int64_t nent, const int32_t *pe_edge, const int32_t *pe_port, const double *pe_J,
+// B[c, r] += aval * J over the port edges of the block (matrixCon.cpp:384,
+// 436).  One thread per port adds its edges in their fixed order, so the
+// sums are the same on every run; ports write disjoint entries of B.
+__global__ void k_rhs_ports(int kk, const int64_t *pptr, const int32_t *pe_edge, const double *pe_J,
                             const int32_t *ecol, const double *eaval, int k, double *B) {
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nent; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t e = pe_edge[t];
-        int r = pe_port[t];
-        double J = pe_J[t];
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= kk) return;
+    for (int64_t t = pptr[r]; t < pptr[r + 1]; t++) {
+        const int64_t e = pe_edge[t];
+        const double J = pe_J[t];
         for (int s = 0; s < 2; s++) {
-            int32_t c = ecol[2 * e + s];
-            if (c >= 0) atomicAdd(&B[(int64_t)c * k + r], eaval[2 * e + s] * J);
+            const int32_t c = ecol[2 * e + s];
+            if (c >= 0) B[(int64_t)c * k + r] += eaval[2 * e + s] * J;
         }
     }
 }
@@ -246,7 +249,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     local.assembly_ms = ms_since(t0);
     // ---- port data: J entries (last side wins, matrixCon.cpp:367-374),
     //      response edges (side 0) and source currents
-    std::vector<int32_t> pe_edge, pe_port;
+    std::vector<int32_t> pe_edge;
     std::vector<double> pe_J, cur(P, 0.0);
     std::vector<int64_t> pptr(P + 1, 0), rptr(P + 1, 0);
     std::vector<int32_t> redge, rdir(P);
@@ -256,18 +259,19 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
             for (int64_t j = m->side_edge_ptr[sd]; j < m->side_edge_ptr[sd + 1]; j++) J[m->side_edges[j]] = m->side_dir[sd];
             cur[q] += m->side_area[sd];
         }
-        for (auto &kv : J) { pe_edge.push_back((int32_t)kv.first); pe_port.push_back(q); pe_J.push_back((double)kv.second); }
+        for (auto &kv : J) { pe_edge.push_back((int32_t)kv.first); pe_J.push_back((double)kv.second); }
         pptr[q + 1] = (int64_t)pe_edge.size();
         int s0 = m->port_side_ptr[q];
         for (int64_t j = m->side_edge_ptr[s0]; j < m->side_edge_ptr[s0 + 1]; j++) redge.push_back((int32_t)m->side_edges[j]);
         rptr[q + 1] = (int64_t)redge.size();
         rdir[q] = m->side_dir[s0];
     }
-    int32_t *d_pe_edge, *d_pe_port, *d_redge, *d_rdir;
+    int32_t *d_pe_edge, *d_redge, *d_rdir;
     double *d_pe_J, *d_cur;
-    int64_t *d_rptr;
+    int64_t *d_rptr, *d_pptr;
     int64_t npe = (int64_t)pe_edge.size();
-    G2P_TRY(dalloc(&d_pe_edge, npe, s)); G2P_TRY(dalloc(&d_pe_port, npe, s)); G2P_TRY(dalloc(&d_pe_J, npe, s));
+    G2P_TRY(dalloc(&d_pe_edge, npe, s)); G2P_TRY(dalloc(&d_pe_J, npe, s)); G2P_TRY(dalloc(&d_pptr, P + 1, s));
+    G2P_CUDA(cudaMemcpyAsync(d_pptr, pptr.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, s));
     G2P_TRY(dalloc(&d_redge, (int64_t)redge.size(), s)); G2P_TRY(dalloc(&d_rdir, P, s));
     G2P_TRY(dalloc(&d_rptr, P + 1, s)); G2P_TRY(dalloc(&d_cur, P, s));
     G2P_CUDA(cudaMemcpyAsync(d_pe_edge, pe_edge.data(), sizeof(int32_t) * npe, cudaMemcpyHostToDevice, s));
@@ -314,14 +318,11 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     for (int p0 = 0; p0 < P; p0 += kb) {
         int kk = std::min(kb, P - p0);
         // entries of this block's ports, renumbered 0..kk-1
-        int64_t e0 = pptr[p0], e1 = pptr[p0 + kk];
-        std::vector<int32_t> port_local(pe_port.begin() + e0, pe_port.begin() + e1);
-        for (auto &v : port_local) v -= p0;
-        G2P_CUDA(cudaMemcpyAsync(d_pe_port + e0, port_local.data(), sizeof(int32_t) * (e1 - e0), cudaMemcpyHostToDevice, s));
+        const int64_t *d_pp = d_pptr + p0;     // entries of port p0 + r: [d_pp[r], d_pp[r + 1])
+        const unsigned rg = (unsigned)((kk + 127) / 128);
         // (1) b_d = -V0da^T J
         G2P_CUDA(cudaMemsetAsync(Bd, 0, sizeof(double) * nd * kk, s));
-        (g2p::kbegin("k_rhs_ports", s), k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
-                                                           m->v0d.ecol, m->v0d.eaval, kk, Bd), g2p::kend(s));
+        (g2p::kbegin("k_rhs_ports", s), k_rhs_ports<<<rg, 128, 0, s>>>(kk, d_pp, d_pe_edge, d_pe_J, m->v0d.ecol, m->v0d.eaval, kk, Bd), g2p::kend(s));
         (g2p::kbegin("k_scale", s), k_scale<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Bd, -1.0), g2p::kend(s));
         g2p_solve_stats ss;
         g2p_status rc = g2p_solver_solve_dev(Sd, Bd, Yd, kk, &ss);
@@ -334,8 +335,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         (g2p::kbegin("k_v0_apply", s), k_v0_apply<<<row_grid(ne, kk), row_block(kk), 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd1), g2p::kend(s));
         // (3) b_c = -V0ca^T J + V0ca^T(-omega D_eps yd1)
         G2P_CUDA(cudaMemsetAsync(Bc, 0, sizeof(double) * nc * kk, s));
-        (g2p::kbegin("k_rhs_ports", s), k_rhs_ports<<<grid_for(e1 - e0), kThreads, 0, s>>>(e1 - e0, d_pe_edge + e0, d_pe_port + e0, d_pe_J + e0,
-                                                           m->v0c.ecol, m->v0c.eaval, kk, Bc), g2p::kend(s));
+        (g2p::kbegin("k_rhs_ports", s), k_rhs_ports<<<rg, 128, 0, s>>>(kk, d_pp, d_pe_edge, d_pe_J, m->v0c.ecol, m->v0c.eaval, kk, Bc), g2p::kend(s));
         (g2p::kbegin("k_scale", s), k_scale<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, -1.0), g2p::kend(s));
         (g2p::kbegin("k_v0t_short", s), k_v0t_short<<<row_grid(nc, kk), row_block(kk), 0, s>>>(nc, kk, m->v0c.cptr, m->v0c.cedge, m->v0c.caval, yd1, f0, crhs), g2p::kend(s));
         (g2p::kbegin("k_add", s), k_add<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, crhs), g2p::kend(s));
@@ -378,7 +378,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     dfree(d_fr, s); dfree(d_out, s);
     dfree(Bd, s); dfree(Yd, s); dfree(Bc, s); dfree(Yc, s); dfree(crhs, s);
     dfree(yd1, s); dfree(yc, s); dfree(yd2, s); dfree(zre, s); dfree(zim, s);
-    dfree(d_pe_edge, s); dfree(d_pe_port, s); dfree(d_pe_J, s); dfree(d_redge, s); dfree(d_rdir, s);
+    dfree(d_pe_edge, s); dfree(d_pptr, s); dfree(d_pe_J, s); dfree(d_redge, s); dfree(d_rdir, s);
     dfree(d_rptr, s); dfree(d_cur, s); lcol.release(s);
     g2p_solver_destroy(Sd);
     g2p_solver_destroy(Sc);

@@ -432,12 +432,11 @@ static int sell_vec(int k) {
 
 // G2P_ELL_PIPE=0 selects the one-group-per-block kernel (for comparisons).
 static bool pipe_ok() {
-    static int on = -1;
-    if (on < 0) {
+    static const bool on = [] {
         const char *e = getenv("G2P_ELL_PIPE");
-        on = e ? atoi(e) != 0 : 1;
-    }
-    return on != 0;
+        return e ? atoi(e) != 0 : true;
+    }();
+    return on;
 }
 
 template <class T, int V>
@@ -452,12 +451,12 @@ static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cu
     if (g < 1) g = 1;
     if (A.ell_w > 0 && A.ell_w <= kSellUnroll && pipe_ok()) {
         // persistent: as many blocks as fit on the SMs at once
-        static int resident = 0;
-        if (!resident) {
+        // one value per instantiation, initialised once even with several host threads
+        static const int resident = [tpr, rows] {
             int per_sm = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmm_ell_pipe<T, V>, tpr * rows, 0);
-            resident = (per_sm > 0 ? per_sm : 4) * kSMs;
-        }
+            return (per_sm > 0 ? per_sm : 4) * kSMs;
+        }();
         const int64_t gp = std::min<int64_t>(g, resident);
         (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_sell<f64>" : "k_spmm_sell<f32>", s),
          k_spmm_ell_pipe<T, V><<<(unsigned)gp, dim3(tpr, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b),

@@ -186,6 +186,33 @@ int64_t g2p_profile_report(char *buf, int64_t cap);
  * (arrays of 8). */
 void g2p_profile_buckets(double *ms, double *bytes, int64_t *launches);
 
+/* ---- extraction service (no counterpart in the reference, which extracts
+ * one layout per process) ----
+ * A queue of extraction jobs, each the work of g2p_mesh_create +
+ * g2p_generate_stiff + g2p_para_generator on its own layout.  The first job
+ * in the queue starts when fewer than max_active jobs run and its device
+ * footprint estimate fits mem_budget_bytes minus the estimates of the
+ * running jobs (a job larger than the budget runs alone).  Each running job
+ * has its own host thread, mesh handle and CUDA stream, so their kernels
+ * overlap on the device; results do not depend on what else runs.  The
+ * estimate is a size model scaled by the largest measured/model ratio of
+ * jobs that ran alone (device pool high-water).  g2p_server_submit copies
+ * the description's arrays (host or device) before it returns.
+ * g2p_server_wait blocks until the job ends, writes Z as
+ * g2p_para_generator does (z_out: nfreq*P*P complex, may be NULL), and
+ * forgets the job.  Use one server from any number of host threads. */
+typedef struct g2p_server g2p_server;
+typedef struct {
+    double queued_ms, run_ms, total_ms;          /* submit->start, start->end, submit->end */
+    int64_t footprint_estimate, footprint_measured;   /* bytes; measured only when it ran alone */
+    int32_t ran_alone;
+} g2p_job_times;
+g2p_status g2p_server_create(int64_t mem_budget_bytes, int32_t max_active, g2p_server **out);
+g2p_status g2p_server_submit(g2p_server *s, const g2p_mesh_desc *desc, const g2p_solver_params *p, int64_t *job);
+g2p_status g2p_server_wait(g2p_server *s, int64_t job, double *z_out, g2p_extract_stats *st, g2p_job_times *t);
+/* Finishes the queued and running jobs, then frees the server. */
+g2p_status g2p_server_destroy(g2p_server *s);
+
 /* ---- setMapEdge without device allocation (no counterpart in the
  * reference; its nearest reference code is setMapEdge, src/fdtd.hpp:1444-1529,
  * with the PEC edges of src/mesh.cpp:943-987) ----
