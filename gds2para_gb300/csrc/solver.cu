@@ -105,42 +105,64 @@ struct XVec {
 
 constexpr int kSellUnroll = 8;
 
-// y = A x (or b - A x) over the short rows.  Block (tpr, 256 / tpr): the
-// tpr = k / V threads of a row each own V consecutive right-hand sides.
-template <class T, int V>
+// Sum over the ES entry-split lanes of one row (lanes tpr apart within a
+// group of G = tpr * ES consecutive lanes), in a fixed tree order.
+template <class T, int V, int ES>
+__device__ __forceinline__ void es_reduce(T (&acc)[V], int tpr) {
+    if constexpr (ES > 1) {
+        const int G = tpr * ES;
+        const int lane = threadIdx.x + threadIdx.y * blockDim.x;   // blockDim.x == G divides 32
+        const unsigned mask = G >= 32 ? 0xffffffffu : (((1u << G) - 1u) << ((lane & 31) & ~(G - 1)));
+#pragma unroll
+        for (int q = 0; q < V; q++)
+            for (int o = tpr; o < G; o <<= 1) acc[q] += __shfl_xor_sync(mask, acc[q], o);
+    }
+}
+
+// y = A x (or b - A x) over the short rows.  Block (tpr * ES, 256 / (tpr *
+// ES)): the tpr = k / V threads of a row each own V consecutive right-hand
+// sides, and ES of them (ES > 1 for wide operators) split the row's entries
+// (entry j to lane j % ES), so a row of w entries costs w / ES dependent
+// gathers per thread instead of w.
+template <class T, int V, int ES>
 __global__ void __launch_bounds__(256) k_spmm_sell(int64_t n, const int64_t *__restrict__ sptr,
                                                    const int32_t *__restrict__ scol, const T *__restrict__ sval,
                                                    const uint8_t *__restrict__ rlen, const T *__restrict__ x,
                                                    T *__restrict__ y, int k, const T *__restrict__ b) {
-    const int xo = threadIdx.x * V;
+    const int tpr = blockDim.x / ES;
+    const int part = threadIdx.x % tpr, e = threadIdx.x / tpr;
+    const int xo = part * V;
     G2P_FOR_ROWS(i, n) {
-        const int len = rlen[i];
-        if (len == kSellLong) continue;
+        const int lr = rlen[i];
+        const bool longrow = lr == kSellLong;
+        const int len = longrow ? 0 : lr;
         const int64_t base = sptr[i >> 5] + (i & 31);
         T acc[V];
 #pragma unroll
         for (int u = 0; u < V; u++) acc[u] = 0;
-        for (int j0 = 0; j0 < len; j0 += kSellUnroll) {
+        for (int j0 = e; j0 < len; j0 += ES * kSellUnroll) {
             // all gathers of the chunk are issued before the first use; past
             // the row's end they repeat its first column and are not added
             int32_t c[kSellUnroll];
             T a[kSellUnroll];
 #pragma unroll
             for (int u = 0; u < kSellUnroll; u++) {
-                const bool in = j0 + u < len;
-                c[u] = in ? __ldg(scol + base + 32 * (int64_t)(j0 + u)) : c[0];
-                a[u] = in ? __ldg(sval + base + 32 * (int64_t)(j0 + u)) : T(0);
+                const bool in = j0 + ES * u < len;
+                c[u] = in ? __ldg(scol + base + 32 * (int64_t)(j0 + ES * u)) : c[0];
+                a[u] = in ? __ldg(sval + base + 32 * (int64_t)(j0 + ES * u)) : T(0);
             }
             XVec<T, V> xv[kSellUnroll];
 #pragma unroll
             for (int u = 0; u < kSellUnroll; u++) xv[u].load(x + (int64_t)c[u] * k + xo);
 #pragma unroll
             for (int u = 0; u < kSellUnroll; u++)
-                if (j0 + u < len) {
+                if (j0 + ES * u < len) {
 #pragma unroll
                     for (int w = 0; w < V; w++) acc[w] += a[u] * xv[u].v[w];
                 }
         }
+        es_reduce<T, V, ES>(acc, tpr);
+        if (longrow || e != 0) continue;
         const int64_t t = i * k + xo;
         XVec<T, V> out;
         if (b) {
@@ -158,27 +180,27 @@ __global__ void __launch_bounds__(256) k_spmm_sell(int64_t n, const int64_t *__r
 
 // The same product on the uniform-width layout: the slot of entry j of row i
 // is 32 (ell_w (i / 32) + j) + i % 32, so the only dependent loads are the
-// column and value, then x.  Padding slots add 0 x_i.
-template <class T, int V>
+// column and value, then x.  Padding slots add 0 x_i.  ES as in k_spmm_sell.
+template <class T, int V, int ES>
 __global__ void __launch_bounds__(256) k_spmm_ell(int64_t n, int w, const int32_t *__restrict__ scol,
                                                   const T *__restrict__ sval, const T *__restrict__ x,
                                                   T *__restrict__ y, int k, const T *__restrict__ b) {
-    const int xo = threadIdx.x * V;
+    const int tpr = blockDim.x / ES;
+    const int part = threadIdx.x % tpr, e = threadIdx.x / tpr;
+    const int xo = part * V;
     G2P_FOR_ROWS(i, n) {
         const int64_t base = 32 * (int64_t)w * (i >> 5) + (i & 31);
         T acc[V];
 #pragma unroll
         for (int u = 0; u < V; u++) acc[u] = 0;
-        XVec<T, V> bv;
-        if (b) bv.load(b + i * k + xo);
-        for (int j0 = 0; j0 < w; j0 += kSellUnroll) {
+        for (int j0 = e; j0 < w; j0 += ES * kSellUnroll) {
             int32_t c[kSellUnroll];
             T a[kSellUnroll];
 #pragma unroll
             for (int u = 0; u < kSellUnroll; u++) {
-                const bool in = j0 + u < w;
-                c[u] = in ? __ldg(scol + base + 32 * (int64_t)(j0 + u)) : (int32_t)i;
-                a[u] = in ? __ldg(sval + base + 32 * (int64_t)(j0 + u)) : T(0);
+                const bool in = j0 + ES * u < w;
+                c[u] = in ? __ldg(scol + base + 32 * (int64_t)(j0 + ES * u)) : (int32_t)i;
+                a[u] = in ? __ldg(sval + base + 32 * (int64_t)(j0 + ES * u)) : T(0);
             }
             XVec<T, V> xv[kSellUnroll];
 #pragma unroll
@@ -188,9 +210,18 @@ __global__ void __launch_bounds__(256) k_spmm_ell(int64_t n, int w, const int32_
 #pragma unroll
                 for (int q = 0; q < V; q++) acc[q] += a[u] * xv[u].v[q];
         }
+        es_reduce<T, V, ES>(acc, tpr);
+        if (e != 0) continue;
         XVec<T, V> out;
+        if (b) {
+            XVec<T, V> bv;
+            bv.load(b + i * k + xo);
 #pragma unroll
-        for (int q = 0; q < V; q++) out.v[q] = b ? bv.v[q] - acc[q] : acc[q];
+            for (int q = 0; q < V; q++) out.v[q] = bv.v[q] - acc[q];
+        } else {
+#pragma unroll
+            for (int q = 0; q < V; q++) out.v[q] = acc[q];
+        }
         out.store(y + i * k + xo);
     }
 }
@@ -439,6 +470,50 @@ static bool pipe_ok() {
     return on;
 }
 
+// Profile name of a sparse-product launch: kernel, precision and operator size
+// class (fine >= 1M rows, mid >= 64k rows, small).
+static const char *spmm_name(int kind, bool f64, int64_t n) {
+    static const char *names[4][2][3] = {
+        {{"k_spmm_sell<f32,fine>", "k_spmm_sell<f32,mid>", "k_spmm_sell<f32,small>"},
+         {"k_spmm_sell<f64,fine>", "k_spmm_sell<f64,mid>", "k_spmm_sell<f64,small>"}},
+        {{"k_spmm_ell<f32,fine>", "k_spmm_ell<f32,mid>", "k_spmm_ell<f32,small>"},
+         {"k_spmm_ell<f64,fine>", "k_spmm_ell<f64,mid>", "k_spmm_ell<f64,small>"}},
+        {{"k_spmm_ell_pipe<f32,fine>", "k_spmm_ell_pipe<f32,mid>", "k_spmm_ell_pipe<f32,small>"},
+         {"k_spmm_ell_pipe<f64,fine>", "k_spmm_ell_pipe<f64,mid>", "k_spmm_ell_pipe<f64,small>"}},
+        {{"k_spmm_mid<f32,fine>", "k_spmm_mid<f32,mid>", "k_spmm_mid<f32,small>"},
+         {"k_spmm_mid<f64,fine>", "k_spmm_mid<f64,mid>", "k_spmm_mid<f64,small>"}}};
+    const int sc = n >= (1 << 20) ? 0 : n >= (1 << 16) ? 1 : 2;
+    return names[kind][f64 ? 1 : 0][sc];
+}
+
+// Entry split for an operator of average slice width wavg: one chunk of
+// kSellUnroll gathers per thread where possible, with tpr * ES <= 32 and tpr
+// a power of two.
+static int entry_split(double wavg, int tpr) {
+    if (tpr & (tpr - 1)) return 1;
+    int es = 1;
+    while (es < 8 && wavg > kSellUnroll * es && tpr * es * 2 <= 32) es <<= 1;
+    return es;
+}
+
+template <class T, int V, int ES>
+static void launch_sell_es(const Csr<T> &A, const T *x, T *y, int k, const T *b, cudaStream_t s) {
+    const int tpr = k / V;
+    const int rows = 256 / (tpr * ES);
+    int64_t g = (A.n + rows - 1) / rows;
+    if (g > 0x7fffffffLL) g = 0x7fffffffLL;
+    if (g < 1) g = 1;
+    if (A.ell_w > 0)
+        (g2p::kbegin(spmm_name(1, sizeof(T) == 8, A.n), s),
+         k_spmm_ell<T, V, ES><<<(unsigned)g, dim3(tpr * ES, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b),
+         g2p::kend(s));
+    else
+        (g2p::kbegin(spmm_name(0, sizeof(T) == 8, A.n), s),
+         k_spmm_sell<T, V, ES><<<(unsigned)g, dim3(tpr * ES, rows), 0, s>>>(A.n, A.sptr, A.scol, A.sval, A.rlen, x, y,
+                                                                             k, b),
+         g2p::kend(s));
+}
+
 template <class T, int V>
 static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cudaStream_t s) {
     // one block per 256 / tpr rows, never grid-strided: blocks retire in row
@@ -458,17 +533,18 @@ static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cu
             return (per_sm > 0 ? per_sm : 4) * kSMs;
         }();
         const int64_t gp = std::min<int64_t>(g, resident);
-        (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_sell<f64>" : "k_spmm_sell<f32>", s),
+        (g2p::kbegin(spmm_name(2, sizeof(T) == 8, A.n), s),
          k_spmm_ell_pipe<T, V><<<(unsigned)gp, dim3(tpr, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b),
          g2p::kend(s));
-    } else if (A.ell_w > 0)
-        (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_sell<f64>" : "k_spmm_sell<f32>", s),
-         k_spmm_ell<T, V><<<(unsigned)g, dim3(tpr, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b),
-         g2p::kend(s));
-    else
-        (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_sell<f64>" : "k_spmm_sell<f32>", s),
-         k_spmm_sell<T, V><<<(unsigned)g, dim3(tpr, rows), 0, s>>>(A.n, A.sptr, A.scol, A.sval, A.rlen, x, y, k, b),
-         g2p::kend(s));
+    } else {
+        const double wavg = A.n > 0 ? (double)A.sell_slots / (32.0 * (double)((A.n + 31) / 32)) : 0.0;
+        switch (entry_split(wavg, tpr)) {
+            case 8: launch_sell_es<T, V, 8>(A, x, y, k, b, s); break;
+            case 4: launch_sell_es<T, V, 4>(A, x, y, k, b, s); break;
+            case 2: launch_sell_es<T, V, 2>(A, x, y, k, b, s); break;
+            default: launch_sell_es<T, V, 1>(A, x, y, k, b, s); break;
+        }
+    }
 }
 
 template <class T>
@@ -513,7 +589,7 @@ void spmm_b(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, const 
     if (lr.nmid > 0) {
         const int kx = k >= 32 ? 32 : pow2_ge(k);
         const int64_t blocks = (lr.nmid + 7) / 8;
-        (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_mid<f64>" : "k_spmm_mid<f32>", s),
+        (g2p::kbegin(spmm_name(3, sizeof(T) == 8, A.n), s),
          k_spmm_mid<T><<<(unsigned)blocks, 256, 0, s>>>(lr.nmid, lr.mid, A.ptr, A.col, A.val, x, k, kx, y, b), g2p::kend(s));
     }
     if (lr.nchunk > 0) {
