@@ -537,8 +537,11 @@ static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cu
          k_spmm_ell_pipe<T, V><<<(unsigned)gp, dim3(tpr, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b),
          g2p::kend(s));
     } else {
+        // the entry split trades coalescing of the column and value loads for
+        // shorter dependent chains: worth it only on small (latency-bound)
+        // operators
         const double wavg = A.n > 0 ? (double)A.sell_slots / (32.0 * (double)((A.n + 31) / 32)) : 0.0;
-        switch (entry_split(wavg, tpr)) {
+        switch (A.n < (1 << 16) ? entry_split(wavg, tpr) : 1) {
             case 8: launch_sell_es<T, V, 8>(A, x, y, k, b, s); break;
             case 4: launch_sell_es<T, V, 4>(A, x, y, k, b, s); break;
             case 2: launch_sell_es<T, V, 2>(A, x, y, k, b, s); break;
