@@ -180,12 +180,17 @@ g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cu
     }
     // sliced-ELL copies of every operator the solves multiply by
     if ((st = sell_build<double>(S->A, s)) != G2P_OK) return fail(st);
+    // and of the prolongations (rows of at most kLongRow + 1 entries)
     if (S->precision == G2P_PREC_MIXED) {
-        for (auto &L : S->H32.lv)
+        for (auto &L : S->H32.lv) {
             if ((st = sell_build<float>(L.A, s)) != G2P_OK) return fail(st);
+            if (L.P.ptr && (st = sell_build<float>(L.P, s, 254)) != G2P_OK) return fail(st);
+        }
     } else {
-        for (auto &L : S->H64.lv)
+        for (auto &L : S->H64.lv) {
             if ((st = sell_build<double>(L.A, s)) != G2P_OK) return fail(st);
+            if (L.P.ptr && (st = sell_build<double>(L.P, s, 254)) != G2P_OK) return fail(st);
+        }
     }
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) { set_last_error(e, "solver setup", __FILE__, __LINE__); return fail(G2P_ERR_CUDA); }

@@ -86,6 +86,11 @@ struct XVec {
             for (int u = 0; u < V; u++) v[u] = __ldg(p + u);
         }
     }
+    // ordinary (coherent) load, for an output read back by the same thread
+    __device__ __forceinline__ void load_plain(const T *p) {
+#pragma unroll
+        for (int u = 0; u < V; u++) v[u] = p[u];
+    }
     __device__ __forceinline__ void store(T *__restrict__ p) const {
         if constexpr (V * sizeof(T) >= 16) {
             constexpr int W = 16 / sizeof(T);
@@ -104,6 +109,26 @@ struct XVec {
 };
 
 constexpr int kSellUnroll = 8;
+
+// Writes y = b - acc (b given), y = y + acc (accum), or y = acc.
+template <class T, int V>
+__device__ __forceinline__ void spmm_out(T *y, const T *b, bool accum, const T (&acc)[V]) {
+    XVec<T, V> out;
+    if (accum) {
+        out.load_plain(y);
+#pragma unroll
+        for (int q = 0; q < V; q++) out.v[q] += acc[q];
+    } else if (b) {
+        XVec<T, V> bv;
+        bv.load(b);
+#pragma unroll
+        for (int q = 0; q < V; q++) out.v[q] = bv.v[q] - acc[q];
+    } else {
+#pragma unroll
+        for (int q = 0; q < V; q++) out.v[q] = acc[q];
+    }
+    out.store(y);
+}
 
 // Sum over the ES entry-split lanes of one row (lanes tpr apart within a
 // group of G = tpr * ES consecutive lanes), in a fixed tree order.
@@ -128,7 +153,7 @@ template <class T, int V, int ES>
 __global__ void __launch_bounds__(256) k_spmm_sell(int64_t n, const int64_t *__restrict__ sptr,
                                                    const int32_t *__restrict__ scol, const T *__restrict__ sval,
                                                    const uint8_t *__restrict__ rlen, const T *__restrict__ x,
-                                                   T *__restrict__ y, int k, const T *__restrict__ b) {
+                                                   T *__restrict__ y, int k, const T *__restrict__ b, bool accum) {
     const int tpr = blockDim.x / ES;
     const int part = threadIdx.x % tpr, e = threadIdx.x / tpr;
     const int xo = part * V;
@@ -164,17 +189,7 @@ __global__ void __launch_bounds__(256) k_spmm_sell(int64_t n, const int64_t *__r
         es_reduce<T, V, ES>(acc, tpr);
         if (longrow || e != 0) continue;
         const int64_t t = i * k + xo;
-        XVec<T, V> out;
-        if (b) {
-            XVec<T, V> bv;
-            bv.load(b + t);
-#pragma unroll
-            for (int w = 0; w < V; w++) out.v[w] = bv.v[w] - acc[w];
-        } else {
-#pragma unroll
-            for (int w = 0; w < V; w++) out.v[w] = acc[w];
-        }
-        out.store(y + t);
+        spmm_out<T, V>(y + t, b ? b + t : nullptr, accum, acc);
     }
 }
 
@@ -184,7 +199,7 @@ __global__ void __launch_bounds__(256) k_spmm_sell(int64_t n, const int64_t *__r
 template <class T, int V, int ES>
 __global__ void __launch_bounds__(256) k_spmm_ell(int64_t n, int w, const int32_t *__restrict__ scol,
                                                   const T *__restrict__ sval, const T *__restrict__ x,
-                                                  T *__restrict__ y, int k, const T *__restrict__ b) {
+                                                  T *__restrict__ y, int k, const T *__restrict__ b, bool accum) {
     const int tpr = blockDim.x / ES;
     const int part = threadIdx.x % tpr, e = threadIdx.x / tpr;
     const int xo = part * V;
@@ -199,7 +214,7 @@ __global__ void __launch_bounds__(256) k_spmm_ell(int64_t n, int w, const int32_
 #pragma unroll
             for (int u = 0; u < kSellUnroll; u++) {
                 const bool in = j0 + ES * u < w;
-                c[u] = in ? __ldg(scol + base + 32 * (int64_t)(j0 + ES * u)) : (int32_t)i;
+                c[u] = in ? __ldg(scol + base + 32 * (int64_t)(j0 + ES * u)) : c[0];
                 a[u] = in ? __ldg(sval + base + 32 * (int64_t)(j0 + ES * u)) : T(0);
             }
             XVec<T, V> xv[kSellUnroll];
@@ -212,17 +227,8 @@ __global__ void __launch_bounds__(256) k_spmm_ell(int64_t n, int w, const int32_
         }
         es_reduce<T, V, ES>(acc, tpr);
         if (e != 0) continue;
-        XVec<T, V> out;
-        if (b) {
-            XVec<T, V> bv;
-            bv.load(b + i * k + xo);
-#pragma unroll
-            for (int q = 0; q < V; q++) out.v[q] = bv.v[q] - acc[q];
-        } else {
-#pragma unroll
-            for (int q = 0; q < V; q++) out.v[q] = acc[q];
-        }
-        out.store(y + i * k + xo);
+        const int64_t t = i * k + xo;
+        spmm_out<T, V>(y + t, b ? b + t : nullptr, accum, acc);
     }
 }
 
@@ -233,7 +239,8 @@ __global__ void __launch_bounds__(256) k_spmm_ell(int64_t n, int w, const int32_
 template <class T, int V>
 __global__ void __launch_bounds__(256) k_spmm_ell_pipe(int64_t n, int w, const int32_t *__restrict__ scol,
                                                        const T *__restrict__ sval, const T *__restrict__ x,
-                                                       T *__restrict__ y, int k, const T *__restrict__ b) {
+                                                       T *__restrict__ y, int k, const T *__restrict__ b,
+                                                       bool accum) {
     const int xo = threadIdx.x * V;
     const int64_t stride = (int64_t)gridDim.x * blockDim.y;
     int64_t i = blockIdx.x * (int64_t)blockDim.y + threadIdx.y;
@@ -244,7 +251,7 @@ __global__ void __launch_bounds__(256) k_spmm_ell_pipe(int64_t n, int w, const i
 #pragma unroll
         for (int u = 0; u < kSellUnroll; u++) {
             const bool in = u < w;
-            c[u] = in ? __ldg(scol + base + 32 * (int64_t)u) : (int32_t)r;
+            c[u] = in ? __ldg(scol + base + 32 * (int64_t)u) : c[0];
             a[u] = in ? __ldg(sval + base + 32 * (int64_t)u) : T(0);
         }
     };
@@ -256,8 +263,6 @@ __global__ void __launch_bounds__(256) k_spmm_ell_pipe(int64_t n, int w, const i
         T av[kSellUnroll];
 #pragma unroll
         for (int u = 0; u < kSellUnroll; u++) av[u] = a[u];
-        XVec<T, V> bv;
-        if (b) bv.load(b + i * k + xo);
         if (i + stride < n) fetch(i + stride);
         T acc[V];
 #pragma unroll
@@ -266,15 +271,13 @@ __global__ void __launch_bounds__(256) k_spmm_ell_pipe(int64_t n, int w, const i
         for (int u = 0; u < kSellUnroll; u++)
 #pragma unroll
             for (int q = 0; q < V; q++) acc[q] += av[u] * xv[u].v[q];
-        XVec<T, V> out;
-#pragma unroll
-        for (int q = 0; q < V; q++) out.v[q] = b ? bv.v[q] - acc[q] : acc[q];
-        out.store(y + i * k + xo);
+        const int64_t t = i * k + xo;
+        spmm_out<T, V>(y + t, b ? b + t : nullptr, accum, acc);
     }
 }
 
-// Padding of the uniform layout: (column = row, value = 0) in every slot a
-// row does not use, and in all slots of long rows.
+// Padding of the uniform layout: (column 0, value 0) in every slot a row does
+// not use, and in all slots of long rows.
 template <class T>
 __global__ void k_ell_pad(int64_t n, int w, const uint8_t *__restrict__ rlen, int32_t *__restrict__ scol,
                           T *__restrict__ sval) {
@@ -282,7 +285,7 @@ __global__ void k_ell_pad(int64_t n, int w, const uint8_t *__restrict__ rlen, in
         const int len = rlen[i] == kSellLong ? 0 : rlen[i];
         const int64_t base = 32 * (int64_t)w * (i >> 5) + (i & 31);
         for (int j = len; j < w; j++) {
-            scol[base + 32 * (int64_t)j] = (int32_t)i;
+            scol[base + 32 * (int64_t)j] = 0;   // any valid column (also for rectangular P)
             sval[base + 32 * (int64_t)j] = T(0);
         }
     }
@@ -301,13 +304,13 @@ __global__ void k_ell_sptr(int64_t *sptr, int64_t nslice, int64_t stride) {
 }
 
 // Slice widths (entries of the slice's longest short row) and row lengths.
-__global__ void k_sell_width(int64_t n, const int64_t *__restrict__ ptr, int64_t nslice, int64_t *__restrict__ width,
-                             uint8_t *__restrict__ rlen) {
+__global__ void k_sell_width(int64_t n, const int64_t *__restrict__ ptr, int64_t nslice, int64_t maxlen,
+                             int64_t *__restrict__ width, uint8_t *__restrict__ rlen) {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nslice; s += (int64_t)gridDim.x * blockDim.x) {
         int64_t w = 0;
         for (int64_t i = 32 * s; i < 32 * s + 32 && i < n; i++) {
             int64_t l = ptr[i + 1] - ptr[i];
-            if (l > kLongRow) { rlen[i] = kSellLong; continue; }
+            if (l > maxlen) { rlen[i] = kSellLong; continue; }
             rlen[i] = (uint8_t)l;
             w = l > w ? l : w;
         }
@@ -497,25 +500,28 @@ static int entry_split(double wavg, int tpr) {
 }
 
 template <class T, int V, int ES>
-static void launch_sell_es(const Csr<T> &A, const T *x, T *y, int k, const T *b, cudaStream_t s) {
+static void launch_sell_es(const Csr<T> &A, const T *x, T *y, int k, const T *b, cudaStream_t s, bool accum,
+                           const char *tag) {
     const int tpr = k / V;
     const int rows = 256 / (tpr * ES);
     int64_t g = (A.n + rows - 1) / rows;
     if (g > 0x7fffffffLL) g = 0x7fffffffLL;
     if (g < 1) g = 1;
     if (A.ell_w > 0)
-        (g2p::kbegin(spmm_name(1, sizeof(T) == 8, A.n), s),
-         k_spmm_ell<T, V, ES><<<(unsigned)g, dim3(tpr * ES, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b),
+        (g2p::kbegin(tag ? tag : spmm_name(1, sizeof(T) == 8, A.n), s),
+         k_spmm_ell<T, V, ES><<<(unsigned)g, dim3(tpr * ES, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b,
+                                                                            accum),
          g2p::kend(s));
     else
-        (g2p::kbegin(spmm_name(0, sizeof(T) == 8, A.n), s),
+        (g2p::kbegin(tag ? tag : spmm_name(0, sizeof(T) == 8, A.n), s),
          k_spmm_sell<T, V, ES><<<(unsigned)g, dim3(tpr * ES, rows), 0, s>>>(A.n, A.sptr, A.scol, A.sval, A.rlen, x, y,
-                                                                             k, b),
+                                                                             k, b, accum),
          g2p::kend(s));
 }
 
 template <class T, int V>
-static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cudaStream_t s) {
+static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cudaStream_t s, bool accum = false,
+                        const char *tag = nullptr) {
     // one block per 256 / tpr rows, never grid-strided: blocks retire in row
     // order, so the rows in flight form one window and the x rows a stencil
     // shares (z-neighbours one layer apart) are still in L2 when reused
@@ -533,8 +539,8 @@ static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cu
             return (per_sm > 0 ? per_sm : 4) * kSMs;
         }();
         const int64_t gp = std::min<int64_t>(g, resident);
-        (g2p::kbegin(spmm_name(2, sizeof(T) == 8, A.n), s),
-         k_spmm_ell_pipe<T, V><<<(unsigned)gp, dim3(tpr, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b),
+        (g2p::kbegin(tag ? tag : spmm_name(2, sizeof(T) == 8, A.n), s),
+         k_spmm_ell_pipe<T, V><<<(unsigned)gp, dim3(tpr, rows), 0, s>>>(A.n, A.ell_w, A.scol, A.sval, x, y, k, b, accum),
          g2p::kend(s));
     } else {
         // the entry split trades coalescing of the column and value loads for
@@ -542,10 +548,10 @@ static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cu
         // operators
         const double wavg = A.n > 0 ? (double)A.sell_slots / (32.0 * (double)((A.n + 31) / 32)) : 0.0;
         switch (A.n < (1 << 16) ? entry_split(wavg, tpr) : 1) {
-            case 8: launch_sell_es<T, V, 8>(A, x, y, k, b, s); break;
-            case 4: launch_sell_es<T, V, 4>(A, x, y, k, b, s); break;
-            case 2: launch_sell_es<T, V, 2>(A, x, y, k, b, s); break;
-            default: launch_sell_es<T, V, 1>(A, x, y, k, b, s); break;
+            case 8: launch_sell_es<T, V, 8>(A, x, y, k, b, s, accum, tag); break;
+            case 4: launch_sell_es<T, V, 4>(A, x, y, k, b, s, accum, tag); break;
+            case 2: launch_sell_es<T, V, 2>(A, x, y, k, b, s, accum, tag); break;
+            default: launch_sell_es<T, V, 1>(A, x, y, k, b, s, accum, tag); break;
         }
     }
 }
@@ -599,6 +605,24 @@ void spmm_b(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, const 
         (g2p::kbegin(A.n >= (1 << 20) ? (sizeof(T) == 8 ? "k_spmm_long<f64,fine>" : "k_spmm_long<f32,fine>")
                                       : (sizeof(T) == 8 ? "k_spmm_long<f64,coarse>" : "k_spmm_long<f32,coarse>"), s),
          k_spmm_long<T><<<(unsigned)lr.nchunk, blk, 0, s>>>(lr.rows, lr.crow, lr.cbeg, lr.rcp, A.ptr, A.col, A.val, x, k, lr.partial, lr.done, y, b), g2p::kend(s));
+    }
+}
+
+// x += P xc with the sliced-ELL copy of P (every row of P is short).
+template <class T>
+static void prolong_sell(const Csr<T> &P, const T *xc, T *x, int k, cudaStream_t s) {
+    int v = sell_vec<T>(k);
+    auto aligned = [&](const void *p) {
+        size_t w = (size_t)v * sizeof(T) >= 16 ? 16 : (size_t)v * sizeof(T);
+        return ((uintptr_t)p % w) == 0;
+    };
+    while (v > 1 && !(aligned(xc) && aligned(x))) v >>= 1;
+    const char *tag = sizeof(T) == 8 ? "k_prolong_sell<f64>" : "k_prolong_sell<f32>";
+    switch (v) {
+        case 8: launch_sell<T, 8>(P, xc, x, k, nullptr, s, true, tag); break;
+        case 4: launch_sell<T, 4>(P, xc, x, k, nullptr, s, true, tag); break;
+        case 2: launch_sell<T, 2>(P, xc, x, k, nullptr, s, true, tag); break;
+        default: launch_sell<T, 1>(P, xc, x, k, nullptr, s, true, tag); break;
     }
 }
 
@@ -712,7 +736,7 @@ g2p_status copy_long_rows(const LongRows &src, LongRows &dst, cudaStream_t s) {
 
 // Sliced-ELL copy of A's short rows (kept beside the CSR).
 template <class T>
-g2p_status sell_build(Csr<T> &A, cudaStream_t s) {
+g2p_status sell_build(Csr<T> &A, cudaStream_t s, int64_t maxlen) {
     A.release_sell(s);
     const int64_t n = A.n, nslice = (n + 31) / 32;
     int64_t *width, *work;
@@ -720,7 +744,7 @@ g2p_status sell_build(Csr<T> &A, cudaStream_t s) {
     G2P_TRY(dalloc(&work, scan_work_size(nslice + 1) + 4, s));
     G2P_TRY(dalloc(&A.rlen, n, s));
     G2P_TRY(dalloc(&A.sptr, nslice + 1, s));
-    (g2p::kbegin("k_sell_width", s), k_sell_width<<<grid_for(nslice), kThreads, 0, s>>>(n, A.ptr, nslice, width, A.rlen), g2p::kend(s));
+    (g2p::kbegin("k_sell_width", s), k_sell_width<<<grid_for(nslice), kThreads, 0, s>>>(n, A.ptr, nslice, maxlen, width, A.rlen), g2p::kend(s));
     const int64_t *wp = width;
     auto op = [wp, nslice] __device__(int64_t i) -> int64_t { return i < nslice ? wp[i] : 0; };
     G2P_TRY(exclusive_scan(op, nslice + 1, A.sptr, work, s));
@@ -757,10 +781,10 @@ g2p_status sell_build(Csr<T> &A, cudaStream_t s) {
     G2P_TRY(dalloc(&lp, n + 1, s));
     G2P_TRY(dalloc(&lw, scan_work_size(n + 1) + 4, s));
     const int64_t *pp = A.ptr;
-    auto lop = [pp, n] __device__(int64_t i) -> int64_t {
+    auto lop = [pp, n, maxlen] __device__(int64_t i) -> int64_t {
         if (i >= n) return 0;
         int64_t l = pp[i + 1] - pp[i];
-        return l > kLongRow ? 0 : l;
+        return l > maxlen ? 0 : l;
     };
     G2P_TRY(exclusive_scan(lop, n + 1, lp, lw, s));
     G2P_CUDA(cudaMemcpyAsync(&A.short_nnz, lp + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -769,8 +793,8 @@ g2p_status sell_build(Csr<T> &A, cudaStream_t s) {
     G2P_CUDA(cudaGetLastError());
     return G2P_OK;
 }
-template g2p_status sell_build<double>(Csr<double> &, cudaStream_t);
-template g2p_status sell_build<float>(Csr<float> &, cudaStream_t);
+template g2p_status sell_build<double>(Csr<double> &, cudaStream_t, int64_t);
+template g2p_status sell_build<float>(Csr<float> &, cudaStream_t, int64_t);
 
 // --------------------------------------------------------------- reductions
 // Deterministic per-column sums of squares: block partials, then an ordered
@@ -971,7 +995,8 @@ static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaS
     Level<T> &C = H.lv[l + 1];
     (g2p::kbegin("k_restrict", s), k_restrict<T><<<row_grid(C.n, k), row_block(k), 0, s>>>(C.n, k, L.rptr, L.rmem, L.t0, C.b), g2p::kend(s));
     vcycle<T>(H, cfg, l + 1, k, s);
-    (g2p::kbegin("k_prolong_csr", s), k_prolong_csr<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, L.P.ptr, L.P.col, L.P.val, C.x, L.x), g2p::kend(s));
+    if (L.P.sptr) prolong_sell<T>(L.P, C.x, L.x, k, s);
+    else (g2p::kbegin("k_prolong_csr", s), k_prolong_csr<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, L.P.ptr, L.P.col, L.P.val, C.x, L.x), g2p::kend(s));
     chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, L.b, L.x, false, k, s);
 }
 

@@ -114,8 +114,9 @@ void colnorms(const T *x, int64_t n, int k, double *partial, double *out, cudaSt
 template <class T>
 g2p_status find_long_rows(const Csr<T> &A, LongRows &lr, cudaStream_t s);
 g2p_status copy_long_rows(const LongRows &src, LongRows &dst, cudaStream_t s);
+// Sliced-ELL copy of the rows of A with at most maxlen (<= 254) entries.
 template <class T>
-g2p_status sell_build(Csr<T> &A, cudaStream_t s);
+g2p_status sell_build(Csr<T> &A, cudaStream_t s, int64_t maxlen = kLongRow);
 
 }  // namespace g2p
 
