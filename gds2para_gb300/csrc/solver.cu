@@ -276,16 +276,20 @@ __global__ void __launch_bounds__(256) k_spmm_ell_pipe(int64_t n, int w, const i
     }
 }
 
-// Padding of the uniform layout: (column 0, value 0) in every slot a row does
-// not use, and in all slots of long rows.
+// Padding of the uniform layout: value 0 in every slot a row does not use
+// (and in all slots of long rows), with the row's own first column -- a
+// valid column also for a rectangular P, and one whose x row the thread
+// gathers anyway, so padding adds no traffic and no shared hot spot.  An
+// empty row uses column min(i, m - 1).
 template <class T>
-__global__ void k_ell_pad(int64_t n, int w, const uint8_t *__restrict__ rlen, int32_t *__restrict__ scol,
+__global__ void k_ell_pad(int64_t n, int64_t m, int w, const uint8_t *__restrict__ rlen, int32_t *__restrict__ scol,
                           T *__restrict__ sval) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int len = rlen[i] == kSellLong ? 0 : rlen[i];
         const int64_t base = 32 * (int64_t)w * (i >> 5) + (i & 31);
+        const int32_t pc = len > 0 ? scol[base] : (int32_t)(i < m ? i : m - 1);
         for (int j = len; j < w; j++) {
-            scol[base + 32 * (int64_t)j] = 0;   // any valid column (also for rectangular P)
+            scol[base + 32 * (int64_t)j] = pc;
             sval[base + 32 * (int64_t)j] = T(0);
         }
     }
@@ -775,7 +779,7 @@ g2p_status sell_build(Csr<T> &A, cudaStream_t s, int64_t maxlen) {
     G2P_TRY(dalloc(&A.sval, slots, s));
     (g2p::kbegin("k_sell_fill", s), k_sell_fill<T><<<grid_for(n), kThreads, 0, s>>>(n, A.ptr, A.col, A.val, A.rlen, A.sptr, A.scol, A.sval), g2p::kend(s));
     if (uniform)
-        (g2p::kbegin("k_ell_pad", s), k_ell_pad<T><<<grid_for(n), kThreads, 0, s>>>(n, A.ell_w, A.rlen, A.scol, A.sval), g2p::kend(s));
+        (g2p::kbegin("k_ell_pad", s), k_ell_pad<T><<<grid_for(n), kThreads, 0, s>>>(n, A.m, A.ell_w, A.rlen, A.scol, A.sval), g2p::kend(s));
     // entries of the long rows are not in the copy
     int64_t *lp, *lw;
     G2P_TRY(dalloc(&lp, n + 1, s));
