@@ -110,23 +110,19 @@ struct XVec {
 
 constexpr int kSellUnroll = 8;
 
-// Writes y = b - acc (b given), y = y + acc (accum), or y = acc.
+// The operand combined with the product, loaded before the gathers so its
+// latency overlaps them: b (y = b - acc), the old y (accum: y = y + acc), or
+// nothing (y = acc).
 template <class T, int V>
-__device__ __forceinline__ void spmm_out(T *y, const T *b, bool accum, const T (&acc)[V]) {
+__device__ __forceinline__ void spmm_pre(XVec<T, V> &pre, const T *y, const T *b, bool accum) {
+    if (accum) pre.load_plain(y);
+    else if (b) pre.load(b);
+}
+template <class T, int V>
+__device__ __forceinline__ void spmm_out(T *y, bool has_b, bool accum, const XVec<T, V> &pre, const T (&acc)[V]) {
     XVec<T, V> out;
-    if (accum) {
-        out.load_plain(y);
 #pragma unroll
-        for (int q = 0; q < V; q++) out.v[q] += acc[q];
-    } else if (b) {
-        XVec<T, V> bv;
-        bv.load(b);
-#pragma unroll
-        for (int q = 0; q < V; q++) out.v[q] = bv.v[q] - acc[q];
-    } else {
-#pragma unroll
-        for (int q = 0; q < V; q++) out.v[q] = acc[q];
-    }
+    for (int q = 0; q < V; q++) out.v[q] = accum ? pre.v[q] + acc[q] : (has_b ? pre.v[q] - acc[q] : acc[q]);
     out.store(y);
 }
 
@@ -162,6 +158,9 @@ __global__ void __launch_bounds__(256) k_spmm_sell(int64_t n, const int64_t *__r
         const bool longrow = lr == kSellLong;
         const int len = longrow ? 0 : lr;
         const int64_t base = sptr[i >> 5] + (i & 31);
+        const int64_t t = i * k + xo;
+        XVec<T, V> pre;
+        if (!longrow && e == 0) spmm_pre<T, V>(pre, y + t, b ? b + t : nullptr, accum);
         T acc[V];
 #pragma unroll
         for (int u = 0; u < V; u++) acc[u] = 0;
@@ -188,8 +187,7 @@ __global__ void __launch_bounds__(256) k_spmm_sell(int64_t n, const int64_t *__r
         }
         es_reduce<T, V, ES>(acc, tpr);
         if (longrow || e != 0) continue;
-        const int64_t t = i * k + xo;
-        spmm_out<T, V>(y + t, b ? b + t : nullptr, accum, acc);
+        spmm_out<T, V>(y + t, b != nullptr, accum, pre, acc);
     }
 }
 
@@ -205,6 +203,9 @@ __global__ void __launch_bounds__(256) k_spmm_ell(int64_t n, int w, const int32_
     const int xo = part * V;
     G2P_FOR_ROWS(i, n) {
         const int64_t base = 32 * (int64_t)w * (i >> 5) + (i & 31);
+        const int64_t t = i * k + xo;
+        XVec<T, V> pre;
+        if (e == 0) spmm_pre<T, V>(pre, y + t, b ? b + t : nullptr, accum);
         T acc[V];
 #pragma unroll
         for (int u = 0; u < V; u++) acc[u] = 0;
@@ -227,8 +228,7 @@ __global__ void __launch_bounds__(256) k_spmm_ell(int64_t n, int w, const int32_
         }
         es_reduce<T, V, ES>(acc, tpr);
         if (e != 0) continue;
-        const int64_t t = i * k + xo;
-        spmm_out<T, V>(y + t, b ? b + t : nullptr, accum, acc);
+        spmm_out<T, V>(y + t, b != nullptr, accum, pre, acc);
     }
 }
 
@@ -263,6 +263,9 @@ __global__ void __launch_bounds__(256) k_spmm_ell_pipe(int64_t n, int w, const i
         T av[kSellUnroll];
 #pragma unroll
         for (int u = 0; u < kSellUnroll; u++) av[u] = a[u];
+        const int64_t t = i * k + xo;
+        XVec<T, V> pre;
+        spmm_pre<T, V>(pre, y + t, b ? b + t : nullptr, accum);
         if (i + stride < n) fetch(i + stride);
         T acc[V];
 #pragma unroll
@@ -271,8 +274,7 @@ __global__ void __launch_bounds__(256) k_spmm_ell_pipe(int64_t n, int w, const i
         for (int u = 0; u < kSellUnroll; u++)
 #pragma unroll
             for (int q = 0; q < V; q++) acc[q] += av[u] * xv[u].v[q];
-        const int64_t t = i * k + xo;
-        spmm_out<T, V>(y + t, b ? b + t : nullptr, accum, acc);
+        spmm_out<T, V>(y + t, b != nullptr, accum, pre, acc);
     }
 }
 
