@@ -101,7 +101,7 @@ extern "C" void g2p_default_params(g2p_solver_params *p, int32_t parity_mode) {
     if (parity_mode) {
         p->restart = 10; p->maxit = 100; p->rtol = 1e-4;     // hypreSolver.h:7-11, hypreSolve.cpp:211
     } else {
-        p->restart = 30; p->maxit = 400; p->rtol = 1e-10;
+        p->restart = 20; p->maxit = 400; p->rtol = 1e-10;
     }
     p->smoother_degree = 2;
     p->coarse_size = 256;
@@ -115,7 +115,7 @@ extern "C" void g2p_default_params(g2p_solver_params *p, int32_t parity_mode) {
 
 static SolverConfig cfg_from(const g2p_solver_params *p) {
     SolverConfig c;
-    c.restart = p->restart > 0 ? p->restart : 30;
+    c.restart = p->restart > 0 ? p->restart : 20;
     if (c.restart > 64) c.restart = 64;
     c.maxit = p->maxit > 0 ? p->maxit : 300;
     c.rtol = p->rtol > 0 ? p->rtol : 1e-10;

@@ -48,7 +48,7 @@ struct Level {
 };
 
 struct SolverConfig {
-    int restart = 30;
+    int restart = 20;
     int maxit = 300;
     double rtol = 1e-10;
     int degree = 2;
