@@ -20,6 +20,7 @@ EXPORTS = [
     "g2p_para_generator", "g2p_launch_count", "g2p_profile_begin", "g2p_profile_end", "g2p_profile_report",
     "g2p_map_edge_noalloc", "g2p_profile_buckets",
     "g2p_server_create", "g2p_server_submit", "g2p_server_wait", "g2p_server_destroy",
+    "g2p_mesh_mark",
 ]
 
 STATUS = {0: "G2P_OK", 1: "G2P_ERR_INVALID", 2: "G2P_ERR_CUDA", 3: "G2P_ERR_NOMEM", 4: "G2P_ERR_NOT_CONVERGED",
@@ -63,6 +64,14 @@ class ExtractStats(C.Structure):
                 ("max_rel_residual", C.c_double), ("assembly_ms", C.c_double), ("setup_ms", C.c_double),
                 ("solve_ms", C.c_double), ("total_ms", C.c_double), ("ad_levels", C.c_int32),
                 ("ac_levels", C.c_int32)]
+
+
+class BoxC(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("x0", "x1", "y0", "y1", "z0", "z1")]
+
+
+class PortSideC(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("sx", "sy", "sz", "rx", "ry", "rz")]
 
 
 class JobTimes(C.Structure):
@@ -119,6 +128,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_profile_end.argtypes = [C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)]
     L.g2p_profile_report.restype = C.c_int64
     L.g2p_profile_report.argtypes = [C.c_char_p, i64]
+    L.g2p_mesh_mark.argtypes = [i64, i64, i64, vp, vp, vp, vp, i64, i32, vp, vp, vp, vp, C.POINTER(i64),
+                                vp, vp, i64, vp, vp, i64, vp, vp]
     L.g2p_server_create.argtypes = [i64, i32, C.POINTER(vp)]
     L.g2p_server_submit.argtypes = [vp, C.POINTER(MeshDescC), C.POINTER(SolverParams), C.POINTER(i64)]
     L.g2p_server_wait.argtypes = [vp, i64, vp, C.POINTER(ExtractStats), C.POINTER(JobTimes)]

@@ -190,8 +190,8 @@ def paraGenerator(sys: FdtdMesh, params: Optional[SolverParams] = None):
     return zc.reshape(d.nfreq, d.num_ports, d.num_ports), st
 
 
-__all__ = ["FdtdMesh", "generateStiff", "hypreSolve", "paraGenerator", "Solver", "Server", "default_params",
-           "G2PError"]
+__all__ = ["FdtdMesh", "generateStiff", "hypreSolve", "paraGenerator", "Solver", "Server", "meshAndMark",
+           "default_params", "G2PError"]
 
 
 class Server:
@@ -251,3 +251,49 @@ def _pack_desc(desc: MeshDesc):
                            p("sep"), p("sed"), p("sa"), p("sd"), desc.freq_start, desc.freq_end,
                            desc.freq_unit, desc.nfreq, desc.freq_scale)
     return keep, cdesc
+
+
+def meshAndMark(layout) -> dict:
+    """Conductor marking, numbering and port edges of a Layout on the GPU
+    (g2p_mesh_mark: findInsideCond, the conductor labelling and portSet of
+    src/mesh.cpp).  Returns the fdtdMesh fields as numpy arrays."""
+    L = _lib.load()
+    nx, ny, nz = layout.nx, layout.ny, layout.nz
+    px, py, pz = layout.pitch
+    xn = np.arange(nx, dtype=np.float64) * px
+    yn = np.arange(ny, dtype=np.float64) * py
+    zn = np.arange(nz, dtype=np.float64) * pz
+    boxes = (_lib.BoxC * max(1, len(layout.boxes)))(*[_lib.BoxC(b.x0, b.x1, b.y0, b.y1, b.z0, b.z1)
+                                                      for b in layout.boxes])
+    sides, sptr = [], [0]
+    for port in layout.ports:
+        for s in port:
+            sides.append(_lib.PortSideC(*s.supply, *s.ret))
+        sptr.append(len(sides))
+    nsides = len(sides)
+    csides = (_lib.PortSideC * max(1, nsides))(*sides)
+    sptr = np.array(sptr, np.int32)
+    N_node = nx * ny * nz
+    Ns = (ny - 1) * nx + (nx - 1) * ny
+    N_edge = Ns * nz + nx * ny * (nz - 1)
+    mark_node = np.zeros(N_node, np.int64)
+    mark_edge = np.zeros(N_edge, np.int64)
+    ncdt = C.c_int64()
+    max_cdt = len(layout.boxes) + 2
+    mark_port = np.zeros(max_cdt, np.int32)
+    cdt_return = np.zeros(max_cdt, np.uint8)
+    max_e = sum(abs(s.supply[0] - s.ret[0]) + abs(s.supply[1] - s.ret[1]) + abs(s.supply[2] - s.ret[2])
+                for p in layout.ports for s in p) + 1
+    side_edge_ptr = np.zeros(nsides + 1, np.int64)
+    side_edges = np.zeros(max_e, np.int64)
+    side_area = np.zeros(max(1, nsides), np.float64)
+    side_dir = np.zeros(max(1, nsides), np.int32)
+    check(L.g2p_mesh_mark(nx, ny, nz, xn.ctypes.data, yn.ctypes.data, zn.ctypes.data, C.cast(boxes, C.c_void_p),
+                          len(layout.boxes), len(layout.ports), sptr.ctypes.data, C.cast(csides, C.c_void_p),
+                          mark_node.ctypes.data, mark_edge.ctypes.data, C.byref(ncdt), mark_port.ctypes.data,
+                          cdt_return.ctypes.data, max_cdt, side_edge_ptr.ctypes.data, side_edges.ctypes.data,
+                          max_e, side_area.ctypes.data, side_dir.ctypes.data))
+    n = ncdt.value
+    return dict(mark_node=mark_node, mark_edge=mark_edge, num_cdt=n, mark_port=mark_port[:n],
+                cdt_return=cdt_return[:n], side_edge_ptr=side_edge_ptr,
+                side_edges=side_edges[:side_edge_ptr[-1]], side_area=side_area[:nsides], side_dir=side_dir[:nsides])

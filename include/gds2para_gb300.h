@@ -186,6 +186,25 @@ int64_t g2p_profile_report(char *buf, int64_t cap);
  * (arrays of 8). */
 void g2p_profile_buckets(double *ms, double *bytes, int64_t *launches);
 
+/* ---- conductor marking and ports: meshAndMark's findInsideCond and conductor
+ * numbering (src/mesh.cpp:683-1020) and portSet (src/mesh.cpp:1196-1594) on
+ * the structured grid already chosen (xn, yn, zn).  Conductors are boxes of
+ * node indices (closed ranges; a later box overwrites an earlier one); the
+ * z = 0 plane is the lower PEC boundary.  Outputs are the g2p_mesh_desc
+ * fields: mark_node [N_node] and mark_edge [N_edge] (host or device
+ * memory), num_cdt, and -- when num_ports > 0 -- mark_port and cdt_return
+ * [max_cdt], side_edge_ptr [nsides + 1], side_edges [max_side_edges],
+ * side_area and side_dir [nsides], nsides = port_side_ptr[num_ports].
+ * Conductors are numbered 1.. in the order of their lowest node, as the
+ * reference's labelling leaves them. ---- */
+typedef struct { int64_t x0, x1, y0, y1, z0, z1; } g2p_box;
+typedef struct { int64_t sx, sy, sz, rx, ry, rz; } g2p_port_side;   /* supply node -> return node */
+g2p_status g2p_mesh_mark(int64_t nx, int64_t ny, int64_t nz, const double *xn, const double *yn, const double *zn,
+                         const g2p_box *boxes, int64_t nbox, int32_t num_ports, const int32_t *port_side_ptr,
+                         const g2p_port_side *sides, int64_t *mark_node, int64_t *mark_edge, int64_t *num_cdt,
+                         int32_t *mark_port, uint8_t *cdt_return, int64_t max_cdt, int64_t *side_edge_ptr,
+                         int64_t *side_edges, int64_t max_side_edges, double *side_area, int32_t *side_dir);
+
 /* ---- extraction service (no counterpart in the reference, which extracts
  * one layout per process) ----
  * A queue of extraction jobs, each the work of g2p_mesh_create +
