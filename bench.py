@@ -151,7 +151,10 @@ def run_gb300(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     L = _lib.load()
-    d = layout.build(layout.config(args.config))
+    lay_cfg = layout.config(args.config)
+    t0 = time.perf_counter()
+    d = layout.build(lay_cfg)
+    host_mesh_s = time.perf_counter() - t0
     params = default_params(precision=args.precision, batch=args.batch, rtol=RTOL[args.config])
     dev = make_desc(d, "cuda", torch)
     pin = make_desc(d, "pinned", torch)
@@ -251,6 +254,13 @@ def run_gb300(args):
             traffic = json.load(open(tf)).get(f"{args.config}_{args.precision}_bytes_per_launch")
         except Exception:
             traffic = None
+    # conductor marking, numbering and ports on the GPU (g2p_mesh_mark), from
+    # host boxes to host arrays, against the host generator's time
+    from gds2para_gb300 import api as _api
+    _api.meshAndMark(lay_cfg)
+    t0 = time.perf_counter()
+    _api.meshAndMark(lay_cfg)
+    gpu_mesh_s = time.perf_counter() - t0
     srt = sorted(step_ms)
     pct = lambda q: srt[min(len(srt) - 1, int(round(q * (len(srt) - 1))))] if srt else None
     out = {
@@ -271,6 +281,9 @@ def run_gb300(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": ms_e2e},
         "gpu_launches": int(launches),
+        "mesher": {"gpu_ms": 1e3 * gpu_mesh_s, "host_generator_ms": 1e3 * host_mesh_s,
+                   "what": "conductor marking, numbering and port edges (g2p_mesh_mark, host arrays in and out) "
+                           "vs the numpy/scipy generator that restates meshAndMark/portSet"},
         "job_ms": {"p50": pct(0.5), "p99": pct(0.99), "per_step": step_ms},
         "accuracy": {"z_rel_err_vs_fp64_gpu": z_err, "bound": 1e-6,
                      "note": "max |Z - Z_fp64| / max |Z_fp64| over all entries and frequencies"},
