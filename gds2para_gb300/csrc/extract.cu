@@ -288,7 +288,12 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     // node gives it a condition number near (length/h)^2, beyond what an FP32
     // refinement sweep resolves; it is an order of magnitude smaller than Ad.
     g2p_solver_params pc = p;
-    pc.precision = G2P_PREC_FP64;
+    // Ac in FP64 unless G2P_AC_MIXED=1 (for comparisons): its condition
+    // number leaves FP32 inner solves little to gain
+    {
+        const char *e = getenv("G2P_AC_MIXED");
+        if (!(e && atoi(e) != 0)) pc.precision = G2P_PREC_FP64;
+    }
     g2p_status rs = g2p_solver_build(m->Ac, &pc, s, &Sc);
     if (rs != G2P_OK) { g2p_solver_destroy(Sd); return rs; }
     local.setup_ms = ms_since(t0);
