@@ -293,6 +293,9 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     {
         const char *e = getenv("G2P_AC_MIXED");
         if (!(e && atoi(e) != 0)) pc.precision = G2P_PREC_FP64;
+        // Ac's own AMG strength and smoother degree (for comparisons)
+        if (const char *t = getenv("G2P_AC_STRENGTH")) pc.strength = atof(t);
+        if (const char *t = getenv("G2P_AC_DEGREE")) pc.smoother_degree = atoi(t);
     }
     g2p_status rs = g2p_solver_build(m->Ac, &pc, s, &Sc);
     if (rs != G2P_OK) { g2p_solver_destroy(Sd); return rs; }
