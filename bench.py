@@ -242,8 +242,8 @@ def run_gb300(args):
     peak_gbs = peaks.get("hbm_gbs", 6800.0)
     k_ms, k_bytes, k_n, b_ms, b_bytes, b_n = kern
     achieved_all = (k_bytes / (k_ms / 1e3)) / 1e9 if k_ms > 0 else None
-    # the fine-level operator's launches (>= 128 MB of algorithmic bytes each)
-    # in the working precision of the preconditioned solves
+    # the fine-level operator's launches (operators of >= 1M rows) in the
+    # working precision of the preconditioned solves
     fi = 3 if args.precision == "mixed" else 7
     f_ms, f_bytes, f_n = b_ms[fi], b_bytes[fi], b_n[fi]
     achieved = (f_bytes / (f_ms / 1e3)) / 1e9 if f_ms > 0 else None
@@ -293,8 +293,8 @@ def run_gb300(args):
         "clocks": clk,
         "roofline": {"bound": "hbm",
                      "kernel": ("k_spmm_sell<f32>" if args.precision == "mixed" else "k_spmm_sell<f64>") +
-                               ": sliced-ELL sparse matrix x block of right-hand sides, fine-level Ad "
-                               "(launches of >= 128 MB algorithmic bytes)",
+                               ": sparse matrix x block of right-hand sides on the fine-level Ad "
+                               "(operators of >= 1M rows)",
                      "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
                      "frac": (achieved / peak_gbs) if achieved else None, "traffic": traffic,
                      "launches": int(f_n), "avg_launch_us": 1e3 * f_ms / max(f_n, 1),
@@ -304,7 +304,7 @@ def run_gb300(args):
                                     "frac": (achieved_all / peak_gbs) if achieved_all else None},
                      "buckets": {f"{p}{nm}": [b_n[o + q], b_ms[o + q], b_bytes[o + q]]
                                  for o, p in ((0, "f32 "), (4, "f64 "))
-                                 for q, nm in enumerate(("<1MB", "1-16MB", "16-128MB", ">=128MB")) if b_n[o + q]},
+                                 for q, nm in enumerate(("rows<64k", "rows<256k", "rows<1M", "rows>=1M")) if b_n[o + q]},
                      "bucket_fields": "launches, ms, algorithmic bytes",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s"},
     }

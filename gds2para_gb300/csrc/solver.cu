@@ -447,6 +447,7 @@ struct KernelProfile {
     int64_t launches = 0;
     std::vector<double> launch_bytes;   // per launch, for the size buckets
     std::vector<char> launch_f64;       // per launch: FP64 operator
+    std::vector<int64_t> launch_rows;   // per launch: operator rows
 };
 static KernelProfile g_prof;
 static double g_bucket_ms[8], g_bucket_bytes[8];
@@ -581,6 +582,7 @@ void spmm_b(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, const 
                                      (double)A.n * k * sizeof(T) * (b ? 3 : 2);
         g_prof.launch_bytes.push_back(lb);
         g_prof.launch_f64.push_back(sizeof(T) == 8);
+        g_prof.launch_rows.push_back(A.n);
     }
     dim3 blk = row_block(k);
     if (sell) {
@@ -2027,6 +2029,7 @@ extern "C" void g2p_profile_begin(void) {
     g2p::g_prof.launches = 0;
     g2p::g_prof.launch_bytes.clear();
     g2p::g_prof.launch_f64.clear();
+    g2p::g_prof.launch_rows.clear();
 }
 
 extern "C" g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, int64_t *launches) {
@@ -2035,8 +2038,9 @@ extern "C" g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, i
     kprof_set(false);
     G2P_TRY(kprof_collect());
     double ms = 0;
-    // size buckets of the SpMM launches by algorithmic bytes
-    const double edges[] = {0, 1e6, 16e6, 128e6, 1e30};
+    // classes of the SpMM launches by operator rows: < 64k, < 256k, < 1M, >= 1M
+    // (the last one is the fine level of the workloads here)
+    const double edges[] = {0, 65536, 262144, 1048576, 1e30};
     double bms[8] = {0}, bby[8] = {0};
     int64_t bn[8] = {0};
     for (size_t i = 0; i + 1 < g_prof.used; i += 2) {
@@ -2046,13 +2050,14 @@ extern "C" g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, i
         const size_t li = i / 2;
         if (li < g_prof.launch_bytes.size()) {
             const double lb = g_prof.launch_bytes[li];
+            const double rows = (double)g_prof.launch_rows[li];
             const int o = g_prof.launch_f64[li] ? 4 : 0;
             for (int q = 0; q < 4; q++)
-                if (lb >= edges[q] && lb < edges[q + 1]) { bms[o + q] += t; bby[o + q] += lb; bn[o + q]++; }
+                if (rows >= edges[q] && rows < edges[q + 1]) { bms[o + q] += t; bby[o + q] += lb; bn[o + q]++; }
         }
     }
     for (int q = 0; q < 8; q++) { g_bucket_ms[q] = bms[q]; g_bucket_bytes[q] = bby[q]; g_bucket_n[q] = bn[q]; }
-    const char *bname[4] = {"<1MB", "1-16MB", "16-128MB", ">=128MB"};
+    const char *bname[4] = {"rows<64k", "rows<256k", "rows<1M", "rows>=1M"};
     for (int q = 0; q < 8; q++)
         if (bn[q]) {
             char nm[96];

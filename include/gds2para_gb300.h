@@ -180,8 +180,8 @@ g2p_status g2p_profile_end(double *kernel_ms, double *kernel_bytes, int64_t *lau
  * cap-1 bytes plus a terminator. */
 int64_t g2p_profile_report(char *buf, int64_t cap);
 /* The short-row SpMM launches (k_spmm_sell) of the last profiled interval
- * in eight classes: FP32 operators then FP64 operators, each split by
- * algorithmic bytes per launch (<1 MB, 1-16 MB, 16-128 MB, >=128 MB).
+ * in eight classes: FP32 operators then FP64 operators, each split by the
+ * operator's rows (< 64k, < 256k, < 1M, >= 1M).
  * Writes device milliseconds, algorithmic bytes and launches per class
  * (arrays of 8). */
 void g2p_profile_buckets(double *ms, double *bytes, int64_t *launches);
