@@ -191,6 +191,58 @@ __global__ void __launch_bounds__(256) k_spmm_sell(int64_t n, const int64_t *__r
     }
 }
 
+// Sliced ELL for wide rows (more than one chunk of kSellUnroll entries),
+// chunk-pipelined: the next chunk's column and value loads are issued while
+// the current chunk's x gathers are in flight, so a row of c chunks exposes
+// c + 1 memory round trips instead of 2 c.  Same summation order as
+// k_spmm_sell with ES = 1.
+template <class T, int V>
+__global__ void __launch_bounds__(256) k_spmm_sell_pipe(int64_t n, const int64_t *__restrict__ sptr,
+                                                        const int32_t *__restrict__ scol, const T *__restrict__ sval,
+                                                        const uint8_t *__restrict__ rlen, const T *__restrict__ x,
+                                                        T *__restrict__ y, int k, const T *__restrict__ b, bool accum) {
+    const int xo = threadIdx.x * V;
+    G2P_FOR_ROWS(i, n) {
+        const int lr = rlen[i];
+        if (lr == kSellLong) continue;
+        const int len = lr;
+        const int64_t base = sptr[i >> 5] + (i & 31);
+        const int64_t t = i * k + xo;
+        XVec<T, V> pre;
+        spmm_pre<T, V>(pre, y + t, b ? b + t : nullptr, accum);
+        T acc[V];
+#pragma unroll
+        for (int u = 0; u < V; u++) acc[u] = 0;
+        int32_t c[kSellUnroll];
+        T a[kSellUnroll];
+        auto fetch = [&](int j0) {
+#pragma unroll
+            for (int u = 0; u < kSellUnroll; u++) {
+                const bool in = j0 + u < len;
+                c[u] = in ? __ldg(scol + base + 32 * (int64_t)(j0 + u)) : c[0];
+                a[u] = in ? __ldg(sval + base + 32 * (int64_t)(j0 + u)) : T(0);
+            }
+        };
+        if (len > 0) fetch(0);
+        for (int j0 = 0; j0 < len; j0 += kSellUnroll) {
+            XVec<T, V> xv[kSellUnroll];
+#pragma unroll
+            for (int u = 0; u < kSellUnroll; u++) xv[u].load(x + (int64_t)c[u] * k + xo);
+            T av[kSellUnroll];
+#pragma unroll
+            for (int u = 0; u < kSellUnroll; u++) av[u] = (j0 + u < len) ? a[u] : T(0);
+            if (j0 + kSellUnroll < len) fetch(j0 + kSellUnroll);
+#pragma unroll
+            for (int u = 0; u < kSellUnroll; u++)
+                if (j0 + u < len) {
+#pragma unroll
+                    for (int w = 0; w < V; w++) acc[w] += av[u] * xv[u].v[w];
+                }
+        }
+        spmm_out<T, V>(y + t, b != nullptr, accum, pre, acc);
+    }
+}
+
 // The same product on the uniform-width layout: the slot of entry j of row i
 // is 32 (ell_w (i / 32) + j) + i % 32, so the only dependent loads are the
 // column and value, then x.  Padding slots add 0 x_i.  ES as in k_spmm_sell.
@@ -554,6 +606,14 @@ static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cu
         // shorter dependent chains: worth it only on small (latency-bound)
         // operators
         const double wavg = A.n > 0 ? (double)A.sell_slots / (32.0 * (double)((A.n + 31) / 32)) : 0.0;
+        if (A.n >= (1 << 16) && A.ell_w == 0 && wavg > kSellUnroll) {
+            // wide rows on a large operator: chunk-pipelined, coalesced loads
+            (g2p::kbegin(tag ? tag : spmm_name(0, sizeof(T) == 8, A.n), s),
+             k_spmm_sell_pipe<T, V><<<(unsigned)g, dim3(tpr, rows), 0, s>>>(A.n, A.sptr, A.scol, A.sval, A.rlen, x, y,
+                                                                           k, b, accum),
+             g2p::kend(s));
+            return;
+        }
         switch (A.n < (1 << 16) ? entry_split(wavg, tpr) : 1) {
             case 8: launch_sell_es<T, V, 8>(A, x, y, k, b, s, accum, tag); break;
             case 4: launch_sell_es<T, V, 4>(A, x, y, k, b, s, accum, tag); break;
