@@ -18,6 +18,8 @@
 #include "solver.h"
 
 g2p_status g2p_run_v0(g2p_mesh *m);
+g2p_status g2p_run_v0_ex(g2p_mesh *m, bool defer_ad);
+g2p_status g2p_v0_finish(g2p_mesh *m);
 g2p_status g2p_solver_build(const g2p::Csr<double> &A, const g2p_solver_params *p, cudaStream_t stream,
                             g2p_solver **out);
 g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k, g2p_solve_stats *st);
@@ -245,7 +247,9 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     g2p_extract_stats local;
     memset(&local, 0, sizeof(local));
     auto t0 = std::chrono::steady_clock::now();
-    G2P_TRY(g2p_run_v0(m));
+    // Ad's ordered conductor sums keep running on the mesh's side stream
+    // while the ports are prepared and Ac's solver is set up
+    G2P_TRY(g2p_run_v0_ex(m, true));
     local.assembly_ms = ms_since(t0);
     // ---- port data: J entries (last side wins, matrixCon.cpp:367-374),
     //      response edges (side 0) and source currents
@@ -283,7 +287,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     // ---- solvers (setup once per operator; the reference rebuilds per call)
     t0 = std::chrono::steady_clock::now();
     g2p_solver *Sd = nullptr, *Sc = nullptr;
-    G2P_TRY(g2p_solver_build(m->Ad, &p, s, &Sd));
+    // Ac first: its setup overlaps Ad's ordered sums on the side stream.
     // Ac, the conductor Laplacian, stays FP64: a floating wire grounded at one
     // node gives it a condition number near (length/h)^2, beyond what an FP32
     // refinement sweep resolves; it is an order of magnitude smaller than Ad.
@@ -304,7 +308,10 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         if (const char *t = getenv("G2P_AC_DEGREE")) pc.smoother_degree = atoi(t);
     }
     g2p_status rs = g2p_solver_build(m->Ac, &pc, s, &Sc);
-    if (rs != G2P_OK) { g2p_solver_destroy(Sd); return rs; }
+    if (rs != G2P_OK) { g2p_v0_finish(m); return rs; }
+    rs = g2p_v0_finish(m);
+    if (rs == G2P_OK) rs = g2p_solver_build(m->Ad, &p, s, &Sd);
+    if (rs != G2P_OK) { g2p_solver_destroy(Sc); return rs; }
     local.setup_ms = ms_since(t0);
     local.ad_levels = Sd->levels;
     local.ac_levels = Sc->levels;

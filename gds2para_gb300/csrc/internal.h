@@ -59,6 +59,9 @@ struct V0Basis {
     }
 };
 
+// A Laplacian whose ordered conductor sums still run on the side stream.
+struct LapPending;
+
 struct Constants {
     double mu, eps0;
 };
@@ -98,6 +101,8 @@ struct g2p_mesh {
     g2p::Csr<double> S;
     // V0 bases and Laplacians
     bool v0_done = false;
+    g2p::LapPending *ad_pending = nullptr;   // Ad's long rows still summing on `side`
+    cudaStream_t side = nullptr;
     double *v0_tab = nullptr;      // per-line quotient tables of the V0 entries
     g2p::V0Basis v0d, v0c;
     g2p::Csr<double> Ad, Ac;

@@ -267,8 +267,12 @@ extern "C" g2p_status g2p_mesh_create(const g2p_mesh_desc *in, g2p_mesh **out) {
     return G2P_OK;
 }
 
+g2p_status g2p_v0_finish(g2p_mesh *m);
+
 extern "C" g2p_status g2p_mesh_destroy(g2p_mesh *m) {
     if (!m) return G2P_OK;
+    if (m->ad_pending) g2p_v0_finish(m);     // joins the side stream and frees its buffers
+    if (m->side) { cudaStreamSynchronize(m->side); cudaStreamDestroy(m->side); m->side = nullptr; }
     cudaStream_t s = m->stream;
     dfree(m->xn, s); dfree(m->yn, s); dfree(m->zn, s);
     dfree(m->dxa, s); dfree(m->dya, s); dfree(m->dza, s); dfree(m->v0_tab, s);

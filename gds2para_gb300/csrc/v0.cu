@@ -531,101 +531,147 @@ static int bits_for(uint64_t v) {
     return b < 8 ? 8 : ((b + 7) / 8) * 8;
 }
 
+// State of a Laplacian between lap_begin and lap_finish.
+struct g2p::LapPending {
+    V0Ctx c;
+    V0Basis *B = nullptr;
+    Csr<double> *A = nullptr;
+    bool is_ac = false;
+    int64_t ncol = 0, nshort = 0, nlong = 0, nseg = 0;
+    int64_t *rowlen = nullptr, *keep = nullptr, *kpos = nullptr, *head = nullptr, *segid = nullptr, *sstart = nullptr;
+    uint64_t *okey = nullptr, *k0 = nullptr, *k1 = nullptr;
+    double *oval = nullptr, *v0 = nullptr, *v1 = nullptr;
+    cudaEvent_t done = nullptr;     // recorded on the side stream after the ordered sums
+};
+
 // Builds one Laplacian (Ad when is_ac false) from a V0 basis; rows [0, nshort)
-// are single-node columns, rows [nshort, ncol) conductor columns.
-static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool is_ac, int64_t nshort, Csr<double> &A) {
+// are single-node columns, rows [nshort, ncol) conductor columns.  Part one:
+// everything up to the ordered per-key sums of the long rows, which go to
+// m->side when `on_side` (the largest conductor's sum is a dependent chain of
+// FP64 additions; other work can run meanwhile).
+static g2p_status lap_begin(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool is_ac, int64_t nshort, Csr<double> &A,
+                            LapPending &P, bool on_side) {
     cudaStream_t s = m->stream;
-    int64_t ncol = B.ncol;
-    int64_t nlong = ncol - nshort;
-    int64_t *rowlen;
-    G2P_TRY(dalloc(&rowlen, ncol + 1, s));
-    G2P_CUDA(cudaMemsetAsync(rowlen, 0, sizeof(int64_t) * (ncol + 1), s));
+    P.c = c; P.B = &B; P.A = &A; P.is_ac = is_ac;
+    const int64_t ncol = B.ncol, nlong = ncol - nshort;
+    P.ncol = ncol; P.nshort = nshort; P.nlong = nlong;
+    G2P_TRY(dalloc(&P.rowlen, ncol + 1, s));
+    G2P_CUDA(cudaMemsetAsync(P.rowlen, 0, sizeof(int64_t) * (ncol + 1), s));
     if (nshort > 0)
-        (g2p::kbegin("k_short_rows_count", s), k_short_rows_count<<<grid_for(nshort), kThreads, 0, s>>>(c, B.map, is_ac, B.cptr, B.cedge, B.caval, nshort, rowlen), g2p::kend(s));
+        (g2p::kbegin("k_short_rows_count", s), k_short_rows_count<<<grid_for(nshort), kThreads, 0, s>>>(c, B.map, is_ac, B.cptr, B.cedge, B.caval, nshort, P.rowlen), g2p::kend(s));
+    if (nlong == 0) return G2P_OK;
     // long rows through sort + ordered reduce
-    uint64_t *okey = nullptr;
-    double *oval = nullptr;
-    int64_t *keep = nullptr, *kpos = nullptr;
-    int64_t nseg = 0;
-    if (nlong > 0) {
-        int64_t h_ent[2];
-        G2P_CUDA(cudaMemcpyAsync(h_ent, B.cptr + nshort, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-        G2P_CUDA(cudaMemcpyAsync(h_ent + 1, B.cptr + ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-        G2P_CUDA(cudaStreamSynchronize(s));
-        int64_t nent = h_ent[1] - h_ent[0];
-        int64_t *nt, *toff;
-        G2P_TRY(dalloc(&nt, nent + 1, s));
-        G2P_TRY(dalloc(&toff, nent + 1, s));
-        if (nent > 0)
-            (g2p::kbegin("k_long_nterms", s), k_long_nterms<<<grid_for(nent), kThreads, 0, s>>>(c, B.map, B.cptr, B.cedge, B.caval, nshort, nlong, nt), g2p::kend(s));
-        G2P_TRY(ensure_scan_work(m, nent + 1));
-        const int64_t *ntp = nt;
-        auto op = [ntp, nent] __device__(int64_t i) -> int64_t { return i < nent ? ntp[i] : 0; };
-        G2P_TRY(exclusive_scan(op, nent + 1, toff, m->scan_work, s));
-        int64_t nterm = 0;
-        G2P_CUDA(cudaMemcpyAsync(&nterm, toff + nent, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-        G2P_CUDA(cudaStreamSynchronize(s));
-        uint64_t *k0, *k1;
-        double *v0, *v1;
-        G2P_TRY(dalloc(&k0, nterm, s)); G2P_TRY(dalloc(&k1, nterm, s));
-        G2P_TRY(dalloc(&v0, nterm, s)); G2P_TRY(dalloc(&v1, nterm, s));
-        if (nent > 0)
-            (g2p::kbegin("k_long_terms", s), k_long_terms<<<grid_for(nent), kThreads, 0, s>>>(c, B.map, B.cptr, B.cedge, B.caval, nshort, nlong, ncol, toff,
-                                                             k0, v0), g2p::kend(s));
-        dfree(nt, s); dfree(toff, s);
-        int64_t *counts;
-        G2P_TRY(dalloc(&counts, sort_counts_size(nterm), s));
-        G2P_TRY(ensure_scan_work(m, sort_counts_size(nterm)));
-        bool in1 = false;
-        G2P_TRY(radix_sort_pairs(k0, v0, k1, v1, nterm, bits_for((uint64_t)nlong * (uint64_t)ncol), counts,
-                                 m->scan_work, &in1, s));
-        dfree(counts, s);
-        uint64_t *sk = in1 ? k1 : k0;
-        double *sv = in1 ? v1 : v0;
-        int64_t *head, *segid;
-        G2P_TRY(dalloc(&head, nterm + 1, s));
-        G2P_TRY(dalloc(&segid, nterm + 1, s));
-        (g2p::kbegin("k_heads", s), k_heads<<<grid_for(nterm), kThreads, 0, s>>>(sk, nterm, head), g2p::kend(s));
-        G2P_TRY(ensure_scan_work(m, nterm + 1));
-        const int64_t *hp = head;
-        auto hop = [hp, nterm] __device__(int64_t i) -> int64_t { return i < nterm ? hp[i] : 0; };
-        G2P_TRY(exclusive_scan(hop, nterm + 1, segid, m->scan_work, s));
-        G2P_CUDA(cudaMemcpyAsync(&nseg, segid + nterm, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-        G2P_CUDA(cudaStreamSynchronize(s));
-        G2P_TRY(dalloc(&okey, nseg, s)); G2P_TRY(dalloc(&oval, nseg, s));
-        G2P_TRY(dalloc(&keep, nseg + 1, s)); G2P_TRY(dalloc(&kpos, nseg + 1, s));
-        int64_t *sstart;
-        G2P_TRY(dalloc(&sstart, nseg + 1, s));
-        (g2p::kbegin("k_seg_bounds", s), k_seg_bounds<<<grid_for(nterm), kThreads, 0, s>>>(head, segid, nterm, nseg, sstart), g2p::kend(s));
-        (g2p::kbegin("k_seg_sum", s), k_seg_sum<<<grid_for(nseg), kThreads, 0, s>>>(sk, sv, nseg, sstart, okey, oval, keep), g2p::kend(s));
-        (g2p::kbegin("k_seg_sum_long", s), k_seg_sum_long<<<grid_for(32 * nseg), kThreads, 0, s>>>(sk, sv, nseg, sstart, okey, oval, keep), g2p::kend(s));
-        dfree(sstart, s);
-        (g2p::kbegin("k_long_rowlen", s), k_long_rowlen<<<grid_for(nseg), kThreads, 0, s>>>(okey, keep, nseg, ncol, rowlen + nshort), g2p::kend(s));
-        const int64_t *kp = keep;
+    int64_t h_ent[2];
+    G2P_CUDA(cudaMemcpyAsync(h_ent, B.cptr + nshort, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaMemcpyAsync(h_ent + 1, B.cptr + ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    const int64_t nent = h_ent[1] - h_ent[0];
+    int64_t *nt, *toff;
+    G2P_TRY(dalloc(&nt, nent + 1, s));
+    G2P_TRY(dalloc(&toff, nent + 1, s));
+    if (nent > 0)
+        (g2p::kbegin("k_long_nterms", s), k_long_nterms<<<grid_for(nent), kThreads, 0, s>>>(c, B.map, B.cptr, B.cedge, B.caval, nshort, nlong, nt), g2p::kend(s));
+    G2P_TRY(ensure_scan_work(m, nent + 1));
+    const int64_t *ntp = nt;
+    auto op = [ntp, nent] __device__(int64_t i) -> int64_t { return i < nent ? ntp[i] : 0; };
+    G2P_TRY(exclusive_scan(op, nent + 1, toff, m->scan_work, s));
+    int64_t nterm = 0;
+    G2P_CUDA(cudaMemcpyAsync(&nterm, toff + nent, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    G2P_TRY(dalloc(&P.k0, nterm, s)); G2P_TRY(dalloc(&P.k1, nterm, s));
+    G2P_TRY(dalloc(&P.v0, nterm, s)); G2P_TRY(dalloc(&P.v1, nterm, s));
+    if (nent > 0)
+        (g2p::kbegin("k_long_terms", s), k_long_terms<<<grid_for(nent), kThreads, 0, s>>>(c, B.map, B.cptr, B.cedge, B.caval, nshort, nlong, ncol, toff,
+                                                         P.k0, P.v0), g2p::kend(s));
+    dfree(nt, s); dfree(toff, s);
+    int64_t *counts;
+    G2P_TRY(dalloc(&counts, sort_counts_size(nterm), s));
+    G2P_TRY(ensure_scan_work(m, sort_counts_size(nterm)));
+    bool in1 = false;
+    G2P_TRY(radix_sort_pairs(P.k0, P.v0, P.k1, P.v1, nterm, bits_for((uint64_t)nlong * (uint64_t)ncol), counts,
+                             m->scan_work, &in1, s));
+    dfree(counts, s);
+    uint64_t *sk = in1 ? P.k1 : P.k0;
+    double *sv = in1 ? P.v1 : P.v0;
+    G2P_TRY(dalloc(&P.head, nterm + 1, s));
+    G2P_TRY(dalloc(&P.segid, nterm + 1, s));
+    (g2p::kbegin("k_heads", s), k_heads<<<grid_for(nterm), kThreads, 0, s>>>(sk, nterm, P.head), g2p::kend(s));
+    G2P_TRY(ensure_scan_work(m, nterm + 1));
+    const int64_t *hp = P.head;
+    auto hop = [hp, nterm] __device__(int64_t i) -> int64_t { return i < nterm ? hp[i] : 0; };
+    G2P_TRY(exclusive_scan(hop, nterm + 1, P.segid, m->scan_work, s));
+    G2P_CUDA(cudaMemcpyAsync(&P.nseg, P.segid + nterm, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    const int64_t nseg = P.nseg;
+    G2P_TRY(dalloc(&P.okey, nseg, s)); G2P_TRY(dalloc(&P.oval, nseg, s));
+    G2P_TRY(dalloc(&P.keep, nseg + 1, s)); G2P_TRY(dalloc(&P.kpos, nseg + 1, s));
+    G2P_TRY(dalloc(&P.sstart, nseg + 1, s));
+    (g2p::kbegin("k_seg_bounds", s), k_seg_bounds<<<grid_for(nterm), kThreads, 0, s>>>(P.head, P.segid, nterm, nseg, P.sstart), g2p::kend(s));
+    cudaStream_t ss = s;
+    if (on_side) {
+        if (!m->side) G2P_CUDA(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+        cudaEvent_t fork;
+        G2P_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+        G2P_CUDA(cudaEventRecord(fork, s));
+        G2P_CUDA(cudaStreamWaitEvent(m->side, fork, 0));
+        cudaEventDestroy(fork);
+        ss = m->side;
+    }
+    (g2p::kbegin("k_seg_sum", ss), k_seg_sum<<<grid_for(nseg), kThreads, 0, ss>>>(sk, sv, nseg, P.sstart, P.okey, P.oval, P.keep), g2p::kend(ss));
+    (g2p::kbegin("k_seg_sum_long", ss), k_seg_sum_long<<<grid_for(32 * nseg), kThreads, 0, ss>>>(sk, sv, nseg, P.sstart, P.okey, P.oval, P.keep), g2p::kend(ss));
+    if (on_side) {
+        G2P_CUDA(cudaEventCreateWithFlags(&P.done, cudaEventDisableTiming));
+        G2P_CUDA(cudaEventRecord(P.done, ss));
+    }
+    return G2P_OK;
+}
+
+// Part two: waits for the ordered sums, then row offsets and entries.  Every
+// buffer the side stream reads is freed here, after the wait.
+static g2p_status lap_finish(g2p_mesh *m, LapPending &P) {
+    cudaStream_t s = m->stream;
+    if (P.done) {
+        G2P_CUDA(cudaStreamWaitEvent(s, P.done, 0));
+        cudaEventDestroy(P.done);
+        P.done = nullptr;
+    }
+    const V0Ctx &c = P.c;
+    V0Basis &B = *P.B;
+    Csr<double> &A = *P.A;
+    const int64_t ncol = P.ncol, nshort = P.nshort, nseg = P.nseg;
+    if (P.nlong > 0) {
+        (g2p::kbegin("k_long_rowlen", s), k_long_rowlen<<<grid_for(nseg), kThreads, 0, s>>>(P.okey, P.keep, nseg, ncol, P.rowlen + nshort), g2p::kend(s));
+        const int64_t *kp = P.keep;
         auto kop = [kp, nseg] __device__(int64_t i) -> int64_t { return i < nseg ? kp[i] : 0; };
         G2P_TRY(ensure_scan_work(m, nseg + 1));
-        G2P_TRY(exclusive_scan(kop, nseg + 1, kpos, m->scan_work, s));
-        dfree(head, s); dfree(segid, s);
-        dfree(k0, s); dfree(k1, s); dfree(v0, s); dfree(v1, s);
+        G2P_TRY(exclusive_scan(kop, nseg + 1, P.kpos, m->scan_work, s));
+        dfree(P.sstart, s); dfree(P.head, s); dfree(P.segid, s);
+        dfree(P.k0, s); dfree(P.k1, s); dfree(P.v0, s); dfree(P.v1, s);
     }
     int64_t nnz = 0;
-    G2P_TRY(g2p_build_rowptr(m, rowlen, ncol, &A.ptr, &nnz));
-    dfree(rowlen, s);
+    G2P_TRY(g2p_build_rowptr(m, P.rowlen, ncol, &A.ptr, &nnz));
+    dfree(P.rowlen, s);
     A.n = A.m = ncol;
     A.nnz = nnz;
     G2P_TRY(dalloc(&A.col, nnz, s));
     G2P_TRY(dalloc(&A.val, nnz, s));
     if (nshort > 0)
-        (g2p::kbegin("k_short_rows_fill", s), k_short_rows_fill<<<grid_for(nshort), kThreads, 0, s>>>(c, B.map, is_ac, B.cptr, B.cedge, B.caval, nshort, A.ptr,
+        (g2p::kbegin("k_short_rows_fill", s), k_short_rows_fill<<<grid_for(nshort), kThreads, 0, s>>>(c, B.map, P.is_ac, B.cptr, B.cedge, B.caval, nshort, A.ptr,
                                                                 A.col, A.val), g2p::kend(s));
-    if (nlong > 0) {
-        (g2p::kbegin("k_long_scatter", s), k_long_scatter<<<grid_for(nseg), kThreads, 0, s>>>(okey, oval, keep, kpos, nseg, ncol, nshort, A.ptr, 0, A.col,
+    if (P.nlong > 0) {
+        (g2p::kbegin("k_long_scatter", s), k_long_scatter<<<grid_for(nseg), kThreads, 0, s>>>(P.okey, P.oval, P.keep, P.kpos, nseg, ncol, nshort, A.ptr, 0, A.col,
                                                            A.val), g2p::kend(s));
-        dfree(okey, s); dfree(oval, s); dfree(keep, s); dfree(kpos, s);
+        dfree(P.okey, s); dfree(P.oval, s); dfree(P.keep, s); dfree(P.kpos, s);
     }
     G2P_CUDA(cudaGetLastError());
     G2P_CUDA(cudaStreamSynchronize(s));
     return G2P_OK;
+}
+
+static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool is_ac, int64_t nshort, Csr<double> &A) {
+    LapPending P;
+    G2P_TRY(lap_begin(m, c, B, is_ac, nshort, A, P, false));
+    return lap_finish(m, P);
 }
 
 __global__ void k_is_cond_node(const int32_t *mark_node, int64_t n, int64_t *flag) {
@@ -638,8 +684,14 @@ __global__ void k_compact_cond(const int32_t *mark_node, int64_t n, const int64_
         if (mark_node[i] != 0) { key[pos[i]] = (uint32_t)mark_node[i]; node[pos[i]] = (int32_t)i; }
 }
 
-g2p_status g2p_run_v0(g2p_mesh *m) {
+g2p_status g2p_v0_finish(g2p_mesh *m);
+
+// V0 bases and Laplacians.  With defer_ad, Ad's ordered conductor sums are
+// left running on the side stream and g2p_v0_finish completes Ad; Ac and
+// everything else is complete on return.
+g2p_status g2p_run_v0_ex(g2p_mesh *m, bool defer_ad) {
     if (m->v0_done) return G2P_OK;
+    if (m->ad_pending) return defer_ad ? G2P_OK : g2p_v0_finish(m);
     G2P_TRY(g2p_run_index_maps(m));
     const Dims &d = m->d;
     cudaStream_t s = m->stream;
@@ -804,14 +856,30 @@ g2p_status g2p_run_v0(g2p_mesh *m) {
         (g2p::kbegin("k_edge_view", s), k_edge_view<<<grid_for(d.N_edge), kThreads, 0, s>>>(c, which == 1, B.map, d1col, B.ecol, B.eval, B.eaval), g2p::kend(s));
     }
     G2P_CUDA(cudaGetLastError());
-    // ---- Laplacians
-    G2P_TRY(build_laplacian(m, c, Vd, false, nd1, m->Ad));
+    // ---- Laplacians: Ad's ordered conductor sums run on the side stream
+    // while Ac is built
+    auto *P = new LapPending();
+    g2p_status st = lap_begin(m, c, Vd, false, nd1, m->Ad, *P, true);
+    if (st != G2P_OK) { delete P; return st; }
+    m->ad_pending = P;
     G2P_TRY(build_laplacian(m, c, Vc, true, Vc.ncol, m->Ac));
     dfree(d1col, s);
     G2P_CUDA(cudaStreamSynchronize(s));
-    m->v0_done = true;
-    return G2P_OK;
+    return defer_ad ? G2P_OK : g2p_v0_finish(m);
 }
+
+g2p_status g2p_v0_finish(g2p_mesh *m) {
+    if (m->v0_done) return G2P_OK;
+    if (!m->ad_pending) return g2p_run_v0_ex(m, false);
+    LapPending *P = m->ad_pending;
+    m->ad_pending = nullptr;
+    g2p_status st = lap_finish(m, *P);
+    delete P;
+    if (st == G2P_OK) m->v0_done = true;
+    return st;
+}
+
+g2p_status g2p_run_v0(g2p_mesh *m) { return g2p_run_v0_ex(m, false); }
 
 extern "C" g2p_status g2p_assemble_v0(g2p_mesh *m, g2p_sizes *out) {
     if (!m) return G2P_ERR_INVALID;
