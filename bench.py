@@ -116,6 +116,23 @@ class Clocks:
         return out
 
 
+def max_over_ranks(ms: float, world: int, device: str = "cuda") -> float:
+    """Step time of the whole job: the slowest replica's (a MAX all-reduce
+    over the ranks; the replicas share no data)."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(units_per_replica: int, world: int, ms: float) -> float:
+    """Port-frequency solves per second of N replicas each doing one job per
+    step, timed by the slowest one (weak scaling)."""
+    return world * units_per_replica / (ms / 1e3)
+
+
 def make_desc(d, place, torch):
     """MeshDesc arrays as torch tensors on `place` ('pinned' or 'cuda')."""
     arrays = dict(
@@ -196,11 +213,7 @@ def run_gb300(args):
             bms, bby, bn = (C.c_double * 8)(), (C.c_double * 8)(), (C.c_int64 * 8)()
             L.g2p_profile_buckets(bms, bby, bn)
             kern = (ms.value, by.value, nl.value, list(bms), list(bby), list(bn))
-        el = e0.elapsed_time(e1) / k
-        if world > 1:
-            t = torch.tensor([el], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            el = float(t.item())
+        el = max_over_ranks(e0.elapsed_time(e1) / k, world)
         return el, L.g2p_launch_count() - n0, kern
 
     if args.once:
@@ -231,8 +244,8 @@ def run_gb300(args):
     z_err = float(np.max(np.abs(zc - z64c)) / max(np.max(np.abs(z64c)), 1e-300))
     fp64_ms, _, _ = timed(dev, 1, prm=p64) if args.precision == "mixed" or args.batch else (ms, 0, None)
     units = d.num_ports * d.nfreq
-    value = world * units / (ms / 1e3)
-    e2e = world * units / (ms_e2e / 1e3)
+    value = whole_job_value(units, world, ms)
+    e2e = whole_job_value(units, world, ms_e2e)
     h2d = sum(int(pin[k].numel() * pin[k].element_size()) for k in pin)
     d2h = int(z.numel() * z.element_size())
     peaks = {}
