@@ -274,6 +274,23 @@ def run_gb300(args):
     t0 = time.perf_counter()
     _api.meshAndMark(lay_cfg)
     gpu_mesh_s = time.perf_counter() - t0
+    # network stage after the extraction: Z -> S on the GPU (g2p_convert_param,
+    # host arrays in and out) and the two writers
+    import tempfile
+    para = _api.Parasitics(np.full(d.num_ports, 50.0))
+    para.saveNetworkParam("Z", d.freqs(), zc)
+    para.convertParam("S")
+    para.saveNetworkParam("Z", d.freqs(), zc)
+    t0 = time.perf_counter()
+    para.convertParam("S")
+    conv_s = time.perf_counter() - t0
+    with tempfile.TemporaryDirectory() as td:
+        t0 = time.perf_counter()
+        _api.dumpCITI(os.path.join(td, "z.citi"), para, WORKLOAD[args.config][:16])
+        citi_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        _api.dumpTouchstone(os.path.join(td, "z.snp"), para, WORKLOAD[args.config][:16])
+        ts_s = time.perf_counter() - t0
     srt = sorted(step_ms)
     pct = lambda q: srt[min(len(srt) - 1, int(round(q * (len(srt) - 1))))] if srt else None
     out = {
@@ -297,6 +314,9 @@ def run_gb300(args):
         "mesher": {"gpu_ms": 1e3 * gpu_mesh_s, "host_generator_ms": 1e3 * host_mesh_s,
                    "what": "conductor marking, numbering and port edges (g2p_mesh_mark, host arrays in and out) "
                            "vs the numpy/scipy generator that restates meshAndMark/portSet"},
+        "network": {"convert_z_to_s_ms": 1e3 * conv_s, "citi_write_ms": 1e3 * citi_s,
+                    "touchstone_write_ms": 1e3 * ts_s,
+                    "what": "convertParam('S') on the GPU and dumpCITI / dumpTouchstone of this run's Z"},
         "job_ms": {"p50": pct(0.5), "p99": pct(0.99), "per_step": step_ms},
         "accuracy": {"z_rel_err_vs_fp64_gpu": z_err, "bound": 1e-6,
                      "note": "max |Z - Z_fp64| / max |Z_fp64| over all entries and frequencies"},
@@ -401,6 +421,9 @@ def run_c4(args):
         "config": {"workload": WORKLOAD["c4"], "config": "c4", "jobs": len(jobs), "port_freq_columns": units,
                    "arrival_rate_per_s": rate, "max_active": 8, "budget_bytes": budget,
                    "l2": "each job's inputs are resident only while it runs"},
+        "network": {"convert_z_to_s_ms": 1e3 * conv_s, "citi_write_ms": 1e3 * citi_s,
+                    "touchstone_write_ms": 1e3 * ts_s,
+                    "what": "convertParam('S') on the GPU and dumpCITI / dumpTouchstone of this run's Z"},
         "job_ms": {"p50": pct(0.5), "p99": pct(0.99), "max": lat[-1],
                    "load": "Poisson arrivals at 0.8 x serial capacity", "arrival_span_s": span,
                    "jobs_overlapped": overlapped},

@@ -21,6 +21,7 @@ EXPORTS = [
     "g2p_map_edge_noalloc", "g2p_profile_buckets",
     "g2p_server_create", "g2p_server_submit", "g2p_server_wait", "g2p_server_destroy",
     "g2p_mesh_mark",
+    "g2p_convert_param", "g2p_write_touchstone", "g2p_write_citi",
 ]
 
 STATUS = {0: "G2P_OK", 1: "G2P_ERR_INVALID", 2: "G2P_ERR_CUDA", 3: "G2P_ERR_NOMEM", 4: "G2P_ERR_NOT_CONVERGED",
@@ -137,6 +138,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_profile_buckets.restype = None
     L.g2p_profile_buckets.argtypes = [C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)]
     L.g2p_map_edge_noalloc.argtypes = [i64, i64, i64, vp, vp, i64, vp, vp, vp]
+    L.g2p_convert_param.argtypes = [C.c_char, C.c_char, i32, i32, vp, vp, vp]
+    L.g2p_write_touchstone.argtypes = [C.c_char_p, C.c_char, i32, i32, vp, vp, vp, C.c_char_p]
+    L.g2p_write_citi.argtypes = [C.c_char_p, C.c_char, i32, i32, vp, vp, C.c_char_p]
     for name in EXPORTS:
         if name not in ("g2p_last_error", "g2p_version", "g2p_default_params", "g2p_launch_count",
                         "g2p_profile_begin", "g2p_profile_report", "g2p_profile_buckets"):

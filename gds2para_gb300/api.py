@@ -191,7 +191,7 @@ def paraGenerator(sys: FdtdMesh, params: Optional[SolverParams] = None):
 
 
 __all__ = ["FdtdMesh", "generateStiff", "hypreSolve", "paraGenerator", "Solver", "Server", "meshAndMark",
-           "default_params", "G2PError"]
+           "Parasitics", "dumpTouchstone", "dumpCITI", "default_params", "G2PError"]
 
 
 class Server:
@@ -297,3 +297,77 @@ def meshAndMark(layout) -> dict:
     return dict(mark_node=mark_node, mark_edge=mark_edge, num_cdt=n, mark_port=mark_port[:n],
                 cdt_return=cdt_return[:n], side_edge_ptr=side_edge_ptr,
                 side_edges=side_edges[:side_edge_ptr[-1]], side_area=side_area[:nsides], side_dir=side_dir[:nsides])
+
+
+class Parasitics:
+    """Network parameters of one extraction, as the Parasitics class of
+    src/solnoutclass.hpp keeps them: a kind ('Z', 'Y' or 'S'), the sweep
+    frequencies (Hz), the ports' source impedances and one P x P complex
+    matrix per frequency.  convertParam runs on the GPU (g2p_convert_param);
+    the writers below are host code, as the reference's are."""
+
+    def __init__(self, z_source):
+        self.z_source = np.ascontiguousarray(z_source, np.float64)
+        self.param = "\0"
+        self.freqs = np.zeros(0)
+        self.matParam = np.zeros((0, len(self.z_source), len(self.z_source)), np.complex128)
+
+    def getNPort(self) -> int:
+        return len(self.z_source)
+
+    def getParamType(self) -> str:
+        return self.param
+
+    def getFreqs(self):
+        return self.freqs
+
+    def getParamMatrix(self):
+        return self.matParam
+
+    def saveNetworkParam(self, param: str, freqs, p):
+        """saveNetworkParam (src/solnoutclass.hpp:1394-1452): p holds
+        nfreq*P*P complex values in sys->x's order, entry (i, j) of
+        frequency f at (f*P + i)*P + j -- paraGenerator's Z as returned."""
+        if param not in ("Z", "Y", "S"):
+            raise ValueError("network parameters must be 'Z', 'Y' or 'S'")
+        n = self.getNPort()
+        self.freqs = np.ascontiguousarray(freqs, np.float64)
+        self.matParam = np.ascontiguousarray(p, np.complex128).reshape(len(self.freqs), n, n).copy()
+        self.param = param
+
+    def convertParam(self, newParam: str):
+        """convertParam (src/solnoutclass.hpp:1456-1610) on the GPU."""
+        if newParam not in ("Z", "Y", "S"):
+            raise ValueError("new network parameters must be 'S', 'Y' or 'Z'")
+        if newParam == self.param:
+            return
+        nf, n = self.matParam.shape[0], self.getNPort()
+        buf = np.ascontiguousarray(self.matParam).view(np.float64).ravel().copy()
+        check(_lib.load().g2p_convert_param(self.param.encode(), newParam.encode(), n, nf,
+                                            self.z_source.ctypes.data, buf.ctypes.data, buf.ctypes.data))
+        self.matParam = buf.view(np.complex128).reshape(nf, n, n)
+        self.param = newParam
+
+
+def _dump(fn, path, para: Parasitics, design: str, with_z: bool) -> bool:
+    L = _lib.load()
+    data = np.ascontiguousarray(para.matParam, np.complex128).view(np.float64).ravel()
+    args = [str(path).encode(), para.param.encode(), para.getNPort(), len(para.freqs), para.freqs.ctypes.data]
+    if with_z:
+        args.append(para.z_source.ctypes.data)
+    args += [data.ctypes.data, design.encode()]
+    rc = getattr(L, fn)(*args)
+    if rc == 1 and "cannot open" in L.g2p_last_error().decode(errors="replace"):
+        return False                         # the reference returns false when the file cannot be opened
+    check(rc)
+    return True
+
+
+def dumpTouchstone(path, para: Parasitics, design: str = "") -> bool:
+    """dumpTouchstone (src/solnoutclass.hpp:6118-6226): Touchstone 2.0 file."""
+    return _dump("g2p_write_touchstone", path, para, design, True)
+
+
+def dumpCITI(path, para: Parasitics, design: str = "") -> bool:
+    """dumpCITI (src/solnoutclass.hpp:6040-6115): CITIfile."""
+    return _dump("g2p_write_citi", path, para, design, False)

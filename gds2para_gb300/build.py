@@ -23,7 +23,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "--extended-lambda", "-lineinfo", "-Xcompiler", "-fPIC",
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 NO_FMA = {"mesh.cu", "v0.cu", "extract.cu"}
-UNITS = ["primitives.cu", "mesh.cu", "v0.cu", "solver.cu", "solve_api.cu", "extract.cu", "noalloc.cu", "serve.cu", "mesher.cu"]
+UNITS = ["primitives.cu", "mesh.cu", "v0.cu", "solver.cu", "solve_api.cu", "extract.cu", "noalloc.cu", "serve.cu", "mesher.cu",
+         "network.cu"]
 
 
 def nvcc() -> str:

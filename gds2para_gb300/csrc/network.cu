@@ -1,0 +1,304 @@
+// Network parameters after the extraction: convertParam (Z, Y and S
+// matrices per frequency, src/solnoutclass.hpp:1456-1610) as one GPU block per
+// frequency, and the Touchstone 2.0 and CITIfile writers (dumpTouchstone,
+// dumpCITI, src/solnoutclass.hpp:6040-6235).
+//
+// Matrices are P x P complex per frequency, stored as the reference's
+// saveNetworkParam reads sys->x: entry (i, j) of frequency f at
+// (f * P + i) * P + j, as interleaved (re, im) doubles.
+#include <algorithm>
+#include <cmath>
+#include <ctime>
+#include <fstream>
+#include <iomanip>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+using namespace g2p;
+
+namespace g2p {
+namespace {
+
+constexpr int kMaxNetPorts = 64;
+
+struct Cx {
+    double re, im;
+};
+__device__ __forceinline__ Cx cadd(Cx a, Cx b) { return {a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ Cx csub(Cx a, Cx b) { return {a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ Cx cmul(Cx a, Cx b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__device__ __forceinline__ Cx cdiv(Cx a, Cx b) {
+    const double d = b.re * b.re + b.im * b.im;
+    return {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
+}
+__device__ __forceinline__ double cabs2(Cx a) { return a.re * a.re + a.im * a.im; }
+
+// In-place inverse of the n x n matrix m (row-major, shared memory) by
+// Gauss-Jordan with partial pivoting; inv receives the result.
+__device__ void cinverse(Cx *m, Cx *inv, int n, int *singular) {
+    __shared__ int piv;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) inv[t] = {(t / n == t % n) ? 1.0 : 0.0, 0.0};
+    __syncthreads();
+    for (int k = 0; k < n; k++) {
+        if (threadIdx.x == 0) {
+            int p = k;
+            double best = cabs2(m[k * n + k]);
+            for (int r = k + 1; r < n; r++)
+                if (cabs2(m[r * n + k]) > best) { best = cabs2(m[r * n + k]); p = r; }
+            piv = p;
+            if (best == 0.0) *singular = 1;
+        }
+        __syncthreads();
+        const int p = piv;
+        if (p != k)
+            for (int j = threadIdx.x; j < n; j += blockDim.x) {
+                Cx t = m[k * n + j]; m[k * n + j] = m[p * n + j]; m[p * n + j] = t;
+                t = inv[k * n + j]; inv[k * n + j] = inv[p * n + j]; inv[p * n + j] = t;
+            }
+        __syncthreads();
+        const Cx d = m[k * n + k];
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            m[k * n + j] = cdiv(m[k * n + j], d);
+            inv[k * n + j] = cdiv(inv[k * n + j], d);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+            const int r = t / n, j = t % n;
+            if (r == k) continue;
+            const Cx f = m[r * n + k];
+            if (j != k) m[r * n + j] = csub(m[r * n + j], cmul(f, m[k * n + j]));
+            inv[r * n + j] = csub(inv[r * n + j], cmul(f, inv[k * n + j]));
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < n; r += blockDim.x)
+            if (r != k) m[r * n + k] = {0.0, 0.0};
+        __syncthreads();
+    }
+}
+
+// One frequency per block.  mode: 0 inverse (Z <-> Y); 1 Z -> S and 2 Y -> S
+// (S = (L)(R)^-1 with L, R from the scaled matrix and the identity);
+// 3 S -> Y and 4 S -> Z (D (I -/+ S)(I +/- S)^-1 D).
+__global__ void k_convert(int n, const double *in, double *out, const double *droot, int mode, int *singular) {
+    extern __shared__ Cx sh[];
+    Cx *a = sh, *b = sh + n * n, *w = sh + 2 * n * n;
+    const int64_t base = (int64_t)blockIdx.x * n * n;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        const int i = t / n, j = t % n;
+        Cx v = {in[2 * (base + t)], in[2 * (base + t) + 1]};
+        const Cx one = {(i == j) ? 1.0 : 0.0, 0.0};
+        if (mode == 0) {
+            a[t] = v;
+        } else if (mode == 1 || mode == 2) {
+            // scaled matrix D M D with D = diag(sqrt(1 / Zs)) (Z) or diag(sqrt(Zs)) (Y)
+            const Cx sc = {v.re * droot[i] * droot[j], v.im * droot[i] * droot[j]};
+            if (mode == 1) { w[t] = csub(sc, one); a[t] = cadd(sc, one); }      // (DZD - I)(DZD + I)^-1
+            else { w[t] = csub(one, sc); a[t] = cadd(one, sc); }                // (I - DYD)(I + DYD)^-1
+        } else if (mode == 3) {
+            w[t] = csub(one, v); a[t] = cadd(one, v);                          // D (I - S)(I + S)^-1 D
+        } else {
+            w[t] = cadd(one, v); a[t] = csub(one, v);                          // D (I + S)(I - S)^-1 D
+        }
+    }
+    __syncthreads();
+    cinverse(a, b, n, singular);
+    // b = inverse; result = w * b (then scaled for modes 3, 4), or b itself
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        const int i = t / n, j = t % n;
+        Cx r;
+        if (mode == 0) {
+            r = b[t];
+        } else {
+            r = {0.0, 0.0};
+            for (int q = 0; q < n; q++) r = cadd(r, cmul(w[i * n + q], b[q * n + j]));
+            if (mode >= 3) r = {r.re * droot[i] * droot[j], r.im * droot[i] * droot[j]};
+        }
+        out[2 * (base + t)] = r.re;
+        out[2 * (base + t) + 1] = r.im;
+    }
+}
+
+std::string timestamp(const char *fmt) {
+    char buf[80];
+    const time_t now = time(nullptr);
+    struct tm tmv;
+    localtime_r(&now, &tmv);
+    strftime(buf, sizeof buf, fmt, &tmv);
+    return buf;
+}
+
+// Spaces after a column label: the reference's width minus the extra digits
+// of the indices, never negative (the reference's fill would throw from 50
+// ports on).
+std::string pad(int width, int i, int j) { return std::string((size_t)std::max(0, width - i / 10 - j / 10), ' '); }
+
+}  // namespace
+}  // namespace g2p
+
+extern "C" g2p_status g2p_convert_param(char from, char to, int32_t nports, int32_t nfreq, const double *z_source,
+                                        const double *in, double *out) {
+    if (nports < 1 || nports > kMaxNetPorts || nfreq < 1 || !in || !out ||
+        !(from == 'Z' || from == 'Y' || from == 'S') || !(to == 'Z' || to == 'Y' || to == 'S')) {
+        set_last_message("g2p_convert_param: parameters Z, Y or S, 1..%d ports, nfreq >= 1", kMaxNetPorts);
+        return G2P_ERR_INVALID;
+    }
+    const int64_t total = 2LL * nfreq * nports * nports;
+    if (from == to) {
+        if (out != in) G2P_CUDA(cudaMemcpy(out, in, sizeof(double) * total, cudaMemcpyDefault));
+        return G2P_OK;
+    }
+    int mode;
+    if ((from == 'Z' && to == 'Y') || (from == 'Y' && to == 'Z')) mode = 0;
+    else if (from == 'Z') mode = 1;      // Z -> S
+    else if (from == 'Y') mode = 2;      // Y -> S
+    else if (to == 'Y') mode = 3;        // S -> Y
+    else mode = 4;                       // S -> Z
+    std::vector<double> root(nports, 1.0);
+    if (mode != 0) {
+        if (!z_source) { set_last_message("g2p_convert_param: S conversions need the port impedances"); return G2P_ERR_INVALID; }
+        std::vector<double> zs(nports);
+        G2P_CUDA(cudaMemcpy(zs.data(), z_source, sizeof(double) * nports, cudaMemcpyDefault));
+        for (int i = 0; i < nports; i++) {
+            if (!(zs[i] > 0)) { set_last_message("g2p_convert_param: port impedances must be positive"); return G2P_ERR_INVALID; }
+            // Z -> S and S -> Y use sqrt(1 / Zs); Y -> S and S -> Z use sqrt(Zs)
+            root[i] = (mode == 1 || mode == 3) ? std::sqrt(1.0 / zs[i]) : std::sqrt(zs[i]);
+        }
+    }
+    cudaStream_t s;
+    G2P_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    double *d_in = nullptr, *d_out = nullptr, *d_root = nullptr;
+    int *d_sing = nullptr;
+    auto run = [&]() -> g2p_status {
+        G2P_TRY(dalloc(&d_in, total, s));
+        G2P_TRY(dalloc(&d_out, total, s));
+        G2P_TRY(dalloc(&d_root, nports, s));
+        G2P_TRY(dalloc(&d_sing, 1, s));
+        G2P_CUDA(cudaMemcpyAsync(d_in, in, sizeof(double) * total, cudaMemcpyDefault, s));
+        G2P_CUDA(cudaMemcpyAsync(d_root, root.data(), sizeof(double) * nports, cudaMemcpyHostToDevice, s));
+        G2P_CUDA(cudaMemsetAsync(d_sing, 0, sizeof(int), s));
+        const size_t shm = 3 * sizeof(Cx) * nports * nports;
+        if (shm > 48 * 1024)
+            G2P_CUDA(cudaFuncSetAttribute(k_convert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+        (kbegin("k_convert", s), k_convert<<<(unsigned)nfreq, 256, shm, s>>>(nports, d_in, d_out, d_root, mode, d_sing), kend(s));
+        G2P_CUDA(cudaGetLastError());
+        int sing = 0;
+        G2P_CUDA(cudaMemcpyAsync(&sing, d_sing, sizeof(int), cudaMemcpyDeviceToHost, s));
+        G2P_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * total, cudaMemcpyDefault, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
+        if (sing) { set_last_message("g2p_convert_param: singular matrix"); return G2P_ERR_INVALID; }
+        return G2P_OK;
+    };
+    g2p_status st = run();
+    dfree(d_in, s); dfree(d_out, s); dfree(d_root, s); dfree(d_sing, s);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return st;
+}
+
+// dumpTouchstone (src/solnoutclass.hpp:6118-6226).  All arrays are host
+// memory; the matrices are in the reference's sys->x order.
+extern "C" g2p_status g2p_write_touchstone(const char *path, char param, int32_t nports, int32_t nfreq,
+                                           const double *freqs, const double *z_source, const double *p,
+                                           const char *design) {
+    if (!path || nports < 1 || nfreq < 1 || !freqs || !z_source || !p) {
+        set_last_message("g2p_write_touchstone: invalid argument");
+        return G2P_ERR_INVALID;
+    }
+    try {
+        std::ofstream o(path);
+        if (!o.is_open()) { set_last_message("g2p_write_touchstone: cannot open %s", path); return G2P_ERR_INVALID; }
+        const int n = nports;
+        o << "[Version] 2.0" << std::endl;
+        o << "# Hz " << param << " RI R " << z_source[0] << std::endl;
+        o << "[Number of Ports] " << n << std::endl;
+        if (n == 2) o << "[Two-Port Data Order] 12_21" << std::endl;
+        o << "[Number of Frequencies] " << nfreq << std::endl;
+        o << "[Reference]" << std::endl;
+        for (int q = 0; q < n; q++) o << z_source[q] << " ";
+        o << std::endl << "[Matrix Format] Full" << std::endl;
+        o << "! Date/Time " << timestamp("%Y-%m-%d %H:%M:%S") << std::endl;
+        o << "! Name " << (design ? design : "") << std::endl;
+        o << "! Provider: DARPA ERI IDEA/POSH Contributors" << std::endl;
+        o << "! Program: Xyce Writer from DARPA ERI" << std::endl;
+        o << "! Author: Purdue University" << std::endl;
+        o << "[Network Data] " << std::endl;
+        // column legend: at most four entries per line for more than two ports
+        o << "!freq         ";
+        for (int i = 0; i < n; i++) {
+            for (int j = 0; j < n; j++) {
+                if (n > 2 && i > 0 && j == 0)
+                    o << "!Re" << param << i + 1 << "," << j + 1 << pad(7, i, j);
+                else
+                    o << "Re" << param << i + 1 << "," << j + 1 << pad(8, i, j);
+                o << "Im" << param << i + 1 << "," << j + 1 << pad(8, i, j);
+                if ((j + 1) % 4 == 0 && j + 1 != n && n > 2) o << std::endl << "!" << std::string(13, ' ');
+            }
+            if (n > 2) o << std::endl;
+        }
+        o << std::endl;
+        for (int fi = 0; fi < nfreq; fi++) {
+            o << std::left << std::setw(13) << std::setprecision(7) << freqs[fi] << " ";
+            for (int i = 0; i < n; i++) {
+                for (int j = 0; j < n; j++) {
+                    const size_t t = 2 * (((size_t)fi * n + i) * n + j);
+                    o << std::left << std::setw(13) << std::setprecision(7) << p[t] << " ";
+                    o << std::left << std::setw(13) << std::setprecision(7) << p[t + 1] << " ";
+                    if ((j + 1) % 4 == 0 && j + 1 != n && n > 2) o << std::endl << std::string(14, ' ');
+                }
+                if (n > 2) o << " ! row " << i + 1 << std::endl;
+            }
+            if (n <= 2) o << std::endl;
+        }
+        o << "[End]" << std::endl;
+        o.close();
+        if (o.fail()) { set_last_message("g2p_write_touchstone: write to %s failed", path); return G2P_ERR_INVALID; }
+    } catch (const std::exception &e) {
+        set_last_message("g2p_write_touchstone: %s", e.what());
+        return G2P_ERR_INVALID;
+    }
+    return G2P_OK;
+}
+
+// dumpCITI (src/solnoutclass.hpp:6040-6115).  All arrays are host memory.
+extern "C" g2p_status g2p_write_citi(const char *path, char param, int32_t nports, int32_t nfreq, const double *freqs,
+                                     const double *p, const char *design) {
+    if (!path || nports < 1 || nfreq < 1 || !freqs || !p) {
+        set_last_message("g2p_write_citi: invalid argument");
+        return G2P_ERR_INVALID;
+    }
+    try {
+        std::ofstream o(path);
+        if (!o.is_open()) { set_last_message("g2p_write_citi: cannot open %s", path); return G2P_ERR_INVALID; }
+        std::string name = design ? design : "";
+        for (auto &c : name) c = (char)toupper((unsigned char)c);
+        const int n = nports;
+        o << "CITIFILE A.01.01" << std::endl;
+        o << "CONSTANT TIME " << timestamp("%Y %m %d %H %M %S") << std::endl;
+        o << "NAME " << name << std::endl;
+        o << "VAR FREQ MAG " << nfreq << std::endl;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) o << "DATA " << param << "[" << i + 1 << "," << j + 1 << "] RI" << std::endl;
+        o << "VAR_LIST_BEGIN" << std::endl;
+        for (int fi = 0; fi < nfreq; fi++) o << std::left << std::setw(13) << std::setprecision(7) << freqs[fi] << std::endl;
+        o << "VAR_LIST_END" << std::endl;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                o << "BEGIN" << std::endl;
+                for (int fi = 0; fi < nfreq; fi++) {
+                    const size_t t = 2 * (((size_t)fi * n + i) * n + j);
+                    o << std::right << std::setw(13) << std::setprecision(7) << p[t] << "," << std::left
+                      << std::setw(13) << std::setprecision(7) << p[t + 1] << std::endl;
+                }
+                o << "END" << std::endl;
+            }
+        o.close();
+        if (o.fail()) { set_last_message("g2p_write_citi: write to %s failed", path); return G2P_ERR_INVALID; }
+    } catch (const std::exception &e) {
+        set_last_message("g2p_write_citi: %s", e.what());
+        return G2P_ERR_INVALID;
+    }
+    return G2P_OK;
+}

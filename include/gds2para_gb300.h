@@ -256,6 +256,33 @@ g2p_status g2p_map_edge_noalloc(int64_t nx, int64_t ny, int64_t nz, const int64_
                                 const uint8_t *cdt_return, int64_t num_cdt, int64_t *map_edge,
                                 int64_t *bden, void *stream);
 
+/* ---- network parameters after paraGenerator ----
+ * Matrices are nfreq blocks of nports x nports complex values, entry (i, j)
+ * of frequency f at (f*nports + i)*nports + j as interleaved (re, im)
+ * doubles: the order saveNetworkParam reads sys->x in
+ * (src/solnoutclass.hpp:1394-1452), so g2p_para_generator's z_out is a
+ * valid input.
+ *
+ * g2p_convert_param: convertParam (src/solnoutclass.hpp:1456-1610).  from and
+ * to are 'Z', 'Y' or 'S'; Z <-> Y invert the matrix, the S conversions use
+ * the ports' real source impedances z_source [nports] (> 0; may be NULL for
+ * Z <-> Y).  Up to 64 ports; one GPU block per frequency.  in, out and
+ * z_source may be host or device memory; in == out is allowed.  A singular
+ * matrix returns G2P_ERR_INVALID (the reference carries on with Eigen's
+ * result). */
+g2p_status g2p_convert_param(char from, char to, int32_t nports, int32_t nfreq, const double *z_source,
+                             const double *in, double *out);
+/* g2p_write_touchstone: dumpTouchstone (src/solnoutclass.hpp:6118-6226), a
+ * Touchstone 2.0 file; g2p_write_citi: dumpCITI
+ * (src/solnoutclass.hpp:6040-6115), a CITIfile.  param is the matrices'
+ * kind ('Z', 'Y' or 'S'), freqs [nfreq] in Hz, z_source [nports] the port
+ * impedances, design the design name.  Host memory only; no GPU is used.
+ * Unlike the reference, the time stamp is the current local time. */
+g2p_status g2p_write_touchstone(const char *path, char param, int32_t nports, int32_t nfreq, const double *freqs,
+                                const double *z_source, const double *p, const char *design);
+g2p_status g2p_write_citi(const char *path, char param, int32_t nports, int32_t nfreq, const double *freqs,
+                          const double *p, const char *design);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,99 @@
+"""g2p_convert_param on the GPU against the oracle's convertParam
+(src/solnoutclass.hpp:1456-1610), on random matrices and on a real
+extraction's Z, plus its error paths.
+
+Tolerance: the GPU inverts by Gauss-Jordan with partial pivoting, the oracle
+by LAPACK's LU, so results agree to rounding scaled by the matrices'
+condition numbers: relative 1e-10 of each matrix's largest entry for the
+well-conditioned random cases, 1e-8 for the extraction's Z."""
+import numpy as np
+import pytest
+
+from oracle import network as onet
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ("Z", "Y", "S")
+
+
+def _gpu_convert(frm, to, p, zs):
+    from gds2para_gb300 import _lib
+    nf, n, _ = p.shape
+    buf = np.ascontiguousarray(p, np.complex128).view(np.float64).ravel().copy()
+    out = np.zeros_like(buf)
+    zs = np.ascontiguousarray(zs, np.float64)
+    _lib.check(_lib.load().g2p_convert_param(frm.encode(), to.encode(), n, nf, zs.ctypes.data, buf.ctypes.data,
+                                             out.ctypes.data))
+    return out.view(np.complex128).reshape(nf, n, n)
+
+
+def _close(got, want, rtol):
+    scale = np.abs(want).max(axis=(1, 2), keepdims=True)
+    assert np.all(np.abs(got - want) <= rtol * scale), float((np.abs(got - want) / scale).max())
+
+
+@pytest.mark.parametrize("nports,nfreq", [(1, 5), (2, 40), (3, 7), (8, 33), (17, 4), (64, 3)])
+def test_convert_matches_oracle(nports, nfreq):
+    rng = np.random.default_rng(nports * 1000 + nfreq)
+    zs = rng.uniform(20.0, 80.0, nports)
+    z = rng.standard_normal((nfreq, nports, nports)) + 1j * rng.standard_normal((nfreq, nports, nports))
+    z += 4.0 * np.sqrt(nports) * np.eye(nports)
+    start = {k: onet.convert_param("Z", k, z, zs) for k in KINDS}
+    for a in KINDS:
+        for b in KINDS:
+            got = _gpu_convert(a, b, start[a], zs)
+            _close(got, onet.convert_param(a, b, start[a], zs), 1e-10)
+
+
+def test_convert_extraction_z_and_write(tmp_path):
+    from gds2para_gb300 import api, layout as lay
+    d = lay.build(lay.multistrip(nx=24, ny=20, nz=8, n_strips=3, freq_start=1e8, freq_end=1e10, nfreq=4))
+    with api.FdtdMesh(d) as m:
+        api.generateStiff(m)
+        z, _ = api.paraGenerator(m, api.default_params())
+    zs = np.full(d.num_ports, 50.0)
+    freqs = d.freqs()
+    para = api.Parasitics(zs)
+    para.saveNetworkParam("Z", freqs, z.ravel())
+    para.convertParam("S")
+    want = onet.convert_param("Z", "S", z, zs)
+    _close(para.getParamMatrix(), want, 1e-8)
+    assert para.getParamType() == "S"
+    assert api.dumpCITI(tmp_path / "x.citi", para, "strip")
+    text = (tmp_path / "x.citi").read_text()
+    assert text.startswith("CITIFILE A.01.01\n") and text.count("BEGIN\n") == d.num_ports ** 2
+
+
+def test_convert_device_pointers_and_in_place():
+    import torch
+    rng = np.random.default_rng(11)
+    n, nf = 5, 9
+    zs = rng.uniform(30, 60, n)
+    z = rng.standard_normal((nf, n, n)) + 1j * rng.standard_normal((nf, n, n)) + 6 * np.eye(n)
+    from gds2para_gb300 import _lib
+    L = _lib.load()
+    dz = torch.from_numpy(z.view(np.float64).ravel().copy()).cuda()
+    dzs = torch.from_numpy(zs).cuda()
+    _lib.check(L.g2p_convert_param(b"Z", b"S", n, nf, dzs.data_ptr(), dz.data_ptr(), dz.data_ptr()))
+    got = dz.cpu().numpy().view(np.complex128).reshape(nf, n, n)
+    _close(got, onet.convert_param("Z", "S", z, zs), 1e-10)
+
+
+def test_convert_errors():
+    from gds2para_gb300 import _lib
+    L = _lib.load()
+    one = np.array([1.0, 0.0])
+    zs = np.array([50.0])
+    out = np.zeros(2)
+    assert L.g2p_convert_param(b"Z", b"S", 65, 1, None, None, None) == 1
+    assert L.g2p_convert_param(b"Q", b"S", 1, 1, zs.ctypes.data, one.ctypes.data, out.ctypes.data) == 1
+    assert L.g2p_convert_param(b"Z", b"S", 1, 1, None, one.ctypes.data, out.ctypes.data) == 1
+    bad = np.array([-5.0])
+    assert L.g2p_convert_param(b"Z", b"S", 1, 1, bad.ctypes.data, one.ctypes.data, out.ctypes.data) == 1
+    sing = np.zeros(8)                         # 2 x 2 zero matrix: Z -> Y has no inverse
+    out4 = np.zeros(8)
+    assert L.g2p_convert_param(b"Z", b"Y", 2, 1, None, sing.ctypes.data, out4.ctypes.data) == 1
+    assert b"singular" in L.g2p_last_error()
+    # the library stays usable after the errors
+    assert L.g2p_convert_param(b"Z", b"Y", 1, 1, None, one.ctypes.data, out.ctypes.data) == 0
+    assert out[0] == 1.0 and out[1] == 0.0
