@@ -61,7 +61,7 @@ def test_convert_extraction_z_and_write(tmp_path):
     assert para.getParamType() == "S"
     assert api.dumpCITI(tmp_path / "x.citi", para, "strip")
     text = (tmp_path / "x.citi").read_text()
-    assert text.startswith("CITIFILE A.01.01\n") and text.count("BEGIN\n") == d.num_ports ** 2
+    assert text.startswith("CITIFILE A.01.01\n") and text.count("\nBEGIN\n") == d.num_ports ** 2
 
 
 def test_convert_device_pointers_and_in_place():
