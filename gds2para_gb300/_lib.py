@@ -22,6 +22,7 @@ EXPORTS = [
     "g2p_server_create", "g2p_server_submit", "g2p_server_wait", "g2p_server_destroy",
     "g2p_mesh_mark",
     "g2p_convert_param", "g2p_write_touchstone", "g2p_write_citi",
+    "g2p_ybus_from_param", "g2p_write_xyce", "g2p_write_spef",
 ]
 
 STATUS = {0: "G2P_OK", 1: "G2P_ERR_INVALID", 2: "G2P_ERR_CUDA", 3: "G2P_ERR_NOMEM", 4: "G2P_ERR_NOT_CONVERGED",
@@ -141,6 +142,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_convert_param.argtypes = [C.c_char, C.c_char, i32, i32, vp, vp, vp]
     L.g2p_write_touchstone.argtypes = [C.c_char_p, C.c_char, i32, i32, vp, vp, vp, C.c_char_p]
     L.g2p_write_citi.argtypes = [C.c_char_p, C.c_char, i32, i32, vp, vp, C.c_char_p]
+    L.g2p_ybus_from_param.argtypes = [C.c_char, i32, dbl, vp, vp, vp]
+    L.g2p_write_xyce.argtypes = [C.c_char_p, C.c_char_p, i32, C.POINTER(C.c_char_p), dbl, vp, vp, dbl]
+    L.g2p_write_spef.argtypes = [C.c_char_p, C.c_char_p, i32, C.POINTER(C.c_char_p), C.c_char_p, vp, vp, dbl]
     for name in EXPORTS:
         if name not in ("g2p_last_error", "g2p_version", "g2p_default_params", "g2p_launch_count",
                         "g2p_profile_begin", "g2p_profile_report", "g2p_profile_buckets"):

@@ -191,7 +191,7 @@ def paraGenerator(sys: FdtdMesh, params: Optional[SolverParams] = None):
 
 
 __all__ = ["FdtdMesh", "generateStiff", "hypreSolve", "paraGenerator", "Solver", "Server", "meshAndMark",
-           "Parasitics", "dumpTouchstone", "dumpCITI", "default_params", "G2PError"]
+           "Parasitics", "dumpTouchstone", "dumpCITI", "dumpXyce", "dumpSPEF", "default_params", "G2PError"]
 
 
 class Server:
@@ -306,11 +306,18 @@ class Parasitics:
     matrix per frequency.  convertParam runs on the GPU (g2p_convert_param);
     the writers below are host code, as the reference's are."""
 
-    def __init__(self, z_source):
+    def __init__(self, z_source, port_names=None, port_dirs=None):
         self.z_source = np.ascontiguousarray(z_source, np.float64)
+        n = len(self.z_source)
+        self.port_names = list(port_names) if port_names is not None else [f"port{i + 1}" for i in range(n)]
+        self.port_dirs = "".join(port_dirs) if port_dirs is not None else "B" * n
+        if len(self.port_names) != n or len(self.port_dirs) != n:
+            raise ValueError("one name and one direction per port")
         self.param = "\0"
         self.freqs = np.zeros(0)
-        self.matParam = np.zeros((0, len(self.z_source), len(self.z_source)), np.complex128)
+        self.matParam = np.zeros((0, n, n), np.complex128)
+        self.matG = None
+        self.matC = None
 
     def getNPort(self) -> int:
         return len(self.z_source)
@@ -334,6 +341,23 @@ class Parasitics:
         self.freqs = np.ascontiguousarray(freqs, np.float64)
         self.matParam = np.ascontiguousarray(p, np.complex128).reshape(len(self.freqs), n, n).copy()
         self.param = param
+        self.computeYBusFromParam(0)
+
+    def computeYBusFromParam(self, indFreq: int):
+        """computeYBusFromParam (src/solnoutclass.hpp:1662-1748): the nodal
+        matrices matG, matC the Xyce and SPEF writers print; None for
+        S-parameters, where the reference has none."""
+        n = self.getNPort()
+        g = np.zeros((n, n))
+        c = np.zeros((n, n))
+        p0 = np.ascontiguousarray(self.matParam[indFreq]).view(np.float64).ravel()
+        rc = _lib.load().g2p_ybus_from_param(self.param.encode(), n, float(self.freqs[indFreq]), p0.ctypes.data,
+                                             g.ctypes.data, c.ctypes.data)
+        if rc == 5:                          # G2P_ERR_UNSUPPORTED: S-parameters
+            self.matG = self.matC = None
+            return
+        check(rc)
+        self.matG, self.matC = g, c
 
     def convertParam(self, newParam: str):
         """convertParam (src/solnoutclass.hpp:1456-1610) on the GPU."""
@@ -359,6 +383,42 @@ def _dump(fn, path, para: Parasitics, design: str, with_z: bool) -> bool:
     rc = getattr(L, fn)(*args)
     if rc == 1 and "cannot open" in L.g2p_last_error().decode(errors="replace"):
         return False                         # the reference returns false when the file cannot be opened
+    check(rc)
+    return True
+
+
+WRITE_THRESH = 1e-5     # src/solnoutclass.hpp:33
+
+
+def _nodal_args(para: Parasitics):
+    if para.matG is None:
+        raise ValueError("no nodal matrices: save Z- or Y-parameters first")
+    names = (C.c_char_p * para.getNPort())(*[nm.encode() for nm in para.port_names])
+    g = np.ascontiguousarray(para.matG, np.float64)
+    c = np.ascontiguousarray(para.matC, np.float64)
+    return names, g, c
+
+
+def dumpXyce(path, para: Parasitics, design: str, save_thresh: float = WRITE_THRESH) -> bool:
+    """dumpXyce / toXyce (src/solnoutclass.hpp:2094-2225): SPICE subcircuit."""
+    L = _lib.load()
+    names, g, c = _nodal_args(para)
+    rc = L.g2p_write_xyce(str(path).encode(), design.encode(), para.getNPort(), names, float(para.freqs[0]),
+                          g.ctypes.data, c.ctypes.data, save_thresh)
+    if rc == 1 and "cannot open" in L.g2p_last_error().decode(errors="replace"):
+        return False
+    check(rc)
+    return True
+
+
+def dumpSPEF(path, para: Parasitics, design: str, save_thresh: float = WRITE_THRESH) -> bool:
+    """dumpSPEF / toSPEF (src/solnoutclass.hpp:1972-2091): SPEF file."""
+    L = _lib.load()
+    names, g, c = _nodal_args(para)
+    rc = L.g2p_write_spef(str(path).encode(), design.encode(), para.getNPort(), names, para.port_dirs.encode(),
+                          g.ctypes.data, c.ctypes.data, save_thresh)
+    if rc == 1 and "cannot open" in L.g2p_last_error().decode(errors="replace"):
+        return False
     check(rc)
     return True
 

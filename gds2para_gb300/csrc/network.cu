@@ -302,3 +302,227 @@ extern "C" g2p_status g2p_write_citi(const char *path, char param, int32_t nport
     }
     return G2P_OK;
 }
+
+namespace g2p {
+namespace {
+
+// The nodal conductance and capacitance matrices the reference's Xyce and
+// SPEF writers print (row-major n x n), symmetrised as makeCSym/makeGSym do
+// (src/solnoutclass.hpp:1319-1390): a matrix that is not approximately
+// symmetric in Eigen's sense (|A - A^T|^2 <= 1e-24 min(|A|^2, |A^T|^2)) is
+// replaced by (A + A^T) * 0.5.
+struct Nodal {
+    int n;
+    std::vector<double> g, c;
+    std::vector<double> g_ground, c_ground;    // row sums (getGNodeGround / getCNodeGround)
+    double g_total = 0, c_total = 0;           // upper-triangle sums (getGTotal / getCTotal)
+};
+
+void symmetrise(std::vector<double> &a, int n) {
+    double d2 = 0, na = 0, nt = 0;
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+            const double x = a[(size_t)i * n + j], y = a[(size_t)j * n + i];
+            d2 += (x - y) * (x - y);
+            na += x * x;
+            nt += y * y;
+        }
+    const double prec = 1e-12;
+    if (d2 <= prec * prec * std::min(na, nt)) return;
+    std::vector<double> s(a.size());
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) s[(size_t)i * n + j] = (a[(size_t)i * n + j] + a[(size_t)j * n + i]) * 0.5;
+    a.swap(s);
+}
+
+Nodal nodal(int n, const double *G, const double *C) {
+    Nodal m;
+    m.n = n;
+    m.g.assign(G, G + (size_t)n * n);
+    m.c.assign(C, C + (size_t)n * n);
+    symmetrise(m.c, n);
+    symmetrise(m.g, n);
+    m.g_ground.assign(n, 0.0);
+    m.c_ground.assign(n, 0.0);
+    for (int i = 0; i < n; i++) {
+        double sg = 0, sc = 0;
+        for (int j = 0; j < n; j++) { sg += m.g[(size_t)i * n + j]; sc += m.c[(size_t)i * n + j]; }
+        m.g_ground[i] = sg;
+        m.c_ground[i] = sc;
+        for (int j = i; j < n; j++) { m.g_total += m.g[(size_t)i * n + j]; m.c_total += m.c[(size_t)i * n + j]; }
+    }
+    return m;
+}
+
+bool valid_names(int32_t n, const char *const *names) {
+    if (!names) return false;
+    for (int i = 0; i < n; i++)
+        if (!names[i]) return false;
+    return true;
+}
+
+}  // namespace
+}  // namespace g2p
+
+// computeYBusFromParam at the first frequency (src/solnoutclass.hpp:1662-1748,
+// the dense-matrix build), as saveNetworkParam calls it: from 'Z' the matrix
+// itself is taken as Y, from 'Y' its inverse (the reference's two branches);
+// G = Re Y and C(i, j) = -1 / (Im Y(i, j) * (2 pi f0)).  'S' is rejected: the
+// reference leaves its Y empty there.
+extern "C" g2p_status g2p_ybus_from_param(char param, int32_t nports, double freq0, const double *p0, double *G,
+                                          double *C) {
+    if (nports < 1 || nports > kMaxNetPorts || !p0 || !G || !C || !(param == 'Z' || param == 'Y')) {
+        set_last_message(param == 'S' ? "g2p_ybus_from_param: S-parameters have no nodal matrices"
+                                      : "g2p_ybus_from_param: invalid argument");
+        return param == 'S' ? G2P_ERR_UNSUPPORTED : G2P_ERR_INVALID;
+    }
+    const int n = nports;
+    std::vector<double> y((size_t)2 * n * n);
+    if (param == 'Y') {
+        G2P_TRY(g2p_convert_param('Y', 'Z', n, 1, nullptr, p0, y.data()));
+    } else {
+        std::copy(p0, p0 + y.size(), y.begin());
+    }
+    const double w = 2. * M_PI * freq0;
+    for (int t = 0; t < n * n; t++) {
+        G[t] = y[2 * t];
+        C[t] = -1 / (y[2 * t + 1] * w);
+    }
+    return G2P_OK;
+}
+
+// toXyce (src/solnoutclass.hpp:2094-2225, dense build): a SPICE subcircuit of
+// capacitors (inductors where a capacitance is negative), and resistors,
+// keeping elements at or above save_thresh times the total.
+extern "C" g2p_status g2p_write_xyce(const char *path, const char *design, int32_t nports,
+                                     const char *const *port_names, double freq0, const double *G, const double *C,
+                                     double save_thresh) {
+    if (!path || !design || nports < 1 || !valid_names(nports, port_names) || !G || !C) {
+        set_last_message("g2p_write_xyce: invalid argument");
+        return G2P_ERR_INVALID;
+    }
+    try {
+        std::ofstream o(path);
+        if (!o.is_open()) { set_last_message("g2p_write_xyce: cannot open %s", path); return G2P_ERR_INVALID; }
+        const int n = nports;
+        const Nodal m = nodal(n, G, C);
+        o << "* File: " << path << std::endl;
+        o << "* Design: " << design << std::endl;
+        o << "* Vendor: DARPA ERI Contributors" << std::endl;
+        o << "* Program: Xyce Writer from DARPA ERI" << std::endl;
+        o << "* Author: Purdue University" << std::endl;
+        o << "* Date: " << timestamp("%d-%m-%Y %H:%M:%S") << std::endl;
+        o << std::endl;
+        o << ".subckt " << design;
+        for (int i = 0; i < n; i++) o << " " << port_names[i];
+        o << std::endl;
+        const double w2 = std::pow(2. * M_PI * freq0, 2.);
+        int ncap = 1, nind = 1, nres = 1;
+        for (int i = 0; i < n; i++) {
+            for (int j = 0; j < n; j++) {
+                if (i == j && std::abs(m.c_ground[i]) >= save_thresh * m.c_total) {
+                    const double cng = m.c_ground[i];
+                    if (cng > 0.0) o << "C" << ncap++ << " " << port_names[i] << " 0 " << cng << std::endl;
+                    else o << "L" << nind++ << " " << port_names[i] << " 0 " << -1.0 / (cng * w2) << std::endl;
+                } else if (j > i && std::abs(-m.c[(size_t)i * n + j]) >= save_thresh * m.c_total) {
+                    const double cnn = -1.0 * m.c[(size_t)i * n + j];
+                    if (cnn > 0.0)
+                        o << "C" << ncap++ << " " << port_names[i] << " " << port_names[j] << " " << cnn << std::endl;
+                    else
+                        o << "L" << nind++ << " " << port_names[i] << " " << port_names[j] << " " << -1.0 / (cnn * w2)
+                          << std::endl;
+                }
+            }
+            for (int j = 0; j < n; j++) {
+                if (i == j && std::abs(m.g_ground[i]) >= save_thresh * m.g_total)
+                    o << "R" << nres++ << " " << port_names[i] << " 0 " << std::abs(1.0 / m.g_ground[i]) << std::endl;
+                else if (j > i && std::abs(-1.0 / m.g[(size_t)i * n + j]) >= save_thresh * m.g_total)
+                    o << "R" << nres++ << " " << port_names[i] << " " << port_names[j] << " "
+                      << std::abs(-1.0 / m.g[(size_t)i * n + j]) << std::endl;
+            }
+        }
+        o << ".ends" << std::endl;
+        o.close();
+        if (o.fail()) { set_last_message("g2p_write_xyce: write to %s failed", path); return G2P_ERR_INVALID; }
+    } catch (const std::exception &e) {
+        set_last_message("g2p_write_xyce: %s", e.what());
+        return G2P_ERR_INVALID;
+    }
+    return G2P_OK;
+}
+
+// toSPEF + dumpSPEF (src/solnoutclass.hpp:1972-2091, 6008-6030): one net
+// "all" connecting every port, with the same capacitor and resistor choices
+// as the Xyce writer, in IEEE 1481-1998 syntax.  Ports are referred to
+// through the name map (*1, *2, ...); port_dirs holds 'I', 'O' or 'B' per
+// port (NULL: all 'B').  The reference prints through the Parser-SPEF
+// library, whose exact layout (spacing, blank lines) this writer does not
+// reproduce.
+extern "C" g2p_status g2p_write_spef(const char *path, const char *design, int32_t nports,
+                                     const char *const *port_names, const char *port_dirs, const double *G,
+                                     const double *C, double save_thresh) {
+    if (!path || !design || nports < 1 || !valid_names(nports, port_names) || !G || !C) {
+        set_last_message("g2p_write_spef: invalid argument");
+        return G2P_ERR_INVALID;
+    }
+    try {
+        std::ofstream o(path);
+        if (!o.is_open()) { set_last_message("g2p_write_spef: cannot open %s", path); return G2P_ERR_INVALID; }
+        const int n = nports;
+        const Nodal m = nodal(n, G, C);
+        auto dir = [&](int i) {
+            const char d = port_dirs ? port_dirs[i] : 'B';
+            return d == 'O' ? "O" : d == 'I' ? "I" : "B";
+        };
+        o << "*SPEF \"IEEE 1481-1998\"" << std::endl;
+        o << "*DESIGN \"" << design << "\"" << std::endl;
+        o << "*DATE \"" << timestamp("%d-%m-%Y %H:%M:%S") << "\"" << std::endl;
+        o << "*VENDOR \"DARPA ERI Contributors\"" << std::endl;
+        o << "*PROGRAM \"SPEF Writer from DARPA ERI\"" << std::endl;
+        o << "*VERSION \"1.0\"" << std::endl;
+        o << "*DESIGN_FLOW \"NETLIST_TYPE_VERILOG\"" << std::endl;
+        o << "*DIVIDER /" << std::endl;
+        o << "*DELIMITER :" << std::endl;
+        o << "*BUS_DELIMITER [ ]" << std::endl;
+        o << "*T_UNIT 1 S" << std::endl;
+        o << "*C_UNIT 1 F" << std::endl;
+        o << "*R_UNIT 1 OHM" << std::endl;
+        o << "*L_UNIT 1 H" << std::endl << std::endl;
+        o << "*NAME_MAP" << std::endl;
+        for (int i = 0; i < n; i++) o << "*" << i + 1 << " " << port_names[i] << std::endl;
+        o << std::endl << "*PORTS" << std::endl;
+        for (int i = 0; i < n; i++) o << "*" << i + 1 << " " << dir(i) << std::endl;
+        o << std::endl << "*D_NET all " << m.c_total << std::endl;
+        o << "*CONN" << std::endl;
+        for (int i = 0; i < n; i++) o << "*P " << port_names[i] << " " << dir(i) << std::endl;
+        std::vector<std::string> caps, ress;
+        char buf[64];
+        auto num = [&](double v) { snprintf(buf, sizeof buf, "%g", v); return std::string(buf); };
+        for (int i = 0; i < n; i++) {
+            const std::string pi = "*" + std::to_string(i + 1);
+            for (int j = 0; j < n; j++) {
+                if (i == j && std::abs(m.c_ground[i]) >= save_thresh * m.c_total)
+                    caps.push_back(pi + " " + num(m.c_ground[i]));
+                else if (j > i && std::abs(-m.c[(size_t)i * n + j]) >= save_thresh * m.c_total)
+                    caps.push_back(pi + " *" + std::to_string(j + 1) + " " + num(-m.c[(size_t)i * n + j]));
+            }
+            for (int j = 0; j < n; j++) {
+                if (i == j && std::abs(m.g_ground[i]) >= save_thresh * m.g_total)
+                    ress.push_back(pi + " " + num(std::abs(1.0 / m.g_ground[i])));
+                else if (j > i && std::abs(-1.0 / m.g[(size_t)i * n + j]) >= save_thresh * m.g_total)
+                    ress.push_back(pi + " *" + std::to_string(j + 1) + " " + num(std::abs(-1.0 / m.g[(size_t)i * n + j])));
+            }
+        }
+        o << "*CAP" << std::endl;
+        for (size_t k = 0; k < caps.size(); k++) o << k + 1 << " " << caps[k] << std::endl;
+        o << "*RES" << std::endl;
+        for (size_t k = 0; k < ress.size(); k++) o << k + 1 << " " << ress[k] << std::endl;
+        o << "*END" << std::endl;
+        o.close();
+        if (o.fail()) { set_last_message("g2p_write_spef: write to %s failed", path); return G2P_ERR_INVALID; }
+    } catch (const std::exception &e) {
+        set_last_message("g2p_write_spef: %s", e.what());
+        return G2P_ERR_INVALID;
+    }
+    return G2P_OK;
+}

@@ -282,6 +282,27 @@ g2p_status g2p_write_touchstone(const char *path, char param, int32_t nports, in
                                 const double *z_source, const double *p, const char *design);
 g2p_status g2p_write_citi(const char *path, char param, int32_t nports, int32_t nfreq, const double *freqs,
                           const double *p, const char *design);
+/* g2p_ybus_from_param: computeYBusFromParam(0) (src/solnoutclass.hpp:1662-1748,
+ * dense build), which saveNetworkParam runs: nodal matrices G and C
+ * [nports*nports, row-major, host] from the first frequency's matrix p0
+ * (nports*nports complex, interleaved, host or device) at freq0 Hz.  As in
+ * the reference, 'Z' takes the matrix itself as Y and 'Y' takes its inverse
+ * (on the GPU); G = Re Y, C(i,j) = -1 / (Im Y(i,j) * 2 pi freq0).  'S'
+ * returns G2P_ERR_UNSUPPORTED (the reference leaves Y empty there). */
+g2p_status g2p_ybus_from_param(char param, int32_t nports, double freq0, const double *p0, double *G, double *C);
+/* g2p_write_xyce: dumpXyce / toXyce (src/solnoutclass.hpp:2094-2225,
+ * 6032-6037), a SPICE subcircuit; g2p_write_spef: dumpSPEF / toSPEF
+ * (src/solnoutclass.hpp:1972-2091, 6008-6030), an IEEE 1481-1998 SPEF file
+ * with one net.  G and C as g2p_ybus_from_param writes them (symmetrised
+ * inside, as makeGSym/makeCSym do); elements below save_thresh times the
+ * matrix total are left out (the reference's WRITE_THRESH is 1e-5).
+ * port_names [nports] are the subcircuit pins; port_dirs [nports] 'I', 'O'
+ * or 'B' (NULL: all 'B').  Host memory only; no GPU is used.  The SPEF
+ * layout is this writer's own (the reference prints through Parser-SPEF). */
+g2p_status g2p_write_xyce(const char *path, const char *design, int32_t nports, const char *const *port_names,
+                          double freq0, const double *G, const double *C, double save_thresh);
+g2p_status g2p_write_spef(const char *path, const char *design, int32_t nports, const char *const *port_names,
+                          const char *port_dirs, const double *G, const double *C, double save_thresh);
 
 #ifdef __cplusplus
 }

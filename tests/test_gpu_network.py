@@ -97,3 +97,19 @@ def test_convert_errors():
     # the library stays usable after the errors
     assert L.g2p_convert_param(b"Z", b"Y", 1, 1, None, one.ctypes.data, out.ctypes.data) == 0
     assert out[0] == 1.0 and out[1] == 0.0
+
+
+def test_ybus_from_y_parameters_inverts_on_the_gpu():
+    from gds2para_gb300 import api
+    rng = np.random.default_rng(5)
+    n = 6
+    y = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + 5 * np.eye(n)
+    para = api.Parasitics(np.full(n, 50.0))
+    para.saveNetworkParam("Y", [1e9], y.ravel())
+    # G = Re Y^-1 and C = -1 / (Im Y^-1 * 2 pi f0): compare Y^-1 entrywise,
+    # relative to its largest entry (the inverse is Gauss-Jordan vs LAPACK LU)
+    inv = np.linalg.inv(y)
+    scale = np.abs(inv).max()
+    w = 2.0 * np.pi * 1e9
+    assert np.abs(para.matG - inv.real).max() <= 1e-12 * scale
+    assert np.abs(-1 / (para.matC * w) - inv.imag).max() <= 1e-12 * scale

@@ -1,7 +1,8 @@
 """Network-parameter stage on the CPU: the oracle's convertParam restatement
-pinned against closed-form results, and the C-ABI Touchstone / CITIfile
-writers (host code, no GPU) against the oracle's text."""
-import os
+pinned against closed-form results; the C-ABI Touchstone, CITIfile and Xyce
+writers (host code, no GPU) against the oracle's text; the nodal matrices of
+computeYBusFromParam bit-exact; the SPEF writer's elements against the
+oracle's choices."""
 import re
 
 import numpy as np
@@ -105,3 +106,97 @@ def test_writer_rejects_bad_arguments():
     L = _lib_or_skip()
     assert L.g2p_write_touchstone(b"/dev/null", b"Z", 0, 1, None, None, None, b"") == 1
     assert L.g2p_write_citi(None, b"Z", 1, 1, None, None, b"") == 1
+
+
+def _nodal_case(n, seed, sym=True):
+    rng = np.random.default_rng(seed)
+    # a capacitive Z at 1 GHz: Im Z < 0 on and near the diagonal
+    z = rng.uniform(0.1, 5.0, (n, n)) - 1j * rng.uniform(50.0, 500.0, (n, n))
+    if sym:
+        z = (z + z.T) / 2
+    return z
+
+
+@pytest.mark.parametrize("n,sym", [(1, True), (2, True), (4, False), (9, True)])
+def test_ybus_and_xyce_match_oracle(tmp_path, n, sym):
+    from gds2para_gb300 import api
+    _lib_or_skip()
+    z = _nodal_case(n, 40 + n, sym)
+    f0 = 1.3e9
+    para = api.Parasitics(np.full(n, 50.0), [f"net_{i}" for i in range(n)])
+    para.saveNetworkParam("Z", [f0], z.ravel())
+    g_ref, c_ref = onet.ybus_from_param("Z", z, f0)
+    assert np.array_equal(para.matG, g_ref) and np.array_equal(para.matC, c_ref)     # same IEEE operations
+    path = tmp_path / "x.cir"
+    for thresh in (api.WRITE_THRESH, 0.05):
+        assert api.dumpXyce(path, para, "dsgn", thresh)
+        got = re.sub(r"^\* Date: .*$", "* Date: T", path.read_text(), flags=re.M)
+        want = onet.xyce_text(str(path), "dsgn", para.port_names, f0, g_ref, c_ref, thresh, "T")
+        assert got == want
+
+
+def test_xyce_writes_inductors_for_negative_capacitance(tmp_path):
+    from gds2para_gb300 import api
+    _lib_or_skip()
+    z = np.array([[1.0 + 80.0j, 0.5 - 200.0j], [0.5 - 200.0j, 2.0 - 90.0j]])
+    para = api.Parasitics([50.0, 50.0])
+    para.saveNetworkParam("Z", [1e9], z.ravel())
+    assert api.dumpXyce(tmp_path / "x.cir", para, "d")
+    text = (tmp_path / "x.cir").read_text()
+    assert re.search(r"^L1 port1 0 ", text, re.M) and text.rstrip().endswith(".ends")
+    want = onet.xyce_text(str(tmp_path / "x.cir"), "d", para.port_names, 1e9, para.matG, para.matC,
+                          api.WRITE_THRESH, "T")
+    assert re.sub(r"^\* Date: .*$", "* Date: T", text, flags=re.M) == want
+
+
+def _parse_spef(text):
+    sec, caps, ress, hdr = None, [], [], {}
+    node = lambda t: int(t[1:])
+    for line in text.splitlines():
+        if line.startswith("*CAP"):
+            sec = caps
+            continue
+        if line.startswith("*RES"):
+            sec = ress
+            continue
+        if line.startswith("*END"):
+            sec = None
+            continue
+        if line.startswith("*D_NET"):
+            hdr["lcap"] = float(line.split()[2])
+        if sec is not None and line.strip():
+            t = line.split()
+            a = node(t[1])
+            b, v = (node(t[2]), float(t[3])) if len(t) == 4 else (0, float(t[2]))
+            sec.append((a, b, v))
+    return caps, ress, hdr
+
+
+def test_spef_elements_match_oracle(tmp_path):
+    from gds2para_gb300 import api
+    _lib_or_skip()
+    z = _nodal_case(5, 77, sym=False)
+    para = api.Parasitics(np.full(5, 50.0), [f"p{i}" for i in range(5)], "IOBBI")
+    para.saveNetworkParam("Z", [2e9], z.ravel())
+    assert api.dumpSPEF(tmp_path / "x.spef", para, "dsgn")
+    text = (tmp_path / "x.spef").read_text()
+    assert text.startswith('*SPEF "IEEE 1481-1998"\n*DESIGN "dsgn"\n')
+    assert "*1 p0\n" in text and "*P p1 O\n" in text and "*P p0 I\n" in text
+    caps, ress, hdr = _parse_spef(text)
+    want_c, want_r, ct = onet.spef_elements(para.matG, para.matC, api.WRITE_THRESH)
+    assert [(a, b) for a, b, _ in caps] == [(a, b) for a, b, _ in want_c]
+    assert [(a, b) for a, b, _ in ress] == [(a, b) for a, b, _ in want_r]
+    np.testing.assert_allclose([v for *_, v in caps], [v for *_, v in want_c], rtol=1e-5)
+    np.testing.assert_allclose([v for *_, v in ress], [v for *_, v in want_r], rtol=1e-5)
+    assert abs(hdr["lcap"] - ct) <= 1e-5 * abs(ct)
+
+
+def test_nodal_writers_reject_s_parameters_and_bad_arguments(tmp_path):
+    from gds2para_gb300 import api
+    L = _lib_or_skip()
+    para = api.Parasitics([50.0])
+    para.saveNetworkParam("S", [1e9], np.array([0.2 + 0.1j]))
+    assert para.matG is None
+    with pytest.raises(ValueError):
+        api.dumpXyce(tmp_path / "x.cir", para, "d")
+    assert L.g2p_write_xyce(b"/dev/null", b"d", 1, None, 1e9, None, None, 1e-5) == 1
