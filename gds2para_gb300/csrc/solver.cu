@@ -1047,25 +1047,28 @@ __global__ void k_prolong_csr(int64_t n, int k, const int64_t *ptr, const int32_
     }
 }
 
+// One V-cycle on level l: x = M_l^-1 b.  Level 0 runs on the caller's
+// vectors (the Krylov basis vector in, the preconditioned vector out), the
+// coarser levels on their own work vectors.
 template <class T>
-static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaStream_t s) {
+static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaStream_t s, const T *b, T *x) {
     Level<T> &L = H.lv[l];
     if (l == (int)H.lv.size() - 1) {
-        if (H.cinv) (g2p::kbegin("k_dense_apply", s), k_dense_apply<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, H.cinv, L.b, L.x), g2p::kend(s));
+        if (H.cinv) (g2p::kbegin("k_dense_apply", s), k_dense_apply<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, H.cinv, b, x), g2p::kend(s));
         else {
-            chebyshev<T>(L, 4, cfg.cheb_ratio, L.b, L.x, true, k, s);
-            for (int q = 0; q < 4; q++) chebyshev<T>(L, 4, cfg.cheb_ratio, L.b, L.x, false, k, s);
+            chebyshev<T>(L, 4, cfg.cheb_ratio, b, x, true, k, s);
+            for (int q = 0; q < 4; q++) chebyshev<T>(L, 4, cfg.cheb_ratio, b, x, false, k, s);
         }
         return;
     }
-    chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, L.b, L.x, true, k, s);
-    spmm_b<T>(L.A, L.lr, L.x, L.t0, k, L.b, s);
+    chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, b, x, true, k, s);
+    spmm_b<T>(L.A, L.lr, x, L.t0, k, b, s);
     Level<T> &C = H.lv[l + 1];
     (g2p::kbegin("k_restrict", s), k_restrict<T><<<row_grid(C.n, k), row_block(k), 0, s>>>(C.n, k, L.rptr, L.rmem, L.t0, C.b), g2p::kend(s));
-    vcycle<T>(H, cfg, l + 1, k, s);
-    if (L.P.sptr) prolong_sell<T>(L.P, C.x, L.x, k, s);
-    else (g2p::kbegin("k_prolong_csr", s), k_prolong_csr<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, L.P.ptr, L.P.col, L.P.val, C.x, L.x), g2p::kend(s));
-    chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, L.b, L.x, false, k, s);
+    vcycle<T>(H, cfg, l + 1, k, s, C.b, C.x);
+    if (L.P.sptr) prolong_sell<T>(L.P, C.x, x, k, s);
+    else (g2p::kbegin("k_prolong_csr", s), k_prolong_csr<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, L.P.ptr, L.P.col, L.P.val, C.x, x), g2p::kend(s));
+    chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, b, x, false, k, s);
 }
 
 // ------------------------------------------------------------- AMG setup
@@ -1857,9 +1860,11 @@ g2p_status amg_to_float(const Hierarchy<double> &H, cudaStream_t s, Hierarchy<fl
 template <class T>
 g2p_status hierarchy_reserve(Hierarchy<T> &H, int k, cudaStream_t s) {
     if (k <= H.kcap) return G2P_OK;
-    for (auto &L : H.lv) {
+    for (size_t l = 0; l < H.lv.size(); l++) {
+        Level<T> &L = H.lv[l];
         dfree(L.x, s); dfree(L.b, s); dfree(L.t0, s); dfree(L.t1, s); dfree(L.d, s);
-        G2P_TRY(dalloc(&L.x, L.n * k, s)); G2P_TRY(dalloc(&L.b, L.n * k, s));
+        // level 0 works on the Krylov vectors directly and needs no x, b
+        if (l > 0) { G2P_TRY(dalloc(&L.x, L.n * k, s)); G2P_TRY(dalloc(&L.b, L.n * k, s)); }
         G2P_TRY(dalloc(&L.t0, L.n * k, s)); G2P_TRY(dalloc(&L.d, L.n * k, s));
     }
     H.kcap = k;
@@ -2042,10 +2047,8 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
         int j = 0;
         for (; j < m && it < cfg.maxit; j++) {
             T *Vj = K.V + (int64_t)j * nk, *Zj = K.Z + (int64_t)j * nk;
-            // Z_j = M^-1 V_j (one V-cycle)
-            G2P_CUDA(cudaMemcpyAsync(L0.b, Vj, sizeof(T) * nk, cudaMemcpyDeviceToDevice, s));
-            vcycle<T>(H, cfg, 0, k, s);
-            G2P_CUDA(cudaMemcpyAsync(Zj, L0.x, sizeof(T) * nk, cudaMemcpyDeviceToDevice, s));
+            // Z_j = M^-1 V_j (one V-cycle, in place on the basis vectors)
+            vcycle<T>(H, cfg, 0, k, s, Vj, Zj);
             spmm<T>(A, L0.lr, Zj, K.w, k, s);
             // classical Gram-Schmidt, optionally twice
             mdot<T>(K.V, n, j + 1, K.w, k, K.partial, K.hcol, s);
