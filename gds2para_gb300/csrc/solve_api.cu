@@ -263,6 +263,9 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
         }
     }
     G2P_CUDA(cudaStreamSynchronize(s));
+    if (getenv("G2P_DEBUG"))
+        fprintf(stderr, "[g2p] n=%lld k=%d solve %.3f ms, %d iterations, %d refinements\n", (long long)n, k,
+                ms_since(t0), iters, refinements);
     if (st) {
         st->iterations = iters;
         st->refinements = refinements;

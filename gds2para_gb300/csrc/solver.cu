@@ -864,6 +864,237 @@ g2p_status sell_build(Csr<T> &A, cudaStream_t s, int64_t maxlen) {
 template g2p_status sell_build<double>(Csr<double> &, cudaStream_t, int64_t);
 template g2p_status sell_build<float>(Csr<float> &, cudaStream_t, int64_t);
 
+// ------------------------------------------- 16-byte chunks of k-interleaved blocks
+// A block of k right-hand sides is stored row-major (entry (i, r) at i*k + r).
+// When k is a power-of-two multiple of the chunk width C = 16 / sizeof(T) and
+// at most kVecMaxK, the kernels below move 16 bytes per thread and access
+// instead of one element: cpr = k / C chunks per row, and a thread's chunk
+// column stays fixed across its grid-stride loop (the stride is a multiple
+// of cpr).  Other widths use the per-element kernels.
+constexpr int kVecMaxK = 64;
+template <class T> struct Chunk;
+template <> struct Chunk<float> {
+    static constexpr int C = 4;
+    float v[4];
+    __device__ __forceinline__ void ld(const float *p) {
+        const float4 t = __ldg(reinterpret_cast<const float4 *>(p)); v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    }
+    __device__ __forceinline__ void ldc(const float *p) {
+        const float4 t = *reinterpret_cast<const float4 *>(p); v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    }
+    __device__ __forceinline__ void st(float *p) const { *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]); }
+};
+template <> struct Chunk<double> {
+    static constexpr int C = 2;
+    double v[2];
+    __device__ __forceinline__ void ld(const double *p) {
+        const double2 t = __ldg(reinterpret_cast<const double2 *>(p)); v[0] = t.x; v[1] = t.y;
+    }
+    __device__ __forceinline__ void ldc(const double *p) {
+        const double2 t = *reinterpret_cast<const double2 *>(p); v[0] = t.x; v[1] = t.y;
+    }
+    __device__ __forceinline__ void st(double *p) const { *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]); }
+};
+
+template <class T>
+static inline int chunk_cpr(int k) {
+    constexpr int C = Chunk<T>::C;
+    if (k % C != 0 || k > kVecMaxK) return 0;
+    const int cpr = k / C;
+    return (cpr & (cpr - 1)) == 0 ? cpr : 0;
+}
+static inline unsigned chunk_grid(int64_t nq) {
+    int64_t b = (nq + 255) / 256;
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 152LL * 16));
+}
+#define G2P_FOR_CHUNKS(q, nq) \
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < (nq); q += (int64_t)gridDim.x * blockDim.x)
+
+// dst = src / h[col] (0 where h = 0): the Krylov start and Arnoldi normalisation
+template <class T>
+__global__ void __launch_bounds__(256) k_scale_cols_v(int64_t nq, int cpr, const double *h, const T *src, T *dst) {
+    constexpr int C = Chunk<T>::C;
+    const int cc = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & (cpr - 1));
+    T inv[C];
+#pragma unroll
+    for (int u = 0; u < C; u++) {
+        const double b = h[cc * C + u];
+        inv[u] = b > 0 ? (T)(1.0 / b) : (T)0;
+    }
+    G2P_FOR_CHUNKS(q, nq) {
+        Chunk<T> a;
+        a.ld(src + q * C);
+#pragma unroll
+        for (int u = 0; u < C; u++) a.v[u] *= inv[u];
+        a.st(dst + q * C);
+    }
+}
+
+// w -= sum_j h[j*k + col] V_j, h staged in shared memory
+template <class T>
+__global__ void __launch_bounds__(256) k_maxpy_v(int64_t nq, int cpr, int k, int J, const T *V, const double *h, T *w) {
+    constexpr int C = Chunk<T>::C;
+    extern __shared__ unsigned char smraw[];
+    T *hs = reinterpret_cast<T *>(smraw);
+    for (int t = threadIdx.x; t < J * k; t += blockDim.x) hs[t] = (T)h[t];
+    __syncthreads();
+    const int cc = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & (cpr - 1));
+    const int64_t nk = nq * C;
+    G2P_FOR_CHUNKS(q, nq) {
+        Chunk<T> acc;
+        acc.ldc(w + q * C);
+        for (int j = 0; j < J; j++) {
+            Chunk<T> v;
+            v.ld(V + (int64_t)j * nk + q * C);
+            const T *hj = hs + j * k + cc * C;
+#pragma unroll
+            for (int u = 0; u < C; u++) acc.v[u] -= hj[u] * v.v[u];
+        }
+        acc.st(w + q * C);
+    }
+}
+
+// Chebyshev: d = theta^-1 D^-1 b, x = d (or x += d)
+template <class T>
+__global__ void __launch_bounds__(256) k_cheb_first_v(int64_t nq, int shift, const T *dinv, const T *b, T *x, T *d,
+                                                      double inv_theta, bool add) {
+    constexpr int C = Chunk<T>::C;
+    G2P_FOR_CHUNKS(q, nq) {
+        const T di = (T)inv_theta * dinv[q >> shift];
+        Chunk<T> bb, dd;
+        bb.ld(b + q * C);
+#pragma unroll
+        for (int u = 0; u < C; u++) dd.v[u] = di * bb.v[u];
+        dd.st(d + q * C);
+        if (add) {
+            Chunk<T> xx;
+            xx.ldc(x + q * C);
+#pragma unroll
+            for (int u = 0; u < C; u++) xx.v[u] += dd.v[u];
+            xx.st(x + q * C);
+        } else {
+            dd.st(x + q * C);
+        }
+    }
+}
+
+// Chebyshev: d = c1 d + c2 D^-1 res ; x += d
+template <class T>
+__global__ void __launch_bounds__(256) k_cheb_step_v(int64_t nq, int shift, const T *dinv, const T *res, T *x, T *d,
+                                                     double c1, double c2) {
+    constexpr int C = Chunk<T>::C;
+    const T a = (T)c1, bcoef = (T)c2;
+    G2P_FOR_CHUNKS(q, nq) {
+        const T di = bcoef * dinv[q >> shift];
+        Chunk<T> rr, dd, xx;
+        rr.ld(res + q * C);
+        dd.ldc(d + q * C);
+        xx.ldc(x + q * C);
+#pragma unroll
+        for (int u = 0; u < C; u++) {
+            const T t = a * dd.v[u] + di * rr.v[u];
+            dd.v[u] = t;
+            xx.v[u] += t;
+        }
+        dd.st(d + q * C);
+        xx.st(x + q * C);
+    }
+}
+
+// b_c[I] = sum over the members of I of res (members ascending)
+template <class T>
+__global__ void __launch_bounds__(256) k_restrict_v(int64_t nc, int shift, int k, const int64_t *rptr,
+                                                    const int32_t *rmem, const T *res, T *bc) {
+    constexpr int C = Chunk<T>::C;
+    const int64_t nq = nc << shift;
+    G2P_FOR_CHUNKS(q, nq) {
+        const int64_t I = q >> shift;
+        const int off = (int)(q & ((1 << shift) - 1)) * C;
+        Chunk<T> acc;
+#pragma unroll
+        for (int u = 0; u < C; u++) acc.v[u] = 0;
+        for (int64_t m = rptr[I]; m < rptr[I + 1]; m++) {
+            Chunk<T> v;
+            v.ld(res + (int64_t)rmem[m] * k + off);
+#pragma unroll
+            for (int u = 0; u < C; u++) acc.v[u] += v.v[u];
+        }
+        acc.st(bc + q * C);
+    }
+}
+
+// Per-column sums over the rows of a (cpr, 256 / cpr) block, cpr <= 16: G
+// groups of C columns per thread.  Lanes of a warp that share a chunk column
+// combine by xor shuffles, then the eight warps' sums are added in order.
+// Result (g, column c) -> partial[(g * k + c) * gridDim.x + blockIdx.x].
+template <int GC, class T>
+__device__ __forceinline__ void chunk_col_reduce(const T (&v)[GC], double *sm, int cpr, int k, int C, int gvalid,
+                                                 int64_t gbase, double *partial) {
+    const int tid = threadIdx.y * cpr + threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int e = 0; e < GC; e++) {
+        double x = (double)v[e];
+        for (int o = cpr; o < 32; o <<= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane < cpr) sm[(warp * GC + e) * cpr + lane] = x;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < GC * cpr; idx += 256) {
+        const int e = idx / cpr, cc = idx % cpr;
+        const int g = e / C, u = e % C;
+        if (g < gvalid) {
+            double acc = 0;
+            for (int w = 0; w < 8; w++) acc += sm[(w * GC + e) * cpr + cc];
+            partial[((gbase + g) * k + cc * C + u) * gridDim.x + blockIdx.x] = acc;
+        }
+    }
+    __syncthreads();
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_colsq_partial_v(const T *x, int64_t n, int k, double *partial) {
+    constexpr int C = Chunk<T>::C;
+    __shared__ double sm[8 * C * 16];
+    const int cpr = blockDim.x, cc = threadIdx.x, ny = blockDim.y;
+    T acc[C];
+#pragma unroll
+    for (int u = 0; u < C; u++) acc[u] = 0;
+    for (int64_t i = blockIdx.x * (int64_t)ny + threadIdx.y; i < n; i += (int64_t)gridDim.x * ny) {
+        Chunk<T> a;
+        a.ld(x + i * k + cc * C);
+#pragma unroll
+        for (int u = 0; u < C; u++) acc[u] += a.v[u] * a.v[u];
+    }
+    chunk_col_reduce<C>(acc, sm, cpr, k, C, 1, 0, partial);
+}
+
+constexpr int kDotGroupV = 8;
+template <class T>
+__global__ void __launch_bounds__(256) k_mdot_partial_v(const T *V, int64_t n, int J, const T *w, int k, double *partial) {
+    constexpr int C = Chunk<T>::C, GC = kDotGroupV * C;
+    __shared__ double sm[8 * GC * 16];
+    const int cpr = blockDim.x, cc = threadIdx.x, ny = blockDim.y;
+    const int64_t nk = n * k;
+    for (int j0 = 0; j0 < J; j0 += kDotGroupV) {
+        T acc[GC];          // acc[g * C + u]
+#pragma unroll
+        for (int e = 0; e < GC; e++) acc[e] = 0;
+        for (int64_t i = blockIdx.x * (int64_t)ny + threadIdx.y; i < n; i += (int64_t)gridDim.x * ny) {
+            const int64_t t = i * k + cc * C;
+            Chunk<T> ww;
+            ww.ld(w + t);
+#pragma unroll
+            for (int g = 0; g < kDotGroupV; g++)
+                if (j0 + g < J) {
+                    Chunk<T> vv;
+                    vv.ld(V + (int64_t)(j0 + g) * nk + t);
+#pragma unroll
+                    for (int u = 0; u < C; u++) acc[g * C + u] += vv.v[u] * ww.v[u];
+                }
+        }
+        chunk_col_reduce<GC>(acc, sm, cpr, k, C, J - j0 < kDotGroupV ? J - j0 : kDotGroupV, j0, partial);
+    }
+}
+
 // --------------------------------------------------------------- reductions
 // Deterministic per-column sums of squares: block partials, then an ordered
 // final pass.
@@ -873,6 +1104,42 @@ constexpr int64_t kMaxDenseCoarse = 768;
 // Block shape (kx, 256 / kx) with kx the power of two >= k: threadIdx.x is
 // the right-hand side, threadIdx.y strides over rows, so every thread keeps
 // one column's partial sum and the block reduces in a fixed order.
+
+// Sums G per-thread values over the threads of a (kx, 256 / kx) block that
+// share column r, in a fixed order: xor shuffles inside each warp, then the
+// warps' (or, for kx >= 32, the rows') sums one after another.  sm holds
+// G * 256 doubles; the result for (g, r) lands in sm[g * 256 + r].
+template <int G>
+__device__ __forceinline__ void block_col_reduce(double (&v)[G], double *sm) {
+    const int kx = blockDim.x, r = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * kx + r, lane = tid & 31, warp = tid >> 5;
+    if (kx < 32) {
+        for (int o = kx; o < 32; o <<= 1)
+#pragma unroll
+            for (int g = 0; g < G; g++) v[g] += __shfl_xor_sync(0xffffffffu, v[g], o);
+    }
+    const int slots = kx < 32 ? 8 : (int)blockDim.y;      // warps, or rows of the block
+    const bool rep = kx < 32 ? lane < kx : true;
+    const int slot = kx < 32 ? warp : ty;
+    if (rep)
+#pragma unroll
+        for (int g = 0; g < G; g++) sm[(g * slots + slot) * kx + r] = v[g];
+    __syncthreads();
+    double out[G];
+    if (tid < kx) {
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            double acc = 0;
+            for (int q = 0; q < slots; q++) acc += sm[(g * slots + q) * kx + r];
+            out[g] = acc;
+        }
+    }
+    __syncthreads();
+    if (tid < kx)
+#pragma unroll
+        for (int g = 0; g < G; g++) sm[g * 256 + r] = out[g];
+    __syncthreads();
+}
 
 template <class T>
 __global__ void __launch_bounds__(256) k_colsq_partial(const T *x, int64_t n, int k, double *partial) {
@@ -884,29 +1151,39 @@ __global__ void __launch_bounds__(256) k_colsq_partial(const T *x, int64_t n, in
             T v = x[i * k + r];
             acc += v * v;
         }
-    sm[ty * blockDim.x + r] = (double)acc;
-    __syncthreads();
-    if (ty == 0 && r < k) {
-        double s = 0;
-        for (int q = 0; q < ny; q++) s += sm[q * blockDim.x + r];
-        partial[(int64_t)r * gridDim.x + blockIdx.x] = s;
-    }
+    double v[1] = {(double)acc};
+    block_col_reduce<1>(v, sm);
+    if (ty == 0 && r < k) partial[(int64_t)r * gridDim.x + blockIdx.x] = sm[r];
 }
 
-__global__ void k_reduce_partials(const double *partial, int nb, int cnt, double *out, bool take_sqrt) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
+// One warp per output: lane l adds partials l, l + 32, ... in order, then a
+// fixed xor tree combines the lanes (an FP64 add chain over all nb partials
+// in one thread costs tens of microseconds on this part).
+constexpr int kReduceWarps = 8;
+__global__ void __launch_bounds__(32 * kReduceWarps) k_reduce_partials(const double *partial, int nb, int cnt,
+                                                                       double *out, bool take_sqrt) {
+    const int c = blockIdx.x * kReduceWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (c >= cnt) return;
+    const double *p = partial + (int64_t)c * nb;
     double s = 0;
-    for (int b = 0; b < nb; b++) s += partial[(int64_t)c * nb + b];
-    out[c] = take_sqrt ? sqrt(s) : s;
+    for (int b = lane; b < nb; b += 32) s += p[b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[c] = take_sqrt ? sqrt(s) : s;
 }
+static inline unsigned reduce_grid(int cnt) { return (unsigned)((cnt + kReduceWarps - 1) / kReduceWarps); }
 
 template <class T>
 void colnorms(const T *x, int64_t n, int k, double *partial, double *out, cudaStream_t s) {
-    int kx = pow2_ge(k);
-    dim3 blk(kx, 256 / kx);
-    (g2p::kbegin("k_colsq_partial", s), k_colsq_partial<T><<<kRedBlocks, blk, 0, s>>>(x, n, k, partial), g2p::kend(s));
-    (g2p::kbegin("k_reduce_partials", s), k_reduce_partials<<<(k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, k, out, true), g2p::kend(s));
+    const int cpr = chunk_cpr<T>(k);
+    if (cpr && cpr <= 16) {
+        (g2p::kbegin("k_colsq_partial", s), k_colsq_partial_v<T><<<kRedBlocks, dim3(cpr, 256 / cpr), 0, s>>>(x, n, k, partial), g2p::kend(s));
+    } else {
+        int kx = pow2_ge(k);
+        dim3 blk(kx, 256 / kx);
+        (g2p::kbegin("k_colsq_partial", s), k_colsq_partial<T><<<kRedBlocks, blk, 0, s>>>(x, n, k, partial), g2p::kend(s));
+    }
+    (g2p::kbegin("k_reduce_partials", s), k_reduce_partials<<<reduce_grid(k), 32 * kReduceWarps, 0, s>>>(partial, kRedBlocks, k, out, true), g2p::kend(s));
 }
 template void colnorms<double>(const double *, int64_t, int, double *, double *, cudaStream_t);
 template void colnorms<float>(const float *, int64_t, int, double *, double *, cudaStream_t);
@@ -931,16 +1208,13 @@ __global__ void __launch_bounds__(256) k_mdot_partial(const T *V, int64_t n, int
                 for (int g = 0; g < kDotGroup; g++)
                     if (j0 + g < J) acc[g] += V[(int64_t)(j0 + g) * nk + t] * wv;
             }
+        double v[kDotGroup];
 #pragma unroll
-        for (int g = 0; g < kDotGroup; g++) sm[g][ty * blockDim.x + r] = (double)acc[g];
-        __syncthreads();
+        for (int g = 0; g < kDotGroup; g++) v[g] = (double)acc[g];
+        block_col_reduce<kDotGroup>(v, &sm[0][0]);
         for (int idx = ty * blockDim.x + r; idx < kDotGroup * (int)blockDim.x; idx += blockDim.x * blockDim.y) {
             int g = idx / blockDim.x, rr = idx % blockDim.x;
-            if (rr < k && j0 + g < J) {
-                double sacc = 0;
-                for (int t2 = 0; t2 < ny; t2++) sacc += sm[g][t2 * blockDim.x + rr];
-                partial[((int64_t)(j0 + g) * k + rr) * gridDim.x + blockIdx.x] = sacc;
-            }
+            if (rr < k && j0 + g < J) partial[((int64_t)(j0 + g) * k + rr) * gridDim.x + blockIdx.x] = sm[g][rr];
         }
         __syncthreads();
     }
@@ -997,16 +1271,24 @@ static void chebyshev(Level<T> &L, int deg, double ratio, const T *b, T *x, bool
     double sigma = theta / delta, rho = 1.0 / sigma;
     unsigned g = row_grid(L.n, k);
     dim3 blk = row_block(k);
+    const int cpr = chunk_cpr<T>(k);
+    const int64_t nq = L.n * cpr;
+    const int shift = cpr ? __builtin_ctz(cpr) : 0;
+    auto first = [&](const T *src, bool add) {
+        if (cpr) (g2p::kbegin("k_cheb_first", s), k_cheb_first_v<T><<<chunk_grid(nq), 256, 0, s>>>(nq, shift, L.dinv, src, x, L.d, 1.0 / theta, add), g2p::kend(s));
+        else (g2p::kbegin("k_cheb_first", s), k_cheb_first<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, src, x, L.d, 1.0 / theta, add), g2p::kend(s));
+    };
     if (zero_guess) {
-        (g2p::kbegin("k_cheb_first", s), k_cheb_first<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, b, x, L.d, 1.0 / theta, false), g2p::kend(s));
+        first(b, false);
     } else {
         spmm_b<T>(L.A, L.lr, x, L.t0, k, b, s);
-        (g2p::kbegin("k_cheb_first", s), k_cheb_first<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, L.t0, x, L.d, 1.0 / theta, true), g2p::kend(s));
+        first(L.t0, true);
     }
     for (int it = 1; it < deg; it++) {
         spmm_b<T>(L.A, L.lr, x, L.t0, k, b, s);
         double rn = 1.0 / (2.0 * sigma - rho);
-        (g2p::kbegin("k_cheb_step", s), k_cheb_step<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, L.t0, x, L.d, rn * rho, 2.0 * rn / delta), g2p::kend(s));
+        if (cpr) (g2p::kbegin("k_cheb_step", s), k_cheb_step_v<T><<<chunk_grid(nq), 256, 0, s>>>(nq, shift, L.dinv, L.t0, x, L.d, rn * rho, 2.0 * rn / delta), g2p::kend(s));
+        else (g2p::kbegin("k_cheb_step", s), k_cheb_step<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, L.t0, x, L.d, rn * rho, 2.0 * rn / delta), g2p::kend(s));
         rho = rn;
     }
 }
@@ -1024,15 +1306,21 @@ __global__ void k_restrict(int64_t nc, int k, const int64_t *rptr, const int32_t
 }
 
 
+// x = A_c^-1 b on the coarsest level: one warp per (row, right-hand side);
+// lane l takes columns l, l + 32, ... and a fixed xor tree combines them.
 template <class T>
-__global__ void k_dense_apply(int64_t n, int k, const double *Ainv, const T *b, T *x) {
-    const int r = threadIdx.x;
-    if (r >= k) return;
-    G2P_FOR_ROWS(i, n) {
-        double acc = 0;
-        for (int64_t j = 0; j < n; j++) acc += Ainv[i * n + j] * (double)b[j * k + r];
-        x[i * k + r] = (T)acc;
-    }
+__global__ void __launch_bounds__(256) k_dense_apply(int64_t n, int k, const double *Ainv, const T *b, T *x) {
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (wid >= n * k) return;
+    const int64_t i = wid / k;
+    const int r = (int)(wid % k);
+    const double *a = Ainv + i * n;
+    double acc = 0;
+    for (int64_t j = lane; j < n; j += 32) acc += a[j] * (double)b[j * k + r];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) x[i * k + r] = (T)acc;
 }
 
 template <class T>
@@ -1054,7 +1342,7 @@ template <class T>
 static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaStream_t s, const T *b, T *x) {
     Level<T> &L = H.lv[l];
     if (l == (int)H.lv.size() - 1) {
-        if (H.cinv) (g2p::kbegin("k_dense_apply", s), k_dense_apply<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, H.cinv, b, x), g2p::kend(s));
+        if (H.cinv) (g2p::kbegin("k_dense_apply", s), k_dense_apply<T><<<(unsigned)((L.n * k * 32 + 255) / 256), 256, 0, s>>>(L.n, k, H.cinv, b, x), g2p::kend(s));
         else {
             chebyshev<T>(L, 4, cfg.cheb_ratio, b, x, true, k, s);
             for (int q = 0; q < 4; q++) chebyshev<T>(L, 4, cfg.cheb_ratio, b, x, false, k, s);
@@ -1064,7 +1352,10 @@ static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaS
     chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, b, x, true, k, s);
     spmm_b<T>(L.A, L.lr, x, L.t0, k, b, s);
     Level<T> &C = H.lv[l + 1];
-    (g2p::kbegin("k_restrict", s), k_restrict<T><<<row_grid(C.n, k), row_block(k), 0, s>>>(C.n, k, L.rptr, L.rmem, L.t0, C.b), g2p::kend(s));
+    if (const int cpr = chunk_cpr<T>(k))
+        (g2p::kbegin("k_restrict", s), k_restrict_v<T><<<chunk_grid(C.n * cpr), 256, 0, s>>>(C.n, __builtin_ctz(cpr), k, L.rptr, L.rmem, L.t0, C.b), g2p::kend(s));
+    else
+        (g2p::kbegin("k_restrict", s), k_restrict<T><<<row_grid(C.n, k), row_block(k), 0, s>>>(C.n, k, L.rptr, L.rmem, L.t0, C.b), g2p::kend(s));
     vcycle<T>(H, cfg, l + 1, k, s, C.b, C.x);
     if (L.P.sptr) prolong_sell<T>(L.P, C.x, x, k, s);
     else (g2p::kbegin("k_prolong_csr", s), k_prolong_csr<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, L.P.ptr, L.P.col, L.P.val, C.x, x), g2p::kend(s));
@@ -1999,10 +2290,15 @@ __global__ void k_xupdate(int64_t n, int k, int m, int j, const T *Z, const doub
 
 template <class T>
 static void mdot(const T *V, int64_t n, int J, const T *w, int k, double *partial, double *out, cudaStream_t s) {
-    int kx = pow2_ge(k);
-    dim3 blk(kx, 256 / kx);
-    (g2p::kbegin("k_mdot_partial", s), k_mdot_partial<T><<<kRedBlocks, blk, 0, s>>>(V, n, J, w, k, partial), g2p::kend(s));
-    (g2p::kbegin("k_reduce_partials", s), k_reduce_partials<<<(J * k + 63) / 64, 64, 0, s>>>(partial, kRedBlocks, J * k, out, false), g2p::kend(s));
+    const int cpr = chunk_cpr<T>(k);
+    if (cpr && cpr <= 16) {
+        (g2p::kbegin("k_mdot_partial", s), k_mdot_partial_v<T><<<kRedBlocks, dim3(cpr, 256 / cpr), 0, s>>>(V, n, J, w, k, partial), g2p::kend(s));
+    } else {
+        int kx = pow2_ge(k);
+        dim3 blk(kx, 256 / kx);
+        (g2p::kbegin("k_mdot_partial", s), k_mdot_partial<T><<<kRedBlocks, blk, 0, s>>>(V, n, J, w, k, partial), g2p::kend(s));
+    }
+    (g2p::kbegin("k_reduce_partials", s), k_reduce_partials<<<reduce_grid(J * k), 32 * kReduceWarps, 0, s>>>(partial, kRedBlocks, J * k, out, false), g2p::kend(s));
 }
 
 __global__ void k_add_vec(double *a, const double *b, int n) {
@@ -2021,6 +2317,14 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
     Level<T> &L0 = H.lv[0];
     const unsigned rg = row_grid(n, k);
     const dim3 rb = row_block(k);
+    const int cpr = chunk_cpr<T>(k);
+    const int64_t nq = n * cpr;
+    auto maxpy = [&](const double *h, int J) {
+        if (cpr)
+            (g2p::kbegin("k_maxpy", s), k_maxpy_v<T><<<chunk_grid(nq), 256, sizeof(T) * J * k, s>>>(nq, cpr, k, J, K.V, h, K.w), g2p::kend(s));
+        else
+            (g2p::kbegin("k_maxpy", s), k_maxpy<T><<<rg, rb, 0, s>>>(K.V, n, J, h, k, K.w), g2p::kend(s));
+    };
     if (bnorm_override) G2P_CUDA(cudaMemcpyAsync(K.bnorm, bnorm_override, sizeof(double) * k, cudaMemcpyDeviceToDevice, s));
     else colnorms<T>(b, n, k, K.partial, K.bnorm, s);
     int it = 0;
@@ -2042,7 +2346,8 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
         rep.rel_residual = worst;
         if (worst <= cfg.rtol) { rep.converged = true; break; }
         if (it >= cfg.maxit) break;
-        (g2p::kbegin("k_start", s), k_start<T><<<rg, rb, 0, s>>>(n, k, K.r, K.beta, K.V), g2p::kend(s));
+        if (cpr) (g2p::kbegin("k_start", s), k_scale_cols_v<T><<<chunk_grid(nq), 256, 0, s>>>(nq, cpr, K.beta, K.r, K.V), g2p::kend(s));
+        else (g2p::kbegin("k_start", s), k_start<T><<<rg, rb, 0, s>>>(n, k, K.r, K.beta, K.V), g2p::kend(s));
         (g2p::kbegin("k_g_init", s), k_g_init<<<(k + 63) / 64, 64, 0, s>>>(k, m, K.beta, K.g), g2p::kend(s));
         int j = 0;
         for (; j < m && it < cfg.maxit; j++) {
@@ -2052,15 +2357,16 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
             spmm<T>(A, L0.lr, Zj, K.w, k, s);
             // classical Gram-Schmidt, optionally twice
             mdot<T>(K.V, n, j + 1, K.w, k, K.partial, K.hcol, s);
-            (g2p::kbegin("k_maxpy", s), k_maxpy<T><<<rg, rb, 0, s>>>(K.V, n, j + 1, K.hcol, k, K.w), g2p::kend(s));
+            maxpy(K.hcol, j + 1);
             if (cfg.reorth) {
                 mdot<T>(K.V, n, j + 1, K.w, k, K.partial, dots2, s);
-                (g2p::kbegin("k_maxpy", s), k_maxpy<T><<<rg, rb, 0, s>>>(K.V, n, j + 1, dots2, k, K.w), g2p::kend(s));
+                maxpy(dots2, j + 1);
                 (g2p::kbegin("k_add_vec", s), k_add_vec<<<((j + 1) * k + 255) / 256, 256, 0, s>>>(K.hcol, dots2, (j + 1) * k), g2p::kend(s));
             }
             double *hnorm = K.beta;   // reuse
             colnorms<T>(K.w, n, k, K.partial, hnorm, s);
-            (g2p::kbegin("k_arnoldi_finish", s), k_arnoldi_finish<T><<<rg, rb, 0, s>>>(n, k, hnorm, K.w, K.V + (int64_t)(j + 1) * nk), g2p::kend(s));
+            if (cpr) (g2p::kbegin("k_arnoldi_finish", s), k_scale_cols_v<T><<<chunk_grid(nq), 256, 0, s>>>(nq, cpr, hnorm, K.w, K.V + (int64_t)(j + 1) * nk), g2p::kend(s));
+            else (g2p::kbegin("k_arnoldi_finish", s), k_arnoldi_finish<T><<<rg, rb, 0, s>>>(n, k, hnorm, K.w, K.V + (int64_t)(j + 1) * nk), g2p::kend(s));
             double *est = K.y;        // scratch for the estimates (k values)
             (g2p::kbegin("k_givens", s), k_givens<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.hcol, hnorm, K.H, K.cs, K.sn, K.g, K.bnorm, est), g2p::kend(s));
             G2P_CUDA(cudaMemcpyAsync(K.h_est, est, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
