@@ -28,7 +28,7 @@ EXPORTS = [
 STATUS = {0: "G2P_OK", 1: "G2P_ERR_INVALID", 2: "G2P_ERR_CUDA", 3: "G2P_ERR_NOMEM", 4: "G2P_ERR_NOT_CONVERGED",
           5: "G2P_ERR_UNSUPPORTED", 6: "G2P_ERR_STATE", 7: "G2P_ERR_ADMISSION"}
 G2P_OK, G2P_ERR_NOT_CONVERGED = 0, 4
-G2P_PREC_FP64, G2P_PREC_MIXED = 0, 1
+G2P_PREC_FP64, G2P_PREC_MIXED, G2P_PREC_FP64_PC32 = 0, 1, 2
 
 
 class MeshDescC(C.Structure):

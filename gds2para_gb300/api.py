@@ -32,7 +32,7 @@ def default_params(parity: bool = False, **kw) -> SolverParams:
     _lib.load().g2p_default_params(C.byref(p), 1 if parity else 0)
     for k, v in kw.items():
         if k == "precision" and isinstance(v, str):
-            v = {"fp64": _lib.G2P_PREC_FP64, "mixed": _lib.G2P_PREC_MIXED}[v]
+            v = {"fp64": _lib.G2P_PREC_FP64, "mixed": _lib.G2P_PREC_MIXED, "fp64_pc32": _lib.G2P_PREC_FP64_PC32}[v]
         setattr(p, k, v)
     return p
 

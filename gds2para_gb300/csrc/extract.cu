@@ -288,15 +288,15 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     t0 = std::chrono::steady_clock::now();
     g2p_solver *Sd = nullptr, *Sc = nullptr;
     // Ac first: its setup overlaps Ad's ordered sums on the side stream.
-    // Ac, the conductor Laplacian, stays FP64: a floating wire grounded at one
-    // node gives it a condition number near (length/h)^2, beyond what an FP32
-    // refinement sweep resolves; it is an order of magnitude smaller than Ad.
+    // Ac, the conductor Laplacian, keeps its Krylov iteration in FP64: a
+    // floating wire grounded at one node gives it a condition number near
+    // (length/h)^2, beyond what an FP32 refinement sweep resolves.  In the
+    // mixed method its V-cycle preconditioner runs in FP32.
+    // G2P_AC_PRECISION overrides the mode (comparisons).
     g2p_solver_params pc = p;
-    // Ac in FP64 unless G2P_AC_MIXED=1 (for comparisons): its condition
-    // number leaves FP32 inner solves little to gain
     {
-        const char *e = getenv("G2P_AC_MIXED");
-        if (!(e && atoi(e) != 0)) pc.precision = G2P_PREC_FP64;
+        if (p.precision == G2P_PREC_MIXED) pc.precision = G2P_PREC_FP64_PC32;
+        if (const char *e = getenv("G2P_AC_PRECISION")) pc.precision = atoi(e);
         // Ac's aggregation wants a stronger threshold than Ad's: twice Ad's,
         // at most 0.1 (c2 sweep: 0.04 -> 37 iterations, 0.08 -> 33, >= 0.15
         // stalls).  G2P_AC_STRENGTH / G2P_AC_DEGREE override (comparisons).

@@ -149,7 +149,12 @@ g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cu
     cudaMemcpyAsync(S->A.col, A.col, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(S->A.val, A.val, sizeof(double) * A.nnz, cudaMemcpyDeviceToDevice, s);
     if ((st = find_long_rows<double>(S->A, S->lr, s)) != G2P_OK) return fail(st);
-    if (S->precision == G2P_PREC_MIXED) {
+    if (S->precision != G2P_PREC_FP64 && S->precision != G2P_PREC_MIXED && S->precision != G2P_PREC_FP64_PC32) {
+        set_last_message("unknown precision mode %d", S->precision);
+        return fail(G2P_ERR_INVALID);
+    }
+    const bool f32_hier = S->precision != G2P_PREC_FP64;
+    if (f32_hier) {
         unsigned long long *mx;
         if ((st = dalloc(&mx, 1, s)) != G2P_OK) return fail(st);
         cudaMemsetAsync(mx, 0, sizeof(unsigned long long), s);
@@ -181,7 +186,7 @@ g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cu
     // sliced-ELL copies of every operator the solves multiply by
     if ((st = sell_build<double>(S->A, s)) != G2P_OK) return fail(st);
     // and of the prolongations (rows of at most kLongRow + 1 entries)
-    if (S->precision == G2P_PREC_MIXED) {
+    if (f32_hier) {
         for (auto &L : S->H32.lv) {
             if ((st = sell_build<float>(L.A, s)) != G2P_OK) return fail(st);
             if (L.P.ptr && (st = sell_build<float>(L.P, s, 254)) != G2P_OK) return fail(st);
@@ -205,7 +210,7 @@ static g2p_status reserve_block(g2p_solver *S, int k) {
     dfree(S->rb, s); dfree(S->rf, s); dfree(S->df, s);
     int64_t nk = S->A.n * k;
     G2P_TRY(dalloc(&S->rb, nk, s));
-    if (S->precision == G2P_PREC_MIXED) {
+    if (S->precision != G2P_PREC_FP64) {
         G2P_TRY(dalloc(&S->rf, nk, s));
         G2P_TRY(dalloc(&S->df, nk, s));
     }
@@ -223,7 +228,10 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
     SolveReport rep;
     int refinements = 0, iters = 0;
     if (S->precision != G2P_PREC_MIXED) {
-        G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep));
+        F32Precond pc;
+        pc.H = &S->H32; pc.lr = &S->lr; pc.in = S->rf; pc.out = S->df;
+        G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep,
+                               S->precision == G2P_PREC_FP64_PC32 ? &pc : nullptr));
         iters = rep.iterations;
         if (getenv("G2P_DEBUG"))
             fprintf(stderr, "[g2p] n=%lld k=%d fp64: its %d rel %.3e\n", (long long)n, k, rep.iterations, rep.rel_residual);

@@ -23,9 +23,11 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "primitives.cuh"
+
 #include "solver.h"
 
 namespace g2p {
@@ -2306,15 +2308,26 @@ __global__ void k_add_vec(double *a, const double *b, int n) {
     if (i < n) a[i] += b[i];
 }
 
+__global__ void k_d_to_f(int64_t nk, const double *a, float *b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nk; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+__global__ void k_f_to_d(int64_t nk, const float *a, double *b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nk; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (double)a[i];
+}
+
 template <class T>
 g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T *x, int k, const SolverConfig &cfg,
-                  const double *bnorm_override, cudaStream_t s, SolveReport &rep) {
+                  const double *bnorm_override, cudaStream_t s, SolveReport &rep, const F32Precond *pc) {
     const int64_t n = A.n, nk = n * k;
     const int m = cfg.restart;
     if (k < 1 || k > kMaxRhs) { set_last_message("block of %d right-hand sides (1..%d supported)", k, kMaxRhs); return G2P_ERR_INVALID; }
+    if (pc && !std::is_same<T, double>::value) { set_last_message("FP32 preconditioning of an FP32 solve"); return G2P_ERR_INVALID; }
     G2P_TRY(krylov_alloc<T>(K, n, k, m, s));
-    G2P_TRY(hierarchy_reserve<T>(H, k, s));
-    Level<T> &L0 = H.lv[0];
+    if (pc) G2P_TRY(hierarchy_reserve<float>(*pc->H, k, s));
+    else G2P_TRY(hierarchy_reserve<T>(H, k, s));
+    const LongRows &lr0 = pc ? *pc->lr : H.lv[0].lr;
     const unsigned rg = row_grid(n, k);
     const dim3 rb = row_block(k);
     const int cpr = chunk_cpr<T>(k);
@@ -2332,7 +2345,7 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
     double *dots2 = K.hcol + (int64_t)k * (m + 1);
     for (;;) {
         // r = b - A x ; beta = ||r||
-        spmm_b<T>(A, L0.lr, x, K.r, k, b, s);
+        spmm_b<T>(A, lr0, x, K.r, k, b, s);
         colnorms<T>(K.r, n, k, K.partial, K.beta, s);
         G2P_CUDA(cudaMemcpyAsync(K.h_est, K.beta, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
         G2P_CUDA(cudaMemcpyAsync(K.h_est + k, K.bnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
@@ -2353,8 +2366,18 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
         for (; j < m && it < cfg.maxit; j++) {
             T *Vj = K.V + (int64_t)j * nk, *Zj = K.Z + (int64_t)j * nk;
             // Z_j = M^-1 V_j (one V-cycle, in place on the basis vectors)
-            vcycle<T>(H, cfg, 0, k, s, Vj, Zj);
-            spmm<T>(A, L0.lr, Zj, K.w, k, s);
+            if constexpr (std::is_same<T, double>::value) {
+                if (pc) {
+                    (g2p::kbegin("k_d_to_f", s), k_d_to_f<<<grid_for(nk), kThreads, 0, s>>>(nk, Vj, pc->in), g2p::kend(s));
+                    vcycle<float>(*pc->H, cfg, 0, k, s, pc->in, pc->out);
+                    (g2p::kbegin("k_f_to_d", s), k_f_to_d<<<grid_for(nk), kThreads, 0, s>>>(nk, pc->out, Zj), g2p::kend(s));
+                } else {
+                    vcycle<T>(H, cfg, 0, k, s, Vj, Zj);
+                }
+            } else {
+                vcycle<T>(H, cfg, 0, k, s, Vj, Zj);
+            }
+            spmm<T>(A, lr0, Zj, K.w, k, s);
             // classical Gram-Schmidt, optionally twice
             mdot<T>(K.V, n, j + 1, K.w, k, K.partial, K.hcol, s);
             maxpy(K.hcol, j + 1);
@@ -2384,9 +2407,10 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
     return G2P_OK;
 }
 template g2p_status fgmres<double>(const Csr<double> &, Hierarchy<double> &, Krylov<double> &, const double *, double *,
-                                   int, const SolverConfig &, const double *, cudaStream_t, SolveReport &);
+                                   int, const SolverConfig &, const double *, cudaStream_t, SolveReport &,
+                                   const F32Precond *);
 template g2p_status fgmres<float>(const Csr<float> &, Hierarchy<float> &, Krylov<float> &, const float *, float *, int,
-                                  const SolverConfig &, const double *, cudaStream_t, SolveReport &);
+                                  const SolverConfig &, const double *, cudaStream_t, SolveReport &, const F32Precond *);
 
 }  // namespace g2p
 

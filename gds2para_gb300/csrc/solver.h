@@ -90,11 +90,23 @@ struct SolveReport {
     bool converged = false;
 };
 
+// An FP32 V-cycle used as the preconditioner of an FP64 FGMRES: the basis
+// vector is rounded to FP32, cycled through H (the hierarchy of the operator
+// scaled by a power of two, which FGMRES does not need undone), and the
+// result widened back.  lr: long rows of the FP64 operator; in, out: n * k
+// FP32 work vectors.
+struct F32Precond {
+    Hierarchy<float> *H = nullptr;
+    const LongRows *lr = nullptr;
+    float *in = nullptr, *out = nullptr;
+};
+
 // FGMRES(m) right-preconditioned by one V-cycle per iteration, for k right-
-// hand sides at once.  x holds the initial guess on entry.
+// hand sides at once.  x holds the initial guess on entry.  With pc (FP64
+// only) the V-cycle runs in FP32 on pc->H and H is not used.
 template <class T>
 g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T *x, int k, const SolverConfig &cfg,
-                  const double *bnorm_override, cudaStream_t s, SolveReport &rep);
+                  const double *bnorm_override, cudaStream_t s, SolveReport &rep, const F32Precond *pc = nullptr);
 
 template <class T>
 g2p_status krylov_alloc(Krylov<T> &K, int64_t n, int k, int m, cudaStream_t s);

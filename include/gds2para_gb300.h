@@ -67,11 +67,14 @@ typedef struct {
 typedef struct g2p_mesh g2p_mesh;
 typedef struct g2p_solver g2p_solver;
 
-enum { G2P_PREC_FP64 = 0, G2P_PREC_MIXED = 1 };
+/* G2P_PREC_FP64: the plain FP64 method.  G2P_PREC_MIXED: FP32 FGMRES and AMG
+ * inside FP64 iterative refinement.  G2P_PREC_FP64_PC32: FP64 FGMRES whose
+ * V-cycle preconditioner runs in FP32 (for operators whose conditioning
+ * stalls FP32 Krylov solves). */
+enum { G2P_PREC_FP64 = 0, G2P_PREC_MIXED = 1, G2P_PREC_FP64_PC32 = 2 };
 
 typedef struct {
-    int32_t precision;        /* G2P_PREC_FP64: plain FP64 method; G2P_PREC_MIXED: FP32
-                                 Krylov/AMG inside FP64 iterative refinement */
+    int32_t precision;        /* G2P_PREC_FP64, G2P_PREC_MIXED or G2P_PREC_FP64_PC32 */
     int32_t restart;          /* FGMRES restart length (KDim) */
     int32_t maxit;            /* max FGMRES iterations (FP64) / refinement sweeps x inner (mixed) */
     double rtol;              /* ||b - A x|| <= rtol * ||b|| per right-hand side */

@@ -67,7 +67,7 @@ def test_gpu_hypre_solve_dropin_matches_reference_solution(g2p):
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-2
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp64_pc32"])
 def test_gpu_solver_multi_rhs_against_direct(precision, g2p, coracle):
     import scipy.sparse as sp
     import scipy.sparse.linalg as spl
@@ -86,6 +86,12 @@ def test_gpu_solver_multi_rhs_against_direct(precision, g2p, coracle):
         res = np.linalg.norm(B - Am @ X, axis=0) / np.linalg.norm(B, axis=0)
         assert res.max() <= 1e-10 * 1.0001, res
         assert np.linalg.norm(X - Xd) / np.linalg.norm(Xd) < 1e-7
+
+
+def test_gpu_solver_rejects_unknown_precision(g2p):
+    rows = np.array([0, 1]); col = np.array([0, 1]); val = np.array([2.0, 3.0])
+    with pytest.raises(g2p.G2PError):
+        g2p.Solver(rows, col, val, 2, g2p.default_params(precision=7))
 
 
 def test_gpu_rejects_bad_coo(g2p):
