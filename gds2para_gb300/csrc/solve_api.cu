@@ -249,16 +249,23 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
         const int max_ref = S->cfg.maxit > 0 ? std::max(2, S->cfg.maxit / std::max(1, S->inner_maxit / 2)) : 20;
         rep.converged = false;
         for (int ref = 0; ref <= max_ref; ref++) {
-            residual64(S->A, S->lr, b, x, S->rb, k, s);
-            colnorms<double>(S->rb, n, k, S->K64.partial, rn, s);
-            G2P_CUDA(cudaMemcpyAsync(hr.data(), rn, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
-            G2P_CUDA(cudaStreamSynchronize(s));
+            // x is zero on the first sweep, so its residual is b itself
+            const double *res = ref == 0 ? b : S->rb;
+            if (ref == 0) {
+                G2P_CUDA(cudaStreamSynchronize(s));
+                hr = hb;
+            } else {
+                residual64(S->A, S->lr, b, x, S->rb, k, s);
+                colnorms<double>(S->rb, n, k, S->K64.partial, rn, s);
+                G2P_CUDA(cudaMemcpyAsync(hr.data(), rn, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+                G2P_CUDA(cudaStreamSynchronize(s));
+            }
             double worst = 0;
             for (int r = 0; r < k; r++) worst = std::max(worst, hb[r] > 0 ? hr[r] / hb[r] : 0.0);
             rep.rel_residual = worst;
             if (worst <= S->cfg.rtol) { rep.converged = true; break; }
             if (ref == max_ref) break;
-            (g2p::kbegin("k_to_f", s), k_to_f<<<grid_for(nk), kThreads, 0, s>>>(nk, S->rb, S->rf), g2p::kend(s));
+            (g2p::kbegin("k_to_f", s), k_to_f<<<grid_for(nk), kThreads, 0, s>>>(nk, res, S->rf), g2p::kend(s));
             G2P_CUDA(cudaMemsetAsync(S->df, 0, sizeof(float) * nk, s));
             SolveReport ir;
             G2P_TRY(fgmres<float>(S->H32.lv[0].A, S->H32, S->K32, S->rf, S->df, k, inner, nullptr, s, ir));
