@@ -424,9 +424,6 @@ def run_c4(args):
         "config": {"workload": WORKLOAD["c4"], "config": "c4", "jobs": len(jobs), "port_freq_columns": units,
                    "arrival_rate_per_s": rate, "max_active": 8, "budget_bytes": budget,
                    "l2": "each job's inputs are resident only while it runs"},
-        "network": {"convert_z_to_s_ms": 1e3 * conv_s, "citi_write_ms": 1e3 * citi_s,
-                    "touchstone_write_ms": 1e3 * ts_s,
-                    "what": "convertParam('S') on the GPU and dumpCITI / dumpTouchstone of this run's Z"},
         "job_ms": {"p50": pct(0.5), "p99": pct(0.99), "max": lat[-1],
                    "load": "Poisson arrivals at 0.8 x serial capacity", "arrival_span_s": span,
                    "jobs_overlapped": overlapped},

@@ -179,9 +179,10 @@ extern "C" g2p_status g2p_convert_param(char from, char to, int32_t nports, int3
         G2P_CUDA(cudaMemcpyAsync(d_in, in, sizeof(double) * total, cudaMemcpyDefault, s));
         G2P_CUDA(cudaMemcpyAsync(d_root, root.data(), sizeof(double) * nports, cudaMemcpyHostToDevice, s));
         G2P_CUDA(cudaMemsetAsync(d_sing, 0, sizeof(int), s));
+        // three working matrices; the opt-in limit also covers the kernel's
+        // own static shared memory beyond the default 48 KB
         const size_t shm = 3 * sizeof(Cx) * nports * nports;
-        if (shm > 48 * 1024)
-            G2P_CUDA(cudaFuncSetAttribute(k_convert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+        G2P_CUDA(cudaFuncSetAttribute(k_convert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
         (kbegin("k_convert", s), k_convert<<<(unsigned)nfreq, 256, shm, s>>>(nports, d_in, d_out, d_root, mode, d_sing), kend(s));
         G2P_CUDA(cudaGetLastError());
         int sing = 0;

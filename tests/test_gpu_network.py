@@ -32,7 +32,7 @@ def _close(got, want, rtol):
     assert np.all(np.abs(got - want) <= rtol * scale), float((np.abs(got - want) / scale).max())
 
 
-@pytest.mark.parametrize("nports,nfreq", [(1, 5), (2, 40), (3, 7), (8, 33), (17, 4), (64, 3)])
+@pytest.mark.parametrize("nports,nfreq", [(1, 5), (2, 40), (3, 7), (8, 33), (17, 4), (32, 64), (33, 2), (64, 3)])
 def test_convert_matches_oracle(nports, nfreq):
     rng = np.random.default_rng(nports * 1000 + nfreq)
     zs = rng.uniform(20.0, 80.0, nports)
