@@ -31,6 +31,7 @@ void retain_pool_memory(int device);
 // Counts kernel launches issued by the library and, while profiling is on,
 // brackets each launch with CUDA events keyed by the kernel's name.
 void launch_tick();
+void launch_add(int64_t n);
 int64_t launch_count();
 void kbegin(const char *name, cudaStream_t s);
 void kend(cudaStream_t s);

@@ -44,6 +44,7 @@ const char *last_error() { return g_err.c_str(); }
 
 static std::atomic<int64_t> g_launches{0};
 void launch_tick() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void launch_add(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 struct NamedProfile {

@@ -110,7 +110,7 @@ extern "C" void g2p_default_params(g2p_solver_params *p, int32_t parity_mode) {
     p->inner_rtol = 3e-3;
     p->inner_maxit = 40;
     p->batch = 1;
-    p->use_graphs = 0;
+    p->use_graphs = 1;
 }
 
 static SolverConfig cfg_from(const g2p_solver_params *p) {
@@ -123,6 +123,7 @@ static SolverConfig cfg_from(const g2p_solver_params *p) {
     c.coarse_size = p->coarse_size > 0 ? p->coarse_size : 256;
     c.strength = p->strength > 0 ? p->strength : 0.04;
     c.max_levels = p->max_levels > 0 ? p->max_levels : 20;
+    c.use_graphs = p->use_graphs != 0;
     c.reorth = false;   // classical Gram-Schmidt once: same iteration counts, half the passes
     if (const char *e = getenv("G2P_REORTH")) c.reorth = atoi(e) != 0;
     return c;

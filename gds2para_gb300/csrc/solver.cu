@@ -2168,7 +2168,16 @@ template g2p_status hierarchy_reserve<float>(Hierarchy<float> &, int, cudaStream
 
 // ------------------------------------------------------------------- FGMRES
 template <class T>
+void Krylov<T>::drop_graphs() {
+    for (auto &st : steps)
+        if (st.exec) cudaGraphExecDestroy(st.exec);
+    steps.clear();
+    graph_key.clear();
+}
+
+template <class T>
 void Krylov<T>::release(cudaStream_t s) {
+    drop_graphs();
     dfree(V, s); dfree(Z, s); dfree(w, s); dfree(r, s);
     dfree(H, s); dfree(cs, s); dfree(sn, s); dfree(g, s); dfree(y, s);
     dfree(beta, s); dfree(bnorm, s); dfree(partial, s); dfree(hcol, s);
@@ -2328,6 +2337,21 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
     if (pc) G2P_TRY(hierarchy_reserve<float>(*pc->H, k, s));
     else G2P_TRY(hierarchy_reserve<T>(H, k, s));
     const LongRows &lr0 = pc ? *pc->lr : H.lv[0].lr;
+    // CUDA graphs of the Arnoldi steps: off while kernels are being timed;
+    // rebuilt when the block width, operator or preconditioner changes
+    const bool graphs = cfg.use_graphs && !kprof_on() && !g_prof.on;
+    if (graphs) {
+        const void *hier = pc ? (const void *)pc->H : (const void *)&H;
+        const int kcap = pc ? pc->H->kcap : H.kcap;
+        const std::vector<const void *> key = {(const void *)(intptr_t)k, (const void *)A.val, hier,
+                                               (const void *)(intptr_t)kcap, (const void *)(intptr_t)cfg.degree,
+                                               (const void *)(intptr_t)cfg.reorth, pc ? (const void *)pc->in : nullptr};
+        if (K.graph_key != key || (int)K.steps.size() != m) {
+            K.drop_graphs();
+            K.graph_key = key;
+            K.steps.resize(m);
+        }
+    }
     const unsigned rg = row_grid(n, k);
     const dim3 rb = row_block(k);
     const int cpr = chunk_cpr<T>(k);
@@ -2365,34 +2389,69 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
         int j = 0;
         for (; j < m && it < cfg.maxit; j++) {
             T *Vj = K.V + (int64_t)j * nk, *Zj = K.Z + (int64_t)j * nk;
-            // Z_j = M^-1 V_j (one V-cycle, in place on the basis vectors)
-            if constexpr (std::is_same<T, double>::value) {
-                if (pc) {
-                    (g2p::kbegin("k_d_to_f", s), k_d_to_f<<<grid_for(nk), kThreads, 0, s>>>(nk, Vj, pc->in), g2p::kend(s));
-                    vcycle<float>(*pc->H, cfg, 0, k, s, pc->in, pc->out);
-                    (g2p::kbegin("k_f_to_d", s), k_f_to_d<<<grid_for(nk), kThreads, 0, s>>>(nk, pc->out, Zj), g2p::kend(s));
+            auto step = [&]() {
+                // Z_j = M^-1 V_j (one V-cycle, in place on the basis vectors)
+                if constexpr (std::is_same<T, double>::value) {
+                    if (pc) {
+                        (g2p::kbegin("k_d_to_f", s), k_d_to_f<<<grid_for(nk), kThreads, 0, s>>>(nk, Vj, pc->in), g2p::kend(s));
+                        vcycle<float>(*pc->H, cfg, 0, k, s, pc->in, pc->out);
+                        (g2p::kbegin("k_f_to_d", s), k_f_to_d<<<grid_for(nk), kThreads, 0, s>>>(nk, pc->out, Zj), g2p::kend(s));
+                    } else {
+                        vcycle<T>(H, cfg, 0, k, s, Vj, Zj);
+                    }
                 } else {
                     vcycle<T>(H, cfg, 0, k, s, Vj, Zj);
                 }
+                spmm<T>(A, lr0, Zj, K.w, k, s);
+                // classical Gram-Schmidt, optionally twice
+                mdot<T>(K.V, n, j + 1, K.w, k, K.partial, K.hcol, s);
+                maxpy(K.hcol, j + 1);
+                if (cfg.reorth) {
+                    mdot<T>(K.V, n, j + 1, K.w, k, K.partial, dots2, s);
+                    maxpy(dots2, j + 1);
+                    (g2p::kbegin("k_add_vec", s), k_add_vec<<<((j + 1) * k + 255) / 256, 256, 0, s>>>(K.hcol, dots2, (j + 1) * k), g2p::kend(s));
+                }
+                double *hnorm = K.beta;   // reuse
+                colnorms<T>(K.w, n, k, K.partial, hnorm, s);
+                if (cpr) (g2p::kbegin("k_arnoldi_finish", s), k_scale_cols_v<T><<<chunk_grid(nq), 256, 0, s>>>(nq, cpr, hnorm, K.w, K.V + (int64_t)(j + 1) * nk), g2p::kend(s));
+                else (g2p::kbegin("k_arnoldi_finish", s), k_arnoldi_finish<T><<<rg, rb, 0, s>>>(n, k, hnorm, K.w, K.V + (int64_t)(j + 1) * nk), g2p::kend(s));
+                double *est = K.y;        // scratch for the estimates (k values)
+                (g2p::kbegin("k_givens", s), k_givens<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.hcol, hnorm, K.H, K.cs, K.sn, K.g, K.bnorm, est), g2p::kend(s));
+                cudaMemcpyAsync(K.h_est, est, sizeof(double) * k, cudaMemcpyDeviceToHost, s);
+            };
+            if (graphs) {
+                auto &st = K.steps[j];
+                if (st.exec) {
+                    G2P_CUDA(cudaGraphLaunch(st.exec, s));
+                    launch_add(st.launches);
+                } else if (st.seen && !st.failed) {
+                    // second use of step j: capture it, then replay
+                    const int64_t n0 = launch_count();
+                    cudaGraph_t gr = nullptr;
+                    bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+                    if (ok) step();
+                    ok = cudaStreamEndCapture(s, &gr) == cudaSuccess && ok && gr != nullptr;
+                    if (ok) ok = cudaGraphInstantiate(&st.exec, gr, 0) == cudaSuccess;
+                    if (gr) cudaGraphDestroy(gr);
+                    st.launches = launch_count() - n0;
+                    launch_add(-st.launches);
+                    if (ok) {
+                        G2P_CUDA(cudaGraphLaunch(st.exec, s));
+                        launch_add(st.launches);
+                    } else {
+                        cudaGetLastError();
+                        st.exec = nullptr;
+                        st.failed = true;
+                        step();
+                    }
+                } else {
+                    st.seen = true;
+                    step();
+                }
             } else {
-                vcycle<T>(H, cfg, 0, k, s, Vj, Zj);
+                step();
             }
-            spmm<T>(A, lr0, Zj, K.w, k, s);
-            // classical Gram-Schmidt, optionally twice
-            mdot<T>(K.V, n, j + 1, K.w, k, K.partial, K.hcol, s);
-            maxpy(K.hcol, j + 1);
-            if (cfg.reorth) {
-                mdot<T>(K.V, n, j + 1, K.w, k, K.partial, dots2, s);
-                maxpy(dots2, j + 1);
-                (g2p::kbegin("k_add_vec", s), k_add_vec<<<((j + 1) * k + 255) / 256, 256, 0, s>>>(K.hcol, dots2, (j + 1) * k), g2p::kend(s));
-            }
-            double *hnorm = K.beta;   // reuse
-            colnorms<T>(K.w, n, k, K.partial, hnorm, s);
-            if (cpr) (g2p::kbegin("k_arnoldi_finish", s), k_scale_cols_v<T><<<chunk_grid(nq), 256, 0, s>>>(nq, cpr, hnorm, K.w, K.V + (int64_t)(j + 1) * nk), g2p::kend(s));
-            else (g2p::kbegin("k_arnoldi_finish", s), k_arnoldi_finish<T><<<rg, rb, 0, s>>>(n, k, hnorm, K.w, K.V + (int64_t)(j + 1) * nk), g2p::kend(s));
-            double *est = K.y;        // scratch for the estimates (k values)
-            (g2p::kbegin("k_givens", s), k_givens<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.hcol, hnorm, K.H, K.cs, K.sn, K.g, K.bnorm, est), g2p::kend(s));
-            G2P_CUDA(cudaMemcpyAsync(K.h_est, est, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+            G2P_CUDA(cudaGetLastError());
             G2P_CUDA(cudaStreamSynchronize(s));
             it++;
             double worst = 0;

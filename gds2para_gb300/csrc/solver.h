@@ -57,6 +57,7 @@ struct SolverConfig {
     int max_levels = 20;
     double cheb_ratio = 0.1;     // lower Chebyshev bound = ratio * lmax
     bool reorth = true;
+    bool use_graphs = false;     // replay each Arnoldi step from a CUDA graph
 };
 
 template <class T>
@@ -81,6 +82,16 @@ struct Krylov {
     double *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr;
     double *beta = nullptr, *bnorm = nullptr, *partial = nullptr, *hcol = nullptr;
     double *h_est = nullptr;    // pinned host copy of residual estimates
+    // Arnoldi step j as a CUDA graph (captured on its second use), valid for
+    // the block width, operator and preconditioner in graph_key
+    struct Step {
+        cudaGraphExec_t exec = nullptr;
+        int64_t launches = 0;
+        bool seen = false, failed = false;
+    };
+    std::vector<Step> steps;
+    std::vector<const void *> graph_key;
+    void drop_graphs();
     void release(cudaStream_t s);
 };
 

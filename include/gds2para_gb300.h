@@ -85,7 +85,9 @@ typedef struct {
     double inner_rtol;        /* mixed: inner FP32 solve tolerance */
     int32_t inner_maxit;      /* mixed: inner FP32 iterations per refinement step */
     int32_t batch;            /* paraGenerator: 1 = all ports as one RHS block, 0 = port by port */
-    int32_t use_graphs;       /* capture Krylov cycles in CUDA graphs */
+    int32_t use_graphs;       /* 1 (default): each Arnoldi step (V-cycle, product,
+                                 Gram-Schmidt, Givens) is captured as a CUDA graph on
+                                 its second use and replayed; results are identical */
 } g2p_solver_params;
 
 typedef struct {

@@ -99,3 +99,18 @@ def test_gpu_rejects_bad_coo(g2p):
         g2p.Solver(np.array([1, 0]), np.array([0, 1]), np.array([1.0, 1.0]), 2)   # not row-sorted
     with pytest.raises(g2p.G2PError):
         g2p.Solver(np.array([0, 1]), np.array([0, 5]), np.array([1.0, 1.0]), 2)   # column out of range
+
+
+@pytest.mark.parametrize("name,precision", [("strip_c1", "mixed"), ("manhattan_sweep", "fp64"), ("multistrip_small", "mixed")])
+def test_gpu_graph_replay_gives_identical_z(name, precision, g2p):
+    """Arnoldi steps replayed from CUDA graphs give the same Z, bit for bit,
+    as the same steps launched one kernel at a time."""
+    d, A, M = golden_layout(name)
+    out = []
+    for graphs in (0, 1):
+        with g2p.FdtdMesh(d) as m:
+            g2p.generateStiff(m)
+            Z, st = g2p.paraGenerator(m, g2p.default_params(precision=precision, rtol=1e-10, use_graphs=graphs))
+        out.append((Z, st.total_iterations))
+    assert out[0][1] == out[1][1]
+    assert np.array_equal(out[0][0], out[1][0])
