@@ -172,7 +172,7 @@ def run_gb300(args):
     t0 = time.perf_counter()
     d = layout.build(lay_cfg)
     host_mesh_s = time.perf_counter() - t0
-    params = default_params(precision=args.precision, batch=args.batch, rtol=RTOL[args.config])
+    params = default_params(precision=args.precision, batch=args.batch, rtol=RTOL[args.config], autotune=1)
     dev = make_desc(d, "cuda", torch)
     pin = make_desc(d, "pinned", torch)
     z =torch.zeros(2 * d.nfreq * d.num_ports * d.num_ports, dtype=torch.float64).pin_memory()
@@ -231,6 +231,8 @@ def run_gb300(args):
     last = {"assembly_ms": stats.assembly_ms, "setup_ms": stats.setup_ms, "solve_ms": stats.solve_ms,
             "total_ms": stats.total_ms, "iterations": stats.total_iterations,
             "max_rel_residual": stats.max_rel_residual, "ad_levels": stats.ad_levels, "ac_levels": stats.ac_levels,
+            "rhs_block": stats.rhs_block, "ad_degree": stats.ad_degree,
+            "autotune": "block width and Chebyshev degree picked in the warm-up (first Ad solve timed per candidate)",
             "note": "host wall-clock of the phases of the last timed step (assembly and setup are mostly "
                     "enqueue time; the solve phase ends with the host copy of Z)"}
     # kernel-level figures from separate profiled steps (events around every

@@ -47,7 +47,7 @@ class SolverParams(C.Structure):
     _fields_ = [("precision", C.c_int32), ("restart", C.c_int32), ("maxit", C.c_int32), ("rtol", C.c_double),
                 ("smoother_degree", C.c_int32), ("coarse_size", C.c_int32), ("strength", C.c_double),
                 ("max_levels", C.c_int32), ("inner_rtol", C.c_double), ("inner_maxit", C.c_int32),
-                ("batch", C.c_int32), ("use_graphs", C.c_int32)]
+                ("batch", C.c_int32), ("use_graphs", C.c_int32), ("autotune", C.c_int32)]
 
 
 class SolveStats(C.Structure):
@@ -65,7 +65,7 @@ class ExtractStats(C.Structure):
     _fields_ = [("sizes", Sizes), ("solves", C.c_int32), ("total_iterations", C.c_int32),
                 ("max_rel_residual", C.c_double), ("assembly_ms", C.c_double), ("setup_ms", C.c_double),
                 ("solve_ms", C.c_double), ("total_ms", C.c_double), ("ad_levels", C.c_int32),
-                ("ac_levels", C.c_int32)]
+                ("ac_levels", C.c_int32), ("rhs_block", C.c_int32), ("ad_degree", C.c_int32)]
 
 
 class BoxC(C.Structure):

@@ -12,6 +12,8 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "primitives.cuh"
@@ -234,6 +236,67 @@ static double freq_of(const g2p_mesh *m, int id) {
     return m->freq_start * m->freq_unit * pow(m->freq_end / m->freq_start, (id * 1.0 / (m->nfreq - 1)));
 }
 
+// Block width of the port right-hand sides and Chebyshev degree of the Ad
+// solves, per grid shape, port count and precision: the first choice made in
+// the process is kept, so every later job of that shape runs the same way.
+struct TuneKey {
+    int64_t nx, ny, nz, nnz;
+    int P, precision;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(nx, ny, nz, nnz, P, precision) < std::tie(o.nx, o.ny, o.nz, o.nnz, o.P, o.precision);
+    }
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, std::pair<int, int>> g_tuned;   // -> (block width, degree)
+
+// Times the Ad solve of the first block of ports with each candidate (after
+// an untimed solve, best of two) and keeps the one with the least estimated
+// time for all blocks.
+template <class F>
+static g2p_status tune_blocks(g2p_mesh *m, g2p_solver *Sd, int P, int precision, F &rhs_d, double *Bd, double *Yd,
+                              int *kb) {
+    const TuneKey key{m->d.nx, m->d.ny, m->d.nz, m->Ad.nnz, P, precision};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) {
+            *kb = it->second.first;
+            Sd->cfg.degree = it->second.second;
+            return G2P_OK;
+        }
+    }
+    std::vector<int> widths = {*kb};
+    for (int w : {64, 32, 16, 8})
+        if (w < *kb) widths.push_back(w);
+    const int degree0 = Sd->cfg.degree;
+    int best_w = *kb, best_d = degree0;
+    double best = 1e300;
+    for (int w : widths) {
+        G2P_TRY(rhs_d(0, w));
+        for (int deg : {2, 3, 4}) {
+            Sd->cfg.degree = deg;
+            g2p_solve_stats ss;
+            // one untimed solve (work vectors, graph captures), then the
+            // better of two timed ones
+            g2p_status rc = g2p_solver_solve_dev(Sd, Bd, Yd, w, &ss);
+            double ms = 1e300;
+            for (int rep = 0; rep < 2 && rc == G2P_OK; rep++) {
+                auto t = std::chrono::steady_clock::now();
+                rc = g2p_solver_solve_dev(Sd, Bd, Yd, w, &ss);
+                ms = std::min(ms, ms_since(t));
+            }
+            if (rc != G2P_OK) continue;
+            const double total = ms * ((P + w - 1) / w);
+            if (total < best) { best = total; best_w = w; best_d = deg; }
+        }
+    }
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto ins = g_tuned.emplace(key, std::make_pair(best_w, best_d)).first;   // an earlier entry wins
+    *kb = ins->second.first;
+    Sd->cfg.degree = ins->second.second;
+    return G2P_OK;
+}
+
 extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *pin, double *z_out,
                                          g2p_extract_stats *st) {
     if (!m || !z_out) { set_last_message("null argument"); return G2P_ERR_INVALID; }
@@ -324,7 +387,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     // long V0d columns: up to kHugeRow entries one block each, longer ones in chunks
     const int32_t *d_mid_d = lcol.mid;
     const int64_t nmid_d = lcol.nmid;
-    const int kb = p.batch ? std::min(P, kMaxRhs) : 1;
+    int kb = p.batch ? std::min(P, kMaxRhs) : 1;
     const int64_t nd = m->v0d.ncol, nc = m->v0c.ncol, ne = d.N_edge;
     double *Bd, *Yd, *Bc, *Yc, *crhs, *yd1, *yc, *yd2, *zre, *zim;
     G2P_TRY(dalloc(&Bd, nd * kb, s)); G2P_TRY(dalloc(&Yd, nd * kb, s));
@@ -334,6 +397,18 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     const double omega = (2 * 3.14159265358979323846 * m->freq_start * m->freq_unit);
     EdgeFactor f0{d, m->epsn, omega, m->k.eps0, 0};
     EdgeFactor f1{d, m->epsn, omega, m->k.eps0, 1};
+    // (1) b_d = -V0da^T J for ports p0 .. p0 + kk - 1
+    auto rhs_d = [&](int p0, int kk) -> g2p_status {
+        const int64_t *d_pp = d_pptr + p0;     // entries of port p0 + r: [d_pp[r], d_pp[r + 1])
+        const unsigned rg = (unsigned)((kk + 127) / 128);
+        G2P_CUDA(cudaMemsetAsync(Bd, 0, sizeof(double) * nd * kk, s));
+        (g2p::kbegin("k_rhs_ports", s), k_rhs_ports<<<rg, 128, 0, s>>>(kk, d_pp, d_pe_edge, d_pe_J, m->v0d.ecol, m->v0d.eaval, kk, Bd), g2p::kend(s));
+        (g2p::kbegin("k_scale", s), k_scale<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Bd, -1.0), g2p::kend(s));
+        return G2P_OK;
+    };
+    if (p.autotune && p.batch) G2P_TRY(tune_blocks(m, Sd, P, p.precision, rhs_d, Bd, Yd, &kb));
+    local.rhs_block = kb;
+    local.ad_degree = Sd->cfg.degree;
     t0 = std::chrono::steady_clock::now();
     g2p_status worst_rc = G2P_OK;
     for (int p0 = 0; p0 < P; p0 += kb) {
@@ -341,10 +416,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         // entries of this block's ports, renumbered 0..kk-1
         const int64_t *d_pp = d_pptr + p0;     // entries of port p0 + r: [d_pp[r], d_pp[r + 1])
         const unsigned rg = (unsigned)((kk + 127) / 128);
-        // (1) b_d = -V0da^T J
-        G2P_CUDA(cudaMemsetAsync(Bd, 0, sizeof(double) * nd * kk, s));
-        (g2p::kbegin("k_rhs_ports", s), k_rhs_ports<<<rg, 128, 0, s>>>(kk, d_pp, d_pe_edge, d_pe_J, m->v0d.ecol, m->v0d.eaval, kk, Bd), g2p::kend(s));
-        (g2p::kbegin("k_scale", s), k_scale<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Bd, -1.0), g2p::kend(s));
+        G2P_TRY(rhs_d(p0, kk));
         g2p_solve_stats ss;
         g2p_status rc = g2p_solver_solve_dev(Sd, Bd, Yd, kk, &ss);
         if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }

@@ -111,6 +111,7 @@ extern "C" void g2p_default_params(g2p_solver_params *p, int32_t parity_mode) {
     p->inner_maxit = 40;
     p->batch = 1;
     p->use_graphs = 1;
+    p->autotune = 0;
 }
 
 static SolverConfig cfg_from(const g2p_solver_params *p) {

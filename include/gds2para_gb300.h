@@ -88,6 +88,13 @@ typedef struct {
     int32_t use_graphs;       /* 1 (default): each Arnoldi step (V-cycle, product,
                                  Gram-Schmidt, Givens) is captured as a CUDA graph on
                                  its second use and replayed; results are identical */
+    int32_t autotune;         /* paraGenerator, 1: pick the block width of the port
+                                 right-hand sides (all ports, or 8/16/32/64 at a time)
+                                 and the Chebyshev degree (2, 3, 4) of the Ad solves by
+                                 timing the first block's Ad solve with each, once per
+                                 grid shape and port count in the process (later jobs
+                                 of that shape reuse the choice); 0 (default): all
+                                 ports, smoother_degree */
 } g2p_solver_params;
 
 typedef struct {
@@ -111,6 +118,7 @@ typedef struct {
     double max_rel_residual;
     double assembly_ms, setup_ms, solve_ms, total_ms;
     int32_t ad_levels, ac_levels;
+    int32_t rhs_block, ad_degree;    /* ports per block solve and Ad's Chebyshev degree used */
 } g2p_extract_stats;
 
 /* ---- library ---- */
