@@ -31,13 +31,15 @@ sys.path.insert(0, ROOT)
 
 METRIC = "port-freq solves/s at 1e-6 rel Z err, mixed+batched vs FP64 GPU; p50/p99 job ms"
 UNIT = "port-freq solves/s"
-RTOL = {"c1": 1e-10, "c2": 1e-8, "c3": 1e-8, "c4": 1e-8}
+RTOL = {"c1": 1e-10, "c2": 1e-8, "c3": 1e-8, "c4": 1e-8, "c5": 1e-8}
 WORKLOAD = {
     "c1": "microstrip 101x41x11 nodes at 1 um, 1 port, 1 GHz, rtol 1e-10",
     "c2": "random Manhattan 512x512x24 nodes, 4 metal layers x 64 wires, 8 ports, 10 GHz, rtol 1e-8",
     "c3": "microstrip stack 256x256x16 nodes, 32 strips/ports x 64 log-spaced points 1e7..1e11 Hz, rtol 1e-8",
     "c4": "served stream of 48 random Manhattan jobs (sides log-uniform 64..384, nz 10..16, 1..8 ports, 1..16 "
           "log-spaced points 1e8..1e10 Hz), Poisson arrivals at 0.8 x the serial capacity, 150 GB budget, rtol 1e-8",
+    "c5": "large random Manhattan 1536x1536x32 nodes (224M edges), 6 metal layers x 256 wires, 16 ports x 8 "
+          "log-spaced points 1e8..1e10 Hz, ports in blocks of 4, rtol 1e-8",
 }
 
 
@@ -172,7 +174,10 @@ def run_gb300(args):
     t0 = time.perf_counter()
     d = layout.build(lay_cfg)
     host_mesh_s = time.perf_counter() - t0
-    params = default_params(precision=args.precision, batch=args.batch, rtol=RTOL[args.config], autotune=1)
+    # c5: the port blocks that fit 280 GB of HBM (4 ports: about 175 GiB)
+    big = args.config == "c5"
+    batch = (args.batch if args.batch > 1 else 4) if big else args.batch
+    params = default_params(precision=args.precision, batch=batch, rtol=RTOL[args.config], autotune=0 if big else 1)
     dev = make_desc(d, "cuda", torch)
     pin = make_desc(d, "pinned", torch)
     z =torch.zeros(2 * d.nfreq * d.num_ports * d.num_ports, dtype=torch.float64).pin_memory()
@@ -242,14 +247,16 @@ def run_gb300(args):
     # accuracy of this run's Z against the plain FP64 GPU method, and that
     # method's own speed (FP64 throughout, one port at a time), untimed above
     z_run = z.numpy().copy()
-    p64 = default_params(precision="fp64", batch=0, rtol=RTOL[args.config])
-    step(dev, p64)
-    z64 = z.numpy().copy()
     zr = z_run.reshape(-1, 2)
-    zf = z64.reshape(-1, 2)
-    zc, z64c = zr[:, 0] + 1j * zr[:, 1], zf[:, 0] + 1j * zf[:, 1]
-    z_err = float(np.max(np.abs(zc - z64c)) / max(np.max(np.abs(z64c)), 1e-300))
-    fp64_ms, _, _ = timed(dev, 1, prm=p64) if args.precision == "mixed" or args.batch else (ms, 0, None)
+    zc = zr[:, 0] + 1j * zr[:, 1]
+    z_err = fp64_ms = None
+    if not big:      # the plain method would take minutes at c5's size
+        p64 = default_params(precision="fp64", batch=0, rtol=RTOL[args.config])
+        step(dev, p64)
+        zf = z.numpy().copy().reshape(-1, 2)
+        z64c = zf[:, 0] + 1j * zf[:, 1]
+        z_err = float(np.max(np.abs(zc - z64c)) / max(np.max(np.abs(z64c)), 1e-300))
+        fp64_ms, _, _ = timed(dev, 1, prm=p64) if args.precision == "mixed" or args.batch else (ms, 0, None)
     units = d.num_ports * d.nfreq
     value = whole_job_value(units, world, ms)
     e2e = whole_job_value(units, world, ms_e2e)
@@ -277,10 +284,12 @@ def run_gb300(args):
     # conductor marking, numbering and ports on the GPU (g2p_mesh_mark), from
     # host boxes to host arrays, against the host generator's time
     from gds2para_gb300 import api as _api
-    _api.meshAndMark(lay_cfg)
-    t0 = time.perf_counter()
-    _api.meshAndMark(lay_cfg)
-    gpu_mesh_s = time.perf_counter() - t0
+    gpu_mesh_s = None
+    if not big:
+        _api.meshAndMark(lay_cfg)
+        t0 = time.perf_counter()
+        _api.meshAndMark(lay_cfg)
+        gpu_mesh_s = time.perf_counter() - t0
     # network stage after the extraction: Z -> S on the GPU (g2p_convert_param,
     # host arrays in and out) and the two writers
     import tempfile
@@ -316,7 +325,8 @@ def run_gb300(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": ms_e2e},
         "gpu_launches": int(launches),
-        "mesher": {"gpu_ms": 1e3 * gpu_mesh_s, "host_generator_ms": 1e3 * host_mesh_s,
+        "mesher": {"gpu_ms": 1e3 * gpu_mesh_s if gpu_mesh_s is not None else None,
+                   "host_generator_ms": 1e3 * host_mesh_s,
                    "what": "conductor marking, numbering and port edges (g2p_mesh_mark, host arrays in and out) "
                            "vs the numpy/scipy generator that restates meshAndMark/portSet"},
         "network": {"convert_z_to_s_ms": 1e3 * conv_s, "citi_write_ms": 1e3 * citi_s,
@@ -325,9 +335,10 @@ def run_gb300(args):
         "job_ms": {"p50": pct(0.5), "p99": pct(0.99), "per_step": step_ms},
         "accuracy": {"z_rel_err_vs_fp64_gpu": z_err, "bound": 1e-6,
                      "note": "max |Z - Z_fp64| / max |Z_fp64| over all entries and frequencies"},
-        "fp64_plain": {"value": world * units / (fp64_ms / 1e3), "unit": UNIT, "ms_per_step": fp64_ms,
-                       "what": "same job, FP64 AMG-FGMRES, one port at a time (batch 0)",
-                       "speedup_of_this_run": (world * units / (ms / 1e3)) / (world * units / (fp64_ms / 1e3))},
+        "fp64_plain": ({"value": world * units / (fp64_ms / 1e3), "unit": UNIT, "ms_per_step": fp64_ms,
+                        "what": "same job, FP64 AMG-FGMRES, one port at a time (batch 0)",
+                        "speedup_of_this_run": fp64_ms / ms} if fp64_ms else
+                       {"value": None, "what": "not run at this size"}),
         "clocks": clk,
         "roofline": {"bound": "hbm",
                      "kernel": ("k_spmm_sell<f32>" if args.precision == "mixed" else "k_spmm_sell<f64>") +
@@ -347,7 +358,9 @@ def run_gb300(args):
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s"},
     }
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(d, args, RTOL[args.config])
+        out["cpu_baseline"] = ({"value": None, "kind": "port", "cores": 1,
+                                "sample": "CPU baseline infeasible at this size (memory)"} if big
+                               else cpu_baseline(d, args, RTOL[args.config]))
     if world > 1:
         torch.distributed.destroy_process_group()
     return out, rank
@@ -485,6 +498,9 @@ def run_reference(args):
     if args.config == "c4":
         return {"impl": "reference", "unavailable": "the reference extracts one layout per process and has no "
                                                     "service to time on a job stream"}, rank
+    if args.config == "c5":
+        return {"impl": "reference", "unavailable": "CPU baseline infeasible at this size (memory): the CPU "
+                                                    "assembly of S alone needs about 68 GB of COO"}, rank
     d = layout.build(layout.config(args.config))
     O = COracle()
     rtol = RTOL[args.config]

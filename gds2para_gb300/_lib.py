@@ -47,7 +47,8 @@ class SolverParams(C.Structure):
     _fields_ = [("precision", C.c_int32), ("restart", C.c_int32), ("maxit", C.c_int32), ("rtol", C.c_double),
                 ("smoother_degree", C.c_int32), ("coarse_size", C.c_int32), ("strength", C.c_double),
                 ("max_levels", C.c_int32), ("inner_rtol", C.c_double), ("inner_maxit", C.c_int32),
-                ("batch", C.c_int32), ("use_graphs", C.c_int32), ("autotune", C.c_int32)]
+                ("batch", C.c_int32), ("use_graphs", C.c_int32), ("autotune", C.c_int32),
+                ("inner_restart", C.c_int32)]
 
 
 class SolveStats(C.Structure):

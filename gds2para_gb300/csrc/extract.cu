@@ -387,7 +387,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     // long V0d columns: up to kHugeRow entries one block each, longer ones in chunks
     const int32_t *d_mid_d = lcol.mid;
     const int64_t nmid_d = lcol.nmid;
-    int kb = p.batch ? std::min(P, kMaxRhs) : 1;
+    int kb = p.batch == 0 ? 1 : std::min(p.batch >= 2 ? p.batch : P, std::min(P, kMaxRhs));
     const int64_t nd = m->v0d.ncol, nc = m->v0c.ncol, ne = d.N_edge;
     double *Bd, *Yd, *Bc, *Yc, *crhs, *yd1, *yc, *yd2, *zre, *zim;
     G2P_TRY(dalloc(&Bd, nd * kb, s)); G2P_TRY(dalloc(&Yd, nd * kb, s));

@@ -90,11 +90,13 @@ double size_model(const g2p_mesh_desc &in, const g2p_solver_params &p) {
     Dims d;
     d.init(in.nx, in.ny, in.nz);
     const int P = std::max(1, in.num_ports);
-    const int k = p.batch ? std::min(P, 256) : 1;
+    const int k = p.batch == 0 ? 1 : std::min(p.batch >= 2 ? p.batch : P, std::min(P, 256));
     const int m = p.restart > 0 ? std::min(p.restart, 64) : 30;
+    const int mi = p.inner_restart > 0 ? std::min(p.inner_restart, 64) : m;
     const double per_edge = 4 + 4 + 1 + 40 + 13 * 12.0 + 8;          // marks, map, flags, edge views, S
     const double per_node = 2 * 7 * 12.0 * 2.5;                        // Ad copies over the AMG levels
-    const double per_rhs = (m + 8) * (p.precision == G2P_PREC_MIXED ? 4.0 : 8.0) + 6 * 8.0;
+    // Krylov basis (V and Z) and work vectors per right-hand side and node
+    const double per_rhs = p.precision == G2P_PREC_MIXED ? (2 * mi + 9) * 4.0 + 6 * 8.0 : (2 * m + 9) * 8.0;
     return d.N_edge * per_edge + d.N_node * per_node + (double)d.N_node * k * per_rhs;
 }
 

@@ -112,6 +112,7 @@ extern "C" void g2p_default_params(g2p_solver_params *p, int32_t parity_mode) {
     p->batch = 1;
     p->use_graphs = 1;
     p->autotune = 0;
+    p->inner_restart = 10;
 }
 
 static SolverConfig cfg_from(const g2p_solver_params *p) {
@@ -140,6 +141,7 @@ g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cu
     S->precision = p->precision;
     S->inner_rtol = p->inner_rtol > 0 ? p->inner_rtol : 3e-3;
     S->inner_maxit = p->inner_maxit > 0 ? p->inner_maxit : 40;
+    S->inner_restart = p->inner_restart > 0 ? std::min(p->inner_restart, 64) : S->cfg.restart;
     cudaStream_t s = stream;
     auto fail = [&](g2p_status st) { g2p_solver_destroy(S); return st; };
     g2p_status st;
@@ -247,6 +249,7 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
         SolverConfig inner = S->cfg;
         inner.rtol = S->inner_rtol;
         inner.maxit = S->inner_maxit;
+        inner.restart = S->inner_restart;
         if (const char *e = getenv("G2P_INNER_REORTH")) inner.reorth = atoi(e) != 0;
         const int max_ref = S->cfg.maxit > 0 ? std::max(2, S->cfg.maxit / std::max(1, S->inner_maxit / 2)) : 20;
         rep.converged = false;

@@ -149,6 +149,7 @@ struct g2p_solver {
     g2p::SolverConfig cfg;
     int precision = 0;
     int inner_maxit = 40;
+    int inner_restart = 10;
     double inner_rtol = 3e-3;
     g2p::Csr<double> A;                 // original FP64 operator
     g2p::LongRows lr;

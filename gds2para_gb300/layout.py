@@ -462,7 +462,8 @@ def manhattan(nx=512, ny=512, nz=24, n_metal=4, wires_per_layer=64, n_ports=8, s
 def config(name: str, **kw) -> Layout:
     """The named workloads: c1 microstrip, c2 random Manhattan at 10 GHz,
     c3 the microstrip stack with 32 strips (32 ports x 64 log-spaced points
-    1e7..1e11 Hz)."""
+    1e7..1e11 Hz), c5 the large random Manhattan layout (1536 x 1536 x 32
+    nodes, 6 metal layers of 256 wires, 16 ports x 8 log-spaced points)."""
     if name == "c1":
         return microstrip(**kw)
     if name == "c2":
@@ -473,4 +474,9 @@ def config(name: str, **kw) -> Layout:
         args = dict(nx=256, ny=256, nz=16, n_strips=32)
         args.update(kw)
         return multistrip(**args)
+    if name == "c5":
+        args = dict(nx=1536, ny=1536, nz=32, n_metal=6, wires_per_layer=256, n_ports=16, seed=1005,
+                    freq_start=1e8, freq_end=1e10, freq_unit=1.0, nfreq=8, freq_scale=0)
+        args.update(kw)
+        return manhattan(**args)
     raise KeyError(name)

@@ -84,7 +84,8 @@ typedef struct {
     int32_t max_levels;
     double inner_rtol;        /* mixed: inner FP32 solve tolerance */
     int32_t inner_maxit;      /* mixed: inner FP32 iterations per refinement step */
-    int32_t batch;            /* paraGenerator: 1 = all ports as one RHS block, 0 = port by port */
+    int32_t batch;            /* paraGenerator: 1 = all ports as one RHS block, 0 = port by
+                                 port, n >= 2 = blocks of at most n ports */
     int32_t use_graphs;       /* 1 (default): each Arnoldi step (V-cycle, product,
                                  Gram-Schmidt, Givens) is captured as a CUDA graph on
                                  its second use and replayed; results are identical */
@@ -95,6 +96,9 @@ typedef struct {
                                  grid shape and port count in the process (later jobs
                                  of that shape reuse the choice); 0 (default): all
                                  ports, smoother_degree */
+    int32_t inner_restart;    /* mixed: restart length of the inner FP32 FGMRES (its
+                                 basis is (2 inner_restart + 1) vectors of n x k; 0 =
+                                 restart) */
 } g2p_solver_params;
 
 typedef struct {
