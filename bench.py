@@ -237,7 +237,8 @@ def run_gb300(args):
             "total_ms": stats.total_ms, "iterations": stats.total_iterations,
             "max_rel_residual": stats.max_rel_residual, "ad_levels": stats.ad_levels, "ac_levels": stats.ac_levels,
             "rhs_block": stats.rhs_block, "ad_degree": stats.ad_degree,
-            "autotune": "block width and Chebyshev degree picked in the warm-up (first Ad solve timed per candidate)",
+            "autotune": ("off: fixed blocks of 4 ports (the HBM budget)" if big else
+                         "block width and Chebyshev degree picked in the warm-up (first Ad solve timed per candidate)"),
             "note": "host wall-clock of the phases of the last timed step (assembly and setup are mostly "
                     "enqueue time; the solve phase ends with the host copy of Z)"}
     # kernel-level figures from separate profiled steps (events around every
