@@ -13,6 +13,8 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -370,11 +372,44 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         if (const char *t = getenv("G2P_AC_STRENGTH")) pc.strength = atof(t);
         if (const char *t = getenv("G2P_AC_DEGREE")) pc.smoother_degree = atoi(t);
     }
-    g2p_status rs = g2p_solver_build(m->Ac, &pc, s, &Sc);
-    if (rs != G2P_OK) { g2p_v0_finish(m); return rs; }
+    // Ac's solver is built by a second host thread on its own stream (after
+    // Ac's assembly, an event on the job's stream) while this thread
+    // finishes Ad and builds its solver: both setups are partly latency-bound
+    // (per-level size read-backs).  Sequential while kernels are being timed
+    // one by one (the timing collectors are single-threaded).
+    g2p_status rs_c = G2P_OK, rs = G2P_OK;
+    std::string err_c;
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ac_ready = nullptr;
+    std::thread tc;
+    if (!kprof_on() && cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) == cudaSuccess &&
+        cudaEventCreateWithFlags(&ac_ready, cudaEventDisableTiming) == cudaSuccess) {
+        G2P_CUDA(cudaEventRecord(ac_ready, s));
+        G2P_CUDA(cudaStreamWaitEvent(s2, ac_ready, 0));
+        int dev = 0;
+        G2P_CUDA(cudaGetDevice(&dev));
+        tc = std::thread([&, dev] {
+            cudaSetDevice(dev);
+            rs_c = g2p_solver_build(m->Ac, &pc, s2, &Sc);
+            if (rs_c != G2P_OK) err_c = g2p_last_error();
+        });
+    } else {
+        cudaGetLastError();
+        rs_c = g2p_solver_build(m->Ac, &pc, s, &Sc);
+        if (rs_c != G2P_OK) err_c = g2p_last_error();
+    }
     rs = g2p_v0_finish(m);
     if (rs == G2P_OK) rs = g2p_solver_build(m->Ad, &p, s, &Sd);
-    if (rs != G2P_OK) { g2p_solver_destroy(Sc); return rs; }
+    if (tc.joinable()) tc.join();
+    if (Sc) Sc->stream = s;           // the solves run on the job's stream
+    if (s2) { cudaStreamSynchronize(s2); cudaStreamDestroy(s2); }
+    if (ac_ready) cudaEventDestroy(ac_ready);
+    if (rs_c != G2P_OK || rs != G2P_OK) {
+        if (rs == G2P_OK) set_last_message("%s", err_c.c_str());
+        g2p_solver_destroy(Sc);
+        g2p_solver_destroy(Sd);
+        return rs != G2P_OK ? rs : rs_c;
+    }
     local.setup_ms = ms_since(t0);
     local.ad_levels = Sd->levels;
     local.ac_levels = Sc->levels;
