@@ -1875,6 +1875,320 @@ static g2p_status offsets_of(const int64_t *cnt, int64_t n, int64_t *off, cudaSt
     return G2P_OK;
 }
 
+// ---- Galerkin product A_c = T^T A P, one coarse row per warp: shared-
+// memory hash tables accumulate B = T^T A's row (member rows in ascending
+// order, one row at a time) and then A_c's row (B's entries in ascending
+// column order, one at a time), so every sum is taken in a fixed order.
+// Only the unique columns are sorted.  Rows whose unique columns overflow
+// the table are flagged and built by expand-sort-compress over those rows.
+constexpr int kRapTable = 256;            // hash slots per warp (power of two)
+constexpr int kRapWarps = 4;              // warps per block (24 KB of shared memory)
+struct RapWarpMem {
+    int32_t hkey[kRapTable];
+    double hval[kRapTable];
+    int32_t bcol[kRapTable];
+    double bval[kRapTable];
+    int32_t flag;
+};
+
+template <class F>
+__global__ void k_for_each(int64_t n, F f) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) f(i);
+}
+
+// w1 = entries of a member row, w2 = its products with the rows of P (rows
+// longer than kLongRow: w2 from k_rap_rowcount_long)
+__global__ void k_rap_rowcount(int64_t n, const int64_t *ptr, const int32_t *col, const int32_t *agg,
+                               const int64_t *pptr, int64_t *w1, int64_t *w2) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t a = 0, b = 0;
+        if (agg[i] >= 0) {
+            a = ptr[i + 1] - ptr[i];
+            if (a <= kLongRow)
+                for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) b += pptr[col[q] + 1] - pptr[col[q]];
+        }
+        w1[i] = a;
+        w2[i] = b;
+    }
+}
+__global__ void __launch_bounds__(256) k_rap_rowcount_long(const int32_t *rows, const int64_t *ptr, const int32_t *col,
+                                                           const int32_t *agg, const int64_t *pptr, int64_t *w2) {
+    __shared__ int64_t sm[8];
+    const int64_t i = rows[blockIdx.x];
+    if (agg[i] < 0) return;
+    int64_t b = 0;
+    for (int64_t q = ptr[i] + threadIdx.x; q < ptr[i + 1]; q += blockDim.x) b += pptr[col[q] + 1] - pptr[col[q]];
+    for (int o = 16; o > 0; o >>= 1) b += __shfl_xor_sync(0xffffffffu, b, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sm[w];
+        w2[i] = t;
+    }
+}
+// m1 = member entries, m2 = product count (bounds of B's and A_c's row)
+__global__ void k_rap_aggcount(int64_t nc, const int64_t *rptr, const int32_t *rmem, const int64_t *w1,
+                               const int64_t *w2, int64_t *m1, int64_t *m2) {
+    for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nc; I += (int64_t)gridDim.x * blockDim.x) {
+        int64_t a = 0, b = 0;
+        for (int64_t q = rptr[I]; q < rptr[I + 1]; q++) { a += w1[rmem[q]]; b += w2[rmem[q]]; }
+        m1[I] = a;
+        m2[I] = b;
+    }
+}
+
+// Adds v to key's slot (inserting the key); false when the table is full.
+// The lanes of one call hold distinct keys.
+__device__ __forceinline__ bool rap_add(RapWarpMem &w, int32_t key, double v) {
+    static_assert(kRapTable == 256, "hash shift below assumes 256 slots");
+    uint32_t h = ((uint32_t)key * 2654435761u) >> (32 - 8);
+    for (int probe = 0; probe < kRapTable; probe++) {
+        const uint32_t slot = (h + probe) & (kRapTable - 1);
+        const int32_t old = atomicCAS(&w.hkey[slot], -1, key);
+        if (old == -1 || old == key) {
+            w.hval[slot] += v;
+            return true;
+        }
+    }
+    return false;
+}
+
+// Compacts the table into (bcol, bval) sorted by column; returns the count.
+__device__ int rap_collect(RapWarpMem &w) {
+    const int lane = threadIdx.x & 31;
+    int n = 0;
+    for (int s0 = 0; s0 < kRapTable; s0 += 32) {
+        const int slot = s0 + lane;
+        const bool used = w.hkey[slot] != -1;
+        const unsigned b = __ballot_sync(0xffffffffu, used);
+        if (used) {
+            const int o = n + __popc(b & ((1u << lane) - 1u));
+            w.bcol[o] = w.hkey[slot];
+            w.bval[o] = w.hval[slot];
+        }
+        n += __popc(b);
+    }
+    int np = 1;
+    while (np < n) np <<= 1;
+    for (int t = n + lane; t < np; t += 32) { w.bcol[t] = 0x7fffffff; w.bval[t] = 0; }
+    __syncwarp();
+    for (int kk = 2; kk <= np; kk <<= 1)
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < np; i += 32) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const int32_t a = w.bcol[i], c = w.bcol[ixj];
+                    if ((a > c) == ((i & kk) == 0)) {
+                        w.bcol[i] = c; w.bcol[ixj] = a;
+                        const double t = w.bval[i]; w.bval[i] = w.bval[ixj]; w.bval[ixj] = t;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    return n;
+}
+
+__device__ __forceinline__ void rap_clear(RapWarpMem &w) {
+    const int lane = threadIdx.x & 31;
+    for (int t = lane; t < kRapTable; t += 32) { w.hkey[t] = -1; w.hval[t] = 0; }
+    if (lane == 0) w.flag = 0;
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(32 * kRapWarps) k_rap_hash(int64_t nc, const int64_t *m1, const int64_t *rptr, const int32_t *rmem,
+                                                             const int64_t *aptr, const int32_t *acol,
+                                                             const double *aval, const int64_t *pptr,
+                                                             const int32_t *pcol, const double *pval,
+                                                             const int64_t *off2, int32_t *tcol, double *tval,
+                                                             int64_t *nnz, uint8_t *over) {
+    __shared__ RapWarpMem mem[kRapWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    RapWarpMem &w = mem[warp];
+    for (int64_t I = (int64_t)blockIdx.x * kRapWarps + warp; I < nc; I += (int64_t)gridDim.x * kRapWarps) {
+        // a member row longer than the table cannot fit (its columns are
+        // distinct): such rows (conductor potentials) go to the sort path
+        if (m1[I] > kRapTable) {
+            bool longrow = false;
+            for (int64_t q = rptr[I] + lane; q < rptr[I + 1]; q += 32)
+                longrow |= aptr[rmem[q] + 1] - aptr[rmem[q]] > kRapTable;
+            if (__any_sync(0xffffffffu, longrow)) { if (lane == 0) over[I] = 1; __syncwarp(); continue; }
+        }
+        // ---- B row I: member rows in ascending order, one at a time
+        rap_clear(w);
+        bool ok = true;
+        for (int64_t q = rptr[I]; q < rptr[I + 1] && ok; q++) {
+            const int64_t i = rmem[q], b0 = aptr[i], len = aptr[i + 1] - b0;
+            for (int64_t t0 = 0; t0 < len && ok; t0 += 32) {
+                const int64_t t = t0 + lane;
+                const bool fit = t >= len || rap_add(w, acol[b0 + t], aval[b0 + t]);
+                ok = __all_sync(0xffffffffu, fit);
+            }
+            __syncwarp();
+        }
+        if (!ok) { if (lane == 0) over[I] = 1; __syncwarp(); continue; }
+        const int nb = rap_collect(w);
+        // ---- A_c row I: B's entries in ascending column order, one at a time
+        for (int t = lane; t < kRapTable; t += 32) { w.hkey[t] = -1; w.hval[t] = 0; }
+        __syncwarp();
+        for (int r = 0; r < nb && ok; r++) {
+            const int64_t j = w.bcol[r], pb = pptr[j], pl = pptr[j + 1] - pb;
+            const double bv = w.bval[r];
+            for (int64_t t0 = 0; t0 < pl && ok; t0 += 32) {
+                const int64_t t = t0 + lane;
+                const bool fit = t >= pl || rap_add(w, pcol[pb + t], bv * pval[pb + t]);
+                ok = __all_sync(0xffffffffu, fit);
+            }
+            __syncwarp();
+        }
+        if (!ok) { if (lane == 0) over[I] = 1; __syncwarp(); continue; }
+        const int nout = rap_collect(w);
+        const int64_t o = off2[I];
+        for (int t = lane; t < nout; t += 32) { tcol[o + t] = w.bcol[t]; tval[o + t] = w.bval[t]; }
+        if (lane == 0) { nnz[I] = nout; over[I] = 0; }
+        __syncwarp();
+    }
+}
+
+// Expansion of T^T A for the listed aggregates: keys h * n + column in
+// member-then-entry order, one block per aggregate.
+__global__ void __launch_bounds__(256) k_rap_expand_list(const int64_t *list, const int64_t *off, const int64_t *rptr,
+                                                         const int32_t *rmem, const int64_t *aptr, const int32_t *acol,
+                                                         const double *aval, uint64_t n, uint64_t *keys, double *vals) {
+    const int64_t h = blockIdx.x, I = list[h];
+    int64_t o = off[h];
+    for (int64_t q = rptr[I]; q < rptr[I + 1]; q++) {
+        const int64_t i = rmem[q], b0 = aptr[i], len = aptr[i + 1] - b0;
+        for (int64_t t = threadIdx.x; t < len; t += blockDim.x) {
+            keys[o + t] = (uint64_t)h * n + (uint64_t)acol[b0 + t];
+            vals[o + t] = aval[b0 + t];
+        }
+        o += len;
+    }
+}
+// Row h of the listed aggregates' product to its place among the coarse rows.
+__global__ void k_rap_place(int64_t nh, const int64_t *list, const int64_t *cptr, const int32_t *ccol,
+                            const double *cval, const int64_t *off2, int32_t *tcol, double *tval, int64_t *nnz) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    for (int64_t h = w; h < nh; h += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const int64_t I = list[h], b = cptr[h], len = cptr[h + 1] - b, o = off2[I];
+        for (int64_t t = lane; t < len; t += 32) { tcol[o + t] = ccol[b + t]; tval[o + t] = cval[b + t]; }
+        if (lane == 0) nnz[I] = len;
+    }
+}
+__global__ void k_rap_compact(int64_t nc, const int64_t *off2, const int64_t *ptr, const int32_t *tcol,
+                              const double *tval, int32_t *col, double *val) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    for (int64_t I = w; I < nc; I += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const int64_t src = off2[I], dst = ptr[I], len = ptr[I + 1] - dst;
+        for (int64_t t = lane; t < len; t += 32) { col[dst + t] = tcol[src + t]; val[dst + t] = tval[src + t]; }
+    }
+}
+
+// Indices I with flag[I] != 0, ascending; returns their count.
+static g2p_status list_flagged(const uint8_t *flag, int64_t n, cudaStream_t s, int64_t **list, int64_t *count) {
+    int64_t *pos, *work;
+    G2P_TRY(dalloc(&pos, n + 1, s));
+    G2P_TRY(dalloc(&work, scan_work_size(n + 1) + 4, s));
+    auto op = [flag, n] __device__(int64_t i) -> int64_t { return i < n ? (flag[i] ? 1 : 0) : 0; };
+    G2P_TRY(exclusive_scan(op, n + 1, pos, work, s));
+    G2P_CUDA(cudaMemcpyAsync(count, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    G2P_TRY(dalloc(list, std::max<int64_t>(*count, 1), s));
+    int64_t *lp = *list;
+    const int64_t *pp = pos;
+    auto put = [flag, pp, lp] __device__(int64_t i) { if (flag[i]) lp[pp[i]] = i; };
+    (g2p::kbegin("k_list_flagged", s), k_for_each<<<grid_for(n), kThreads, 0, s>>>(n, put), g2p::kend(s));
+    dfree(pos, s); dfree(work, s);
+    return G2P_OK;
+}
+
+// A_c = T^T A P: per coarse row in shared memory, and by expand-sort-
+// compress over the rows whose unique columns overflow the table.
+static g2p_status rap_rows(const Level<double> &L, int64_t n, int64_t nc, cudaStream_t s, Csr<double> &out) {
+    int64_t *w1, *w2, *m1, *m2;
+    G2P_TRY(dalloc(&w1, n, s)); G2P_TRY(dalloc(&w2, n, s));
+    G2P_TRY(dalloc(&m1, nc, s)); G2P_TRY(dalloc(&m2, nc, s));
+    (g2p::kbegin("k_rap_rowcount", s), k_rap_rowcount<<<grid_for(n), kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.agg, L.P.ptr, w1, w2), g2p::kend(s));
+    if (L.lr.n > 0)
+        (g2p::kbegin("k_rap_rowcount_long", s), k_rap_rowcount_long<<<(unsigned)L.lr.n, 256, 0, s>>>(L.lr.rows, L.A.ptr, L.A.col, L.agg, L.P.ptr, w2), g2p::kend(s));
+    (g2p::kbegin("k_rap_aggcount", s), k_rap_aggcount<<<grid_for(nc), kThreads, 0, s>>>(nc, L.rptr, L.rmem, w1, w2, m1, m2), g2p::kend(s));
+    dfree(w1, s); dfree(w2, s);
+    int64_t *off2, ne2 = 0;
+    G2P_TRY(dalloc(&off2, nc + 1, s));
+    G2P_TRY(offsets_of(m2, nc, off2, s, &ne2));
+    dfree(m2, s);
+    int32_t *tcol;
+    double *tval;
+    int64_t *nnzr;
+    uint8_t *over;
+    G2P_TRY(dalloc(&tcol, std::max<int64_t>(ne2, 1), s)); G2P_TRY(dalloc(&tval, std::max<int64_t>(ne2, 1), s));
+    G2P_TRY(dalloc(&nnzr, nc, s)); G2P_TRY(dalloc(&over, nc, s));
+    {
+        const int64_t g = std::min<int64_t>((nc + kRapWarps - 1) / kRapWarps, (int64_t)kSMs * 64);
+        (g2p::kbegin("k_rap_hash", s), k_rap_hash<<<(unsigned)std::max<int64_t>(g, 1), 32 * kRapWarps, 0, s>>>(
+             nc, m1, L.rptr, L.rmem, L.A.ptr, L.A.col, L.A.val, L.P.ptr, L.P.col, L.P.val, off2, tcol, tval, nnzr, over),
+         g2p::kend(s));
+    }
+    int64_t *hl, nh = 0;
+    G2P_TRY(list_flagged(over, nc, s, &hl, &nh));
+    dfree(over, s);
+    if (nh > 0) {
+        // B_h = T^T A over the flagged aggregates (rows renumbered 0..nh-1)
+        int64_t *cnt, *off1, ne1 = 0;
+        G2P_TRY(dalloc(&cnt, nh, s)); G2P_TRY(dalloc(&off1, nh + 1, s));
+        const int64_t *hp = hl, *m1p = m1;
+        int64_t *cp = cnt;
+        auto gcnt = [hp, m1p, cp] __device__(int64_t h) { cp[h] = m1p[hp[h]]; };
+        (g2p::kbegin("k_rap_hcount", s), k_for_each<<<grid_for(nh), kThreads, 0, s>>>(nh, gcnt), g2p::kend(s));
+        G2P_TRY(offsets_of(cnt, nh, off1, s, &ne1));
+        dfree(cnt, s);
+        uint64_t *ek0;
+        double *ev0;
+        G2P_TRY(dalloc(&ek0, std::max<int64_t>(ne1, 1), s)); G2P_TRY(dalloc(&ev0, std::max<int64_t>(ne1, 1), s));
+        (g2p::kbegin("k_rap_expand_list", s), k_rap_expand_list<<<(unsigned)nh, 256, 0, s>>>(hl, off1, L.rptr, L.rmem, L.A.ptr, L.A.col, L.A.val, (uint64_t)n, ek0, ev0), g2p::kend(s));
+        dfree(off1, s);
+        Csr<double> B;
+        G2P_TRY(esc_to_csr(ek0, ev0, ne1, nh, n, s, B));
+        // C_h = B_h P
+        int64_t *off, ne = 0;
+        G2P_TRY(dalloc(&off, B.nnz + 1, s));
+        {
+            int64_t *wk;
+            G2P_TRY(dalloc(&wk, scan_work_size(B.nnz + 1) + 4, s));
+            const int32_t *bc = B.col;
+            const int64_t *pp = L.P.ptr;
+            int64_t nb = B.nnz;
+            auto pop = [bc, pp, nb] __device__(int64_t q) -> int64_t { return q < nb ? pp[bc[q] + 1] - pp[bc[q]] : 0; };
+            G2P_TRY(exclusive_scan(pop, nb + 1, off, wk, s));
+            G2P_CUDA(cudaMemcpyAsync(&ne, off + nb, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+            G2P_CUDA(cudaStreamSynchronize(s));
+            dfree(wk, s);
+        }
+        G2P_TRY(dalloc(&ek0, std::max<int64_t>(ne, 1), s)); G2P_TRY(dalloc(&ev0, std::max<int64_t>(ne, 1), s));
+        (g2p::kbegin("k_bp_expand", s), k_bp_expand<<<grid_for(B.nnz), kThreads, 0, s>>>(nh, B.nnz, B.ptr, B.col, B.val, L.P.ptr, L.P.col, L.P.val, off, (uint64_t)nc, ek0, ev0), g2p::kend(s));
+        dfree(off, s);
+        B.release(s);
+        Csr<double> Ch;
+        G2P_TRY(esc_to_csr(ek0, ev0, ne, nh, nc, s, Ch));
+        (g2p::kbegin("k_rap_place", s), k_rap_place<<<grid_for(nh * 32), kThreads, 0, s>>>(nh, hl, Ch.ptr, Ch.col, Ch.val, off2, tcol, tval, nnzr), g2p::kend(s));
+        Ch.release(s);
+    }
+    dfree(hl, s); dfree(m1, s);
+    out.n = nc; out.m = nc;
+    G2P_TRY(dalloc(&out.ptr, nc + 1, s));
+    int64_t nnz = 0;
+    G2P_TRY(offsets_of(nnzr, nc, out.ptr, s, &nnz));
+    out.nnz = nnz;
+    G2P_TRY(dalloc(&out.col, std::max<int64_t>(nnz, 1), s)); G2P_TRY(dalloc(&out.val, std::max<int64_t>(nnz, 1), s));
+    (g2p::kbegin("k_rap_compact", s), k_rap_compact<<<grid_for(nc * 32), kThreads, 0, s>>>(nc, off2, out.ptr, tcol, tval, out.col, out.val), g2p::kend(s));
+    dfree(off2, s); dfree(tcol, s); dfree(tval, s); dfree(nnzr, s);
+    return G2P_OK;
+}
+
 // Host wall time of setup phases, printed with G2P_DEBUG >= 2 (synchronizes).
 struct PhaseClock {
     bool on = false;
@@ -2024,41 +2338,48 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 G2P_TRY(dalloc(&L.P.col, pnnz, s)); G2P_TRY(dalloc(&L.P.val, pnnz, s));
                 (g2p::kbegin("k_ps_fill", s), k_ps_fill<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.A.col, L.A.val, diag, L.agg, w, L.P.ptr, L.P.col, L.P.val), g2p::kend(s));
                 pc_.mark("prolongation", l, s);
-                // ---- B = T^T A (nc x n)
-                int64_t *cnt, *off;
-                G2P_TRY(dalloc(&cnt, n + 1, s)); G2P_TRY(dalloc(&off, n + 1, s));
-                (g2p::kbegin("k_ta_count", s), k_ta_count<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.agg, cnt), g2p::kend(s));
-                int64_t ne = 0;
-                G2P_TRY(offsets_of(cnt, n, off, s, &ne));
-                uint64_t *ek0;
-                double *ev0;
-                G2P_TRY(dalloc(&ek0, ne, s)); G2P_TRY(dalloc(&ev0, ne, s));
-                (g2p::kbegin("k_ta_expand", s), k_ta_expand<<<grid_for(L.A.nnz), kThreads, 0, s>>>(n, L.A.nnz, L.A.ptr, L.A.col, L.A.val, L.agg, off, (uint64_t)n, ek0, ev0), g2p::kend(s));
-                dfree(cnt, s); dfree(off, s);
-                Csr<double> B;
-                G2P_TRY(esc_to_csr(ek0, ev0, ne, nc, n, s, B));
-                pc_.mark("T^T A", l, s);
-                // ---- A_c = B P (nc x nc), entry-parallel over B
-                G2P_TRY(dalloc(&off, B.nnz + 1, s));
-                {
-                    int64_t *wk;
-                    G2P_TRY(dalloc(&wk, scan_work_size(B.nnz + 1) + 4, s));
-                    const int32_t *bc = B.col;
-                    const int64_t *pp = L.P.ptr;
-                    int64_t nb = B.nnz;
-                    auto pop = [bc, pp, nb] __device__(int64_t q) -> int64_t { return q < nb ? pp[bc[q] + 1] - pp[bc[q]] : 0; };
-                    G2P_TRY(exclusive_scan(pop, nb + 1, off, wk, s));
-                    G2P_CUDA(cudaMemcpyAsync(&ne, off + nb, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-                    G2P_CUDA(cudaStreamSynchronize(s));
-                    dfree(wk, s);
-                }
-                G2P_TRY(dalloc(&ek0, ne, s)); G2P_TRY(dalloc(&ev0, ne, s));
-                (g2p::kbegin("k_bp_expand", s), k_bp_expand<<<grid_for(B.nnz), kThreads, 0, s>>>(nc, B.nnz, B.ptr, B.col, B.val, L.P.ptr, L.P.col, L.P.val, off, (uint64_t)nc, ek0, ev0), g2p::kend(s));
-                dfree(off, s);
-                B.release(s);
+                // ---- A_c = T^T A P: per coarse row in shared memory, or
+                // (G2P_RAP_ESC=1, for comparisons) by expand-sort-compress over
+                // all rows
                 Level<double> C;
                 C.n = nc;
-                G2P_TRY(esc_to_csr(ek0, ev0, ne, nc, nc, s, C.A));
+                if (!getenv("G2P_RAP_ESC")) {
+                    G2P_TRY(rap_rows(L, n, nc, s, C.A));
+                } else {
+                    // ---- B = T^T A (nc x n)
+                    int64_t *cnt, *off;
+                    G2P_TRY(dalloc(&cnt, n + 1, s)); G2P_TRY(dalloc(&off, n + 1, s));
+                    (g2p::kbegin("k_ta_count", s), k_ta_count<<<g, kThreads, 0, s>>>(n, L.A.ptr, L.agg, cnt), g2p::kend(s));
+                    int64_t ne = 0;
+                    G2P_TRY(offsets_of(cnt, n, off, s, &ne));
+                    uint64_t *ek0;
+                    double *ev0;
+                    G2P_TRY(dalloc(&ek0, ne, s)); G2P_TRY(dalloc(&ev0, ne, s));
+                    (g2p::kbegin("k_ta_expand", s), k_ta_expand<<<grid_for(L.A.nnz), kThreads, 0, s>>>(n, L.A.nnz, L.A.ptr, L.A.col, L.A.val, L.agg, off, (uint64_t)n, ek0, ev0), g2p::kend(s));
+                    dfree(cnt, s); dfree(off, s);
+                    Csr<double> B;
+                    G2P_TRY(esc_to_csr(ek0, ev0, ne, nc, n, s, B));
+                    pc_.mark("T^T A", l, s);
+                    // ---- A_c = B P (nc x nc), entry-parallel over B
+                    G2P_TRY(dalloc(&off, B.nnz + 1, s));
+                    {
+                        int64_t *wk;
+                        G2P_TRY(dalloc(&wk, scan_work_size(B.nnz + 1) + 4, s));
+                        const int32_t *bc = B.col;
+                        const int64_t *pp = L.P.ptr;
+                        int64_t nb = B.nnz;
+                        auto pop = [bc, pp, nb] __device__(int64_t q) -> int64_t { return q < nb ? pp[bc[q] + 1] - pp[bc[q]] : 0; };
+                        G2P_TRY(exclusive_scan(pop, nb + 1, off, wk, s));
+                        G2P_CUDA(cudaMemcpyAsync(&ne, off + nb, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+                        G2P_CUDA(cudaStreamSynchronize(s));
+                        dfree(wk, s);
+                    }
+                    G2P_TRY(dalloc(&ek0, ne, s)); G2P_TRY(dalloc(&ev0, ne, s));
+                    (g2p::kbegin("k_bp_expand", s), k_bp_expand<<<grid_for(B.nnz), kThreads, 0, s>>>(nc, B.nnz, B.ptr, B.col, B.val, L.P.ptr, L.P.col, L.P.val, off, (uint64_t)nc, ek0, ev0), g2p::kend(s));
+                    dfree(off, s);
+                    B.release(s);
+                    G2P_TRY(esc_to_csr(ek0, ev0, ne, nc, nc, s, C.A));
+                }
                 L.nc = nc;
                 H.lv.push_back(C);
                 pc_.mark("galerkin", l, s);

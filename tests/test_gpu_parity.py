@@ -134,3 +134,24 @@ def test_gpu_autotune_picks_a_candidate_and_keeps_it(g2p):
     assert np.array_equal(res[1][0], res[2][0])
     err = np.abs(res[1][0] - res[0][0]).max() / np.abs(res[0][0]).max()
     assert err < 1e-7, err
+
+
+@pytest.mark.parametrize("name,precision", [("strip_c1", "mixed"), ("manhattan_sweep", "fp64"), ("multistrip_small", "mixed")])
+def test_gpu_galerkin_hash_path_matches_sort_path(name, precision, g2p, monkeypatch):
+    """The per-row shared-memory Galerkin product sums in the same member and
+    column order as the global expand-sort-compress product (sums of more
+    than 32 terms excepted), and it is deterministic: Z agrees to solver
+    tolerance and repeats bit for bit."""
+    d, A, M = golden_layout(name)
+    out = []
+    for esc in (False, False, True):
+        if esc:
+            monkeypatch.setenv("G2P_RAP_ESC", "1")
+        else:
+            monkeypatch.delenv("G2P_RAP_ESC", raising=False)
+        with g2p.FdtdMesh(d) as m:
+            g2p.generateStiff(m)
+            Z, st = g2p.paraGenerator(m, g2p.default_params(precision=precision, rtol=1e-10))
+        out.append(Z)
+    assert np.array_equal(out[0], out[1])
+    assert np.abs(out[0] - out[2]).max() / np.abs(out[2]).max() < 1e-8
