@@ -388,19 +388,26 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         G2P_CUDA(cudaStreamWaitEvent(s2, ac_ready, 0));
         int dev = 0;
         G2P_CUDA(cudaGetDevice(&dev));
-        tc = std::thread([&, dev] {
-            cudaSetDevice(dev);
-            rs_c = g2p_solver_build(m->Ac, &pc, s2, &Sc);
-            if (rs_c != G2P_OK) err_c = g2p_last_error();
-        });
+        try {
+            tc = std::thread([&, dev] {
+                cudaSetDevice(dev);
+                rs_c = g2p_solver_build(m->Ac, &pc, s2, &Sc);
+                if (rs_c != G2P_OK) err_c = g2p_last_error();
+            });
+        } catch (const std::exception &) {
+            // no thread to be had: build Ac's solver here, after Ad's
+        }
     } else {
         cudaGetLastError();
-        rs_c = g2p_solver_build(m->Ac, &pc, s, &Sc);
-        if (rs_c != G2P_OK) err_c = g2p_last_error();
     }
+    const bool ac_here = !tc.joinable();
     rs = g2p_v0_finish(m);
     if (rs == G2P_OK) rs = g2p_solver_build(m->Ad, &p, s, &Sd);
     if (tc.joinable()) tc.join();
+    if (ac_here && rs == G2P_OK) {
+        rs_c = g2p_solver_build(m->Ac, &pc, s, &Sc);
+        if (rs_c != G2P_OK) err_c = g2p_last_error();
+    }
     if (Sc) Sc->stream = s;           // the solves run on the job's stream
     if (s2) { cudaStreamSynchronize(s2); cudaStreamDestroy(s2); }
     if (ac_ready) cudaEventDestroy(ac_ready);
