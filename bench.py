@@ -177,7 +177,10 @@ def run_gb300(args):
     # c5: the port blocks that fit 280 GB of HBM (4 ports: about 175 GiB)
     big = args.config == "c5"
     batch = (args.batch if args.batch > 1 else 4) if big else args.batch
-    params = default_params(precision=args.precision, batch=batch, rtol=RTOL[args.config], autotune=0 if big else 1)
+    # --once (profiler captures) runs one step without the autotuner's trial
+    # solves; c2's tuned choice is the untuned one (all ports, degree 2)
+    params = default_params(precision=args.precision, batch=batch, rtol=RTOL[args.config],
+                            autotune=0 if (big or args.once) else 1)
     dev = make_desc(d, "cuda", torch)
     pin = make_desc(d, "pinned", torch)
     z =torch.zeros(2 * d.nfreq * d.num_ports * d.num_ports, dtype=torch.float64).pin_memory()
