@@ -2067,25 +2067,31 @@ __global__ void __launch_bounds__(256) k_rap_expand_list(const int64_t *list, co
         o += len;
     }
 }
-// Row h of the listed aggregates' product to its place among the coarse rows.
-__global__ void k_rap_place(int64_t nh, const int64_t *list, const int64_t *cptr, const int32_t *ccol,
-                            const double *cval, const int64_t *off2, int32_t *tcol, double *tval, int64_t *nnz) {
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    for (int64_t h = w; h < nh; h += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-        const int64_t I = list[h], b = cptr[h], len = cptr[h + 1] - b, o = off2[I];
-        for (int64_t t = lane; t < len; t += 32) { tcol[o + t] = ccol[b + t]; tval[o + t] = cval[b + t]; }
-        if (lane == 0) nnz[I] = len;
-    }
+// Row h of the listed aggregates' product to its place among the coarse
+// rows, one block per row (these rows are the long ones).
+__global__ void k_rap_place(const int64_t *list, const int64_t *cptr, const int32_t *ccol, const double *cval,
+                            const int64_t *off2, int32_t *tcol, double *tval, int64_t *nnz) {
+    const int64_t h = blockIdx.x, I = list[h], b = cptr[h], len = cptr[h + 1] - b, o = off2[I];
+    for (int64_t t = threadIdx.x; t < len; t += blockDim.x) { tcol[o + t] = ccol[b + t]; tval[o + t] = cval[b + t]; }
+    if (threadIdx.x == 0) nnz[I] = len;
 }
+// Coarse rows to their final places: one warp per row of at most kRapTable
+// entries (the table's rows); longer rows by k_rap_compact_list.
 __global__ void k_rap_compact(int64_t nc, const int64_t *off2, const int64_t *ptr, const int32_t *tcol,
                               const double *tval, int32_t *col, double *val) {
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     for (int64_t I = w; I < nc; I += ((int64_t)gridDim.x * blockDim.x) >> 5) {
         const int64_t src = off2[I], dst = ptr[I], len = ptr[I + 1] - dst;
+        if (len > kRapTable) continue;
         for (int64_t t = lane; t < len; t += 32) { col[dst + t] = tcol[src + t]; val[dst + t] = tval[src + t]; }
     }
+}
+__global__ void k_rap_compact_list(const int64_t *list, const int64_t *off2, const int64_t *ptr, const int32_t *tcol,
+                                   const double *tval, int32_t *col, double *val) {
+    const int64_t I = list[blockIdx.x], src = off2[I], dst = ptr[I], len = ptr[I + 1] - dst;
+    if (len <= kRapTable) return;
+    for (int64_t t = threadIdx.x; t < len; t += blockDim.x) { col[dst + t] = tcol[src + t]; val[dst + t] = tval[src + t]; }
 }
 
 // Indices I with flag[I] != 0, ascending; returns their count.
@@ -2174,10 +2180,10 @@ static g2p_status rap_rows(const Level<double> &L, int64_t n, int64_t nc, cudaSt
         B.release(s);
         Csr<double> Ch;
         G2P_TRY(esc_to_csr(ek0, ev0, ne, nh, nc, s, Ch));
-        (g2p::kbegin("k_rap_place", s), k_rap_place<<<grid_for(nh * 32), kThreads, 0, s>>>(nh, hl, Ch.ptr, Ch.col, Ch.val, off2, tcol, tval, nnzr), g2p::kend(s));
+        (g2p::kbegin("k_rap_place", s), k_rap_place<<<(unsigned)nh, 256, 0, s>>>(hl, Ch.ptr, Ch.col, Ch.val, off2, tcol, tval, nnzr), g2p::kend(s));
         Ch.release(s);
     }
-    dfree(hl, s); dfree(m1, s);
+    dfree(m1, s);
     out.n = nc; out.m = nc;
     G2P_TRY(dalloc(&out.ptr, nc + 1, s));
     int64_t nnz = 0;
@@ -2185,6 +2191,10 @@ static g2p_status rap_rows(const Level<double> &L, int64_t n, int64_t nc, cudaSt
     out.nnz = nnz;
     G2P_TRY(dalloc(&out.col, std::max<int64_t>(nnz, 1), s)); G2P_TRY(dalloc(&out.val, std::max<int64_t>(nnz, 1), s));
     (g2p::kbegin("k_rap_compact", s), k_rap_compact<<<grid_for(nc * 32), kThreads, 0, s>>>(nc, off2, out.ptr, tcol, tval, out.col, out.val), g2p::kend(s));
+    // rows longer than the table come only from the flagged aggregates
+    if (nh > 0)
+        (g2p::kbegin("k_rap_compact_list", s), k_rap_compact_list<<<(unsigned)nh, 256, 0, s>>>(hl, off2, out.ptr, tcol, tval, out.col, out.val), g2p::kend(s));
+    dfree(hl, s);
     dfree(off2, s); dfree(tcol, s); dfree(tval, s); dfree(nnzr, s);
     return G2P_OK;
 }
