@@ -409,23 +409,35 @@ __global__ void __launch_bounds__(256) k_spmm_long(const int32_t *__restrict__ r
     const int l = crow[blockIdx.x];
     const int64_t row = rows[l];
     const int64_t q0 = cbeg[blockIdx.x], q1 = min(q0 + (int64_t)kLongChunk, ptr[row + 1]);
-    T acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;
+    // eight independent gathers in flight per thread
+    T a[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) a[u] = 0;
     if (r < k) {
         int64_t q = q0 + ty;
-        for (; q + 3 * ny < q1; q += 4 * ny) {
-            const int32_t c0 = col[q], c1 = col[q + ny], c2 = col[q + 2 * ny], c3 = col[q + 3 * ny];
-            const T v0 = val[q], v1 = val[q + ny], v2 = val[q + 2 * ny], v3 = val[q + 3 * ny];
-            const T x0 = x[(int64_t)c0 * k + r], x1 = x[(int64_t)c1 * k + r];
-            const T x2 = x[(int64_t)c2 * k + r], x3 = x[(int64_t)c3 * k + r];
-            acc0 += v0 * x0; acc1 += v1 * x1; acc2 += v2 * x2; acc3 += v3 * x3;
+        for (; q + 7 * ny < q1; q += 8 * ny) {
+            int32_t c[8];
+            T v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) { c[u] = col[q + u * ny]; v[u] = val[q + u * ny]; }
+#pragma unroll
+            for (int u = 0; u < 8; u++) a[u] += v[u] * x[(int64_t)c[u] * k + r];
         }
-        for (; q < q1; q += ny) acc0 += val[q] * x[(int64_t)col[q] * k + r];
+        for (; q < q1; q += ny) a[0] += val[q] * x[(int64_t)col[q] * k + r];
     }
-    sm[ty * blockDim.x + r] = (double)((acc0 + acc1) + (acc2 + acc3));
+    // the block's entry lanes (threadIdx.y) combine in a fixed tree: xor
+    // shuffles inside a warp, then the warps' sums in order (an FP64 chain
+    // over all lanes costs microseconds on this part)
+    const int tid = ty * blockDim.x + r, lane = tid & 31, wi = tid >> 5, kxb = blockDim.x;
+    double v = (double)(((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7])));
+    for (int off = kxb; off < 32; off <<= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    const int nw = (int)((blockDim.x * blockDim.y + 31) >> 5);
+    const int slots = kxb < 32 ? nw : ny;                   // warps, or rows of the block when kxb >= 32
+    if (kxb < 32 ? lane < kxb : true) sm[(kxb < 32 ? wi : ty) * kxb + r] = v;
     __syncthreads();
     if (ty == 0 && r < k) {
         double s = 0;
-        for (int t = 0; t < ny; t++) s += sm[t * blockDim.x + r];
+        for (int t = 0; t < slots; t++) s += sm[t * kxb + r];
         partial[(int64_t)blockIdx.x * kMaxRhs + r] = s;
     }
     __threadfence();
@@ -439,15 +451,16 @@ __global__ void __launch_bounds__(256) k_spmm_long(const int32_t *__restrict__ r
     if (!last) return;
     __threadfence();
     // the row's chunk partials: thread ty adds chunks ty, ty + ny, ... in
-    // order, then thread 0 of each column adds the ny sums in order
+    // order, then the same fixed tree as above over the entry lanes
     double s = 0;
     if (r < k)
         for (int64_t c = rcp[l] + ty; c < rcp[l + 1]; c += ny) s += __ldcg(partial + c * kMaxRhs + r);
-    sm[ty * blockDim.x + r] = s;
+    for (int off = kxb; off < 32; off <<= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (kxb < 32 ? lane < kxb : true) sm[(kxb < 32 ? wi : ty) * kxb + r] = s;
     __syncthreads();
     if (ty != 0 || r >= k) return;
     double t = 0;
-    for (int q = 0; q < ny; q++) t += sm[q * blockDim.x + r];
+    for (int q = 0; q < slots; q++) t += sm[q * kxb + r];
     const int64_t o = row * k + r;
     y[o] = b ? (T)((double)b[o] - t) : (T)t;
 }
@@ -461,32 +474,43 @@ __global__ void __launch_bounds__(256) k_spmm_mid(int64_t nmid, const int32_t *_
                                                   const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
                                                   const T *__restrict__ val, const T *__restrict__ x, int k, int kx,
                                                   T *__restrict__ y, const T *__restrict__ b) {
-    const int lane = threadIdx.x & 31;
-    const int r = lane % kx, e = lane / kx, ey = 32 / kx;
-    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (w >= nmid) return;
-    const int64_t row = mid[w];
+    // one block per row: thread (e, r) with r = tid % kx the right-hand side
+    // and e = tid / kx one of 256 / kx entry lanes; entry lanes combine by a
+    // fixed xor tree inside each warp, then the warps' sums in warp order
+    __shared__ T wsum[8][32];
+    const int tid = threadIdx.x, lane = tid & 31, wi = tid >> 5;
+    const int r = tid % kx, e = tid / kx, ey = 256 / kx;
+    const int64_t row = mid[blockIdx.x];
     const int64_t q0 = ptr[row], q1 = ptr[row + 1];
     for (int r0 = 0; r0 < k; r0 += kx) {
         const int rr = r0 + r;
         const bool on = rr < k;
-        T a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        T a[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) a[u] = 0;
         if (on) {
             int64_t q = q0 + e;
-            for (; q + 3 * ey < q1; q += 4 * ey) {
-                const int32_t c0 = col[q], c1 = col[q + ey], c2 = col[q + 2 * ey], c3 = col[q + 3 * ey];
-                const T v0 = val[q], v1 = val[q + ey], v2 = val[q + 2 * ey], v3 = val[q + 3 * ey];
-                a0 += v0 * x[(int64_t)c0 * k + rr]; a1 += v1 * x[(int64_t)c1 * k + rr];
-                a2 += v2 * x[(int64_t)c2 * k + rr]; a3 += v3 * x[(int64_t)c3 * k + rr];
+            for (; q + 7 * ey < q1; q += 8 * ey) {
+                int32_t c[8];
+                T v[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) { c[u] = col[q + u * ey]; v[u] = val[q + u * ey]; }
+#pragma unroll
+                for (int u = 0; u < 8; u++) a[u] += v[u] * x[(int64_t)c[u] * k + rr];
             }
-            for (; q < q1; q += ey) a0 += val[q] * x[(int64_t)col[q] * k + rr];
+            for (; q < q1; q += ey) a[0] += val[q] * x[(int64_t)col[q] * k + rr];
         }
-        T acc = (a0 + a1) + (a2 + a3);
-        for (int off = kx; off < 32; off <<= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-        if (e == 0 && on) {
+        T acc = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+        for (int off = kx; off < 32; off <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        if (lane < kx) wsum[wi][lane] = acc;
+        __syncthreads();
+        if (tid < kx && on) {
+            T t = 0;
+            for (int w = 0; w < 8; w++) t += wsum[w][tid];
             const int64_t o = row * k + rr;
-            y[o] = b ? b[o] - acc : acc;
+            y[o] = b ? b[o] - t : t;
         }
+        __syncthreads();
     }
 }
 
@@ -667,9 +691,8 @@ void spmm_b(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, const 
     if (prof) prof_event(s);
     if (lr.nmid > 0) {
         const int kx = k >= 32 ? 32 : pow2_ge(k);
-        const int64_t blocks = (lr.nmid + 7) / 8;
         (g2p::kbegin(spmm_name(3, sizeof(T) == 8, A.n), s),
-         k_spmm_mid<T><<<(unsigned)blocks, 256, 0, s>>>(lr.nmid, lr.mid, A.ptr, A.col, A.val, x, k, kx, y, b), g2p::kend(s));
+         k_spmm_mid<T><<<(unsigned)lr.nmid, 256, 0, s>>>(lr.nmid, lr.mid, A.ptr, A.col, A.val, x, k, kx, y, b), g2p::kend(s));
     }
     if (lr.nchunk > 0) {
         (g2p::kbegin(A.n >= (1 << 20) ? (sizeof(T) == 8 ? "k_spmm_long<f64,fine>" : "k_spmm_long<f32,fine>")
