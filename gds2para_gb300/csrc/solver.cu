@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(256) k_spmm_sell(int64_t n, const int64_t *__r
 // c + 1 memory round trips instead of 2 c.  Same summation order as
 // k_spmm_sell with ES = 1.
 template <class T, int V>
-__global__ void __launch_bounds__(256) k_spmm_sell_pipe(int64_t n, const int64_t *__restrict__ sptr,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_spmm_sell_pipe(int64_t n, const int64_t *__restrict__ sptr,
                                                         const int32_t *__restrict__ scol, const T *__restrict__ sval,
                                                         const uint8_t *__restrict__ rlen, const T *__restrict__ x,
                                                         T *__restrict__ y, int k, const T *__restrict__ b, bool accum) {
