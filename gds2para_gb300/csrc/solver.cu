@@ -1725,6 +1725,73 @@ __global__ void __launch_bounds__(256) k_gj_step(const double *__restrict__ a_in
     }
 }
 
+// All n pivot steps of k_gj_step in one cooperative launch (one block per
+// row, every block resident): the same per-step arithmetic, with a grid-wide
+// barrier between steps instead of a launch.  Buffers ping-pong as in the
+// per-step loop; the inverse ends in inv1 when n is odd, inv0 otherwise.
+// flags[0] is the singular flag, flags[1] the barrier's arrival count and
+// flags[2] set when a block gave up waiting (bounded spin), in which case the
+// caller recomputes with one launch per pivot.
+constexpr int kGjSpinLimit = 1 << 22;
+__global__ void __launch_bounds__(256) k_gj_coop(double *a0, double *inv0, double *a1, double *inv1, int64_t n,
+                                                 int *flags) {
+    __shared__ double bv[256];
+    __shared__ int64_t bi[256];
+    __shared__ int quit;
+    const int t = threadIdx.x;
+    const int64_t i = blockIdx.x;
+    unsigned *arrived = reinterpret_cast<unsigned *>(flags + 1);
+    volatile int *abandon = flags + 2;
+    for (int64_t kk = 0; kk < n; kk++) {
+        const double *a_in = (kk & 1) ? a1 : a0, *inv_in = (kk & 1) ? inv1 : inv0;
+        double *a_out = (kk & 1) ? a0 : a1, *inv_out = (kk & 1) ? inv0 : inv1;
+        double mv = -1.0;
+        int64_t mi = n;
+        for (int64_t r = kk + t; r < n; r += blockDim.x) {
+            const double v = fabs(a_in[r * n + kk]);
+            if (v > mv) { mv = v; mi = r; }
+        }
+        bv[t] = mv; bi[t] = mi;
+        __syncthreads();
+        for (int o = 128; o > 0; o >>= 1) {
+            if (t < o && (bv[t + o] > bv[t] || (bv[t + o] == bv[t] && bi[t + o] < bi[t]))) { bv[t] = bv[t + o]; bi[t] = bi[t + o]; }
+            __syncthreads();
+        }
+        const int64_t p = bi[0];
+        double pval = a_in[p * n + kk];
+        if (pval == 0.0) {
+            if (i == 0 && t == 0) flags[0] = 1;
+            pval = 1e-300;
+        }
+        const int64_t src = i == kk ? p : (i == p ? kk : i);
+        const double f = i == kk ? 0.0 : a_in[src * n + kk];
+        for (int64_t c = kk + 1 + t; c < n; c += blockDim.x) {
+            const double pr = a_in[p * n + c] / pval;
+            a_out[i * n + c] = i == kk ? pr : a_in[src * n + c] - f * pr;
+        }
+        for (int64_t c = t; c < n; c += blockDim.x) {
+            const double pr = inv_in[p * n + c] / pval;
+            inv_out[i * n + c] = i == kk ? pr : inv_in[src * n + c] - f * pr;
+        }
+        // grid barrier: every block's writes of step kk before any read of step kk+1
+        __syncthreads();
+        if (t == 0) {
+            __threadfence();
+            atomicAdd(arrived, 1u);
+            const unsigned target = (unsigned)((kk + 1) * gridDim.x);
+            int it = 0, q = 0;
+            while (*(volatile unsigned *)arrived < target) {
+                if (*abandon || ++it > kGjSpinLimit) { *abandon = 1; q = 1; break; }
+                __nanosleep(64);
+            }
+            __threadfence();
+            quit = q;
+        }
+        __syncthreads();
+        if (quit) return;
+    }
+}
+
 __global__ void k_identity(double *m, int64_t n) {
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = t / n;
@@ -2429,13 +2496,45 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
             G2P_TRY(dalloc(&H.cinv, nn * nn, s));
             G2P_CUDA(cudaMemsetAsync(Dm, 0, sizeof(double) * nn * nn, s));
             (g2p::kbegin("k_dense_fill", s), k_dense_fill<<<grid_for(nn), kThreads, 0, s>>>(nn, Cl.A.ptr, Cl.A.col, Cl.A.val, Dm), g2p::kend(s));
-            G2P_CUDA(cudaMemsetAsync(d_int, 0, sizeof(int), s));
+            G2P_CUDA(cudaMemsetAsync(d_int, 0, 3 * sizeof(int), s));
             {
                 double *a1, *i0, *i1;
                 G2P_TRY(dalloc(&a1, nn * nn, s)); G2P_TRY(dalloc(&i0, nn * nn, s)); G2P_TRY(dalloc(&i1, nn * nn, s));
                 (g2p::kbegin("k_identity", s), k_identity<<<grid_for(nn * nn), kThreads, 0, s>>>(i0, nn), g2p::kend(s));
                 double *ain = Dm, *aout = a1, *iin = i0, *iout = i1;
-                for (int64_t kk = 0; kk < nn; kk++) {
+                // one cooperative launch when every row's block fits on the
+                // device at once, else (or with G2P_GJ_STEPS=1, for
+                // comparisons) one launch per pivot
+                int coop_attr = 0, dev = 0, per_sm = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&coop_attr, cudaDevAttrCooperativeLaunch, dev);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_coop, 256, 0);
+                bool coop = false;
+                if (coop_attr && (int64_t)per_sm * kSMs >= nn && !getenv("G2P_GJ_STEPS")) {
+                    int64_t nn_arg = nn;
+                    void *args[] = {&ain, &iin, &aout, &iout, &nn_arg, &d_int};
+                    g2p::kbegin("k_gj_coop", s);
+                    coop = cudaLaunchCooperativeKernel((void *)k_gj_coop, dim3((unsigned)nn), dim3(256), args, 0, s) == cudaSuccess;
+                    g2p::kend(s);
+                    if (coop) {
+                        int gave_up = 0;
+                        G2P_CUDA(cudaMemcpyAsync(&gave_up, d_int + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+                        G2P_CUDA(cudaStreamSynchronize(s));
+                        if (gave_up) {           // start again from A and I
+                            coop = false;
+                            G2P_CUDA(cudaMemsetAsync(d_int, 0, sizeof(int), s));
+                            G2P_CUDA(cudaMemsetAsync(Dm, 0, sizeof(double) * nn * nn, s));
+                            (g2p::kbegin("k_dense_fill", s), k_dense_fill<<<grid_for(nn), kThreads, 0, s>>>(nn, Cl.A.ptr, Cl.A.col, Cl.A.val, Dm), g2p::kend(s));
+                            (g2p::kbegin("k_identity", s), k_identity<<<grid_for(nn * nn), kThreads, 0, s>>>(i0, nn), g2p::kend(s));
+                        } else if (nn & 1) {
+                            std::swap(ain, aout);
+                            std::swap(iin, iout);
+                        }
+                    } else {
+                        cudaGetLastError();
+                    }
+                }
+                for (int64_t kk = 0; kk < nn && !coop; kk++) {
                     (g2p::kbegin("k_gj_step", s), k_gj_step<<<(unsigned)nn, 256, 0, s>>>(ain, iin, aout, iout, nn, kk, d_int), g2p::kend(s));
                     std::swap(ain, aout);
                     std::swap(iin, iout);

@@ -155,3 +155,22 @@ def test_gpu_galerkin_hash_path_matches_sort_path(name, precision, g2p, monkeypa
         out.append(Z)
     assert np.array_equal(out[0], out[1])
     assert np.abs(out[0] - out[2]).max() / np.abs(out[2]).max() < 1e-8
+
+
+@pytest.mark.parametrize("name,precision", [("strip_c1", "mixed"), ("manhattan_sweep", "fp64")])
+def test_gpu_coarse_inverse_one_launch_matches_per_pivot(name, precision, g2p, monkeypatch):
+    """The coarsest level's dense inverse from one cooperative launch (a grid
+    barrier between pivots) does the per-pivot launches' arithmetic: Z is
+    bit-identical either way."""
+    d, A, M = golden_layout(name)
+    out = []
+    for steps in (False, True):
+        if steps:
+            monkeypatch.setenv("G2P_GJ_STEPS", "1")
+        else:
+            monkeypatch.delenv("G2P_GJ_STEPS", raising=False)
+        with g2p.FdtdMesh(d) as m:
+            g2p.generateStiff(m)
+            Z, st = g2p.paraGenerator(m, g2p.default_params(precision=precision, rtol=1e-10))
+        out.append(Z)
+    assert np.array_equal(out[0], out[1])
