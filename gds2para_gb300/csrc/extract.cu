@@ -23,9 +23,11 @@
 
 g2p_status g2p_run_v0(g2p_mesh *m);
 g2p_status g2p_run_v0_ex(g2p_mesh *m, bool defer_ad);
-g2p_status g2p_v0_finish(g2p_mesh *m);
+g2p_status g2p_v0_finish(g2p_mesh *m, bool *repatterned = nullptr);
+g2p_status g2p_v0_provisional(g2p_mesh *m);
 g2p_status g2p_solver_build(const g2p::Csr<double> &A, const g2p_solver_params *p, cudaStream_t stream,
                             g2p_solver **out);
+g2p_status g2p_solver_set_operator(g2p_solver *S, const g2p::Csr<double> &A, bool same_pattern);
 g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k, g2p_solve_stats *st);
 
 namespace g2p {
@@ -313,7 +315,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     memset(&local, 0, sizeof(local));
     auto t0 = std::chrono::steady_clock::now();
     // Ad's ordered conductor sums keep running on the mesh's side stream
-    // while the ports are prepared and Ac's solver is set up
+    // while the ports are prepared and the solvers are set up
     G2P_TRY(g2p_run_v0_ex(m, true));
     local.assembly_ms = ms_since(t0);
     // ---- port data: J entries (last side wins, matrixCon.cpp:367-374),
@@ -401,8 +403,16 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         cudaGetLastError();
     }
     const bool ac_here = !tc.joinable();
-    rs = g2p_v0_finish(m);
+    // Ad's preconditioner is built from Ad with stand-in sums for its
+    // longest segments while their ordered sums finish on the side stream;
+    // the solver's operator then gets the exact Ad
+    rs = g2p_v0_provisional(m);
     if (rs == G2P_OK) rs = g2p_solver_build(m->Ad, &p, s, &Sd);
+    if (rs == G2P_OK) {
+        bool repatterned = false;
+        rs = g2p_v0_finish(m, &repatterned);
+        if (rs == G2P_OK) rs = g2p_solver_set_operator(Sd, m->Ad, !repatterned);
+    }
     if (tc.joinable()) tc.join();
     if (ac_here && rs == G2P_OK) {
         rs_c = g2p_solver_build(m->Ac, &pc, s, &Sc);

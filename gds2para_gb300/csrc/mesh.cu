@@ -268,7 +268,7 @@ extern "C" g2p_status g2p_mesh_create(const g2p_mesh_desc *in, g2p_mesh **out) {
     return G2P_OK;
 }
 
-g2p_status g2p_v0_finish(g2p_mesh *m);
+g2p_status g2p_v0_finish(g2p_mesh *m, bool *repatterned = nullptr);
 
 extern "C" g2p_status g2p_mesh_destroy(g2p_mesh *m) {
     if (!m) return G2P_OK;

@@ -208,6 +208,31 @@ g2p_status g2p_solver_build(const Csr<double> &A, const g2p_solver_params *p, cu
     return G2P_OK;
 }
 
+// Replaces the operator of the Krylov products and residuals by A and keeps
+// the preconditioner, which may have been built from an approximation of A.
+// same_pattern: A has the current operator's pattern, so only the values
+// are copied.  Before the first solve (no captured graphs hold the old
+// operator's buffers).
+g2p_status g2p_solver_set_operator(g2p_solver *S, const Csr<double> &A, bool same_pattern) {
+    cudaStream_t s = S->stream;
+    if (A.n != S->A.n) { set_last_message("operator size %lld, solver built for %lld", (long long)A.n, (long long)S->A.n); return G2P_ERR_INVALID; }
+    if (same_pattern && A.nnz == S->A.nnz) {
+        G2P_CUDA(cudaMemcpyAsync(S->A.val, A.val, sizeof(double) * A.nnz, cudaMemcpyDeviceToDevice, s));
+        return sell_refill<double>(S->A, s);
+    }
+    S->A.release(s);
+    S->lr.release(s);
+    S->A.n = S->A.m = A.n; S->A.nnz = A.nnz;
+    G2P_TRY(dalloc(&S->A.ptr, A.n + 1, s));
+    G2P_TRY(dalloc(&S->A.col, A.nnz, s));
+    G2P_TRY(dalloc(&S->A.val, A.nnz, s));
+    G2P_CUDA(cudaMemcpyAsync(S->A.ptr, A.ptr, sizeof(int64_t) * (A.n + 1), cudaMemcpyDeviceToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(S->A.col, A.col, sizeof(int32_t) * A.nnz, cudaMemcpyDeviceToDevice, s));
+    G2P_CUDA(cudaMemcpyAsync(S->A.val, A.val, sizeof(double) * A.nnz, cudaMemcpyDeviceToDevice, s));
+    G2P_TRY(find_long_rows<double>(S->A, S->lr, s));
+    return sell_build<double>(S->A, s);
+}
+
 static g2p_status reserve_block(g2p_solver *S, int k) {
     if (k <= S->kcap) return G2P_OK;
     cudaStream_t s = S->stream;

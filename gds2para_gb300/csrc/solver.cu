@@ -889,6 +889,17 @@ g2p_status sell_build(Csr<T> &A, cudaStream_t s, int64_t maxlen) {
 template g2p_status sell_build<double>(Csr<double> &, cudaStream_t, int64_t);
 template g2p_status sell_build<float>(Csr<float> &, cudaStream_t, int64_t);
 
+// New values, same pattern: rewrites the sliced-ELL copy's values from A.val
+// (padding and long rows are untouched).
+template <class T>
+g2p_status sell_refill(Csr<T> &A, cudaStream_t s) {
+    if (!A.sptr) return G2P_OK;
+    (g2p::kbegin("k_sell_fill", s), k_sell_fill<T><<<grid_for(A.n), kThreads, 0, s>>>(A.n, A.ptr, A.col, A.val, A.rlen, A.sptr, A.scol, A.sval), g2p::kend(s));
+    G2P_CUDA(cudaGetLastError());
+    return G2P_OK;
+}
+template g2p_status sell_refill<double>(Csr<double> &, cudaStream_t);
+
 // ------------------------------------------- 16-byte chunks of k-interleaved blocks
 // A block of k right-hand sides is stored row-major (entry (i, r) at i*k + r).
 // When k is a power-of-two multiple of the chunk width C = 16 / sizeof(T) and

@@ -140,6 +140,8 @@ g2p_status copy_long_rows(const LongRows &src, LongRows &dst, cudaStream_t s);
 // Sliced-ELL copy of the rows of A with at most maxlen (<= 254) entries.
 template <class T>
 g2p_status sell_build(Csr<T> &A, cudaStream_t s, int64_t maxlen = kLongRow);
+template <class T>
+g2p_status sell_refill(Csr<T> &A, cudaStream_t s);
 
 }  // namespace g2p
 

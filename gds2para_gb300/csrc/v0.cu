@@ -479,10 +479,49 @@ __global__ void __launch_bounds__(256) k_seg_sum_long(const uint64_t *keys, cons
             __syncwarp();
         }
         if (lane == 0) {
+            if (okey) okey[sg] = keys[b];
+            oval[sg] = s;
+            keep[sg] = fabs(s) > 1e-8 ? 1 : 0;
+        }
+    }
+}
+
+// Stand-in for k_seg_sum_long while it runs: each lane adds a strided share
+// of the segment and a shuffle tree adds the 32 partials.  Deterministic but
+// not the left-to-right sum; these values only build the preconditioner's
+// copy of the Laplacian, and k_long_patch later writes the ordered sums.
+__global__ void __launch_bounds__(256) k_seg_sum_tree(const uint64_t *keys, const double *vals, int64_t nseg,
+                                                      const int64_t *sstart, uint64_t *okey, double *oval,
+                                                      int64_t *keep) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t sg = warp; sg < nseg; sg += nwarp) {
+        const int64_t b = sstart[sg], e = sstart[sg + 1];
+        if (e - b <= kSegWarp) continue;
+        double s = 0.0;
+        for (int64_t j = b + lane; j < e; j += 32) s += vals[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) {
             okey[sg] = keys[b];
             oval[sg] = s;
             keep[sg] = fabs(s) > 1e-8 ? 1 : 0;
         }
+    }
+}
+
+// Writes the ordered sums (xval, xkeep from k_seg_sum_long) of the segments
+// longer than kSegWarp into a Laplacian assembled from k_seg_sum_tree's
+// values.  A segment kept by one and dropped by the other changes the
+// pattern: it sets *changed and the caller reassembles.
+__global__ void k_long_patch(const int64_t *sstart, const int64_t *keep, const int64_t *kpos, const double *xval,
+                             const int64_t *xkeep, int64_t nseg, const int64_t *rowptr, int64_t row0, double *val,
+                             int *changed) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nseg; i += (int64_t)gridDim.x * blockDim.x) {
+        if (sstart[i + 1] - sstart[i] <= kSegWarp) continue;
+        if (xkeep[i] != keep[i]) { *changed = 1; continue; }
+        if (keep[i]) val[rowptr[row0] + kpos[i]] = xval[i];
     }
 }
 
@@ -542,13 +581,22 @@ struct g2p::LapPending {
     uint64_t *okey = nullptr, *k0 = nullptr, *k1 = nullptr;
     double *oval = nullptr, *v0 = nullptr, *v1 = nullptr;
     cudaEvent_t done = nullptr;     // recorded on the side stream after the ordered sums
+    // split: the long segments' ordered sums go to xval/xkeep on the side
+    // stream, k_seg_sum_tree's stand-ins to oval/keep on the job's stream;
+    // provisional: A is assembled from the stand-ins, k_long_patch pending
+    bool split = false, provisional = false;
+    double *xval = nullptr;
+    int64_t *xkeep = nullptr;
 };
 
 // Builds one Laplacian (Ad when is_ac false) from a V0 basis; rows [0, nshort)
 // are single-node columns, rows [nshort, ncol) conductor columns.  Part one:
-// everything up to the ordered per-key sums of the long rows, which go to
-// m->side when `on_side` (the largest conductor's sum is a dependent chain of
-// FP64 additions; other work can run meanwhile).
+// everything up to the ordered per-key sums of the long rows.  With
+// `on_side` the sums of segments longer than kSegWarp (the largest
+// conductor's is a dependent chain of FP64 additions) run on m->side, and the
+// job's stream gets tree-summed stand-ins for them at once, so a
+// provisional Laplacian can be assembled (lap_finish) and the exact one
+// completed later (lap_exact).
 static g2p_status lap_begin(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool is_ac, int64_t nshort, Csr<double> &A,
                             LapPending &P, bool on_side) {
     cudaStream_t s = m->stream;
@@ -607,34 +655,36 @@ static g2p_status lap_begin(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool is_ac,
     G2P_TRY(dalloc(&P.keep, nseg + 1, s)); G2P_TRY(dalloc(&P.kpos, nseg + 1, s));
     G2P_TRY(dalloc(&P.sstart, nseg + 1, s));
     (g2p::kbegin("k_seg_bounds", s), k_seg_bounds<<<grid_for(nterm), kThreads, 0, s>>>(P.head, P.segid, nterm, nseg, P.sstart), g2p::kend(s));
-    cudaStream_t ss = s;
     if (on_side) {
         if (!m->side) G2P_CUDA(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+        G2P_TRY(dalloc(&P.xval, nseg, s));
+        G2P_TRY(dalloc(&P.xkeep, nseg, s));
         cudaEvent_t fork;
         G2P_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
         G2P_CUDA(cudaEventRecord(fork, s));
         G2P_CUDA(cudaStreamWaitEvent(m->side, fork, 0));
         cudaEventDestroy(fork);
-        ss = m->side;
-    }
-    (g2p::kbegin("k_seg_sum", ss), k_seg_sum<<<grid_for(nseg), kThreads, 0, ss>>>(sk, sv, nseg, P.sstart, P.okey, P.oval, P.keep), g2p::kend(ss));
-    (g2p::kbegin("k_seg_sum_long", ss), k_seg_sum_long<<<grid_for(32 * nseg), kThreads, 0, ss>>>(sk, sv, nseg, P.sstart, P.okey, P.oval, P.keep), g2p::kend(ss));
-    if (on_side) {
+        cudaStream_t ss = m->side;
+        (g2p::kbegin("k_seg_sum_long", ss), k_seg_sum_long<<<grid_for(32 * nseg), kThreads, 0, ss>>>(sk, sv, nseg, P.sstart, nullptr, P.xval, P.xkeep), g2p::kend(ss));
         G2P_CUDA(cudaEventCreateWithFlags(&P.done, cudaEventDisableTiming));
         G2P_CUDA(cudaEventRecord(P.done, ss));
+        P.split = true;
     }
+    (g2p::kbegin("k_seg_sum", s), k_seg_sum<<<grid_for(nseg), kThreads, 0, s>>>(sk, sv, nseg, P.sstart, P.okey, P.oval, P.keep), g2p::kend(s));
+    if (on_side)
+        (g2p::kbegin("k_seg_sum_tree", s), k_seg_sum_tree<<<grid_for(32 * nseg), kThreads, 0, s>>>(sk, sv, nseg, P.sstart, P.okey, P.oval, P.keep), g2p::kend(s));
+    else
+        (g2p::kbegin("k_seg_sum_long", s), k_seg_sum_long<<<grid_for(32 * nseg), kThreads, 0, s>>>(sk, sv, nseg, P.sstart, P.okey, P.oval, P.keep), g2p::kend(s));
     return G2P_OK;
 }
 
-// Part two: waits for the ordered sums, then row offsets and entries.  Every
-// buffer the side stream reads is freed here, after the wait.
+static g2p_status build_laplacian(g2p_mesh *m, const V0Ctx &c, V0Basis &B, bool is_ac, int64_t nshort, Csr<double> &A);
+
+// Part two: row offsets and entries.  When split, from the stand-in sums
+// and without waiting for the side stream: the buffers it reads (sorted
+// terms, segment starts) and those lap_exact needs stay allocated.
 static g2p_status lap_finish(g2p_mesh *m, LapPending &P) {
     cudaStream_t s = m->stream;
-    if (P.done) {
-        G2P_CUDA(cudaStreamWaitEvent(s, P.done, 0));
-        cudaEventDestroy(P.done);
-        P.done = nullptr;
-    }
     const V0Ctx &c = P.c;
     V0Basis &B = *P.B;
     Csr<double> &A = *P.A;
@@ -645,8 +695,11 @@ static g2p_status lap_finish(g2p_mesh *m, LapPending &P) {
         auto kop = [kp, nseg] __device__(int64_t i) -> int64_t { return i < nseg ? kp[i] : 0; };
         G2P_TRY(ensure_scan_work(m, nseg + 1));
         G2P_TRY(exclusive_scan(kop, nseg + 1, P.kpos, m->scan_work, s));
-        dfree(P.sstart, s); dfree(P.head, s); dfree(P.segid, s);
-        dfree(P.k0, s); dfree(P.k1, s); dfree(P.v0, s); dfree(P.v1, s);
+        dfree(P.head, s); dfree(P.segid, s);
+        if (!P.split) {
+            dfree(P.sstart, s);
+            dfree(P.k0, s); dfree(P.k1, s); dfree(P.v0, s); dfree(P.v1, s);
+        }
     }
     int64_t nnz = 0;
     G2P_TRY(g2p_build_rowptr(m, P.rowlen, ncol, &A.ptr, &nnz));
@@ -661,10 +714,43 @@ static g2p_status lap_finish(g2p_mesh *m, LapPending &P) {
     if (P.nlong > 0) {
         (g2p::kbegin("k_long_scatter", s), k_long_scatter<<<grid_for(nseg), kThreads, 0, s>>>(P.okey, P.oval, P.keep, P.kpos, nseg, ncol, nshort, A.ptr, 0, A.col,
                                                            A.val), g2p::kend(s));
-        dfree(P.okey, s); dfree(P.oval, s); dfree(P.keep, s); dfree(P.kpos, s);
+        dfree(P.okey, s); dfree(P.oval, s);
+        if (!P.split) { dfree(P.keep, s); dfree(P.kpos, s); }
     }
     G2P_CUDA(cudaGetLastError());
     G2P_CUDA(cudaStreamSynchronize(s));
+    P.provisional = P.split;
+    return G2P_OK;
+}
+
+// Part three of a split Laplacian: waits for the ordered sums and writes them
+// over the stand-ins.  Every buffer the side stream reads is freed here,
+// after the wait.  If a long segment's kept/dropped status differs from its
+// stand-in's, the Laplacian is assembled again in one pass and *repatterned
+// is set (G2P_AD_REPATTERN=1 takes that path always, for comparisons).
+static g2p_status lap_exact(g2p_mesh *m, LapPending &P, bool *repatterned) {
+    cudaStream_t s = m->stream;
+    G2P_CUDA(cudaStreamWaitEvent(s, P.done, 0));
+    cudaEventDestroy(P.done);
+    P.done = nullptr;
+    Csr<double> &A = *P.A;
+    int *changed;
+    G2P_TRY(dalloc(&changed, 1, s));
+    G2P_CUDA(cudaMemsetAsync(changed, 0, sizeof(int), s));
+    (g2p::kbegin("k_long_patch", s), k_long_patch<<<grid_for(P.nseg), kThreads, 0, s>>>(P.sstart, P.keep, P.kpos, P.xval, P.xkeep, P.nseg, A.ptr, P.nshort, A.val, changed), g2p::kend(s));
+    int h = 0;
+    G2P_CUDA(cudaMemcpyAsync(&h, changed, sizeof(int), cudaMemcpyDeviceToHost, s));
+    G2P_CUDA(cudaStreamSynchronize(s));
+    dfree(changed, s);
+    if (getenv("G2P_AD_REPATTERN")) h = 1;
+    dfree(P.sstart, s); dfree(P.keep, s); dfree(P.kpos, s); dfree(P.xval, s); dfree(P.xkeep, s);
+    dfree(P.k0, s); dfree(P.k1, s); dfree(P.v0, s); dfree(P.v1, s);
+    P.provisional = false;
+    if (repatterned) *repatterned = h != 0;
+    if (h) {
+        A.release(s);
+        G2P_TRY(build_laplacian(m, P.c, *P.B, P.is_ac, P.nshort, A));
+    }
     return G2P_OK;
 }
 
@@ -684,7 +770,7 @@ __global__ void k_compact_cond(const int32_t *mark_node, int64_t n, const int64_
         if (mark_node[i] != 0) { key[pos[i]] = (uint32_t)mark_node[i]; node[pos[i]] = (int32_t)i; }
 }
 
-g2p_status g2p_v0_finish(g2p_mesh *m);
+g2p_status g2p_v0_finish(g2p_mesh *m, bool *repatterned = nullptr);
 
 // V0 bases and Laplacians.  With defer_ad, Ad's ordered conductor sums are
 // left running on the side stream and g2p_v0_finish completes Ad; Ac and
@@ -868,15 +954,29 @@ g2p_status g2p_run_v0_ex(g2p_mesh *m, bool defer_ad) {
     return defer_ad ? G2P_OK : g2p_v0_finish(m);
 }
 
-g2p_status g2p_v0_finish(g2p_mesh *m) {
+g2p_status g2p_v0_finish(g2p_mesh *m, bool *repatterned) {
+    if (repatterned) *repatterned = false;
     if (m->v0_done) return G2P_OK;
     if (!m->ad_pending) return g2p_run_v0_ex(m, false);
     LapPending *P = m->ad_pending;
     m->ad_pending = nullptr;
-    g2p_status st = lap_finish(m, *P);
+    g2p_status st = P->provisional ? G2P_OK : lap_finish(m, *P);
+    if (st == G2P_OK && P->split) st = lap_exact(m, *P, repatterned);
     delete P;
     if (st == G2P_OK) m->v0_done = true;
     return st;
+}
+
+// Ad assembled with the stand-in sums of its longest segments, for a
+// preconditioner to be built while the ordered sums run on; g2p_v0_finish
+// then writes the exact values (Ad stays pending until then).
+g2p_status g2p_v0_provisional(g2p_mesh *m) {
+    if (m->v0_done) return G2P_OK;
+    if (!m->ad_pending) return g2p_run_v0_ex(m, false);
+    LapPending *P = m->ad_pending;
+    if (!P->split) return g2p_v0_finish(m);
+    if (P->provisional) return G2P_OK;
+    return lap_finish(m, *P);
 }
 
 g2p_status g2p_run_v0(g2p_mesh *m) { return g2p_run_v0_ex(m, false); }

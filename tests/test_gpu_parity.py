@@ -174,3 +174,29 @@ def test_gpu_coarse_inverse_one_launch_matches_per_pivot(name, precision, g2p, m
             Z, st = g2p.paraGenerator(m, g2p.default_params(precision=precision, rtol=1e-10))
         out.append(Z)
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("name", ["strip_c1", "multistrip_small"])
+def test_gpu_extraction_leaves_exact_ad_and_repattern_path_agrees(name, g2p, monkeypatch):
+    """Ad's preconditioner is built from tree-summed stand-ins for its longest
+    conductor segments while their ordered sums run; the Ad an extraction
+    leaves behind, and multiplies by, is still the reference's bit for bit.
+    Forcing the reassembly taken when a stand-in's kept/dropped status
+    differs gives the same Ad and the same Z."""
+    d, A, M = golden_layout(name)
+    out = []
+    for force in (False, True):
+        if force:
+            monkeypatch.setenv("G2P_AD_REPATTERN", "1")
+        else:
+            monkeypatch.delenv("G2P_AD_REPATTERN", raising=False)
+        with g2p.FdtdMesh(d) as m:
+            g2p.generateStiff(m)
+            Z, st = g2p.paraGenerator(m, g2p.default_params(precision="mixed", rtol=1e-10))
+            r, c, v = m.export_laplacian("d")
+        check_golden_array(A, M, "Ad_row", r)
+        check_golden_array(A, M, "Ad_col", c)
+        check_golden_array(A, M, "Ad_val", v)
+        assert st.max_rel_residual <= 1e-10
+        out.append(Z)
+    assert np.array_equal(out[0], out[1])
