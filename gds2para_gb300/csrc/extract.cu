@@ -366,13 +366,15 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         if (const char *e = getenv("G2P_AC_PRECISION")) pc.precision = atoi(e);
         // Ac's aggregation wants a stronger threshold than Ad's: twice Ad's,
         // at most 0.1 (c2 sweep: 0.04 -> 37 iterations, 0.08 -> 33, >= 0.15
-        // stalls).  G2P_AC_STRENGTH / G2P_AC_DEGREE override (comparisons).
+        // stalls).  G2P_AC_STRENGTH / G2P_AC_DEGREE / G2P_AC_RESTART
+        // override (comparisons).
         {
             const double st0 = p.strength > 0 ? p.strength : 0.04;
             pc.strength = std::min(2 * st0, 0.1);
         }
         if (const char *t = getenv("G2P_AC_STRENGTH")) pc.strength = atof(t);
         if (const char *t = getenv("G2P_AC_DEGREE")) pc.smoother_degree = atoi(t);
+        if (const char *t = getenv("G2P_AC_RESTART")) pc.restart = atoi(t);
     }
     // Ac's solver is built by a second host thread on its own stream (after
     // Ac's assembly, an event on the job's stream) while this thread

@@ -260,7 +260,7 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
         F32Precond pc;
         pc.H = &S->H32; pc.lr = &S->lr; pc.in = S->rf; pc.out = S->df;
         G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep,
-                               S->precision == G2P_PREC_FP64_PC32 ? &pc : nullptr));
+                               S->precision == G2P_PREC_FP64_PC32 ? &pc : nullptr, &S->lr));
         iters = rep.iterations;
         if (getenv("G2P_DEBUG"))
             fprintf(stderr, "[g2p] n=%lld k=%d fp64: its %d rel %.3e\n", (long long)n, k, rep.iterations, rep.rel_residual);

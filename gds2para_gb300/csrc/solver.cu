@@ -2792,7 +2792,8 @@ __global__ void k_f_to_d(int64_t nk, const float *a, double *b) {
 
 template <class T>
 g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T *x, int k, const SolverConfig &cfg,
-                  const double *bnorm_override, cudaStream_t s, SolveReport &rep, const F32Precond *pc) {
+                  const double *bnorm_override, cudaStream_t s, SolveReport &rep, const F32Precond *pc,
+                  const LongRows *op_lr) {
     const int64_t n = A.n, nk = n * k;
     const int m = cfg.restart;
     if (k < 1 || k > kMaxRhs) { set_last_message("block of %d right-hand sides (1..%d supported)", k, kMaxRhs); return G2P_ERR_INVALID; }
@@ -2800,7 +2801,7 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
     G2P_TRY(krylov_alloc<T>(K, n, k, m, s));
     if (pc) G2P_TRY(hierarchy_reserve<float>(*pc->H, k, s));
     else G2P_TRY(hierarchy_reserve<T>(H, k, s));
-    const LongRows &lr0 = pc ? *pc->lr : H.lv[0].lr;
+    const LongRows &lr0 = op_lr ? *op_lr : (pc ? *pc->lr : H.lv[0].lr);
     // CUDA graphs of the Arnoldi steps: off while kernels are being timed;
     // rebuilt when the block width, operator or preconditioner changes
     const bool graphs = cfg.use_graphs && !kprof_on() && !g_prof.on;
@@ -2931,9 +2932,10 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
 }
 template g2p_status fgmres<double>(const Csr<double> &, Hierarchy<double> &, Krylov<double> &, const double *, double *,
                                    int, const SolverConfig &, const double *, cudaStream_t, SolveReport &,
-                                   const F32Precond *);
+                                   const F32Precond *, const LongRows *);
 template g2p_status fgmres<float>(const Csr<float> &, Hierarchy<float> &, Krylov<float> &, const float *, float *, int,
-                                  const SolverConfig &, const double *, cudaStream_t, SolveReport &, const F32Precond *);
+                                  const SolverConfig &, const double *, cudaStream_t, SolveReport &, const F32Precond *,
+                                  const LongRows *);
 
 }  // namespace g2p
 

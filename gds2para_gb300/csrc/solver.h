@@ -114,10 +114,13 @@ struct F32Precond {
 
 // FGMRES(m) right-preconditioned by one V-cycle per iteration, for k right-
 // hand sides at once.  x holds the initial guess on entry.  With pc (FP64
-// only) the V-cycle runs in FP32 on pc->H and H is not used.
+// only) the V-cycle runs in FP32 on pc->H and H is not used.  op_lr: the long
+// rows of A (default: those of pc, or of H's level 0, which must then have
+// A's pattern).
 template <class T>
 g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T *x, int k, const SolverConfig &cfg,
-                  const double *bnorm_override, cudaStream_t s, SolveReport &rep, const F32Precond *pc = nullptr);
+                  const double *bnorm_override, cudaStream_t s, SolveReport &rep, const F32Precond *pc = nullptr,
+                  const LongRows *op_lr = nullptr);
 
 template <class T>
 g2p_status krylov_alloc(Krylov<T> &K, int64_t n, int k, int m, cudaStream_t s);

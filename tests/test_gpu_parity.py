@@ -176,8 +176,8 @@ def test_gpu_coarse_inverse_one_launch_matches_per_pivot(name, precision, g2p, m
     assert np.array_equal(out[0], out[1])
 
 
-@pytest.mark.parametrize("name", ["strip_c1", "multistrip_small"])
-def test_gpu_extraction_leaves_exact_ad_and_repattern_path_agrees(name, g2p, monkeypatch):
+@pytest.mark.parametrize("name,precision", [("strip_c1", "mixed"), ("multistrip_small", "mixed"), ("strip_c1", "fp64")])
+def test_gpu_extraction_leaves_exact_ad_and_repattern_path_agrees(name, precision, g2p, monkeypatch):
     """Ad's preconditioner is built from tree-summed stand-ins for its longest
     conductor segments while their ordered sums run; the Ad an extraction
     leaves behind, and multiplies by, is still the reference's bit for bit.
@@ -192,7 +192,7 @@ def test_gpu_extraction_leaves_exact_ad_and_repattern_path_agrees(name, g2p, mon
             monkeypatch.delenv("G2P_AD_REPATTERN", raising=False)
         with g2p.FdtdMesh(d) as m:
             g2p.generateStiff(m)
-            Z, st = g2p.paraGenerator(m, g2p.default_params(precision="mixed", rtol=1e-10))
+            Z, st = g2p.paraGenerator(m, g2p.default_params(precision=precision, rtol=1e-10))
             r, c, v = m.export_laplacian("d")
         check_golden_array(A, M, "Ad_row", r)
         check_golden_array(A, M, "Ad_col", c)
