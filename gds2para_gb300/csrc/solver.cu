@@ -1104,31 +1104,32 @@ __global__ void __launch_bounds__(256) k_colsq_partial_v(const T *x, int64_t n, 
 }
 
 constexpr int kDotGroupV = 8;
-template <class T>
-__global__ void __launch_bounds__(256) k_mdot_partial_v(const T *V, int64_t n, int J, const T *w, int k, double *partial) {
-    constexpr int C = Chunk<T>::C, GC = kDotGroupV * C;
+// Dots of basis vectors j0 .. j0 + G - 1 with w.  G is a compile-time count
+// (one launch per group of at most kDotGroupV), so exactly G products per
+// element are issued: an FP64 dot is bound by the FP64 pipe on this part.
+template <class T, int G>
+__global__ void __launch_bounds__(256) k_mdot_partial_v(const T *V, int64_t n, int j0, const T *w, int k,
+                                                        double *partial) {
+    constexpr int C = Chunk<T>::C, GC = G * C;
     __shared__ double sm[8 * GC * 16];
     const int cpr = blockDim.x, cc = threadIdx.x, ny = blockDim.y;
     const int64_t nk = n * k;
-    for (int j0 = 0; j0 < J; j0 += kDotGroupV) {
-        T acc[GC];          // acc[g * C + u]
+    T acc[GC];          // acc[g * C + u]
 #pragma unroll
-        for (int e = 0; e < GC; e++) acc[e] = 0;
-        for (int64_t i = blockIdx.x * (int64_t)ny + threadIdx.y; i < n; i += (int64_t)gridDim.x * ny) {
-            const int64_t t = i * k + cc * C;
-            Chunk<T> ww;
-            ww.ld(w + t);
+    for (int e = 0; e < GC; e++) acc[e] = 0;
+    for (int64_t i = blockIdx.x * (int64_t)ny + threadIdx.y; i < n; i += (int64_t)gridDim.x * ny) {
+        const int64_t t = i * k + cc * C;
+        Chunk<T> ww;
+        ww.ld(w + t);
 #pragma unroll
-            for (int g = 0; g < kDotGroupV; g++)
-                if (j0 + g < J) {
-                    Chunk<T> vv;
-                    vv.ld(V + (int64_t)(j0 + g) * nk + t);
+        for (int g = 0; g < G; g++) {
+            Chunk<T> vv;
+            vv.ld(V + (int64_t)(j0 + g) * nk + t);
 #pragma unroll
-                    for (int u = 0; u < C; u++) acc[g * C + u] += vv.v[u] * ww.v[u];
-                }
+            for (int u = 0; u < C; u++) acc[g * C + u] += vv.v[u] * ww.v[u];
         }
-        chunk_col_reduce<GC>(acc, sm, cpr, k, C, J - j0 < kDotGroupV ? J - j0 : kDotGroupV, j0, partial);
     }
+    chunk_col_reduce<GC>(acc, sm, cpr, k, C, G, j0, partial);
 }
 
 // --------------------------------------------------------------- reductions
@@ -1227,32 +1228,29 @@ template void colnorms<float>(const float *, int64_t, int, double *, double *, c
 // dots[j*k + r] = <V_j[:, r], w[:, r]> for j < J, eight basis vectors per pass
 // over w; block partials are reduced in a fixed order.
 constexpr int kDotGroup = 8;
-template <class T>
-__global__ void __launch_bounds__(256) k_mdot_partial(const T *V, int64_t n, int J, const T *w, int k, double *partial) {
-    __shared__ double sm[kDotGroup][256];
+template <class T, int G>
+__global__ void __launch_bounds__(256) k_mdot_partial(const T *V, int64_t n, int j0, const T *w, int k,
+                                                      double *partial) {
+    __shared__ double sm[G][256];
     const int r = threadIdx.x, ty = threadIdx.y, ny = blockDim.y;
     const int64_t nk = n * k;
-    for (int j0 = 0; j0 < J; j0 += kDotGroup) {
-        T acc[kDotGroup];
+    T acc[G];
 #pragma unroll
-        for (int g = 0; g < kDotGroup; g++) acc[g] = 0;
-        if (r < k)
-            for (int64_t i = blockIdx.x * (int64_t)ny + ty; i < n; i += (int64_t)gridDim.x * ny) {
-                int64_t t = i * k + r;
-                T wv = w[t];
+    for (int g = 0; g < G; g++) acc[g] = 0;
+    if (r < k)
+        for (int64_t i = blockIdx.x * (int64_t)ny + ty; i < n; i += (int64_t)gridDim.x * ny) {
+            int64_t t = i * k + r;
+            T wv = w[t];
 #pragma unroll
-                for (int g = 0; g < kDotGroup; g++)
-                    if (j0 + g < J) acc[g] += V[(int64_t)(j0 + g) * nk + t] * wv;
-            }
-        double v[kDotGroup];
-#pragma unroll
-        for (int g = 0; g < kDotGroup; g++) v[g] = (double)acc[g];
-        block_col_reduce<kDotGroup>(v, &sm[0][0]);
-        for (int idx = ty * blockDim.x + r; idx < kDotGroup * (int)blockDim.x; idx += blockDim.x * blockDim.y) {
-            int g = idx / blockDim.x, rr = idx % blockDim.x;
-            if (rr < k && j0 + g < J) partial[((int64_t)(j0 + g) * k + rr) * gridDim.x + blockIdx.x] = sm[g][rr];
+            for (int g = 0; g < G; g++) acc[g] += V[(int64_t)(j0 + g) * nk + t] * wv;
         }
-        __syncthreads();
+    double v[G];
+#pragma unroll
+    for (int g = 0; g < G; g++) v[g] = (double)acc[g];
+    block_col_reduce<G>(v, &sm[0][0]);
+    for (int idx = ty * blockDim.x + r; idx < G * (int)blockDim.x; idx += blockDim.x * blockDim.y) {
+        int g = idx / blockDim.x, rr = idx % blockDim.x;
+        if (rr < k) partial[((int64_t)(j0 + g) * k + rr) * gridDim.x + blockIdx.x] = sm[g][rr];
     }
 }
 
@@ -2766,12 +2764,24 @@ __global__ void k_xupdate(int64_t n, int k, int m, int j, const T *Z, const doub
 template <class T>
 static void mdot(const T *V, int64_t n, int J, const T *w, int k, double *partial, double *out, cudaStream_t s) {
     const int cpr = chunk_cpr<T>(k);
-    if (cpr && cpr <= 16) {
-        (g2p::kbegin("k_mdot_partial", s), k_mdot_partial_v<T><<<kRedBlocks, dim3(cpr, 256 / cpr), 0, s>>>(V, n, J, w, k, partial), g2p::kend(s));
-    } else {
-        int kx = pow2_ge(k);
-        dim3 blk(kx, 256 / kx);
-        (g2p::kbegin("k_mdot_partial", s), k_mdot_partial<T><<<kRedBlocks, blk, 0, s>>>(V, n, J, w, k, partial), g2p::kend(s));
+    const bool vec = cpr && cpr <= 16;
+    const dim3 vblk(vec ? cpr : 1, vec ? 256 / cpr : 1);
+    const int kx = pow2_ge(k);
+    const dim3 blk(kx, 256 / kx);
+    for (int j0 = 0; j0 < J; j0 += kDotGroup) {
+        const int g = J - j0 < kDotGroup ? J - j0 : kDotGroup;
+        g2p::kbegin("k_mdot_partial", s);
+#define G2P_MDOT_CASE(G)                                                                                  \
+    case G:                                                                                               \
+        if (vec) k_mdot_partial_v<T, G><<<kRedBlocks, vblk, 0, s>>>(V, n, j0, w, k, partial);             \
+        else k_mdot_partial<T, G><<<kRedBlocks, blk, 0, s>>>(V, n, j0, w, k, partial);                    \
+        break;
+        switch (g) {
+            G2P_MDOT_CASE(1) G2P_MDOT_CASE(2) G2P_MDOT_CASE(3) G2P_MDOT_CASE(4)
+            G2P_MDOT_CASE(5) G2P_MDOT_CASE(6) G2P_MDOT_CASE(7) default: G2P_MDOT_CASE(8)
+        }
+#undef G2P_MDOT_CASE
+        g2p::kend(s);
     }
     (g2p::kbegin("k_reduce_partials", s), k_reduce_partials<<<reduce_grid(J * k), 32 * kReduceWarps, 0, s>>>(partial, kRedBlocks, J * k, out, false), g2p::kend(s));
 }
