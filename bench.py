@@ -239,9 +239,10 @@ def run_gb300(args):
     last = {"assembly_ms": stats.assembly_ms, "setup_ms": stats.setup_ms, "solve_ms": stats.solve_ms,
             "total_ms": stats.total_ms, "iterations": stats.total_iterations,
             "max_rel_residual": stats.max_rel_residual, "ad_levels": stats.ad_levels, "ac_levels": stats.ac_levels,
-            "rhs_block": stats.rhs_block, "ad_degree": stats.ad_degree,
+            "rhs_block": stats.rhs_block, "ad_degree": stats.ad_degree, "ac_strength": stats.ac_strength,
             "autotune": ("off: fixed blocks of 4 ports (the HBM budget)" if big else
-                         "block width and Chebyshev degree picked in the warm-up (first Ad solve timed per candidate)"),
+                         "block width and Chebyshev degree (first Ad solve timed per candidate) and Ac's "
+                         "aggregation strength (first Ac solve timed per candidate) picked in the warm-up"),
             "note": "host wall-clock of the phases of the last timed step (assembly and setup are mostly "
                     "enqueue time; the solve phase ends with the host copy of Z)"}
     # kernel-level figures from separate profiled steps (events around every

@@ -66,7 +66,8 @@ class ExtractStats(C.Structure):
     _fields_ = [("sizes", Sizes), ("solves", C.c_int32), ("total_iterations", C.c_int32),
                 ("max_rel_residual", C.c_double), ("assembly_ms", C.c_double), ("setup_ms", C.c_double),
                 ("solve_ms", C.c_double), ("total_ms", C.c_double), ("ad_levels", C.c_int32),
-                ("ac_levels", C.c_int32), ("rhs_block", C.c_int32), ("ad_degree", C.c_int32)]
+                ("ac_levels", C.c_int32), ("rhs_block", C.c_int32), ("ad_degree", C.c_int32),
+                ("ac_strength", C.c_double)]
 
 
 class BoxC(C.Structure):

@@ -252,6 +252,60 @@ struct TuneKey {
 };
 static std::mutex g_tune_mu;
 static std::map<TuneKey, std::pair<int, int>> g_tuned;   // -> (block width, degree)
+// Aggregation strength of Ac's AMG, keyed by Ac's entry count in nnz.  Ac's
+// iteration count is far from monotonic in it (c3: 24 iterations at 0.02, 54
+// at 0.04, 76 at 0.08; c2: 45, 37 and 33), so it is measured per shape.
+static std::map<TuneKey, double> g_ac_tuned;
+
+static bool ac_tuned(const TuneKey &key, double *strength) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_ac_tuned.find(key);
+    if (it == g_ac_tuned.end()) return false;
+    *strength = it->second;
+    return true;
+}
+
+// Times Ac's solve of the first block with the strength thresholds st0 / 2,
+// st0 and 2 st0 (at most 0.1), st0 being Ad's; *Sc (built with pc) is one of
+// them.  Each candidate: one untimed solve, then the better of two timed
+// ones.  *Sc is replaced by the fastest candidate's solver.
+static g2p_status tune_ac(g2p_mesh *m, const TuneKey &key, const g2p_solver_params &pc, double st0, g2p_solver **Sc,
+                          const double *Bc, double *Yc, int kk, cudaStream_t s) {
+    std::vector<double> cands = {st0 / 2, st0, std::min(2 * st0, 0.1)};
+    double best_ms = 1e300, best_st = pc.strength;
+    g2p_solver *best = nullptr;
+    for (double cs : cands) {
+        g2p_solver *S = nullptr;
+        if (cs == pc.strength) {
+            S = *Sc;
+        } else {
+            g2p_solver_params q = pc;
+            q.strength = cs;
+            if (g2p_solver_build(m->Ac, &q, s, &S) != G2P_OK) { cudaGetLastError(); continue; }
+        }
+        g2p_solve_stats ss;
+        g2p_status rc = g2p_solver_solve_dev(S, Bc, Yc, kk, &ss);
+        double ms = 1e300;
+        for (int rep = 0; rep < 2 && rc == G2P_OK; rep++) {
+            auto t = std::chrono::steady_clock::now();
+            rc = g2p_solver_solve_dev(S, Bc, Yc, kk, &ss);
+            ms = std::min(ms, ms_since(t));
+        }
+        if (rc == G2P_OK && ms < best_ms) {
+            if (best && best != *Sc) g2p_solver_destroy(best);
+            best = S; best_ms = ms; best_st = cs;
+        } else if (S != *Sc) {
+            g2p_solver_destroy(S);
+        }
+    }
+    if (best && best != *Sc) {
+        g2p_solver_destroy(*Sc);
+        *Sc = best;
+    }
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_ac_tuned.emplace(key, best ? best_st : pc.strength);   // an earlier entry wins
+    return G2P_OK;
+}
 
 // Times the Ad solve of the first block of ports with each candidate (after
 // an untimed solve, best of two) and keeps the one with the least estimated
@@ -361,6 +415,11 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     // mixed method its V-cycle preconditioner runs in FP32.
     // G2P_AC_PRECISION overrides the mode (comparisons).
     g2p_solver_params pc = p;
+    const double st0 = p.strength > 0 ? p.strength : 0.04;
+    const TuneKey ac_key{m->d.nx, m->d.ny, m->d.nz, m->Ac.nnz, P, p.precision};
+    const bool ac_fixed = getenv("G2P_AC_STRENGTH") != nullptr;
+    double ac_st = 0;
+    const bool ac_known = ac_tuned(ac_key, &ac_st);
     {
         if (p.precision == G2P_PREC_MIXED) pc.precision = G2P_PREC_FP64_PC32;
         if (const char *e = getenv("G2P_AC_PRECISION")) pc.precision = atoi(e);
@@ -368,11 +427,9 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         // at most 0.1 (c2 sweep: 0.04 -> 37 iterations, 0.08 -> 33, >= 0.15
         // stalls).  G2P_AC_STRENGTH / G2P_AC_DEGREE / G2P_AC_RESTART
         // override (comparisons).
-        {
-            const double st0 = p.strength > 0 ? p.strength : 0.04;
-            pc.strength = std::min(2 * st0, 0.1);
-        }
-        if (const char *t = getenv("G2P_AC_STRENGTH")) pc.strength = atof(t);
+        pc.strength = std::min(2 * st0, 0.1);
+        if (ac_fixed) pc.strength = atof(getenv("G2P_AC_STRENGTH"));
+        else if (ac_known) pc.strength = ac_st;
         if (const char *t = getenv("G2P_AC_DEGREE")) pc.smoother_degree = atoi(t);
         if (const char *t = getenv("G2P_AC_RESTART")) pc.restart = atoi(t);
     }
@@ -432,6 +489,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     local.setup_ms = ms_since(t0);
     local.ad_levels = Sd->levels;
     local.ac_levels = Sc->levels;
+    local.ac_strength = pc.strength;
     LongRows lcol;   // long columns of V0d (conductor columns)
     {
         Csr<double> tmp;
@@ -487,6 +545,12 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         (g2p::kbegin("k_v0t_short", s), k_v0t_short<<<row_grid(nc, kk), row_block(kk), 0, s>>>(nc, kk, m->v0c.cptr, m->v0c.cedge, m->v0c.caval, yd1, f0, crhs), g2p::kend(s));
         (g2p::kbegin("k_add", s), k_add<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, crhs), g2p::kend(s));
         // (4) Ac y0c = b_c
+        if (p0 == 0 && p.autotune && !ac_fixed && !ac_known) {
+            G2P_TRY(tune_ac(m, ac_key, pc, st0, &Sc, Bc, Yc, kk, s));
+            double tuned = 0;
+            if (ac_tuned(ac_key, &tuned)) local.ac_strength = tuned;
+            local.ac_levels = Sc->levels;
+        }
         rc = g2p_solver_solve_dev(Sc, Bc, Yc, kk, &ss);
         if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }
         if (rc == G2P_ERR_NOT_CONVERGED) worst_rc = rc;

@@ -92,10 +92,13 @@ typedef struct {
     int32_t autotune;         /* paraGenerator, 1: pick the block width of the port
                                  right-hand sides (all ports, or 8/16/32/64 at a time)
                                  and the Chebyshev degree (2, 3, 4) of the Ad solves by
-                                 timing the first block's Ad solve with each, once per
-                                 grid shape and port count in the process (later jobs
-                                 of that shape reuse the choice); 0 (default): all
-                                 ports, smoother_degree */
+                                 timing the first block's Ad solve with each, and the
+                                 aggregation strength of Ac's AMG (strength / 2,
+                                 strength, 2 strength) by timing its first Ac solve,
+                                 once per grid shape and port count in the process
+                                 (later jobs of that shape reuse the choice); 0
+                                 (default): all ports, smoother_degree, Ac at
+                                 min(2 strength, 0.1) */
     int32_t inner_restart;    /* mixed: restart length of the inner FP32 FGMRES (its
                                  basis is (2 inner_restart + 1) vectors of n x k; 0 =
                                  restart) */
@@ -123,6 +126,7 @@ typedef struct {
     double assembly_ms, setup_ms, solve_ms, total_ms;
     int32_t ad_levels, ac_levels;
     int32_t rhs_block, ad_degree;    /* ports per block solve and Ad's Chebyshev degree used */
+    double ac_strength;              /* aggregation strength threshold of Ac's AMG */
 } g2p_extract_stats;
 
 /* ---- library ---- */
