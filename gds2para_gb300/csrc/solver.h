@@ -55,7 +55,7 @@ struct SolverConfig {
     int coarse_size = 256;
     double strength = 0.04;
     int max_levels = 20;
-    double cheb_ratio = 0.1;     // lower Chebyshev bound = ratio * lmax
+    double cheb_ratio = 0.15;    // lower Chebyshev bound = ratio * lmax
     bool reorth = true;
     bool use_graphs = false;     // replay each Arnoldi step from a CUDA graph
 };
