@@ -129,6 +129,7 @@ static SolverConfig cfg_from(const g2p_solver_params *p) {
     c.reorth = false;   // classical Gram-Schmidt once: same iteration counts, half the passes
     if (const char *e = getenv("G2P_REORTH")) c.reorth = atoi(e) != 0;
     if (const char *e = getenv("G2P_CHEB_RATIO")) c.cheb_ratio = atof(e);   // comparisons
+    if (const char *e = getenv("G2P_CHEB_UPPER")) c.cheb_upper = atof(e);
     return c;
 }
 

@@ -1299,8 +1299,9 @@ __global__ void k_cheb_step(int64_t n, int k, const T *dinv, const T *res, T *x,
 }
 
 template <class T>
-static void chebyshev(Level<T> &L, int deg, double ratio, const T *b, T *x, bool zero_guess, int k, cudaStream_t s) {
-    double lmax = L.lmax * 1.05, lmin = L.lmax * ratio;
+static void chebyshev(Level<T> &L, int deg, double ratio, double upper, const T *b, T *x, bool zero_guess, int k,
+                      cudaStream_t s) {
+    double lmax = L.lmax * upper, lmin = L.lmax * ratio;
     double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
     double sigma = theta / delta, rho = 1.0 / sigma;
     unsigned g = row_grid(L.n, k);
@@ -1378,12 +1379,12 @@ static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaS
     if (l == (int)H.lv.size() - 1) {
         if (H.cinv) (g2p::kbegin("k_dense_apply", s), k_dense_apply<T><<<(unsigned)((L.n * k * 32 + 255) / 256), 256, 0, s>>>(L.n, k, H.cinv, b, x), g2p::kend(s));
         else {
-            chebyshev<T>(L, 4, cfg.cheb_ratio, b, x, true, k, s);
-            for (int q = 0; q < 4; q++) chebyshev<T>(L, 4, cfg.cheb_ratio, b, x, false, k, s);
+            chebyshev<T>(L, 4, cfg.cheb_ratio, cfg.cheb_upper, b, x, true, k, s);
+            for (int q = 0; q < 4; q++) chebyshev<T>(L, 4, cfg.cheb_ratio, cfg.cheb_upper, b, x, false, k, s);
         }
         return;
     }
-    chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, b, x, true, k, s);
+    chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, cfg.cheb_upper, b, x, true, k, s);
     spmm_b<T>(L.A, L.lr, x, L.t0, k, b, s);
     Level<T> &C = H.lv[l + 1];
     if (const int cpr = chunk_cpr<T>(k))
@@ -1393,7 +1394,7 @@ static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaS
     vcycle<T>(H, cfg, l + 1, k, s, C.b, C.x);
     if (L.P.sptr) prolong_sell<T>(L.P, C.x, x, k, s);
     else (g2p::kbegin("k_prolong_csr", s), k_prolong_csr<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, L.P.ptr, L.P.col, L.P.val, C.x, x), g2p::kend(s));
-    chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, b, x, false, k, s);
+    chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, cfg.cheb_upper, b, x, false, k, s);
 }
 
 // ------------------------------------------------------------- AMG setup

@@ -56,6 +56,7 @@ struct SolverConfig {
     double strength = 0.04;
     int max_levels = 20;
     double cheb_ratio = 0.15;    // lower Chebyshev bound = ratio * lmax
+    double cheb_upper = 1.05;    // upper Chebyshev bound = upper * lmax (lmax: Gershgorin)
     bool reorth = true;
     bool use_graphs = false;     // replay each Arnoldi step from a CUDA graph
 };
