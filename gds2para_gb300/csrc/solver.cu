@@ -2436,7 +2436,7 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 dfree(k0, s); dfree(k1, s); dfree(pos, s);
                 pc_.mark("members", l, s);
                 // ---- smoothed prolongation P = (I - w D^-1 A) T
-                double w = 4.0 / (3.0 * L.lmax);
+                double w = cfg.psmooth / L.lmax;
                 int64_t *pc;
                 G2P_TRY(dalloc(&pc, n + 1, s));
                 G2P_TRY(dalloc(&L.P.ptr, n + 1, s));

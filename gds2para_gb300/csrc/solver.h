@@ -57,6 +57,7 @@ struct SolverConfig {
     int max_levels = 20;
     double cheb_ratio = 0.15;    // lower Chebyshev bound = ratio * lmax
     double cheb_upper = 1.05;    // upper Chebyshev bound = upper * lmax (lmax: Gershgorin)
+    double psmooth = 4.0 / 3.0;  // prolongation smoothing weight = psmooth / lmax
     bool reorth = true;
     bool use_graphs = false;     // replay each Arnoldi step from a CUDA graph
 };
