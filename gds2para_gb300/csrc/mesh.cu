@@ -480,67 +480,39 @@ struct FaceRef {
     int64_t a, b, c;
 };
 
-__device__ __forceinline__ int edge_faces(const Dims &d, int64_t e, FaceRef *fr) {
-    int64_t n1, n2, z, x, y;
-    int kind = d.edge_nodes(e, n1, n2, z, x, y);
-    int nf = 0;
-    if (kind == 0) {  // y-edge: plane z, node x, cell y
-        if (x >= 1) fr[nf++] = {fid_xy(d, z, x - 1, y), 0, z, x - 1, y};
-        if (x < d.Nx) fr[nf++] = {fid_xy(d, z, x, y), 0, z, x, y};
-        if (z >= 1) fr[nf++] = {fid_yz(d, x, z - 1, y), 1, x, z - 1, y};
-        if (z < d.Nz) fr[nf++] = {fid_yz(d, x, z, y), 1, x, z, y};
-    } else if (kind == 1) {  // x-edge: plane z, cell x, node y
-        if (y >= 1) fr[nf++] = {fid_xy(d, z, x, y - 1), 0, z, x, y - 1};
-        if (y < d.Ny) fr[nf++] = {fid_xy(d, z, x, y), 0, z, x, y};
-        if (z >= 1) fr[nf++] = {fid_xz(d, y, z - 1, x), 2, y, z - 1, x};
-        if (z < d.Nz) fr[nf++] = {fid_xz(d, y, z, x), 2, y, z, x};
-    } else {  // z-edge: layer z, node (x, y)
-        if (y >= 1) fr[nf++] = {fid_yz(d, x, z, y - 1), 1, x, z, y - 1};
-        if (y < d.Ny) fr[nf++] = {fid_yz(d, x, z, y), 1, x, z, y};
-        if (x >= 1) fr[nf++] = {fid_xz(d, y, z, x - 1), 2, y, z, x - 1};
-        if (x < d.Nx) fr[nf++] = {fid_xz(d, y, z, x), 2, y, z, x};
-    }
-    // increasing face number (insertion sort of <= 4)
-    for (int i = 1; i < nf; i++) {
-        FaceRef t = fr[i];
-        int j = i - 1;
-        while (j >= 0 && fr[j].id > t.id) { fr[j + 1] = fr[j]; j--; }
-        fr[j + 1] = t;
-    }
-    return nf;
+__device__ __forceinline__ void face_cx(FaceRef &a, FaceRef &b) {
+    if (b.id < a.id) { const FaceRef t = a; a = b; b = t; }
 }
 
-constexpr int kMaxS = 16;
-
-// Accumulates the row of edge e in (cols, vals), sorted by column; returns the
-// number of columns (PEC columns included).
-__device__ __forceinline__ int stiff_row(const Geo &g, int64_t e, int64_t *cols, double *vals) {
-    FaceRef fr[4];
-    int nf = edge_faces(g.d, e, fr);
-    int nc = 0;
-    for (int t = 0; t < nf; t++) {
-        FaceEnt f;
-        if (fr[t].kind == 0) face_xy(g, fr[t].a, fr[t].b, fr[t].c, f);
-        else if (fr[t].kind == 1) face_yz(g, fr[t].a, fr[t].b, fr[t].c, f);
-        else face_xz(g, fr[t].a, fr[t].b, fr[t].c, f);
-        double sh = 0.0;
-#pragma unroll
-        for (int k = 0; k < 4; k++) if (f.e[k] == e) sh = f.sh[k];
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            int q = 0;
-            while (q < nc && cols[q] != f.e[k]) q++;
-            if (q == nc) { cols[nc] = f.e[k]; vals[nc] = 0.0; nc++; }
-            vals[q] += sh * f.se[k];
-        }
+// The candidate faces sit in fixed slots (absent ones keyed last) and a
+// five-step compare-exchange network orders them, so fr stays in registers.
+__device__ __forceinline__ int edge_faces(const Dims &d, int64_t e, FaceRef *fr) {
+    constexpr int64_t kNone = INT64_MAX;
+    int64_t n1, n2, z, x, y;
+    int kind = d.edge_nodes(e, n1, n2, z, x, y);
+    if (kind == 0) {  // y-edge: plane z, node x, cell y
+        fr[0] = {x >= 1 ? fid_xy(d, z, x - 1, y) : kNone, 0, z, x - 1, y};
+        fr[1] = {x < d.Nx ? fid_xy(d, z, x, y) : kNone, 0, z, x, y};
+        fr[2] = {z >= 1 ? fid_yz(d, x, z - 1, y) : kNone, 1, x, z - 1, y};
+        fr[3] = {z < d.Nz ? fid_yz(d, x, z, y) : kNone, 1, x, z, y};
+    } else if (kind == 1) {  // x-edge: plane z, cell x, node y
+        fr[0] = {y >= 1 ? fid_xy(d, z, x, y - 1) : kNone, 0, z, x, y - 1};
+        fr[1] = {y < d.Ny ? fid_xy(d, z, x, y) : kNone, 0, z, x, y};
+        fr[2] = {z >= 1 ? fid_xz(d, y, z - 1, x) : kNone, 2, y, z - 1, x};
+        fr[3] = {z < d.Nz ? fid_xz(d, y, z, x) : kNone, 2, y, z, x};
+    } else {  // z-edge: layer z, node (x, y)
+        fr[0] = {y >= 1 ? fid_yz(d, x, z, y - 1) : kNone, 1, x, z, y - 1};
+        fr[1] = {y < d.Ny ? fid_yz(d, x, z, y) : kNone, 1, x, z, y};
+        fr[2] = {x >= 1 ? fid_xz(d, y, z, x - 1) : kNone, 2, y, z, x - 1};
+        fr[3] = {x < d.Nx ? fid_xz(d, y, z, x) : kNone, 2, y, z, x};
     }
-    for (int i = 1; i < nc; i++) {
-        int64_t c = cols[i]; double v = vals[i];
-        int j = i - 1;
-        while (j >= 0 && cols[j] > c) { cols[j + 1] = cols[j]; vals[j + 1] = vals[j]; j--; }
-        cols[j + 1] = c; vals[j + 1] = v;
-    }
-    return nc;
+    // increasing face number
+    face_cx(fr[0], fr[1]);
+    face_cx(fr[2], fr[3]);
+    face_cx(fr[0], fr[2]);
+    face_cx(fr[1], fr[3]);
+    face_cx(fr[1], fr[2]);
+    return (fr[0].id != kNone) + (fr[1].id != kNone) + (fr[2].id != kNone) + (fr[3].id != kNone);
 }
 
 __global__ void __launch_bounds__(256) k_stiff_count(Geo g, const uint8_t *__restrict__ pec, const int32_t *__restrict__ map,
@@ -563,21 +535,78 @@ __global__ void __launch_bounds__(256) k_stiff_count(Geo g, const uint8_t *__res
     }
 }
 
+// v / d rounded to nearest, from y = RN(1 / d) with one product and two
+// FMAs instead of a division (FP64 division is an iterative sequence on the
+// FP64 pipe, the limit of this kernel).  Markstein's theorem (P. Markstein,
+// IBM J. Res. Dev. 34(1), 1990; Muller et al., Handbook of Floating-Point
+// Arithmetic, "division with a correction step"): q = RN(v y) is within one
+// ulp of v / d, r = v - q d is exact by FMA, and RN(q + r y) = RN(v / d),
+// barring underflow and overflow.  Operands outside [2^-900, 2^900] take the
+// division; zero keeps its sign.  The range test reads the exponent bits
+// (integer pipe), leaving three FP64 operations.
+__device__ __forceinline__ double div_rn(double v, double d, double y) {
+    const int ex = (int)((__double_as_longlong(v) >> 52) & 0x7ff);   // biased exponent
+    if (ex < 1023 - 900 || ex > 1023 + 899) return v / d;
+    const double q = v * y;
+    const double r = fma(-q, d, v);
+    return fma(r, y, q);
+}
+
+// The row of edge e in registers.  Slot 0 is the diagonal; slot 1 + 4t + k
+// is the k-th edge of e's t-th face (faces in increasing number).  e's own
+// slot in each face, the slots of absent faces and PEC columns are empty.
+// Two faces of the grid share at most one edge, e, so every other column has
+// exactly one slot.  As in the reference's row (Sh Se^T accumulated per
+// face, then sorted by column), the diagonal sums its per-face products from
+// 0.0 in face order and every other entry is 0.0 plus its one product.  Each
+// entry is written at its rank among the row's columns, so nothing is sorted
+// in memory and the row never leaves registers.
 __global__ void __launch_bounds__(256) k_stiff_fill(Geo g, const uint8_t *__restrict__ pec, const int32_t *__restrict__ map,
                                                     const int64_t *__restrict__ rowptr, int32_t *__restrict__ col,
-                                                    double *__restrict__ val, double mu) {
+                                                    double *__restrict__ val, double mu, double inv_mu) {
     const Dims &d = g.d;
+    constexpr int64_t kNone = INT64_MAX;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < d.N_edge; e += (int64_t)gridDim.x * blockDim.x) {
         if (pec[e]) continue;
-        int64_t cols[kMaxS];
-        double vals[kMaxS];
-        int nc = stiff_row(g, e, cols, vals);
-        int64_t o = rowptr[map[e]];
-        for (int q = 0; q < nc; q++) {
-            if (pec[cols[q]]) continue;
-            col[o] = map[cols[q]];
-            val[o] = vals[q] / mu;
-            o++;
+        FaceRef fr[4];
+        const int nf = edge_faces(d, e, fr);
+        int64_t c[17];
+        double v[17];
+        double diag = 0.0;
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            FaceEnt f = {};
+            if (t < nf) {
+                if (fr[t].kind == 0) face_xy(g, fr[t].a, fr[t].b, fr[t].c, f);
+                else if (fr[t].kind == 1) face_yz(g, fr[t].a, fr[t].b, fr[t].c, f);
+                else face_xz(g, fr[t].a, fr[t].b, fr[t].c, f);
+            }
+            double sh = 0.0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) if (t < nf && f.e[k] == e) sh = f.sh[k];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const bool self = t < nf && f.e[k] == e;
+                if (self) diag += sh * f.se[k];
+                const bool keep = t < nf && !self && !pec[f.e[k]];
+                c[1 + 4 * t + k] = keep ? f.e[k] : kNone;
+                // 0.0 + p: p itself except that -0.0 becomes +0.0 (a bit test,
+                // not an FP64 add)
+                const double p = sh * f.se[k];
+                v[1 + 4 * t + k] = keep && __double_as_longlong(p) != (long long)0x8000000000000000ULL ? p : 0.0;
+            }
+        }
+        c[0] = e;
+        v[0] = diag;
+        const int64_t o = rowptr[map[e]];
+#pragma unroll
+        for (int i = 0; i < 17; i++) {
+            if (c[i] == kNone) continue;
+            int r = 0;
+#pragma unroll
+            for (int j = 0; j < 17; j++) r += c[j] < c[i] ? 1 : 0;
+            col[o + r] = map[c[i]];
+            val[o + r] = div_rn(v[i], mu, inv_mu);
         }
     }
 }
@@ -646,7 +675,7 @@ g2p_status g2p_run_stiff(g2p_mesh *m) {
     G2P_TRY(dalloc(&m->S.col, nnz, s));
     G2P_TRY(dalloc(&m->S.val, nnz, s));
     (g2p::kbegin("k_stiff_fill", s), k_stiff_fill<<<grid_for(d.N_edge, 256, 152LL * 32), 256, 0, s>>>(g, m->pec_edge, m->map_edge, m->S.ptr, m->S.col,
-                                                                     m->S.val, m->k.mu), g2p::kend(s));
+                                                                     m->S.val, m->k.mu, 1.0 / m->k.mu), g2p::kend(s));
     dfree(tab, s);
     G2P_CUDA(cudaGetLastError());
     G2P_CUDA(cudaStreamSynchronize(s));
