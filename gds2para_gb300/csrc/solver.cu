@@ -1690,19 +1690,15 @@ __global__ void k_dense_fill(int64_t n, const int64_t *ptr, const int32_t *col, 
         for (int64_t q = ptr[i]; q < ptr[i + 1]; q++) Dm[i * n + col[q]] += val[q];
 }
 
-// Gauss-Jordan inverse with partial pivoting in one block (n <= a few 1000).
-// Gauss-Jordan inversion with partial pivoting, one launch per pivot step
-// over the whole GPU.  Step kk reads (a_in, inv_in) and writes (a_out,
-// inv_out), so no block waits on another: block i owns row i, repeats the
-// (cheap) pivot search of column kk itself -- largest |a_ik|, i >= kk, the
-// first one on ties -- and writes its row after the swap of rows kk and p
-// and the elimination.  Columns of a at or left of kk are never read again
-// and are not written.
-__global__ void __launch_bounds__(256) k_gj_step(const double *__restrict__ a_in, const double *__restrict__ inv_in,
-                                                 double *__restrict__ a_out, double *__restrict__ inv_out, int64_t n,
-                                                 int64_t kk, int *singular) {
-    __shared__ double bv[256];
-    __shared__ int64_t bi[256];
+// Gauss-Jordan inversion with partial pivoting.  Step kk reads (a_in,
+// inv_in) and writes (a_out, inv_out), so no block waits on another within a
+// step: block i owns row i, repeats the (cheap) pivot search of column kk
+// itself -- largest |a_ik|, i >= kk, the first one on ties -- and writes its
+// row after the swap of rows kk and p and the elimination.  Columns of a at
+// or left of kk are never read again and are not written.  bv, bi: 256
+// doubles and indices of shared memory.
+__device__ __forceinline__ void gj_step(const double *a_in, const double *inv_in, double *a_out, double *inv_out,
+                                        int64_t n, int64_t kk, int *singular, double *bv, int64_t *bi) {
     const int t = threadIdx.x;
     double mv = -1.0;
     int64_t mi = n;
@@ -1735,13 +1731,22 @@ __global__ void __launch_bounds__(256) k_gj_step(const double *__restrict__ a_in
     }
 }
 
-// All n pivot steps of k_gj_step in one cooperative launch (one block per
-// row, every block resident): the same per-step arithmetic, with a grid-wide
-// barrier between steps instead of a launch.  Buffers ping-pong as in the
-// per-step loop; the inverse ends in inv1 when n is odd, inv0 otherwise.
-// flags[0] is the singular flag, flags[1] the barrier's arrival count and
-// flags[2] set when a block gave up waiting (bounded spin), in which case the
-// caller recomputes with one launch per pivot.
+// One launch per pivot step over the whole GPU.
+__global__ void __launch_bounds__(256) k_gj_step(const double *__restrict__ a_in, const double *__restrict__ inv_in,
+                                                 double *__restrict__ a_out, double *__restrict__ inv_out, int64_t n,
+                                                 int64_t kk, int *singular) {
+    __shared__ double bv[256];
+    __shared__ int64_t bi[256];
+    gj_step(a_in, inv_in, a_out, inv_out, n, kk, singular, bv, bi);
+}
+
+// All n pivot steps in one cooperative launch (one block per row, every
+// block resident), with a grid-wide barrier between steps instead of a
+// launch.  Buffers ping-pong as in the per-step loop; the inverse ends in
+// inv1 when n is odd, inv0 otherwise.  flags[0] is the singular flag,
+// flags[1] the barrier's arrival count and flags[2] set when a block gave up
+// waiting (bounded spin), in which case the caller recomputes with one
+// launch per pivot.
 constexpr int kGjSpinLimit = 1 << 22;
 __global__ void __launch_bounds__(256) k_gj_coop(double *a0, double *inv0, double *a1, double *inv1, int64_t n,
                                                  int *flags) {
@@ -1749,40 +1754,11 @@ __global__ void __launch_bounds__(256) k_gj_coop(double *a0, double *inv0, doubl
     __shared__ int64_t bi[256];
     __shared__ int quit;
     const int t = threadIdx.x;
-    const int64_t i = blockIdx.x;
     unsigned *arrived = reinterpret_cast<unsigned *>(flags + 1);
     volatile int *abandon = flags + 2;
     for (int64_t kk = 0; kk < n; kk++) {
-        const double *a_in = (kk & 1) ? a1 : a0, *inv_in = (kk & 1) ? inv1 : inv0;
-        double *a_out = (kk & 1) ? a0 : a1, *inv_out = (kk & 1) ? inv0 : inv1;
-        double mv = -1.0;
-        int64_t mi = n;
-        for (int64_t r = kk + t; r < n; r += blockDim.x) {
-            const double v = fabs(a_in[r * n + kk]);
-            if (v > mv) { mv = v; mi = r; }
-        }
-        bv[t] = mv; bi[t] = mi;
-        __syncthreads();
-        for (int o = 128; o > 0; o >>= 1) {
-            if (t < o && (bv[t + o] > bv[t] || (bv[t + o] == bv[t] && bi[t + o] < bi[t]))) { bv[t] = bv[t + o]; bi[t] = bi[t + o]; }
-            __syncthreads();
-        }
-        const int64_t p = bi[0];
-        double pval = a_in[p * n + kk];
-        if (pval == 0.0) {
-            if (i == 0 && t == 0) flags[0] = 1;
-            pval = 1e-300;
-        }
-        const int64_t src = i == kk ? p : (i == p ? kk : i);
-        const double f = i == kk ? 0.0 : a_in[src * n + kk];
-        for (int64_t c = kk + 1 + t; c < n; c += blockDim.x) {
-            const double pr = a_in[p * n + c] / pval;
-            a_out[i * n + c] = i == kk ? pr : a_in[src * n + c] - f * pr;
-        }
-        for (int64_t c = t; c < n; c += blockDim.x) {
-            const double pr = inv_in[p * n + c] / pval;
-            inv_out[i * n + c] = i == kk ? pr : inv_in[src * n + c] - f * pr;
-        }
+        const bool odd = kk & 1;
+        gj_step(odd ? a1 : a0, odd ? inv1 : inv0, odd ? a0 : a1, odd ? inv0 : inv1, n, kk, flags, bv, bi);
         // grid barrier: every block's writes of step kk before any read of step kk+1
         __syncthreads();
         if (t == 0) {
