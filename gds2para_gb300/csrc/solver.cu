@@ -1103,9 +1103,8 @@ __global__ void __launch_bounds__(256) k_colsq_partial_v(const T *x, int64_t n, 
     chunk_col_reduce<C>(acc, sm, cpr, k, C, 1, 0, partial);
 }
 
-constexpr int kDotGroupV = 8;
 // Dots of basis vectors j0 .. j0 + G - 1 with w.  G is a compile-time count
-// (one launch per group of at most kDotGroupV), so exactly G products per
+// (one launch per group of at most 8, see mdot), so exactly G products per
 // element are issued: an FP64 dot is bound by the FP64 pipe on this part.
 template <class T, int G>
 __global__ void __launch_bounds__(256) k_mdot_partial_v(const T *V, int64_t n, int j0, const T *w, int k,
