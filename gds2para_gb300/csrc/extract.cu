@@ -268,7 +268,8 @@ static bool ac_tuned(const TuneKey &key, double *strength) {
 // Times Ac's solve of the first block with the strength thresholds st0 / 2,
 // st0 and 2 st0 (at most 0.1), st0 being Ad's; *Sc (built with pc) is one of
 // them.  Each candidate: one untimed solve, then the better of two timed
-// ones.  *Sc is replaced by the fastest candidate's solver.
+// ones.  *Sc is replaced by the solver of the recorded choice: the fastest
+// candidate, unless another job of the shape recorded its choice first.
 static g2p_status tune_ac(g2p_mesh *m, const TuneKey &key, const g2p_solver_params &pc, double st0, g2p_solver **Sc,
                           const double *Bc, double *Yc, int kk, cudaStream_t s) {
     std::vector<double> cands = {st0 / 2, st0, std::min(2 * st0, 0.1)};
@@ -302,8 +303,21 @@ static g2p_status tune_ac(g2p_mesh *m, const TuneKey &key, const g2p_solver_para
         g2p_solver_destroy(*Sc);
         *Sc = best;
     }
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_ac_tuned.emplace(key, best ? best_st : pc.strength);   // an earlier entry wins
+    double kept = best ? best_st : pc.strength;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        kept = g_ac_tuned.emplace(key, kept).first->second;   // an earlier entry wins
+    }
+    if (best && kept != best_st) {
+        // another job of this shape recorded its choice first: follow it, so
+        // every job of the shape runs the same way
+        g2p_solver_params q = pc;
+        q.strength = kept;
+        g2p_solver *S = nullptr;
+        G2P_TRY(g2p_solver_build(m->Ac, &q, s, &S));
+        g2p_solver_destroy(*Sc);
+        *Sc = S;
+    }
     return G2P_OK;
 }
 
