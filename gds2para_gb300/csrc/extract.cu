@@ -63,10 +63,15 @@ __global__ void k_v0_apply(int64_t nedge, int k, const int32_t *ecol, const doub
     if (r >= k) return;
     G2P_FOR_ROWS(e, nedge) {
         int64_t t = e * k + r;
-        double acc = 0.0;
         int32_t c0 = ecol[2 * e], c1 = ecol[2 * e + 1];
-        if (c0 >= 0) acc += eval[2 * e] * (1.0 * X[(int64_t)c0 * k + r]);
-        if (c1 >= 0) acc += eval[2 * e + 1] * (1.0 * X[(int64_t)c1 * k + r]);
+        // (0.0 + a0 x0) + a1 x1: the first addition only turns -0.0 into +0.0,
+        // so it is a bit test here (the FP64 pipe is this kernel's limit)
+        double acc = 0.0;
+        if (c0 >= 0) {
+            const double p = eval[2 * e] * X[(int64_t)c0 * k + r];
+            acc = __double_as_longlong(p) == (long long)0x8000000000000000ULL ? 0.0 : p;
+        }
+        if (c1 >= 0) acc += eval[2 * e + 1] * X[(int64_t)c1 * k + r];
         Y[t] = acc;
     }
 }
