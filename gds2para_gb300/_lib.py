@@ -23,6 +23,7 @@ EXPORTS = [
     "g2p_mesh_mark",
     "g2p_convert_param", "g2p_write_touchstone", "g2p_write_citi",
     "g2p_ybus_from_param", "g2p_write_xyce", "g2p_write_spef",
+    "g2p_gdsii_read", "g2p_polygons_size", "g2p_polygons_get", "g2p_polygons_free",
 ]
 
 STATUS = {0: "G2P_OK", 1: "G2P_ERR_INVALID", 2: "G2P_ERR_CUDA", 3: "G2P_ERR_NOMEM", 4: "G2P_ERR_NOT_CONVERGED",
@@ -147,9 +148,14 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_ybus_from_param.argtypes = [C.c_char, i32, dbl, vp, vp, vp]
     L.g2p_write_xyce.argtypes = [C.c_char_p, C.c_char_p, i32, C.POINTER(C.c_char_p), dbl, vp, vp, dbl]
     L.g2p_write_spef.argtypes = [C.c_char_p, C.c_char_p, i32, C.POINTER(C.c_char_p), C.c_char_p, vp, vp, dbl]
+    L.g2p_gdsii_read.argtypes = [C.c_char_p, vp, i32, C.POINTER(vp)]
+    L.g2p_polygons_size.argtypes = [vp, C.POINTER(i64), C.POINTER(i64)]
+    L.g2p_polygons_get.argtypes = [vp, vp, vp, vp, vp]
+    L.g2p_polygons_free.argtypes = [vp]
+    L.g2p_polygons_free.restype = None
     for name in EXPORTS:
         if name not in ("g2p_last_error", "g2p_version", "g2p_default_params", "g2p_launch_count",
-                        "g2p_profile_begin", "g2p_profile_report", "g2p_profile_buckets"):
+                        "g2p_profile_begin", "g2p_profile_report", "g2p_profile_buckets", "g2p_polygons_free"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L

@@ -120,6 +120,27 @@ class FdtdMesh:
         return r, c, v
 
 
+def readGDSII(path, ignore_layers=()):
+    """The conductor polygons of a GDSII file's top cell, flattened as the
+    reference's AsciiDataBase::saveToMesh flattens them (limboint.hpp:2823):
+    returns (layer[npoly], vert_ptr[npoly + 1], x[nvert], y[nvert]) with
+    coordinates in metres.  Host code; no GPU needed."""
+    L = _lib.load()
+    ign = np.ascontiguousarray(np.asarray(ignore_layers, np.int32))
+    h = C.c_void_p()
+    check(L.g2p_gdsii_read(str(path).encode(), ign.ctypes.data if ign.size else None, int(ign.size), C.byref(h)))
+    try:
+        npoly, nvert = C.c_int64(), C.c_int64()
+        check(L.g2p_polygons_size(h, C.byref(npoly), C.byref(nvert)))
+        layer = np.empty(npoly.value, np.int32)
+        vptr = np.empty(npoly.value + 1, np.int64)
+        x, y = np.empty(nvert.value), np.empty(nvert.value)
+        check(L.g2p_polygons_get(h, layer.ctypes.data, vptr.ctypes.data, x.ctypes.data, y.ctypes.data))
+    finally:
+        L.g2p_polygons_free(h)
+    return layer, vptr, x, y
+
+
 def generateStiff(sys: FdtdMesh) -> int:
     """generateStiff (src/generateStiff.cpp:6): builds S on the device and
     returns leng_S."""

@@ -23,8 +23,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "--extended-lambda", "-lineinfo", "-Xcompiler", "-fPIC",
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 NO_FMA = {"mesh.cu", "v0.cu", "extract.cu"}
+# host code whose results must not depend on the host compiler contracting
+# a * b + c into one rounding (the oracle builds with -ffp-contract=off)
+NO_HOST_CONTRACT = {"gdsii.cu"}
 UNITS = ["primitives.cu", "mesh.cu", "v0.cu", "solver.cu", "solve_api.cu", "extract.cu", "noalloc.cu", "serve.cu", "mesher.cu",
-         "network.cu"]
+         "network.cu", "gdsii.cu"]
 
 
 def nvcc() -> str:
@@ -37,7 +40,8 @@ def nvcc() -> str:
 def _compile(unit: str) -> str:
     src = os.path.join(CSRC, unit)
     obj = os.path.join(OUT, unit.replace(".cu", ".o"))
-    flags = ARCH + COMMON + (["--fmad=false"] if unit in NO_FMA else [])
+    flags = ARCH + COMMON + (["--fmad=false"] if unit in NO_FMA else []) + \
+        (["-Xcompiler", "-ffp-contract=off"] if unit in NO_HOST_CONTRACT else [])
     cmd = [nvcc()] + flags + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

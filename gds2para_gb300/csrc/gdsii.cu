@@ -1,0 +1,341 @@
+// GDSII ingest: reads a GDSII stream file and flattens its top cell into the
+// conductor polygons that the reference hands to its mesher
+// (fdtdMesh::conductorIn), host code only.
+//
+// The reference reads the stream with Limbo's parser into AsciiDataBase and
+// flattens it with AsciiDataBase::saveToMesh (limboint.hpp:2823-3150, records
+// at limboint.hpp:3413-3990, transforms at limboint.hpp:104-306, arrays at
+// limboint.hpp:1535-1594).  This file restates that behaviour:
+//   * coordinates, widths and begin extensions are scaled by the UNITS
+//     record's metres per database unit;
+//   * the end extension is never stored (the reference tests for a record
+//     named ENDTEXTN, which does not exist), so it stays 0;
+//   * boundaries and boxes are put in the reference's preferred order when
+//     their element ends (see reorder), then keep every vertex but the
+//     closing one; a box with a nonzero BOXTYPE is skipped; datatypes are
+//     not checked;
+//   * each path segment becomes a 4-vertex rectangle: a segment whose two x
+//     coordinates are equal runs along y, every other one along x; the ends
+//     of the first and last segment overshoot by half the width except for
+//     PATHTYPE 0 (no overshoot) and 4 (2 * begin extension / width at the
+//     start, the end extension 0 at the end); interior joints overshoot by
+//     half the width; the corner order follows the segment's direction;
+//   * STRANS resets magnification and angle, MAG and ANGLE (degrees) set
+//     them; a point is mirrored in y, rotated, then magnified; nested
+//     transforms compose by the reference's case table and wrap the angle to
+//     [-pi, pi);
+//   * an array reference places (cols - 1) x (rows - 1) instances at
+//     p0 + i * colsep.x + j * rowsep.x in both coordinates;
+//   * the top cell is the last cell of the file; references to unknown
+//     cells are skipped.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace {
+
+struct Xform {
+    bool mirror = false, abs_mag = false, abs_rot = false;
+    double mag = 1.0, rot = 0.0;   // rot in radians
+
+    // net transform of this one applied after `old` (the enclosing one)
+    Xform after(const Xform &old) const {
+        Xform t;
+        t.mag = abs_mag ? mag : mag * old.mag;
+        t.mirror = mirror != old.mirror;
+        double r = rot;
+        if (!abs_rot && old.rot != 0.) {
+            if (!old.mirror && !mirror && rot == 0.) r = old.rot;
+            else if (!old.mirror && !mirror) r += old.rot;
+            else if (!old.mirror && mirror && rot == 0.) r = -1. * old.rot;
+            else if (old.mirror && mirror && rot == 0.) r = -1. * old.rot;
+            else if (old.mirror && !mirror && rot != 0.) r += old.rot;
+            else if (mirror && rot != 0.) r -= old.rot;
+        }
+        t.rot = std::fmod(r + M_PI, 2. * M_PI) - M_PI;
+        t.abs_mag = abs_mag;
+        t.abs_rot = abs_rot;
+        return t;
+    }
+    void apply(double x, double y, double &ox, double &oy) const {
+        if (mirror) y = -y;
+        if (rot != 0.) {
+            const double wx = x, wy = y;
+            x = +std::cos(rot) * wx + -std::sin(rot) * wy;
+            y = +std::sin(rot) * wx + +std::cos(rot) * wy;
+        }
+        if (mag != 1.) { x *= mag; y *= mag; }
+        ox = x;
+        oy = y;
+    }
+};
+
+struct Shape {              // boundary, box or path
+    int layer = 0, type = 0;
+    double width = 0., bext = 0.;
+    std::vector<double> xy;
+};
+struct Ref {
+    std::string name;
+    Xform t;
+    int cols = 0, rows = 0;
+    std::vector<double> xy;
+};
+struct Cell {
+    std::string name;
+    std::vector<Shape> bounds, paths, boxes;
+    std::vector<Ref> srefs, arefs;
+};
+
+// The order boundaries and boxes are stored in once their element ends
+// (limboint.hpp:453-496, 1031-1075): a closing point equal to the first is
+// dropped, the list is rotated to start at the lower-right point found by
+// the reference's scan (x >= and y <= the current pick), reversed after its
+// first point when that first step goes left and not up, then closed again.
+void reorder(std::vector<double> &v) {
+    size_t n = v.size() / 2;
+    if (n < 2) return;
+    if (v[0] == v[2 * (n - 1)] && v[1] == v[2 * (n - 1) + 1]) {
+        v.pop_back();
+        v.pop_back();
+        n--;
+    }
+    if (n < 2) return;
+    size_t lr = 0;
+    for (size_t i = 1; i < n; i++)
+        if (v[2 * i] >= v[2 * lr] && v[2 * i + 1] <= v[2 * lr + 1]) lr = i;
+    std::rotate(v.begin(), v.begin() + 2 * lr, v.end());
+    if (v[0] > v[2] && v[1] >= v[3]) {
+        std::vector<double> r = {v[0], v[1]};
+        for (size_t i = n - 1; i > 0; i--) { r.push_back(v[2 * i]); r.push_back(v[2 * i + 1]); }
+        v = r;
+    }
+    v.push_back(v[0]);
+    v.push_back(v[1]);
+}
+
+double real8(const unsigned char *p) {
+    uint64_t m = 0;
+    for (int i = 1; i < 8; i++) m = (m << 8) | p[i];
+    const double v = std::ldexp((double)m, 4 * ((p[0] & 0x7f) - 64) - 56);
+    return (p[0] & 0x80) ? -v : v;
+}
+
+bool parse(const std::vector<unsigned char> &b, std::vector<Cell> &cells) {
+    enum { NONE, BOUND, PATH, BOX, SREF, AREF, OTHER } el = NONE;
+    double unit = 0.0;   // metres per database unit
+    size_t o = 0;
+    while (o + 4 <= b.size()) {
+        const size_t len = ((size_t)b[o] << 8) | b[o + 1];
+        if (len < 4 || o + len > b.size()) return false;
+        const int rt = b[o + 2], dt = b[o + 3];
+        const unsigned char *d = &b[o + 4];
+        const size_t nd = len - 4;
+        std::vector<int> iv;
+        if (dt == 1 || dt == 2)
+            for (size_t i = 0; i + 1 < nd; i += 2) {
+                const int w = (d[i] << 8) | d[i + 1];
+                iv.push_back(dt == 2 ? (int)(int16_t)w : w);
+            }
+        else if (dt == 3)
+            for (size_t i = 0; i + 3 < nd; i += 4)
+                iv.push_back((int)(int32_t)(((uint32_t)d[i] << 24) | ((uint32_t)d[i + 1] << 16) | ((uint32_t)d[i + 2] << 8) | d[i + 3]));
+        std::vector<double> rv;
+        if (dt == 5)
+            for (size_t i = 0; i + 7 < nd; i += 8) rv.push_back(real8(d + i));
+        std::string str;
+        if (dt == 6)
+            for (size_t i = 0; i < nd && d[i]; i++) str.push_back((char)d[i]);
+        Cell *c = cells.empty() ? nullptr : &cells.back();
+        Shape *sh = !c ? nullptr : el == BOUND ? (c->bounds.empty() ? nullptr : &c->bounds.back())
+                               : el == PATH  ? (c->paths.empty() ? nullptr : &c->paths.back())
+                               : el == BOX   ? (c->boxes.empty() ? nullptr : &c->boxes.back()) : nullptr;
+        Ref *rf = !c ? nullptr : el == SREF ? (c->srefs.empty() ? nullptr : &c->srefs.back())
+                             : el == AREF ? (c->arefs.empty() ? nullptr : &c->arefs.back()) : nullptr;
+        switch (rt) {
+        case 0x03: if (rv.size() >= 2) unit = rv[1]; break;                            // UNITS
+        case 0x05: cells.emplace_back(); el = NONE; break;                              // BGNSTR
+        case 0x06: if (c) c->name = str; break;                                         // STRNAME
+        case 0x08: if (c) { c->bounds.emplace_back(); el = BOUND; } break;              // BOUNDARY
+        case 0x09: if (c) { c->paths.emplace_back(); c->paths.back().type = 2; el = PATH; } break;   // PATH
+        case 0x2D: if (c) { c->boxes.emplace_back(); el = BOX; } break;                 // BOX
+        case 0x0A: if (c) { c->srefs.emplace_back(); el = SREF; } break;                // SREF
+        case 0x0B: if (c) { c->arefs.emplace_back(); el = AREF; } break;                // AREF
+        case 0x0C: case 0x15: el = OTHER; break;                                        // TEXT, NODE
+        case 0x0D: if (sh && !iv.empty()) sh->layer = iv[0]; break;                     // LAYER
+        case 0x21: if (el == PATH && sh && !iv.empty()) sh->type = iv[0]; break;        // PATHTYPE
+        case 0x2E: if (el == BOX && sh && !iv.empty()) sh->type = iv[0]; break;         // BOXTYPE
+        case 0x0F: if (el == PATH && sh && !iv.empty()) sh->width = unit * iv[0]; break;    // WIDTH
+        case 0x30: if (el == PATH && sh && !iv.empty()) sh->bext = unit * iv[0]; break;     // BGNEXTN
+        case 0x10:                                                                      // XY
+            if (sh || rf) {
+                std::vector<double> &xy = sh ? sh->xy : rf->xy;
+                xy.clear();
+                for (int v : iv) xy.push_back(unit * v);
+            }
+            break;
+        case 0x12: if (rf) rf->name = str; break;                                       // SNAME
+        case 0x13: if (el == AREF && rf && iv.size() >= 2) { rf->cols = iv[0]; rf->rows = iv[1]; } break;   // COLROW
+        case 0x1A:                                                                      // STRANS
+            if (rf && !iv.empty()) {
+                rf->t = Xform();
+                rf->t.mirror = (iv[0] & 0x8000) != 0;
+                rf->t.abs_mag = (iv[0] & 0x4) != 0;
+                rf->t.abs_rot = (iv[0] & 0x2) != 0;
+            }
+            break;
+        case 0x1B: if (rf && !rv.empty()) rf->t.mag = rv[0]; break;                     // MAG
+        case 0x1C: if (rf && !rv.empty()) rf->t.rot = M_PI / 180. * rv[0]; break;       // ANGLE
+        case 0x11:                                                                      // ENDEL
+            if ((el == BOUND || el == BOX) && sh) reorder(sh->xy);
+            el = NONE;
+            break;
+        default: break;
+        }
+        o += len;
+        if (rt == 0x04) break;   // ENDLIB
+    }
+    return true;
+}
+
+struct Flat {
+    std::vector<int32_t> layer;
+    std::vector<int64_t> vptr{0};
+    std::vector<double> x, y;
+};
+
+bool ignored(int layer, const std::vector<int> &ign) {
+    for (int l : ign) if (l == layer) return true;
+    return false;
+}
+
+void flatten(const std::vector<Cell> &cells, const std::string &name, double xo, double yo, const Xform &t,
+             const std::vector<int> &ign, Flat &out, int depth) {
+    size_t ci = 0;
+    while (ci < cells.size() && cells[ci].name != name) ci++;
+    if (ci == cells.size() || depth > 64) return;
+    const Cell &c = cells[ci];
+    auto put = [&](double px, double py) {
+        double ox, oy;
+        t.apply(px, py, ox, oy);
+        out.x.push_back(ox + xo);
+        out.y.push_back(oy + yo);
+    };
+    auto close = [&](int layer) {
+        out.layer.push_back(layer);
+        out.vptr.push_back((int64_t)out.x.size());
+    };
+    for (const Shape &s : c.bounds) {
+        if (ignored(s.layer, ign) || s.xy.size() < 4) continue;
+        for (size_t j = 0; j + 2 < s.xy.size(); j += 2) put(s.xy[j], s.xy[j + 1]);
+        close(s.layer);
+    }
+    for (const Shape &s : c.paths) {
+        if (ignored(s.layer, ign) || s.xy.size() < 4) continue;
+        const double w = s.width, h = w / 2.;
+        const std::vector<double> &p = s.xy;
+        for (size_t j = 0; j + 2 < p.size(); j += 2) {
+            double o1 = 1.0, o2 = 1.0;
+            if (j == 0) { if (s.type == 0) o1 = 0.0; else if (s.type == 4) o1 = 2. / w * s.bext; }
+            if (j == p.size() - 4) { if (s.type == 0) o2 = 0.0; else if (s.type == 4) o2 = 2. / w * 0.0; }
+            const double x1 = p[j], y1 = p[j + 1], x2 = p[j + 2], y2 = p[j + 3];
+            if (x1 == x2) {            // along y
+                if (y1 > y2) {
+                    put(x1 - h, y1 + o1 * h); put(x1 + h, y1 + o1 * h); put(x2 + h, y2 - o2 * h); put(x2 - h, y2 - o2 * h);
+                } else {
+                    put(x1 - h, y1 - o1 * h); put(x1 + h, y1 - o1 * h); put(x2 + h, y2 + o2 * h); put(x2 - h, y2 + o2 * h);
+                }
+            } else {                   // along x
+                if (x1 > x2) {
+                    put(x1 + o1 * h, y1 + h); put(x1 + o1 * h, y1 - h); put(x2 - o2 * h, y2 - h); put(x2 - o2 * h, y2 + h);
+                } else {
+                    put(x1 - o1 * h, y1 + h); put(x1 - o1 * h, y1 - h); put(x2 + o2 * h, y2 - h); put(x2 + o2 * h, y2 + h);
+                }
+            }
+            close(s.layer);
+        }
+    }
+    for (const Shape &s : c.boxes) {
+        if (s.type != 0 || ignored(s.layer, ign) || s.xy.size() < 4) continue;
+        for (size_t j = 0; j + 2 < s.xy.size(); j += 2) put(s.xy[j], s.xy[j + 1]);
+        close(s.layer);
+    }
+    for (const Ref &r : c.srefs) {
+        if (r.xy.size() != 2) continue;
+        double px, py;
+        t.apply(r.xy[0], r.xy[1], px, py);
+        flatten(cells, r.name, px + xo, py + yo, r.t.after(t), ign, out, depth + 1);
+    }
+    for (const Ref &r : c.arefs) {
+        if (r.xy.size() < 6) continue;
+        const double cx = r.cols >= 2 ? (r.xy[2] - r.xy[0]) / (r.cols - 1.) : 0.;
+        const double rx = r.rows >= 2 ? (r.xy[4] - r.xy[0]) / (r.rows - 1.) : 0.;
+        for (int i = 0; i < r.cols - 1; i++)
+            for (int j = 0; j < r.rows - 1; j++) {
+                const double ix = r.xy[0] + i * cx + j * rx + 0., iy = r.xy[1] + i * cx + j * rx + 0.;
+                double px, py;
+                t.apply(ix, iy, px, py);
+                flatten(cells, r.name, px + xo, py + yo, r.t.after(t), ign, out, depth + 1);
+            }
+    }
+}
+
+}  // namespace
+
+struct g2p_polygons {
+    Flat f;
+};
+
+extern "C" g2p_status g2p_gdsii_read(const char *path, const int32_t *ignore_layers, int32_t n_ignore,
+                                     g2p_polygons **out) {
+    if (!path || !out || n_ignore < 0 || (n_ignore > 0 && !ignore_layers)) {
+        g2p::set_last_message("bad arguments");
+        return G2P_ERR_INVALID;
+    }
+    *out = nullptr;
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) { g2p::set_last_message("cannot open %s", path); return G2P_ERR_INVALID; }
+    std::vector<unsigned char> b;
+    unsigned char buf[65536];
+    size_t n;
+    while ((n = std::fread(buf, 1, sizeof buf, fp)) > 0) b.insert(b.end(), buf, buf + n);
+    std::fclose(fp);
+    try {
+        std::vector<Cell> cells;
+        if (!parse(b, cells) || cells.empty()) {
+            g2p::set_last_message("%s: not a GDSII stream with a cell", path);
+            return G2P_ERR_INVALID;
+        }
+        std::vector<int> ign(ignore_layers, ignore_layers + n_ignore);
+        auto *p = new g2p_polygons();
+        flatten(cells, cells.back().name, 0., 0., Xform(), ign, p->f, 0);
+        *out = p;
+    } catch (const std::exception &e) {
+        g2p::set_last_message("GDSII read: %s", e.what());
+        return G2P_ERR_INVALID;
+    }
+    return G2P_OK;
+}
+
+extern "C" g2p_status g2p_polygons_size(const g2p_polygons *p, int64_t *npoly, int64_t *nvert) {
+    if (!p || !npoly || !nvert) { g2p::set_last_message("bad arguments"); return G2P_ERR_INVALID; }
+    *npoly = (int64_t)p->f.layer.size();
+    *nvert = (int64_t)p->f.x.size();
+    return G2P_OK;
+}
+
+extern "C" g2p_status g2p_polygons_get(const g2p_polygons *p, int32_t *layer, int64_t *vert_ptr, double *x, double *y) {
+    if (!p || !layer || !vert_ptr || !x || !y) { g2p::set_last_message("bad arguments"); return G2P_ERR_INVALID; }
+    std::memcpy(layer, p->f.layer.data(), sizeof(int32_t) * p->f.layer.size());
+    std::memcpy(vert_ptr, p->f.vptr.data(), sizeof(int64_t) * p->f.vptr.size());
+    std::memcpy(x, p->f.x.data(), sizeof(double) * p->f.x.size());
+    std::memcpy(y, p->f.y.data(), sizeof(double) * p->f.y.size());
+    return G2P_OK;
+}
+
+extern "C" void g2p_polygons_free(g2p_polygons *p) { delete p; }

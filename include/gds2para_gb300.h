@@ -226,6 +226,22 @@ g2p_status g2p_mesh_mark(int64_t nx, int64_t ny, int64_t nz, const double *xn, c
                          int32_t *mark_port, uint8_t *cdt_return, int64_t max_cdt, int64_t *side_edge_ptr,
                          int64_t *side_edges, int64_t max_side_edges, double *side_area, int32_t *side_dir);
 
+/* ---- GDSII ingest (host code; the reference reads GDSII with Limbo into
+ * AsciiDataBase and flattens it with saveToMesh, limboint.hpp:2823-3150,
+ * TestMain.cpp:258-292) ----
+ * g2p_gdsii_read flattens the file's last cell (the top cell) into the
+ * conductor polygons the reference stores in fdtdMesh::conductorIn, in the
+ * same order and with the same vertices (metres): boundaries, one rectangle
+ * per path segment, boxes with BOXTYPE 0, then structure and array
+ * references, recursively.  Polygons on the ignored GDSII layers are left
+ * out.  g2p_polygons_get fills layer[npoly], vert_ptr[npoly + 1] (offsets of
+ * each polygon's vertices) and x, y[nvert], sized by g2p_polygons_size. */
+typedef struct g2p_polygons g2p_polygons;
+g2p_status g2p_gdsii_read(const char *path, const int32_t *ignore_layers, int32_t n_ignore, g2p_polygons **out);
+g2p_status g2p_polygons_size(const g2p_polygons *p, int64_t *npoly, int64_t *nvert);
+g2p_status g2p_polygons_get(const g2p_polygons *p, int32_t *layer, int64_t *vert_ptr, double *x, double *y);
+void g2p_polygons_free(g2p_polygons *p);
+
 /* ---- extraction service (no counterpart in the reference, which extracts
  * one layout per process) ----
  * A queue of extraction jobs, each the work of g2p_mesh_create +

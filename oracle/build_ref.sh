@@ -1,7 +1,9 @@
 #!/bin/sh
 # Builds oracle/_ref/ref_pipeline: the reference's own hot-path sources,
 # compiled unmodified from the reference checkout, linked with the project's
-# shims (oracle/ref_shims/) and CPU solver (oracle/solver.c).
+# shims (oracle/ref_shims/) and CPU solver (oracle/solver.c); and
+# oracle/_ref/ref_gds: the reference's GDSII database and saveToMesh
+# (limboint.hpp) with the project's stand-in for Limbo's stream reader.
 # Test infrastructure only; output stays in oracle/_ref/ (git-ignored).
 # usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
 set -e
@@ -17,7 +19,9 @@ g++ $CXXFLAGS -c "$REF/src/generateStiff.cpp" -o "$OUT/generateStiff.o" &
 g++ $CXXFLAGS -c "$REF/src/matrixCon.cpp" -o "$OUT/matrixCon.o" &
 g++ $CXXFLAGS -c "$HERE/ref_shims/mkl_sparse_shim.cpp" -o "$OUT/mkl_sparse_shim.o" &
 g++ $CXXFLAGS -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness.o" &
+g++ $CXXFLAGS -c "$HERE/ref_gds.cpp" -o "$OUT/ref_gds.o" &
 wait
+g++ -o "$OUT/ref_gds" "$OUT/ref_gds.o" -lm
 g++ -o "$OUT/ref_pipeline" "$OUT/ref_harness.o" "$OUT/mesh.o" "$OUT/generateStiff.o" "$OUT/matrixCon.o" \
     "$OUT/mkl_sparse_shim.o" "$OUT/solver.o" -lm
-echo "built $OUT/ref_pipeline"
+echo "built $OUT/ref_pipeline $OUT/ref_gds"
