@@ -23,7 +23,7 @@ EXPORTS = [
     "g2p_mesh_mark",
     "g2p_convert_param", "g2p_write_touchstone", "g2p_write_citi",
     "g2p_ybus_from_param", "g2p_write_xyce", "g2p_write_spef",
-    "g2p_gdsii_read", "g2p_polygons_size", "g2p_polygons_get", "g2p_polygons_free",
+    "g2p_gdsii_read", "g2p_polygons_size", "g2p_polygons_get", "g2p_polygons_free", "g2p_mesh_grid",
 ]
 
 STATUS = {0: "G2P_OK", 1: "G2P_ERR_INVALID", 2: "G2P_ERR_CUDA", 3: "G2P_ERR_NOMEM", 4: "G2P_ERR_NOT_CONVERGED",
@@ -153,6 +153,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_polygons_get.argtypes = [vp, vp, vp, vp, vp]
     L.g2p_polygons_free.argtypes = [vp]
     L.g2p_polygons_free.restype = None
+    L.g2p_mesh_grid.argtypes = [vp, i64, vp, vp, vp, i32, vp, i32, vp, i64, i64, vp, vp, vp, vp, vp, vp]
     for name in EXPORTS:
         if name not in ("g2p_last_error", "g2p_version", "g2p_default_params", "g2p_launch_count",
                         "g2p_profile_begin", "g2p_profile_report", "g2p_profile_buckets", "g2p_polygons_free"):

@@ -141,6 +141,38 @@ def readGDSII(path, ignore_layers=()):
     return layer, vptr, x, y
 
 
+def meshGrid(limits, polygons, port_sides, stack):
+    """The grid lines of the reference's meshAndMark (mesh.cpp:5-330).
+    limits: (xlim1, xlim2, ylim1, ylim2, zlim1, zlim2); polygons: (layer,
+    vert_ptr, x, y) as readGDSII returns them; port_sides: (n, 6) rows
+    x1 y1 z1 x2 y2 z2; stack: (m, 4) rows z_begin z_end eps_r sigma; metres.
+    Returns xn, yn, zn, stack_epsn, stack_sign."""
+    L = _lib.load()
+    lim = _c(limits, np.float64)
+    _, vptr, x, y = polygons
+    vptr, x, y = _c(vptr, np.int64), _c(x, np.float64), _c(y, np.float64)
+    sides = _c(np.asarray(port_sides, np.float64).reshape(-1, 6), np.float64)
+    st = _c(np.asarray(stack, np.float64).reshape(-1, 4), np.float64)
+    counts = np.zeros(3, np.int64)
+    cap_xy = max(16, 4 * (len(x) + 2 * len(sides)) + 1024)
+    cap_z = 2 * (len(st) + len(sides)) + 1
+    for _ in range(2):
+        xn, yn, zn = np.empty(cap_xy), np.empty(cap_xy), np.empty(cap_z)
+        epsn, sign = np.empty(cap_z), np.empty(cap_z)
+        rc = L.g2p_mesh_grid(lim.ctypes.data, len(vptr) - 1, vptr.ctypes.data, x.ctypes.data, y.ctypes.data,
+                             len(sides), sides.ctypes.data if len(sides) else None, len(st), st.ctypes.data, cap_xy,
+                             cap_z, xn.ctypes.data, yn.ctypes.data, zn.ctypes.data, epsn.ctypes.data,
+                             sign.ctypes.data, counts.ctypes.data)
+        if rc == _lib.G2P_OK:
+            nx, ny, nz = (int(v) for v in counts)
+            return xn[:nx].copy(), yn[:ny].copy(), zn[:nz].copy(), epsn[:nz].copy(), sign[:nz].copy()
+        if counts[0] > cap_xy or counts[1] > cap_xy:
+            cap_xy = int(max(counts[0], counts[1]))
+            continue
+        check(rc)
+    check(rc)
+
+
 def generateStiff(sys: FdtdMesh) -> int:
     """generateStiff (src/generateStiff.cpp:6): builds S on the device and
     returns leng_S."""

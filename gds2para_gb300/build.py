@@ -25,9 +25,9 @@ COMMON = ["-O3", "-std=c++17", "--extended-lambda", "-lineinfo", "-Xcompiler", "
 NO_FMA = {"mesh.cu", "v0.cu", "extract.cu"}
 # host code whose results must not depend on the host compiler contracting
 # a * b + c into one rounding (the oracle builds with -ffp-contract=off)
-NO_HOST_CONTRACT = {"gdsii.cu"}
+NO_HOST_CONTRACT = {"ingest.cu"}
 UNITS = ["primitives.cu", "mesh.cu", "v0.cu", "solver.cu", "solve_api.cu", "extract.cu", "noalloc.cu", "serve.cu", "mesher.cu",
-         "network.cu", "gdsii.cu"]
+         "network.cu", "ingest.cu"]
 
 
 def nvcc() -> str:

@@ -1,6 +1,9 @@
-// GDSII ingest: reads a GDSII stream file and flattens its top cell into the
-// conductor polygons that the reference hands to its mesher
-// (fdtdMesh::conductorIn), host code only.
+// Layout ingest, host code only:
+//   * g2p_gdsii_read: reads a GDSII stream file and flattens its top cell
+//     into the conductor polygons that the reference hands to its mesher
+//     (fdtdMesh::conductorIn);
+//   * g2p_mesh_grid: the mesher's grid lines from those polygons, the port
+//     sides and the layer stack (below).
 //
 // The reference reads the stream with Limbo's parser into AsciiDataBase and
 // flattens it with AsciiDataBase::saveToMesh (limboint.hpp:2823-3150, records
@@ -339,3 +342,124 @@ extern "C" g2p_status g2p_polygons_get(const g2p_polygons *p, int32_t *layer, in
 }
 
 extern "C" void g2p_polygons_free(g2p_polygons *p) { delete p; }
+
+// ------------------------------------------------------------ grid lines
+// The grid of the reference's meshAndMark (mesh.cpp:5-330), restated:
+//   * x (and y) candidates are every polygon vertex and both ends of every
+//     port side, sorted.  Walking them with `last` the last coordinate
+//     accepted: a candidate more than disMin but at most disMax from `last`
+//     is kept and becomes `last`; one more than disMax away first gets lines
+//     every disMax from the previous line until within disMax, becomes
+//     `last` only if still more than disMin away, and is kept; any other is
+//     kept without moving `last`.  The kept lines are sorted again and every
+//     line within disMin of the last one kept is merged away.
+//     disMin = 1e-3 * min(x extent, y extent), disMax = 0.005 * extent.
+//   * z candidates are both ends of every stack layer and of every port
+//     side; a sorted candidate within 0.05 * (thinnest layer, or the z
+//     extent) of the previous candidate is merged away.
+//   * each cell layer takes eps and sigma of the stack layer that contains
+//     its midpoint, scanning layers upward from the first when the first
+//     layer starts at the lowest line and downward from the last otherwise;
+//     one more entry repeats the last layer found (the top surface).
+namespace {
+std::vector<double> axis_lines(std::vector<double> o, double dmin, double dmax) {
+    std::sort(o.begin(), o.end());
+    std::vector<double> v{o[0]};
+    double last = o[0];
+    for (size_t i = 1; i < o.size(); i++) {
+        const double d = std::fabs(o[i] - last);
+        if (d > dmin && d <= dmax) {
+            v.push_back(o[i]);
+            last = o[i];
+        } else if (d > dmin) {
+            while (std::fabs(o[i] - last) > dmax) {
+                v.push_back(v.back() + dmax);
+                last = v.back();
+            }
+            if (std::fabs(o[i] - last) > dmin) last = o[i];
+            v.push_back(o[i]);
+        } else {
+            v.push_back(o[i]);
+        }
+    }
+    std::sort(v.begin(), v.end());
+    std::vector<double> out{v[0]};
+    last = v[0];
+    for (size_t i = 1; i < v.size(); i++)
+        if (std::fabs(v[i] - last) > dmin) { out.push_back(v[i]); last = v[i]; }
+    return out;
+}
+}  // namespace
+
+extern "C" g2p_status g2p_mesh_grid(const double *lim, int64_t npoly, const int64_t *vert_ptr, const double *vx,
+                                    const double *vy, int32_t nside, const double *sides, int32_t nstack,
+                                    const double *stack, int64_t cap_xy, int64_t cap_z, double *xn, double *yn,
+                                    double *zn, double *stack_epsn, double *stack_sign, int64_t *counts) {
+    if (!lim || npoly < 0 || nside < 0 || nstack < 1 || !stack || !counts || (npoly > 0 && (!vert_ptr || !vx || !vy)) ||
+        (nside > 0 && !sides)) {
+        g2p::set_last_message("bad arguments");
+        return G2P_ERR_INVALID;
+    }
+    try {
+        std::vector<double> ox, oy, oz;
+        const int64_t nv = npoly > 0 ? vert_ptr[npoly] : 0;
+        for (int64_t i = 0; i < nv; i++) { ox.push_back(vx[i]); oy.push_back(vy[i]); }
+        for (int32_t k = 0; k < nside; k++) {
+            const double *c = sides + 6 * (int64_t)k;
+            ox.push_back(c[0]); oy.push_back(c[1]);
+            ox.push_back(c[3]); oy.push_back(c[4]);
+        }
+        if (ox.empty()) { g2p::set_last_message("no polygon vertices or port sides"); return G2P_ERR_INVALID; }
+        double minlayer = lim[5] - lim[4];
+        for (int32_t k = 0; k < nstack; k++) {
+            const double b = stack[4 * k], e = stack[4 * k + 1];
+            oz.push_back(b);
+            oz.push_back(e);
+            if (e - b > 0) minlayer = std::fmin(minlayer, e - b);
+        }
+        for (int32_t k = 0; k < nside; k++) { oz.push_back(sides[6 * k + 2]); oz.push_back(sides[6 * k + 5]); }
+        const double dmin = 1e-3 * std::fmin(lim[3] - lim[2], lim[1] - lim[0]);
+        const std::vector<double> gx = axis_lines(ox, dmin, 0.005 * (lim[1] - lim[0]));
+        const std::vector<double> gy = axis_lines(oy, dmin, 0.005 * (lim[3] - lim[2]));
+        std::sort(oz.begin(), oz.end());
+        const double dminz = minlayer * 0.05;
+        std::vector<double> gz{oz[0]};
+        for (size_t i = 1; i < oz.size(); i++)
+            if (std::fabs(oz[i] - oz[i - 1]) > dminz) gz.push_back(oz[i]);
+        const int64_t nz = (int64_t)gz.size();
+        std::vector<double> eps, sig;
+        const bool up = stack[0] == gz[0];
+        int32_t j = up ? 0 : nstack - 1;
+        for (int64_t i = 0; i < nz - 1;) {
+            if (j < 0 || j >= nstack) { g2p::set_last_message("grid layer %lld lies in no stack layer", (long long)i); return G2P_ERR_INVALID; }
+            const double mid = (gz[i] + gz[i + 1]) / 2;
+            if (mid >= stack[4 * j] && mid <= stack[4 * j + 1]) {
+                eps.push_back(stack[4 * j + 2]);
+                sig.push_back(stack[4 * j + 3]);
+                i++;
+            } else {
+                j += up ? 1 : -1;
+            }
+        }
+        if (j < 0 || j >= nstack) { g2p::set_last_message("top surface lies in no stack layer"); return G2P_ERR_INVALID; }
+        eps.push_back(stack[4 * j + 2]);
+        sig.push_back(stack[4 * j + 3]);
+        counts[0] = (int64_t)gx.size();
+        counts[1] = (int64_t)gy.size();
+        counts[2] = nz;
+        if (counts[0] > cap_xy || counts[1] > cap_xy || nz > cap_z || !xn || !yn || !zn || !stack_epsn || !stack_sign) {
+            g2p::set_last_message("grid needs %lld x %lld x %lld lines", (long long)counts[0], (long long)counts[1],
+                                  (long long)nz);
+            return G2P_ERR_INVALID;
+        }
+        std::copy(gx.begin(), gx.end(), xn);
+        std::copy(gy.begin(), gy.end(), yn);
+        std::copy(gz.begin(), gz.end(), zn);
+        std::copy(eps.begin(), eps.end(), stack_epsn);
+        std::copy(sig.begin(), sig.end(), stack_sign);
+    } catch (const std::exception &e) {
+        g2p::set_last_message("grid: %s", e.what());
+        return G2P_ERR_INVALID;
+    }
+    return G2P_OK;
+}

@@ -226,7 +226,7 @@ g2p_status g2p_mesh_mark(int64_t nx, int64_t ny, int64_t nz, const double *xn, c
                          int32_t *mark_port, uint8_t *cdt_return, int64_t max_cdt, int64_t *side_edge_ptr,
                          int64_t *side_edges, int64_t max_side_edges, double *side_area, int32_t *side_dir);
 
-/* ---- GDSII ingest (host code; the reference reads GDSII with Limbo into
+/* ---- layout ingest (host code; the reference reads GDSII with Limbo into
  * AsciiDataBase and flattens it with saveToMesh, limboint.hpp:2823-3150,
  * TestMain.cpp:258-292) ----
  * g2p_gdsii_read flattens the file's last cell (the top cell) into the
@@ -241,6 +241,21 @@ g2p_status g2p_gdsii_read(const char *path, const int32_t *ignore_layers, int32_
 g2p_status g2p_polygons_size(const g2p_polygons *p, int64_t *npoly, int64_t *nvert);
 g2p_status g2p_polygons_get(const g2p_polygons *p, int32_t *layer, int64_t *vert_ptr, double *x, double *y);
 void g2p_polygons_free(g2p_polygons *p);
+
+/* The mesher's grid lines (meshAndMark, mesh.cpp:5-330): x/y lines from the
+ * polygon vertices and port-side ends, merged and filled by the reference's
+ * disMin/disMax rules against the limits lim[6] = {xlim1, xlim2, ylim1,
+ * ylim2, zlim1, zlim2}; z lines from the stack layers and port sides; and
+ * per cell layer the eps and sigma of the stack layer containing it, plus the
+ * top surface (stack_epsn, stack_sign: nz entries).  Polygons as
+ * g2p_polygons_get returns them; sides: 6 per port side (x1 y1 z1 x2 y2 z2);
+ * stack: 4 per layer (z begin, z end, eps_r, sigma), all lengths in metres.
+ * counts[3] = {nx, ny, nz} is always set; G2P_ERR_INVALID when nx or ny
+ * exceeds cap_xy or nz exceeds cap_z. */
+g2p_status g2p_mesh_grid(const double *lim, int64_t npoly, const int64_t *vert_ptr, const double *vx, const double *vy,
+                         int32_t nside, const double *sides, int32_t nstack, const double *stack, int64_t cap_xy,
+                         int64_t cap_z, double *xn, double *yn, double *zn, double *stack_epsn, double *stack_sign,
+                         int64_t *counts);
 
 /* ---- extraction service (no counterpart in the reference, which extracts
  * one layout per process) ----

@@ -21,7 +21,7 @@ g++ $CXXFLAGS -c "$HERE/ref_shims/mkl_sparse_shim.cpp" -o "$OUT/mkl_sparse_shim.
 g++ $CXXFLAGS -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness.o" &
 g++ $CXXFLAGS -c "$HERE/ref_gds.cpp" -o "$OUT/ref_gds.o" &
 wait
-g++ -o "$OUT/ref_gds" "$OUT/ref_gds.o" -lm
+g++ -o "$OUT/ref_gds" "$OUT/ref_gds.o" "$OUT/mesh.o" "$OUT/mkl_sparse_shim.o" -lm
 g++ -o "$OUT/ref_pipeline" "$OUT/ref_harness.o" "$OUT/mesh.o" "$OUT/generateStiff.o" "$OUT/matrixCon.o" \
     "$OUT/mkl_sparse_shim.o" "$OUT/solver.o" -lm
 echo "built $OUT/ref_pipeline $OUT/ref_gds"

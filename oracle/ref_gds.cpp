@@ -5,11 +5,26 @@
  * "P layer nvert x0 y0 x1 y1 ..." (metres, %.17g); other lines are the
  * reference's own messages.  The top cell is the last
  * cell of the file, as the reference's command-line driver takes it.
+ * With --grid <settings>, it then fills the remaining fdtdMesh members the
+ * way the reference's convertToFDTDMesh does (solnoutclass.hpp:5894-5984):
+ * limits, the layer stack, each polygon's z range from the stack layer with
+ * its GDSII number, the port sides; runs the reference's meshAndMark
+ * (mesh.cpp:5) and prints its grid lines and per-layer constants as lines
+ * "X x0 x1 ...", "Y ...", "Z ...", "E eps ...", "S sigma ...".  The settings
+ * file holds: xlim1 xlim2 ylim1 ylim2 zlim1 zlim2 / nstack, then per layer
+ * "z_begin z_end eps sigma gdsii_number" / nport, then per port side
+ * "x1 y1 z1 x2 y2 z2 direction" (one side per port), all lengths in metres.
  * TEST INFRASTRUCTURE ONLY: built by oracle/build_ref.sh into oracle/_ref/.
- * usage: ref_gds <file.gds> [ignored GDSII layer ...] */
+ * usage: ref_gds <file.gds> [--grid settings] [ignored GDSII layer ...] */
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <unordered_set>
 #include "limboint.hpp"
+
+int meshAndMark(fdtdMesh *sys, unordered_map<double, int> &xi, unordered_map<double, int> &yi,
+                unordered_map<double, int> &zi, unordered_set<double> *portCoorx, unordered_set<double> *portCoory);
 
 int main(int argc, char **argv) {
     if (argc < 2) { fprintf(stderr, "usage: ref_gds <file.gds> [ignored layer ...]\n"); return 2; }
@@ -18,7 +33,11 @@ int main(int argc, char **argv) {
     GdsParser::GdsReader rd(adb);
     if (!rd(argv[1])) { fprintf(stderr, "cannot read %s\n", argv[1]); return 3; }
     std::vector<int> ignore;
-    for (int i = 2; i < argc; i++) ignore.push_back(atoi(argv[i]));
+    const char *grid = nullptr;
+    for (int i = 2; i < argc; i++) {
+        if (!strcmp(argv[i], "--grid") && i + 1 < argc) grid = argv[++i];
+        else ignore.push_back(atoi(argv[i]));
+    }
     fdtdMesh sys;
     const std::string top = adb.getCell(adb.getNumCell() - 1).getCellName();
     adb.saveToMesh(top, {0., 0.}, strans(), &sys, ignore);
@@ -28,5 +47,61 @@ int main(int argc, char **argv) {
         for (int v = 0; v < c.numVert; v++) printf(" %.17g %.17g", c.x[v], c.y[v]);
         printf("\n");
     }
+    if (!grid) return 0;
+    std::ifstream in(grid);
+    double lim[6];
+    for (double &v : lim) in >> v;
+    sys.xlim1 = lim[0]; sys.xlim2 = lim[1]; sys.ylim1 = lim[2]; sys.ylim2 = lim[3]; sys.zlim1 = lim[4]; sys.zlim2 = lim[5];
+    int ns = 0;
+    in >> ns;
+    sys.numStack = ns;
+    std::vector<int> gds(ns);
+    for (int k = 0; k < ns; k++) {
+        double b, e, eps, sig;
+        in >> b >> e >> eps >> sig >> gds[k];
+        sys.stackBegCoor.push_back(b); sys.stackEndCoor.push_back(e);
+        sys.stackEps.push_back(eps); sys.stackSig.push_back(sig);
+        sys.stackName.push_back(std::to_string(gds[k]));
+    }
+    sys.numCdtRow = (int)sys.conductorIn.size();
+    sys.stackCdtMark = (double *)calloc(ns > 0 ? ns : 1, sizeof(double));
+    for (int i = 0; i < sys.numCdtRow; i++)
+        for (int k = 0; k < ns; k++)
+            if (sys.conductorIn[i].layer == gds[k]) {
+                sys.conductorIn[i].zmin = sys.stackBegCoor[k];
+                sys.conductorIn[i].zmax = sys.stackEndCoor[k];
+                sys.stackCdtMark[k] = 1;
+            }
+    int np = 0;
+    in >> np;
+    sys.numPorts = np;
+    unordered_set<double> pcx, pcy;
+    for (int p = 0; p < np; p++) {
+        double c[6];
+        int dir;
+        for (double &v : c) in >> v;
+        in >> dir;
+        sys.portCoor.emplace_back(fdtdPort());
+        fdtdPort &pc = sys.portCoor.back();
+        pc.x1.push_back(c[0]); pc.y1.push_back(c[1]); pc.z1.push_back(c[2]);
+        pc.x2.push_back(c[3]); pc.y2.push_back(c[4]); pc.z2.push_back(c[5]);
+        pc.multiplicity = 1;
+        pc.portDirection.push_back(dir);
+        if (c[0] == c[3]) pcx.insert(c[0]);
+        if (c[1] == c[4]) pcy.insert(c[1]);
+    }
+    unordered_map<double, int> xi, yi, zi;
+    const int st = meshAndMark(&sys, xi, yi, zi, &pcx, &pcy);
+    auto line = [](const char *tag, const double *v, long n) {
+        printf("%s", tag);
+        for (long i = 0; i < n; i++) printf(" %.17g", v[i]);
+        printf("\n");
+    };
+    line("X", sys.xn, sys.nx);
+    line("Y", sys.yn, sys.ny);
+    line("Z", sys.zn, sys.nz);
+    line("E", sys.stackEpsn.data(), (long)sys.stackEpsn.size());
+    line("S", sys.stackSign.data(), (long)sys.stackSign.size());
+    printf("STATUS %d\n", st);
     return 0;
 }

@@ -11,8 +11,13 @@ x and y in both directions and a diagonal one, references with mirroring,
 rotation, magnification and the absolute flags, nested references, and array
 references.
 
+It also runs the reference's meshAndMark on two of the layouts with made-up
+limits, layer stacks and port sides (GRID_CASES) and stores its grid lines
+and per-layer constants.
+
 When the reference's example designs are present (argument: their folder),
-the library's reader is also compared with the reference on each of them.
+the library's reader and grid are also compared with the reference on each
+of them (the grid where the .sim_input names its layers by GDSII number).
 
 usage: python tests/golden/make_gds_golden.py [examples_dir]
 """
@@ -147,6 +152,66 @@ def cases():
     return {"flat": (flat, []), "hier": (hier, []), "hier_ignore": (hier, [11, 13])}
 
 
+# Grid cases: limits, stack layers (z begin, z end, eps_r, sigma, GDSII layer)
+# and port sides (x1 y1 z1 x2 y2 z2 direction), in metres, for the layouts
+# above; run through the reference's meshAndMark by ref_gds --grid.
+GRID_CASES = {
+    "flat": ((-1e-6, 9e-6, -1e-6, 1e-5, 0.0, 6e-6),
+             [(0.0, 1e-6, 3.9, 0.0, 100), (1e-6, 2e-6, 3.9, 5.8e7, 1), (2e-6, 2.5e-6, 2.5, 5.8e7, 2),
+              (2.5e-6, 3e-6, 2.5, 5.8e7, 3), (3e-6, 3.2e-6, 2.5, 5.8e7, 4), (3.2e-6, 4e-6, 4.2, 5.8e7, 5),
+              (4e-6, 6e-6, 3.9, 0.0, 101)],
+             [(2e-6, 1e-6, 2e-6, 2e-6, 1e-6, 1e-6, -1), (3e-6, 5e-6, 3.2e-6, 3e-6, 5e-6, 3e-6, 1)]),
+    "hier": ((-4e-4, 4e-4, -4e-4, 4e-4, 0.0, 5e-6),
+             [(0.0, 1e-6, 3.9, 0.0, 100), (1e-6, 1.5e-6, 3.2, 5.8e7, 10), (1.5e-6, 2e-6, 3.2, 5.8e7, 11),
+              (2e-6, 3e-6, 2.7, 5.8e7, 12), (3e-6, 3.5e-6, 2.7, 5.8e7, 13), (3.5e-6, 5e-6, 3.9, 0.0, 101)],
+             [(5e-6, 2e-6, 1.5e-6, 5e-6, 2e-6, 0.0, 1)]),
+}
+
+
+def grid_settings(lim, stack, sides):
+    out = " ".join(repr(v) for v in lim) + "\n%d\n" % len(stack)
+    out += "".join("%r %r %r %r %d\n" % layer for layer in stack)
+    return out + "%d\n" % len(sides) + "".join(" ".join(repr(v) for v in sd[:6]) + " %d\n" % sd[6] for sd in sides)
+
+
+def run_ref_grid(gds_bytes, settings):
+    with tempfile.TemporaryDirectory() as d:
+        gp, sp = os.path.join(d, "in.gds"), os.path.join(d, "in.txt")
+        with open(gp, "wb") as f:
+            f.write(gds_bytes)
+        with open(sp, "w") as f:
+            f.write(settings)
+        out = subprocess.run([REF_GDS, gp, "--grid", sp], check=True, capture_output=True, text=True).stdout
+    lines = {t[0]: np.array([float(v) for v in t[1:]]) for t in (l.split() for l in out.splitlines())
+             if t and t[0] in ("X", "Y", "Z", "E", "S")}
+    return [lines[k] for k in "XYZES"]
+
+
+def sim_input_settings(path):
+    """Limits, stack and port sides of a .sim_input file in metres (stack
+    layers must be named by GDSII number); None when the file does not fit."""
+    import re
+    t = [line.split("#")[0].strip() for line in open(path)]
+    t = [line for line in t if line]
+    try:
+        i = t.index("TOTAL SIZE")
+        lu = float(t[i + 2].split("=")[1])
+        lim = [float(v) * lu for v in t[i + 1].split()]
+        j = t.index("DIELECTRIC STACK")
+        stack = []
+        for line in t[j + 2:j + 2 + int(t[j + 1].split("=")[1])]:
+            kv = dict(re.findall(r"(\w+)\s*=\s*([-+.\deE]+)", line))
+            z, h = float(kv["z"]), float(kv["h"])
+            stack.append((z * lu, (z + h) * lu, float(kv["e"]), float(kv.get("sigma", 0.0)),
+                          int(line.split()[0].lstrip("M"))))
+        k = t.index("PORT")
+        sides = [[float(v) * lu for v in line.split()[1:7]] + [int(line.split()[7])]
+                 for line in t[k + 2:k + 2 + int(t[k + 1].split("=")[1])]]
+    except (ValueError, IndexError, KeyError):
+        return None
+    return lim, stack, sides
+
+
 def run_ref(gds_bytes, ignore):
     with tempfile.NamedTemporaryFile(suffix=".gds", delete=False) as f:
         f.write(gds_bytes)
@@ -184,6 +249,15 @@ def main():
         arrays[f"{name}_layer"], arrays[f"{name}_vptr"] = layer, vptr
         arrays[f"{name}_x"], arrays[f"{name}_y"] = x, y
         print(f"{name}: {len(layer)} polygons")
+    all_cases = cases()
+    for name, (lim, stack, sides) in GRID_CASES.items():
+        grid = run_ref_grid(all_cases[name][0], grid_settings(lim, stack, sides))
+        arrays[f"{name}_grid_lim"] = np.array(lim)
+        arrays[f"{name}_grid_stack"] = np.array([layer[:4] for layer in stack])
+        arrays[f"{name}_grid_sides"] = np.array([sd[:6] for sd in sides])
+        for key, v in zip("XYZES", grid):
+            arrays[f"{name}_grid_{key}"] = v
+        print(f"{name} grid: {len(grid[0])} x {len(grid[1])} x {len(grid[2])} lines")
     np.savez_compressed(os.path.join(ROOT, "tests", "golden", "gdsii_cases.npz"), **arrays)
     if len(sys.argv) > 1:
         sys.path.insert(0, ROOT)
@@ -196,7 +270,17 @@ def main():
             want = parse_ref(subprocess.run([REF_GDS, path], check=True, capture_output=True, text=True).stdout)
             got = api.readGDSII(path)
             same = all(np.array_equal(a, b) for a, b in zip(got, want))
-            print(f"{fn}: {len(want[0])} polygons, library {'identical' if same else 'DIFFERS'}")
+            msg = f"{fn}: {len(want[0])} polygons, library {'identical' if same else 'DIFFERS'}"
+            sim = path[:-4] + ".sim_input"
+            st = sim_input_settings(sim) if os.path.exists(sim) else None
+            if st:
+                lim, stack, sides = st
+                with open(path, "rb") as f:
+                    ref_grid = run_ref_grid(f.read(), grid_settings(lim, stack, sides))
+                grid = api.meshGrid(lim, got, [sd[:6] for sd in sides], [layer[:4] for layer in stack])
+                same = all(np.array_equal(a, b) for a, b in zip(grid, ref_grid))
+                msg += f"; grid {len(grid[0])} x {len(grid[1])} x {len(grid[2])}, {'identical' if same else 'DIFFERS'}"
+            print(msg)
 
 
 if __name__ == "__main__":

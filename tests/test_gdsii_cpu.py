@@ -51,3 +51,34 @@ def test_gdsii_rejects_missing_and_malformed_files(tmp_path):
     bad.write_bytes(b"\x00\x02\x00\x00not gdsii")
     with pytest.raises(G2PError):
         api.readGDSII(bad)
+
+
+@pytest.mark.parametrize("case", ["flat", "hier"])
+def test_mesh_grid_matches_reference_mesher(tmp_path, case):
+    """Grid lines and per-layer constants (g2p_mesh_grid) against the
+    reference's own meshAndMark on the same polygons, limits, layer stack
+    and port sides (mesh.cpp:5-330): bit-exact."""
+    api = _api_or_skip()
+    g = np.load(GOLDEN)
+    path = tmp_path / f"{case}.gds"
+    path.write_bytes(g[f"{case}_gds"].tobytes())
+    polys = api.readGDSII(path)
+    got = api.meshGrid(g[f"{case}_grid_lim"], polys, g[f"{case}_grid_sides"], g[f"{case}_grid_stack"])
+    for key, v in zip("XYZES", got):
+        np.testing.assert_array_equal(v, g[f"{case}_grid_{key}"], err_msg=key)
+    # lines ascend and the merge leaves none within disMin of the previous
+    lim = g[f"{case}_grid_lim"]
+    dmin = 1e-3 * min(lim[1] - lim[0], lim[3] - lim[2])
+    assert np.diff(got[0]).min() > dmin and np.diff(got[1]).min() > dmin
+
+
+def test_mesh_grid_rejects_a_stack_that_misses_the_grid(tmp_path):
+    api = _api_or_skip()
+    from gds2para_gb300._lib import G2PError
+    g = np.load(GOLDEN)
+    path = tmp_path / "flat.gds"
+    path.write_bytes(g["flat_gds"].tobytes())
+    polys = api.readGDSII(path)
+    with pytest.raises(G2PError):
+        # one layer covering only the lower half of the z range
+        api.meshGrid(g["flat_grid_lim"], polys, [(0, 0, 5e-6, 0, 0, 6e-6)], [(0.0, 1e-6, 3.9, 0.0)])
