@@ -362,7 +362,12 @@ extern "C" void g2p_polygons_free(g2p_polygons *p) { delete p; }
 //     layer starts at the lowest line and downward from the last otherwise;
 //     one more entry repeats the last layer found (the top surface).
 namespace {
-std::vector<double> axis_lines(std::vector<double> o, double dmin, double dmax) {
+constexpr double kMaxGridLines = 67108864.0;   // 2^26 lines per axis
+
+// The fill loop gives up once more than `cap` lines have been placed and sets
+// *over (a guard: the caller sizes `cap` from the vertex span, which bounds
+// the fill).
+std::vector<double> axis_lines(std::vector<double> o, double dmin, double dmax, int64_t cap, bool *over) {
     std::sort(o.begin(), o.end());
     std::vector<double> v{o[0]};
     double last = o[0];
@@ -373,6 +378,7 @@ std::vector<double> axis_lines(std::vector<double> o, double dmin, double dmax) 
             last = o[i];
         } else if (d > dmin) {
             while (std::fabs(o[i] - last) > dmax) {
+                if ((int64_t)v.size() > cap) { *over = true; return v; }
                 v.push_back(v.back() + dmax);
                 last = v.back();
             }
@@ -410,6 +416,13 @@ extern "C" g2p_status g2p_mesh_grid(const double *lim, int64_t npoly, const int6
             ox.push_back(c[3]); oy.push_back(c[4]);
         }
         if (ox.empty()) { g2p::set_last_message("no polygon vertices or port sides"); return G2P_ERR_INVALID; }
+        for (int k = 0; k < 6; k++)
+            if (!std::isfinite(lim[k])) { g2p::set_last_message("layout limits must be finite"); return G2P_ERR_INVALID; }
+        if (!(lim[1] > lim[0]) || !(lim[3] > lim[2])) {
+            g2p::set_last_message("layout limits need xlim2 > xlim1 and ylim2 > ylim1 (got %g..%g, %g..%g)", lim[0],
+                                  lim[1], lim[2], lim[3]);
+            return G2P_ERR_INVALID;
+        }
         double minlayer = lim[5] - lim[4];
         for (int32_t k = 0; k < nstack; k++) {
             const double b = stack[4 * k], e = stack[4 * k + 1];
@@ -419,8 +432,27 @@ extern "C" g2p_status g2p_mesh_grid(const double *lim, int64_t npoly, const int6
         }
         for (int32_t k = 0; k < nside; k++) { oz.push_back(sides[6 * k + 2]); oz.push_back(sides[6 * k + 5]); }
         const double dmin = 1e-3 * std::fmin(lim[3] - lim[2], lim[1] - lim[0]);
-        const std::vector<double> gx = axis_lines(ox, dmin, 0.005 * (lim[1] - lim[0]));
-        const std::vector<double> gy = axis_lines(oy, dmin, 0.005 * (lim[3] - lim[2]));
+        // Each axis gets at most (vertex span / disMax) fill lines besides its
+        // candidates; a span that would need more than 2^26 lines is refused
+        // before any is placed.
+        auto fill_bound = [](const std::vector<double> &o, double dmax) {
+            const auto mm = std::minmax_element(o.begin(), o.end());
+            return (*mm.second - *mm.first) / dmax + (double)o.size() + 1;
+        };
+        const double dmax_x = 0.005 * (lim[1] - lim[0]), dmax_y = 0.005 * (lim[3] - lim[2]);
+        const double bx = fill_bound(ox, dmax_x), by = fill_bound(oy, dmax_y);
+        if (!(bx < kMaxGridLines) || !(by < kMaxGridLines)) {
+            g2p::set_last_message("grid would need more than %lld lines along %s: the vertices span far more than "
+                                  "the layout limits", (long long)kMaxGridLines, bx < kMaxGridLines ? "y" : "x");
+            return G2P_ERR_INVALID;
+        }
+        bool over_x = false, over_y = false;
+        const std::vector<double> gx = axis_lines(ox, dmin, dmax_x, (int64_t)bx, &over_x);
+        const std::vector<double> gy = axis_lines(oy, dmin, dmax_y, (int64_t)by, &over_y);
+        if (over_x || over_y) {
+            g2p::set_last_message("grid fill along %s exceeded its bound", over_x ? "x" : "y");
+            return G2P_ERR_INVALID;
+        }
         std::sort(oz.begin(), oz.end());
         const double dminz = minlayer * 0.05;
         std::vector<double> gz{oz[0]};

@@ -33,7 +33,9 @@ std::mutex g_addr_mu;
 int64_t *g_addr[kMaxDevices];
 
 // Address of the buffer on the current device, looked up on the first call
-// made with that device current.
+// made with that device current and kept for the life of the process.  The
+// cache does not survive cudaDeviceReset (which unloads the module): a
+// process that resets a device must not call this entry point afterwards.
 g2p_status partials_on_current_device(int64_t **out) {
     int dev = -1;
     G2P_CUDA(cudaGetDevice(&dev));
@@ -108,8 +110,9 @@ extern "C" g2p_status g2p_map_edge_noalloc(int64_t nx, int64_t ny, int64_t nz, c
         return G2P_ERR_INVALID;
     }
     if (nx > (int64_t)1 << 20 || ny > (int64_t)1 << 20 || nz > (int64_t)1 << 20) {
-        set_last_message("g2p_map_edge_noalloc: grid %lld x %lld x %lld exceeds its limit of %lld edges",
-                         (long long)nx, (long long)ny, (long long)nz, (long long)kNoAllocMaxEdges);
+        set_last_message("g2p_map_edge_noalloc: grid %lld x %lld x %lld has more than 2^20 (1,048,576) nodes "
+                         "along an axis",
+                         (long long)nx, (long long)ny, (long long)nz);
         return G2P_ERR_INVALID;
     }
     Dims d;

@@ -284,23 +284,25 @@ g2p_status g2p_server_wait(g2p_server *s, int64_t job, double *z_out, g2p_extrac
 /* Finishes the queued and running jobs, then frees the server. */
 g2p_status g2p_server_destroy(g2p_server *s);
 
-/* ---- setMapEdge without device allocation (no counterpart in the
- * reference; its nearest reference code is setMapEdge, src/fdtd.hpp:1444-1529,
- * with the PEC edges of src/mesh.cpp:943-987) ----
+/* ---- edge map without device allocation (no counterpart in the
+ * reference) ----
  * Same map_edge and bden as g2p_index_maps, on device pointers and without
  * a mesh handle, for callers that cannot let the library take device memory:
  * a host runtime whose own arena or caching allocator holds the device's
  * memory, or a per-layout loop on a fixed latency budget.  Its one temporary
  * (the scan's per-tile partial sums) is a static 256 KiB device buffer, so
- * it takes at most 67,106,816 edges (32,767 tiles of 2,048) and returns
- * G2P_ERR_INVALID, with the limit in g2p_last_error, beyond that.
+ * it takes at most 67,106,816 edges (32,767 tiles of 2,048) and at most
+ * 2^20 nodes along each axis, and returns G2P_ERR_INVALID, with the limit in
+ * g2p_last_error, beyond either.
  * mark_edge [N_edge] and cdt_return [num_cdt] are inputs; map_edge [N_edge]
  * and bden [1] are outputs; all four must be device, managed or mapped
  * pinned host memory.  Nothing needs to be zeroed first.  Work is queued on
  * `stream` (a cudaStream_t; NULL = the default stream) and the call returns
  * without synchronizing.  The first call on each device also looks the
  * buffer's address up (cudaGetSymbolAddress, which can load the module):
- * make that first call outside any stream capture.  All calls on one device
+ * make that first call outside any stream capture.  That address is kept
+ * for the life of the process and does not survive cudaDeviceReset: do not
+ * call this entry point on a device after resetting it.  All calls on one device
  * share the buffer, so two calls whose work can overlap on the device (other
  * streams, other host threads) race: order them on one stream or with
  * events. */

@@ -5,9 +5,10 @@
 # oracle/_ref/ref_gds: the reference's GDSII database and saveToMesh
 # (limboint.hpp) with the project's stand-in for Limbo's stream reader.
 # Test infrastructure only; output stays in oracle/_ref/ (git-ignored).
-# usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+# usage: oracle/build_ref.sh [reference_root]
+#   (default: $G2P_REFERENCE_ROOT, else /root/reference)
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${G2P_REFERENCE_ROOT:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 [ -f "$REF/src/fdtd.hpp" ] || { echo "reference sources not found under $REF" >&2; exit 1; }

@@ -181,7 +181,10 @@ def run_ref_grid(gds_bytes, settings):
             f.write(gds_bytes)
         with open(sp, "w") as f:
             f.write(settings)
-        out = subprocess.run([REF_GDS, gp, "--grid", sp], check=True, capture_output=True, text=True).stdout
+        # the reference's meshAndMark writes debug dumps (x.txt, cond.txt, ...)
+        # into its working directory: keep them in the temporary one
+        out = subprocess.run([REF_GDS, gp, "--grid", sp], check=True, capture_output=True, text=True,
+                             cwd=d).stdout
     lines = {t[0]: np.array([float(v) for v in t[1:]]) for t in (l.split() for l in out.splitlines())
              if t and t[0] in ("X", "Y", "Z", "E", "S")}
     return [lines[k] for k in "XYZES"]
@@ -218,7 +221,7 @@ def run_ref(gds_bytes, ignore):
         name = f.name
     try:
         out = subprocess.run([REF_GDS, name] + [str(i) for i in ignore], check=True, capture_output=True,
-                             text=True).stdout
+                             text=True, cwd=tempfile.gettempdir()).stdout
     finally:
         os.unlink(name)
     return parse_ref(out)
@@ -267,7 +270,8 @@ def main():
             if not fn.endswith(".gds"):
                 continue
             path = os.path.join(folder, fn)
-            want = parse_ref(subprocess.run([REF_GDS, path], check=True, capture_output=True, text=True).stdout)
+            want = parse_ref(subprocess.run([REF_GDS, path], check=True, capture_output=True, text=True,
+                                            cwd=tempfile.gettempdir()).stdout)
             got = api.readGDSII(path)
             same = all(np.array_equal(a, b) for a, b in zip(got, want))
             msg = f"{fn}: {len(want[0])} polygons, library {'identical' if same else 'DIFFERS'}"

@@ -7,8 +7,8 @@ stores what it produced.  Arrays up to SMALL elements are stored whole;
 larger ones as a SHA-256 of their bytes plus a few statistics, which is
 enough to check bit-exact integer and FP64 results.
 
-Needs the reference checkout (default /root/reference); the fixtures it
-writes are self-contained.  Usage:
+Needs the reference checkout (the argument, else $G2P_REFERENCE_ROOT, else
+/root/reference); the fixtures it writes are self-contained.  Usage:
     python tests/golden/make_golden.py [reference_root]
 """
 from __future__ import annotations
@@ -53,7 +53,7 @@ def make_layout(gen: str, kw: dict):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("G2P_REFERENCE_ROOT", "/root/reference")
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), ref])
     for name, (gen, kw) in CASES.items():
         d = make_layout(gen, kw)

@@ -82,3 +82,26 @@ def test_mesh_grid_rejects_a_stack_that_misses_the_grid(tmp_path):
     with pytest.raises(G2PError):
         # one layer covering only the lower half of the z range
         api.meshGrid(g["flat_grid_lim"], polys, [(0, 0, 5e-6, 0, 0, 6e-6)], [(0.0, 1e-6, 3.9, 0.0)])
+
+
+def test_mesh_grid_rejects_empty_limits_and_runaway_fills(tmp_path):
+    """Limits with no x or y extent (disMax = 0) and limits so small against
+    the vertices' span that the disMax fill would need billions of lines are
+    refused before any line is placed."""
+    api = _api_or_skip()
+    from gds2para_gb300._lib import G2PError
+    g = np.load(GOLDEN)
+    path = tmp_path / "flat.gds"
+    path.write_bytes(g["flat_gds"].tobytes())
+    polys = api.readGDSII(path)
+    lim = np.array(g["flat_grid_lim"], np.float64)
+    sides, stack = g["flat_grid_sides"], g["flat_grid_stack"]
+    for bad in ((1, lim[0]), (1, lim[0] - 1e-6), (3, lim[2]), (2, float("nan"))):
+        l2 = lim.copy()
+        l2[bad[0]] = bad[1]
+        with pytest.raises(G2PError):
+            api.meshGrid(l2, polys, sides, stack)
+    tiny = lim.copy()
+    tiny[1] = tiny[0] + 1e-15          # disMax = 5e-18 m against micron spans
+    with pytest.raises(G2PError, match="lines along"):
+        api.meshGrid(tiny, polys, sides, stack)

@@ -66,6 +66,12 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
                                 None)
     assert st == 1
     assert b"67106816" in L.g2p_last_error()
+    # An axis longer than 2^20 nodes is refused by its own check, whatever the
+    # edge count says.
+    st = L.g2p_map_edge_noalloc((1 << 20) + 1, 3, 3, buf.data_ptr(), cr.data_ptr(), 1, buf.data_ptr(),
+                                buf.data_ptr(), None)
+    assert st == 1
+    assert b"2^20" in L.g2p_last_error()
     # Host memory the device cannot address is refused too.
     host = np.zeros(64, np.int64)
     st = L.g2p_map_edge_noalloc(3, 3, 3, host.ctypes.data, cr.data_ptr(), 1, buf.data_ptr(), buf.data_ptr(), None)
