@@ -25,4 +25,16 @@ wait
 g++ -o "$OUT/ref_gds" "$OUT/ref_gds.o" "$OUT/mesh.o" "$OUT/mkl_sparse_shim.o" -lm
 g++ -o "$OUT/ref_pipeline" "$OUT/ref_harness.o" "$OUT/mesh.o" "$OUT/generateStiff.o" "$OUT/matrixCon.o" \
     "$OUT/mkl_sparse_shim.o" "$OUT/solver.o" -lm
+# oracle/_ref/ref_pipeline_gb300: the same harness with generateStiff,
+# hypreSolve and paraGenerator taken from the library's reference-side shim
+# (oracle/gb300_path.cpp), linked with libgds2para_gb300.so when it is built
+LIB="$HERE/../gds2para_gb300/_build"
+if [ -f "$LIB/libgds2para_gb300.so" ]; then
+    g++ $CXXFLAGS -I"$HERE/../include" -c "$HERE/gb300_path.cpp" -o "$OUT/gb300_path.o" &
+    g++ $CXXFLAGS -DG2P_REF_WITH_GB300_SHIM -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness_gb300.o" &
+    wait
+    g++ -o "$OUT/ref_pipeline_gb300" "$OUT/ref_harness_gb300.o" "$OUT/mesh.o" "$OUT/gb300_path.o" \
+        "$OUT/mkl_sparse_shim.o" -L"$LIB" -lgds2para_gb300 -Wl,-rpath,"$LIB" -lm
+    echo "built $OUT/ref_pipeline_gb300"
+fi
 echo "built $OUT/ref_pipeline $OUT/ref_gds"

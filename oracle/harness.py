@@ -96,6 +96,13 @@ class COracle:
         L.g2po_solve_coo.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                                      C.c_void_p, C.POINTER(SolverOpts), C.POINTER(SolveStats)]
 
+        L.g2po_job_create.restype = C.c_void_p
+        L.g2po_job_create.argtypes = [C.POINTER(_Mesh), C.POINTER(ParaStats)]
+        L.g2po_job_port_stage.argtypes = [C.c_void_p, C.c_int, C.POINTER(SolverOpts), C.POINTER(SolveStats),
+                                          C.POINTER(C.c_double)]
+        L.g2po_job_z.argtypes = [C.c_void_p, C.c_void_p]
+        L.g2po_job_destroy.argtypes = [C.c_void_p]
+
     def _mesh(self, d):
         keep = {
             "xn": _arr(d.xn, np.float64), "yn": _arr(d.yn, np.float64), "zn": _arr(d.zn, np.float64),
@@ -180,6 +187,11 @@ class COracle:
         zc = z[0::2] + 1j * z[1::2]
         return zc.reshape(d.nfreq, d.num_ports, d.num_ports), st
 
+    def job(self, d):
+        """The extraction as a job whose ports can run on several host
+        threads (g2po_job_*); see OracleJob."""
+        return OracleJob(self, d)
+
     def solve_csr(self, ptr, col, val, b, opts: SolverOpts = None):
         n = len(ptr) - 1
         rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(ptr))
@@ -238,3 +250,54 @@ def run_reference(d, workdir: str = None, skip_stiff: bool = False, skip_para: b
             out[k] = int(v)
     out["_log"] = r.stderr
     return out
+
+
+class OracleJob:
+    """One V0 extraction on the host: the assembly happens at construction
+    (index maps, V0d/Ad, V0c/Ac); stage(k, threads) then runs solve k of
+    every port (0: Ad, 1: Ac, 2: Ad, each with its own AMG setup as
+    hypreSolve does), the ports spread over host threads (ctypes releases
+    the GIL during each call).  z() gives Z once stage 2 has run."""
+
+    def __init__(self, oracle: "COracle", d):
+        self.O, self.d = oracle, d
+        self.m = oracle._mesh(d)
+        self.st = ParaStats()
+        self.h = oracle.lib.g2po_job_create(C.byref(self.m), C.byref(self.st))
+        self.iterations = 0
+        self.max_rel_residual = 0.0
+
+    def stage(self, k: int, opts: SolverOpts, threads: int = 1):
+        import concurrent.futures as cf
+
+        def one(p):
+            ss, ts = SolveStats(), C.c_double()
+            rc = self.O.lib.g2po_job_port_stage(self.h, p, C.byref(opts), C.byref(ss), C.byref(ts))
+            if rc != 0:
+                raise RuntimeError(f"g2po_job_port_stage(port {p}, stage {k}) failed")
+            return ss.iterations, ss.rel_residual
+
+        ports = range(self.d.num_ports)
+        if threads <= 1:
+            res = [one(p) for p in ports]
+        else:
+            with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+                res = list(ex.map(one, ports))
+        for it, rel in res:
+            self.iterations += it
+            self.max_rel_residual = max(self.max_rel_residual, rel)
+
+    def z(self):
+        d = self.d
+        z = np.zeros(2 * d.nfreq * d.num_ports * d.num_ports, np.float64)
+        self.O.lib.g2po_job_z(self.h, z.ctypes.data_as(C.c_void_p))
+        zc = z[0::2] + 1j * z[1::2]
+        return zc.reshape(d.nfreq, d.num_ports, d.num_ports)
+
+    def close(self):
+        if self.h:
+            self.O.lib.g2po_job_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

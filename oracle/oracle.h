@@ -116,6 +116,19 @@ typedef struct {
 int g2po_para_generator(const g2po_mesh *m, const g2po_solver_opts *o, int max_ports,
                         double *z_out, g2po_para_stats *st);
 
+/* The same extraction as a job whose ports can run on several host threads:
+ * g2po_job_create does the assembly (index maps, V0d/Ad, V0c/Ac; the mesh
+ * must outlive the job); g2po_job_port_stage runs port p's next solve
+ * (0: Ad, 1: Ac, 2: Ad and the port's Z column), each with its own AMG setup
+ * as hypreSolve does.  Calls for different ports may run concurrently;
+ * calls for one port must be ordered.  g2po_job_z writes Z as
+ * g2po_para_generator does. */
+typedef struct g2po_job g2po_job;
+g2po_job *g2po_job_create(const g2po_mesh *m, g2po_para_stats *st);
+int g2po_job_port_stage(g2po_job *j, int port, const g2po_solver_opts *o, g2po_solve_stats *ss, double *t_setup);
+void g2po_job_z(const g2po_job *j, double *z_out);
+void g2po_job_destroy(g2po_job *j);
+
 #ifdef __cplusplus
 }
 #endif

@@ -532,142 +532,216 @@ static double freq_of(const g2po_mesh *m, int id) {
     return m->freq_start * m->freq_unit * pow(m->freq_end / m->freq_start, (id * 1.0 / (m->nfreq - 1)));
 }
 
-int g2po_para_generator(const g2po_mesh *m, const g2po_solver_opts *o, int max_ports,
-                        double *z_out, g2po_para_stats *st) {
-    dims_t d = dims(m);
-    double t0 = now_s();
-    memset(st, 0, sizeof(*st));
-    int64_t *map_edge = (int64_t *)malloc(sizeof(int64_t) * (size_t)d.N_edge);
-    uint8_t *pec_edge = (uint8_t *)malloc((size_t)d.N_edge);
-    uint8_t *pec_node = (uint8_t *)malloc((size_t)d.N_node);
-    st->bden = g2po_index_maps(m, map_edge, pec_edge, pec_node);
+/* ---------------------------------------------------------- the V0 job
+ * paraGenerator's default path (matrixCon.cpp:11-907 with SKIP_VH) split
+ * into its assembly and, per port, its three solves (Ad, Ac, Ad), so that a
+ * caller can run the ports of one job on several host threads: the ports
+ * share only read-only data (V0 bases, Ad, Ac) and, without setup reuse,
+ * each solve builds its own hierarchy as hypreSolve does. */
+typedef struct {
+    double *J, *y0d, *yd1, *yc, *yd2, *ydt, *bd, *bc, *crhs, *y0c;
+    int stage;     /* next stage to run: 0 first Ad solve, 1 Ac solve, 2 second Ad solve, 3 done */
+} port_state;
+
+struct g2po_job {
+    const g2po_mesh *m;
+    dims_t d;
+    int64_t *map_edge;
+    uint8_t *pec_edge, *pec_node;
     g2po_v0 vd, vc;
     g2po_csr Ad, Ac;
-    g2po_v0d(m, pec_node, &vd);
-    g2po_ad(m, &vd, &Ad);
-    g2po_v0c(m, pec_node, &vc);
-    g2po_ac(m, &vc, &Ac);
-    st->leng_v0d = vd.ncol; st->leng_v0c = vc.ncol;
-    st->nnz_ad = Ad.ptr[Ad.n]; st->nnz_ac = Ac.ptr[Ac.n];
-    double t1 = now_s();
-    st->t_assembly = t1 - t0;
-    int P = m->num_ports;
-    int np = (max_ports > 0 && max_ports < P) ? max_ports : P;
-    int64_t ne = d.N_edge;
-    double *J = (double *)calloc((size_t)ne, sizeof(double));
-    double *bd = (double *)calloc((size_t)vd.ncol, sizeof(double));
-    double *y0d = (double *)calloc((size_t)vd.ncol, sizeof(double));
-    double *bc = (double *)calloc((size_t)vc.ncol, sizeof(double));
-    double *crhs = (double *)calloc((size_t)vc.ncol, sizeof(double));
-    double *y0c = (double *)calloc((size_t)vc.ncol, sizeof(double));
-    double *ydt = (double *)calloc((size_t)ne, sizeof(double));
-    double *yd1 = (double *)calloc((size_t)ne, sizeof(double));
-    double *yc = (double *)calloc((size_t)ne, sizeof(double));
-    double *yd2 = (double *)calloc((size_t)ne, sizeof(double));
-    double *zr = (double *)calloc((size_t)P * P, sizeof(double));
-    double *zi = (double *)calloc((size_t)P * P, sizeof(double));
-    double omega = (2 * M_PI * m->freq_start * m->freq_unit);
-    g2po_amg_handle *Hd = NULL, *Hc = NULL;
-    double t_setup = 0.0;
-    int reuse = o->reuse_setup;
-    g2po_solver_opts so = *o;
-    double ts = now_s();
-    if (reuse) { Hd = g2po_amg_create(&Ad, &so); Hc = g2po_amg_create(&Ac, &so); }
-    t_setup += now_s() - ts;
-    g2po_solve_stats ss;
-#define SOLVE(H, A, b, x) do {                                             \
-        double _t = now_s();                                                \
-        g2po_amg_handle *_h = (H);                                          \
-        if (!reuse) _h = g2po_amg_create(&(A), &so);                        \
-        t_setup += reuse ? 0.0 : now_s() - _t;                              \
-        g2po_amg_solve(_h, (b), (x), &so, &ss);                             \
-        if (!reuse) g2po_amg_destroy(_h);                                   \
-        st->solves++; st->total_iterations += ss.iterations;                \
-        if (ss.rel_residual > st->max_rel_residual) st->max_rel_residual = ss.rel_residual; \
-        if (st->solves <= 3) st->t_each[st->solves - 1] = now_s() - _t;     \
-        if (o->stop_after_solves > 0 && st->solves >= o->stop_after_solves) goto sampled; \
-    } while (0)
-    for (int p = 0; p < np; p++) {
+    port_state *ps;
+    double *zr, *zi;
+};
+
+g2po_job *g2po_job_create(const g2po_mesh *m, g2po_para_stats *st) {
+    double t0 = now_s();
+    g2po_job *j = (g2po_job *)calloc(1, sizeof(*j));
+    j->m = m;
+    j->d = dims(m);
+    memset(st, 0, sizeof(*st));
+    j->map_edge = (int64_t *)malloc(sizeof(int64_t) * (size_t)j->d.N_edge);
+    j->pec_edge = (uint8_t *)malloc((size_t)j->d.N_edge);
+    j->pec_node = (uint8_t *)malloc((size_t)j->d.N_node);
+    st->bden = g2po_index_maps(m, j->map_edge, j->pec_edge, j->pec_node);
+    g2po_v0d(m, j->pec_node, &j->vd);
+    g2po_ad(m, &j->vd, &j->Ad);
+    g2po_v0c(m, j->pec_node, &j->vc);
+    g2po_ac(m, &j->vc, &j->Ac);
+    st->leng_v0d = j->vd.ncol; st->leng_v0c = j->vc.ncol;
+    st->nnz_ad = j->Ad.ptr[j->Ad.n]; st->nnz_ac = j->Ac.ptr[j->Ac.n];
+    j->ps = (port_state *)calloc((size_t)m->num_ports, sizeof(port_state));
+    j->zr = (double *)calloc((size_t)m->num_ports * m->num_ports, sizeof(double));
+    j->zi = (double *)calloc((size_t)m->num_ports * m->num_ports, sizeof(double));
+    st->t_assembly = now_s() - t0;
+    return j;
+}
+
+static void port_free(port_state *q) {
+    free(q->J); free(q->y0d); free(q->yd1); free(q->yc); free(q->yd2); free(q->ydt); free(q->bd); free(q->bc);
+    free(q->crhs); free(q->y0c);
+    memset(q, 0, sizeof(*q));
+}
+
+static void job_solve(const g2po_csr *A, g2po_amg_handle *H, const double *b, double *x,
+                      const g2po_solver_opts *o, g2po_solve_stats *ss, double *t_setup) {
+    double t = now_s();
+    g2po_amg_handle *h = H ? H : g2po_amg_create(A, o);
+    *t_setup = H ? 0.0 : now_s() - t;
+    g2po_amg_solve(h, b, x, o, ss);
+    if (!H) g2po_amg_destroy(h);
+}
+
+/* Runs port p's next stage; H is a prebuilt hierarchy for the stage's matrix
+ * (Ad for stages 0 and 2, Ac for stage 1) or NULL for a fresh setup.  Stage 2
+ * also writes the port's column of Z (Construct_Z_V0, fdtd.hpp:4173-4215). */
+static int job_stage(g2po_job *j, int p, g2po_amg_handle *H, const g2po_solver_opts *o, g2po_solve_stats *ss,
+                     double *t_setup) {
+    const g2po_mesh *m = j->m;
+    const dims_t d = j->d;
+    const int64_t ne = d.N_edge;
+    const int P = m->num_ports;
+    port_state *q = &j->ps[p];
+    const double omega = (2 * M_PI * m->freq_start * m->freq_unit);
+    if (q->stage == 0) {
+        q->J = (double *)calloc((size_t)ne, sizeof(double));
+        q->bd = (double *)calloc((size_t)j->vd.ncol, sizeof(double));
+        q->y0d = (double *)calloc((size_t)j->vd.ncol, sizeof(double));
+        q->bc = (double *)calloc((size_t)j->vc.ncol, sizeof(double));
+        q->crhs = (double *)calloc((size_t)j->vc.ncol, sizeof(double));
+        q->y0c = (double *)calloc((size_t)j->vc.ncol, sizeof(double));
+        q->ydt = (double *)calloc((size_t)ne, sizeof(double));
+        q->yd1 = (double *)calloc((size_t)ne, sizeof(double));
+        q->yc = (double *)calloc((size_t)ne, sizeof(double));
+        q->yd2 = (double *)calloc((size_t)ne, sizeof(double));
         /* matrixCon.cpp:365-374 */
-        memset(J, 0, sizeof(double) * (size_t)ne);
         for (int s = m->port_side_ptr[p]; s < m->port_side_ptr[p + 1]; s++)
             for (int64_t k = m->side_edge_ptr[s]; k < m->side_edge_ptr[s + 1]; k++)
-                J[m->side_edges[k]] = m->side_dir[s];
+                q->J[m->side_edges[k]] = m->side_dir[s];
         /* :384-392 */
-        v0t_mv(&vd, 1, J, bd);
-        for (int64_t i = 0; i < vd.ncol; i++) bd[i] *= -1.0;
-        SOLVE(Hd, Ad, bd, y0d);
+        v0t_mv(&j->vd, 1, q->J, q->bd);
+        for (int64_t i = 0; i < j->vd.ncol; i++) q->bd[i] *= -1.0;
+        job_solve(&j->Ad, H, q->bd, q->y0d, o, ss, t_setup);
+    } else if (q->stage == 1) {
         /* :401-412 */
-        for (int64_t i = 0; i < vd.ncol; i++) y0d[i] /= omega;
-        v0_mv(&vd, 0, y0d, ydt, ne);
+        for (int64_t i = 0; i < j->vd.ncol; i++) q->y0d[i] /= omega;
+        v0_mv(&j->vd, 0, q->y0d, q->ydt, ne);
         /* :436-461 */
-        v0t_mv(&vc, 1, J, bc);
-        for (int64_t i = 0; i < vc.ncol; i++) bc[i] *= -1.0;
+        v0t_mv(&j->vc, 1, q->J, q->bc);
+        for (int64_t i = 0; i < j->vc.ncol; i++) q->bc[i] *= -1.0;
         for (int64_t e = 0; e < ne; e++) {
-            yd1[e] = ydt[e];
-            ydt[e] *= -1.0 * (2 * M_PI * m->freq_start * m->freq_unit) * m->stack_epsn[e / d.L] * EPSILON0;
+            q->yd1[e] = q->ydt[e];
+            q->ydt[e] *= -1.0 * (2 * M_PI * m->freq_start * m->freq_unit) * m->stack_epsn[e / d.L] * EPSILON0;
         }
-        v0t_mv(&vc, 1, ydt, crhs);
-        for (int64_t i = 0; i < vc.ncol; i++) bc[i] += crhs[i];
+        v0t_mv(&j->vc, 1, q->ydt, q->crhs);
+        for (int64_t i = 0; i < j->vc.ncol; i++) q->bc[i] += q->crhs[i];
         /* :511 */
-        SOLVE(Hc, Ac, bc, y0c);
+        job_solve(&j->Ac, H, q->bc, q->y0c, o, ss, t_setup);
+    } else if (q->stage == 2) {
         /* :528-544 */
-        v0_mv(&vc, 0, y0c, yc, ne);
-        for (int64_t e = 0; e < ne; e++) ydt[e] = -yc[e] * m->stack_epsn[e / d.L] * EPSILON0;
-        v0t_mv(&vd, 1, ydt, bd);
-        SOLVE(Hd, Ad, bd, y0d);
+        v0_mv(&j->vc, 0, q->y0c, q->yc, ne);
+        for (int64_t e = 0; e < ne; e++) q->ydt[e] = -q->yc[e] * m->stack_epsn[e / d.L] * EPSILON0;
+        v0t_mv(&j->vd, 1, q->ydt, q->bd);
+        job_solve(&j->Ad, H, q->bd, q->y0d, o, ss, t_setup);
         /* :553-584: yd = (yd2 + yc) - i*yd1 */
-        v0_mv(&vd, 0, y0d, yd2, ne);
+        v0_mv(&j->vd, 0, q->y0d, q->yd2, ne);
         /* Construct_Z_V0 (fdtd.hpp:4173-4215) */
         double cur = 0.0;
         for (int s = m->port_side_ptr[p]; s < m->port_side_ptr[p + 1]; s++) cur += m->side_area[s];
-        for (int q = 0; q < P; q++) {
-            int s = m->port_side_ptr[q];
+        for (int r = 0; r < P; r++) {
+            int s = m->port_side_ptr[r];
             double re = 0.0, im = 0.0;
             for (int64_t k = m->side_edge_ptr[s]; k < m->side_edge_ptr[s + 1]; k++) {
                 int64_t e = m->side_edges[k];
-                int64_t r = e % d.L;
+                int64_t rr = e % d.L;
                 double leng;
-                if (r >= d.Ns) { int64_t inz = e / d.L; leng = m->zn[inz + 1] - m->zn[inz]; }
-                else if (r >= d.Ny * (d.Nx + 1)) { int64_t inx = (r - d.Ny * (d.Nx + 1)) / (d.Ny + 1); leng = m->xn[inx + 1] - m->xn[inx]; }
-                else { int64_t iny = r % d.Ny; leng = m->yn[iny + 1] - m->yn[iny]; }
+                if (rr >= d.Ns) { int64_t inz = e / d.L; leng = m->zn[inz + 1] - m->zn[inz]; }
+                else if (rr >= d.Ny * (d.Nx + 1)) { int64_t inx = (rr - d.Ny * (d.Nx + 1)) / (d.Ny + 1); leng = m->xn[inx + 1] - m->xn[inx]; }
+                else { int64_t iny = rr % d.Ny; leng = m->yn[iny + 1] - m->yn[iny]; }
                 double dir = m->side_dir[s] * 1.0;
-                double yre = (yd2[e] - 0.0) + yc[e];
-                double yim = 0.0 - yd1[e];
+                double yre = (q->yd2[e] - 0.0) + q->yc[e];
+                double yim = 0.0 - q->yd1[e];
                 re -= yre * leng * dir;
                 im -= yim * leng * dir;
             }
-            zr[q + (int64_t)P * p] = re / cur;
-            zi[q + (int64_t)P * p] = im / cur;
+            j->zr[r + (int64_t)P * p] = re / cur;
+            j->zi[r + (int64_t)P * p] = im / cur;
         }
+        port_free(q);
+    } else {
+        return -1;
     }
-sampled:
-#undef SOLVE
-    /* print_z_V0 (fdtd.hpp:4249-4316): freq 0 as stored, others transposed
-       with Im scaled by f0/f */
+    q->stage++;
+    return 0;
+}
+
+int g2po_job_port_stage(g2po_job *j, int port, const g2po_solver_opts *o, g2po_solve_stats *ss, double *t_setup) {
+    if (!j || port < 0 || port >= j->m->num_ports) return -1;
+    double ts = 0.0;
+    int rc = job_stage(j, port, NULL, o, ss, &ts);
+    if (t_setup) *t_setup = ts;
+    return rc;
+}
+
+/* print_z_V0 (fdtd.hpp:4249-4316): freq 0 as stored, others transposed with
+   Im scaled by f0/f */
+void g2po_job_z(const g2po_job *j, double *z_out) {
+    const g2po_mesh *m = j->m;
+    const int P = m->num_ports;
     for (int f = 0; f < m->nfreq; f++) {
         double fr = freq_of(m, f);
         for (int i = 0; i < P; i++)
-            for (int j = 0; j < P; j++) {
+            for (int k = 0; k < P; k++) {
                 int64_t o0 = (int64_t)f * P * P;
                 if (f == 0) {
-                    z_out[2 * (o0 + j + (int64_t)i * P)] = zr[j + (int64_t)i * P];
-                    z_out[2 * (o0 + j + (int64_t)i * P) + 1] = zi[j + (int64_t)i * P];
+                    z_out[2 * (o0 + k + (int64_t)i * P)] = j->zr[k + (int64_t)i * P];
+                    z_out[2 * (o0 + k + (int64_t)i * P) + 1] = j->zi[k + (int64_t)i * P];
                 } else {
-                    z_out[2 * (o0 + i + (int64_t)j * P)] = zr[j + (int64_t)i * P] + 0.0;
-                    z_out[2 * (o0 + i + (int64_t)j * P) + 1] = zi[j + (int64_t)i * P] * m->freq_start * m->freq_unit / fr;
+                    z_out[2 * (o0 + i + (int64_t)k * P)] = j->zr[k + (int64_t)i * P] + 0.0;
+                    z_out[2 * (o0 + i + (int64_t)k * P) + 1] = j->zi[k + (int64_t)i * P] * m->freq_start * m->freq_unit / fr;
                 }
             }
     }
-    double t2 = now_s();
+}
+
+void g2po_job_destroy(g2po_job *j) {
+    if (!j) return;
+    for (int p = 0; p < j->m->num_ports; p++) port_free(&j->ps[p]);
+    free(j->ps); free(j->zr); free(j->zi);
+    g2po_v0_free(&j->vd); g2po_v0_free(&j->vc);
+    g2po_csr_free(&j->Ad); g2po_csr_free(&j->Ac);
+    free(j->map_edge); free(j->pec_edge); free(j->pec_node);
+    free(j);
+}
+
+int g2po_para_generator(const g2po_mesh *m, const g2po_solver_opts *o, int max_ports,
+                        double *z_out, g2po_para_stats *st) {
+    g2po_job *j = g2po_job_create(m, st);
+    double t1 = now_s();
+    const int P = m->num_ports;
+    const int np = (max_ports > 0 && max_ports < P) ? max_ports : P;
+    g2po_amg_handle *Hd = NULL, *Hc = NULL;
+    double t_setup = 0.0, ts = now_s();
+    if (o->reuse_setup) { Hd = g2po_amg_create(&j->Ad, o); Hc = g2po_amg_create(&j->Ac, o); }
+    t_setup += now_s() - ts;
+    for (int p = 0; p < np; p++) {
+        for (int stage = 0; stage < 3; stage++) {
+            g2po_solve_stats ss;
+            double t = now_s(), tsu = 0.0;
+            job_stage(j, p, stage == 1 ? Hc : Hd, o, &ss, &tsu);
+            t_setup += tsu;
+            st->solves++; st->total_iterations += ss.iterations;
+            if (ss.rel_residual > st->max_rel_residual) st->max_rel_residual = ss.rel_residual;
+            if (st->solves <= 3) st->t_each[st->solves - 1] = now_s() - t;
+            if (o->stop_after_solves > 0 && st->solves >= o->stop_after_solves) goto sampled;
+        }
+    }
+sampled:
+    g2po_job_z(j, z_out);
     st->t_setup = t_setup;
-    st->t_solve = t2 - t1 - t_setup;
+    st->t_solve = now_s() - t1 - t_setup;
     if (Hd) g2po_amg_destroy(Hd);
     if (Hc) g2po_amg_destroy(Hc);
-    free(J); free(bd); free(y0d); free(bc); free(crhs); free(y0c); free(ydt); free(yd1); free(yc); free(yd2);
-    free(zr); free(zi);
-    g2po_v0_free(&vd); g2po_v0_free(&vc);
-    g2po_csr_free(&Ad); g2po_csr_free(&Ac);
-    free(map_edge); free(pec_edge); free(pec_node);
+    g2po_job_destroy(j);
     return 0;
 }

@@ -51,15 +51,22 @@ template <class T> static void write_arr(const char *name, const T *p, size_t n)
     fclose(f);
 }
 
+#ifndef G2P_REF_WITH_GB300_SHIM
 /* The reference's hypreSolve boundary (hypreSolve.cpp:9), served by the
  * project FP64 CPU solver at a tight tolerance; each call's right-hand side
- * and solution are recorded for the fixtures. */
+ * and solution are recorded for the fixtures.  (Built with
+ * G2P_REF_WITH_GB300_SHIM, the harness leaves hypreSolve, generateStiff and
+ * paraGenerator to oracle/gb300_path.cpp, the library's reference-side
+ * shim.) */
 int hypreSolve(fdtdMesh *sys, myint *ARowId, myint *AColId, double *Aval, myint leng_A, double *bin,
                myint leng_v0, double *solution) {
     (void)sys;
     g2po_solver_opts o;
     g2po_solver_default_opts(&o);
     o.rtol = 1e-13; o.maxit = 4000; o.restart = 60;
+    /* the bench-size fixtures take their solves to a looser tolerance
+       (G2P_REF_SOLVE_RTOL), which keeps each one to minutes here */
+    if (const char *e = getenv("G2P_REF_SOLVE_RTOL")) o.rtol = atof(e);
     g2po_solve_stats st;
     int rc = g2po_solve_coo((const int64_t *)ARowId, (const int64_t *)AColId, Aval, leng_A, bin, leng_v0,
                             solution, &o, &st);
@@ -73,6 +80,7 @@ int hypreSolve(fdtdMesh *sys, myint *ARowId, myint *AColId, double *Aval, myint 
     g_solve_calls++;
     return 0;
 }
+#endif
 
 int main(int argc, char **argv) {
     if (argc < 3) { fprintf(stderr, "usage: %s in_dir out_dir\n", argv[0]); return 2; }

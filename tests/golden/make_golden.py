@@ -9,7 +9,7 @@ enough to check bit-exact integer and FP64 results.
 
 Needs the reference checkout (the argument, else $G2P_REFERENCE_ROOT, else
 /root/reference); the fixtures it writes are self-contained.  Usage:
-    python tests/golden/make_golden.py [reference_root]
+    python tests/golden/make_golden.py [reference_root] [--cases a,b,...]
 """
 from __future__ import annotations
 
@@ -43,6 +43,16 @@ CASES = {
                                           freq_scale=0)),
 }
 
+# The bench configurations, pinned by digests of everything the reference
+# path produces (its solves take minutes here, so they are generated only
+# when named: make_golden.py --cases manhattan_c2,multistrip_c3).  Their
+# hypreSolve stand-in stops at SOLVE_RTOL instead of 1e-13.
+BENCH_CASES = {
+    "manhattan_c2": ("manhattan", dict(nx=512, ny=512, nz=24, n_ports=8, seed=1001)),
+    "multistrip_c3": ("multistrip", dict(nx=256, ny=256, nz=16, n_strips=32)),
+}
+SOLVE_RTOL = {"manhattan_c2": 1e-10}
+
 
 def digest(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
@@ -53,13 +63,28 @@ def make_layout(gen: str, kw: dict):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("G2P_REFERENCE_ROOT", "/root/reference")
-    subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), ref])
-    for name, (gen, kw) in CASES.items():
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("reference_root", nargs="?", default=os.environ.get("G2P_REFERENCE_ROOT", "/root/reference"))
+    ap.add_argument("--cases", default=",".join(CASES),
+                    help="comma-separated case names (default: the small cases; bench cases: "
+                         + ",".join(BENCH_CASES) + ")")
+    ap.add_argument("--no-build", action="store_true", help="use the oracle/_ref binaries already built")
+    args = ap.parse_args()
+    if not args.no_build:
+        subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), args.reference_root])
+    every = dict(CASES, **BENCH_CASES)
+    for name in args.cases.split(","):
+        gen, kw = every[name]
+        if name in SOLVE_RTOL:
+            os.environ["G2P_REF_SOLVE_RTOL"] = repr(SOLVE_RTOL[name])
+        else:
+            os.environ.pop("G2P_REF_SOLVE_RTOL", None)
         d = make_layout(gen, kw)
         R = run_reference(d)
         out = {}
-        meta = {"generator": gen, "kwargs": kw, "hashes": {}, "stats": {}}
+        meta = {"generator": gen, "kwargs": kw, "hashes": {}, "stats": {},
+                "solve_rtol": SOLVE_RTOL.get(name, 1e-13)}
         for k, v in R.items():
             if k == "_log":
                 continue

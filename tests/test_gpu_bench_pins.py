@@ -1,0 +1,59 @@
+"""The bench configurations themselves, pinned against the reference path.
+
+c2 (random Manhattan, 512 x 512 x 24 nodes, 8 ports) and c3 (32 strips,
+256 x 256 x 16 nodes, 32 ports x 64 frequencies) are the workloads the bench
+line is quoted on.  tests/golden/manhattan_c2.npz and multistrip_c3.npz hold
+what the reference's own sources (oracle/_ref/ref_pipeline) produced for
+them: SHA-256 digests of the edge map, the S COO (231M entries at c2), the
+V0d/V0c bases with a-values and maps and the Ad/Ac COO, and the whole Z.
+Here the GPU path, through the C ABI, must give the same bytes for every
+assembled array, and Z within the stated tolerances: the reference path's
+solves were taken to 1e-13, the bench's mixed method stops at 1e-8 (bound
+1e-6 on Z, the spec accuracy), the FP64 method here at 1e-10 (bound
+1e-7)."""
+import numpy as np
+import pytest
+
+from conftest import BENCH_CASES, check_golden_array, golden_layout
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", BENCH_CASES)
+def test_gpu_bench_config_assembly_bit_exact(name, g2p):
+    d, A, M = golden_layout(name)
+    with g2p.FdtdMesh(d) as m:
+        me, bden = m.index_maps()
+        assert bden == M["bden"]
+        check_golden_array(A, M, "map_edge", me)
+        del me
+        assert g2p.generateStiff(m) == M["leng_S"]
+        r, c, v = m.export_stiff()
+        check_golden_array(A, M, "S_row", r)
+        check_golden_array(A, M, "S_col", c)
+        check_golden_array(A, M, "S_val", v)
+        del r, c, v
+        s = m.assemble_v0()
+        assert s.leng_v0d == M["leng_v0d"] and s.leng_v0c == M["leng_v0c"]
+        for t in "dc":
+            v0 = m.export_v0(t)
+            for k in ("row", "col", "val", "aval", "map"):
+                check_golden_array(A, M, f"v0{t}_{k}", v0[k])
+            r, c, val = m.export_laplacian(t)
+            check_golden_array(A, M, f"A{t}_row", r)
+            check_golden_array(A, M, f"A{t}_col", c)
+            check_golden_array(A, M, f"A{t}_val", val)
+
+
+@pytest.mark.parametrize("name", BENCH_CASES)
+@pytest.mark.parametrize("precision,rtol,bound", [("mixed", 1e-8, 1e-6), ("fp64", 1e-10, 1e-7)])
+def test_gpu_bench_config_z_matches_reference(name, precision, rtol, bound, g2p):
+    d, A, M = golden_layout(name)
+    with g2p.FdtdMesh(d) as m:
+        g2p.generateStiff(m)
+        Z, st = g2p.paraGenerator(m, g2p.default_params(precision=precision, batch=1, rtol=rtol))
+    Zr = A["Z"].reshape(Z.shape)
+    err = np.abs(Z - Zr).max() / np.abs(Zr).max()
+    assert err < bound, (err, st.total_iterations)
+    assert st.max_rel_residual <= rtol
+    assert st.solves == 3 * d.num_ports

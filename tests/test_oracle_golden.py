@@ -3,10 +3,15 @@ by the reference's own sources (tests/golden/make_golden.py)."""
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, check_golden_array, golden_layout
+from conftest import BENCH_CASES, GOLDEN_CASES, check_golden_array, golden_layout
+
+# the assembly pins also cover the bench configurations (c2: 231M S entries,
+# about 5 s of oracle time on one thread); the CPU Z checks stay on the small
+# layouts, the bench configurations' Z is checked on the GPU
+ASSEMBLY_CASES = GOLDEN_CASES + BENCH_CASES
 
 
-@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("name", ASSEMBLY_CASES)
 def test_generator_matches_reference_meshing(name):
     # conductor labelling, recolouring, ports (mesh.cpp:683-1020, portSet)
     d, A, M = golden_layout(name)
@@ -20,7 +25,7 @@ def test_generator_matches_reference_meshing(name):
     assert M["numCdt"] == d.num_cdt
 
 
-@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("name", ASSEMBLY_CASES)
 def test_oracle_index_maps_and_stiffness(name, coracle):
     d, A, M = golden_layout(name)
     me, pe, pn, bden = coracle.index_maps(d)
@@ -34,7 +39,7 @@ def test_oracle_index_maps_and_stiffness(name, coracle):
     check_golden_array(A, M, "S_val", val)       # bit-exact
 
 
-@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("name", ASSEMBLY_CASES)
 def test_oracle_v0_and_laplacians(name, coracle):
     d, A, M = golden_layout(name)
     V = coracle.v0_and_laplacians(d)
@@ -74,3 +79,18 @@ def test_oracle_solver_matches_direct_solve(coracle):
     xd = spl.spsolve(Ad.tocsc(), b)
     assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-8
     assert st.rel_residual < 1e-11
+
+
+@pytest.mark.parametrize("name", ["manhattan_small", "multistrip_small"])
+def test_oracle_job_on_threads_matches_reference(name, coracle):
+    """The job form the CPU baseline times (ports spread over host threads,
+    a fresh AMG setup per solve as hypreSolve does) gives the reference's Z."""
+    d, A, M = golden_layout(name)
+    job = coracle.job(d)
+    o = coracle.default_opts(rtol=1e-12, maxit=3000, restart=50, reuse_setup=0)
+    for k in range(3):
+        job.stage(k, o, threads=3)
+    Z = job.z()
+    job.close()
+    Zr = A["Z"].reshape(Z.shape)
+    assert np.abs(Z - Zr).max() / np.abs(Zr).max() < 1e-9
