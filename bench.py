@@ -36,8 +36,9 @@ WORKLOAD = {
     "c1": "microstrip 101x41x11 nodes at 1 um, 1 port, 1 GHz, rtol 1e-10",
     "c2": "random Manhattan 512x512x24 nodes, 4 metal layers x 64 wires, 8 ports, 10 GHz, rtol 1e-8",
     "c3": "microstrip stack 256x256x16 nodes, 32 strips/ports x 64 log-spaced points 1e7..1e11 Hz, rtol 1e-8",
-    "c4": "served stream of 48 random Manhattan jobs (sides log-uniform 64..384, nz 10..16, 1..8 ports, 1..16 "
-          "log-spaced points 1e8..1e10 Hz), Poisson arrivals at 0.8 x the serial capacity, 150 GB budget, rtol 1e-8",
+    "c4": "served stream of 200 random Manhattan jobs (sides log-uniform 64..1024 nodes in x and y, nz uniform in "
+          "{8, 16, 32}, 1..16 ports, 1..32 log-spaced points 1e8..1e10 Hz), Poisson arrivals at 0.8 x the serial "
+          "capacity, 150 GB budget, rtol 1e-8",
     "c5": "large random Manhattan 1536x1536x32 nodes (224M edges), 6 metal layers x 256 wires, 16 ports x 8 "
           "log-spaced points 1e8..1e10 Hz, ports in blocks of 4, rtol 1e-8",
 }
@@ -376,18 +377,20 @@ def run_gb300(args):
     return out, rank
 
 
-def c4_jobs(n=48, seed=1004):
-    """The served workload: seeded random Manhattan layouts of mixed sizes."""
+def c4_jobs(n=200, seed=1004):
+    """The served workload: seeded random Manhattan layouts of mixed sizes,
+    sides log-uniform in 64..1024 nodes, nz in {8, 16, 32} (2, 3 or 4 metal
+    layers), 1..16 ports and 1..32 frequency points."""
     from gds2para_gb300 import layout
     rng = np.random.default_rng(seed)
     jobs = []
     while len(jobs) < n:
-        side = int(round(np.exp(rng.uniform(np.log(64), np.log(384)))))
-        nz = int(rng.choice([10, 12, 16]))
-        ports = int(rng.integers(1, 9))
-        nfreq = int(rng.integers(1, 17))
+        side = int(round(np.exp(rng.uniform(np.log(64), np.log(1024)))))
+        nz = int(rng.choice([8, 16, 32]))
+        ports = int(rng.integers(1, 17))
+        nfreq = int(rng.integers(1, 33))
         try:
-            lay = layout.manhattan(nx=side, ny=side, nz=nz, n_metal=3 if nz < 16 else 4,
+            lay = layout.manhattan(nx=side, ny=side, nz=nz, n_metal={8: 2, 16: 3, 32: 4}[nz],
                                    wires_per_layer=max(8, side // 8), n_ports=ports, seed=int(rng.integers(1 << 30)),
                                    lmin=max(6, side // 16), lmax=max(12, side // 3), freq_start=1e8, freq_end=1e10,
                                    freq_unit=1.0, nfreq=nfreq, freq_scale=0 if nfreq > 1 else 1)

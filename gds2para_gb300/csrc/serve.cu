@@ -5,11 +5,15 @@
 // flight overlap on the device.  The reference runs one layout per process
 // and has no counterpart.
 //
-// Admission: a job starts when it is at the head of the queue, fewer than
-// max_active jobs run, and its footprint estimate fits the budget minus the
-// estimates of the running jobs.  The estimate is a size model (edges,
-// nodes, right-hand sides, Krylov restart) scaled by the largest ratio of
-// measured pool high-water to estimate seen on jobs that ran alone.
+// Admission: while fewer than max_active jobs run, the first queued job
+// whose footprint estimate fits the budget minus the estimates of the
+// running jobs starts.  A job further back may pass one that does not fit
+// yet, but only 2 * max_active times: after that the bypassed job holds the
+// queue until it fits.  A job that fits no budget runs alone.  The estimate
+// is a size model (edges, nodes, right-hand sides, Krylov restart) scaled by
+// the largest ratio of measured pool high-water to estimate seen on jobs that
+// ran alone.  A job whose estimate with all ports in one block exceeds the
+// budget runs its ports in the widest power-of-two blocks that fit.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -113,7 +117,22 @@ struct Job {
     std::vector<double> z;
     g2p_extract_stats stats{};
     uint64_t measured = 0;
+    int bypassed = 0;                   // times a later job started ahead of it
 };
+
+// The port block width a job runs with: its own setting, narrowed to the
+// widest power-of-two block whose estimate fits the budget.
+int32_t fitting_batch(const g2p_mesh_desc &d, g2p_solver_params p, double scale, double budget) {
+    const int P = std::max(1, d.num_ports);
+    if (p.batch == 0 || size_model(d, p) * scale <= budget) return p.batch;
+    int w = 1;
+    while (w * 2 < P) w *= 2;
+    for (; w >= 2; w /= 2) {
+        p.batch = w;
+        if (size_model(d, p) * scale <= budget) return w;
+    }
+    return 0;          // one port at a time
+}
 
 }  // namespace
 
@@ -180,16 +199,29 @@ void g2p_server::run_job(std::shared_ptr<Job> job) {
 void g2p_server::dispatch_loop() {
     cudaSetDevice(device);
     std::unique_lock<std::mutex> lock(mu);
+    const int max_bypass = 2 * max_active;
+    size_t pick = 0;
+    // the queue position of the job to start now, or queue.size() for none
+    auto admissible = [&]() -> size_t {
+        if (queue.empty() || active >= max_active) return queue.size();
+        for (size_t i = 0; i < queue.size(); i++) {
+            const Job &q = *queue[i];
+            const double est = size_model(q.desc.d, q.params) * scale;
+            if (active == 0 || committed + est <= (double)budget) return i;
+            if (q.bypassed >= max_bypass) break;      // it holds the queue until it fits
+        }
+        return queue.size();
+    };
     for (;;) {
         cv.wait(lock, [&] {
             if (stopping && queue.empty()) return true;
-            if (queue.empty() || active >= max_active) return false;
-            const double est = size_model(queue.front()->desc.d, queue.front()->params) * scale;
-            return active == 0 || committed + est <= (double)budget;
+            pick = admissible();
+            return pick < queue.size();
         });
         if (stopping && queue.empty()) return;
-        std::shared_ptr<Job> job = queue.front();
-        queue.pop_front();
+        std::shared_ptr<Job> job = queue[pick];
+        for (size_t i = 0; i < pick; i++) queue[i]->bypassed++;
+        queue.erase(queue.begin() + (std::ptrdiff_t)pick);
         job->model = size_model(job->desc.d, job->params);
         job->estimate = job->model * scale;
         job->solo = active == 0;
@@ -225,6 +257,9 @@ extern "C" g2p_status g2p_server_submit(g2p_server *s, const g2p_mesh_desc *desc
     if (p) job->params = *p;
     else g2p_default_params(&job->params, 0);
     std::lock_guard<std::mutex> lock(s->mu);
+    // fixed margin, not the measured scale: a job's block width (and so its
+    // result) depends only on its own description and the budget
+    job->params.batch = fitting_batch(job->desc.d, job->params, 1.5, (double)s->budget);
     if (s->stopping) { set_last_message("server is shutting down"); return G2P_ERR_STATE; }
     // a job whose estimate exceeds the budget is still run, alone
     job->id = s->next_id++;

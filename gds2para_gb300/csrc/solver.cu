@@ -1744,11 +1744,11 @@ __global__ void __launch_bounds__(256) k_gj_step(const double *__restrict__ a_in
 // launch.  Buffers ping-pong as in the per-step loop; the inverse ends in
 // inv1 when n is odd, inv0 otherwise.  flags[0] is the singular flag,
 // flags[1] the barrier's arrival count and flags[2] set when a block gave up
-// waiting (bounded spin), in which case the caller recomputes with one
-// launch per pivot.
+// waiting (bounded spin: spin_limit polls of 64 ns or more), in which case
+// the caller recomputes with one launch per pivot.
 constexpr int kGjSpinLimit = 1 << 22;
 __global__ void __launch_bounds__(256) k_gj_coop(double *a0, double *inv0, double *a1, double *inv1, int64_t n,
-                                                 int *flags) {
+                                                 int *flags, int spin_limit) {
     __shared__ double bv[256];
     __shared__ int64_t bi[256];
     __shared__ int quit;
@@ -1766,7 +1766,7 @@ __global__ void __launch_bounds__(256) k_gj_coop(double *a0, double *inv0, doubl
             const unsigned target = (unsigned)((kk + 1) * gridDim.x);
             int it = 0, q = 0;
             while (*(volatile unsigned *)arrived < target) {
-                if (*abandon || ++it > kGjSpinLimit) { *abandon = 1; q = 1; break; }
+                if (*abandon || ++it > spin_limit) { *abandon = 1; q = 1; break; }
                 __nanosleep(64);
             }
             __threadfence();
@@ -2497,7 +2497,11 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                 bool coop = false;
                 if (coop_attr && (int64_t)per_sm * kSMs >= nn && !getenv("G2P_GJ_STEPS")) {
                     int64_t nn_arg = nn;
-                    void *args[] = {&ain, &iin, &aout, &iout, &nn_arg, &d_int};
+                    // G2P_GJ_SPIN_LIMIT (comparisons only) shortens the
+                    // barrier's patience so that the give-up path runs
+                    int spin = kGjSpinLimit;
+                    if (const char *e = getenv("G2P_GJ_SPIN_LIMIT")) spin = std::max(1, atoi(e));
+                    void *args[] = {&ain, &iin, &aout, &iout, &nn_arg, &d_int, &spin};
                     g2p::kbegin("k_gj_coop", s);
                     coop = cudaLaunchCooperativeKernel((void *)k_gj_coop, dim3((unsigned)nn), dim3(256), args, 0, s) == cudaSuccess;
                     g2p::kend(s);
@@ -2506,6 +2510,9 @@ g2p_status amg_setup(const Csr<double> &A0, const SolverConfig &cfg, cudaStream_
                         G2P_CUDA(cudaMemcpyAsync(&gave_up, d_int + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
                         G2P_CUDA(cudaStreamSynchronize(s));
                         if (gave_up) {           // start again from A and I
+                            if (getenv("G2P_DEBUG"))
+                                fprintf(stderr, "[g2p] coarse inverse (n=%lld): the cooperative launch's barrier gave "
+                                                "up; recomputed with one launch per pivot\n", (long long)nn);
                             coop = false;
                             G2P_CUDA(cudaMemsetAsync(d_int, 0, sizeof(int), s));
                             G2P_CUDA(cudaMemsetAsync(Dm, 0, sizeof(double) * nn * nn, s));

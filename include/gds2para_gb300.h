@@ -260,10 +260,15 @@ g2p_status g2p_mesh_grid(const double *lim, int64_t npoly, const int64_t *vert_p
 /* ---- extraction service (no counterpart in the reference, which extracts
  * one layout per process) ----
  * A queue of extraction jobs, each the work of g2p_mesh_create +
- * g2p_generate_stiff + g2p_para_generator on its own layout.  The first job
- * in the queue starts when fewer than max_active jobs run and its device
- * footprint estimate fits mem_budget_bytes minus the estimates of the
- * running jobs (a job larger than the budget runs alone).  Each running job
+ * g2p_generate_stiff + g2p_para_generator on its own layout.  While fewer
+ * than max_active jobs run, the first queued job whose device footprint
+ * estimate fits mem_budget_bytes minus the estimates of the running jobs
+ * starts; a later job may pass one that does not fit yet at most
+ * 2 * max_active times, after which the passed job holds the queue until it
+ * fits (a job larger than the budget runs alone).  A job whose estimate with
+ * all its ports in one block (batch 1) exceeds 2/3 of the budget runs them in
+ * the widest power-of-two blocks that fit (one at a time if none does).
+ * Each running job
  * has its own host thread, mesh handle and CUDA stream, so their kernels
  * overlap on the device; results do not depend on what else runs.  The
  * estimate is a size model scaled by the largest measured/model ratio of

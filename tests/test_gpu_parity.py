@@ -176,6 +176,27 @@ def test_gpu_coarse_inverse_one_launch_matches_per_pivot(name, precision, g2p, m
     assert np.array_equal(out[0], out[1])
 
 
+def test_gpu_coarse_inverse_barrier_give_up_recomputes_the_same(g2p, monkeypatch, capfd):
+    """The cooperative inverse's grid barrier gives up after a bounded number
+    of polls; with that bound cut to one poll it does give up, the host
+    recomputes with one launch per pivot, and Z is bit-identical to the
+    normal path's."""
+    d, A, M = golden_layout("strip_c1")
+    out = []
+    for limit in (None, "1"):
+        if limit:
+            monkeypatch.setenv("G2P_GJ_SPIN_LIMIT", limit)
+            monkeypatch.setenv("G2P_DEBUG", "1")
+        with g2p.FdtdMesh(d) as m:
+            g2p.generateStiff(m)
+            Z, st = g2p.paraGenerator(m, g2p.default_params(precision="fp64", rtol=1e-10))
+        out.append(Z)
+    monkeypatch.delenv("G2P_GJ_SPIN_LIMIT")
+    monkeypatch.delenv("G2P_DEBUG")
+    assert "barrier gave up; recomputed with one launch per pivot" in capfd.readouterr().err
+    assert np.array_equal(out[0], out[1])
+
+
 @pytest.mark.parametrize("name,precision", [("strip_c1", "mixed"), ("multistrip_small", "mixed"), ("strip_c1", "fp64")])
 def test_gpu_extraction_leaves_exact_ad_and_repattern_path_agrees(name, precision, g2p, monkeypatch):
     """Ad's preconditioner is built from tree-summed stand-ins for its longest

@@ -63,3 +63,28 @@ def test_submit_rejects_a_bad_description(g2p):
         assert L.g2p_server_submit(h, C.byref(bad), None, C.byref(job)) == 1
     finally:
         L.g2p_server_destroy(h)
+
+
+def _model_estimate(g2p, d, p):
+    """The service's footprint estimate of a job: the first job of a fresh
+    server is estimated by the size model alone (no measured scale yet)."""
+    with g2p.Server(mem_budget_bytes=1 << 40, max_active=1) as srv:
+        _, _, t = srv.wait(srv.submit(d, p))
+    return t.footprint_estimate
+
+
+def test_a_job_that_fits_passes_one_that_does_not(g2p):
+    """Admission is not head-of-line: with X running, Y does not fit the
+    remaining budget but Z does, so Z starts first although Y was queued
+    before it."""
+    p = g2p.default_params(precision="fp64", batch=1, rtol=1e-12)
+    X, Y, Z = (golden_layout(n)[0] for n in ("strip_c1", "manhattan_small", "strip_tiny"))
+    ex, ey, ez = (_model_estimate(g2p, d, p) for d in (X, Y, Z))
+    assert ey > ez
+    budget = ex + (ey + ez) // 2          # X + Z fit, X + Y do not; each fits alone
+    assert ex + ez <= budget < ex + ey and max(ex, ey, ez) <= budget
+    with g2p.Server(mem_budget_bytes=budget, max_active=3) as srv:
+        jobs = [srv.submit(d, p) for d in (X, Y, Z)]
+        (_, _, tx), (_, _, ty), (_, _, tz) = [srv.wait(j) for j in jobs]
+    assert tz.queued_ms < ty.queued_ms
+    assert ty.queued_ms > 0
