@@ -262,8 +262,16 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
     if (S->precision != G2P_PREC_MIXED) {
         F32Precond pc;
         pc.H = &S->H32; pc.lr = &S->lr; pc.in = S->rf; pc.out = S->df;
-        G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep,
-                               S->precision == G2P_PREC_FP64_PC32 ? &pc : nullptr, &S->lr));
+        const F32Precond *pcp = S->precision == G2P_PREC_FP64_PC32 ? &pc : nullptr;
+        G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep, pcp, &S->lr));
+        bool gave_up = false;
+        if (pcp) G2P_TRY(coarse_gave_up<float>(S->H32, s, &gave_up));
+        else G2P_TRY(coarse_gave_up<double>(S->H64, s, &gave_up));
+        if (gave_up) {       // again, with the launch-per-kernel V-cycle
+            if (getenv("G2P_DEBUG")) fprintf(stderr, "[g2p] fused coarse cycle gave up; solve repeated unfused\n");
+            G2P_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * nk, s));
+            G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep, pcp, &S->lr));
+        }
         iters = rep.iterations;
         if (getenv("G2P_DEBUG"))
             fprintf(stderr, "[g2p] n=%lld k=%d fp64: its %d rel %.3e\n", (long long)n, k, rep.iterations, rep.rel_residual);
@@ -302,6 +310,13 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
             G2P_CUDA(cudaMemsetAsync(S->df, 0, sizeof(float) * nk, s));
             SolveReport ir;
             G2P_TRY(fgmres<float>(S->H32.lv[0].A, S->H32, S->K32, S->rf, S->df, k, inner, nullptr, s, ir));
+            bool gave_up = false;
+            G2P_TRY(coarse_gave_up<float>(S->H32, s, &gave_up));
+            if (gave_up) {   // again, with the launch-per-kernel V-cycle
+                if (getenv("G2P_DEBUG")) fprintf(stderr, "[g2p] fused coarse cycle gave up; solve repeated unfused\n");
+                G2P_CUDA(cudaMemsetAsync(S->df, 0, sizeof(float) * nk, s));
+                G2P_TRY(fgmres<float>(S->H32.lv[0].A, S->H32, S->K32, S->rf, S->df, k, inner, nullptr, s, ir));
+            }
             if (getenv("G2P_DEBUG"))
                 fprintf(stderr, "[g2p] n=%lld k=%d refinement %d: outer rel %.3e, inner its %d inner rel %.3e\n",
                         (long long)n, k, ref, worst, ir.iterations, ir.rel_residual);

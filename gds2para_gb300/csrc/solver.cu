@@ -1374,6 +1374,10 @@ __global__ void k_prolong_csr(int64_t n, int k, const int64_t *ptr, const int32_
 // coarser levels on their own work vectors.
 template <class T>
 static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaStream_t s, const T *b, T *x) {
+    if (l > 0 && l == H.fuse_from) {       // b, x are the level's own vectors
+        coarse_cycle<T>(H, k, s);
+        return;
+    }
     Level<T> &L = H.lv[l];
     if (l == (int)H.lv.size() - 1) {
         if (H.cinv) (g2p::kbegin("k_dense_apply", s), k_dense_apply<T><<<(unsigned)((L.n * k * 32 + 255) / 256), 256, 0, s>>>(L.n, k, H.cinv, b, x), g2p::kend(s));
@@ -1868,6 +1872,14 @@ __global__ void k_bp_expand(int64_t nr, int64_t nnzb, const int64_t *bptr, const
 
 template <class T>
 void Hierarchy<T>::release(cudaStream_t s) {
+    if (fuse_tab) cudaFree(fuse_tab);
+    if (fuse_bar) cudaFree(fuse_bar);
+    if (fuse_trace) cudaFree(fuse_trace);
+    fuse_tab = nullptr;
+    fuse_bar = nullptr;
+    fuse_trace = nullptr;
+    fuse_from = -1;
+    fuse_key.clear();
     for (auto &L : lv) {
         L.A.release(s);
         L.P.release(s);
@@ -2794,6 +2806,14 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
     G2P_TRY(krylov_alloc<T>(K, n, k, m, s));
     if (pc) G2P_TRY(hierarchy_reserve<float>(*pc->H, k, s));
     else G2P_TRY(hierarchy_reserve<T>(H, k, s));
+    int fuse_from;
+    if (pc) {
+        G2P_TRY(coarse_prepare<float>(*pc->H, cfg, k, s));
+        fuse_from = pc->H->fuse_from;
+    } else {
+        G2P_TRY(coarse_prepare<T>(H, cfg, k, s));
+        fuse_from = H.fuse_from;
+    }
     const LongRows &lr0 = op_lr ? *op_lr : (pc ? *pc->lr : H.lv[0].lr);
     // CUDA graphs of the Arnoldi steps: off while kernels are being timed;
     // rebuilt when the block width, operator or preconditioner changes
@@ -2803,7 +2823,8 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
         const int kcap = pc ? pc->H->kcap : H.kcap;
         const std::vector<const void *> key = {(const void *)(intptr_t)k, (const void *)A.val, hier,
                                                (const void *)(intptr_t)kcap, (const void *)(intptr_t)cfg.degree,
-                                               (const void *)(intptr_t)cfg.reorth, pc ? (const void *)pc->in : nullptr};
+                                               (const void *)(intptr_t)cfg.reorth, pc ? (const void *)pc->in : nullptr,
+                                               (const void *)(intptr_t)fuse_from};
         if (K.graph_key != key || (int)K.steps.size() != m) {
             K.drop_graphs();
             K.graph_key = key;

@@ -62,14 +62,47 @@ struct SolverConfig {
     bool use_graphs = false;     // replay each Arnoldi step from a CUDA graph
 };
 
+// The fused coarse tail of the V-cycle (coarse.cu): levels of at most
+// kFuseRows rows, down to the coarsest, in one cooperative launch.
+constexpr int kFuseRows = 65536;
+constexpr int kFuseMaxLevels = 24;
+constexpr int kFuseMaxDeg = 8;
+
 template <class T>
 struct Hierarchy {
     std::vector<Level<T>> lv;
     double *cinv = nullptr;     // coarsest inverse (FP64, row-major)
     int64_t nc = 0;
     int kcap = 0;               // RHS capacity of the work vectors
+    // fused coarse tail: first fused level (-1: none), the device table of
+    // its levels, barrier words, grid size; fuse_off after a give-up
+    int fuse_from = -1;
+    void *fuse_tab = nullptr;
+    unsigned *fuse_bar = nullptr;
+    unsigned long long *fuse_trace = nullptr;   // G2P_FUSE_TRACE time stamps
+    int fuse_blocks = 0;
+    bool fuse_off = false;
+    bool fuse_failed = false;   // a fused launch could not be issued
+    std::vector<double> fuse_key;
     void release(cudaStream_t s);
 };
+
+// First level of the fused tail for k right-hand sides, or -1 (the tail
+// needs at least two levels, k <= 32, and G2P_FUSE unset or nonzero).
+template <class T>
+int coarse_fuse_level(const Hierarchy<T> &H, int k);
+// Builds the device table of the fused levels for k right-hand sides (call
+// outside stream capture; sets H.fuse_from, or leaves it -1).
+template <class T>
+g2p_status coarse_prepare(Hierarchy<T> &H, const SolverConfig &cfg, int k, cudaStream_t s);
+// The V-cycle from level H.fuse_from down and up again, on that level's own
+// b (in) and x (out).
+template <class T>
+void coarse_cycle(Hierarchy<T> &H, int k, cudaStream_t s);
+// Whether a fused launch gave up since the last check; if so the fused path
+// is switched off for this hierarchy (synchronizes s).
+template <class T>
+g2p_status coarse_gave_up(Hierarchy<T> &H, cudaStream_t s, bool *gave_up);
 
 // FP64 hierarchy built from A64 (device CSR); an FP32 copy can be derived.
 g2p_status amg_setup(const Csr<double> &A, const SolverConfig &cfg, cudaStream_t s, int64_t *scan_work_holder,

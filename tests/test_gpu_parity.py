@@ -221,3 +221,52 @@ def test_gpu_extraction_leaves_exact_ad_and_repattern_path_agrees(name, precisio
         assert st.max_rel_residual <= 1e-10
         out.append(Z)
     assert np.array_equal(out[0], out[1])
+
+
+def _extract(g2p, d, precision):
+    from gds2para_gb300 import _lib
+    L = _lib.load()
+    n0 = L.g2p_launch_count()
+    with g2p.FdtdMesh(d) as m:
+        g2p.generateStiff(m)
+        Z, st = g2p.paraGenerator(m, g2p.default_params(precision=precision, rtol=1e-10))
+    return Z, st, L.g2p_launch_count() - n0
+
+
+@pytest.mark.parametrize("name,precision", [("strip_c1", "mixed"), ("manhattan_sweep", "fp64"),
+                                            ("multistrip_small", "mixed")])
+def test_gpu_fused_coarse_cycle_matches_launch_per_kernel(name, precision, g2p, monkeypatch):
+    """The coarse tail of the V-cycle in one cooperative launch (k_coarse_cycle)
+    against the same levels launched kernel by kernel (G2P_FUSE=0): the same
+    arithmetic up to summation order, so Z agrees to the solves' tolerance,
+    with far fewer launches."""
+    d, A, M = golden_layout(name)
+    monkeypatch.setenv("G2P_FUSE", "0")
+    Z0, st0, n0 = _extract(g2p, d, precision)
+    monkeypatch.delenv("G2P_FUSE")
+    Z1, st1, n1 = _extract(g2p, d, precision)
+    assert np.abs(Z1 - Z0).max() / np.abs(Z0).max() < 1e-8
+    assert st1.max_rel_residual <= 1e-10
+    assert n1 < n0, (n1, n0)
+    Zr = A["Z"].reshape(Z1.shape)
+    assert np.abs(Z1 - Zr).max() / np.abs(Zr).max() < 1e-7
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_gpu_fused_coarse_cycle_give_up_repeats_the_solve_unfused(precision, g2p, monkeypatch, capfd):
+    """The fused cycle's grid barrier gives up after a bounded number of
+    polls; with the bound cut to one poll it does, the solver notices at the
+    end of the solve and repeats it with the launch-per-kernel V-cycle, and Z
+    is bit-identical to a run that never fused."""
+    d, A, M = golden_layout("strip_c1")
+    monkeypatch.setenv("G2P_FUSE", "0")
+    Z0, _, _ = _extract(g2p, d, precision)
+    monkeypatch.delenv("G2P_FUSE")
+    monkeypatch.setenv("G2P_FUSE_SPIN_LIMIT", "1")
+    monkeypatch.setenv("G2P_DEBUG", "1")
+    capfd.readouterr()
+    Z1, _, _ = _extract(g2p, d, precision)
+    monkeypatch.delenv("G2P_FUSE_SPIN_LIMIT")
+    monkeypatch.delenv("G2P_DEBUG")
+    assert "fused coarse cycle gave up; solve repeated unfused" in capfd.readouterr().err
+    assert np.array_equal(Z0, Z1)
