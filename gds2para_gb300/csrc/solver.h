@@ -88,7 +88,8 @@ struct Hierarchy {
 };
 
 // First level of the fused tail for k right-hand sides, or -1 (the tail
-// needs at least two levels, k <= 32, and G2P_FUSE unset or nonzero).
+// needs at least two levels, k <= 32, and G2P_FUSE=1: the fused tail is a
+// comparison switch, off by default).
 template <class T>
 int coarse_fuse_level(const Hierarchy<T> &H, int k);
 // Builds the device table of the fused levels for k right-hand sides (call

@@ -236,15 +236,16 @@ def _extract(g2p, d, precision):
 @pytest.mark.parametrize("name,precision", [("strip_c1", "mixed"), ("manhattan_sweep", "fp64"),
                                             ("multistrip_small", "mixed")])
 def test_gpu_fused_coarse_cycle_matches_launch_per_kernel(name, precision, g2p, monkeypatch):
-    """The coarse tail of the V-cycle in one cooperative launch (k_coarse_cycle)
-    against the same levels launched kernel by kernel (G2P_FUSE=0): the same
+    """The coarse tail of the V-cycle in one cooperative launch (k_coarse_cycle,
+    G2P_FUSE=1) against the same levels launched kernel by kernel: the same
     arithmetic up to summation order, so Z agrees to the solves' tolerance,
     with far fewer launches."""
     d, A, M = golden_layout(name)
     monkeypatch.setenv("G2P_FUSE", "0")
     Z0, st0, n0 = _extract(g2p, d, precision)
-    monkeypatch.delenv("G2P_FUSE")
+    monkeypatch.setenv("G2P_FUSE", "1")
     Z1, st1, n1 = _extract(g2p, d, precision)
+    monkeypatch.delenv("G2P_FUSE")
     assert np.abs(Z1 - Z0).max() / np.abs(Z0).max() < 1e-8
     assert st1.max_rel_residual <= 1e-10
     assert n1 < n0, (n1, n0)
@@ -261,11 +262,12 @@ def test_gpu_fused_coarse_cycle_give_up_repeats_the_solve_unfused(precision, g2p
     d, A, M = golden_layout("strip_c1")
     monkeypatch.setenv("G2P_FUSE", "0")
     Z0, _, _ = _extract(g2p, d, precision)
-    monkeypatch.delenv("G2P_FUSE")
+    monkeypatch.setenv("G2P_FUSE", "1")
     monkeypatch.setenv("G2P_FUSE_SPIN_LIMIT", "1")
     monkeypatch.setenv("G2P_DEBUG", "1")
     capfd.readouterr()
     Z1, _, _ = _extract(g2p, d, precision)
+    monkeypatch.delenv("G2P_FUSE")
     monkeypatch.delenv("G2P_FUSE_SPIN_LIMIT")
     monkeypatch.delenv("G2P_DEBUG")
     assert "fused coarse cycle gave up; solve repeated unfused" in capfd.readouterr().err
