@@ -303,12 +303,14 @@ def _side_len(coord, i, c, N):
 # Named workloads
 # --------------------------------------------------------------------------
 
-def microstrip(nx=101, ny=41, nz=11, pitch=1e-6, freq_ghz=1.0) -> Layout:
+def microstrip(nx=101, ny=41, nz=11, pitch=1e-6, freq_ghz=1.0, freq_end_ghz=None, nfreq=1,
+               freq_scale=1) -> Layout:
     """Single microstrip over a ground slab, one lumped port at x = 0.
 
     Cell layers: z 0-1 ground (sigma Cu), 1-8 dielectric (eps_r 3.9), 8-9
     strip (4 cells wide at y 18..22 of 41 nodes, full x), 9-10 air.  The
-    default is 101 x 41 x 11 nodes at 1 um."""
+    default is 101 x 41 x 11 nodes at 1 um and one frequency; nfreq > 1
+    sweeps freq_ghz..freq_end_ghz (freq_scale 1 linear, 0 logarithmic)."""
     assert nz >= 5
     zs = nz - 1
     strip_z = zs - 2
@@ -323,7 +325,8 @@ def microstrip(nx=101, ny=41, nz=11, pitch=1e-6, freq_ghz=1.0) -> Layout:
     boxes = [Box(0, nx - 1, 0, ny - 1, 0, 1), Box(0, nx - 1, y0, y0 + w, strip_z, strip_z + 1)]
     ports = [[PortSpec((0, yc, strip_z), (0, yc, 1))]]
     return Layout("microstrip", nx, ny, nz, (pitch, pitch, pitch), eps, sig, boxes, ports,
-                  freq_start=freq_ghz, freq_end=freq_ghz, freq_unit=1e9, nfreq=1)
+                  freq_start=freq_ghz, freq_end=freq_ghz if freq_end_ghz is None else freq_end_ghz, freq_unit=1e9,
+                  nfreq=nfreq, freq_scale=freq_scale)
 
 
 def multistrip(nx=256, ny=256, nz=16, n_strips=32, pitch=1e-6, width=None, freq_start=1e7, freq_end=1e11,

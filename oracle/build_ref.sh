@@ -25,6 +25,17 @@ wait
 g++ -o "$OUT/ref_gds" "$OUT/ref_gds.o" "$OUT/mesh.o" "$OUT/mkl_sparse_shim.o" -lm
 g++ -o "$OUT/ref_pipeline" "$OUT/ref_harness.o" "$OUT/mesh.o" "$OUT/generateStiff.o" "$OUT/matrixCon.o" \
     "$OUT/mkl_sparse_shim.o" "$OUT/solver.o" -lm
+# oracle/_ref/ref_pipeline_vh: the same harness with the reference's
+# full-wave (Vh) path compiled in (oracle/ref_matrixcon_vh.cpp) and the
+# dense LAPACK/PARDISO stand-ins; findVh.cpp supplies matrix_multi
+g++ $CXXFLAGS -c "$HERE/ref_matrixcon_vh.cpp" -o "$OUT/matrixCon_vh.o" &
+g++ $CXXFLAGS -DG2P_REF_VH -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness_vh.o" &
+g++ $CXXFLAGS -c "$REF/src/findVh.cpp" -o "$OUT/findVh.o" &
+g++ $CXXFLAGS -c "$HERE/lapacke_shim.cpp" -o "$OUT/lapacke_shim.o" &
+wait
+g++ -o "$OUT/ref_pipeline_vh" "$OUT/ref_harness_vh.o" "$OUT/mesh.o" "$OUT/generateStiff.o" "$OUT/matrixCon_vh.o" \
+    "$OUT/findVh.o" "$OUT/mkl_sparse_shim.o" "$OUT/lapacke_shim.o" "$OUT/solver.o" -lm
+echo "built $OUT/ref_pipeline_vh"
 # oracle/_ref/ref_pipeline_gb300: the same harness with generateStiff,
 # hypreSolve and paraGenerator taken from the library's reference-side shim
 # (oracle/gb300_path.cpp), linked with libgds2para_gb300.so when it is built

@@ -26,15 +26,27 @@ REF_BIN = os.path.join(HERE, "_ref", "ref_pipeline")
 
 def build_coracle(force: bool = False) -> str:
     srcs = [os.path.join(HERE, f) for f in ("solver.c", "pipeline.c")]
+    shim = os.path.join(HERE, "lapacke_shim.cpp")
     hdr = os.path.join(HERE, "oracle.h")
     if not force and os.path.exists(LIB):
         mt = os.path.getmtime(LIB)
-        if all(os.path.getmtime(s) <= mt for s in srcs + [hdr]):
+        if all(os.path.getmtime(s) <= mt for s in srcs + [hdr, shim]):
             return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + f".tmp{os.getpid()}"
-    subprocess.check_call(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
-                           "-o", tmp] + srcs + ["-lm"])
+    objs = []
+    for src in srcs:
+        obj = os.path.join(BUILD, os.path.basename(src) + f".{os.getpid()}.o")
+        subprocess.check_call(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-c", src, "-o", obj])
+        objs.append(obj)
+    # the dense stand-ins of the full-wave path, built with the flags the
+    # reference-compiled oracle uses for them (oracle/build_ref.sh)
+    obj = os.path.join(BUILD, f"lapacke_shim.{os.getpid()}.o")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-c", shim, "-o", obj])
+    objs.append(obj)
+    subprocess.check_call(["g++", "-shared", "-o", tmp] + objs + ["-lm"])
+    for o in objs:
+        os.remove(o)
     os.replace(tmp, LIB)
     return LIB
 
@@ -102,6 +114,12 @@ class COracle:
                                           C.POINTER(C.c_double)]
         L.g2po_job_z.argtypes = [C.c_void_p, C.c_void_p]
         L.g2po_job_destroy.argtypes = [C.c_void_p]
+        L.g2po_job_enable_vh.argtypes = [C.c_void_p]
+        L.g2po_job_nr.argtypes = [C.c_void_p]
+        L.g2po_job_nr.restype = C.c_int64
+        L.g2po_find_vh.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int64)]
+        L.g2po_job_vh_z.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+        L.free.argtypes = [C.c_void_p]
 
     def _mesh(self, d):
         keep = {
@@ -286,6 +304,41 @@ class OracleJob:
         for it, rel in res:
             self.iterations += it
             self.max_rel_residual = max(self.max_rel_residual, rel)
+
+    def enable_vh(self):
+        """Keep each port's V0 fields for the full-wave path and build S
+        (call before any stage)."""
+        if self.O.lib.g2po_job_enable_vh(self.h) != 0:
+            raise RuntimeError("g2po_job_enable_vh failed")
+
+    def find_vh(self, k: int):
+        """find_Vh(k): returns Vh as an (nr, mm) complex array."""
+        p = C.POINTER(C.c_double)()
+        mm = C.c_int64()
+        self.O.lib.g2po_find_vh(self.h, k, C.byref(p), C.byref(mm))
+        nr = int(self.O.lib.g2po_job_nr(self.h))
+        a = np.ctypeslib.as_array(p, (max(2 * nr * mm.value, 1),))[: 2 * nr * mm.value].copy()
+        self.O.lib.free(p)
+        vh = (a[0::2] + 1j * a[1::2]).reshape(mm.value, nr).T
+        return vh
+
+    def vh_z(self, vh):
+        """The Vh-corrected Z of every port and frequency: (z_vh, z_ref),
+        each (nfreq, P, P) complex with z[f, p, q] = response at port q to
+        port p (sys->x's order before any transposition); z_ref carries the
+        reference's first-frequency start from the V0 Z."""
+        d = self.d
+        nr, mm = vh.shape
+        buf = np.empty(2 * nr * mm)
+        buf[0::2] = vh.T.reshape(-1).real
+        buf[1::2] = vh.T.reshape(-1).imag
+        zv = np.zeros(2 * d.nfreq * d.num_ports ** 2)
+        zf = np.zeros_like(zv)
+        rc = self.O.lib.g2po_job_vh_z(self.h, buf.ctypes.data, mm, zv.ctypes.data, zf.ctypes.data)
+        if rc != 0:
+            raise RuntimeError("g2po_job_vh_z failed (run every port's stages with enable_vh first)")
+        shape = (d.nfreq, d.num_ports, d.num_ports)
+        return (zv[0::2] + 1j * zv[1::2]).reshape(shape), (zf[0::2] + 1j * zf[1::2]).reshape(shape)
 
     def z(self):
         d = self.d

@@ -129,6 +129,19 @@ int g2po_job_port_stage(g2po_job *j, int port, const g2po_solver_opts *o, g2po_s
 void g2po_job_z(const g2po_job *j, double *z_out);
 void g2po_job_destroy(g2po_job *j);
 
+/* The full-wave (Vh) path, which the reference compiles out (SKIP_VH,
+ * fdtd.hpp:76): g2po_job_enable_vh before any port's stages keeps the V0
+ * fields it needs and builds S; g2po_find_vh restates find_Vh(k)
+ * (fdtd.hpp:3577-3859) into vh (nr x mm complex, column-major, interleaved,
+ * malloc'd; nr = N_edge - bden); g2po_job_vh_z restates the per-port,
+ * per-frequency Vh correction (matrixCon.cpp:609-805) and
+ * Construct_Z_V0_Vh (fdtd.hpp:4133-4170).  The dense eigen and linear
+ * solves come from oracle/lapacke_shim.cpp. */
+int g2po_job_enable_vh(g2po_job *j);
+int64_t g2po_job_nr(const g2po_job *j);
+int g2po_find_vh(g2po_job *j, int k, double **vh, int64_t *mm);
+int g2po_job_vh_z(g2po_job *j, const double *vh, int64_t mm, double *z_vh, double *z_ref);
+
 #ifdef __cplusplus
 }
 #endif

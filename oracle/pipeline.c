@@ -540,7 +540,11 @@ static double freq_of(const g2po_mesh *m, int id) {
  * each solve builds its own hierarchy as hypreSolve does. */
 typedef struct {
     double *J, *y0d, *yd1, *yc, *yd2, *ydt, *bd, *bc, *crhs, *y0c;
+    double *ydat;  /* V0da * y0d (the full-wave path's u0a) */
     int stage;     /* next stage to run: 0 first Ad solve, 1 Ac solve, 2 second Ad solve, 3 done */
+    /* kept for the full-wave path (g2po_job_enable_vh): u0, u0a (2 columns
+       over the non-PEC edges, real), yd (complex over all edges) and J */
+    double *u0, *u0a, *yd_re, *yd_im, *Jkeep;
 } port_state;
 
 struct g2po_job {
@@ -552,6 +556,10 @@ struct g2po_job {
     g2po_csr Ad, Ac;
     port_state *ps;
     double *zr, *zi;
+    int keep_vh;                 /* keep each port's fields for the full-wave path */
+    g2po_csr S;                  /* stiffness over the non-PEC edges (full-wave path) */
+    int64_t *map_r;              /* mapEdgeR: non-PEC edge index -> edge */
+    int64_t nr;                  /* N_edge - bden */
 };
 
 g2po_job *g2po_job_create(const g2po_mesh *m, g2po_para_stats *st) {
@@ -577,10 +585,59 @@ g2po_job *g2po_job_create(const g2po_mesh *m, g2po_para_stats *st) {
     return j;
 }
 
-static void port_free(port_state *q) {
+static void port_free_work(port_state *q) {
     free(q->J); free(q->y0d); free(q->yd1); free(q->yc); free(q->yd2); free(q->ydt); free(q->bd); free(q->bc);
-    free(q->crhs); free(q->y0c);
+    free(q->crhs); free(q->y0c); free(q->ydat);
+    q->J = q->y0d = q->yd1 = q->yc = q->yd2 = q->ydt = q->bd = q->bc = q->crhs = q->y0c = q->ydat = NULL;
+}
+
+static void port_free(port_state *q) {
+    port_free_work(q);
+    free(q->u0); free(q->u0a); free(q->yd_re); free(q->yd_im); free(q->Jkeep);
     memset(q, 0, sizeof(*q));
+}
+
+/* The port's V0 fields the full-wave path reads (matrixCon.cpp:414-430,
+ * 545-576): u0 and u0a, two unit columns over the non-PEC edges (the first
+ * Ad solve's V0d and V0da products, then the second Ad and the Ac solves'
+ * sums), and yd = (yd2 + yc) - i yd1 over all edges, with J. */
+static void keep_vh_fields(struct g2po_job *j, port_state *q) {
+    const int64_t ne = j->d.N_edge, nr = j->nr;
+    double *yd2a = (double *)calloc((size_t)ne, sizeof(double)), *yca = (double *)calloc((size_t)ne, sizeof(double));
+    v0_mv(&j->vd, 1, q->y0d, yd2a, ne);
+    v0_mv(&j->vc, 1, q->y0c, yca, ne);
+    double nn = 0, nna = 0;
+    for (int64_t e = 0; e < ne; e++) { nn += q->yd1[e] * q->yd1[e]; nna += q->ydat[e] * q->ydat[e]; }
+    nn = sqrt(nn);
+    nna = sqrt(nna);
+    q->u0 = (double *)calloc((size_t)(2 * nr), sizeof(double));
+    q->u0a = (double *)calloc((size_t)(2 * nr), sizeof(double));
+    for (int64_t i = 0; i < nr; i++) {
+        q->u0[i] = q->yd1[j->map_r[i]] / nn;
+        q->u0a[i] = q->ydat[j->map_r[i]] / nna;
+    }
+    nn = 0;
+    nna = 0;
+    for (int64_t e = 0; e < ne; e++) {
+        nn += (q->yd2[e] + q->yc[e]) * (q->yd2[e] + q->yc[e]);
+        nna += (yd2a[e] + yca[e]) * (yd2a[e] + yca[e]);
+    }
+    nn = sqrt(nn);
+    nna = sqrt(nna);
+    for (int64_t i = 0; i < nr; i++) {
+        q->u0[nr + i] = (q->yd2[j->map_r[i]] + q->yc[j->map_r[i]]) / nn;
+        q->u0a[nr + i] = (yd2a[j->map_r[i]] + yca[j->map_r[i]]) / nna;
+    }
+    q->yd_re = (double *)malloc(sizeof(double) * (size_t)ne);
+    q->yd_im = (double *)malloc(sizeof(double) * (size_t)ne);
+    for (int64_t e = 0; e < ne; e++) {
+        q->yd_re[e] = (q->yd2[e] - 0.0) + q->yc[e];
+        q->yd_im[e] = 0.0 - q->yd1[e];
+    }
+    q->Jkeep = q->J;
+    q->J = NULL;
+    free(yd2a);
+    free(yca);
 }
 
 static void job_solve(const g2po_csr *A, g2po_amg_handle *H, const double *b, double *x,
@@ -626,6 +683,10 @@ static int job_stage(g2po_job *j, int p, g2po_amg_handle *H, const g2po_solver_o
         /* :401-412 */
         for (int64_t i = 0; i < j->vd.ncol; i++) q->y0d[i] /= omega;
         v0_mv(&j->vd, 0, q->y0d, q->ydt, ne);
+        if (j->keep_vh) {
+            q->ydat = (double *)calloc((size_t)ne, sizeof(double));
+            v0_mv(&j->vd, 1, q->y0d, q->ydat, ne);
+        }
         /* :436-461 */
         v0t_mv(&j->vc, 1, q->J, q->bc);
         for (int64_t i = 0; i < j->vc.ncol; i++) q->bc[i] *= -1.0;
@@ -667,7 +728,8 @@ static int job_stage(g2po_job *j, int p, g2po_amg_handle *H, const g2po_solver_o
             j->zr[r + (int64_t)P * p] = re / cur;
             j->zi[r + (int64_t)P * p] = im / cur;
         }
-        port_free(q);
+        if (j->keep_vh) keep_vh_fields(j, q);
+        port_free_work(q);
     } else {
         return -1;
     }
@@ -706,6 +768,8 @@ void g2po_job_z(const g2po_job *j, double *z_out) {
 
 void g2po_job_destroy(g2po_job *j) {
     if (!j) return;
+    g2po_csr_free(&j->S);
+    free(j->map_r);
     for (int p = 0; p < j->m->num_ports; p++) port_free(&j->ps[p]);
     free(j->ps); free(j->zr); free(j->zi);
     g2po_v0_free(&j->vd); g2po_v0_free(&j->vc);
@@ -743,5 +807,311 @@ sampled:
     if (Hd) g2po_amg_destroy(Hd);
     if (Hc) g2po_amg_destroy(Hc);
     g2po_job_destroy(j);
+    return 0;
+}
+
+/* ------------------------------------------------- the full-wave (Vh) path
+ * The reference compiles it out (SKIP_VH, fdtd.hpp:76).  With it in,
+ * paraGenerator runs find_Vh(1000) once (matrixCon.cpp:331-333) and, for
+ * every port and frequency, corrects the V0 field by a Galerkin projection on
+ * the Vh eigenmodes (matrixCon.cpp:609-805); the dense LAPACK calls go to
+ * oracle/lapacke_shim.cpp. */
+typedef struct { double re, im; } zc;
+long long LAPACKE_dhseqr(int, char, char, long long, long long, long long, double *, long long, double *, double *,
+                         double *, long long);
+long long LAPACKE_dhsein(int, char, char, char, long long *, long long, const double *, long long, double *,
+                         const double *, double *, long long, double *, long long, long long, long long *,
+                         long long *, long long *);
+long long LAPACKE_zcgesv(int, long long, long long, zc *, long long, long long *, zc *, long long, zc *, long long,
+                         long long *);
+long long LAPACKE_zgesv(int, long long, long long, zc *, long long, long long *, zc *, long long);
+
+#define SIGMA_CU (5.8e+7)     /* fdtd.hpp:50, the Vh products' conductivity */
+
+int g2po_job_enable_vh(g2po_job *j) {
+    if (!j) return -1;
+    j->keep_vh = 1;
+    if (g2po_stiffness(j->m, j->map_edge, j->pec_edge, &j->S) != 0) return -1;
+    j->nr = j->S.n;
+    j->map_r = (int64_t *)malloc(sizeof(int64_t) * (size_t)(j->nr > 0 ? j->nr : 1));
+    for (int64_t e = 0; e < j->d.N_edge; e++)
+        if (j->map_edge[e] >= 0) j->map_r[j->map_edge[e]] = e;
+    for (int64_t r = 0; r < j->nr; r++)
+        if (j->S.ptr[r + 1] == j->S.ptr[r]) return -2;      /* every row of S has its diagonal */
+    return 0;
+}
+
+int64_t g2po_job_nr(const g2po_job *j) { return j->nr; }
+
+/* find_Vh(k) (fdtd.hpp:3577-3859): k Arnoldi steps (modified Gram-Schmidt)
+ * on the 2N operator [[0, I], [-eps^-1 S / scale^2, -eps^-1 sigma / scale]],
+ * the Hessenberg matrix's eigenvalues, right eigenvectors of those with
+ * |Im| > 1e-6, and Vh = V(1:N, 1:k) * eigenvectors.  *vh: nr x mm complex,
+ * column-major, (re, im) interleaved; malloc'd. */
+int g2po_find_vh(g2po_job *jb, int k, double **vh_out, int64_t *mm_out) {
+    const g2po_mesh *m = jb->m;
+    const dims_t d = jb->d;
+    const int64_t nr = jb->nr, n2 = 2 * nr;
+    const double scale = 1.e+14;
+    const g2po_csr *S = &jb->S;
+    double *V = (double *)calloc((size_t)((k + 1) * n2), sizeof(double));
+    double *w = (double *)calloc((size_t)n2, sizeof(double));
+    double *H = (double *)calloc((size_t)k * k, sizeof(double));
+    for (int64_t i = 0; i < n2; i++) V[i] = 1 / sqrt(2 * nr);
+    for (int jj = 1; jj <= k; jj++) {
+        const double *vp = V + (int64_t)(jj - 1) * n2;
+        for (int64_t row = 0; row < nr; row++) {
+            const int64_t e = jb->map_r[row];
+            w[nr + row] = 0;
+            w[row] = vp[nr + row];
+            for (int64_t q = S->ptr[row]; q < S->ptr[row + 1]; q++)
+                w[nr + row] += -S->val[q] * vp[S->col[q]] / (m->stack_epsn[e / d.L] * EPSILON0 * pow(scale, 2));
+            if (m->mark_edge[e] != 0)
+                w[nr + row] += -vp[nr + row] * m->stack_sign[e / d.L] / (m->stack_epsn[e / d.L] * EPSILON0 * scale);
+        }
+        double *hcol = H + (int64_t)(jj - 1) * k;
+        for (int i = 0; i <= jj - 1; i++) {
+            const double *vi = V + (int64_t)i * n2;
+            for (int64_t in = 0; in < n2; in++) hcol[i] += vi[in] * w[in];
+            for (int64_t in = 0; in < n2; in++) w[in] -= hcol[i] * vi[in];
+        }
+        double temp;
+        if (jj == k) {
+            temp = 0;
+            for (int64_t i = 0; i < n2; i++) temp += pow(w[i], 2);
+            temp = sqrt(temp);
+        } else {
+            for (int64_t i = 0; i < n2; i++) hcol[jj] += pow(w[i], 2);
+            hcol[jj] = sqrt(hcol[jj]);
+            temp = hcol[jj];
+        }
+        for (int64_t i = 0; i < n2; i++) V[(int64_t)jj * n2 + i] = w[i] / temp;
+    }
+    double *H1 = (double *)calloc((size_t)k * k, sizeof(double));
+    for (int i = 0; i < k; i++)
+        for (int c = 0; c < k; c++)
+            if (i <= c + 1) H1[c * k + i] = H[c * k + i];
+    double *wr = (double *)malloc(sizeof(double) * k), *wi = (double *)malloc(sizeof(double) * k);
+    LAPACKE_dhseqr(102, 'E', 'N', k, 1, k, H, k, wr, wi, NULL, k);
+    long long *select = (long long *)calloc((size_t)k, sizeof(long long));
+    long long mm = 0;
+    for (int i = 0; i < k; i++) {
+        if (fabs(wi[i]) > 1e-6) { select[i] = 1; mm++; }
+    }
+    long long mret = 0;
+    long long *ifaill = (long long *)calloc((size_t)(mm > 0 ? mm : 1), sizeof(long long));
+    long long *ifailr = (long long *)calloc((size_t)(mm > 0 ? mm : 1), sizeof(long long));
+    double *vr = (double *)calloc((size_t)(k * (mm > 0 ? mm : 1)), sizeof(double));
+    LAPACKE_dhsein(102, 'R', 'Q', 'N', select, k, H1, k, wr, wi, NULL, k, vr, k, mm, &mret, ifaill, ifailr);
+    zc *v = (zc *)calloc((size_t)(k * (mm > 0 ? mm : 1)), sizeof(zc));
+    for (int i = 0; i < k; i++) {
+        int64_t t = 0;
+        for (int c = 0; c < k; c++)
+            if (select[c] == 1) {
+                v[t * k + i].re = vr[t * k + i];
+                v[t * k + i].im = vr[(t + 1) * k + i];
+                v[(t + 1) * k + i].re = vr[t * k + i];
+                v[(t + 1) * k + i].im = -vr[(t + 1) * k + i];
+                t += 2;
+                c++;
+            }
+    }
+    double *vh = (double *)malloc(sizeof(double) * (size_t)(2 * nr * (mm > 0 ? mm : 1)));
+    for (int64_t i = 0; i < mm; i++)
+        for (int64_t r = 0; r < nr; r++) {
+            double re = 0, im = 0;
+            for (int in = 0; in < k; in++) {
+                re += V[(int64_t)in * n2 + r] * v[i * k + in].re;
+                im += V[(int64_t)in * n2 + r] * v[i * k + in].im;
+            }
+            vh[2 * (i * nr + r)] = re;
+            vh[2 * (i * nr + r) + 1] = im;
+        }
+    free(V); free(w); free(H); free(H1); free(wr); free(wi); free(select); free(ifaill); free(ifailr); free(vr);
+    free(v);
+    *vh_out = vh;
+    *mm_out = mm;
+    return 0;
+}
+
+/* matrix_multi (findVh.cpp:1205): 'T' gives conj(a)^T b, 'N' gives a b, for
+ * column-major complex a (arow x acol) and b (brow x bcol). */
+static void zmulti(char op, const zc *a, int64_t arow, int64_t acol, const zc *b, int64_t brow, int64_t bcol, zc *out) {
+    if (op == 'T') {
+        for (int64_t i = 0; i < acol; i++)
+            for (int64_t c = 0; c < bcol; c++) {
+                double re = 0, im = 0;
+                for (int64_t r = 0; r < arow; r++) {
+                    re = re + a[i * arow + r].re * b[c * brow + r].re + a[i * arow + r].im * b[c * brow + r].im;
+                    im = im - a[i * arow + r].im * b[c * brow + r].re + a[i * arow + r].re * b[c * brow + r].im;
+                }
+                out[c * acol + i].re = re;
+                out[c * acol + i].im = im;
+            }
+    } else {
+        for (int64_t i = 0; i < arow; i++)
+            for (int64_t c = 0; c < bcol; c++) {
+                double re = 0, im = 0;
+                for (int64_t r = 0; r < acol; r++) {
+                    re = re + a[r * arow + i].re * b[c * brow + r].re - a[r * arow + i].im * b[c * brow + r].im;
+                    im = im + a[r * arow + i].im * b[c * brow + r].re + a[r * arow + i].re * b[c * brow + r].im;
+                }
+                out[c * arow + i].re = re;
+                out[c * arow + i].im = im;
+            }
+    }
+}
+
+/* (-w^2 D_eps + i w D_sig) on one complex entry of the non-PEC edge r, as the
+ * Vh products write it (matrixCon.cpp:625-634): the layer index of edge e is
+ * (e + N_edge_v) / L there, and sigma is SIGMA (fdtd.hpp:50). */
+static zc diag_op(const g2po_job *jb, int64_t r, zc x, double freq) {
+    const int64_t e = jb->map_r[r];
+    const double eps = jb->m->stack_epsn[(e + jb->d.Nv) / jb->d.L];
+    zc y;
+    if (jb->m->mark_edge[e] != 0) {
+        y.re = x.re * (-freq * freq * 4 * pow(M_PI, 2)) * eps * EPSILON0 - 2 * M_PI * freq * x.im * SIGMA_CU;
+        y.im = x.re * (freq * 2 * M_PI) * SIGMA_CU - x.im * (freq * freq * 4 * pow(M_PI, 2)) * eps * EPSILON0;
+    } else {
+        y.re = x.re * (-freq * freq * 4 * pow(M_PI, 2)) * eps * EPSILON0;
+        y.im = -x.im * (freq * freq * 4 * pow(M_PI, 2)) * eps * EPSILON0;
+    }
+    return y;
+}
+
+/* The Vh correction of every port at every frequency (matrixCon.cpp:609-805)
+ * and Construct_Z_V0_Vh (fdtd.hpp:4133-4170).  Every port must have run its
+ * three stages with g2po_job_enable_vh on.  z_vh[f][q + P p] (complex,
+ * interleaved): Construct_Z_V0_Vh into zeros.  z_ref: sys->x as the
+ * reference leaves it with PRINT_V0_Vh_Z_PARAM, where the first frequency's
+ * entries start from Construct_Z_V0's V0 values instead of zero. */
+int g2po_job_vh_z(g2po_job *jb, const double *vh_in, int64_t mm, double *z_vh, double *z_ref) {
+    const g2po_mesh *m = jb->m;
+    const dims_t d = jb->d;
+    const int64_t nr = jb->nr;
+    const int P = m->num_ports;
+    const zc *Vh0 = (const zc *)vh_in;
+    const g2po_csr *S = &jb->S;
+    zc *V_re2 = (zc *)malloc(sizeof(zc) * (size_t)(nr * mm)), *Vh = (zc *)malloc(sizeof(zc) * (size_t)(nr * mm));
+    zc *tmp = (zc *)malloc(sizeof(zc) * (size_t)(nr * (mm > 2 ? mm : 2)));
+    zc *y_re = (zc *)calloc((size_t)(2 * mm), sizeof(zc)), *y_new = (zc *)calloc((size_t)(2 * mm), sizeof(zc));
+    zc *m_new = (zc *)calloc((size_t)(nr * mm), sizeof(zc)), *m_h = (zc *)calloc((size_t)(mm * mm), sizeof(zc));
+    zc *rhs_h = (zc *)calloc((size_t)mm, sizeof(zc)), *rhs_h0 = (zc *)calloc((size_t)mm, sizeof(zc));
+    zc *Jc = (zc *)calloc((size_t)nr, sizeof(zc)), *y_h = (zc *)calloc((size_t)nr, sizeof(zc));
+    zc *final_x = (zc *)malloc(sizeof(zc) * (size_t)nr);
+    zc u0[2], tmp4[4];
+    long long ipiv2[2], iter = 0;
+    long long *ipiv = (long long *)malloc(sizeof(long long) * (size_t)(mm > 0 ? mm : 1));
+    memset(z_vh, 0, sizeof(double) * 2 * (size_t)m->nfreq * P * P);
+    memset(z_ref, 0, sizeof(double) * 2 * (size_t)m->nfreq * P * P);
+    for (int p = 0; p < P; p++) {
+        const port_state *q = &jb->ps[p];
+        if (!q->u0) return -1;
+        zc *U0 = (zc *)calloc((size_t)(2 * nr), sizeof(zc)), *U0a = (zc *)calloc((size_t)(2 * nr), sizeof(zc));
+        for (int64_t i = 0; i < 2 * nr; i++) { U0[i].re = q->u0[i]; U0a[i].re = q->u0a[i]; }
+        /* the reference's first frequency starts from Construct_Z_V0 */
+        for (int r = 0; r < P; r++) {
+            z_ref[2 * (r + (int64_t)P * p)] = jb->zr[r + (int64_t)P * p];
+            z_ref[2 * (r + (int64_t)P * p) + 1] = jb->zi[r + (int64_t)P * p];
+        }
+        for (int fi = 0; fi < m->nfreq; fi++) {
+            const double freq = freq_of(m, fi);
+            /* Vh = Vh - u0 ((u0a' A u0) \\ (u0a' A Vh)) */
+            for (int64_t r = 0; r < nr; r++)
+                for (int64_t c = 0; c < mm; c++) V_re2[c * nr + r] = diag_op(jb, r, Vh0[c * nr + r], freq);
+            zmulti('T', U0a, nr, 2, V_re2, nr, mm, y_re);
+            for (int64_t r = 0; r < nr; r++)
+                for (int c = 0; c < 2; c++) tmp[c * nr + r] = diag_op(jb, r, U0[c * nr + r], freq);
+            zmulti('T', U0a, nr, 2, tmp, nr, 2, tmp4);
+            LAPACKE_zcgesv(102, 2, mm, tmp4, 2, ipiv2, y_re, 2, y_new, 2, &iter);
+            zmulti('N', U0, nr, 2, y_new, 2, mm, m_new);
+            for (int64_t r = 0; r < nr; r++)
+                for (int64_t c = 0; c < mm; c++) {
+                    Vh[c * nr + r].re = Vh0[c * nr + r].re - m_new[c * nr + r].re;
+                    Vh[c * nr + r].im = Vh0[c * nr + r].im - m_new[c * nr + r].im;
+                }
+            /* Vh' (S - w^2 D_eps + i w D_sig) Vh */
+            for (int64_t c = 0; c < mm; c++) {
+                zc *t = tmp + c * nr;
+                for (int64_t r = 0; r < nr; r++) t[r].re = t[r].im = 0;
+                for (int64_t r = 0; r < nr; r++)
+                    for (int64_t qq = S->ptr[r]; qq < S->ptr[r + 1]; qq++) {
+                        t[r].re += S->val[qq] * Vh[c * nr + S->col[qq]].re;
+                        t[r].im += S->val[qq] * Vh[c * nr + S->col[qq]].im;
+                    }
+                for (int64_t r = 0; r < nr; r++) {
+                    const int64_t e = jb->map_r[r];
+                    const double eps = m->stack_epsn[(e + d.Nv) / d.L];
+                    const zc x = Vh[c * nr + r];
+                    if (m->mark_edge[e] != 0) {
+                        t[r].re += -pow(freq * 2 * M_PI, 2) * eps * EPSILON0 * x.re - freq * 2 * M_PI * SIGMA_CU * x.im;
+                        t[r].im += -pow(freq * 2 * M_PI, 2) * eps * EPSILON0 * x.im + freq * 2 * M_PI * SIGMA_CU * x.re;
+                    } else {
+                        t[r].re += -pow(freq * 2 * M_PI, 2) * eps * EPSILON0 * x.re;
+                        t[r].im += -pow(freq * 2 * M_PI, 2) * eps * EPSILON0 * x.im;
+                    }
+                }
+            }
+            zmulti('T', Vh, nr, mm, tmp, nr, mm, m_h);
+            /* -i w Vh' J */
+            memset(Jc, 0, sizeof(zc) * (size_t)nr);
+            for (int64_t e = 0; e < d.N_edge; e++)
+                if (q->Jkeep[e] != 0) Jc[jb->map_edge[e]].im = -1 * freq * 2 * M_PI;
+            zmulti('T', Vh, nr, mm, Jc, nr, 1, rhs_h);
+            /* minus Vh' A u, u the V0 field at this frequency */
+            const double fS = m->freq_start, fU = m->freq_unit;
+            for (int64_t r = 0; r < nr; r++) {
+                const int64_t e = jb->map_r[r];
+                const double eps = m->stack_epsn[(e + d.Nv) / d.L];
+                const double yr = q->yd_re[e], yi = q->yd_im[e];
+                if (m->mark_edge[e] != 0) {
+                    tmp[r].re = -pow(freq * 2 * M_PI, 2) * eps * EPSILON0 * yr - freq * 2 * M_PI * SIGMA_CU * yi * fS * fU / freq;
+                    tmp[r].im = freq * 2 * M_PI * SIGMA_CU * yr - pow(freq * 2 * M_PI, 2) * eps * EPSILON0 * yi * fS * fU / freq;
+                } else {
+                    tmp[r].re = -pow(freq * 2 * M_PI, 2) * eps * EPSILON0 * yr;
+                    tmp[r].im = -pow(freq * 2 * M_PI, 2) * eps * EPSILON0 * yi * fS * fU / freq;
+                }
+            }
+            zmulti('T', Vh, nr, mm, tmp, nr, 1, rhs_h0);
+            for (int64_t c = 0; c < mm; c++) {
+                rhs_h[c].re = rhs_h[c].re - rhs_h0[c].re;
+                rhs_h[c].im = rhs_h[c].im - rhs_h0[c].im;
+            }
+            LAPACKE_zgesv(102, mm, 1, m_h, mm, ipiv, rhs_h, mm);
+            zmulti('N', Vh, nr, mm, rhs_h, mm, 1, y_h);
+            for (int64_t r = 0; r < nr; r++) {
+                const int64_t e = jb->map_r[r];
+                final_x[r].re = q->yd_re[e] + y_h[r].re + 0.0;
+                final_x[r].im = q->yd_im[e] * m->freq_start * m->freq_unit / freq + y_h[r].im;
+            }
+            /* Construct_Z_V0_Vh (fdtd.hpp:4133-4170) */
+            double cur = 0.;
+            for (int s = m->port_side_ptr[p]; s < m->port_side_ptr[p + 1]; s++) cur += m->side_area[s];
+            for (int r = 0; r < P; r++) {
+                const int s = m->port_side_ptr[r];
+                double *zv = z_vh + 2 * ((int64_t)fi * P * P + r + (int64_t)P * p);
+                double *zf = z_ref + 2 * ((int64_t)fi * P * P + r + (int64_t)P * p);
+                for (int64_t kk = m->side_edge_ptr[s]; kk < m->side_edge_ptr[s + 1]; kk++) {
+                    const int64_t e = m->side_edges[kk], rr = e % d.L;
+                    double leng;
+                    if (rr >= d.Ns) { int64_t inz = e / d.L; leng = m->zn[inz + 1] - m->zn[inz]; }
+                    else if (rr >= d.Ny * (d.Nx + 1)) { int64_t inx = (rr - d.Ny * (d.Nx + 1)) / (d.Ny + 1); leng = m->xn[inx + 1] - m->xn[inx]; }
+                    else { int64_t iny = rr % d.Ny; leng = m->yn[iny + 1] - m->yn[iny]; }
+                    const double dir = m->side_dir[s] * 1.0;
+                    const zc fx = final_x[jb->map_edge[e]];
+                    zv[0] -= fx.re * leng * dir;
+                    zv[1] -= fx.im * leng * dir;
+                    zf[0] -= fx.re * leng * dir;
+                    zf[1] -= fx.im * leng * dir;
+                }
+                zv[0] /= cur; zv[1] /= cur;
+                zf[0] /= cur; zf[1] /= cur;
+            }
+        }
+        free(U0); free(U0a);
+    }
+    (void)u0;
+    free(V_re2); free(Vh); free(tmp); free(y_re); free(y_new); free(m_new); free(m_h); free(rhs_h); free(rhs_h0);
+    free(Jc); free(y_h); free(final_x); free(ipiv);
     return 0;
 }

@@ -302,6 +302,17 @@ int main(int argc, char **argv) {
         sys.acu_cnno.clear();
         free(map);
     }
+#ifdef G2P_REF_VH
+    /* the full-wave build: the reference's own find_Vh(1000), as
+       paraGenerator runs it (matrixCon.cpp:332-333), dumped once */
+    if (meta["skipPara"] == 0) {
+        sys.find_Vh(1000);
+        write_arr("Vh.c128", (double *)sys.Vh, 2 * (size_t)(sys.N_edge - sys.bden) * (size_t)sys.leng_Vh);
+        meta_out << "leng_Vh " << sys.leng_Vh << "\n";
+        delete[] sys.Vh;
+        sys.Vh = NULL;
+    }
+#endif
     if (meta["skipPara"] == 0) {
         paraGenerator(&sys, xi, yi, zi);
         write_arr("Z.c128", (double *)sys.x.data(), 2 * sys.x.size());

@@ -119,14 +119,17 @@ extern "C" sparse_status_t mkl_sparse_destroy(sparse_matrix_t A) {
 }
 
 extern "C" sparse_status_t mkl_sparse_d_mm(...) { abort(); }
-extern "C" lapack_int LAPACKE_dgeev(...) { abort(); }
-extern "C" lapack_int LAPACKE_dggev(...) { abort(); }
-extern "C" lapack_int LAPACKE_dhsein(...) { abort(); }
-extern "C" lapack_int LAPACKE_dhseqr(...) { abort(); }
-extern "C" lapack_int LAPACKE_zcgesv(...) { abort(); }
-extern "C" lapack_int LAPACKE_zgesv(...) { abort(); }
-extern "C" void pardiso(...) { abort(); }
-extern "C" void pardisoinit(...) { abort(); }
+// Weak: oracle/ref_shims/lapacke_shim.cpp defines the dense routines of the
+// full-wave path for the build that compiles it in.
+#define G2P_WEAK __attribute__((weak))
+extern "C" G2P_WEAK lapack_int LAPACKE_dgeev(...) { abort(); }
+extern "C" G2P_WEAK lapack_int LAPACKE_dggev(...) { abort(); }
+extern "C" G2P_WEAK lapack_int LAPACKE_dhsein(...) { abort(); }
+extern "C" G2P_WEAK lapack_int LAPACKE_dhseqr(...) { abort(); }
+extern "C" G2P_WEAK lapack_int LAPACKE_zcgesv(...) { abort(); }
+extern "C" G2P_WEAK lapack_int LAPACKE_zgesv(...) { abort(); }
+extern "C" G2P_WEAK void pardiso(...) { abort(); }
+extern "C" G2P_WEAK void pardisoinit(...) { abort(); }
 
 /* MPI as a single rank (the reference only ever ran with one). */
 extern "C" int MPI_Init(int *, char ***) { return 0; }

@@ -53,6 +53,13 @@ BENCH_CASES = {
 }
 SOLVE_RTOL = {"manhattan_c2": 1e-10}
 
+# The full-wave (Vh) path, which the reference compiles out: run with
+# oracle/_ref/ref_pipeline_vh (find_Vh(1000) and the Vh correction built in),
+# which also dumps the reference's Vh
+VH_CASES = {
+    "strip_tiny_vh": ("microstrip", dict(nx=13, ny=9, nz=6, freq_ghz=1.0, freq_end_ghz=10.0, nfreq=3)),
+}
+
 
 def digest(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
@@ -73,7 +80,8 @@ def main():
     args = ap.parse_args()
     if not args.no_build:
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), args.reference_root])
-    every = dict(CASES, **BENCH_CASES)
+    every = dict(CASES, **BENCH_CASES, **VH_CASES)
+    import oracle.harness as harness
     for name in args.cases.split(","):
         gen, kw = every[name]
         if name in SOLVE_RTOL:
@@ -81,6 +89,7 @@ def main():
         else:
             os.environ.pop("G2P_REF_SOLVE_RTOL", None)
         d = make_layout(gen, kw)
+        harness.REF_BIN = os.path.join(ROOT, "oracle", "_ref", "ref_pipeline_vh" if name in VH_CASES else "ref_pipeline")
         R = run_reference(d)
         out = {}
         meta = {"generator": gen, "kwargs": kw, "hashes": {}, "stats": {},
