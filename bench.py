@@ -275,9 +275,12 @@ def run_gb300(args):
     peak_gbs = peaks.get("hbm_gbs", 6800.0)
     k_ms, k_bytes, k_n, b_ms, b_bytes, b_n = kern
     achieved_all = (k_bytes / (k_ms / 1e3)) / 1e9 if k_ms > 0 else None
-    # the fine-level operator's launches (operators of >= 1M rows) in the
-    # working precision of the preconditioned solves
-    fi = 3 if args.precision == "mixed" else 7
+    # the fine-level operator's launches in the working precision of the
+    # preconditioned solves: the largest row class that launched (>= 1M rows
+    # for c2 and c4; c3's Ad has fewer rows)
+    base = 0 if args.precision == "mixed" else 4
+    fi = next((base + q for q in (3, 2, 1, 0) if b_n[base + q]), base + 3)
+    row_class = ("rows<64k", "rows<256k", "rows<1M", "rows>=1M")[fi - base]
     f_ms, f_bytes, f_n = b_ms[fi], b_bytes[fi], b_n[fi]
     achieved = (f_bytes / (f_ms / 1e3)) / 1e9 if f_ms > 0 else None
     traffic = None
@@ -354,7 +357,7 @@ def run_gb300(args):
         "roofline": {"bound": "hbm",
                      "kernel": ("k_spmm_sell<f32>" if args.precision == "mixed" else "k_spmm_sell<f64>") +
                                ": sparse matrix x block of right-hand sides on the fine-level Ad "
-                               "(operators of >= 1M rows)",
+                               f"(operators of {row_class})",
                      "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
                      "frac": (achieved / peak_gbs) if achieved else None, "traffic": traffic,
                      "launches": int(f_n), "avg_launch_us": 1e3 * f_ms / max(f_n, 1),

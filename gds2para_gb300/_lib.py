@@ -24,6 +24,7 @@ EXPORTS = [
     "g2p_convert_param", "g2p_write_touchstone", "g2p_write_citi",
     "g2p_ybus_from_param", "g2p_write_xyce", "g2p_write_spef",
     "g2p_gdsii_read", "g2p_polygons_size", "g2p_polygons_get", "g2p_polygons_free", "g2p_mesh_grid",
+    "g2p_find_vh", "g2p_export_vh", "g2p_set_vh", "g2p_para_generator_vh", "g2p_hessenberg_eig",
 ]
 
 STATUS = {0: "G2P_OK", 1: "G2P_ERR_INVALID", 2: "G2P_ERR_CUDA", 3: "G2P_ERR_NOMEM", 4: "G2P_ERR_NOT_CONVERGED",
@@ -154,6 +155,11 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_polygons_free.argtypes = [vp]
     L.g2p_polygons_free.restype = None
     L.g2p_mesh_grid.argtypes = [vp, i64, vp, vp, vp, i32, vp, i32, vp, i64, i64, vp, vp, vp, vp, vp, vp]
+    L.g2p_find_vh.argtypes = [vp, i32, C.POINTER(i64)]
+    L.g2p_export_vh.argtypes = [vp, vp]
+    L.g2p_set_vh.argtypes = [vp, vp, i64]
+    L.g2p_para_generator_vh.argtypes = [vp, C.POINTER(SolverParams), i32, vp, vp, C.POINTER(ExtractStats)]
+    L.g2p_hessenberg_eig.argtypes = [i64, vp, vp, vp]
     for name in EXPORTS:
         if name not in ("g2p_last_error", "g2p_version", "g2p_default_params", "g2p_launch_count",
                         "g2p_profile_begin", "g2p_profile_report", "g2p_profile_buckets", "g2p_polygons_free"):

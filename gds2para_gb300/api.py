@@ -243,7 +243,63 @@ def paraGenerator(sys: FdtdMesh, params: Optional[SolverParams] = None):
     return zc.reshape(d.nfreq, d.num_ports, d.num_ports), st
 
 
+def findVh(sys: FdtdMesh, k: int = 1000) -> np.ndarray:
+    """find_Vh (src/fdtd.hpp:3577-3859): k Arnoldi steps on the device, the
+    Hessenberg eigenproblem on the host; returns Vh, complex (N, leng_Vh)
+    over the non-PEC edges.  generateStiff must have run."""
+    L = _lib.load()
+    mm = C.c_int64()
+    check(L.g2p_find_vh(sys.handle, int(k), C.byref(mm)))
+    n = int(sys.desc.N_edge - sys.sizes().bden)
+    v = np.zeros(2 * n * int(mm.value), np.float64)
+    if mm.value:
+        check(L.g2p_export_vh(sys.handle, v.ctypes.data))
+    return (v[0::2] + 1j * v[1::2]).reshape(int(mm.value), n).T
+
+
+def setVh(sys: FdtdMesh, vh: np.ndarray) -> None:
+    """Installs Vh, complex (N, leng_Vh), in place of findVh's (for reuse, or
+    to run the correction stage on a Vh computed elsewhere)."""
+    vh = np.asarray(vh, np.complex128)
+    buf = np.empty(2 * vh.size, np.float64)
+    buf[0::2] = vh.T.reshape(-1).real
+    buf[1::2] = vh.T.reshape(-1).imag
+    if vh.shape[0] != sys.desc.N_edge - sys.sizes().bden:
+        raise ValueError("Vh must have one row per non-PEC edge")
+    check(_lib.load().g2p_set_vh(sys.handle, buf.ctypes.data, int(vh.shape[1])))
+
+
+def paraGeneratorVh(sys: FdtdMesh, params: Optional[SolverParams] = None, k: int = 1000):
+    """paraGenerator's full-wave path (src/matrixCon.cpp:609-805 with
+    Construct_Z_V0_Vh, src/fdtd.hpp:4133-4170): returns (Z_vh, Z_v0, stats).
+    Z_vh is (nfreq, P, P) with Z_vh[f].ravel()[q + P*p] the response at port
+    q to port p, not rescaled or transposed; Z_v0 is paraGenerator's Z.
+    Runs findVh(sys, k) first if it has not run."""
+    d = sys.desc
+    nz = d.nfreq * d.num_ports * d.num_ports
+    zvh = np.zeros(2 * nz, np.float64)
+    zv0 = np.zeros(2 * nz, np.float64)
+    st = ExtractStats()
+    p = params if params is not None else default_params()
+    check(_lib.load().g2p_para_generator_vh(sys.handle, C.byref(p), int(k), zvh.ctypes.data, zv0.ctypes.data,
+                                            C.byref(st)))
+    shape = (d.nfreq, d.num_ports, d.num_ports)
+    return (zvh[0::2] + 1j * zvh[1::2]).reshape(shape), (zv0[0::2] + 1j * zv0[1::2]).reshape(shape), st
+
+
+def hessenbergEigenvalues(h: np.ndarray) -> np.ndarray:
+    """Eigenvalues of a real upper Hessenberg matrix with the library's
+    dhseqr stand-in (Francis double-shift QR); complex array of length n."""
+    a = np.asfortranarray(np.asarray(h, np.float64))
+    n = a.shape[0]
+    wr = np.zeros(n, np.float64)
+    wi = np.zeros(n, np.float64)
+    check(_lib.load().g2p_hessenberg_eig(n, a.ctypes.data, wr.ctypes.data, wi.ctypes.data))
+    return wr + 1j * wi
+
+
 __all__ = ["FdtdMesh", "generateStiff", "hypreSolve", "paraGenerator", "Solver", "Server", "meshAndMark",
+           "findVh", "setVh", "paraGeneratorVh", "hessenbergEigenvalues",
            "Parasitics", "dumpTouchstone", "dumpCITI", "dumpXyce", "dumpSPEF", "default_params", "G2PError"]
 
 

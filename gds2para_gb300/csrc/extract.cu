@@ -525,6 +525,10 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     G2P_TRY(dalloc(&Bc, nc * kb, s)); G2P_TRY(dalloc(&Yc, nc * kb, s)); G2P_TRY(dalloc(&crhs, nc * kb, s));
     G2P_TRY(dalloc(&yd1, ne * kb, s)); G2P_TRY(dalloc(&yc, ne * kb, s)); G2P_TRY(dalloc(&yd2, ne * kb, s));
     G2P_TRY(dalloc(&zre, (int64_t)P * P, s)); G2P_TRY(dalloc(&zim, (int64_t)P * P, s));
+    // full-wave mode keeps each port's V0 fields: the a-value products too
+    const bool fw = fullwave_active(m->fw);
+    double *ydat = nullptr, *yd2a = nullptr, *yca = nullptr;
+    if (fw) { G2P_TRY(dalloc(&ydat, ne * kb, s)); G2P_TRY(dalloc(&yd2a, ne * kb, s)); G2P_TRY(dalloc(&yca, ne * kb, s)); }
     const double omega = (2 * 3.14159265358979323846 * m->freq_start * m->freq_unit);
     EdgeFactor f0{d, m->epsn, omega, m->k.eps0, 0};
     EdgeFactor f1{d, m->epsn, omega, m->k.eps0, 1};
@@ -557,6 +561,8 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         // (2) y0d /= omega ; yd1 = V0d y0d
         (g2p::kbegin("k_div", s), k_div<<<grid_for(nd * kk), kThreads, 0, s>>>(nd * kk, Yd, omega), g2p::kend(s));
         (g2p::kbegin("k_v0_apply", s), k_v0_apply<<<row_grid(ne, kk), row_block(kk), 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd1), g2p::kend(s));
+        if (fw)
+            (g2p::kbegin("k_v0_apply", s), k_v0_apply<<<row_grid(ne, kk), row_block(kk), 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eaval, Yd, ydat), g2p::kend(s));
         // (3) b_c = -V0ca^T J + V0ca^T(-omega D_eps yd1)
         G2P_CUDA(cudaMemsetAsync(Bc, 0, sizeof(double) * nc * kk, s));
         (g2p::kbegin("k_rhs_ports", s), k_rhs_ports<<<rg, 128, 0, s>>>(kk, d_pp, d_pe_edge, d_pe_J, m->v0c.ecol, m->v0c.eaval, kk, Bc), g2p::kend(s));
@@ -577,6 +583,8 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
         // (5) yc = V0c y0c ; b_d2 = V0da^T(-D_eps yc)
         (g2p::kbegin("k_v0_apply", s), k_v0_apply<<<row_grid(ne, kk), row_block(kk), 0, s>>>(ne, kk, m->v0c.ecol, m->v0c.eval, Yc, yc), g2p::kend(s));
+        if (fw)
+            (g2p::kbegin("k_v0_apply", s), k_v0_apply<<<row_grid(ne, kk), row_block(kk), 0, s>>>(ne, kk, m->v0c.ecol, m->v0c.eaval, Yc, yca), g2p::kend(s));
         (g2p::kbegin("k_v0t_short", s), k_v0t_short<<<row_grid(nd, kk), row_block(kk), 0, s>>>(nd, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd), g2p::kend(s));
         if (nmid_d > 0)
             (g2p::kbegin("k_v0t_long", s), k_v0t_long<<<(unsigned)nmid_d, 256, 0, s>>>(d_mid_d, kk, m->v0d.cptr, m->v0d.cedge, m->v0d.caval, yc, f1, Bd), g2p::kend(s));
@@ -589,6 +597,10 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         local.solves += kk; local.total_iterations += ss.iterations;
         local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
         (g2p::kbegin("k_v0_apply", s), k_v0_apply<<<row_grid(ne, kk), row_block(kk), 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eval, Yd, yd2), g2p::kend(s));
+        if (fw) {
+            (g2p::kbegin("k_v0_apply", s), k_v0_apply<<<row_grid(ne, kk), row_block(kk), 0, s>>>(ne, kk, m->v0d.ecol, m->v0d.eaval, Yd, yd2a), g2p::kend(s));
+            G2P_TRY(fullwave_keep_ports(m, p0, kk, yd1, ydat, yd2, yc, yd2a, yca));
+        }
         // (7) Construct_Z_V0
         (g2p::kbegin("k_construct_z", s), k_construct_z<<<(P * kk + 127) / 128, 128, 0, s>>>(P, p0, kk, d_rptr, d_redge, d_rdir, d, m->xn, m->yn, m->zn, yd1,
                                                           yc, yd2, d_cur, zre, zim), g2p::kend(s));
@@ -608,6 +620,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     dfree(d_fr, s); dfree(d_out, s);
     dfree(Bd, s); dfree(Yd, s); dfree(Bc, s); dfree(Yc, s); dfree(crhs, s);
     dfree(yd1, s); dfree(yc, s); dfree(yd2, s); dfree(zre, s); dfree(zim, s);
+    dfree(ydat, s); dfree(yd2a, s); dfree(yca, s);
     dfree(d_pe_edge, s); dfree(d_pptr, s); dfree(d_pe_J, s); dfree(d_redge, s); dfree(d_rdir, s);
     dfree(d_rptr, s); dfree(d_cur, s); lcol.release(s);
     g2p_solver_destroy(Sd);

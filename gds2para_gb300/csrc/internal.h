@@ -62,6 +62,14 @@ struct V0Basis {
 // A Laplacian whose ordered conductor sums still run on the side stream.
 struct LapPending;
 
+// The full-wave (Vh) state of a mesh: Vh and, while the V0 path runs for it,
+// the ports' V0 field directions (fullwave.cu).
+struct FullWave;
+void fullwave_release(FullWave *fw, cudaStream_t s);
+bool fullwave_active(const FullWave *fw);
+g2p_status fullwave_keep_ports(g2p_mesh *m, int p0, int kk, const double *yd1, const double *ydat, const double *yd2,
+                               const double *yc, const double *yd2a, const double *yca);
+
 struct Constants {
     double mu, eps0;
 };
@@ -106,6 +114,8 @@ struct g2p_mesh {
     double *v0_tab = nullptr;      // per-line quotient tables of the V0 entries
     g2p::V0Basis v0d, v0c;
     g2p::Csr<double> Ad, Ac;
+    // full-wave mode (g2p_find_vh)
+    g2p::FullWave *fw = nullptr;
     // scratch for scans
     int64_t *scan_work = nullptr;
     int64_t scan_work_n = 0;

@@ -284,6 +284,8 @@ extern "C" g2p_status g2p_mesh_destroy(g2p_mesh *m) {
     m->v0d.release(s); m->v0c.release(s);
     m->Ad.release(s); m->Ac.release(s);
     dfree(m->scan_work, s);
+    g2p::fullwave_release(m->fw, s);
+    m->fw = nullptr;
     if (s) { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
     delete m;
     return G2P_OK;

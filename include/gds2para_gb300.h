@@ -13,6 +13,9 @@
  *   hypreSolve (src/hypreSolve.cpp:9,
  *            src/hypreSolver.h:14)              -> g2p_hypre_solve, g2p_solver_*
  *   paraGenerator (src/matrixCon.cpp:11)       -> g2p_para_generator
+ *   find_Vh (src/fdtd.hpp:3577)                -> g2p_find_vh (+ g2p_export_vh, g2p_set_vh)
+ *   paraGenerator's full-wave part
+ *            (src/matrixCon.cpp:609-805)        -> g2p_para_generator_vh
  *
  * Arrays in g2p_mesh_desc may live in host or device memory (they are
  * copied with unified addressing); every output buffer is a HOST pointer
@@ -185,6 +188,40 @@ g2p_status g2p_solver_destroy(g2p_solver *s);
  * reference's transposed storage of frequencies after the first.  Runs
  * g2p_index_maps and g2p_assemble_v0 first if they have not run. ---- */
 g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p, double *z_out, g2p_extract_stats *st);
+
+/* ---- full-wave (Vh) mode: find_Vh (src/fdtd.hpp:3577-3859) and the Vh
+ * correction of paraGenerator (src/matrixCon.cpp:609-805) with
+ * Construct_Z_V0_Vh (src/fdtd.hpp:4133-4170); the reference compiles this
+ * path out (SKIP_VH, src/fdtd.hpp:76).
+ * g2p_find_vh: k Arnoldi steps (modified Gram-Schmidt, on the device) on the
+ * 2N operator [[0, I], [-D_eps^-1 S/s^2, -D_eps^-1 D_sig/s]], s = 1e14, the
+ * Hessenberg eigenproblem on the host, and Vh = V(1:N,1:k) * (the
+ * eigenvectors of the eigenvalues with |Im| > 1e-6, a conjugate pair giving
+ * two columns).  *leng_vh = Vh's column count.  Needs g2p_generate_stiff.
+ * g2p_export_vh: Vh (host or device), column-major N x leng_vh complex as
+ * interleaved (re, im) doubles, N = leng_S's row count (non-PEC edges).
+ * g2p_para_generator_vh: runs g2p_find_vh if it has not run, the V0 path
+ * (z_v0, nullable, as g2p_para_generator writes it) keeping each port's V0
+ * field directions, then per port and frequency the deflated Galerkin
+ * correction; z_vh (host) receives nfreq*P*P complex values, entry
+ * f*P*P + q + P*p for response port q and source port p, NOT rescaled or
+ * transposed (print_z_V0_Vh's layout).  The reference's own output for the
+ * first frequency adds Construct_Z_V0's value to this one (it accumulates
+ * into sys->x without clearing it).  The 2 x 2 and leng_vh x leng_vh
+ * complex solves run on the host, as LAPACK does them in the reference.
+ * g2p_set_vh: installs a Vh computed elsewhere (same layout as
+ * g2p_export_vh writes, leng_vh columns) in place of g2p_find_vh's, for
+ * reuse across calls or for checking the correction stage on its own.
+ * g2p_hessenberg_eig: eigenvalues (wr, wi) of the real upper Hessenberg
+ * n x n matrix h (column-major; entries below the subdiagonal ignored), a
+ * complex pair at consecutive positions, positive imaginary part first:
+ * the library's dhseqr stand-in, exported for tests. ---- */
+g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh);
+g2p_status g2p_export_vh(g2p_mesh *m, double *vh);
+g2p_status g2p_set_vh(g2p_mesh *m, const double *vh, int64_t leng_vh);
+g2p_status g2p_para_generator_vh(g2p_mesh *m, const g2p_solver_params *p, int32_t k, double *z_vh, double *z_v0,
+                                 g2p_extract_stats *st);
+g2p_status g2p_hessenberg_eig(int64_t n, const double *h, double *wr, double *wi);
 
 /* ---- diagnostics (no counterpart in the reference) ----
  * g2p_launch_count: kernels launched by the library so far in this process.
