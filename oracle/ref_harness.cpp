@@ -25,6 +25,7 @@
 #include <queue>
 #include "fdtd.hpp"
 #include "hypreSolver.h"
+#include <chrono>
 #include "oracle.h"
 
 static std::string g_out;
@@ -43,7 +44,19 @@ template <class T> static std::vector<T> read_arr(const std::string &dir, const 
     return v;
 }
 
+/* G2P_REF_NO_DUMP=1: time the reference's functions without writing their
+   arrays (the bench-size timings) */
+static bool no_dump() {
+    static const bool v = getenv("G2P_REF_NO_DUMP") != nullptr;
+    return v;
+}
+
+static double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
 template <class T> static void write_arr(const char *name, const T *p, size_t n) {
+    if (no_dump()) return;
     std::string path = g_out + "/" + name;
     FILE *f = fopen(path.c_str(), "wb");
     if (!f) { fprintf(stderr, "cannot write %s\n", path.c_str()); exit(3); }
@@ -253,8 +266,13 @@ int main(int argc, char **argv) {
     std::ofstream meta_out(g_out + "/meta_out.txt");
     meta_out << "numCdt " << sys.numCdt << "\nbden " << sys.bden << "\n";
 
+    /* wall time of each of the reference's own assembly functions, in
+       meta_out (t_*_ms) */
+    double tm = 0;
     if (meta["skipStiff"] == 0) {
+        tm = now_ms();
         generateStiff(&sys);
+        meta_out << "t_stiff_ms " << (long long)(now_ms() - tm) << "\n";
         write_arr("S_row.i64", (int64_t *)sys.SRowId, sys.leng_S);
         write_arr("S_col.i64", (int64_t *)sys.SColId, sys.leng_S);
         write_arr("S_val.f64", sys.Sval, sys.leng_S);
@@ -263,13 +281,17 @@ int main(int argc, char **argv) {
     {
         myint *map = (myint *)calloc(sys.N_node, sizeof(myint));
         myint v0d1num = 0, leng_v0d1 = 0, v0d1anum = 0, leng_v0d1a = 0, leng_Ad = 0;
+        tm = now_ms();
         sys.merge_v0d1(0, 0, 0, 0, 0, 0, v0d1num, leng_v0d1, v0d1anum, leng_v0d1a, map, 0.);
+        meta_out << "t_v0d_ms " << (long long)(now_ms() - tm) << "\n";
         write_arr("v0d_row.i64", (int64_t *)sys.v0d1RowId, v0d1num);
         write_arr("v0d_col.i64", (int64_t *)sys.v0d1ColId, v0d1num);
         write_arr("v0d_val.f64", sys.v0d1val, v0d1num);
         write_arr("v0d_aval.f64", sys.v0d1aval, v0d1anum);
         write_arr("v0d_map.i64", (int64_t *)map, sys.N_node);
+        tm = now_ms();
         sys.generateAd(map, v0d1num, v0d1anum, leng_v0d1, leng_Ad);
+        meta_out << "t_ad_ms " << (long long)(now_ms() - tm) << "\n";
         write_arr("Ad_row.i64", (int64_t *)sys.AdRowId, leng_Ad);
         write_arr("Ad_col.i64", (int64_t *)sys.AdColId, leng_Ad);
         write_arr("Ad_val.f64", sys.Adval, leng_Ad);
@@ -283,13 +305,17 @@ int main(int argc, char **argv) {
         myint v0cnum = 0, leng_v0c = 0, v0canum = 0, leng_v0ca = 0, leng_Ac = 0;
         sys.cindex.push_back(-1);
         sys.acu_cnno.push_back(0);
+        tm = now_ms();
         sys.merge_v0c(0, 0, 0, 0, v0cnum, leng_v0c, v0canum, leng_v0ca, map);
+        meta_out << "t_v0c_ms " << (long long)(now_ms() - tm) << "\n";
         write_arr("v0c_row.i64", (int64_t *)sys.v0cRowId, v0cnum);
         write_arr("v0c_col.i64", (int64_t *)sys.v0cColId, v0cnum);
         write_arr("v0c_val.f64", sys.v0cval, v0cnum);
         write_arr("v0c_aval.f64", sys.v0caval, v0canum);
         write_arr("v0c_map.i64", (int64_t *)map, sys.N_node);
+        tm = now_ms();
         sys.generateAc(map, v0cnum, v0canum, leng_v0c, leng_Ac);
+        meta_out << "t_ac_ms " << (long long)(now_ms() - tm) << "\n";
         write_arr("Ac_row.i64", (int64_t *)sys.AcRowId, leng_Ac);
         write_arr("Ac_col.i64", (int64_t *)sys.AcColId, leng_Ac);
         write_arr("Ac_val.f64", sys.Acval, leng_Ac);
