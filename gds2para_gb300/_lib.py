@@ -20,10 +20,11 @@ EXPORTS = [
     "g2p_para_generator", "g2p_launch_count", "g2p_profile_begin", "g2p_profile_end", "g2p_profile_report",
     "g2p_map_edge_noalloc", "g2p_profile_buckets",
     "g2p_server_create", "g2p_server_submit", "g2p_server_wait", "g2p_server_destroy",
-    "g2p_mesh_mark",
+    "g2p_mesh_mark", "g2p_mesh_mark_polygons",
     "g2p_convert_param", "g2p_write_touchstone", "g2p_write_citi",
     "g2p_ybus_from_param", "g2p_write_xyce", "g2p_write_spef",
     "g2p_gdsii_read", "g2p_polygons_size", "g2p_polygons_get", "g2p_polygons_free", "g2p_mesh_grid",
+    "g2p_sim_input_read", "g2p_sim_input_sizes", "g2p_sim_input_get", "g2p_sim_input_free",
     "g2p_find_vh", "g2p_export_vh", "g2p_set_vh", "g2p_para_generator_vh", "g2p_hessenberg_eig",
 ]
 
@@ -136,6 +137,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_profile_report.argtypes = [C.c_char_p, i64]
     L.g2p_mesh_mark.argtypes = [i64, i64, i64, vp, vp, vp, vp, i64, i32, vp, vp, vp, vp, C.POINTER(i64),
                                 vp, vp, i64, vp, vp, i64, vp, vp]
+    L.g2p_mesh_mark_polygons.argtypes = [i64, i64, i64, vp, vp, vp, i64, vp, vp, vp, vp, i32, vp, vp, vp, vp, vp,
+                                         C.POINTER(i64), vp, vp, i64, vp, vp, i64, vp, vp]
     L.g2p_server_create.argtypes = [i64, i32, C.POINTER(vp)]
     L.g2p_server_submit.argtypes = [vp, C.POINTER(MeshDescC), C.POINTER(SolverParams), C.POINTER(i64)]
     L.g2p_server_wait.argtypes = [vp, i64, vp, C.POINTER(ExtractStats), C.POINTER(JobTimes)]
@@ -155,6 +158,11 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_polygons_free.argtypes = [vp]
     L.g2p_polygons_free.restype = None
     L.g2p_mesh_grid.argtypes = [vp, i64, vp, vp, vp, i32, vp, i32, vp, i64, i64, vp, vp, vp, vp, vp, vp]
+    L.g2p_sim_input_read.argtypes = [C.c_char_p, C.POINTER(vp)]
+    L.g2p_sim_input_sizes.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]
+    L.g2p_sim_input_get.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.g2p_sim_input_free.argtypes = [vp]
+    L.g2p_sim_input_free.restype = None
     L.g2p_find_vh.argtypes = [vp, i32, C.POINTER(i64)]
     L.g2p_export_vh.argtypes = [vp, vp]
     L.g2p_set_vh.argtypes = [vp, vp, i64]
@@ -162,7 +170,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_hessenberg_eig.argtypes = [i64, vp, vp, vp]
     for name in EXPORTS:
         if name not in ("g2p_last_error", "g2p_version", "g2p_default_params", "g2p_launch_count",
-                        "g2p_profile_begin", "g2p_profile_report", "g2p_profile_buckets", "g2p_polygons_free"):
+                        "g2p_profile_begin", "g2p_profile_report", "g2p_profile_buckets", "g2p_polygons_free",
+                        "g2p_sim_input_free"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L

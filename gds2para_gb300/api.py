@@ -299,6 +299,7 @@ def hessenbergEigenvalues(h: np.ndarray) -> np.ndarray:
 
 
 __all__ = ["FdtdMesh", "generateStiff", "hypreSolve", "paraGenerator", "Solver", "Server", "meshAndMark",
+           "readSimInput", "polygonZ", "meshAndMarkPolygons", "layoutFromGDS",
            "findVh", "setVh", "paraGeneratorVh", "hessenbergEigenvalues",
            "Parasitics", "dumpTouchstone", "dumpCITI", "dumpXyce", "dumpSPEF", "default_params", "G2PError"]
 
@@ -406,6 +407,111 @@ def meshAndMark(layout) -> dict:
     return dict(mark_node=mark_node, mark_edge=mark_edge, num_cdt=n, mark_port=mark_port[:n],
                 cdt_return=cdt_return[:n], side_edge_ptr=side_edge_ptr,
                 side_edges=side_edges[:side_edge_ptr[-1]], side_area=side_area[:nsides], side_dir=side_dir[:nsides])
+
+
+def readSimInput(path) -> dict:
+    """The reference's .sim_input reader (SolverDataBase::readSimInput,
+    src/solnoutclass.hpp:5412) as convertToFDTDMesh hands it on: limits and
+    lengths in metres, the frequency sweep, the valid stack layers (rows z
+    begin, z end, eps_r, sigma) with their GDSII numbers, and the ports
+    (port_side_ptr, side_coords rows supply xyz + return xyz, side_dir).
+    Host code; no GPU needed."""
+    L = _lib.load()
+    h = C.c_void_p()
+    check(L.g2p_sim_input_read(str(path).encode(), C.byref(h)))
+    try:
+        nl, npt, ns = C.c_int32(), C.c_int32(), C.c_int32()
+        check(L.g2p_sim_input_sizes(h, C.byref(nl), C.byref(npt), C.byref(ns)))
+        lim, units, fc = np.zeros(6), np.zeros(4), np.zeros(2, np.int32)
+        layers, gds = np.zeros((nl.value, 4)), np.zeros(nl.value, np.int32)
+        sptr, coords, sdir = np.zeros(npt.value + 1, np.int32), np.zeros((ns.value, 6)), np.zeros(ns.value, np.int32)
+        check(L.g2p_sim_input_get(h, lim.ctypes.data, units.ctypes.data, fc.ctypes.data, layers.ctypes.data,
+                                  gds.ctypes.data, sptr.ctypes.data, coords.ctypes.data, sdir.ctypes.data))
+    finally:
+        L.g2p_sim_input_free(h)
+    return dict(lim=lim, length_unit=units[0], freq_unit=units[1], freq_start=units[2], freq_end=units[3],
+                nfreq=int(fc[0]), freq_scale=int(fc[1]), layers=layers, layer_gdsii=gds, port_side_ptr=sptr,
+                side_coords=coords, side_dir=sdir)
+
+
+def polygonZ(polygons, layers, layer_gdsii) -> np.ndarray:
+    """Each polygon's (z bottom, z top) from the stack layer with its GDSII
+    number, the last such layer winning (convertToFDTDMesh,
+    solnoutclass.hpp:5928-5939); (0, 0) when none has it."""
+    lay = np.asarray(polygons[0])
+    z = np.zeros((len(lay), 2))
+    for k in range(len(layer_gdsii)):
+        z[lay == layer_gdsii[k]] = layers[k, :2]
+    return z
+
+
+def meshAndMarkPolygons(grid, polygons, poly_z, port_side_ptr, side_coords, side_dir) -> dict:
+    """Conductor marking from polygons on the GPU (g2p_mesh_mark_polygons:
+    findInsideCond, the conductor numbering, findPortNode and portSet).
+    grid: (xn, yn, zn); polygons as readGDSII returns them; poly_z from
+    polygonZ; port sides as readSimInput returns them.  Returns the fdtdMesh
+    fields as numpy arrays, with the side coordinates as findPortNode left
+    them."""
+    L = _lib.load()
+    xn, yn, zn = (_c(v, np.float64) for v in grid[:3])
+    nx, ny, nz = len(xn), len(yn), len(zn)
+    _, vptr, vx, vy = polygons
+    vptr, vx, vy = _c(vptr, np.int64), _c(vx, np.float64), _c(vy, np.float64)
+    pz = _c(np.asarray(poly_z, np.float64).reshape(-1, 2), np.float64)
+    sptr = _c(port_side_ptr, np.int32)
+    coords = np.array(side_coords, np.float64).reshape(-1, 6).copy()
+    sdir_in = _c(side_dir, np.int32)
+    nports, nsides = len(sptr) - 1, len(coords)
+    N_node = nx * ny * nz
+    Ns = (ny - 1) * nx + (nx - 1) * ny
+    N_edge = Ns * nz + nx * ny * (nz - 1)
+    mark_node = np.zeros(N_node, np.int64)
+    mark_edge = np.zeros(N_edge, np.int64)
+    ncdt = C.c_int64()
+    max_cdt = len(vptr) + 1
+    mark_port = np.zeros(max_cdt, np.int32)
+    cdt_return = np.zeros(max_cdt, np.uint8)
+    max_e = nsides * max(nx, ny, nz) + 1
+    side_edge_ptr = np.zeros(nsides + 1, np.int64)
+    side_edges = np.zeros(max_e, np.int64)
+    side_area = np.zeros(max(1, nsides), np.float64)
+    side_dir = np.zeros(max(1, nsides), np.int32)
+    check(L.g2p_mesh_mark_polygons(nx, ny, nz, xn.ctypes.data, yn.ctypes.data, zn.ctypes.data, len(vptr) - 1,
+                                   vptr.ctypes.data, vx.ctypes.data, vy.ctypes.data, pz.ctypes.data, nports,
+                                   sptr.ctypes.data, coords.ctypes.data, sdir_in.ctypes.data, mark_node.ctypes.data,
+                                   mark_edge.ctypes.data, C.byref(ncdt), mark_port.ctypes.data,
+                                   cdt_return.ctypes.data, max_cdt, side_edge_ptr.ctypes.data,
+                                   side_edges.ctypes.data, max_e, side_area.ctypes.data, side_dir.ctypes.data))
+    n = ncdt.value
+    return dict(mark_node=mark_node, mark_edge=mark_edge, num_cdt=n, mark_port=mark_port[:n],
+                cdt_return=cdt_return[:n], side_edge_ptr=side_edge_ptr,
+                side_edges=side_edges[:side_edge_ptr[-1]], side_area=side_area[:nsides],
+                side_dir=side_dir[:nsides], side_coords=coords)
+
+
+def layoutFromGDS(gds_path, sim_input_path, ignore_layers=()) -> MeshDesc:
+    """A design file and its .sim_input to the fdtdMesh fields of the V0
+    path, as the reference's command-line flow gets there (TestMain.cpp:
+    readSimInput, the GDSII read and saveToMesh, convertToFDTDMesh,
+    meshAndMark, portSet): readSimInput and readGDSII on the host, the grid
+    (g2p_mesh_grid) on the host, marking, numbering and ports on the GPU."""
+    sim = readSimInput(sim_input_path)
+    polys = readGDSII(gds_path, ignore_layers)
+    sides = sim["side_coords"]
+    xn, yn, zn, epsn, sign = meshGrid(sim["lim"], polys, sides, sim["layers"])
+    pz = polygonZ(polys, sim["layers"], sim["layer_gdsii"])
+    mk = meshAndMarkPolygons((xn, yn, zn), polys, pz, sim["port_side_ptr"], sides, sim["side_dir"])
+    nports = len(sim["port_side_ptr"]) - 1
+    return MeshDesc(nx=len(xn), ny=len(yn), nz=len(zn), xn=xn, yn=yn, zn=zn, stack_epsn=epsn, stack_sign=sign,
+                    mark_node=mk["mark_node"], mark_edge=mk["mark_edge"],
+                    mark_node_raw=(mk["mark_node"] != 0).astype(np.int64),
+                    mark_edge_raw=(mk["mark_edge"] != 0).astype(np.int64), num_cdt=mk["num_cdt"],
+                    mark_port=mk["mark_port"], cdt_return=mk["cdt_return"], num_ports=nports,
+                    port_side_ptr=np.asarray(sim["port_side_ptr"], np.int32), side_edge_ptr=mk["side_edge_ptr"],
+                    side_edges=mk["side_edges"], side_area=mk["side_area"], side_dir=mk["side_dir"],
+                    side_coords=mk["side_coords"], freq_start=sim["freq_start"], freq_end=sim["freq_end"],
+                    freq_unit=sim["freq_unit"], nfreq=sim["nfreq"], freq_scale=sim["freq_scale"],
+                    name=str(gds_path))
 
 
 class Parasitics:

@@ -22,10 +22,10 @@ LIB = os.path.join(OUT, "libgds2para_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "--extended-lambda", "-lineinfo", "-Xcompiler", "-fPIC",
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]
-NO_FMA = {"mesh.cu", "v0.cu", "extract.cu"}
+NO_FMA = {"mesh.cu", "v0.cu", "extract.cu", "mesher.cu"}
 # host code whose results must not depend on the host compiler contracting
 # a * b + c into one rounding (the oracle builds with -ffp-contract=off)
-NO_HOST_CONTRACT = {"ingest.cu"}
+NO_HOST_CONTRACT = {"ingest.cu", "mesher.cu"}
 UNITS = ["primitives.cu", "mesh.cu", "v0.cu", "solver.cu", "coarse.cu", "solve_api.cu", "extract.cu", "fullwave.cu", "noalloc.cu", "serve.cu", "mesher.cu",
          "network.cu", "ingest.cu"]
 

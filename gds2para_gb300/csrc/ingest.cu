@@ -495,3 +495,270 @@ extern "C" g2p_status g2p_mesh_grid(const double *lim, int64_t npoly, const int6
     }
     return G2P_OK;
 }
+
+// ---------------------------------------------------------------------------
+// .sim_input reader: the reference's SolverDataBase::readSimInput
+// (src/solnoutclass.hpp:5412-5886) followed by what convertToFDTDMesh takes
+// from it (src/solnoutclass.hpp:5894-5984): the limits and length unit, the
+// frequency sweep, the physically valid stack layers (height > 0, eps_r >= 1,
+// sigma >= 0) with their GDSII numbers, and the ports with their sides and
+// each side's current direction (Port::positiveCoordFlow: +1 when a supply
+// coordinate exceeds the return's).
+//
+// The text rules are the reference's: a section starts at a line beginning
+// "TOTAL SIZE", "FREQUENCY", "DIELECTRIC STACK" or "PORT"; lines starting
+// with '#' are skipped inside a section; values follow "key = "; a port line
+// is told apart by its count of spaces before " #" (4: x y x y GDSII-layer,
+// the z range that layer's; 6: six coordinates and the direction; more: a
+// name first), sides with the same name make one port, and unnamed lines are
+// all named "port1" (the reference never advances that counter); a stack
+// layer's GDSII number is its name, or the digits after an 'M' in it; a
+// missing "z = " continues from the layer below.  Like the reference, the
+// line loop stops at the end of the file, so a last line without a newline
+// is not read.
+namespace {
+
+struct SimLayer {
+    std::string name;
+    int gdsii;
+    double z, h, eps, sigma;
+    bool valid() const { return h > 0.0 && eps >= 1.0 && sigma >= 0.0; }
+};
+
+struct SimPort {
+    std::string name;
+    std::vector<double> coord;   // 6 per side
+};
+
+// stod of the text after position `at`, as the reference's
+// stod(line.substr(at, ...)) reads it; false when no number is there
+bool num_at(const std::string &line, size_t at, double *v) {
+    if (at == std::string::npos || at > line.size()) return false;
+    const char *b = line.c_str() + at;
+    char *e = nullptr;
+    *v = strtod(b, &e);
+    return e != b;
+}
+
+}  // namespace
+
+struct g2p_sim_input {
+    double lim[6] = {0, 0, 0, 0, 0, 0};
+    double length_unit = 1, freq_unit = 1, freq_start = 0, freq_end = 0;
+    int32_t nfreq = 1, freq_scale = 1;
+    std::vector<SimLayer> layers;
+    std::vector<SimPort> ports;
+};
+
+extern "C" g2p_status g2p_sim_input_read(const char *path, g2p_sim_input **out) {
+    if (!path || !out) { g2p::set_last_message("g2p_sim_input_read: null argument"); return G2P_ERR_INVALID; }
+    FILE *f = fopen(path, "rb");
+    if (!f) { g2p::set_last_message("g2p_sim_input_read: cannot open %s", path); return G2P_ERR_INVALID; }
+    std::string text;
+    char buf[65536];
+    for (size_t n; (n = fread(buf, 1, sizeof buf, f)) > 0;) text.append(buf, n);
+    fclose(f);
+    // std::getline over the text: each call returns the next line and
+    // reports the end of the file when it ran into it
+    size_t pos = 0;
+    bool eof = false;
+    auto getline = [&](std::string &line) {
+        line.clear();
+        if (pos >= text.size()) { eof = true; return; }
+        const size_t nl = text.find('\n', pos);
+        if (nl == std::string::npos) { line = text.substr(pos); pos = text.size(); eof = true; return; }
+        line = text.substr(pos, nl - pos);
+        pos = nl + 1;
+    };
+    auto skip_comments = [&](std::string &line) {
+        while (line.compare(0, 1, "#") == 0 && !eof) getline(line);
+    };
+    auto value_after = [](const std::string &line, const char *key, double *v) {
+        const size_t at = line.find(key);
+        return at != std::string::npos && num_at(line, at + strlen(key), v);
+    };
+    auto bad = [&](const char *what) {
+        g2p::set_last_message("g2p_sim_input_read: %s: %s", path, what);
+        return G2P_ERR_INVALID;
+    };
+    g2p_sim_input r;
+    std::string line;
+    getline(line);
+    while (!eof) {
+        if (line.compare(0, 10, "TOTAL SIZE") == 0) {
+            getline(line);
+            skip_comments(line);
+            const std::string nc = line.substr(0, line.find(" #"));
+            if (std::count(nc.begin(), nc.end(), ' ') < 5) {
+                g2p::set_last_message("g2p_sim_input_read: %s: a board outline file in place of the x/y limits is not "
+                                 "supported", path);
+                return G2P_ERR_UNSUPPORTED;
+            }
+            double v[6];
+            size_t at = 0;
+            for (int k = 0; k < 6; k++) {
+                if (!num_at(line, at, &v[k])) return bad("TOTAL SIZE limits");
+                at = line.find(' ', at);
+                if (k < 5 && at == std::string::npos) return bad("TOTAL SIZE limits");
+                at += 1;
+            }
+            getline(line);
+            skip_comments(line);
+            if (!value_after(line, "lengthUnit = ", &r.length_unit)) return bad("lengthUnit");
+            for (int k = 0; k < 6; k++) r.lim[k] = v[k] * r.length_unit;
+        } else if (line.compare(0, 9, "FREQUENCY") == 0) {
+            double nf = 0, fs = 0;
+            const char *keys[5] = {"freqUnit = ", "freqStart = ", "freqEnd = ", "nfreq = ", "freqScale = "};
+            double *dst[5] = {&r.freq_unit, &r.freq_start, &r.freq_end, &nf, &fs};
+            for (int k = 0; k < 5; k++) {
+                getline(line);
+                skip_comments(line);
+                if (!value_after(line, keys[k], dst[k])) return bad(keys[k]);
+            }
+            r.nfreq = (int32_t)nf;
+            r.freq_scale = (int32_t)fs;
+            if (r.nfreq < 1) return bad("nfreq");
+            // convertToFDTDMesh takes the first and last of the frequency
+            // list, which holds freqStart alone for one point
+            if (r.nfreq == 1) r.freq_end = r.freq_start;
+        } else if (line.compare(0, 16, "DIELECTRIC STACK") == 0) {
+            getline(line);
+            skip_comments(line);
+            double ns = 0;
+            if (!value_after(line, "numStack = ", &ns) && !value_after(line, "numLayer = ", &ns)) ns = 0;
+            getline(line);
+            skip_comments(line);
+            for (int64_t k = 0; k < (int64_t)ns; k++) {
+                SimLayer L;
+                L.name = line.substr(0, line.find(' '));
+                L.gdsii = -1;
+                const size_t m = L.name.find('M');
+                const std::string digits = m != std::string::npos ? L.name.substr(m + 1) : L.name;
+                if (!digits.empty() && std::all_of(digits.begin(), digits.end(), [](char c) { return c >= '0' && c <= '9'; }))
+                    L.gdsii = atoi(digits.c_str());
+                if (line.find("z = ") != std::string::npos) {
+                    if (!value_after(line, "z = ", &L.z)) return bad("stack layer z");
+                    L.z *= r.length_unit;
+                } else {
+                    L.z = r.layers.empty() ? 0.0 : r.layers.back().z + r.layers.back().h;
+                }
+                if (!value_after(line, "h = ", &L.h) || !value_after(line, "e = ", &L.eps)) return bad("stack layer h or e");
+                L.h *= r.length_unit;
+                L.sigma = 0.;
+                if (line.find("sigma = ") != std::string::npos && !value_after(line, "sigma = ", &L.sigma))
+                    return bad("stack layer sigma");
+                r.layers.push_back(L);
+                getline(line);
+                skip_comments(line);
+            }
+        } else if (line.compare(0, 4, "PORT") == 0 && r.ports.empty()) {
+            getline(line);
+            skip_comments(line);
+            getline(line);
+            skip_comments(line);
+            while (line.size() >= 3 && !eof) {
+                const std::string nc = line.substr(0, line.find(" #"));
+                const size_t nsp = (size_t)std::count(nc.begin(), nc.end(), ' ');
+                std::string name;
+                double c[6];
+                std::vector<double> vals;
+                size_t at = 0;
+                auto next_num = [&](double *v) {
+                    if (!num_at(line, at, v)) return false;
+                    at = line.find(' ', at);
+                    at = at == std::string::npos ? line.size() : at + 1;
+                    return true;
+                };
+                if (nsp == 4) {
+                    double xs, ys, xr, yr, lay;
+                    if (!next_num(&xs) || !next_num(&ys) || !next_num(&xr) || !next_num(&yr) || !next_num(&lay))
+                        return bad("port line");
+                    const SimLayer *L = nullptr;
+                    for (const auto &l : r.layers)
+                        if (l.gdsii == (int)lay) { L = &l; break; }
+                    if (!L) return bad("port layer not in the stack");
+                    name = "port1";
+                    const double u = r.length_unit;
+                    const double cc[6] = {xs * u, ys * u, L->z, xr * u, yr * u, L->z + L->h};
+                    std::copy(cc, cc + 6, c);
+                } else if (nsp >= 6) {
+                    if (nsp > 6) {
+                        const size_t sp = line.find(' ');
+                        name = line.substr(0, sp);
+                        at = sp + 1;
+                    } else {
+                        name = "port1";
+                    }
+                    for (int k = 0; k < 6; k++) {
+                        if (!next_num(&c[k])) return bad("port line");
+                        c[k] *= r.length_unit;
+                    }
+                    double dir;
+                    if (!next_num(&dir)) return bad("port line direction");
+                } else {
+                    return bad("port line");
+                }
+                SimPort *P = nullptr;
+                for (auto &p : r.ports)
+                    if (p.name == name) { P = &p; break; }
+                if (!P) { r.ports.push_back(SimPort{name, {}}); P = &r.ports.back(); }
+                P->coord.insert(P->coord.end(), c, c + 6);
+                getline(line);
+                while (line.compare(0, 1, "#") == 0 && !eof) getline(line);
+            }
+        }
+        getline(line);
+    }
+    *out = new g2p_sim_input(r);
+    return G2P_OK;
+}
+
+extern "C" g2p_status g2p_sim_input_sizes(const g2p_sim_input *s, int32_t *nlayer, int32_t *nport, int32_t *nside) {
+    if (!s || !nlayer || !nport || !nside) return G2P_ERR_INVALID;
+    int32_t nl = 0, ns = 0;
+    for (const auto &l : s->layers) nl += l.valid() ? 1 : 0;
+    for (const auto &p : s->ports) ns += (int32_t)(p.coord.size() / 6);
+    *nlayer = nl;
+    *nport = (int32_t)s->ports.size();
+    *nside = ns;
+    return G2P_OK;
+}
+
+extern "C" g2p_status g2p_sim_input_get(const g2p_sim_input *s, double *lim, double *units, int32_t *freq_counts,
+                                        double *layers, int32_t *layer_gdsii, int32_t *port_side_ptr,
+                                        double *side_coords, int32_t *side_dir) {
+    if (!s) return G2P_ERR_INVALID;
+    if (lim) std::copy(s->lim, s->lim + 6, lim);
+    if (units) {
+        units[0] = s->length_unit;
+        units[1] = s->freq_unit;
+        units[2] = s->freq_start;
+        units[3] = s->freq_end;
+    }
+    if (freq_counts) { freq_counts[0] = s->nfreq; freq_counts[1] = s->freq_scale; }
+    int64_t k = 0;
+    for (const auto &l : s->layers) {
+        if (!l.valid()) continue;
+        if (layers) {
+            layers[4 * k] = l.z;
+            layers[4 * k + 1] = l.z + l.h;
+            layers[4 * k + 2] = l.eps;
+            layers[4 * k + 3] = l.sigma;
+        }
+        if (layer_gdsii) layer_gdsii[k] = l.gdsii;
+        k++;
+    }
+    int32_t side = 0;
+    if (port_side_ptr) port_side_ptr[0] = 0;
+    for (size_t p = 0; p < s->ports.size(); p++) {
+        const auto &c = s->ports[p].coord;
+        for (size_t q = 0; q + 6 <= c.size(); q += 6, side++) {
+            if (side_coords) std::copy(c.begin() + q, c.begin() + q + 6, side_coords + 6 * (int64_t)side);
+            if (side_dir) side_dir[side] = (c[q] > c[q + 3] || c[q + 1] > c[q + 4] || c[q + 2] > c[q + 5]) ? 1 : -1;
+        }
+        if (port_side_ptr) port_side_ptr[p + 1] = side;
+    }
+    return G2P_OK;
+}
+
+extern "C" void g2p_sim_input_free(g2p_sim_input *s) { delete s; }

@@ -263,6 +263,27 @@ g2p_status g2p_mesh_mark(int64_t nx, int64_t ny, int64_t nz, const double *xn, c
                          int32_t *mark_port, uint8_t *cdt_return, int64_t max_cdt, int64_t *side_edge_ptr,
                          int64_t *side_edges, int64_t max_side_edges, double *side_area, int32_t *side_dir);
 
+/* Conductor marking from polygons, the rest of meshAndMark and portSet
+ * (findInsideCond, src/fdtd.hpp:534-826; the conductor numbering, port
+ * placement and boundary marks of src/mesh.cpp:456-1020; portSet,
+ * src/mesh.cpp:1196-1356) on the grid g2p_mesh_grid made from the same
+ * polygons and port sides.  Polygons as g2p_polygons_get returns them, with
+ * poly_z[2 * npoly] their (z bottom, z top) in metres from the stack layer of
+ * their GDSII number (equal values: on no layer; such a polygon marks
+ * nothing).  Port sides: side_coords[6 * nside] (supply x y z, return x y z,
+ * metres) for the sides of port p at port_side_ptr[p] ..
+ * port_side_ptr[p + 1] - 1, and side_dir_in[nside] (+1/-1).  A port end
+ * outside every conductor moves along the port axis to the nearest
+ * conductor node within 50 lines, as findPortNode moves it, and
+ * side_coords is updated in place.  Outputs as g2p_mesh_mark. */
+g2p_status g2p_mesh_mark_polygons(int64_t nx, int64_t ny, int64_t nz, const double *xn, const double *yn,
+                                  const double *zn, int64_t npoly, const int64_t *vert_ptr, const double *vx,
+                                  const double *vy, const double *poly_z, int32_t num_ports,
+                                  const int32_t *port_side_ptr, double *side_coords, const int32_t *side_dir_in,
+                                  int64_t *mark_node, int64_t *mark_edge, int64_t *num_cdt, int32_t *mark_port,
+                                  uint8_t *cdt_return, int64_t max_cdt, int64_t *side_edge_ptr, int64_t *side_edges,
+                                  int64_t max_side_edges, double *side_area, int32_t *side_dir);
+
 /* ---- layout ingest (host code; the reference reads GDSII with Limbo into
  * AsciiDataBase and flattens it with saveToMesh, limboint.hpp:2823-3150,
  * TestMain.cpp:258-292) ----
@@ -278,6 +299,25 @@ g2p_status g2p_gdsii_read(const char *path, const int32_t *ignore_layers, int32_
 g2p_status g2p_polygons_size(const g2p_polygons *p, int64_t *npoly, int64_t *nvert);
 g2p_status g2p_polygons_get(const g2p_polygons *p, int32_t *layer, int64_t *vert_ptr, double *x, double *y);
 void g2p_polygons_free(g2p_polygons *p);
+
+/* .sim_input reader (SolverDataBase::readSimInput, src/solnoutclass.hpp:
+ * 5412-5886, as convertToFDTDMesh passes it on, :5894-5984).  Sizes: the
+ * physically valid stack layers, the ports (sides with the same name form
+ * one port) and their sides.  g2p_sim_input_get (any output may be null):
+ * lim[6] (xlim1 xlim2 ylim1 ylim2 zlim1 zlim2, metres); units[4] = length
+ * unit, freqUnit, freqStart, freqEnd (freqEnd = freqStart for one point);
+ * freq_counts[2] = nfreq, freqScale; layers[4 * nlayer] = z begin, z end
+ * (metres), eps_r, sigma and layer_gdsii[nlayer]; port_side_ptr[nport + 1],
+ * side_coords[6 * nside] (supply x y z, return x y z, metres) and
+ * side_dir[nside] (+1 when a supply coordinate exceeds the return's).  A
+ * board-outline file in place of the x/y limits is G2P_ERR_UNSUPPORTED. */
+typedef struct g2p_sim_input g2p_sim_input;
+g2p_status g2p_sim_input_read(const char *path, g2p_sim_input **out);
+g2p_status g2p_sim_input_sizes(const g2p_sim_input *s, int32_t *nlayer, int32_t *nport, int32_t *nside);
+g2p_status g2p_sim_input_get(const g2p_sim_input *s, double *lim, double *units, int32_t *freq_counts,
+                             double *layers, int32_t *layer_gdsii, int32_t *port_side_ptr, double *side_coords,
+                             int32_t *side_dir);
+void g2p_sim_input_free(g2p_sim_input *s);
 
 /* The mesher's grid lines (meshAndMark, mesh.cpp:5-330): x/y lines from the
  * polygon vertices and port-side ends, merged and filled by the reference's

@@ -190,6 +190,41 @@ def run_ref_grid(gds_bytes, settings):
     return [lines[k] for k in "XYZES"]
 
 
+def mark_settings(sim):
+    """ref_gds --mark settings from the library's readSimInput result: the
+    limits, the valid stack layers with their GDSII numbers, and every port
+    with its sides and directions."""
+    out = " ".join(repr(float(v)) for v in sim["lim"]) + "\n%d\n" % len(sim["layers"])
+    for (zb, ze, eps, sig), g in zip(sim["layers"], sim["layer_gdsii"]):
+        out += "%r %r %r %r %d\n" % (float(zb), float(ze), float(eps), float(sig), int(g))
+    sptr = sim["port_side_ptr"]
+    out += "%d\n" % (len(sptr) - 1)
+    for p in range(len(sptr) - 1):
+        out += "%d\n" % (sptr[p + 1] - sptr[p])
+        for k in range(sptr[p], sptr[p + 1]):
+            out += " ".join(repr(float(v)) for v in sim["side_coords"][k]) + " %d\n" % int(sim["side_dir"][k])
+    return out
+
+
+def run_ref_mark(gds_path, settings):
+    """The reference's meshAndMark + portSet on a GDSII file (ref_gds
+    --mark): grid, marks, conductor ports and port sides."""
+    with tempfile.TemporaryDirectory() as d:
+        sp, dd = os.path.join(d, "in.txt"), os.path.join(d, "dump")
+        os.makedirs(dd)
+        with open(sp, "w") as f:
+            f.write(settings)
+        subprocess.run([REF_GDS, gds_path, "--mark", sp, dd], check=True, capture_output=True, text=True, cwd=d)
+        meta = open(os.path.join(dd, "meta.txt")).read().split()
+        out = {"meta": np.array([int(v) for v in meta], np.int64)}
+        ext = {"i64": np.int64, "f64": np.float64, "i32": np.int32}
+        for fn in os.listdir(dd):
+            stem, _, e = fn.rpartition(".")
+            if e in ext:
+                out[stem] = np.fromfile(os.path.join(dd, fn), ext[e])
+    return out
+
+
 def sim_input_settings(path):
     """Limits, stack and port sides of a .sim_input file in metres (stack
     layers must be named by GDSII number); None when the file does not fit."""
