@@ -250,6 +250,73 @@ static g2p_status reserve_block(g2p_solver *S, int k) {
     return G2P_OK;
 }
 
+// The FP64 hierarchy of A (as the FP64 method builds it), for a solver whose
+// FP32 V-cycle does not precondition A.
+static g2p_status build_fp64_vcycle(g2p_solver *S) {
+    cudaStream_t s = S->stream;
+    S->H64.release(s);
+    G2P_TRY(amg_setup(S->A, S->cfg, s, nullptr, S->H64));
+    for (auto &L : S->H64.lv) {
+        G2P_TRY(sell_build<double>(L.A, s));
+        if (L.P.ptr) G2P_TRY(sell_build<double>(L.P, s, 254));
+    }
+    S->fp64_vcycle = true;
+    S->levels = (int)S->H64.lv.size();
+    S->coarse_rows = S->H64.nc;
+    return G2P_OK;
+}
+
+// FP64 FGMRES from the current x: with the FP32 V-cycle as preconditioner,
+// unless that leaves the residual within a factor 100 of where it started
+// after four restart cycles; the solver then builds the FP64 hierarchy,
+// keeps it for its later solves and solves again from zero.
+static g2p_status fgmres64(g2p_solver *S, const double *b, double *x, int k, SolveReport &rep, bool use_pc32) {
+    cudaStream_t s = S->stream;
+    const int64_t nk = S->A.n * (int64_t)k;
+    if (use_pc32 && !S->fp64_vcycle) {
+        F32Precond pc;
+        pc.H = &S->H32; pc.lr = &S->lr; pc.in = S->rf; pc.out = S->df;
+        SolverConfig c1 = S->cfg;
+        c1.maxit = std::min(S->cfg.maxit, 4 * std::max(1, S->cfg.restart));
+        G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, c1, nullptr, s, rep, &pc, &S->lr));
+        bool gave_up = false;
+        G2P_TRY(coarse_gave_up<float>(S->H32, s, &gave_up));
+        if (gave_up) {       // again, with the launch-per-kernel V-cycle
+            if (getenv("G2P_DEBUG")) fprintf(stderr, "[g2p] fused coarse cycle gave up; solve repeated unfused\n");
+            G2P_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * nk, s));
+            G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, c1, nullptr, s, rep, &pc, &S->lr));
+        }
+        if (rep.converged) return G2P_OK;
+        if (rep.rel_residual <= 1e-2) {
+            SolveReport r2;
+            SolverConfig c2 = S->cfg;
+            c2.maxit = std::max(0, S->cfg.maxit - rep.iterations);
+            G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, c2, nullptr, s, r2, &pc, &S->lr));
+            r2.iterations += rep.iterations;
+            rep = r2;
+            return G2P_OK;
+        }
+        if (getenv("G2P_DEBUG"))
+            fprintf(stderr, "[g2p] n=%lld k=%d FP32 V-cycle leaves %.3e after %d iterations; FP64 hierarchy built\n",
+                    (long long)S->A.n, k, rep.rel_residual, rep.iterations);
+        const int spent = rep.iterations;
+        G2P_TRY(build_fp64_vcycle(S));
+        G2P_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * nk, s));
+        G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep, nullptr, &S->lr));
+        rep.iterations += spent;
+        return G2P_OK;
+    }
+    G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep, nullptr, &S->lr));
+    bool gave_up = false;
+    G2P_TRY(coarse_gave_up<double>(S->H64, s, &gave_up));
+    if (gave_up) {
+        if (getenv("G2P_DEBUG")) fprintf(stderr, "[g2p] fused coarse cycle gave up; solve repeated unfused\n");
+        G2P_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * nk, s));
+        G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep, nullptr, &S->lr));
+    }
+    return G2P_OK;
+}
+
 // Solve with device right-hand sides b (n x k interleaved); x is zeroed first.
 g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k, g2p_solve_stats *st) {
     auto t0 = std::chrono::steady_clock::now();
@@ -259,19 +326,8 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
     G2P_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * nk, s));
     SolveReport rep;
     int refinements = 0, iters = 0;
-    if (S->precision != G2P_PREC_MIXED) {
-        F32Precond pc;
-        pc.H = &S->H32; pc.lr = &S->lr; pc.in = S->rf; pc.out = S->df;
-        const F32Precond *pcp = S->precision == G2P_PREC_FP64_PC32 ? &pc : nullptr;
-        G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep, pcp, &S->lr));
-        bool gave_up = false;
-        if (pcp) G2P_TRY(coarse_gave_up<float>(S->H32, s, &gave_up));
-        else G2P_TRY(coarse_gave_up<double>(S->H64, s, &gave_up));
-        if (gave_up) {       // again, with the launch-per-kernel V-cycle
-            if (getenv("G2P_DEBUG")) fprintf(stderr, "[g2p] fused coarse cycle gave up; solve repeated unfused\n");
-            G2P_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * nk, s));
-            G2P_TRY(fgmres<double>(S->A, S->H64, S->K64, b, x, k, S->cfg, nullptr, s, rep, pcp, &S->lr));
-        }
+    if (S->precision != G2P_PREC_MIXED || S->fp64_vcycle) {
+        G2P_TRY(fgmres64(S, b, x, k, rep, S->precision != G2P_PREC_FP64));
         iters = rep.iterations;
         if (getenv("G2P_DEBUG"))
             fprintf(stderr, "[g2p] n=%lld k=%d fp64: its %d rel %.3e\n", (long long)n, k, rep.iterations, rep.rel_residual);
@@ -289,6 +345,8 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
         if (const char *e = getenv("G2P_INNER_REORTH")) inner.reorth = atoi(e) != 0;
         const int max_ref = S->cfg.maxit > 0 ? std::max(2, S->cfg.maxit / std::max(1, S->inner_maxit / 2)) : 20;
         rep.converged = false;
+        double prev_worst = 0;
+        bool stalled = false;
         for (int ref = 0; ref <= max_ref; ref++) {
             // x is zero on the first sweep, so its residual is b itself
             const double *res = ref == 0 ? b : S->rb;
@@ -306,6 +364,10 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
             rep.rel_residual = worst;
             if (worst <= S->cfg.rtol) { rep.converged = true; break; }
             if (ref == max_ref) break;
+            // a sweep that no longer gains a factor of 3: the FP32 inner
+            // solve has met the operator's conditioning
+            if (ref >= 2 && worst > prev_worst / 3) { stalled = true; break; }
+            prev_worst = worst;
             (g2p::kbegin("k_to_f", s), k_to_f<<<grid_for(nk), kThreads, 0, s>>>(nk, res, S->rf), g2p::kend(s));
             G2P_CUDA(cudaMemsetAsync(S->df, 0, sizeof(float) * nk, s));
             SolveReport ir;
@@ -324,6 +386,18 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
             iters += ir.iterations;
             refinements++;
         }
+        if (!rep.converged) {
+            // finish in FP64 Krylov with the FP32 V-cycle as preconditioner,
+            // from the refined solution
+            if (getenv("G2P_DEBUG"))
+                fprintf(stderr, "[g2p] n=%lld k=%d mixed refinement %s at %.3e; FP64 FGMRES with the FP32 V-cycle "
+                        "continues\n", (long long)n, k, stalled ? "stalled" : "ran out", rep.rel_residual);
+            SolveReport fr;
+            G2P_TRY(fgmres64(S, b, x, k, fr, true));
+            iters += fr.iterations;
+            rep.converged = fr.converged;
+            rep.rel_residual = fr.rel_residual;
+        }
     }
     G2P_CUDA(cudaStreamSynchronize(s));
     if (getenv("G2P_DEBUG"))
@@ -339,7 +413,12 @@ g2p_status g2p_solver_solve_dev(g2p_solver *S, const double *b, double *x, int k
         st->setup_ms = S->setup_ms;
         st->solve_ms = ms_since(t0);
     }
-    return rep.converged ? G2P_OK : G2P_ERR_NOT_CONVERGED;
+    if (!rep.converged) {
+        set_last_message("solve of %lld rows x %d right-hand sides stopped at relative residual %.3e above rtol %.1e "
+                         "after %d iterations", (long long)n, k, rep.rel_residual, S->cfg.rtol, iters);
+        return G2P_ERR_NOT_CONVERGED;
+    }
+    return G2P_OK;
 }
 
 extern "C" g2p_status g2p_solver_create(const int64_t *ARowId, const int64_t *AColId, const double *Aval,

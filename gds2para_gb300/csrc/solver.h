@@ -207,4 +207,5 @@ struct g2p_solver {
     double setup_ms = 0;
     int levels = 0;
     int64_t coarse_rows = 0;
+    bool fp64_vcycle = false;           // the FP32 V-cycle did not precondition A: FP64 hierarchy built
 };
