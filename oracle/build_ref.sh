@@ -3,7 +3,9 @@
 # compiled unmodified from the reference checkout, linked with the project's
 # shims (oracle/ref_shims/) and CPU solver (oracle/solver.c); and
 # oracle/_ref/ref_gds: the reference's GDSII database and saveToMesh
-# (limboint.hpp) with the project's stand-in for Limbo's stream reader.
+# (limboint.hpp) with the project's stand-in for Limbo's stream reader;
+# oracle/_ref/ref_network: its output stage and .sim_input reader
+# (solnoutclass.hpp) with stand-ins for Eigen and Parser-SPEF.
 # Test infrastructure only; output stays in oracle/_ref/ (git-ignored).
 # usage: oracle/build_ref.sh [reference_root]
 #   (default: $G2P_REFERENCE_ROOT, else /root/reference)
@@ -23,6 +25,12 @@ g++ $CXXFLAGS -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness.o" &
 g++ $CXXFLAGS -c "$HERE/ref_gds.cpp" -o "$OUT/ref_gds.o" &
 wait
 g++ -o "$OUT/ref_gds" "$OUT/ref_gds.o" "$OUT/mesh.o" "$OUT/mkl_sparse_shim.o" -lm
+# oracle/_ref/ref_network: the reference's output stage and .sim_input
+# reader (solnoutclass.hpp) against the project's Eigen and Parser-SPEF
+# stand-ins; the writers read an uninitialised time_t, which
+# -ftrivial-auto-var-init=zero makes the epoch
+g++ $CXXFLAGS -ftrivial-auto-var-init=zero -c "$HERE/ref_network.cpp" -o "$OUT/ref_network.o"
+g++ -o "$OUT/ref_network" "$OUT/ref_network.o" "$OUT/mkl_sparse_shim.o" -lm
 g++ -o "$OUT/ref_pipeline" "$OUT/ref_harness.o" "$OUT/mesh.o" "$OUT/generateStiff.o" "$OUT/matrixCon.o" \
     "$OUT/mkl_sparse_shim.o" "$OUT/solver.o" -lm
 # oracle/_ref/ref_pipeline_vh: the same harness with the reference's
@@ -48,4 +56,4 @@ if [ -f "$LIB/libgds2para_gb300.so" ]; then
         "$OUT/mkl_sparse_shim.o" -L"$LIB" -lgds2para_gb300 -Wl,-rpath,"$LIB" -lm
     echo "built $OUT/ref_pipeline_gb300"
 fi
-echo "built $OUT/ref_pipeline $OUT/ref_gds"
+echo "built $OUT/ref_pipeline $OUT/ref_gds $OUT/ref_network"

@@ -113,3 +113,32 @@ def test_ybus_from_y_parameters_inverts_on_the_gpu():
     w = 2.0 * np.pi * 1e9
     assert np.abs(para.matG - inv.real).max() <= 1e-12 * scale
     assert np.abs(-1 / (para.matC * w) - inv.imag).max() <= 1e-12 * scale
+
+
+# ---- convertParam on the GPU against the reference's own convertParam
+# (src/solnoutclass.hpp compiled with an Eigen stand-in whose inverse is
+# Gauss-Jordan with partial pivoting: equal to rounding, not bit for bit)
+
+def _network_ref():
+    import json
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "network_ref.npz"))
+    return z, json.loads(bytes(z["_meta"]).decode())
+
+
+@pytest.mark.parametrize("name", ["one_port", "two_port", "three_port", "five_port_small", "eight_port"])
+def test_gpu_convert_param_matches_reference_convert_param(name, g2p):
+    Z, meta = _network_ref()
+    M = meta["network"][name]
+    pre = name + "_"
+    base = {"Z": Z[pre + "z"], "Y": Z[pre + "Z_to_Y"], "S": Z[pre + "Z_to_S"]}
+    for a in "ZYS":
+        for b in "ZYS":
+            if a == b:
+                continue
+            para = g2p.Parasitics(Z[pre + "zs"], M["names"], M["dirs"])
+            para.saveNetworkParam(a, Z[pre + "freqs"], base[a].reshape(-1))
+            para.convertParam(b)
+            want = Z[pre + f"{a}_to_{b}"]
+            err = np.abs(para.matParam - want).max() / np.abs(want).max()
+            assert err < 1e-12, (a, b, err)
