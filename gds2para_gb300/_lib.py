@@ -22,7 +22,7 @@ EXPORTS = [
     "g2p_server_create", "g2p_server_submit", "g2p_server_wait", "g2p_server_destroy",
     "g2p_mesh_mark", "g2p_mesh_mark_polygons",
     "g2p_convert_param", "g2p_write_touchstone", "g2p_write_citi",
-    "g2p_ybus_from_param", "g2p_write_xyce", "g2p_write_spef",
+    "g2p_ybus_from_param", "g2p_write_xyce", "g2p_write_spef", "g2p_terminate_port", "g2p_y_from_circuit",
     "g2p_gdsii_read", "g2p_polygons_size", "g2p_polygons_get", "g2p_polygons_free", "g2p_mesh_grid",
     "g2p_sim_input_read", "g2p_sim_input_sizes", "g2p_sim_input_get", "g2p_sim_input_free",
     "g2p_find_vh", "g2p_export_vh", "g2p_set_vh", "g2p_para_generator_vh", "g2p_hessenberg_eig",
@@ -150,6 +150,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_write_touchstone.argtypes = [C.c_char_p, C.c_char, i32, i32, vp, vp, vp, C.c_char_p]
     L.g2p_write_citi.argtypes = [C.c_char_p, C.c_char, i32, i32, vp, vp, C.c_char_p]
     L.g2p_ybus_from_param.argtypes = [C.c_char, i32, dbl, vp, vp, vp]
+    L.g2p_terminate_port.argtypes = [C.c_char, i32, i32, vp, i32, i32, vp, vp, vp]
+    L.g2p_y_from_circuit.argtypes = [i32, i32, vp, vp, vp, vp]
     L.g2p_write_xyce.argtypes = [C.c_char_p, C.c_char_p, i32, C.POINTER(C.c_char_p), dbl, vp, vp, dbl]
     L.g2p_write_spef.argtypes = [C.c_char_p, C.c_char_p, i32, C.POINTER(C.c_char_p), C.c_char_p, vp, vp, dbl]
     L.g2p_gdsii_read.argtypes = [C.c_char_p, vp, i32, C.POINTER(vp)]

@@ -574,6 +574,28 @@ class Parasitics:
         check(rc)
         self.matG, self.matC = g, c
 
+    def terminatePortZ(self, indPort: int, ZLoad):
+        """terminatePortZ (src/solnoutclass.hpp:1767-1842) on the GPU: the
+        port loaded by ZLoad (its first value, imaginary part scaled with
+        frequency) and removed by Kron reduction."""
+        _terminate(self, "Z", indPort, ZLoad)
+
+    def terminatePortY(self, indPort: int, YLoad):
+        """terminatePortY (src/solnoutclass.hpp:1844-1921), as terminatePortZ."""
+        _terminate(self, "Y", indPort, YLoad)
+
+    def computeYParamFromCircuit(self):
+        """computeYParamFromCircuit (src/solnoutclass.hpp:1617-1678) on the
+        GPU: Y = G + j 2 pi f C at every frequency."""
+        n, nf = self.getNPort(), len(self.freqs)
+        g = np.ascontiguousarray(self.matG, np.float64)
+        c = np.ascontiguousarray(self.matC, np.float64)
+        out = np.zeros(2 * nf * n * n)
+        check(_lib.load().g2p_y_from_circuit(n, nf, self.freqs.ctypes.data, g.ctypes.data, c.ctypes.data,
+                                             out.ctypes.data))
+        self.matParam = out.view(np.complex128).reshape(nf, n, n)
+        self.param = "Y"
+
     def convertParam(self, newParam: str):
         """convertParam (src/solnoutclass.hpp:1456-1610) on the GPU."""
         if newParam not in ("Z", "Y", "S"):
@@ -586,6 +608,23 @@ class Parasitics:
                                             self.z_source.ctypes.data, buf.ctypes.data, buf.ctypes.data))
         self.matParam = buf.view(np.complex128).reshape(nf, n, n)
         self.param = newParam
+
+
+def _terminate(para: "Parasitics", kind: str, indPort: int, load):
+    if para.param != kind:
+        raise ValueError(f"terminating a port with {'an impedance' if kind == 'Z' else 'an admittance'} needs "
+                         f"{kind}-parameters")
+    n, nf = para.getNPort(), len(para.freqs)
+    ld = np.ascontiguousarray(np.atleast_1d(np.asarray(load, np.complex128))).view(np.float64).ravel()
+    buf = np.ascontiguousarray(para.matParam, np.complex128).view(np.float64).ravel()
+    out = np.zeros(2 * nf * (n - 1) * (n - 1))
+    check(_lib.load().g2p_terminate_port(kind.encode(), n, nf, para.freqs.ctypes.data, int(indPort), len(ld) // 2,
+                                         ld.ctypes.data, buf.ctypes.data, out.ctypes.data))
+    para.matParam = out.view(np.complex128).reshape(nf, n - 1, n - 1)
+    keep = [i for i in range(n) if i != indPort]
+    para.z_source = para.z_source[keep].copy()
+    para.port_names = [para.port_names[i] for i in keep]
+    para.port_dirs = "".join(para.port_dirs[i] for i in keep)
 
 
 def _dump(fn, path, para: Parasitics, design: str, with_z: bool) -> bool:

@@ -527,3 +527,117 @@ extern "C" g2p_status g2p_write_spef(const char *path, const char *design, int32
     }
     return G2P_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Port termination (Parasitics::terminatePortZ / terminatePortY,
+// src/solnoutclass.hpp:1767-1921) and the circuit's Y-parameters
+// (computeYParamFromCircuit, :1617-1678).
+namespace g2p {
+namespace {
+
+// Kron reduction of port k loaded by l[f]: p'_ij = p_ij - p_ik p_kj / (p_kk + l)
+// for i, j != k, one thread per output entry of every frequency
+__global__ void k_kron(int n, int nfreq, int k, const double *in, const double *load, double *out) {
+    const int m = n - 1;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)nfreq * m * m;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t f = t / ((int64_t)m * m);
+        const int r = (int)(t % ((int64_t)m * m));
+        const int i = r / m + (r / m >= k ? 1 : 0), j = r % m + (r % m >= k ? 1 : 0);
+        const double *p = in + 2 * f * n * n;
+        const Cx pij = {p[2 * (i * n + j)], p[2 * (i * n + j) + 1]};
+        const Cx pik = {p[2 * (i * n + k)], p[2 * (i * n + k) + 1]};
+        const Cx pkj = {p[2 * (k * n + j)], p[2 * (k * n + j) + 1]};
+        const Cx den = cadd({p[2 * (k * n + k)], p[2 * (k * n + k) + 1]}, {load[2 * f], load[2 * f + 1]});
+        const Cx v = csub(pij, cdiv(cmul(pik, pkj), den));
+        out[2 * t] = v.re;
+        out[2 * t + 1] = v.im;
+    }
+}
+
+__global__ void k_y_circuit(int n, int nfreq, const double *freqs, const double *G, const double *C, double *out) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)nfreq * n * n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t f = t / ((int64_t)n * n);
+        const int e = (int)(t % ((int64_t)n * n));
+        out[2 * t] = G[e];
+        out[2 * t + 1] = 2. * 3.14159265358979323846 * freqs[f] * C[e];
+    }
+}
+
+}  // namespace
+}  // namespace g2p
+
+extern "C" g2p_status g2p_terminate_port(char param, int32_t nports, int32_t nfreq, const double *freqs, int32_t port,
+                                         int32_t nload, const double *load, const double *in, double *out) {
+    if ((param != 'Z' && param != 'Y') || nports < 2 || nfreq < 1 || port < 0 || port >= nports || !freqs || !load ||
+        !in || !out) {
+        set_last_message("g2p_terminate_port: Z or Y parameters, 2 or more ports, a port index in range");
+        return G2P_ERR_INVALID;
+    }
+    if (nload != 1 && nfreq == 1) {
+        set_last_message("g2p_terminate_port: %d load values for one frequency", nload);
+        return G2P_ERR_INVALID;
+    }
+    // the load at the first frequency, its imaginary part scaled with
+    // frequency (the reference's rule whenever the sweep has more than one
+    // point or one load value is given)
+    std::vector<double> f(nfreq), l(2 * (size_t)nfreq);
+    double l0[2];
+    G2P_CUDA(cudaMemcpy(f.data(), freqs, sizeof(double) * nfreq, cudaMemcpyDefault));
+    G2P_CUDA(cudaMemcpy(l0, load, sizeof(double) * 2, cudaMemcpyDefault));
+    for (int q = 0; q < nfreq; q++) {
+        l[2 * q] = l0[0];
+        l[2 * q + 1] = l0[1] * f[q] / f[0];
+    }
+    const int64_t nin = 2LL * nfreq * nports * nports, nout = 2LL * nfreq * (nports - 1) * (nports - 1);
+    cudaStream_t s;
+    G2P_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    double *d_in = nullptr, *d_out = nullptr, *d_l = nullptr;
+    auto run = [&]() -> g2p_status {
+        G2P_TRY(dalloc(&d_in, nin, s));
+        G2P_TRY(dalloc(&d_out, nout, s));
+        G2P_TRY(dalloc(&d_l, 2LL * nfreq, s));
+        G2P_CUDA(cudaMemcpyAsync(d_in, in, sizeof(double) * nin, cudaMemcpyDefault, s));
+        G2P_CUDA(cudaMemcpyAsync(d_l, l.data(), sizeof(double) * 2 * nfreq, cudaMemcpyHostToDevice, s));
+        (kbegin("k_kron", s), k_kron<<<grid_for(nout / 2), kThreads, 0, s>>>(nports, nfreq, port, d_in, d_l, d_out), kend(s));
+        G2P_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * nout, cudaMemcpyDefault, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
+        return G2P_OK;
+    };
+    g2p_status st = run();
+    dfree(d_in, s); dfree(d_out, s); dfree(d_l, s);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return st;
+}
+
+extern "C" g2p_status g2p_y_from_circuit(int32_t nports, int32_t nfreq, const double *freqs, const double *G,
+                                         const double *C, double *out) {
+    if (nports < 1 || nfreq < 1 || !freqs || !G || !C || !out) {
+        set_last_message("g2p_y_from_circuit: bad arguments");
+        return G2P_ERR_INVALID;
+    }
+    const int64_t nn = (int64_t)nports * nports, nout = 2LL * nfreq * nn;
+    cudaStream_t s;
+    G2P_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    double *d_f = nullptr, *d_g = nullptr, *d_c = nullptr, *d_o = nullptr;
+    auto run = [&]() -> g2p_status {
+        G2P_TRY(dalloc(&d_f, nfreq, s));
+        G2P_TRY(dalloc(&d_g, nn, s));
+        G2P_TRY(dalloc(&d_c, nn, s));
+        G2P_TRY(dalloc(&d_o, nout, s));
+        G2P_CUDA(cudaMemcpyAsync(d_f, freqs, sizeof(double) * nfreq, cudaMemcpyDefault, s));
+        G2P_CUDA(cudaMemcpyAsync(d_g, G, sizeof(double) * nn, cudaMemcpyDefault, s));
+        G2P_CUDA(cudaMemcpyAsync(d_c, C, sizeof(double) * nn, cudaMemcpyDefault, s));
+        (kbegin("k_y_circuit", s), k_y_circuit<<<grid_for(nout / 2), kThreads, 0, s>>>(nports, nfreq, d_f, d_g, d_c, d_o), kend(s));
+        G2P_CUDA(cudaMemcpyAsync(out, d_o, sizeof(double) * nout, cudaMemcpyDefault, s));
+        G2P_CUDA(cudaStreamSynchronize(s));
+        return G2P_OK;
+    };
+    g2p_status st = run();
+    dfree(d_f, s); dfree(d_g, s); dfree(d_c, s); dfree(d_o, s);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return st;
+}

@@ -426,6 +426,22 @@ g2p_status g2p_write_citi(const char *path, char param, int32_t nports, int32_t 
  * (on the GPU); G = Re Y, C(i,j) = -1 / (Im Y(i,j) * 2 pi freq0).  'S'
  * returns G2P_ERR_UNSUPPORTED (the reference leaves Y empty there). */
 g2p_status g2p_ybus_from_param(char param, int32_t nports, double freq0, const double *p0, double *G, double *C);
+/* g2p_terminate_port: terminatePortZ / terminatePortY (src/solnoutclass.hpp:
+ * 1767-1921) on the GPU: port `port` of Z- ('Z') or Y-parameters ('Y') loaded
+ * by an impedance or admittance and reduced away (Kron reduction,
+ * p'_ij = p_ij - p_ik p_kj / (p_kk + load) for i, j != k); out holds
+ * nfreq (nports-1)^2 complex values.  As in the reference the load is
+ * load[0] at the first frequency with its imaginary part scaled by f / f0
+ * (nload must be 1 for a single frequency).  The reference's own version
+ * assigns where it compares (`if (indi = indPort)`) and fills only the upper
+ * triangle, so it never finishes for a port after the first and leaves the
+ * lower triangle zero otherwise; this one reduces the whole matrix.
+ * g2p_y_from_circuit: computeYParamFromCircuit (:1617-1678), Y_f = G +
+ * j 2 pi f C for every frequency. */
+g2p_status g2p_terminate_port(char param, int32_t nports, int32_t nfreq, const double *freqs, int32_t port,
+                              int32_t nload, const double *load, const double *in, double *out);
+g2p_status g2p_y_from_circuit(int32_t nports, int32_t nfreq, const double *freqs, const double *G, const double *C,
+                              double *out);
 /* g2p_write_xyce: dumpXyce / toXyce (src/solnoutclass.hpp:2094-2225,
  * 6032-6037), a SPICE subcircuit; g2p_write_spef: dumpSPEF / toSPEF
  * (src/solnoutclass.hpp:1972-2091, 6008-6030), an IEEE 1481-1998 SPEF file

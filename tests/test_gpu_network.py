@@ -142,3 +142,42 @@ def test_gpu_convert_param_matches_reference_convert_param(name, g2p):
             want = Z[pre + f"{a}_to_{b}"]
             err = np.abs(para.matParam - want).max() / np.abs(want).max()
             assert err < 1e-12, (a, b, err)
+
+
+def test_gpu_terminate_port_kron_reduction(g2p):
+    rng = np.random.default_rng(5)
+    n, freqs = 4, np.array([1e8, 2e8, 5e8])
+    z = rng.normal(size=(3, n, n)) + 1j * rng.normal(size=(3, n, n)) + 10 * np.eye(n)
+    zl = 50.0 + 10.0j
+    for k in range(n):
+        para = g2p.Parasitics([50.0] * n, [f"p{i}" for i in range(n)], "IOBI")
+        para.saveNetworkParam("Z", freqs, z.reshape(-1))
+        para.terminatePortZ(k, [zl])
+        keep = [i for i in range(n) if i != k]
+        for f in range(3):
+            load = complex(zl.real, zl.imag * freqs[f] / freqs[0])
+            want = z[f][np.ix_(keep, keep)] - np.outer(z[f][keep, k], z[f][k, keep]) / (z[f][k, k] + load)
+            np.testing.assert_allclose(para.matParam[f], want, rtol=1e-13, atol=1e-13)
+        assert para.getNPort() == n - 1 and para.port_names == [f"p{i}" for i in keep]
+
+
+def test_gpu_terminate_port_t_network_input_impedance(g2p):
+    za, zb, zc, zl = 10 + 2j, 20 - 5j, 30 + 1j, 50.0 + 0j
+    z = np.array([[[za + zc, zc], [zc, zb + zc]]])
+    para = g2p.Parasitics([50.0, 50.0])
+    para.saveNetworkParam("Z", [1e9], z.reshape(-1))
+    para.terminatePortZ(1, [zl])
+    assert abs(para.matParam[0, 0, 0] - (za + zc * (zb + zl) / (zc + zb + zl))) < 1e-12
+
+
+def test_gpu_y_from_circuit(g2p):
+    rng = np.random.default_rng(6)
+    g, c = rng.normal(size=(3, 3)), rng.normal(size=(3, 3)) * 1e-12
+    freqs = np.array([1e8, 1e9])
+    para = g2p.Parasitics([50.0] * 3)
+    para.freqs = freqs
+    para.matG, para.matC = g, c
+    para.computeYParamFromCircuit()
+    assert para.param == "Y"
+    for f in range(2):
+        np.testing.assert_allclose(para.matParam[f], g + 2j * np.pi * freqs[f] * c, rtol=1e-15, atol=0)
