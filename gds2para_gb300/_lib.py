@@ -24,7 +24,7 @@ EXPORTS = [
     "g2p_convert_param", "g2p_write_touchstone", "g2p_write_citi",
     "g2p_ybus_from_param", "g2p_write_xyce", "g2p_write_spef", "g2p_terminate_port", "g2p_y_from_circuit",
     "g2p_gdsii_read", "g2p_polygons_size", "g2p_polygons_get", "g2p_polygons_free", "g2p_mesh_grid",
-    "g2p_sim_input_read", "g2p_sim_input_sizes", "g2p_sim_input_get", "g2p_sim_input_free",
+    "g2p_stiff_apply", "g2p_sim_input_read", "g2p_sim_input_sizes", "g2p_sim_input_get", "g2p_sim_input_free",
     "g2p_find_vh", "g2p_export_vh", "g2p_set_vh", "g2p_para_generator_vh", "g2p_hessenberg_eig",
 ]
 
@@ -165,6 +165,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.g2p_sim_input_get.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.g2p_sim_input_free.argtypes = [vp]
     L.g2p_sim_input_free.restype = None
+    L.g2p_stiff_apply.argtypes = [vp, i32, i32, vp, vp, C.POINTER(dbl)]
     L.g2p_find_vh.argtypes = [vp, i32, C.POINTER(i64)]
     L.g2p_export_vh.argtypes = [vp, vp]
     L.g2p_set_vh.argtypes = [vp, vp, i64]

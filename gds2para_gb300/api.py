@@ -243,6 +243,17 @@ def paraGenerator(sys: FdtdMesh, params: Optional[SolverParams] = None):
     return zc.reshape(d.nfreq, d.num_ports, d.num_ports), st
 
 
+def stiffApply(sys: FdtdMesh, x: np.ndarray, matrix_free: bool = True, reps: int = 1):
+    """y = S x over the non-PEC edges, by the matrix-free curl-curl stencil
+    or the assembled CSR; returns (y, device ms per product)."""
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.zeros_like(x)
+    ms = C.c_double()
+    check(_lib.load().g2p_stiff_apply(sys.handle, 1 if matrix_free else 0, int(reps), x.ctypes.data, y.ctypes.data,
+                                      C.byref(ms)))
+    return y, ms.value
+
+
 def findVh(sys: FdtdMesh, k: int = 1000) -> np.ndarray:
     """find_Vh (src/fdtd.hpp:3577-3859): k Arnoldi steps on the device, the
     Hessenberg eigenproblem on the host; returns Vh, complex (N, leng_Vh)
@@ -300,7 +311,7 @@ def hessenbergEigenvalues(h: np.ndarray) -> np.ndarray:
 
 __all__ = ["FdtdMesh", "generateStiff", "hypreSolve", "paraGenerator", "Solver", "Server", "meshAndMark",
            "readSimInput", "polygonZ", "meshAndMarkPolygons", "layoutFromGDS",
-           "findVh", "setVh", "paraGeneratorVh", "hessenbergEigenvalues",
+           "stiffApply", "findVh", "setVh", "paraGeneratorVh", "hessenbergEigenvalues",
            "Parasitics", "dumpTouchstone", "dumpCITI", "dumpXyce", "dumpSPEF", "default_params", "G2PError"]
 
 

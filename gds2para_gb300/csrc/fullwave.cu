@@ -80,6 +80,22 @@ __global__ void k_fw_apply(int64_t nr, const int64_t *ptr, const int32_t *col, c
     }
 }
 
+// The same product with S v already in t (the matrix-free stencil):
+// w[r] = v[nr + r]; w[nr + r] = -t[r] / (eps eps0 s^2) (+ the conductor term)
+__global__ void k_fw_apply_sv(int64_t nr, const double *t, const int32_t *map_r, const int32_t *mark_edge,
+                              const double *epsn, const double *sign, int64_t L, double eps0, double scale,
+                              const double *v, double *w) {
+    const double s2 = scale * scale;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nr; r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = map_r[r];
+        const double eps = epsn[e / L];
+        double acc = -t[r] / (eps * eps0 * s2);
+        if (mark_edge[e] != 0) acc += -v[nr + r] * sign[e / L] / (eps * eps0 * scale);
+        w[r] = v[nr + r];
+        w[nr + r] = acc;
+    }
+}
+
 // Block partial sums of x . y (FP64), a fixed tree per block.
 __global__ void __launch_bounds__(kFwThreads) k_fw_dot(int64_t n, const double *x, const double *y, double *partial) {
     __shared__ double sm[kFwThreads / 32];
@@ -729,8 +745,18 @@ extern "C" g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh) {
     F.nr = nr;
     G2P_TRY(dalloc(&F.map_r, nr, s));
     (kbegin("k_fw_map_r", s), k_fw_map_r<<<grid_for(d.N_edge), kThreads, 0, s>>>(d.N_edge, m->map_edge, F.map_r), kend(s));
-    double *V, *w, *Hd, *partial;
+    double *V, *w, *Hd, *partial, *sv = nullptr;
     const int nb = 152 * 4;
+    // S v by the assembled CSR rows, each summed in S's entry order as the
+    // reference sums them; G2P_FW_STENCIL=1 applies the matrix-free stencil
+    // instead (equal to rounding, and no S traffic, but at k = 1000 the
+    // Arnoldi basis amplifies rounding: the count of eigenvalues past the
+    // |Im| > 1e-6 filter can then differ from the reference's by a few)
+    const bool csr = getenv("G2P_FW_STENCIL") == nullptr;
+    if (!csr) {
+        if (!m->stencil) G2P_TRY(stencil_build(m, &m->stencil));
+        G2P_TRY(dalloc(&sv, nr, s));
+    }
     G2P_TRY(dalloc(&V, (int64_t)(k + 1) * n2, s));
     G2P_TRY(dalloc(&w, n2, s));
     G2P_TRY(dalloc(&Hd, (int64_t)k * k + k, s));
@@ -741,7 +767,12 @@ extern "C" g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh) {
     double *hnext = Hd + (int64_t)k * k;       // the norm after the last step (not part of H)
     for (int j = 1; j <= k; j++) {
         const double *vp = V + (int64_t)(j - 1) * n2;
-        (kbegin("k_fw_apply", s), k_fw_apply<<<fw_grid(nr), kFwThreads, 0, s>>>(nr, m->S.ptr, m->S.col, m->S.val, F.map_r, m->mark_edge, m->epsn, m->sign, d.L, m->k.eps0, scale, vp, w), kend(s));
+        if (csr) {
+            (kbegin("k_fw_apply", s), k_fw_apply<<<fw_grid(nr), kFwThreads, 0, s>>>(nr, m->S.ptr, m->S.col, m->S.val, F.map_r, m->mark_edge, m->epsn, m->sign, d.L, m->k.eps0, scale, vp, w), kend(s));
+        } else {
+            G2P_TRY(stencil_apply(m, m->stencil, vp, sv, s));
+            (kbegin("k_fw_apply_sv", s), k_fw_apply_sv<<<fw_grid(nr), kFwThreads, 0, s>>>(nr, sv, F.map_r, m->mark_edge, m->epsn, m->sign, d.L, m->k.eps0, scale, vp, w), kend(s));
+        }
         double *hcol = Hd + (int64_t)(j - 1) * k;
         // modified Gram-Schmidt: h_i = V_i . w, w -= h_i V_i, in order; the
         // last update also gives the partials of |w|^2
@@ -759,6 +790,11 @@ extern "C" g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh) {
     std::vector<double> H((size_t)k * k);
     G2P_CUDA(cudaMemcpyAsync(H.data(), Hd, sizeof(double) * k * k, cudaMemcpyDeviceToHost, s));
     G2P_CUDA(cudaStreamSynchronize(s));
+    dfree(sv, s);
+    if (!csr) {
+        const g2p_status sc = stencil_check(m->stencil, s);
+        if (sc != G2P_OK) { dfree(V, s); dfree(w, s); dfree(Hd, s); dfree(partial, s); return sc; }
+    }
     // eigenvalues, and the right eigenvectors of those with |Im| > 1e-6
     std::vector<double> H1((size_t)k * k, 0.0), wr(k), wi(k);
     for (int i = 0; i < k; i++)

@@ -62,6 +62,13 @@ struct V0Basis {
 // A Laplacian whose ordered conductor sums still run on the side stream.
 struct LapPending;
 
+// The matrix-free curl-curl stencil of a mesh's S (stencil.cu).
+struct CurlStencil;
+void stencil_release(CurlStencil *st, cudaStream_t s);
+g2p_status stencil_build(g2p_mesh *m, CurlStencil **out);
+g2p_status stencil_apply(g2p_mesh *m, CurlStencil *st, const double *x, double *y, cudaStream_t s);
+g2p_status stencil_check(CurlStencil *st, cudaStream_t s);
+
 // The full-wave (Vh) state of a mesh: Vh and, while the V0 path runs for it,
 // the ports' V0 field directions (fullwave.cu).
 struct FullWave;
@@ -114,8 +121,9 @@ struct g2p_mesh {
     double *v0_tab = nullptr;      // per-line quotient tables of the V0 entries
     g2p::V0Basis v0d, v0c;
     g2p::Csr<double> Ad, Ac;
-    // full-wave mode (g2p_find_vh)
+    // full-wave mode (g2p_find_vh) and the matrix-free S it applies
     g2p::FullWave *fw = nullptr;
+    g2p::CurlStencil *stencil = nullptr;
     // scratch for scans
     int64_t *scan_work = nullptr;
     int64_t scan_work_n = 0;

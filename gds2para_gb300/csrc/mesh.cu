@@ -286,6 +286,8 @@ extern "C" g2p_status g2p_mesh_destroy(g2p_mesh *m) {
     dfree(m->scan_work, s);
     g2p::fullwave_release(m->fw, s);
     m->fw = nullptr;
+    g2p::stencil_release(m->stencil, s);
+    m->stencil = nullptr;
     if (s) { cudaStreamSynchronize(s); cudaStreamDestroy(s); }
     delete m;
     return G2P_OK;

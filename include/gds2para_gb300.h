@@ -222,6 +222,13 @@ g2p_status g2p_set_vh(g2p_mesh *m, const double *vh, int64_t leng_vh);
 g2p_status g2p_para_generator_vh(g2p_mesh *m, const g2p_solver_params *p, int32_t k, double *z_vh, double *z_v0,
                                  g2p_extract_stats *st);
 g2p_status g2p_hessenberg_eig(int64_t n, const double *h, double *wr, double *wi);
+/* g2p_stiff_apply: y = S x (x, y: host or device, leng_S's row count each)
+ * by the assembled CSR (matrix_free = 0) or by the matrix-free curl-curl
+ * stencil (1: face circulations then edge sums over full-grid arrays staged
+ * by TMA tiles; the same coefficients as generateStiff, equal to rounding;
+ * g2p_find_vh applies S this way).  *ms (nullable) receives the device time
+ * of one product averaged over reps >= 1 repetitions. */
+g2p_status g2p_stiff_apply(g2p_mesh *m, int32_t matrix_free, int32_t reps, const double *x, double *y, double *ms);
 
 /* ---- diagnostics (no counterpart in the reference) ----
  * g2p_launch_count: kernels launched by the library so far in this process.
