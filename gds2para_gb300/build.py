@@ -26,7 +26,7 @@ NO_FMA = {"mesh.cu", "v0.cu", "extract.cu", "mesher.cu"}
 # host code whose results must not depend on the host compiler contracting
 # a * b + c into one rounding (the oracle builds with -ffp-contract=off)
 NO_HOST_CONTRACT = {"ingest.cu", "mesher.cu"}
-UNITS = ["primitives.cu", "mesh.cu", "v0.cu", "solver.cu", "coarse.cu", "solve_api.cu", "extract.cu", "fullwave.cu", "stencil.cu", "noalloc.cu", "serve.cu", "mesher.cu",
+UNITS = ["primitives.cu", "mesh.cu", "v0.cu", "solver.cu", "block_krylov.cu", "coarse.cu", "solve_api.cu", "extract.cu", "fullwave.cu", "stencil.cu", "noalloc.cu", "serve.cu", "mesher.cu",
          "network.cu", "ingest.cu"]
 
 

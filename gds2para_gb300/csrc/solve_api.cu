@@ -131,6 +131,7 @@ static SolverConfig cfg_from(const g2p_solver_params *p) {
     if (const char *e = getenv("G2P_CHEB_RATIO")) c.cheb_ratio = atof(e);   // comparisons
     if (const char *e = getenv("G2P_CHEB_UPPER")) c.cheb_upper = atof(e);
     if (const char *e = getenv("G2P_PSMOOTH")) c.psmooth = atof(e);
+    if (const char *e = getenv("G2P_BLOCK_KRYLOV")) c.block = atoi(e) != 0;
     return c;
 }
 

@@ -2640,6 +2640,10 @@ void Krylov<T>::release(cudaStream_t s) {
     dfree(beta, s); dfree(bnorm, s); dfree(partial, s); dfree(hcol, s);
     if (h_est) cudaFreeHost(h_est);
     h_est = nullptr;
+    dfree(bdev, s); dfree(bpart, s);
+    if (bhost) cudaFreeHost(bhost);
+    bhost = nullptr;
+    bk = 0; bm = 0;
     n = 0; k = 0; m = 0;
 }
 template struct Krylov<double>;
@@ -2799,6 +2803,8 @@ template <class T>
 g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T *x, int k, const SolverConfig &cfg,
                   const double *bnorm_override, cudaStream_t s, SolveReport &rep, const F32Precond *pc,
                   const LongRows *op_lr) {
+    if (cfg.block && !pc && block_krylov_supported<T>(k, b, x))
+        return block_fgmres<T>(A, H, K, b, x, k, cfg, bnorm_override, s, rep, op_lr);
     const int64_t n = A.n, nk = n * k;
     const int m = cfg.restart;
     if (k < 1 || k > kMaxRhs) { set_last_message("block of %d right-hand sides (1..%d supported)", k, kMaxRhs); return G2P_ERR_INVALID; }
@@ -2944,6 +2950,24 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
     G2P_CUDA(cudaGetLastError());
     return G2P_OK;
 }
+template <class T>
+void precond_vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int k, cudaStream_t s, const T *b, T *x) {
+    vcycle<T>(H, cfg, 0, k, s, b, x);
+}
+template void precond_vcycle<double>(Hierarchy<double> &, const SolverConfig &, int, cudaStream_t, const double *,
+                                     double *);
+template void precond_vcycle<float>(Hierarchy<float> &, const SolverConfig &, int, cudaStream_t, const float *,
+                                    float *);
+
+template <class T>
+void spmm_residual(const Csr<T> &A, const LongRows &lr, const T *x, T *r, int k, const T *b, cudaStream_t s) {
+    spmm_b<T>(A, lr, x, r, k, b, s);
+}
+template void spmm_residual<double>(const Csr<double> &, const LongRows &, const double *, double *, int,
+                                    const double *, cudaStream_t);
+template void spmm_residual<float>(const Csr<float> &, const LongRows &, const float *, float *, int, const float *,
+                                   cudaStream_t);
+
 template g2p_status fgmres<double>(const Csr<double> &, Hierarchy<double> &, Krylov<double> &, const double *, double *,
                                    int, const SolverConfig &, const double *, cudaStream_t, SolveReport &,
                                    const F32Precond *, const LongRows *);

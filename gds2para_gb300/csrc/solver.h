@@ -60,6 +60,7 @@ struct SolverConfig {
     double psmooth = 4.0 / 3.0;  // prolongation smoothing weight = psmooth / lmax
     bool reorth = true;
     bool use_graphs = false;     // replay each Arnoldi step from a CUDA graph
+    bool block = false;          // the k right-hand sides share one block Krylov space
 };
 
 // The fused coarse tail of the V-cycle (coarse.cu): levels of at most
@@ -127,6 +128,10 @@ struct Krylov {
     };
     std::vector<Step> steps;
     std::vector<const void *> graph_key;
+    // block iteration (block_krylov.cu): device scratch, Gram-Schmidt
+    // partial sums, pinned host copies; sized for bk right-hand sides, bm steps
+    double *bdev = nullptr, *bpart = nullptr, *bhost = nullptr;
+    int bk = 0, bm = 0;
     void drop_graphs();
     void release(cudaStream_t s);
 };
@@ -153,10 +158,29 @@ struct F32Precond {
 // only) the V-cycle runs in FP32 on pc->H and H is not used.  op_lr: the long
 // rows of A (default: those of pc, or of H's level 0, which must then have
 // A's pattern).
+// With cfg.block (and no pc, k in {2, 4, 8, 16, 32}, b and x 16-byte
+// aligned) the solve is block FGMRES (block_fgmres).
 template <class T>
 g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T *x, int k, const SolverConfig &cfg,
                   const double *bnorm_override, cudaStream_t s, SolveReport &rep, const F32Precond *pc = nullptr,
                   const LongRows *op_lr = nullptr);
+
+// Block FGMRES(m) (block_krylov.cu): the k right-hand sides share one block
+// Krylov space (block Arnoldi with block Gram-Schmidt and Cholesky QR, one
+// V-cycle of the k columns per step, block Givens least squares on the
+// host).  Same arguments and report as fgmres without pc.
+template <class T>
+bool block_krylov_supported(int k, const T *b, const T *x);
+template <class T>
+g2p_status block_fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T *x, int k,
+                        const SolverConfig &cfg, const double *bnorm_override, cudaStream_t s, SolveReport &rep,
+                        const LongRows *op_lr = nullptr);
+// One V-cycle of H from level 0 (x = M^-1 b) for k right-hand sides.
+template <class T>
+void precond_vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int k, cudaStream_t s, const T *b, T *x);
+// r = b - A x for k right-hand sides (FP64 or FP32).
+template <class T>
+void spmm_residual(const Csr<T> &A, const LongRows &lr, const T *x, T *r, int k, const T *b, cudaStream_t s);
 
 template <class T>
 g2p_status krylov_alloc(Krylov<T> &K, int64_t n, int k, int m, cudaStream_t s);
