@@ -241,6 +241,8 @@ def run_gb300(args):
             "total_ms": stats.total_ms, "iterations": stats.total_iterations,
             "max_rel_residual": stats.max_rel_residual, "ad_levels": stats.ad_levels, "ac_levels": stats.ac_levels,
             "rhs_block": stats.rhs_block, "ad_degree": stats.ad_degree, "ac_strength": stats.ac_strength,
+            "ac_precision": {0: "fp64", 1: "mixed", 2: "fp64_pc32"}.get(stats.ac_precision, stats.ac_precision),
+            "ac_iterations": stats.ac_iterations,
             "autotune": ("off: fixed blocks of 4 ports (the HBM budget)" if big else
                          "block width and Chebyshev degree (first Ad solve timed per candidate) and Ac's "
                          "aggregation strength (first Ac solve timed per candidate) picked in the warm-up"),

@@ -70,7 +70,7 @@ class ExtractStats(C.Structure):
                 ("max_rel_residual", C.c_double), ("assembly_ms", C.c_double), ("setup_ms", C.c_double),
                 ("solve_ms", C.c_double), ("total_ms", C.c_double), ("ad_levels", C.c_int32),
                 ("ac_levels", C.c_int32), ("rhs_block", C.c_int32), ("ad_degree", C.c_int32),
-                ("ac_strength", C.c_double)]
+                ("ac_strength", C.c_double), ("ac_precision", C.c_int32), ("ac_iterations", C.c_int32)]
 
 
 class BoxC(C.Structure):

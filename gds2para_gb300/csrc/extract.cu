@@ -260,33 +260,49 @@ static std::map<TuneKey, std::pair<int, int>> g_tuned;   // -> (block width, deg
 // Aggregation strength of Ac's AMG, keyed by Ac's entry count in nnz.  Ac's
 // iteration count is far from monotonic in it (c3: 24 iterations at 0.02, 54
 // at 0.04, 76 at 0.08; c2: 45, 37 and 33), so it is measured per shape.
-static std::map<TuneKey, double> g_ac_tuned;
+// Ac's tuned solver: aggregation strength and precision mode
+struct AcChoice {
+    double strength;
+    int precision;
+    bool operator!=(const AcChoice &o) const { return strength != o.strength || precision != o.precision; }
+};
+static std::map<TuneKey, AcChoice> g_ac_tuned;
 
-static bool ac_tuned(const TuneKey &key, double *strength) {
+static bool ac_tuned(const TuneKey &key, AcChoice *c) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_ac_tuned.find(key);
     if (it == g_ac_tuned.end()) return false;
-    *strength = it->second;
+    *c = it->second;
     return true;
 }
 
 // Times Ac's solve of the first block with the strength thresholds st0 / 2,
-// st0 and 2 st0 (at most 0.1), st0 being Ad's; *Sc (built with pc) is one of
-// them.  Each candidate: one untimed solve, then the better of two timed
-// ones.  *Sc is replaced by the solver of the recorded choice: the fastest
-// candidate, unless another job of the shape recorded its choice first.
-static g2p_status tune_ac(g2p_mesh *m, const TuneKey &key, const g2p_solver_params &pc, double st0, g2p_solver **Sc,
-                          const double *Bc, double *Yc, int kk, cudaStream_t s) {
-    std::vector<double> cands = {st0 / 2, st0, std::min(2 * st0, 0.1)};
-    double best_ms = 1e300, best_st = pc.strength;
+// st0 and 2 st0 (at most 0.1), st0 being Ad's, and, when modes lists more
+// than one precision mode, with each of them; *Sc (built with pc) is one of
+// the candidates.  Each candidate: one untimed solve, then the better of two
+// timed ones.  *Sc is replaced by the solver of the recorded choice: the
+// fastest candidate, unless another job of the shape recorded its choice
+// first.  (Ac in the mixed mode's FP32 refinement is faster where its sweeps
+// converge, e.g. c3's 256 x 256 x 16 layout, and stalls into the FP64
+// fallback where they do not, e.g. c2's; only timing tells them apart.)
+static g2p_status tune_ac(g2p_mesh *m, const TuneKey &key, const g2p_solver_params &pc, double st0,
+                          const std::vector<int> &modes, g2p_solver **Sc, const double *Bc, double *Yc, int kk,
+                          cudaStream_t s) {
+    std::vector<AcChoice> cands;
+    for (int mode : modes)
+        for (double st : {st0 / 2, st0, std::min(2 * st0, 0.1)}) cands.push_back({st, mode});
+    const AcChoice cur{pc.strength, pc.precision};
+    double best_ms = 1e300;
+    AcChoice best_c = cur;
     g2p_solver *best = nullptr;
-    for (double cs : cands) {
+    for (const AcChoice &c : cands) {
         g2p_solver *S = nullptr;
-        if (cs == pc.strength) {
+        if (!(c != cur)) {
             S = *Sc;
         } else {
             g2p_solver_params q = pc;
-            q.strength = cs;
+            q.strength = c.strength;
+            q.precision = c.precision;
             if (g2p_solver_build(m->Ac, &q, s, &S) != G2P_OK) { cudaGetLastError(); continue; }
         }
         g2p_solve_stats ss;
@@ -297,10 +313,14 @@ static g2p_status tune_ac(g2p_mesh *m, const TuneKey &key, const g2p_solver_para
             rc = g2p_solver_solve_dev(S, Bc, Yc, kk, &ss);
             ms = std::min(ms, ms_since(t));
         }
+        if (getenv("G2P_DEBUG"))
+            fprintf(stderr, "[g2p tune] Ac strength %.3g precision %d: %.3f ms%s\n", c.strength, c.precision, ms,
+                    rc == G2P_OK ? "" : " (not converged)");
         if (rc == G2P_OK && ms < best_ms) {
             if (best && best != *Sc) g2p_solver_destroy(best);
-            best = S; best_ms = ms; best_st = cs;
+            best = S; best_ms = ms; best_c = c;
         } else if (S != *Sc) {
+            cudaGetLastError();
             g2p_solver_destroy(S);
         }
     }
@@ -308,16 +328,17 @@ static g2p_status tune_ac(g2p_mesh *m, const TuneKey &key, const g2p_solver_para
         g2p_solver_destroy(*Sc);
         *Sc = best;
     }
-    double kept = best ? best_st : pc.strength;
+    AcChoice kept = best ? best_c : cur;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         kept = g_ac_tuned.emplace(key, kept).first->second;   // an earlier entry wins
     }
-    if (best && kept != best_st) {
+    if (best && kept != best_c) {
         // another job of this shape recorded its choice first: follow it, so
         // every job of the shape runs the same way
         g2p_solver_params q = pc;
-        q.strength = kept;
+        q.strength = kept.strength;
+        q.precision = kept.precision;
         g2p_solver *S = nullptr;
         G2P_TRY(g2p_solver_build(m->Ac, &q, s, &S));
         g2p_solver_destroy(*Sc);
@@ -428,27 +449,31 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     t0 = std::chrono::steady_clock::now();
     g2p_solver *Sd = nullptr, *Sc = nullptr;
     // Ac first: its setup overlaps Ad's ordered sums on the side stream.
-    // Ac, the conductor Laplacian, keeps its Krylov iteration in FP64: a
-    // floating wire grounded at one node gives it a condition number near
-    // (length/h)^2, beyond what an FP32 refinement sweep resolves.  In the
-    // mixed method its V-cycle preconditioner runs in FP32.
+    // Ac, the conductor Laplacian, keeps its Krylov iteration in FP64 by
+    // default: a floating wire grounded at one node gives it a condition
+    // number near (length/h)^2, beyond what an FP32 refinement sweep
+    // resolves.  In the mixed method its V-cycle preconditioner runs in
+    // FP32; with autotune the first job of a grid shape also times Ac in the
+    // mixed method's FP32 refinement and keeps it where that is faster.
     // G2P_AC_PRECISION overrides the mode (comparisons).
     g2p_solver_params pc = p;
     const double st0 = p.strength > 0 ? p.strength : 0.04;
     const TuneKey ac_key{m->d.nx, m->d.ny, m->d.nz, m->Ac.nnz, P, p.precision};
     const bool ac_fixed = getenv("G2P_AC_STRENGTH") != nullptr;
-    double ac_st = 0;
-    const bool ac_known = ac_tuned(ac_key, &ac_st);
+    AcChoice ac_c{0.0, 0};
+    const bool ac_known = ac_tuned(ac_key, &ac_c);
+    const bool ac_prec_fixed = getenv("G2P_AC_PRECISION") != nullptr;
     {
         if (p.precision == G2P_PREC_MIXED) pc.precision = G2P_PREC_FP64_PC32;
-        if (const char *e = getenv("G2P_AC_PRECISION")) pc.precision = atoi(e);
+        if (ac_prec_fixed) pc.precision = atoi(getenv("G2P_AC_PRECISION"));
+        else if (ac_known) pc.precision = ac_c.precision;
         // Ac's aggregation wants a stronger threshold than Ad's: twice Ad's,
         // at most 0.1 (c2 sweep: 0.04 -> 37 iterations, 0.08 -> 33, >= 0.15
         // stalls).  G2P_AC_STRENGTH / G2P_AC_DEGREE / G2P_AC_RESTART
         // override (comparisons).
         pc.strength = std::min(2 * st0, 0.1);
         if (ac_fixed) pc.strength = atof(getenv("G2P_AC_STRENGTH"));
-        else if (ac_known) pc.strength = ac_st;
+        else if (ac_known) pc.strength = ac_c.strength;
         if (const char *t = getenv("G2P_AC_DEGREE")) pc.smoother_degree = atoi(t);
         if (const char *t = getenv("G2P_AC_RESTART")) pc.restart = atoi(t);
     }
@@ -509,6 +534,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     local.ad_levels = Sd->levels;
     local.ac_levels = Sc->levels;
     local.ac_strength = pc.strength;
+    local.ac_precision = pc.precision;
     LongRows lcol;   // long columns of V0d (conductor columns)
     {
         Csr<double> tmp;
@@ -571,14 +597,21 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         (g2p::kbegin("k_add", s), k_add<<<grid_for(nc * kk), kThreads, 0, s>>>(nc * kk, Bc, crhs), g2p::kend(s));
         // (4) Ac y0c = b_c
         if (p0 == 0 && p.autotune && !ac_fixed && !ac_known) {
-            G2P_TRY(tune_ac(m, ac_key, pc, st0, &Sc, Bc, Yc, kk, s));
-            double tuned = 0;
-            if (ac_tuned(ac_key, &tuned)) local.ac_strength = tuned;
+            std::vector<int> modes = {pc.precision};
+            if (p.precision == G2P_PREC_MIXED && !ac_prec_fixed && pc.precision != G2P_PREC_MIXED)
+                modes.push_back(G2P_PREC_MIXED);
+            G2P_TRY(tune_ac(m, ac_key, pc, st0, modes, &Sc, Bc, Yc, kk, s));
+            AcChoice tuned{0.0, 0};
+            if (ac_tuned(ac_key, &tuned)) {
+                local.ac_strength = tuned.strength;
+                local.ac_precision = tuned.precision;
+            }
             local.ac_levels = Sc->levels;
         }
         rc = g2p_solver_solve_dev(Sc, Bc, Yc, kk, &ss);
         if (rc != G2P_OK && rc != G2P_ERR_NOT_CONVERGED) { worst_rc = rc; break; }
         if (rc == G2P_ERR_NOT_CONVERGED) worst_rc = rc;
+        local.ac_iterations += ss.iterations;
         local.solves += kk; local.total_iterations += ss.iterations;
         local.max_rel_residual = std::max(local.max_rel_residual, ss.rel_residual);
         // (5) yc = V0c y0c ; b_d2 = V0da^T(-D_eps yc)

@@ -130,6 +130,8 @@ typedef struct {
     int32_t ad_levels, ac_levels;
     int32_t rhs_block, ad_degree;    /* ports per block solve and Ad's Chebyshev degree used */
     double ac_strength;              /* aggregation strength threshold of Ac's AMG */
+    int32_t ac_precision;            /* Ac's solver mode (G2P_PREC_*; tuned with autotune) */
+    int32_t ac_iterations;           /* iterations of the Ac solves */
 } g2p_extract_stats;
 
 /* ---- library ---- */

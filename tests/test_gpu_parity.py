@@ -117,9 +117,9 @@ def test_gpu_graph_replay_gives_identical_z(name, precision, g2p):
 
 
 def test_gpu_autotune_picks_a_candidate_and_keeps_it(g2p):
-    """The autotuner's block width, degree and Ac strength come from its
-    candidate sets, are kept for later jobs of the same shape, and give Z
-    within the solve tolerance of the untuned run."""
+    """The autotuner's block width, degree, Ac strength and Ac precision mode
+    come from its candidate sets, are kept for later jobs of the same shape,
+    and give Z within the solve tolerance of the untuned run."""
     from gds2para_gb300 import layout as lay
     d = lay.build(lay.multistrip(nx=40, ny=64, nz=8, n_strips=16, freq_start=1e8, freq_end=1e10, nfreq=3))
     res = []
@@ -127,9 +127,10 @@ def test_gpu_autotune_picks_a_candidate_and_keeps_it(g2p):
         with g2p.FdtdMesh(d) as m:
             g2p.generateStiff(m)
             Z, st = g2p.paraGenerator(m, g2p.default_params(precision="mixed", rtol=1e-10, autotune=tune))
-        res.append((Z, st.rhs_block, st.ad_degree, st.ac_strength))
-    assert res[0][1] == 16 and res[0][2] == 2 and res[0][3] == 0.08
+        res.append((Z, st.rhs_block, st.ad_degree, st.ac_strength, st.ac_precision))
+    assert res[0][1] == 16 and res[0][2] == 2 and res[0][3] == 0.08 and res[0][4] == 2
     assert res[1][1] in (16, 8) and res[1][2] in (2, 3, 4) and res[1][3] in (0.02, 0.04, 0.08)
+    assert res[1][4] in (1, 2)        # mixed refinement or FP64 Krylov with the FP32 V-cycle
     assert res[2][1:] == res[1][1:]
     assert np.array_equal(res[1][0], res[2][0])
     err = np.abs(res[1][0] - res[0][0]).max() / np.abs(res[0][0]).max()
