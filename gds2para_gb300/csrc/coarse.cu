@@ -11,10 +11,19 @@
 // smoothing, smoothed prolongation); the two Chebyshev iterates ping-pong
 // between a level's x and t0 vectors, so a step needs one barrier.
 //
-// The barrier is an arrival counter with a bounded spin.  A block that waits
-// too long sets an abandon flag and returns, and every other block returns at
-// its next barrier; the flag is sticky, and the solver, which checks it once
-// per solve, then repeats that solve with the launch-per-kernel V-cycle.
+// Two launch forms (G2P_FUSE=1 or 2):
+// * grid: a cooperative launch over every SM, levels of up to kFuseRows
+//   rows.  The barrier is an arrival counter with a bounded spin.  A block
+//   that waits too long sets an abandon flag and returns, and every other
+//   block returns at its next barrier; the flag is sticky, and the solver,
+//   which checks it once per solve, then repeats that solve with the
+//   launch-per-kernel V-cycle.
+// * cluster: one thread-block cluster (16 CTAs where the part allows it,
+//   else 8), levels of up to kClusterRows rows.  The barrier is the
+//   hardware cluster barrier (barrier.cluster arrive.release /
+//   wait.acquire): the cluster's CTAs are co-scheduled, so it needs no spin
+//   and cannot give up, and it costs a fraction of a grid-wide barrier over
+//   two dies.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -31,6 +40,7 @@ constexpr int kFuseThreads = 512;
 constexpr int kFuseLongRow = 64;       // longer rows take a warp
 constexpr int kFuseSpin = 1 << 22;     // polls of >= 32 ns before a block gives up
 constexpr int kFuseTraceLen = 512;     // phase time stamps kept by G2P_FUSE_TRACE
+constexpr int64_t kClusterRows = 16384; // largest level of the cluster form (G2P_FUSE_ROWS overrides)
 
 template <class T>
 struct FuseLevel {
@@ -98,6 +108,19 @@ __device__ __forceinline__ bool grid_sync(unsigned *bar, unsigned &phase, int sp
     }
     __syncthreads();
     return quit == 0;
+}
+
+// Barrier of every thread of the cluster (the whole grid in the cluster
+// form), with the memory ordering of a release/acquire pair at cluster scope.
+__device__ __forceinline__ bool cluster_sync(unsigned &phase, unsigned long long *trace) {
+    if (trace && blockIdx.x == 0 && threadIdx.x == 0 && phase < kFuseTraceLen) {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        trace[phase] = t;
+    }
+    ++phase;
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+    return true;
 }
 
 template <class T>
@@ -225,7 +248,7 @@ __device__ void spmm_phase_long(int kind, const FuseLevel<T> &L, int it, const T
     }
 }
 
-template <class T, int KG>
+template <class T, int KG, bool CL>
 __global__ void __launch_bounds__(kFuseThreads, 1) k_coarse_cycle(const FuseLevel<T> *__restrict__ lv, int nlev,
                                                                const double *__restrict__ cinv, int k, unsigned *bar,
                                                                int spin_limit, unsigned long long *trace) {
@@ -237,7 +260,10 @@ __global__ void __launch_bounds__(kFuseThreads, 1) k_coarse_cycle(const FuseLeve
     const int64_t warp = tid >> 5, nwarps = nthreads >> 5;
     unsigned phase = 0;
     T *cur[kFuseMaxLevels];
-    auto sync = [&]() { return grid_sync(bar, phase, spin_limit, trace); };
+    auto sync = [&]() {
+        if constexpr (CL) return cluster_sync(phase, trace);
+        else return grid_sync(bar, phase, spin_limit, trace);
+    };
     // a whole SpMM phase: rows, mid rows and chunks; then the chunked rows
     // after a barrier when the level has any
     auto spmm = [&](int kind, const FuseLevel<T> &L, int it, const T *X, T *Y) {
@@ -369,16 +395,27 @@ void cheb_coefficients(FuseLevel<T> &f, double lmax_est, int deg, double ratio, 
 template <class T>
 using CoarseKernel = void (*)(const FuseLevel<T> *, int, const double *, int, unsigned *, int, unsigned long long *);
 
-template <class T>
-CoarseKernel<T> coarse_kernel(int kg) {
+template <class T, bool CL>
+CoarseKernel<T> coarse_kernel_of(int kg) {
     switch (kg) {
-        case 1: return k_coarse_cycle<T, 1>;
-        case 2: return k_coarse_cycle<T, 2>;
-        case 4: return k_coarse_cycle<T, 4>;
-        case 8: return k_coarse_cycle<T, 8>;
-        case 16: return k_coarse_cycle<T, 16>;
-        default: return k_coarse_cycle<T, 32>;
+        case 1: return k_coarse_cycle<T, 1, CL>;
+        case 2: return k_coarse_cycle<T, 2, CL>;
+        case 4: return k_coarse_cycle<T, 4, CL>;
+        case 8: return k_coarse_cycle<T, 8, CL>;
+        case 16: return k_coarse_cycle<T, 16, CL>;
+        default: return k_coarse_cycle<T, 32, CL>;
     }
+}
+template <class T>
+CoarseKernel<T> coarse_kernel(int kg, bool cluster) {
+    return cluster ? coarse_kernel_of<T, true>(kg) : coarse_kernel_of<T, false>(kg);
+}
+
+// G2P_FUSE: 0 or unset = off, 1 = grid form, 2 = cluster form
+int fuse_mode() {
+    const char *e = getenv("G2P_FUSE");
+    const int m = e ? atoi(e) : 0;
+    return m == 1 || m == 2 ? m : 0;
 }
 
 }  // namespace
@@ -388,14 +425,15 @@ CoarseKernel<T> coarse_kernel(int kg) {
 template <class T>
 int coarse_fuse_level(const Hierarchy<T> &H, int k) {
     if (k < 1 || k > 32 || H.lv.size() < 3) return -1;
-    // opt-in (G2P_FUSE=1): measured slower than the launch-per-kernel cycle
-    // replayed from CUDA graphs on the workloads here
-    const char *e = getenv("G2P_FUSE");
-    if (!e || atoi(e) == 0) return -1;
-    if (H.fuse_off) return -1;
+    // opt-in (G2P_FUSE=1 or 2): the grid form measured slower than the
+    // launch-per-kernel cycle replayed from CUDA graphs on the workloads here
+    const int mode = fuse_mode();
+    if (mode == 0 || H.fuse_off) return -1;
+    int64_t rows = mode == 2 ? kClusterRows : kFuseRows;
+    if (const char *r = getenv("G2P_FUSE_ROWS")) rows = std::max<int64_t>(1, atoll(r));
     const int nlev = (int)H.lv.size();
     for (int l = 1; l < nlev - 1; l++)
-        if (H.lv[l].n <= kFuseRows) return nlev - l <= kFuseMaxLevels ? l : -1;
+        if (H.lv[l].n <= rows) return nlev - l <= kFuseMaxLevels ? l : -1;
     return -1;
 }
 
@@ -404,8 +442,9 @@ g2p_status coarse_prepare(Hierarchy<T> &H, const SolverConfig &cfg, int k, cudaS
     const int lc = coarse_fuse_level(H, k);
     H.fuse_from = -1;
     if (lc < 0) return G2P_OK;
+    const int mode = fuse_mode();
     const std::vector<double> key = {(double)k, (double)H.kcap, (double)cfg.degree, cfg.cheb_ratio, cfg.cheb_upper,
-                                     (double)lc};
+                                     (double)lc, (double)mode};
     if (H.fuse_tab && H.fuse_key == key) {
         H.fuse_from = lc;
         return G2P_OK;
@@ -455,13 +494,48 @@ g2p_status coarse_prepare(Hierarchy<T> &H, const SolverConfig &cfg, int k, cudaS
                     l == nlev - 1 ? (H.cinv ? " (dense inverse)" : " (smoothed)") : "");
     G2P_CUDA(cudaMemcpyAsync(H.fuse_tab, tab.data(), sizeof(FuseLevel<T>) * tab.size(), cudaMemcpyHostToDevice, s));
     G2P_CUDA(cudaStreamSynchronize(s));
-    int dev = 0, per_sm = 0;
-    G2P_CUDA(cudaGetDevice(&dev));
-    G2P_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coarse_kernel<T>(pow2_ge(k)), kFuseThreads, 0));
-    int nsm = kSMs;
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    H.fuse_blocks = std::min(per_sm, 1) * nsm;
-    if (H.fuse_blocks < 1) return G2P_OK;
+    if (mode == 2) {
+        // the largest cluster of these blocks that the part can place: 16
+        // (non-portable) or 8
+        const CoarseKernel<T> kfn = coarse_kernel<T>(pow2_ge(k), true);
+        H.fuse_cluster = 0;
+        for (int c : {16, 8}) {
+            if (c > 8 && cudaFuncSetAttribute((const void *)kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                             cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            cudaLaunchConfig_t lc_cfg = {};
+            lc_cfg.gridDim = dim3((unsigned)c);
+            lc_cfg.blockDim = dim3(kFuseThreads);
+            cudaLaunchAttribute at;
+            at.id = cudaLaunchAttributeClusterDimension;
+            at.val.clusterDim.x = (unsigned)c;
+            at.val.clusterDim.y = 1;
+            at.val.clusterDim.z = 1;
+            lc_cfg.attrs = &at;
+            lc_cfg.numAttrs = 1;
+            int nclusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&nclusters, (const void *)kfn, &lc_cfg) == cudaSuccess &&
+                nclusters > 0) {
+                H.fuse_cluster = c;
+                break;
+            }
+            cudaGetLastError();
+        }
+        if (H.fuse_cluster == 0) return G2P_OK;
+        H.fuse_blocks = H.fuse_cluster;
+    } else {
+        int dev = 0, per_sm = 0;
+        G2P_CUDA(cudaGetDevice(&dev));
+        G2P_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coarse_kernel<T>(pow2_ge(k), false),
+                                                               kFuseThreads, 0));
+        int nsm = kSMs;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        H.fuse_blocks = std::min(per_sm, 1) * nsm;
+        H.fuse_cluster = 0;
+        if (H.fuse_blocks < 1) return G2P_OK;
+    }
     H.fuse_key = key;
     H.fuse_from = lc;
     return G2P_OK;
@@ -485,12 +559,20 @@ void coarse_cycle(Hierarchy<T> &H, int k, cudaStream_t s) {
     cfg.blockDim = dim3(kFuseThreads);
     cfg.stream = s;
     cudaLaunchAttribute attr;
-    attr.id = cudaLaunchAttributeCooperative;
-    attr.val.cooperative = 1;
+    const bool cluster = H.fuse_cluster > 0;
+    if (cluster) {
+        attr.id = cudaLaunchAttributeClusterDimension;
+        attr.val.clusterDim.x = (unsigned)H.fuse_cluster;
+        attr.val.clusterDim.y = 1;
+        attr.val.clusterDim.z = 1;
+    } else {
+        attr.id = cudaLaunchAttributeCooperative;
+        attr.val.cooperative = 1;
+    }
     cfg.attrs = &attr;
     cfg.numAttrs = 1;
-    g2p::kbegin("k_coarse_cycle", s);
-    if (cudaLaunchKernelExC(&cfg, (const void *)coarse_kernel<T>(pow2_ge(k)), args) != cudaSuccess) {
+    g2p::kbegin(cluster ? "k_coarse_cycle<cluster>" : "k_coarse_cycle", s);
+    if (cudaLaunchKernelExC(&cfg, (const void *)coarse_kernel<T>(pow2_ge(k), cluster), args) != cudaSuccess) {
         cudaGetLastError();
         H.fuse_failed = true;    // reported as a give-up: the solve is repeated unfused
     }

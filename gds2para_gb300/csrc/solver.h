@@ -82,6 +82,7 @@ struct Hierarchy {
     unsigned *fuse_bar = nullptr;
     unsigned long long *fuse_trace = nullptr;   // G2P_FUSE_TRACE time stamps
     int fuse_blocks = 0;
+    int fuse_cluster = 0;       // cluster form: CTAs of the one cluster (grid = cluster)
     bool fuse_off = false;
     bool fuse_failed = false;   // a fused launch could not be issued
     std::vector<double> fuse_key;

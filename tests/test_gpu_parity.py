@@ -234,17 +234,19 @@ def _extract(g2p, d, precision):
     return Z, st, L.g2p_launch_count() - n0
 
 
+@pytest.mark.parametrize("mode", ["1", "2"])
 @pytest.mark.parametrize("name,precision", [("strip_c1", "mixed"), ("manhattan_sweep", "fp64"),
                                             ("multistrip_small", "mixed")])
-def test_gpu_fused_coarse_cycle_matches_launch_per_kernel(name, precision, g2p, monkeypatch):
-    """The coarse tail of the V-cycle in one cooperative launch (k_coarse_cycle,
-    G2P_FUSE=1) against the same levels launched kernel by kernel: the same
-    arithmetic up to summation order, so Z agrees to the solves' tolerance,
-    with far fewer launches."""
+def test_gpu_fused_coarse_cycle_matches_launch_per_kernel(name, precision, mode, g2p, monkeypatch):
+    """The coarse tail of the V-cycle in one launch (k_coarse_cycle: G2P_FUSE=1
+    cooperative over the grid, G2P_FUSE=2 one thread-block cluster with the
+    hardware cluster barrier) against the same levels launched kernel by
+    kernel: the same arithmetic up to summation order, so Z agrees to the
+    solves' tolerance, with far fewer launches."""
     d, A, M = golden_layout(name)
     monkeypatch.setenv("G2P_FUSE", "0")
     Z0, st0, n0 = _extract(g2p, d, precision)
-    monkeypatch.setenv("G2P_FUSE", "1")
+    monkeypatch.setenv("G2P_FUSE", mode)
     Z1, st1, n1 = _extract(g2p, d, precision)
     monkeypatch.delenv("G2P_FUSE")
     assert np.abs(Z1 - Z0).max() / np.abs(Z0).max() < 1e-8
