@@ -991,7 +991,10 @@ __global__ void __launch_bounds__(256) k_maxpy_v(int64_t nq, int cpr, int k, int
 }
 
 // Chebyshev: d = theta^-1 D^-1 b, x = d (or x += d)
-template <class T>
+// Chebyshev first step: d = D^-1 b / theta, x = d (or x += d with add).
+// STX / STD: whether x and d are stored (a zero-guess smoother of degree >= 2
+// keeps its first iterate in d only; a last step's d is never read).
+template <class T, bool STX, bool STD>
 __global__ void __launch_bounds__(256) k_cheb_first_v(int64_t nq, int shift, const T *dinv, const T *b, T *x, T *d,
                                                       double inv_theta, bool add) {
     constexpr int C = Chunk<T>::C;
@@ -1001,21 +1004,23 @@ __global__ void __launch_bounds__(256) k_cheb_first_v(int64_t nq, int shift, con
         bb.ld(b + q * C);
 #pragma unroll
         for (int u = 0; u < C; u++) dd.v[u] = di * bb.v[u];
-        dd.st(d + q * C);
+        if (STD) dd.st(d + q * C);
         if (add) {
             Chunk<T> xx;
             xx.ldc(x + q * C);
 #pragma unroll
             for (int u = 0; u < C; u++) xx.v[u] += dd.v[u];
             xx.st(x + q * C);
-        } else {
+        } else if (STX) {
             dd.st(x + q * C);
         }
     }
 }
 
-// Chebyshev: d = c1 d + c2 D^-1 res ; x += d
-template <class T>
+// Chebyshev: d = c1 d + c2 D^-1 res ; x += d.  XD: the iterate is d itself
+// (the step after a zero-guess first step that stored d only), so x is
+// written but not read; STD: whether d is stored.
+template <class T, bool XD, bool STD>
 __global__ void __launch_bounds__(256) k_cheb_step_v(int64_t nq, int shift, const T *dinv, const T *res, T *x, T *d,
                                                      double c1, double c2) {
     constexpr int C = Chunk<T>::C;
@@ -1025,14 +1030,15 @@ __global__ void __launch_bounds__(256) k_cheb_step_v(int64_t nq, int shift, cons
         Chunk<T> rr, dd, xx;
         rr.ld(res + q * C);
         dd.ldc(d + q * C);
-        xx.ldc(x + q * C);
+        if (XD) xx = dd;
+        else xx.ldc(x + q * C);
 #pragma unroll
         for (int u = 0; u < C; u++) {
             const T t = a * dd.v[u] + di * rr.v[u];
             dd.v[u] = t;
             xx.v[u] += t;
         }
-        dd.st(d + q * C);
+        if (STD) dd.st(d + q * C);
         xx.st(x + q * C);
     }
 }
@@ -1308,21 +1314,48 @@ static void chebyshev(Level<T> &L, int deg, double ratio, double upper, const T 
     const int cpr = chunk_cpr<T>(k);
     const int64_t nq = L.n * cpr;
     const int shift = cpr ? __builtin_ctz(cpr) : 0;
-    auto first = [&](const T *src, bool add) {
-        if (cpr) (g2p::kbegin("k_cheb_first", s), k_cheb_first_v<T><<<chunk_grid(nq), 256, 0, s>>>(nq, shift, L.dinv, src, x, L.d, 1.0 / theta, add), g2p::kend(s));
-        else (g2p::kbegin("k_cheb_first", s), k_cheb_first<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, src, x, L.d, 1.0 / theta, add), g2p::kend(s));
+    // the chunked kernels store only what later steps read: a zero-guess
+    // first step of a smoother of degree >= 2 leaves its iterate in d alone
+    // (x == d there), and the last step does not store d (the next smoother
+    // call starts it afresh); the arithmetic is unchanged
+    auto first = [&](const T *src, bool add, bool stx, bool std_) {
+        const double it_ = 1.0 / theta;
+        if (cpr) {
+            g2p::kbegin("k_cheb_first", s);
+            const unsigned cg = chunk_grid(nq);
+            if (stx && std_) k_cheb_first_v<T, true, true><<<cg, 256, 0, s>>>(nq, shift, L.dinv, src, x, L.d, it_, add);
+            else if (stx) k_cheb_first_v<T, true, false><<<cg, 256, 0, s>>>(nq, shift, L.dinv, src, x, L.d, it_, add);
+            else k_cheb_first_v<T, false, true><<<cg, 256, 0, s>>>(nq, shift, L.dinv, src, x, L.d, it_, add);
+            g2p::kend(s);
+        } else {
+            (g2p::kbegin("k_cheb_first", s), k_cheb_first<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, src, x, L.d, it_, add), g2p::kend(s));
+        }
     };
+    bool x_in_d = false;
     if (zero_guess) {
-        first(b, false);
+        x_in_d = cpr && deg >= 2;
+        first(b, false, !x_in_d, deg >= 2);
     } else {
         spmm_b<T>(L.A, L.lr, x, L.t0, k, b, s);
-        first(L.t0, true);
+        first(L.t0, true, true, deg >= 2);
     }
     for (int it = 1; it < deg; it++) {
-        spmm_b<T>(L.A, L.lr, x, L.t0, k, b, s);
+        spmm_b<T>(L.A, L.lr, x_in_d ? L.d : x, L.t0, k, b, s);
         double rn = 1.0 / (2.0 * sigma - rho);
-        if (cpr) (g2p::kbegin("k_cheb_step", s), k_cheb_step_v<T><<<chunk_grid(nq), 256, 0, s>>>(nq, shift, L.dinv, L.t0, x, L.d, rn * rho, 2.0 * rn / delta), g2p::kend(s));
-        else (g2p::kbegin("k_cheb_step", s), k_cheb_step<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, L.t0, x, L.d, rn * rho, 2.0 * rn / delta), g2p::kend(s));
+        const double c1 = rn * rho, c2 = 2.0 * rn / delta;
+        const bool last = it == deg - 1;
+        if (cpr) {
+            g2p::kbegin("k_cheb_step", s);
+            const unsigned cg = chunk_grid(nq);
+            if (x_in_d && last) k_cheb_step_v<T, true, false><<<cg, 256, 0, s>>>(nq, shift, L.dinv, L.t0, x, L.d, c1, c2);
+            else if (x_in_d) k_cheb_step_v<T, true, true><<<cg, 256, 0, s>>>(nq, shift, L.dinv, L.t0, x, L.d, c1, c2);
+            else if (last) k_cheb_step_v<T, false, false><<<cg, 256, 0, s>>>(nq, shift, L.dinv, L.t0, x, L.d, c1, c2);
+            else k_cheb_step_v<T, false, true><<<cg, 256, 0, s>>>(nq, shift, L.dinv, L.t0, x, L.d, c1, c2);
+            g2p::kend(s);
+        } else {
+            (g2p::kbegin("k_cheb_step", s), k_cheb_step<T><<<g, blk, 0, s>>>(L.n, k, L.dinv, L.t0, x, L.d, c1, c2), g2p::kend(s));
+        }
+        x_in_d = false;
         rho = rn;
     }
 }
