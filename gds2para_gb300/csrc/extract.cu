@@ -264,7 +264,10 @@ static std::map<TuneKey, std::pair<int, int>> g_tuned;   // -> (block width, deg
 struct AcChoice {
     double strength;
     int precision;
-    bool operator!=(const AcChoice &o) const { return strength != o.strength || precision != o.precision; }
+    int restart;
+    bool operator!=(const AcChoice &o) const {
+        return strength != o.strength || precision != o.precision || restart != o.restart;
+    }
 };
 static std::map<TuneKey, AcChoice> g_ac_tuned;
 
@@ -278,20 +281,23 @@ static bool ac_tuned(const TuneKey &key, AcChoice *c) {
 
 // Times Ac's solve of the first block with the strength thresholds st0 / 2,
 // st0 and 2 st0 (at most 0.1), st0 being Ad's, and, when modes lists more
-// than one precision mode, with each of them; *Sc (built with pc) is one of
-// the candidates.  Each candidate: one untimed solve, then the better of two
+// than one precision mode, with each of them (and, for FP64 Krylov with the
+// FP32 V-cycle, with each restart length in restarts: its Gram-Schmidt is
+// bound by the FP64 pipe, so a shorter restart pays where the iteration
+// count does not grow much); *Sc (built with pc) is one of the candidates.  Each candidate: one untimed solve, then the better of two
 // timed ones.  *Sc is replaced by the solver of the recorded choice: the
 // fastest candidate, unless another job of the shape recorded its choice
 // first.  (Ac in the mixed mode's FP32 refinement is faster where its sweeps
 // converge, e.g. c3's 256 x 256 x 16 layout, and stalls into the FP64
 // fallback where they do not, e.g. c2's; only timing tells them apart.)
 static g2p_status tune_ac(g2p_mesh *m, const TuneKey &key, const g2p_solver_params &pc, double st0,
-                          const std::vector<int> &modes, g2p_solver **Sc, const double *Bc, double *Yc, int kk,
-                          cudaStream_t s) {
+                          const std::vector<int> &modes, const std::vector<int> &restarts, g2p_solver **Sc,
+                          const double *Bc, double *Yc, int kk, cudaStream_t s) {
     std::vector<AcChoice> cands;
     for (int mode : modes)
-        for (double st : {st0 / 2, st0, std::min(2 * st0, 0.1)}) cands.push_back({st, mode});
-    const AcChoice cur{pc.strength, pc.precision};
+        for (int rs : mode == G2P_PREC_FP64_PC32 ? restarts : std::vector<int>{pc.restart})
+            for (double st : {st0 / 2, st0, std::min(2 * st0, 0.1)}) cands.push_back({st, mode, rs});
+    const AcChoice cur{pc.strength, pc.precision, pc.restart};
     double best_ms = 1e300;
     AcChoice best_c = cur;
     g2p_solver *best = nullptr;
@@ -303,6 +309,7 @@ static g2p_status tune_ac(g2p_mesh *m, const TuneKey &key, const g2p_solver_para
             g2p_solver_params q = pc;
             q.strength = c.strength;
             q.precision = c.precision;
+            q.restart = c.restart;
             if (g2p_solver_build(m->Ac, &q, s, &S) != G2P_OK) { cudaGetLastError(); continue; }
         }
         g2p_solve_stats ss;
@@ -314,8 +321,8 @@ static g2p_status tune_ac(g2p_mesh *m, const TuneKey &key, const g2p_solver_para
             ms = std::min(ms, ms_since(t));
         }
         if (getenv("G2P_DEBUG"))
-            fprintf(stderr, "[g2p tune] Ac strength %.3g precision %d: %.3f ms%s\n", c.strength, c.precision, ms,
-                    rc == G2P_OK ? "" : " (not converged)");
+            fprintf(stderr, "[g2p tune] Ac strength %.3g precision %d restart %d: %.3f ms%s\n", c.strength, c.precision,
+                    c.restart, ms, rc == G2P_OK ? "" : " (not converged)");
         if (rc == G2P_OK && ms < best_ms) {
             if (best && best != *Sc) g2p_solver_destroy(best);
             best = S; best_ms = ms; best_c = c;
@@ -339,6 +346,7 @@ static g2p_status tune_ac(g2p_mesh *m, const TuneKey &key, const g2p_solver_para
         g2p_solver_params q = pc;
         q.strength = kept.strength;
         q.precision = kept.precision;
+        q.restart = kept.restart;
         g2p_solver *S = nullptr;
         G2P_TRY(g2p_solver_build(m->Ac, &q, s, &S));
         g2p_solver_destroy(*Sc);
@@ -460,7 +468,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
     const double st0 = p.strength > 0 ? p.strength : 0.04;
     const TuneKey ac_key{m->d.nx, m->d.ny, m->d.nz, m->Ac.nnz, P, p.precision};
     const bool ac_fixed = getenv("G2P_AC_STRENGTH") != nullptr;
-    AcChoice ac_c{0.0, 0};
+    AcChoice ac_c{0.0, 0, 0};
     const bool ac_known = ac_tuned(ac_key, &ac_c);
     const bool ac_prec_fixed = getenv("G2P_AC_PRECISION") != nullptr;
     {
@@ -476,6 +484,7 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
         else if (ac_known) pc.strength = ac_c.strength;
         if (const char *t = getenv("G2P_AC_DEGREE")) pc.smoother_degree = atoi(t);
         if (const char *t = getenv("G2P_AC_RESTART")) pc.restart = atoi(t);
+        else if (ac_known) pc.restart = ac_c.restart;
     }
     // Ac's solver is built by a second host thread on its own stream (after
     // Ac's assembly, an event on the job's stream) while this thread
@@ -600,8 +609,10 @@ extern "C" g2p_status g2p_para_generator(g2p_mesh *m, const g2p_solver_params *p
             std::vector<int> modes = {pc.precision};
             if (p.precision == G2P_PREC_MIXED && !ac_prec_fixed && pc.precision != G2P_PREC_MIXED)
                 modes.push_back(G2P_PREC_MIXED);
-            G2P_TRY(tune_ac(m, ac_key, pc, st0, modes, &Sc, Bc, Yc, kk, s));
-            AcChoice tuned{0.0, 0};
+            std::vector<int> restarts = {pc.restart};
+            if (!getenv("G2P_AC_RESTART") && pc.restart > 10) restarts.push_back(10);
+            G2P_TRY(tune_ac(m, ac_key, pc, st0, modes, restarts, &Sc, Bc, Yc, kk, s));
+            AcChoice tuned{0.0, 0, 0};
             if (ac_tuned(ac_key, &tuned)) {
                 local.ac_strength = tuned.strength;
                 local.ac_precision = tuned.precision;
