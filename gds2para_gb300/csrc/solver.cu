@@ -649,9 +649,72 @@ static void launch_sell(const Csr<T> &A, const T *x, T *y, int k, const T *b, cu
     }
 }
 
+// A side stream per launching stream (and host thread) for the long-row
+// kernels of coarse operators, with the fork and join events.
+struct SideStream {
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    bool ok = false;
+};
+static SideStream *side_stream_of(cudaStream_t s) {
+    thread_local std::vector<std::pair<cudaStream_t, SideStream>> tab;
+    for (auto &e : tab)
+        if (e.first == s) return e.second.ok ? &e.second : nullptr;
+    if (tab.size() >= 64) return nullptr;      // many launching streams: keep their long rows in line
+    SideStream ss;
+    ss.ok = cudaStreamCreateWithFlags(&ss.side, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming) == cudaSuccess;
+    if (!ss.ok) cudaGetLastError();
+    tab.emplace_back(s, ss);
+    return ss.ok ? &tab.back().second : nullptr;
+}
+
+// G2P_LONG_FORK=0 keeps the long-row kernels behind the short-row kernel on
+// the launching stream (comparison).
+static bool long_fork_on() {
+    static const bool on = [] {
+        const char *e = getenv("G2P_LONG_FORK");
+        return e ? atoi(e) != 0 : true;
+    }();
+    return on;
+}
+
 template <class T>
 void spmm_b(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, const T *b, cudaStream_t s) {
     bool prof = g_prof.on && g_prof.used + 2 <= (size_t)1 << 20;
+    // coarse operators with long rows (conductor potentials): the long-row
+    // kernels run on a side stream beside the short-row kernel and join
+    // before the next launch.  Only with the sliced-ELL short-row kernels,
+    // which leave the long rows of y alone (the uniform-width kernels write
+    // every row and rely on the long-row kernels coming after them); not on
+    // operators of 1M rows or more, whose persistent kernel wants every SM;
+    // not while kernels are being timed one by one.
+    SideStream *fork = nullptr;
+    if ((lr.nmid > 0 || lr.nchunk > 0) && A.sptr != nullptr && A.ell_w == 0 && A.n < (1 << 20) && !prof &&
+        !kprof_on() && long_fork_on())
+        fork = side_stream_of(s);
+    cudaStream_t sl = s;
+    if (fork) {
+        if (cudaEventRecord(fork->fork, s) == cudaSuccess && cudaStreamWaitEvent(fork->side, fork->fork, 0) == cudaSuccess) {
+            sl = fork->side;
+        } else {
+            cudaGetLastError();
+            fork = nullptr;
+        }
+    }
+    if (fork) {
+        dim3 lblk = row_block(k);
+        if (lr.nmid > 0) {
+            const int kx = k >= 32 ? 32 : pow2_ge(k);
+            (g2p::kbegin(spmm_name(3, sizeof(T) == 8, A.n), sl),
+             k_spmm_mid<T><<<(unsigned)lr.nmid, 256, 0, sl>>>(lr.nmid, lr.mid, A.ptr, A.col, A.val, x, k, kx, y, b), g2p::kend(sl));
+        }
+        if (lr.nchunk > 0)
+            (g2p::kbegin(sizeof(T) == 8 ? "k_spmm_long<f64,coarse>" : "k_spmm_long<f32,coarse>", sl),
+             k_spmm_long<T><<<(unsigned)lr.nchunk, lblk, 0, sl>>>(lr.rows, lr.crow, lr.cbeg, lr.rcp, A.ptr, A.col, A.val, x, k, lr.partial, lr.done, y, b), g2p::kend(sl));
+        cudaEventRecord(fork->join, sl);
+    }
     const bool sell = A.sptr != nullptr;
     if (prof) {
         prof_event(s);
@@ -689,6 +752,10 @@ void spmm_b(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, const 
         (g2p::kbegin("k_spmm", s), k_spmm<T><<<row_grid(A.n, k, 152LL * 48), blk, 0, s>>>(A.n, A.ptr, A.col, A.val, x, y, k, b), g2p::kend(s));
     }
     if (prof) prof_event(s);
+    if (fork) {
+        cudaStreamWaitEvent(s, fork->join, 0);
+        return;
+    }
     if (lr.nmid > 0) {
         const int kx = k >= 32 ? 32 : pow2_ge(k);
         (g2p::kbegin(spmm_name(3, sizeof(T) == 8, A.n), s),
@@ -1405,6 +1472,13 @@ __global__ void k_prolong_csr(int64_t n, int k, const int64_t *ptr, const int32_
 // One V-cycle on level l: x = M_l^-1 b.  Level 0 runs on the caller's
 // vectors (the Krylov basis vector in, the preconditioned vector out), the
 // coarser levels on their own work vectors.
+// x += y over n * k entries
+template <class T>
+__global__ void k_vec_add(int64_t nk, const T *y, T *x) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nk; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] += y[i];
+}
+
 template <class T>
 static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaStream_t s, const T *b, T *x) {
     if (l > 0 && l == H.fuse_from) {       // b, x are the level's own vectors
@@ -1428,6 +1502,17 @@ static void vcycle(Hierarchy<T> &H, const SolverConfig &cfg, int l, int k, cudaS
     else
         (g2p::kbegin("k_restrict", s), k_restrict<T><<<row_grid(C.n, k), row_block(k), 0, s>>>(C.n, k, L.rptr, L.rmem, L.t0, C.b), g2p::kend(s));
     vcycle<T>(H, cfg, l + 1, k, s, C.b, C.x);
+    // G2P_COARSE_CYCLES=n (comparison): n - 1 further cycles of the first
+    // coarse level on its residual, through the fine level's scratch
+    // vectors (free between restriction and prolongation)
+    if (l == 0 && H.lv.size() > 2) {
+        static const int extra = getenv("G2P_COARSE_CYCLES") ? atoi(getenv("G2P_COARSE_CYCLES")) - 1 : 0;
+        for (int c = 0; c < extra; c++) {
+            spmm_b<T>(C.A, C.lr, C.x, L.t0, k, C.b, s);
+            vcycle<T>(H, cfg, l + 1, k, s, L.t0, L.d);
+            (g2p::kbegin("k_vec_add", s), k_vec_add<T><<<grid_for(C.n * k), kThreads, 0, s>>>(C.n * k, L.d, C.x), g2p::kend(s));
+        }
+    }
     if (L.P.sptr) prolong_sell<T>(L.P, C.x, x, k, s);
     else (g2p::kbegin("k_prolong_csr", s), k_prolong_csr<T><<<row_grid(L.n, k), row_block(k), 0, s>>>(L.n, k, L.P.ptr, L.P.col, L.P.val, C.x, x), g2p::kend(s));
     chebyshev<T>(L, cfg.degree, cfg.cheb_ratio, cfg.cheb_upper, b, x, false, k, s);
