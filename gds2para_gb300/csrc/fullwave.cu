@@ -19,9 +19,11 @@
 // and the mm x mm Galerkin matrix.  Host work, as the reference does it with
 // LAPACK: the k x k eigenproblem, the 2 x 2 and mm x mm complex solves.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "primitives.cuh"
@@ -131,6 +133,100 @@ __global__ void __launch_bounds__(kFwThreads) k_fw_axpy_dot(int64_t n, const dou
         for (int w2 = 0; w2 < kFwThreads / 32; w2++) t += sm[w2];
         partial[blockIdx.x] = t;
     }
+}
+
+// One whole modified Gram-Schmidt step of find_Vh in one launch, for an
+// operator of at most 4 * 1024 rows: the same arithmetic, in the same order,
+// as k_fw_dot, then per basis vector k_fw_finish and k_fw_axpy_dot, then
+// the norm and k_fw_scale, launched on a grid of kFwNb blocks of kFwThreads
+// threads.  Those kernels give row e to thread e % 256 of block e / 256;
+// this block of 1024 threads plays four such blocks at a time (group g =
+// tid / 256 is block 4 r + g in round r), keeps its rows of w in registers,
+// and reduces each emulated block's eight warp sums and then the block
+// partials exactly as those kernels do.  Blocks past the rows contribute
+// zero partials, which leave the sums unchanged.  The result (hcol, the
+// norm, the next basis vector) is bit-identical, in 2 launches per step
+// instead of 2 j + 3.
+constexpr int kFwNb = 152 * 4;
+template <int R>
+__global__ void __launch_bounds__(1024) k_fw_mgs_step(int64_t n, int j, const double *V, double *w, double *hcol,
+                                                      double *hn, double *vout) {
+    __shared__ double sm[4 * R][kFwThreads / 32];
+    __shared__ double pval;
+    const int tid = threadIdx.x, g = tid >> 8, t = tid & 255, wg = t >> 5;
+    const int nbv = (int)((n + kFwThreads - 1) / kFwThreads);
+    auto row = [&](int r) -> int64_t { return (int64_t)(4 * r + g) * kFwThreads + t; };
+    // the emulated blocks' sums of their eight warp sums (k_fw_dot's block
+    // partials), and the sum over the blocks as k_fw_finish adds them: lane l
+    // takes block l (at most 16 blocks here), then the xor tree
+    auto finish = [&]() -> double {
+        __syncthreads();
+        if (tid < 32) {
+            double acc = 0;
+            for (int q = tid; q < nbv; q += 32) {
+                double tt = 0;
+                for (int u = 0; u < kFwThreads / 32; u++) tt += sm[q][u];
+                acc += tt;
+            }
+            acc = warp_sum(acc);
+            if (tid == 0) pval = acc;
+        }
+        __syncthreads();
+        return pval;
+    };
+    double wv[R], xv[R], yv[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const bool in = row(r) < n;
+        wv[r] = in ? w[row(r)] : 0.0;
+        xv[r] = in ? V[row(r)] : 0.0;
+        yv[r] = in && j > 1 ? V[n + row(r)] : 0.0;
+    }
+    // p = V_0 . w (k_fw_dot)
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        double acc = 0;
+        if (row(r) < n) acc += xv[r] * wv[r];
+        acc = warp_sum(acc);
+        if ((tid & 31) == 0) sm[4 * r + g][wg] = acc;
+    }
+    double p = finish();
+    for (int i = 0; i < j; i++) {
+        const double hv = p;
+        if (tid == 0) hcol[i] = hv;
+        const bool more = i + 1 < j;
+        // V_{i+2}, for the next projection, while this one's sums run
+        double zv[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) zv[r] = (i + 2 < j && row(r) < n) ? V[(int64_t)(i + 2) * n + row(r)] : 0.0;
+        // w -= h V_i, then the partials of y . w with y = V_{i+1}, or w
+        // itself after the last basis vector (k_fw_axpy_dot)
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            double acc = 0;
+            if (row(r) < n) {
+                const double wi = wv[r] - hv * xv[r];
+                wv[r] = wi;
+                acc += (more ? yv[r] : wi) * wi;
+            }
+            acc = warp_sum(acc);
+            if ((tid & 31) == 0) sm[4 * r + g][wg] = acc;
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            xv[r] = yv[r];
+            yv[r] = zv[r];
+        }
+        p = finish();
+    }
+    const double nrm = sqrt(p);
+    if (tid == 0) *hn = nrm;
+#pragma unroll
+    for (int r = 0; r < R; r++)
+        if (row(r) < n) {
+            w[row(r)] = wv[r];
+            vout[row(r)] = wv[r] / nrm;
+        }
 }
 
 // out = sum of the nb partials (one warp, fixed tree); sqrt when asked
@@ -493,6 +589,13 @@ int hqr_eigenvalues(int64_t n, double *a, double *wr, double *wi) {
 // Eigenvector of the real upper Hessenberg h (column-major) for lambda:
 // three steps of inverse iteration on h - lambda I (one row interchange
 // per column in its LU), scaled so that the largest |re| + |im| is 1.
+// a * b by the textbook formula (the library's operator calls a routine that
+// recovers infinities from NaN results, several times slower; the values
+// here are finite)
+static inline cd cmul(cd a, cd b) {
+    return cd(a.real() * b.real() - a.imag() * b.imag(), a.real() * b.imag() + a.imag() * b.real());
+}
+
 std::vector<cd> hessenberg_eigvec(int64_t n, const double *h, cd lambda, double hnorm) {
     std::vector<cd> a((size_t)(n * n), cd(0));
     auto A = [&](int64_t i, int64_t j) -> cd & { return a[(size_t)(i + j * n)]; };
@@ -510,18 +613,18 @@ std::vector<cd> hessenberg_eigvec(int64_t n, const double *h, cd lambda, double 
         if (A(k, k) == cd(0)) A(k, k) = cd(tiny, 0);
         const cd f = A(k + 1, k) / A(k, k);
         mul[(size_t)k] = f;
-        for (int64_t j = k + 1; j < n; j++) A(k + 1, j) -= f * A(k, j);
+        for (int64_t j = k + 1; j < n; j++) A(k + 1, j) -= cmul(f, A(k, j));
     }
     if (A(n - 1, n - 1) == cd(0)) A(n - 1, n - 1) = cd(tiny, 0);
     std::vector<cd> x((size_t)n, cd(1.0 / std::sqrt((double)n), 0));
     for (int it = 0; it < 3; it++) {
         for (int64_t k = 0; k + 1 < n; k++) {
             if (swp[(size_t)k]) std::swap(x[(size_t)k], x[(size_t)k + 1]);
-            x[(size_t)k + 1] -= mul[(size_t)k] * x[(size_t)k];
+            x[(size_t)k + 1] -= cmul(mul[(size_t)k], x[(size_t)k]);
         }
         for (int64_t k = n - 1; k >= 0; k--) {
             x[(size_t)k] /= A(k, k);
-            for (int64_t i = 0; i < k; i++) x[(size_t)i] -= A(i, k) * x[(size_t)k];
+            for (int64_t i = 0; i < k; i++) x[(size_t)i] -= cmul(A(i, k), x[(size_t)k]);
         }
         double mx = 0;
         for (auto &v : x) mx = std::max(mx, std::abs(v));
@@ -737,6 +840,7 @@ extern "C" g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh) {
     if (!m->stiff_done) { set_last_message("g2p_find_vh: g2p_generate_stiff has not run"); return G2P_ERR_STATE; }
     cudaStream_t s = m->stream;
     const Dims &d = m->d;
+    const auto t_start = std::chrono::steady_clock::now();
     if (!m->fw) m->fw = new FullWave();
     FullWave &F = *m->fw;
     F.release(s);
@@ -746,7 +850,13 @@ extern "C" g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh) {
     G2P_TRY(dalloc(&F.map_r, nr, s));
     (kbegin("k_fw_map_r", s), k_fw_map_r<<<grid_for(d.N_edge), kThreads, 0, s>>>(d.N_edge, m->map_edge, F.map_r), kend(s));
     double *V, *w, *Hd, *partial, *sv = nullptr;
-    const int nb = 152 * 4;
+    const int nb = kFwNb;
+    // operators of at most 4 * 1024 rows (the register budget of 1024
+    // threads): one launch per Gram-Schmidt step (G2P_FW_MGS_LAUNCHES=1 keeps
+    // the launch per basis vector, comparison)
+    int rounds = 1;
+    while (rounds < 4 && (int64_t)rounds * 1024 < n2) rounds <<= 1;
+    const bool one_launch = (int64_t)rounds * 1024 >= n2 && !getenv("G2P_FW_MGS_LAUNCHES");
     // S v by the assembled CSR rows, each summed in S's entry order as the
     // reference sums them; G2P_FW_STENCIL=1 applies the matrix-free stencil
     // instead (equal to rounding, and no S traffic, but at k = 1000 the
@@ -774,6 +884,19 @@ extern "C" g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh) {
             (kbegin("k_fw_apply_sv", s), k_fw_apply_sv<<<fw_grid(nr), kFwThreads, 0, s>>>(nr, sv, F.map_r, m->mark_edge, m->epsn, m->sign, d.L, m->k.eps0, scale, vp, w), kend(s));
         }
         double *hcol = Hd + (int64_t)(j - 1) * k;
+        double *hn = j < k ? hcol + j : hnext;
+        if (one_launch) {
+            // the whole step in one launch (bit-identical to the loop below)
+            kbegin("k_fw_mgs_step", s);
+            switch (rounds) {
+                case 1: k_fw_mgs_step<1><<<1, 1024, 0, s>>>(n2, j, V, w, hcol, hn, V + (int64_t)j * n2); break;
+                case 2: k_fw_mgs_step<2><<<1, 1024, 0, s>>>(n2, j, V, w, hcol, hn, V + (int64_t)j * n2); break;
+                default: k_fw_mgs_step<4><<<1, 1024, 0, s>>>(n2, j, V, w, hcol, hn, V + (int64_t)j * n2); break;
+            }
+            kend(s);
+            G2P_CUDA(cudaGetLastError());
+            continue;
+        }
         // modified Gram-Schmidt: h_i = V_i . w, w -= h_i V_i, in order; the
         // last update also gives the partials of |w|^2
         (kbegin("k_fw_dot", s), k_fw_dot<<<nb, kFwThreads, 0, s>>>(n2, V, w, partial), kend(s));
@@ -782,7 +905,6 @@ extern "C" g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh) {
             const double *next = i + 1 < j ? V + (int64_t)(i + 1) * n2 : w;
             (kbegin("k_fw_axpy_dot", s), k_fw_axpy_dot<<<nb, kFwThreads, 0, s>>>(n2, hcol + i, V + (int64_t)i * n2, w, next, partial), kend(s));
         }
-        double *hn = j < k ? hcol + j : hnext;
         (kbegin("k_fw_finish", s), k_fw_finish<<<1, 32, 0, s>>>(partial, nb, hn, 1), kend(s));
         (kbegin("k_fw_scale", s), k_fw_scale<<<fw_grid(n2), kFwThreads, 0, s>>>(n2, w, hn, V + (int64_t)j * n2), kend(s));
         G2P_CUDA(cudaGetLastError());
@@ -800,6 +922,8 @@ extern "C" g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh) {
     for (int i = 0; i < k; i++)
         for (int c = 0; c < k; c++)
             if (i <= c + 1) H1[(size_t)c * k + i] = H[(size_t)c * k + i];
+    const bool dbg = getenv("G2P_DEBUG") != nullptr;
+    auto tq = std::chrono::steady_clock::now();
     std::vector<double> Hq = H1;
     if (hqr_eigenvalues(k, Hq.data(), wr.data(), wi.data()) != 0) {
         set_last_message("g2p_find_vh: QR iteration on the %d x %d Hessenberg matrix did not converge", k);
@@ -809,20 +933,57 @@ extern "C" g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh) {
     double hnorm = 0;
     for (int c = 0; c < k; c++)
         for (int i = 0; i <= std::min(c + 1, k - 1); i++) hnorm += std::fabs(H1[(size_t)c * k + i]);
-    std::vector<double> vcols;       // [mm][k] complex, interleaved
-    int64_t mm = 0;
+    auto te = std::chrono::steady_clock::now();
+    // the eigenvalues kept (|Im| > 1e-6, positive imaginary part of each
+    // pair), in order; their eigenvectors are independent, so host threads
+    // share them out and each result lands in its own slot
+    std::vector<int> keep;
     for (int j = 0; j < k; j++) {
         if (!(std::fabs(wi[j]) > 1e-6)) continue;
         if (wi[j] > 0 && j + 1 < k) {
-            const std::vector<cd> x = hessenberg_eigvec(k, H1.data(), cd(wr[j], wi[j]), hnorm);
-            for (int t = 0; t < 2; t++)
-                for (int i = 0; i < k; i++) {
-                    vcols.push_back(x[(size_t)i].real());
-                    vcols.push_back(t == 0 ? x[(size_t)i].imag() : -x[(size_t)i].imag());
-                }
-            mm += 2;
+            keep.push_back(j);
             j++;
         }
+    }
+    std::vector<std::vector<cd>> xs(keep.size());
+    {
+        const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        const size_t nt = std::min<size_t>(hw, keep.size());
+        std::vector<std::thread> pool;
+        auto work = [&](size_t t0) {
+            for (size_t q = t0; q < keep.size(); q += std::max<size_t>(nt, 1))
+                xs[q] = hessenberg_eigvec(k, H1.data(), cd(wr[keep[q]], wi[keep[q]]), hnorm);
+        };
+        try {
+            for (size_t t = 1; t < nt; t++) pool.emplace_back(work, t);
+        } catch (const std::exception &) {
+            // fewer threads: the remaining strides are done below
+        }
+        const size_t started = pool.size() + 1;
+        if (started == nt || nt <= 1) {
+            work(0);
+        } else {
+            for (size_t q = 0; q < keep.size(); q++)
+                if (q % nt == 0 || q % nt >= started) xs[q] = hessenberg_eigvec(k, H1.data(), cd(wr[keep[q]], wi[keep[q]]), hnorm);
+        }
+        for (auto &th : pool) th.join();
+    }
+    std::vector<double> vcols;       // [mm][k] complex, interleaved
+    int64_t mm = 0;
+    for (const std::vector<cd> &x : xs) {
+        for (int t = 0; t < 2; t++)
+            for (int i = 0; i < k; i++) {
+                vcols.push_back(x[(size_t)i].real());
+                vcols.push_back(t == 0 ? x[(size_t)i].imag() : -x[(size_t)i].imag());
+            }
+        mm += 2;
+    }
+    if (dbg) {
+        auto tv = std::chrono::steady_clock::now();
+        fprintf(stderr, "[g2p find_vh] k=%d: Arnoldi %.1f ms, Hessenberg eigenvalues %.1f ms, %zu eigenvectors %.1f ms\n",
+                k, std::chrono::duration<double, std::milli>(tq - t_start).count(),
+                std::chrono::duration<double, std::milli>(te - tq).count(), keep.size(),
+                std::chrono::duration<double, std::milli>(tv - te).count());
     }
     F.mm = mm;
     if (mm > 0) {

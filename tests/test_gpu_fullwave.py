@@ -110,3 +110,21 @@ def test_gpu_find_vh_rejects_bad_k(g2p):
         n = d.N_edge - m.sizes().bden
         with pytest.raises(g2p.G2PError):
             g2p.findVh(m, 2 * n + 1)
+
+
+@pytest.mark.parametrize("name,k", [("strip_tiny_vh", 200), ("strip_tiny", 60)])
+def test_gpu_find_vh_one_launch_step_is_bit_identical(name, k, g2p, monkeypatch):
+    """find_Vh's Gram-Schmidt step in one launch (k_fw_mgs_step) against the
+    launch per basis vector it replays: the same Vh, bit for bit."""
+    d, A, M = golden_layout(name)
+    out = []
+    for launches in (True, False):
+        if launches:
+            monkeypatch.setenv("G2P_FW_MGS_LAUNCHES", "1")
+        else:
+            monkeypatch.delenv("G2P_FW_MGS_LAUNCHES", raising=False)
+        with g2p.FdtdMesh(d) as m:
+            g2p.generateStiff(m)
+            out.append(g2p.findVh(m, k))
+    assert out[0].shape == out[1].shape
+    assert np.array_equal(out[0], out[1])
