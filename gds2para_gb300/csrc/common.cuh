@@ -35,6 +35,10 @@ void launch_add(int64_t n);
 int64_t launch_count();
 void kbegin(const char *name, cudaStream_t s);
 void kend(cudaStream_t s);
+// Called right after kbegin's own event and right before kend's (when set):
+// an inner bracket around exactly one launch, for the sparse-product timing.
+extern void (*kbracket_begin)(cudaStream_t);
+extern void (*kbracket_end)(cudaStream_t);
 bool kprof_on();
 void kprof_set(bool on);
 g2p_status kprof_collect();

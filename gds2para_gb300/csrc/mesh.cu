@@ -64,13 +64,18 @@ static void np_record(cudaStream_t s) {
     }
     cudaEventRecord(g_np.ev[g_np.used++], s);
 }
+void (*kbracket_begin)(cudaStream_t) = nullptr;
+void (*kbracket_end)(cudaStream_t) = nullptr;
 void kbegin(const char *name, cudaStream_t s) {
     launch_tick();
-    if (!g_np.on) return;
-    g_np.names.push_back(name);
-    np_record(s);
+    if (g_np.on) {
+        g_np.names.push_back(name);
+        np_record(s);
+    }
+    if (kbracket_begin) kbracket_begin(s);
 }
 void kend(cudaStream_t s) {
+    if (kbracket_end) kbracket_end(s);
     if (g_np.on) np_record(s);
 }
 bool kprof_on() { return g_np.on; }
