@@ -1065,6 +1065,64 @@ __global__ void __launch_bounds__(256) k_maxpy_v(int64_t nq, int cpr, int k, int
     }
 }
 
+// The unnormalised Arnoldi basis (W_i = s_i V_i, s_i = |W_i| per column):
+// out = w - sum_i c[i*k + col] W_i, the next basis vector as it stands, and
+// the block partial sums of its squared columns (so no separate norm pass
+// and no normalised copy).  c staged in shared memory.
+template <int GC, class T>
+__device__ __forceinline__ void chunk_col_reduce(const T (&v)[GC], double *sm, int cpr, int k, int C, int gvalid,
+                                                 int64_t gbase, double *partial);
+template <class T>
+__global__ void __launch_bounds__(256) k_maxpy_norm_v(int64_t nq, int cpr, int k, int J, const T *V, const double *c,
+                                                      const T *w, T *out, double *partial) {
+    constexpr int C = Chunk<T>::C;
+    extern __shared__ unsigned char smraw[];
+    __shared__ double sm[8 * C * 16];
+    T *hs = reinterpret_cast<T *>(smraw);
+    for (int t = threadIdx.x; t < J * k; t += blockDim.x) hs[t] = (T)c[t];
+    __syncthreads();
+    const int cc = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) & (cpr - 1));
+    const int64_t nk = nq * C;
+    T sq[C];
+#pragma unroll
+    for (int u = 0; u < C; u++) sq[u] = 0;
+    G2P_FOR_CHUNKS(q, nq) {
+        Chunk<T> acc;
+        acc.ld(w + q * C);
+        for (int j = 0; j < J; j++) {
+            Chunk<T> v;
+            v.ld(V + (int64_t)j * nk + q * C);
+            const T *hj = hs + j * k + cc * C;
+#pragma unroll
+            for (int u = 0; u < C; u++) acc.v[u] -= hj[u] * v.v[u];
+        }
+        acc.st(out + q * C);
+#pragma unroll
+        for (int u = 0; u < C; u++) sq[u] += acc.v[u] * acc.v[u];
+    }
+    chunk_col_reduce<C>(sq, sm, cpr, k, C, 1, 0, partial);
+}
+
+// From the dots d_i = W_i . w (w = A M^-1 W_j): the Hessenberg entries
+// h_i = d_i / (s_i s_j), in place, and the update coefficients
+// c_i = d_i / s_i^2 (zero for a zero column)
+__global__ void k_unnorm_coef(int k, int j, const double *sc, double *h, double *c) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (j + 1) * k) return;
+    const int i = t / k, r = t - i * k;
+    const double si = sc[i * k + r], sj = sc[j * k + r], d = h[t];
+    c[t] = si > 0 ? d / (si * si) : 0.0;
+    h[t] = si > 0 && sj > 0 ? d / (si * sj) : 0.0;
+}
+
+// h_{j+1,j} = s_{j+1} / s_j
+__global__ void k_unnorm_hnorm(int k, int j, const double *sc, double *hnorm) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= k) return;
+    const double sj = sc[j * k + r];
+    hnorm[r] = sj > 0 ? sc[(j + 1) * k + r] / sj : 0.0;
+}
+
 // Chebyshev: d = theta^-1 D^-1 b, x = d (or x += d)
 // Chebyshev first step: d = D^-1 b / theta, x = d (or x += d with add).
 // STX / STD: whether x and d are stored (a zero-guess smoother of degree >= 2
@@ -2763,7 +2821,7 @@ void Krylov<T>::release(cudaStream_t s) {
     drop_graphs();
     dfree(V, s); dfree(Z, s); dfree(w, s); dfree(r, s);
     dfree(H, s); dfree(cs, s); dfree(sn, s); dfree(g, s); dfree(y, s);
-    dfree(beta, s); dfree(bnorm, s); dfree(partial, s); dfree(hcol, s);
+    dfree(beta, s); dfree(bnorm, s); dfree(partial, s); dfree(hcol, s); dfree(sc, s);
     if (h_est) cudaFreeHost(h_est);
     h_est = nullptr;
     dfree(bdev, s); dfree(bpart, s);
@@ -2793,6 +2851,7 @@ g2p_status krylov_alloc(Krylov<T> &K, int64_t n, int k, int m, cudaStream_t s) {
     G2P_TRY(dalloc(&K.bnorm, k, s));
     G2P_TRY(dalloc(&K.partial, (int64_t)kRedBlocks * k * (m + 2), s));
     G2P_TRY(dalloc(&K.hcol, (int64_t)k * (2 * m + 4), s));
+    G2P_TRY(dalloc(&K.sc, (int64_t)k * (m + 1), s));
     G2P_CUDA(cudaMallocHost(&K.h_est, sizeof(double) * 2 * k));
     return G2P_OK;
 }
@@ -2872,12 +2931,17 @@ __global__ void k_backsolve(int k, int m, int j, const double *H, const double *
 
 // x += sum_i Z_i y_i, and y is laid out [r * m + i]
 template <class T>
-__global__ void k_xupdate(int64_t n, int k, int m, int j, const T *Z, const double *y, T *x) {
+__global__ void k_xupdate(int64_t n, int k, int m, int j, const T *Z, const double *y, T *x, const double *sc) {
     const int r = threadIdx.x;
     if (r >= k) return;
     const int64_t nk = n * k;
     T yr[64];
-    for (int q = 0; q < j; q++) yr[q] = (T)y[(int64_t)r * m + q];
+    // with the unnormalised basis Z_q holds s_q M^-1 V_q: its weight is y_q / s_q
+    for (int q = 0; q < j; q++) {
+        const double yq = y[(int64_t)r * m + q];
+        const double sq = sc ? sc[(int64_t)q * k + r] : 1.0;
+        yr[q] = (T)(sc ? (sq > 0 ? yq / sq : 0.0) : yq);
+    }
     G2P_FOR_ROWS(i, n) {
         int64_t t = i * k + r;
         T acc = x[t];
@@ -2978,10 +3042,26 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
     int it = 0;
     rep.converged = false;
     double *dots2 = K.hcol + (int64_t)k * (m + 1);
+    // FP32 solves keep the basis unnormalised (W_0 = r, W_{j+1} = the
+    // orthogonalised remainder, their column norms in K.sc): no norm pass and
+    // no normalised copy per step.  Chunked vectors, Gram-Schmidt once.  The
+    // V-cycle is linear, so Z_j holds s_j M^-1 V_j and w = A Z_j carries s_j;
+    // the preconditioned operator is near the identity there, so the norms
+    // stay of the order of the residual's.  Not in FP64: its Gram-Schmidt is
+    // bound by the FP64 pipe, which the fused norm loads further (measured
+    // slower); nor with an FP32 preconditioner of the scaled operator, whose
+    // outputs are off the basis' scale by that factor per step.
+    // (G2P_UNNORM_BASIS=0: the normalised basis, comparison)
+    static const bool unnorm_on = [] {
+        const char *e = getenv("G2P_UNNORM_BASIS");
+        return e ? atoi(e) != 0 : true;
+    }();
+    const bool unnorm = unnorm_on && sizeof(T) == 4 && cpr != 0 && !cfg.reorth;
+    T *const r0 = unnorm ? K.V : K.r;
     for (;;) {
         // r = b - A x ; beta = ||r||
-        spmm_b<T>(A, lr0, x, K.r, k, b, s);
-        colnorms<T>(K.r, n, k, K.partial, K.beta, s);
+        spmm_b<T>(A, lr0, x, r0, k, b, s);
+        colnorms<T>(r0, n, k, K.partial, K.beta, s);
         G2P_CUDA(cudaMemcpyAsync(K.h_est, K.beta, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
         G2P_CUDA(cudaMemcpyAsync(K.h_est + k, K.bnorm, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
         G2P_CUDA(cudaStreamSynchronize(s));
@@ -2994,7 +3074,8 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
         rep.rel_residual = worst;
         if (worst <= cfg.rtol) { rep.converged = true; break; }
         if (it >= cfg.maxit) break;
-        if (cpr) (g2p::kbegin("k_start", s), k_scale_cols_v<T><<<chunk_grid(nq), 256, 0, s>>>(nq, cpr, K.beta, K.r, K.V), g2p::kend(s));
+        if (unnorm) G2P_CUDA(cudaMemcpyAsync(K.sc, K.beta, sizeof(double) * k, cudaMemcpyDeviceToDevice, s));
+        else if (cpr) (g2p::kbegin("k_start", s), k_scale_cols_v<T><<<chunk_grid(nq), 256, 0, s>>>(nq, cpr, K.beta, K.r, K.V), g2p::kend(s));
         else (g2p::kbegin("k_start", s), k_start<T><<<rg, rb, 0, s>>>(n, k, K.r, K.beta, K.V), g2p::kend(s));
         (g2p::kbegin("k_g_init", s), k_g_init<<<(k + 63) / 64, 64, 0, s>>>(k, m, K.beta, K.g), g2p::kend(s));
         int j = 0;
@@ -3014,6 +3095,22 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
                     vcycle<T>(H, cfg, 0, k, s, Vj, Zj);
                 }
                 spmm<T>(A, lr0, Zj, K.w, k, s);
+                double *est = K.y;        // scratch for the estimates (k values)
+                if (unnorm) {
+                    // classical Gram-Schmidt once against the unnormalised basis
+                    mdot<T>(K.V, n, j + 1, K.w, k, K.partial, K.hcol, s);
+                    const int nc = (j + 1) * k;
+                    (g2p::kbegin("k_unnorm_coef", s), k_unnorm_coef<<<(nc + 127) / 128, 128, 0, s>>>(k, j, K.sc, K.hcol, dots2), g2p::kend(s));
+                    const unsigned cg = chunk_grid(nq);
+                    (g2p::kbegin("k_maxpy_norm", s),
+                     k_maxpy_norm_v<T><<<cg, 256, sizeof(T) * nc, s>>>(nq, cpr, k, j + 1, K.V, dots2, K.w, K.V + (int64_t)(j + 1) * nk, K.partial),
+                     g2p::kend(s));
+                    (g2p::kbegin("k_reduce_partials", s), k_reduce_partials<<<reduce_grid(k), 32 * kReduceWarps, 0, s>>>(K.partial, (int)cg, k, K.sc + (int64_t)(j + 1) * k, true), g2p::kend(s));
+                    (g2p::kbegin("k_unnorm_hnorm", s), k_unnorm_hnorm<<<(k + 63) / 64, 64, 0, s>>>(k, j, K.sc, K.beta), g2p::kend(s));
+                    (g2p::kbegin("k_givens", s), k_givens<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.hcol, K.beta, K.H, K.cs, K.sn, K.g, K.bnorm, est), g2p::kend(s));
+                    cudaMemcpyAsync(K.h_est, est, sizeof(double) * k, cudaMemcpyDeviceToHost, s);
+                    return;
+                }
                 // classical Gram-Schmidt, optionally twice
                 mdot<T>(K.V, n, j + 1, K.w, k, K.partial, K.hcol, s);
                 maxpy(K.hcol, j + 1);
@@ -3026,7 +3123,6 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
                 colnorms<T>(K.w, n, k, K.partial, hnorm, s);
                 if (cpr) (g2p::kbegin("k_arnoldi_finish", s), k_scale_cols_v<T><<<chunk_grid(nq), 256, 0, s>>>(nq, cpr, hnorm, K.w, K.V + (int64_t)(j + 1) * nk), g2p::kend(s));
                 else (g2p::kbegin("k_arnoldi_finish", s), k_arnoldi_finish<T><<<rg, rb, 0, s>>>(n, k, hnorm, K.w, K.V + (int64_t)(j + 1) * nk), g2p::kend(s));
-                double *est = K.y;        // scratch for the estimates (k values)
                 (g2p::kbegin("k_givens", s), k_givens<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.hcol, hnorm, K.H, K.cs, K.sn, K.g, K.bnorm, est), g2p::kend(s));
                 cudaMemcpyAsync(K.h_est, est, sizeof(double) * k, cudaMemcpyDeviceToHost, s);
             };
@@ -3070,7 +3166,7 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
             if (worst <= cfg.rtol) { j++; break; }
         }
         (g2p::kbegin("k_backsolve", s), k_backsolve<<<(k + 63) / 64, 64, 0, s>>>(k, m, j, K.H, K.g, K.y), g2p::kend(s));
-        (g2p::kbegin("k_xupdate", s), k_xupdate<T><<<rg, rb, 0, s>>>(n, k, m, j, K.Z, K.y, x), g2p::kend(s));
+        (g2p::kbegin("k_xupdate", s), k_xupdate<T><<<rg, rb, 0, s>>>(n, k, m, j, K.Z, K.y, x, unnorm ? K.sc : nullptr), g2p::kend(s));
     }
     rep.iterations = it;
     G2P_CUDA(cudaGetLastError());

@@ -119,6 +119,7 @@ struct Krylov {
     T *V = nullptr, *Z = nullptr, *w = nullptr, *r = nullptr;
     double *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr;
     double *beta = nullptr, *bnorm = nullptr, *partial = nullptr, *hcol = nullptr;
+    double *sc = nullptr;       // (m + 1) x k norms of the unnormalised basis vectors
     double *h_est = nullptr;    // pinned host copy of residual estimates
     // Arnoldi step j as a CUDA graph (captured on its second use), valid for
     // the block width, operator and preconditioner in graph_key
