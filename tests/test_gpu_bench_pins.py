@@ -9,8 +9,8 @@ V0d/V0c bases with a-values and maps and the Ad/Ac COO, and the whole Z.
 Here the GPU path, through the C ABI, must give the same bytes for every
 assembled array, and Z within the stated tolerances: the reference path's
 solves were taken to 1e-13, the bench's mixed method stops at 1e-8 (bound
-1e-6 on Z, the spec accuracy), the FP64 method here at 1e-10 (bound
-1e-7)."""
+1e-6 on Z, the accuracy the mixed method is held to), the FP64 method here
+at 1e-10 (bound 1e-7)."""
 import numpy as np
 import pytest
 
