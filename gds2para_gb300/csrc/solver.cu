@@ -656,8 +656,22 @@ struct SideStream {
     cudaEvent_t fork = nullptr, join = nullptr;
     bool ok = false;
 };
+struct SideStreams {
+    std::vector<std::pair<cudaStream_t, SideStream>> tab;
+    ~SideStreams() {
+        // errors at process exit (runtime already unloading) are ignored
+        for (auto &e : tab)
+            if (e.second.ok) {
+                cudaEventDestroy(e.second.fork);
+                cudaEventDestroy(e.second.join);
+                cudaStreamDestroy(e.second.side);
+            }
+        cudaGetLastError();
+    }
+};
 static SideStream *side_stream_of(cudaStream_t s) {
-    thread_local std::vector<std::pair<cudaStream_t, SideStream>> tab;
+    thread_local SideStreams held;
+    auto &tab = held.tab;
     for (auto &e : tab)
         if (e.first == s) return e.second.ok ? &e.second : nullptr;
     if (tab.size() >= 64) return nullptr;      // many launching streams: keep their long rows in line
@@ -673,11 +687,8 @@ static SideStream *side_stream_of(cudaStream_t s) {
 // G2P_LONG_FORK=0 keeps the long-row kernels behind the short-row kernel on
 // the launching stream (comparison).
 static bool long_fork_on() {
-    static const bool on = [] {
-        const char *e = getenv("G2P_LONG_FORK");
-        return e ? atoi(e) != 0 : true;
-    }();
-    return on;
+    const char *e = getenv("G2P_LONG_FORK");
+    return e ? atoi(e) != 0 : true;
 }
 
 template <class T>
@@ -3011,6 +3022,19 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
         fuse_from = H.fuse_from;
     }
     const LongRows &lr0 = op_lr ? *op_lr : (pc ? *pc->lr : H.lv[0].lr);
+    // FP32 solves keep the basis unnormalised (W_0 = r, W_{j+1} = the
+    // orthogonalised remainder, their column norms in K.sc): no norm pass and
+    // no normalised copy per step.  Chunked vectors, Gram-Schmidt once.  The
+    // V-cycle is linear, so Z_j holds s_j M^-1 V_j and w = A Z_j carries s_j;
+    // the preconditioned operator is near the identity there, so the norms
+    // stay of the order of the residual's.  Not in FP64: its Gram-Schmidt is
+    // bound by the FP64 pipe, which the fused norm loads further (measured
+    // slower); nor with an FP32 preconditioner of the scaled operator, whose
+    // outputs are off the basis' scale by that factor per step.
+    // (G2P_UNNORM_BASIS=0: the normalised basis, comparison)
+    const char *une = getenv("G2P_UNNORM_BASIS");
+    const bool unnorm_on = une ? atoi(une) != 0 : true;
+    const bool unnorm = unnorm_on && sizeof(T) == 4 && chunk_cpr<T>(k) != 0 && !cfg.reorth;
     // CUDA graphs of the Arnoldi steps: off while kernels are being timed;
     // rebuilt when the block width, operator or preconditioner changes
     const bool graphs = cfg.use_graphs && !kprof_on() && !g_prof.on;
@@ -3020,7 +3044,8 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
         const std::vector<const void *> key = {(const void *)(intptr_t)k, (const void *)A.val, hier,
                                                (const void *)(intptr_t)kcap, (const void *)(intptr_t)cfg.degree,
                                                (const void *)(intptr_t)cfg.reorth, pc ? (const void *)pc->in : nullptr,
-                                               (const void *)(intptr_t)fuse_from};
+                                               (const void *)(intptr_t)fuse_from, (const void *)(intptr_t)unnorm,
+                                               (const void *)(intptr_t)long_fork_on()};
         if (K.graph_key != key || (int)K.steps.size() != m) {
             K.drop_graphs();
             K.graph_key = key;
@@ -3042,21 +3067,6 @@ g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T 
     int it = 0;
     rep.converged = false;
     double *dots2 = K.hcol + (int64_t)k * (m + 1);
-    // FP32 solves keep the basis unnormalised (W_0 = r, W_{j+1} = the
-    // orthogonalised remainder, their column norms in K.sc): no norm pass and
-    // no normalised copy per step.  Chunked vectors, Gram-Schmidt once.  The
-    // V-cycle is linear, so Z_j holds s_j M^-1 V_j and w = A Z_j carries s_j;
-    // the preconditioned operator is near the identity there, so the norms
-    // stay of the order of the residual's.  Not in FP64: its Gram-Schmidt is
-    // bound by the FP64 pipe, which the fused norm loads further (measured
-    // slower); nor with an FP32 preconditioner of the scaled operator, whose
-    // outputs are off the basis' scale by that factor per step.
-    // (G2P_UNNORM_BASIS=0: the normalised basis, comparison)
-    static const bool unnorm_on = [] {
-        const char *e = getenv("G2P_UNNORM_BASIS");
-        return e ? atoi(e) != 0 : true;
-    }();
-    const bool unnorm = unnorm_on && sizeof(T) == 4 && cpr != 0 && !cfg.reorth;
     T *const r0 = unnorm ? K.V : K.r;
     for (;;) {
         // r = b - A x ; beta = ||r||

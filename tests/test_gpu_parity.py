@@ -275,3 +275,41 @@ def test_gpu_fused_coarse_cycle_give_up_repeats_the_solve_unfused(precision, g2p
     monkeypatch.delenv("G2P_DEBUG")
     assert "fused coarse cycle gave up; solve repeated unfused" in capfd.readouterr().err
     assert np.array_equal(Z0, Z1)
+
+
+@pytest.mark.parametrize("name,precision", [("multistrip_small", "mixed"), ("manhattan_sweep", "fp64"),
+                                            ("strip_c1", "mixed")])
+def test_gpu_long_rows_beside_short_rows_give_identical_z(name, precision, g2p, monkeypatch):
+    """The long-row kernels of coarse sliced-ELL operators on a side stream
+    beside the short-row kernel (the default) write other rows than it does:
+    Z is bit-identical to the serial order (G2P_LONG_FORK=0), graphs on."""
+    d, A, M = golden_layout(name)
+    out = []
+    for fork in ("0", "1"):
+        monkeypatch.setenv("G2P_LONG_FORK", fork)
+        with g2p.FdtdMesh(d) as m:
+            g2p.generateStiff(m)
+            Z, st = g2p.paraGenerator(m, g2p.default_params(precision=precision, rtol=1e-10))
+        out.append((Z, st.total_iterations))
+    assert out[0][1] == out[1][1]
+    assert np.array_equal(out[0][0], out[1][0])
+
+
+@pytest.mark.parametrize("name", ["multistrip_small", "manhattan_small"])
+def test_gpu_unnormalised_basis_matches_normalised(name, g2p, monkeypatch):
+    """The FP32 solves' unnormalised Arnoldi basis (the default) against the
+    normalised one (G2P_UNNORM_BASIS=0): the same Krylov spaces in another
+    scaling, so Z agrees to the solves' tolerance, and both match the
+    reference."""
+    d, A, M = golden_layout(name)
+    out = []
+    for un in ("0", "1"):
+        monkeypatch.setenv("G2P_UNNORM_BASIS", un)
+        with g2p.FdtdMesh(d) as m:
+            g2p.generateStiff(m)
+            Z, st = g2p.paraGenerator(m, g2p.default_params(precision="mixed", rtol=1e-10))
+        assert st.max_rel_residual <= 1e-10
+        out.append(Z)
+    assert np.abs(out[1] - out[0]).max() / np.abs(out[0]).max() < 1e-8
+    Zr = A["Z"].reshape(out[1].shape)
+    assert np.abs(out[1] - Zr).max() / np.abs(Zr).max() < 1e-7
