@@ -411,10 +411,12 @@ CoarseKernel<T> coarse_kernel(int kg, bool cluster) {
     return cluster ? coarse_kernel_of<T, true>(kg) : coarse_kernel_of<T, false>(kg);
 }
 
-// G2P_FUSE: 0 or unset = off, 1 = grid form, 2 = cluster form
+// G2P_FUSE: 0 = off, 1 = grid form, 2 = cluster form; unset = the cluster
+// form where its levels have no long rows (-1)
 int fuse_mode() {
     const char *e = getenv("G2P_FUSE");
-    const int m = e ? atoi(e) : 0;
+    if (!e) return -1;
+    const int m = atoi(e);
     return m == 1 || m == 2 ? m : 0;
 }
 
@@ -429,11 +431,23 @@ int coarse_fuse_level(const Hierarchy<T> &H, int k) {
     // launch-per-kernel cycle replayed from CUDA graphs on the workloads here
     const int mode = fuse_mode();
     if (mode == 0 || H.fuse_off) return -1;
-    int64_t rows = mode == 2 ? kClusterRows : kFuseRows;
+    int64_t rows = mode == 1 ? kFuseRows : kClusterRows;
     if (const char *r = getenv("G2P_FUSE_ROWS")) rows = std::max<int64_t>(1, atoll(r));
     const int nlev = (int)H.lv.size();
     for (int l = 1; l < nlev - 1; l++)
-        if (H.lv[l].n <= rows) return nlev - l <= kFuseMaxLevels ? l : -1;
+        if (H.lv[l].n <= rows) {
+            if (nlev - l > kFuseMaxLevels) return -1;
+            if (mode == -1) {
+                // by default only for blocks of at most 8 right-hand sides and
+                // where no fused level has long rows (measured: faster for Ac
+                // on c2 and c1; slower at 32 right-hand sides (c3) and where
+                // conductor rows need the whole GPU (Ad))
+                if (k > 8) return -1;
+                for (int q = l; q < nlev; q++)
+                    if (H.lv[q].lr.n > 0) return -1;
+            }
+            return l;
+        }
     return -1;
 }
 
@@ -494,7 +508,7 @@ g2p_status coarse_prepare(Hierarchy<T> &H, const SolverConfig &cfg, int k, cudaS
                     l == nlev - 1 ? (H.cinv ? " (dense inverse)" : " (smoothed)") : "");
     G2P_CUDA(cudaMemcpyAsync(H.fuse_tab, tab.data(), sizeof(FuseLevel<T>) * tab.size(), cudaMemcpyHostToDevice, s));
     G2P_CUDA(cudaStreamSynchronize(s));
-    if (mode == 2) {
+    if (mode != 1) {
         // the largest cluster of these blocks that the part can place: 16
         // (non-portable) or 8
         const CoarseKernel<T> kfn = coarse_kernel<T>(pow2_ge(k), true);

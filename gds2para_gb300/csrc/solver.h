@@ -90,8 +90,9 @@ struct Hierarchy {
 };
 
 // First level of the fused tail for k right-hand sides, or -1 (the tail
-// needs at least two levels, k <= 32, and G2P_FUSE=1: the fused tail is a
-// comparison switch, off by default).
+// needs at least two levels and k <= 32; by default the cluster form for
+// k <= 8 where none of its levels has long rows; G2P_FUSE=0/1/2: off / grid
+// / cluster).
 template <class T>
 int coarse_fuse_level(const Hierarchy<T> &H, int k);
 // Builds the device table of the fused levels for k right-hand sides (call
