@@ -11,7 +11,8 @@
 // smoothing, smoothed prolongation); the two Chebyshev iterates ping-pong
 // between a level's x and t0 vectors, so a step needs one barrier.
 //
-// Two launch forms (G2P_FUSE=1 or 2):
+// Two launch forms (G2P_FUSE=1 or 2; unset: the cluster form for blocks of
+// at most 8 right-hand sides whose tail levels have no long rows):
 // * grid: a cooperative launch over every SM, levels of up to kFuseRows
 //   rows.  The barrier is an arrival counter with a bounded spin.  A block
 //   that waits too long sets an abandon flag and returns, and every other
@@ -423,12 +424,13 @@ int fuse_mode() {
 }  // namespace
 
 // The first level of the fused tail for k right-hand sides, or -1: the
-// first level below kFuseRows rows, if at least one level lies below it.
+// first level of at most kFuseRows (grid form) or kClusterRows (cluster
+// form) rows, if at least one level lies below it.
 template <class T>
 int coarse_fuse_level(const Hierarchy<T> &H, int k) {
     if (k < 1 || k > 32 || H.lv.size() < 3) return -1;
-    // opt-in (G2P_FUSE=1 or 2): the grid form measured slower than the
-    // launch-per-kernel cycle replayed from CUDA graphs on the workloads here
+    // the grid form measured slower than the launch-per-kernel cycle
+    // replayed from CUDA graphs on the workloads here (a comparison switch)
     const int mode = fuse_mode();
     if (mode == 0 || H.fuse_off) return -1;
     int64_t rows = mode == 1 ? kFuseRows : kClusterRows;
