@@ -19,6 +19,7 @@
 // and the mm x mm Galerkin matrix.  Host work, as the reference does it with
 // LAPACK: the k x k eigenproblem, the 2 x 2 and mm x mm complex solves.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <complex>
@@ -946,13 +947,20 @@ extern "C" g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh) {
         }
     }
     std::vector<std::vector<cd>> xs(keep.size());
+    std::atomic<bool> no_mem(false);     // an allocation failed in a worker
     {
         const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
         const size_t nt = std::min<size_t>(hw, keep.size());
         std::vector<std::thread> pool;
-        auto work = [&](size_t t0) {
-            for (size_t q = t0; q < keep.size(); q += std::max<size_t>(nt, 1))
+        auto one = [&](size_t q) {
+            try {
                 xs[q] = hessenberg_eigvec(k, H1.data(), cd(wr[keep[q]], wi[keep[q]]), hnorm);
+            } catch (const std::exception &) {
+                no_mem = true;
+            }
+        };
+        auto work = [&](size_t t0) {
+            for (size_t q = t0; q < keep.size(); q += std::max<size_t>(nt, 1)) one(q);
         };
         try {
             for (size_t t = 1; t < nt; t++) pool.emplace_back(work, t);
@@ -964,9 +972,14 @@ extern "C" g2p_status g2p_find_vh(g2p_mesh *m, int32_t k, int64_t *leng_vh) {
             work(0);
         } else {
             for (size_t q = 0; q < keep.size(); q++)
-                if (q % nt == 0 || q % nt >= started) xs[q] = hessenberg_eigvec(k, H1.data(), cd(wr[keep[q]], wi[keep[q]]), hnorm);
+                if (q % nt == 0 || q % nt >= started) one(q);
         }
         for (auto &th : pool) th.join();
+    }
+    if (no_mem) {
+        set_last_message("g2p_find_vh: out of host memory for the %d x %d eigenvector solves", k, k);
+        dfree(V, s); dfree(w, s); dfree(Hd, s); dfree(partial, s);
+        return G2P_ERR_NOMEM;
     }
     std::vector<double> vcols;       // [mm][k] complex, interleaved
     int64_t mm = 0;
