@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstring>
 #include <type_traits>
+#include <atomic>
 #include <vector>
 
 #include "primitives.cuh"
@@ -685,11 +686,14 @@ static SideStream *side_stream_of(cudaStream_t s) {
 }
 
 // G2P_LONG_FORK=0 keeps the long-row kernels behind the short-row kernel on
-// the launching stream (comparison).
-static bool long_fork_on() {
+// the launching stream (comparison).  Read at the start of each solve
+// (refresh_long_fork), not per launch.
+static std::atomic<bool> g_long_fork{true};
+static void refresh_long_fork() {
     const char *e = getenv("G2P_LONG_FORK");
-    return e ? atoi(e) != 0 : true;
+    g_long_fork = e ? atoi(e) != 0 : true;
 }
+static bool long_fork_on() { return g_long_fork.load(std::memory_order_relaxed); }
 
 template <class T>
 void spmm_b(const Csr<T> &A, const LongRows &lr, const T *x, T *y, int k, const T *b, cudaStream_t s) {
@@ -3004,6 +3008,7 @@ template <class T>
 g2p_status fgmres(const Csr<T> &A, Hierarchy<T> &H, Krylov<T> &K, const T *b, T *x, int k, const SolverConfig &cfg,
                   const double *bnorm_override, cudaStream_t s, SolveReport &rep, const F32Precond *pc,
                   const LongRows *op_lr) {
+    refresh_long_fork();
     if (cfg.block && !pc && block_krylov_supported<T>(k, b, x))
         return block_fgmres<T>(A, H, K, b, x, k, cfg, bnorm_override, s, rep, op_lr);
     const int64_t n = A.n, nk = n * k;
