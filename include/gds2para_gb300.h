@@ -36,7 +36,7 @@ typedef enum {
     G2P_OK = 0,
     G2P_ERR_INVALID = 1,        /* bad argument or inconsistent mesh description */
     G2P_ERR_CUDA = 2,           /* CUDA runtime failure (see g2p_last_error) */
-    G2P_ERR_NOMEM = 3,          /* device allocation failed */
+    G2P_ERR_NOMEM = 3,          /* device (or, for find_Vh's eigenvectors, host) allocation failed */
     G2P_ERR_NOT_CONVERGED = 4,  /* solver hit maxit above rtol (result still written) */
     G2P_ERR_UNSUPPORTED = 5,    /* layout outside what the path handles (message says which) */
     G2P_ERR_STATE = 6,          /* a required earlier step has not run */
